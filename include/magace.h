@@ -1,0 +1,123 @@
+/*
+ * magace.h - C ABI of the GB300 implementation of the mag-ace potential
+ * evaluation (non-collinear magnetic Atomic Cluster Expansion).
+ *
+ * Two layers:
+ *
+ *  1. The drop-in boundary. acelibini_ and acelib_ have exactly the symbol
+ *     names and argument lists that the reference's LAMMPS pair style binds
+ *     (lammps/pair_spin_ace.cpp:59-62) and that gfortran emits for the
+ *     reference's Fortran entry points (src/ace.F90:10-21 and :79-107):
+ *     lower-case name plus trailing underscore, every argument by reference,
+ *     no hidden string lengths. A caller built against the reference links
+ *     against libmagace.so unchanged. Like the reference they return nothing;
+ *     where the reference would stop the process, this library records an
+ *     error code (ace_last_error), prints one line to stderr and, for acelib_,
+ *     fills the outputs with NaN.
+ *
+ *  2. The extended API (ace_*): explicit potential path, status codes,
+ *     precision selection, and evaluation on device-resident arrays.
+ *
+ * All entry points serialise on one library-owned CUDA stream per process and
+ * are not re-entrant (the reference keeps module-global state too).
+ */
+#ifndef MAGACE_H_
+#define MAGACE_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MAGACE_OK 0
+#define MAGACE_ERR_FILE 1        /* potential file missing or unreadable */
+#define MAGACE_ERR_FORMAT 2      /* malformed / inconsistent potential file */
+#define MAGACE_ERR_UNSUPPORTED 3 /* nele != 1, 5/6-body clusters, radtype 0-2, nfemb 3/4 */
+#define MAGACE_ERR_SMALL_R 4     /* bond shorter than one LUT bin (src/radial.F90:71-75) */
+#define MAGACE_ERR_MOMENT 5      /* |m| < 0, NaN, or >= magnetic cutoff (LUT overrun in the reference) */
+#define MAGACE_ERR_NOT_INIT 6    /* evaluation before a successful init */
+#define MAGACE_ERR_ARGS 7        /* inconsistent arguments (ranges, element indices) */
+#define MAGACE_ERR_CUDA 8        /* CUDA runtime failure (no device, out of memory, ...) */
+#define MAGACE_ERR_NAN 9         /* non-finite density or energy */
+
+/* ---- drop-in boundary (reference: src/ace.F90) -------------------------- */
+
+/* Replaces acelibini (src/ace.F90:10-75). nele must be 1; elenumbers[0] is
+ * the atomic number + 1 (the reference's element table starts with 'X',
+ * lammps/pair_spin_ace.cpp:283-285). xcnumber 1 = pbe, 2 = lda. Reads
+ * "<El>.<xc>.in" from the current working directory (src/util.F90:525).
+ * Idempotent after the first success (src/util.F90:29-33). */
+void acelibini_(int* nele, double* rcut, double* rcut_magnetic, double* smear, int* xcnumber,
+                int* elenumbers);
+
+/* Replaces acelib (src/ace.F90:79-321). Inputs (caller-owned, read-only):
+ *   nlist[nei] 1-based j (unused), occ[natom], occlist[nei] (must be 1),
+ *   nstart/nstop[natom] 1-based inclusive bond ranges,
+ *   dlist[nei] = r_ij, elist[3*nei] = (x_i - x_j)/r_ij,
+ *   dlist_momi[natom] = |m_i|, elist_momi[3*natom] = m_hat_i,
+ *   dlist_mom[nei] = |m_j|, elist_mom[3*nei] = m_hat_j.
+ * Outputs: eout[natom] = E_i; flist[3*nei] = dE_i/d(x_i - x_j) per bond;
+ *   tlist[3*nei] = dE_i/dm_j per bond; tlist0[3*natom] = dE_i/dm_i.
+ *   Per-bond outputs are packed atom by atom in bond order
+ *   (src/ace.F90:291-318). Computed on the GPU in the precision selected by
+ *   ace_set_precision (default: FP64). */
+void acelib_(int* natom, int* nall, int* nei, int* nlist, int* occ, int* occlist, int* nstart,
+             int* nstop, double* eout, double* dlist, double* elist, double* flist,
+             double* dlist_momi, double* elist_momi, double* dlist_mom, double* elist_mom,
+             double* tlist, double* tlist0);
+
+/* ---- status (no counterpart in the reference, which stops instead) ----- */
+int ace_last_error(void);
+const char* ace_error_string(int code);
+const char* ace_last_error_message(void);
+void ace_clear_error(void);
+
+/* ---- extended API -------------------------------------------------------- */
+
+/* As acelibini_ but with an explicit file path and element symbol; replaces
+ * any previous potential. Host-only: builds every table but touches no GPU. */
+int ace_init_file(const char* path, const char* element, double rcut, double rcut_magnetic,
+                  double smear, int xcnumber);
+
+/* 0 = plain FP64 throughout (the drop-in default, parity <= 1e-10 relative).
+ * 1 = split precision: FP32 basis/products with FP64 accumulation of the
+ *     per-atom energy and the embedding near zero density. */
+int ace_set_precision(int mode);
+int ace_get_precision(void);
+
+/* Basis sizes after init: out[0..3] = number of 1-,2-,3-,4-body clusters
+ * (nvar1..nvar4), out[4..6] = 2-,3-,4-body product terms, out[7] = cluster
+ * records in the file that matched no enumerated cluster. */
+int ace_basis_sizes(int* out);
+
+/* Cluster index rows as in the file's 'clu' records: rank 1 -> 1 int per
+ * cluster, 2 -> 4, 3 -> 9, 4 -> 15. */
+int ace_basis_rows(int rank, int* out);
+
+/* Evaluation on device-resident arrays (no host copies). Bonds of atom i are
+ * bond_offset[i] .. bond_offset[i+1]-1 (0-based CSR, natom+1 entries).
+ * r[nei], e[3*nei] = (x_i - x_j)/r, mag_j[nei], mhat_j[3*nei], mag_i[natom],
+ * mhat_i[3*natom]; outputs energy[natom], fij[3*nei], tij[3*nei], ti0[3*natom].
+ * `stream` is a cudaStream_t or NULL for the library stream; the call is
+ * asynchronous with respect to the host. Check ace_device_status() after the
+ * stream has completed. */
+int ace_compute_device(int natom, int nei, const int* bond_offset, const double* r,
+                       const double* e, const double* mag_j, const double* mhat_j,
+                       const double* mag_i, const double* mhat_i, double* energy, double* fij,
+                       double* tij, double* ti0, void* stream);
+
+/* Reads (and clears) the device-side error word of the last ace_compute_device
+ * call; synchronises the library stream. */
+int ace_device_status(void);
+
+/* Number of kernel launches issued by the last evaluation call. */
+int ace_last_launch_count(void);
+
+/* Releases every device buffer held by the library (tables stay on the host). */
+void ace_release_device(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAGACE_H_ */

@@ -1,0 +1,553 @@
+// C ABI and runtime: the drop-in acelibini_/acelib_ entry points, the
+// extended ace_* API, device-table upload and device work buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "device_model.hpp"
+#include "kernels.hpp"
+#include "magace.h"
+#include "model.hpp"
+#include "potential.hpp"
+
+namespace magace {
+namespace {
+
+// element symbols indexed by atomic number + 1 - 1 (index 0 is the
+// placeholder 'X'; the caller passes atomic number + 1, src/ace.F90:30-37)
+const char* const kElements[] = {
+    "X",  "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",  "Ne", "Na", "Mg", "Al", "Si", "P",  "S",
+    "Cl", "Ar", "K",  "Ca", "Sc", "Ti", "V",  "Cr", "Mn", "Fe", "Co", "Ni", "Cu", "Zn", "Ga", "Ge", "As",
+    "Se", "Br", "Kr", "Rb", "Sr", "Y",  "Zr", "Nb", "Mo", "Tc", "Ru", "Rh", "Pd", "Ag", "Cd", "In", "Sn",
+    "Sb", "Te", "I",  "Xe", "Cs", "Ba", "La", "Ce", "Pr", "Nd", "Pm", "Sm", "Eu", "Gd", "Tb", "Dy", "Ho",
+    "Er", "Tm", "Yb", "Lu", "Hf", "Ta", "W",  "Re", "Os", "Ir", "Pt", "Au", "Hg", "Tl", "Pb", "Bi", "Po",
+    "At", "Rn", "Fr", "Ra", "Ac", "Th", "Pa", "U",  "Np", "Pu", "Am", "Cm", "Bk", "Cf", "Es", "Fm", "Md",
+    "No", "Lr"};
+const int kNumElements = sizeof(kElements) / sizeof(kElements[0]);
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    size_t want = std::max<size_t>(count, 1);
+    want += want / 4;  // geometric headroom for growing systems
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), want * sizeof(T));
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  cudaError_t upload(const std::vector<T>& v) {
+    cudaError_t e = reserve(v.size());
+    if (e != cudaSuccess) return e;
+    if (!v.empty()) e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct Runtime {
+  Model model;
+  bool ready = false;
+  bool ini_done = false;  // acelibini_ succeeded once (src/util.F90:29-33)
+  int precision = 0;
+  int last_error = MAGACE_OK;
+  std::string last_msg;
+  int last_launches = 0;
+
+  // device tables
+  bool dev_tables = false;
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  DevBuf<double> lut_a, lut_m, c1, k1, k2, k3, slot_mult;
+  DevBuf<float> lut_a32, lut_m32, k1f, k2f, k3f;
+  DevBuf<uint16_t> o1, o2, o3;
+  DevBuf<SegmentInfo> seg;
+  DevBuf<int32_t> order, slot_seg, slot_factor, slot_weight;
+  DeviceModel dm{};
+  int grid_cap = 0;
+
+  // work buffers
+  DevBuf<int> off, err;
+  DevBuf<double> r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0, rho1, core, edf, dedrho;
+  DevBuf<unsigned char> F, W;
+  std::vector<int> h_off;
+};
+
+Runtime& rt() {
+  static Runtime r;
+  return r;
+}
+
+int set_error(int code, const std::string& msg) {
+  Runtime& R = rt();
+  R.last_error = code;
+  R.last_msg = msg;
+  if (code != MAGACE_OK) std::fprintf(stderr, "magace: %s\n", msg.c_str());
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  return set_error(MAGACE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(call)                                \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_error(e_, #call); \
+  } while (0)
+
+void ylm_constants(double* alm, double* blm, double* cl, double* dl) {
+  // recurrence constants of src/spherical.F90:18-49, indexed by l(l+1)/2 + m
+  for (int i = 0; i < kMaxHalf; ++i) alm[i] = blm[i] = 0.0;
+  for (int l = 0; l <= kMaxL; ++l) cl[l] = dl[l] = 0.0;
+  for (int l = 1; l <= kMaxL; ++l) {
+    const double lsq = l * l, ld = 2 * l, l1 = 4 * lsq - 1, l2 = lsq - ld + 1;
+    for (int m = 0; m <= l - 2; ++m) {
+      const double msq = m * m;
+      alm[l * (l + 1) / 2 + m] = std::sqrt(l1 / (lsq - msq));
+      blm[l * (l + 1) / 2 + m] = -std::sqrt((l2 - msq) / (4 * l2 - 1));
+    }
+    cl[l] = -std::sqrt(1.0 + 0.5 / static_cast<double>(l));
+    dl[l] = std::sqrt(2.0 * (l - 1) + 3.0);
+  }
+}
+
+template <class T>
+std::vector<float> to_float(const std::vector<T>& v) {
+  return std::vector<float>(v.begin(), v.end());
+}
+
+int upload_tables() {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (R.dev_tables && R.device == dev) return MAGACE_OK;
+  R.device = dev;
+  if (!R.stream) CUDA_TRY(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
+  const Model& M = R.model;
+  const GatherTable& g = M.gt;
+  CUDA_TRY(R.lut_a.upload(M.lut.a));
+  CUDA_TRY(R.lut_m.upload(M.lut.m));
+  CUDA_TRY(R.lut_a32.upload(to_float(M.lut.a)));
+  CUDA_TRY(R.lut_m32.upload(to_float(M.lut.m)));
+  std::vector<double> c1(2 * M.L.nbm);
+  for (int d = 0; d < 2; ++d)
+    for (int n = 0; n < M.L.nbm; ++n) c1[d * M.L.nbm + n] = M.c1[d][n];
+  CUDA_TRY(R.c1.upload(c1));
+  auto cat = [](const std::vector<double>* k) {
+    std::vector<double> v(k[0]);
+    v.insert(v.end(), k[1].begin(), k[1].end());
+    return v;
+  };
+  std::vector<double> k1 = cat(g.k1), k2 = cat(g.k2), k3 = cat(g.k3);
+  CUDA_TRY(R.k1.upload(k1));
+  CUDA_TRY(R.k2.upload(k2));
+  CUDA_TRY(R.k3.upload(k3));
+  CUDA_TRY(R.k1f.upload(to_float(k1)));
+  CUDA_TRY(R.k2f.upload(to_float(k2)));
+  CUDA_TRY(R.k3f.upload(to_float(k3)));
+  CUDA_TRY(R.o1.upload(g.o1));
+  CUDA_TRY(R.o2.upload(g.o2));
+  CUDA_TRY(R.o3.upload(g.o3));
+  std::vector<SegmentInfo> seg(g.seg_slot.size());
+  for (size_t s = 0; s < seg.size(); ++s) seg[s] = {g.seg_arity[s], g.seg_first[s], g.seg_count[s], g.seg_slot[s]};
+  CUDA_TRY(R.seg.upload(seg));
+  CUDA_TRY(R.order.upload(g.order));
+  CUDA_TRY(R.slot_seg.upload(g.slot_seg_begin));
+  CUDA_TRY(R.slot_factor.upload(g.slot_factor));
+  CUDA_TRY(R.slot_weight.upload(g.slot_weight));
+  CUDA_TRY(R.slot_mult.upload(g.slot_mult));
+  double alm[kMaxHalf], blm[kMaxHalf], cl[kMaxL + 1], dl[kMaxL + 1];
+  ylm_constants(alm, blm, cl, dl);
+  upload_ylm_constants(alm, blm, cl, dl);
+
+  DeviceModel& d = R.dm;
+  const FactorLayout& L = M.L;
+  d.n3a = L.n3a; d.n3m = L.n3m; d.l3a = L.l3a; d.l3m = L.l3m;
+  d.nba = L.nba; d.n2m = L.n2m; d.l2m = L.l2m; d.nbm = L.nbm;
+  d.lsa = L.lsa; d.ls3 = L.ls3; d.ls2 = L.ls2; d.h3 = L.h3; d.h2 = L.h2;
+  d.offA = L.offA; d.offA2 = L.offA2; d.offA0 = L.offA0; d.offOne = L.offOne; d.offZero = L.offZero;
+  d.nF = L.nF; d.nWA = L.nWA; d.offW2 = L.offW2; d.offW0 = L.offW0; d.nW = L.nW;
+  d.nd = M.ndensity;
+  d.nfemb = M.nfemb;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) d.par[a][b] = M.par[a][b];
+  d.ecut = M.ecut;
+  d.decut = M.decut;
+  d.nlut = M.lut.nlut;
+  d.nfa = M.lut.nfa;
+  d.nfm = M.lut.nfm;
+  d.rscale_a = M.lut.rscale_a;
+  d.rscale_m = M.lut.rscale_m;
+  d.lut_a = R.lut_a.p;
+  d.lut_m = R.lut_m.p;
+  d.lut_a32 = R.lut_a32.p;
+  d.lut_m32 = R.lut_m32.p;
+  d.c1 = R.c1.p;
+  d.nslot = g.nslot;
+  d.nG0 = g.nG0;
+  d.nseg = static_cast<int>(g.seg_slot.size());
+  d.ne1 = static_cast<int>(g.k1[0].size());
+  d.ne2 = static_cast<int>(g.k2[0].size());
+  d.ne3 = static_cast<int>(g.k3[0].size());
+  d.k1 = R.k1.p; d.k2 = R.k2.p; d.k3 = R.k3.p;
+  d.k1f = R.k1f.p; d.k2f = R.k2f.p; d.k3f = R.k3f.p;
+  d.o1 = R.o1.p; d.o2 = R.o2.p; d.o3 = R.o3.p;
+  d.seg = R.seg.p;
+  d.order = R.order.p;
+  d.slot_seg = R.slot_seg.p;
+  d.slot_factor = R.slot_factor.p;
+  d.slot_weight = R.slot_weight.p;
+  d.slot_mult = R.slot_mult.p;
+  int sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  R.grid_cap = std::max(1, sms) * 64;
+  int smem_max = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  for (int p = 0; p < 2; ++p)
+    for (int w = 0; w < 3; ++w)
+      if (eval_smem_bytes(d, p, w) > static_cast<size_t>(smem_max))
+        return set_error(MAGACE_ERR_UNSUPPORTED, "basis too large for the kernels' shared-memory tiles");
+  R.dev_tables = true;
+  return MAGACE_OK;
+}
+
+int reserve_work(int natom, int nei) {
+  Runtime& R = rt();
+  const size_t na = static_cast<size_t>(natom), nb = static_cast<size_t>(nei);
+  const size_t csz = R.precision == 0 ? 16 : 8;
+  CUDA_TRY(R.off.reserve(na + 1));
+  CUDA_TRY(R.err.reserve(1));
+  CUDA_TRY(R.energy.reserve(na));
+  CUDA_TRY(R.rho1.reserve(2 * na));
+  CUDA_TRY(R.core.reserve(na));
+  CUDA_TRY(R.edf.reserve(na));
+  CUDA_TRY(R.dedrho.reserve(2 * na));
+  CUDA_TRY(R.F.reserve(na * R.dm.nF * csz));
+  CUDA_TRY(R.W.reserve(na * R.dm.nW * csz));
+  (void)nb;
+  return MAGACE_OK;
+}
+
+int run_eval(EvalBuffers& b, cudaStream_t st) {
+  Runtime& R = rt();
+  b.F = R.F.p;
+  b.W = R.W.p;
+  b.rho1 = R.rho1.p;
+  b.core = R.core.p;
+  b.edf = R.edf.p;
+  b.dedrho = R.dedrho.p;
+  b.err = R.err.p;
+  CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), st));
+  R.last_launches = R.precision == 0 ? launch_eval_fp64(R.dm, b, st, R.grid_cap)
+                                     : launch_eval_fp32(R.dm, b, st, R.grid_cap);
+  CUDA_TRY(cudaGetLastError());
+  return MAGACE_OK;
+}
+
+int device_error_to_status(int dev) {
+  switch (dev) {
+    case kDevOk: return MAGACE_OK;
+    case kDevSmallR: return set_error(MAGACE_ERR_SMALL_R, "encountered a very small distance");
+    case kDevMoment: return set_error(MAGACE_ERR_MOMENT, "moment magnitude negative, NaN or beyond the magnetic cutoff");
+    case kDevNaN: return set_error(MAGACE_ERR_NAN, "non-finite density");
+    default: return set_error(MAGACE_ERR_ARGS, "inconsistent bond tile");
+  }
+}
+
+int init_file(const char* path, const char* element, double rcut, double rcut_magnetic, double smear,
+              int xcnumber) {
+  Runtime& R = rt();
+  std::string xc;
+  if (xcnumber == 1) xc = "pbe";
+  else if (xcnumber == 2) xc = "lda";
+  else return set_error(MAGACE_ERR_ARGS, "unknown XC functional received by acelibini");
+  Potential pot;
+  std::string msg;
+  int st = read_potential(path, element, xc, smear, pot, msg);
+  if (st) return set_error(st, msg);
+  Model mdl;
+  st = build_model(pot, rcut, rcut_magnetic, mdl, msg);
+  if (st) return set_error(st, msg);
+  const FactorLayout& L = mdl.L;
+  if (L.l3a > kMaxL || L.l2m > kMaxL || L.nba > kMaxFeat || L.nbm > kMaxFeat ||
+      L.n3a * (L.l3a + 1) > kMaxFeat || L.n2m * (L.l2m + 1) > kMaxFeat)
+    return set_error(MAGACE_ERR_UNSUPPORTED, "basis exceeds the kernels' compile-time limits (l <= 4, <= 32 radial functions)");
+  R.model = std::move(mdl);
+  R.ready = true;
+  R.dev_tables = false;
+  return set_error(MAGACE_OK, "");
+}
+
+}  // namespace
+}  // namespace magace
+
+using namespace magace;
+
+extern "C" {
+
+int ace_last_error(void) { return rt().last_error; }
+
+const char* ace_last_error_message(void) { return rt().last_msg.c_str(); }
+
+void ace_clear_error(void) {
+  rt().last_error = MAGACE_OK;
+  rt().last_msg.clear();
+}
+
+const char* ace_error_string(int code) {
+  switch (code) {
+    case MAGACE_OK: return "ok";
+    case MAGACE_ERR_FILE: return "potential file missing or unreadable";
+    case MAGACE_ERR_FORMAT: return "malformed or inconsistent potential file";
+    case MAGACE_ERR_UNSUPPORTED: return "unsupported potential or argument";
+    case MAGACE_ERR_SMALL_R: return "bond shorter than one lookup-table bin";
+    case MAGACE_ERR_MOMENT: return "moment magnitude out of the tabulated range";
+    case MAGACE_ERR_NOT_INIT: return "not initialised";
+    case MAGACE_ERR_ARGS: return "inconsistent arguments";
+    case MAGACE_ERR_CUDA: return "CUDA runtime failure";
+    case MAGACE_ERR_NAN: return "non-finite density";
+    default: return "unknown error";
+  }
+}
+
+int ace_init_file(const char* path, const char* element, double rcut, double rcut_magnetic, double smear,
+                  int xcnumber) {
+  if (!path || !element) return set_error(MAGACE_ERR_ARGS, "null path or element");
+  return init_file(path, element, rcut, rcut_magnetic, smear, xcnumber);
+}
+
+void acelibini_(int* nele, double* rcut, double* rcut_magnetic, double* smear, int* xcnumber, int* elenumbers) {
+  Runtime& R = rt();
+  if (R.ini_done) return;  // later calls are no-ops, as in src/util.F90:29-33
+  if (!nele || *nele != 1) {
+    set_error(MAGACE_ERR_UNSUPPORTED, "multiple elements require fixing acelibini call first");
+    return;
+  }
+  const int idx = elenumbers ? elenumbers[0] - 1 : -1;
+  if (idx < 1 || idx >= kNumElements) {
+    set_error(MAGACE_ERR_ARGS, "element number out of range");
+    return;
+  }
+  const char* el = kElements[idx];
+  const char* xc = *xcnumber == 1 ? "pbe" : (*xcnumber == 2 ? "lda" : "");
+  std::string path = std::string(el) + "." + xc + ".in";
+  if (init_file(path.c_str(), el, *rcut, *rcut_magnetic, *smear, *xcnumber) == MAGACE_OK) R.ini_done = true;
+}
+
+int ace_set_precision(int mode) {
+  if (mode != 0 && mode != 1) return set_error(MAGACE_ERR_ARGS, "precision mode must be 0 or 1");
+  rt().precision = mode;
+  return MAGACE_OK;
+}
+
+int ace_get_precision(void) { return rt().precision; }
+
+int ace_basis_sizes(int* out) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  for (int r = 1; r <= 4; ++r) out[r - 1] = static_cast<int>(R.model.rows[r].size());
+  out[4] = static_cast<int>(R.model.nterms[2]);
+  out[5] = static_cast<int>(R.model.nterms[3]);
+  out[6] = static_cast<int>(R.model.nterms[4]);
+  out[7] = R.model.unmatched_records;
+  return MAGACE_OK;
+}
+
+int ace_basis_rows(int rank, int* out) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  if (rank < 1 || rank > 4) return set_error(MAGACE_ERR_ARGS, "rank must be 1..4");
+  size_t k = 0;
+  for (const auto& row : R.model.rows[rank])
+    for (int v : row) out[k++] = v;
+  return MAGACE_OK;
+}
+
+int ace_last_launch_count(void) { return rt().last_launches; }
+
+int ace_compute_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
+                       const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
+                       double* energy, double* fij, double* tij, double* ti0, void* stream) {
+  Runtime& R = rt();
+  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
+  int st = upload_tables();
+  if (st) return st;
+  st = reserve_work(natom, nei);
+  if (st) return st;
+  EvalBuffers b;
+  b.natom = natom;
+  b.nei = nei;
+  b.off = bond_offset;
+  b.r = r;
+  b.e = e;
+  b.magj = mag_j;
+  b.mhj = mhat_j;
+  b.magi = mag_i;
+  b.mhi = mhat_i;
+  b.energy = energy;
+  b.fij = fij;
+  b.tij = tij;
+  b.ti0 = ti0;
+  return run_eval(b, stream ? static_cast<cudaStream_t>(stream) : R.stream);
+}
+
+int ace_device_status(void) {
+  Runtime& R = rt();
+  if (!R.err.p) return MAGACE_OK;
+  int dev = 0;
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(&dev, R.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemset(R.err.p, 0, sizeof(int)));
+  return device_error_to_status(dev);
+}
+
+void ace_release_device(void) {
+  Runtime& R = rt();
+  for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.k1, &R.k2, &R.k3, &R.slot_mult, &R.r, &R.e, &R.magj, &R.mhj,
+                  &R.magi, &R.mhi, &R.energy, &R.fij, &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
+    b->release();
+  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.k1f, &R.k2f, &R.k3f}) b->release();
+  for (auto* b : {&R.o1, &R.o2, &R.o3}) b->release();
+  for (auto* b : {&R.order, &R.slot_seg, &R.slot_factor, &R.slot_weight}) b->release();
+  R.seg.release();
+  R.off.release();
+  R.err.release();
+  R.F.release();
+  R.W.release();
+  if (R.stream) cudaStreamDestroy(R.stream);
+  R.stream = nullptr;
+  R.dev_tables = false;
+}
+
+void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occlist, int* nstart, int* nstop,
+             double* eout, double* dlist, double* elist, double* flist, double* dlist_momi, double* elist_momi,
+             double* dlist_mom, double* elist_mom, double* tlist, double* tlist0) {
+  (void)nall;
+  (void)nlist;
+  Runtime& R = rt();
+  const int natom = natom_p ? *natom_p : -1, nei = nei_p ? *nei_p : -1;
+  // total packed bonds and contiguity of the caller's ranges
+  auto fail = [&](int code, const char* msg, long npacked) {
+    set_error(code, msg);
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    if (natom > 0) {
+      std::fill(eout, eout + natom, nan);
+      std::fill(tlist0, tlist0 + 3L * natom, nan);
+    }
+    if (npacked > 0) {
+      std::fill(flist, flist + 3 * npacked, nan);
+      std::fill(tlist, tlist + 3 * npacked, nan);
+    }
+  };
+  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes"), void();
+  if (!R.ready) return fail(MAGACE_ERR_NOT_INIT, "acelib_ called before a successful acelibini_", 0);
+  std::vector<int>& off = R.h_off;
+  off.assign(natom + 1, 0);
+  bool contiguous = true;
+  for (int i = 0; i < natom; ++i) {
+    const int cnt = nstop[i] >= nstart[i] ? nstop[i] - nstart[i] + 1 : 0;
+    if (cnt > 0 && (nstart[i] < 1 || nstop[i] > nei)) return fail(MAGACE_ERR_ARGS, "bond range outside 1..nei", 0);
+    if (occ && occ[i] != 1) return fail(MAGACE_ERR_ARGS, "element index other than 1 (single element)", 0);
+    if (cnt > 0 && nstart[i] != off[i] + 1) contiguous = false;
+    off[i + 1] = off[i] + cnt;
+  }
+  const long npacked = off[natom];
+  if (occlist)
+    for (int j = 0; j < nei; ++j)
+      if (occlist[j] != 1) return fail(MAGACE_ERR_ARGS, "neighbour element index other than 1", npacked);
+  int st = upload_tables();
+  if (st) return fail(st, R.last_msg.c_str(), npacked);
+  st = reserve_work(natom, static_cast<int>(npacked));
+  if (st) return fail(st, R.last_msg.c_str(), npacked);
+  const size_t na = natom, nb = npacked;
+  cudaStream_t s = R.stream;
+  auto res = [&](DevBuf<double>& b, size_t n) { return b.reserve(n) == cudaSuccess; };
+  if (!(res(R.r, nb) && res(R.e, 3 * nb) && res(R.magj, nb) && res(R.mhj, 3 * nb) && res(R.magi, na) &&
+        res(R.mhi, 3 * na) && res(R.fij, 3 * nb) && res(R.tij, 3 * nb) && res(R.ti0, 3 * na)) ||
+      R.off.reserve(na + 1) != cudaSuccess)
+    return fail(MAGACE_ERR_CUDA, "device allocation failed", npacked);
+  // inputs; non-contiguous ranges are gathered into atom order first
+  std::vector<double> gr, ge, gm, gmh;
+  const double *pr = dlist, *pe = elist, *pm = dlist_mom, *pmh = elist_mom;
+  if (!contiguous) {
+    gr.resize(nb);
+    ge.resize(3 * nb);
+    gm.resize(nb);
+    gmh.resize(3 * nb);
+    for (int i = 0; i < natom; ++i)
+      for (int k = 0; k < off[i + 1] - off[i]; ++k) {
+        const size_t src = nstart[i] - 1 + k, dst = off[i] + k;
+        gr[dst] = dlist[src];
+        gm[dst] = dlist_mom[src];
+        for (int c = 0; c < 3; ++c) {
+          ge[3 * dst + c] = elist[3 * src + c];
+          gmh[3 * dst + c] = elist_mom[3 * src + c];
+        }
+      }
+    pr = gr.data();
+    pe = ge.data();
+    pm = gm.data();
+    pmh = gmh.data();
+  }
+  cudaError_t ce = cudaSuccess;
+  auto h2d = [&](void* d, const void* h, size_t bytes) {
+    if (ce == cudaSuccess && bytes) ce = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
+  };
+  h2d(R.off.p, off.data(), (na + 1) * sizeof(int));
+  h2d(R.r.p, pr, nb * sizeof(double));
+  h2d(R.e.p, pe, 3 * nb * sizeof(double));
+  h2d(R.magj.p, pm, nb * sizeof(double));
+  h2d(R.mhj.p, pmh, 3 * nb * sizeof(double));
+  h2d(R.magi.p, dlist_momi, na * sizeof(double));
+  h2d(R.mhi.p, elist_momi, 3 * na * sizeof(double));
+  if (ce != cudaSuccess) return fail(MAGACE_ERR_CUDA, cudaGetErrorString(ce), npacked);
+  EvalBuffers b;
+  b.natom = natom;
+  b.nei = static_cast<int>(npacked);
+  b.off = R.off.p;
+  b.r = R.r.p;
+  b.e = R.e.p;
+  b.magj = R.magj.p;
+  b.mhj = R.mhj.p;
+  b.magi = R.magi.p;
+  b.mhi = R.mhi.p;
+  b.energy = R.energy.p;
+  b.fij = R.fij.p;
+  b.tij = R.tij.p;
+  b.ti0 = R.ti0.p;
+  if (run_eval(b, s)) return fail(R.last_error, R.last_msg.c_str(), npacked);
+  int dev_err = 0;
+  auto d2h = [&](void* h, const void* d, size_t bytes) {
+    if (ce == cudaSuccess && bytes) ce = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, s);
+  };
+  d2h(eout, R.energy.p, na * sizeof(double));
+  d2h(flist, R.fij.p, 3 * nb * sizeof(double));
+  d2h(tlist, R.tij.p, 3 * nb * sizeof(double));
+  d2h(tlist0, R.ti0.p, 3 * na * sizeof(double));
+  d2h(&dev_err, R.err.p, sizeof(int));
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return fail(MAGACE_ERR_CUDA, cudaGetErrorString(ce), npacked);
+  if (dev_err) {
+    const int code = device_error_to_status(dev_err);
+    return fail(code, R.last_msg.c_str(), npacked);
+  }
+  set_error(MAGACE_OK, "");
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// Plain-old-data view of the model for the kernels: sizes, constants and
+// device pointers. Passed by value as a kernel argument.
+#pragma once
+
+#include <cstdint>
+
+namespace magace {
+
+// largest angular momentum the kernels' fixed-size scratch arrays support
+constexpr int kMaxL = 4;
+constexpr int kMaxHalf = (kMaxL + 1) * (kMaxL + 2) / 2;  // packed (l, m >= 0)
+constexpr int kMaxFull = (kMaxL + 1) * (kMaxL + 1);      // packed (l, -l..l)
+
+// device-side error codes (first one wins)
+enum DeviceError : int {
+  kDevOk = 0,
+  kDevSmallR = 1,  // r below the first LUT bin
+  kDevMoment = 2,  // |m| negative, NaN or beyond the magnetic cutoff
+  kDevNaN = 3,     // non-finite density
+  kDevShape = 4,   // more bonds than a tile index can address
+};
+
+struct SegmentInfo {
+  int32_t arity;  // number of other factors (1..3)
+  int32_t first;  // first entry in the arity's arrays
+  int32_t count;  // entries in this segment
+  int32_t slot;   // output slot
+};
+
+struct DeviceModel {
+  // basis dims (see model.hpp for the layouts)
+  int n3a, n3m, l3a, l3m, nba, n2m, l2m, nbm;
+  int lsa, ls3, ls2, h3, h2;
+  int offA, offA2, offA0, offOne, offZero, nF;
+  int nWA, offW2, offW0, nW;
+  int nd, nfemb;
+  double par[2][2];  // embedding parameters [order][density]
+  double ecut, decut;
+  // radial lookup tables: [(nlut+1)][nf] double4 of cubic coefficients
+  int nlut, nfa, nfm;
+  double rscale_a, rscale_m;
+  const double* lut_a;
+  const double* lut_m;
+  const float* lut_a32;  // FP32 copies for the split-precision path
+  const float* lut_m32;
+  // 1-body coefficients c1[d * nbm + n]
+  const double* c1;
+  // gather table
+  int nslot, nG0, nseg;
+  int ne1, ne2, ne3;        // entries per arity (stride of the second density)
+  const double* k1;          // [nd][ne1]
+  const double* k2;
+  const double* k3;
+  const float* k1f;          // FP32 copies (split path)
+  const float* k2f;
+  const float* k3f;
+  const uint16_t* o1;        // [ne1]
+  const uint16_t* o2;        // [2*ne2]
+  const uint16_t* o3;        // [3*ne3]
+  const SegmentInfo* seg;    // [nseg]
+  const int32_t* order;      // [nseg] processing order
+  const int32_t* slot_seg;   // [nslot+1]
+  const int32_t* slot_factor;  // [nslot] (G0 slots only)
+  const int32_t* slot_weight;  // [nslot]
+  const double* slot_mult;     // [nslot]
+};
+
+}  // namespace magace

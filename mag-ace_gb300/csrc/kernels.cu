@@ -1,0 +1,814 @@
+// Hot-path kernels for sm_103a.
+//
+//   k_abasis   one CTA per atom: per-bond radial lookups and spherical
+//              harmonics, then the bond sums A, A2 (m' >= 0 half, completed by
+//              conjugate symmetry), the on-site A0 and the 1-body density.
+//              (reference: src/a_basis.F90:5-361, src/radial.F90:53-160,
+//              src/spherical.F90:55-282)
+//   k_density  one CTA per atom: density rho = sum kappa * prod(factors) and
+//              the weights dE/dA as a deterministic gather over the folded
+//              term tables, the embedding F(rho) and the inner cutoff.
+//              (reference: src/b_basis.F90:6-307, src/forces.F90:5-362,
+//              :976-1289)
+//   k_forces   one CTA per atom, one thread per bond: recomputes the bond's
+//              features with derivatives and contracts them with the weights
+//              into dE_i/d(x_i - x_j) and dE_i/dm_j; thread 0 adds dE_i/dm_i.
+//              (reference: src/forces.F90:366-972)
+//
+// The kernels are templated on the arithmetic type R of features, factors
+// and weights (double: the drop-in FP64 path; float: the split path, whose
+// per-atom density, energy and output sums stay in double).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_model.hpp"
+#include "kernels.hpp"
+
+namespace magace {
+
+__constant__ double c_alm[kMaxHalf];
+__constant__ double c_blm[kMaxHalf];
+__constant__ double c_cl[kMaxL + 1];
+__constant__ double c_dl[kMaxL + 1];
+
+template <class R>
+struct C {
+  R x, y;
+};
+template <class R>
+__device__ __forceinline__ C<R> cmul(C<R> a, C<R> b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <class R>
+__device__ __forceinline__ C<R> cscale(C<R> a, R s) {
+  return {a.x * s, a.y * s};
+}
+template <class R>
+__device__ __forceinline__ C<R> cconj(C<R> a) {
+  return {a.x, -a.y};
+}
+template <class R>
+__device__ __forceinline__ R re_mul(C<R> a, C<R> b) {
+  return a.x * b.x - a.y * b.y;
+}
+
+__device__ __forceinline__ int ph(int l, int m) { return l * (l + 1) / 2 + m; }
+__device__ __forceinline__ double parity(int m) { return (m & 1) ? -1.0 : 1.0; }
+
+__device__ __forceinline__ void raise_error(int* err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+// Spherical harmonics Y_lm (m >= 0 half, packed by ph) of a unit vector and,
+// optionally, their tangential gradients dY = grad Y - (r . grad Y) r, in the
+// normalisation and recurrence of src/spherical.F90:55-260 (Y_00 = 1,
+// Condon-Shortley phase through cl).
+template <class R, bool GRAD>
+__device__ void ylm_half(int L, R rx, R ry, R rz, C<R>* Y, C<R> (*dY)[3]) {
+  R plm[kMaxHalf], dplm[kMaxHalf];
+  const R sq3 = R(1.73205080756887719318), sq3o2 = R(1.22474487139158894067);
+  plm[0] = R(1);
+  dplm[0] = R(0);
+  if (L > 0) {
+    plm[ph(1, 0)] = sq3 * rz;
+    dplm[ph(1, 0)] = sq3;
+    plm[ph(1, 1)] = -sq3o2;
+    dplm[ph(1, 1)] = R(0);
+    for (int l = 2; l <= L; ++l) {
+      for (int m = 0; m <= l - 2; ++m) {
+        const int k = ph(l, m), k1 = ph(l - 1, m), k2 = ph(l - 2, m);
+        const R a = R(c_alm[k]), b = R(c_blm[k]);
+        plm[k] = a * (rz * plm[k1] + b * plm[k2]);
+        dplm[k] = a * (plm[k1] + rz * dplm[k1] + b * dplm[k2]);
+      }
+      const int k = ph(l - 1, l - 1);
+      const R t = R(c_dl[l]) * plm[k];
+      plm[ph(l, l - 1)] = t * rz;
+      dplm[ph(l, l - 1)] = t;
+      plm[ph(l, l)] = R(c_cl[l]) * plm[k];
+      dplm[ph(l, l)] = R(0);
+    }
+  }
+  for (int l = 0; l <= L; ++l) {  // m = 0
+    const int k = ph(l, 0);
+    Y[k] = {plm[k], R(0)};
+    if (GRAD) {
+      const R dyz = dplm[k], rdy = dyz * rz;
+      dY[k][0] = {-rdy * rx, R(0)};
+      dY[k][1] = {-rdy * ry, R(0)};
+      dY[k][2] = {dyz - rdy * rz, R(0)};
+    }
+  }
+  for (int l = 1; l <= L; ++l) {  // m = 1
+    const int k = ph(l, 1);
+    Y[k] = {rx * plm[k], ry * plm[k]};
+    if (GRAD) {
+      const C<R> dyz = {rx * dplm[k], ry * dplm[k]};
+      const C<R> rdy = {rx * plm[k] + rz * dyz.x, ry * plm[k] + rz * dyz.y};
+      dY[k][0] = {plm[k] - rdy.x * rx, -(rdy.y * rx)};
+      dY[k][1] = {-rdy.x * ry, plm[k] - rdy.y * ry};
+      dY[k][2] = {dyz.x - rdy.x * rz, dyz.y - rdy.y * rz};
+    }
+  }
+  C<R> phasem = {rx, ry};
+  const C<R> phase = {rx, ry};
+  for (int m = 2; m <= L; ++m) {  // m > 1
+    const C<R> mph = {phasem.x * R(m), phasem.y * R(m)};
+    phasem = cmul(phasem, phase);
+    for (int l = m; l <= L; ++l) {
+      const int k = ph(l, m);
+      Y[k] = {phasem.x * plm[k], phasem.y * plm[k]};
+      if (GRAD) {
+        const C<R> dyx = cscale(mph, plm[k]);
+        const C<R> dyy = {-dyx.y, dyx.x};
+        const C<R> dyz = cscale(phasem, dplm[k]);
+        const C<R> rdy = {rx * dyx.x + ry * dyy.x + rz * dyz.x, rx * dyx.y + ry * dyy.y + rz * dyz.y};
+        dY[k][0] = {dyx.x - rdy.x * rx, dyx.y - rdy.y * rx};
+        dY[k][1] = {dyy.x - rdy.x * ry, dyy.y - rdy.y * ry};
+        dY[k][2] = {dyz.x - rdy.x * rz, dyz.y - rdy.y * rz};
+      }
+    }
+  }
+}
+
+// full-range Y_lm (packed l*l+l+m) from the half
+template <class R>
+__device__ __forceinline__ C<R> y_full(const C<R>* Yh, int l, int m) {
+  if (m >= 0) return Yh[ph(l, m)];
+  const C<R> y = Yh[ph(l, -m)];
+  const R s = R(parity(m));
+  return {y.x * s, -y.y * s};
+}
+
+// Cubic-Hermite lookup of `count` consecutive functions starting at `f0` of a
+// table with `nf` functions per bin (src/radial.F90:85-105).
+template <class R, bool GRAD>
+__device__ __forceinline__ void lut_eval(const double* __restrict__ lut, int nf, int f0, int count, int nl,
+                                         double wl, double rscale, R* v, R* dv) {
+  const double wl2 = wl * wl, wl3 = wl2 * wl, w2 = 2.0 * wl, w3 = 3.0 * wl2;
+  const double2* c2 = reinterpret_cast<const double2*>(lut) + 2 * (static_cast<size_t>(nl) * nf + f0);
+  for (int f = 0; f < count; ++f) {
+    const double2 a = __ldg(c2 + 2 * f), b = __ldg(c2 + 2 * f + 1);
+    v[f] = R(a.x + a.y * wl + b.x * wl2 + b.y * wl3);
+    if (GRAD) dv[f] = R((a.y + b.x * w2 + b.y * w3) * rscale);
+  }
+}
+
+// bins of the atomic table: returns false (features zero) beyond the cutoff
+__device__ __forceinline__ int atomic_bin(const DeviceModel& m, double r, double& wl, int* err) {
+  const double x = r * m.rscale_a;
+  if (!(x >= 1.0)) {
+    raise_error(err, kDevSmallR);
+    return -1;
+  }
+  if (x >= static_cast<double>(m.nlut)) return 0;  // zero features (src/radial.F90:77-83)
+  const int nl = static_cast<int>(floor(x));
+  wl = x - static_cast<double>(nl);
+  return nl;
+}
+
+// bins of the magnetic table: 0 means |m| inside the first bin, where every
+// function is 1 and every derivative 0 (src/radial.F90:135-139)
+__device__ __forceinline__ int magnetic_bin(const DeviceModel& m, double mag, double& wl, int* err) {
+  const double x = mag * m.rscale_m;
+  if (!(x >= 0.0) || x >= static_cast<double>(m.nlut)) {
+    raise_error(err, kDevMoment);
+    return -1;
+  }
+  const int nl = static_cast<int>(floor(x));
+  wl = x - static_cast<double>(nl);
+  return nl;
+}
+
+// ===========================================================================
+// k_abasis
+// Shared memory: acc[nWA + nba*n2m*h2] (complex R), then per tile of TB bonds
+// (SoA, [feature][TB]): g[nba], RY[n3a*lsa] (complex), Q[n2m*h2] (complex),
+// core[1].
+template <class R>
+__global__ void __launch_bounds__(kAbasisThreads)
+    k_abasis(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
+             const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
+             const double* __restrict__ magi, const double* __restrict__ mhi, C<R>* __restrict__ F,
+             double* __restrict__ rho1, double* __restrict__ core_out, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int TB = kAbasisTile;
+  const int nA2h = m.nba * m.n2m * m.h2;
+  const int nacc = m.nWA + nA2h;
+  C<R>* acc = reinterpret_cast<C<R>*>(smem);
+  C<R>* sRY = acc + nacc;                      // [n3a*lsa][TB]
+  C<R>* sQ = sRY + m.n3a * m.lsa * TB;         // [n2m*h2][TB]
+  R* sg = reinterpret_cast<R*>(sQ + m.n2m * m.h2 * TB);  // [nba][TB]
+  double* score = reinterpret_cast<double*>(sg + m.nba * TB);  // [TB]
+  __shared__ double s_core;
+
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    for (int s = threadIdx.x; s < nacc; s += blockDim.x) acc[s] = {R(0), R(0)};
+    if (threadIdx.x == 0) s_core = 0.0;
+    const int b0 = off[atom], b1 = off[atom + 1];
+    __syncthreads();
+    for (int t0 = b0; t0 < b1; t0 += TB) {
+      const int nb = min(TB, b1 - t0);
+      if (threadIdx.x < nb) {
+        const int b = threadIdx.x, j = t0 + b;
+        const double r = rr[j];
+        R g[32], Rv[16], Mv[32], cv[1], dummy[1];
+        double wl = 0.0;
+        const int nla = atomic_bin(m, r, wl, err);
+        if (nla > 0) {
+          lut_eval<R, false>(m.lut_a, m.nfa, 0, m.nba, nla, wl, m.rscale_a, g, dummy);
+          lut_eval<R, false>(m.lut_a, m.nfa, m.nba, m.n3a * (m.l3a + 1), nla, wl, m.rscale_a, Rv, dummy);
+          lut_eval<R, false>(m.lut_a, m.nfa, m.nba + m.n3a * (m.l3a + 1), 1, nla, wl, m.rscale_a, cv, dummy);
+        } else {
+          for (int q = 0; q < m.nba; ++q) g[q] = R(0);
+          for (int q = 0; q < m.n3a * (m.l3a + 1); ++q) Rv[q] = R(0);
+          cv[0] = R(0);
+        }
+        double wm = 0.0;
+        const int nlm = magnetic_bin(m, magj[j], wm, err);
+        const int nM = m.n2m * (m.l2m + 1);
+        if (nlm > 0) {
+          lut_eval<R, false>(m.lut_m, m.nfm, 0, nM, nlm, wm, m.rscale_m, Mv, dummy);
+        } else {
+          for (int q = 0; q < nM; ++q) Mv[q] = R(nlm == 0 ? 1 : 0);
+        }
+        C<R> Ya[kMaxHalf], Ym[kMaxHalf];
+        ylm_half<R, false>(m.l3a, R(ee[3 * j]), R(ee[3 * j + 1]), R(ee[3 * j + 2]), Ya, nullptr);
+        ylm_half<R, false>(m.l2m, R(mhj[3 * j]), R(mhj[3 * j + 1]), R(mhj[3 * j + 2]), Ym, nullptr);
+        for (int n1 = 0; n1 < m.n3a; ++n1)
+          for (int l1 = 0; l1 <= m.l3a; ++l1)
+            for (int m1 = -l1; m1 <= l1; ++m1)
+              sRY[(n1 * m.lsa + l1 * l1 + l1 + m1) * TB + b] = cscale(y_full(Ya, l1, m1), Rv[n1 * (m.l3a + 1) + l1]);
+        for (int nr = 0; nr < m.n2m; ++nr)
+          for (int l = 0; l <= m.l2m; ++l)
+            for (int mm = 0; mm <= l; ++mm)
+              sQ[(nr * m.h2 + ph(l, mm)) * TB + b] = cscale(Ym[ph(l, mm)], Mv[nr * (m.l2m + 1) + l]);
+        for (int n = 0; n < m.nba; ++n) sg[n * TB + b] = g[n];
+        score[b] = static_cast<double>(cv[0]);
+      }
+      __syncthreads();
+      for (int s = threadIdx.x; s < nacc; s += blockDim.x) {
+        C<R> a = acc[s];
+        if (s < m.nWA) {
+          // s = ((n1*lsa + lma)*n3m + n2)*h3 + h
+          const int h = s % m.h3;
+          const int q = s / m.h3;
+          const int n2 = q % m.n3m;
+          const int ia = q / m.n3m;  // n1*lsa + lma
+          const C<R>* ry = sRY + ia * TB;
+          const C<R>* qq = sQ + (n2 * m.h2 + h) * TB;
+          for (int b = 0; b < nb; ++b) {
+            const C<R> u = ry[b], v = qq[b];
+            a.x += u.x * v.x - u.y * v.y;
+            a.y += u.x * v.y + u.y * v.x;
+          }
+        } else {
+          // A2 half: (s - nWA) = (n*n2m + nr)*h2 + h
+          const int t = s - m.nWA;
+          const int h = t % m.h2;
+          const int q = t / m.h2;
+          const int nr = q % m.n2m;
+          const int n = q / m.n2m;
+          const R* gg = sg + n * TB;
+          const C<R>* qq = sQ + (nr * m.h2 + h) * TB;
+          for (int b = 0; b < nb; ++b) {
+            a.x += gg[b] * qq[b].x;
+            a.y += gg[b] * qq[b].y;
+          }
+        }
+        acc[s] = a;
+      }
+      if (threadIdx.x == 0)
+        for (int b = 0; b < nb; ++b) s_core += score[b];
+      __syncthreads();
+    }
+    // complete A and A2 by A(m1,m2) = (-1)^(m1+m2) conj A(-m1,-m2) and write F
+    C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
+    const int nA = m.offA2 - m.offA;
+    for (int s = threadIdx.x; s < nA; s += blockDim.x) {
+      const int lmm = s % m.ls3;
+      const int q = s / m.ls3;
+      const int n2 = q % m.n3m;
+      const int ia = q / m.n3m;
+      const int n1 = ia / m.lsa, lma = ia % m.lsa;
+      int l2 = 0;
+      while ((l2 + 1) * (l2 + 1) <= lmm) ++l2;
+      const int m2 = lmm - l2 * l2 - l2;
+      int l1 = 0;
+      while ((l1 + 1) * (l1 + 1) <= lma) ++l1;
+      const int m1 = lma - l1 * l1 - l1;
+      C<R> v;
+      if (m2 >= 0) {
+        v = acc[((n1 * m.lsa + lma) * m.n3m + n2) * m.h3 + ph(l2, m2)];
+      } else {
+        const int lmb = l1 * l1 + l1 - m1;
+        const C<R> w = acc[((n1 * m.lsa + lmb) * m.n3m + n2) * m.h3 + ph(l2, -m2)];
+        const R sgn = R(parity(m1 + m2));
+        v = {w.x * sgn, -w.y * sgn};
+      }
+      Fa[m.offA + s] = v;
+    }
+    const int nA2 = m.offA0 - m.offA2;
+    for (int s = threadIdx.x; s < nA2; s += blockDim.x) {
+      const int lm = s % m.ls2;
+      const int q = s / m.ls2;  // n*n2m + nr
+      int l = 0;
+      while ((l + 1) * (l + 1) <= lm) ++l;
+      const int mm = lm - l * l - l;
+      const C<R> w = acc[m.nWA + q * m.h2 + ph(l, mm < 0 ? -mm : mm)];
+      C<R> v = w;
+      if (mm < 0) {
+        const R sgn = R(parity(mm));
+        v = {w.x * sgn, -w.y * sgn};
+      }
+      Fa[m.offA2 + s] = v;
+    }
+    if (threadIdx.x == 0) {
+      // on-site A0, the 1-body density and the constants
+      double wl = 0.0;
+      const int nl = magnetic_bin(m, magi[atom], wl, err);
+      R Mv[32], gm[32], dummy[1];
+      const int nM = m.n2m * (m.l2m + 1);
+      if (nl > 0) {
+        lut_eval<R, false>(m.lut_m, m.nfm, 0, nM, nl, wl, m.rscale_m, Mv, dummy);
+        lut_eval<R, false>(m.lut_m, m.nfm, nM, m.nbm, nl, wl, m.rscale_m, gm, dummy);
+      } else {
+        for (int q = 0; q < nM; ++q) Mv[q] = R(nl == 0 ? 1 : 0);
+        for (int q = 0; q < m.nbm; ++q) gm[q] = R(nl == 0 ? 1 : 0);
+      }
+      C<R> Yi[kMaxHalf];
+      ylm_half<R, false>(m.l2m, R(mhi[3 * atom]), R(mhi[3 * atom + 1]), R(mhi[3 * atom + 2]), Yi, nullptr);
+      for (int nr = 0; nr < m.n2m; ++nr)
+        for (int l = 0; l <= m.l2m; ++l)
+          for (int mm = -l; mm <= l; ++mm)
+            Fa[m.offA0 + nr * m.ls2 + l * l + l + mm] = cscale(y_full(Yi, l, mm), Mv[nr * (m.l2m + 1) + l]);
+      Fa[m.offOne] = {R(1), R(0)};
+      Fa[m.offZero] = {R(0), R(0)};
+      for (int d = 0; d < m.nd; ++d) {
+        double s = 0.0;
+        for (int n = 0; n < m.nbm; ++n) s += m.c1[d * m.nbm + n] * (static_cast<double>(gm[n]) - 1.0);
+        rho1[static_cast<size_t>(atom) * 2 + d] = s;
+      }
+      core_out[atom] = s_core;
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// Embedding F(rho) and derivative (src/forces.F90:1134-1266, nfemb 0-2)
+__device__ void embed(int nfemb, double rho, double wpre, double mexp, double& F, double& dF) {
+  const double w = 10.0, eps = 1e-10;
+  if (nfemb == 0) {
+    F = rho;
+    dF = 1.0;
+    return;
+  }
+  const double s = (nfemb == 2) ? 1.0 + rho : rho;
+  if (fabs(s) > eps) {
+    double y1 = w * s * s;
+    const double g = (y1 > 30.0) ? 0.0 : exp(-y1);
+    const double omg = 1.0 - g, a = fabs(s), sg = copysign(1.0, s);
+    y1 = pow(omg * a, mexp);
+    const double y2 = mexp * g * a;
+    F = (nfemb == 2) ? wpre * (sg * (y1 + y2) - 1.0) : wpre * sg * (y1 + y2);
+    const double dg = -2.0 * w * s * g, da = sg;
+    const double dy = (fabs(y1) < eps) ? 0.0 : mexp * y1 / (omg * a);
+    const double dy1 = dy * (-dg * a + omg * da), dy2 = mexp * (dg * a + g * da);
+    dF = wpre * sg * (dy1 + dy2);
+  } else {
+    F = (nfemb == 2) ? wpre * mexp * (s - 1.0) : wpre * mexp * rho;
+    dF = wpre * mexp;
+  }
+}
+
+// ===========================================================================
+// k_density
+// Shared memory: Fs[nF] (complex R), part[nseg][ND] (complex R),
+// tot[nslot][ND] (complex double).
+template <class R, int ND>
+__global__ void __launch_bounds__(kDensityThreads)
+    k_density(DeviceModel m, int natom, const C<R>* __restrict__ F, const double* __restrict__ rho1,
+              const double* __restrict__ core, C<R>* __restrict__ W, double* __restrict__ energy,
+              double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  C<R>* Fs = reinterpret_cast<C<R>*>(smem);
+  C<R>* part = Fs + ((m.nF + 1) & ~1);
+  C<double>* tot = reinterpret_cast<C<double>*>(part + ((m.nseg * ND + 1) & ~1));
+  __shared__ double s_red[kDensityThreads / 32][ND];
+  __shared__ double s_dE[ND];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    const C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
+    for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
+    __syncthreads();
+    for (int i = threadIdx.x; i < m.nseg; i += blockDim.x) {
+      const int sid = m.order[i];
+      const SegmentInfo sg = m.seg[sid];
+      C<R> acc[ND];
+      for (int d = 0; d < ND; ++d) acc[d] = {R(0), R(0)};
+      const int e0 = sg.first, e1 = sg.first + sg.count;
+      if (sg.arity == 2) {
+        for (int e = e0; e < e1; ++e) {
+          const C<R> p = cmul(Fs[m.o2[2 * e]], Fs[m.o2[2 * e + 1]]);
+          for (int d = 0; d < ND; ++d) {
+            const R k = R(m.k2[d * m.ne2 + e]);
+            acc[d].x += k * p.x;
+            acc[d].y += k * p.y;
+          }
+        }
+      } else if (sg.arity == 1) {
+        for (int e = e0; e < e1; ++e) {
+          const C<R> p = Fs[m.o1[e]];
+          for (int d = 0; d < ND; ++d) {
+            const R k = R(m.k1[d * m.ne1 + e]);
+            acc[d].x += k * p.x;
+            acc[d].y += k * p.y;
+          }
+        }
+      } else {
+        for (int e = e0; e < e1; ++e) {
+          const C<R> p = cmul(cmul(Fs[m.o3[3 * e]], Fs[m.o3[3 * e + 1]]), Fs[m.o3[3 * e + 2]]);
+          for (int d = 0; d < ND; ++d) {
+            const R k = R(m.k3[d * m.ne3 + e]);
+            acc[d].x += k * p.x;
+            acc[d].y += k * p.y;
+          }
+        }
+      }
+      for (int d = 0; d < ND; ++d) part[sid * ND + d] = acc[d];
+    }
+    __syncthreads();
+    double rloc[ND];
+    for (int d = 0; d < ND; ++d) rloc[d] = 0.0;
+    for (int s = threadIdx.x; s < m.nslot; s += blockDim.x) {
+      const int q0 = m.slot_seg[s], q1 = m.slot_seg[s + 1];
+      for (int d = 0; d < ND; ++d) {
+        C<double> t = {0.0, 0.0};
+        for (int q = q0; q < q1; ++q) {
+          t.x += static_cast<double>(part[q * ND + d].x);
+          t.y += static_cast<double>(part[q * ND + d].y);
+        }
+        tot[s * ND + d] = t;
+        if (s < m.nG0) {
+          const C<R> f = Fs[m.slot_factor[s]];
+          rloc[d] += static_cast<double>(f.x) * t.x - static_cast<double>(f.y) * t.y;
+        }
+      }
+    }
+    // deterministic block reduction of rho
+    for (int d = 0; d < ND; ++d) {
+      double v = rloc[d];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) s_red[warp][d] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double energyi = 0.0, dE[ND];
+      for (int d = 0; d < ND; ++d) {
+        double rho = rho1[static_cast<size_t>(atom) * 2 + d];
+        for (int w = 0; w < kDensityThreads / 32; ++w) rho += s_red[w][d];
+        if (!isfinite(rho)) raise_error(err, kDevNaN);
+        double Fd, dFd;
+        embed(m.nfemb, rho, m.par[0][d], m.par[1][d], Fd, dFd);
+        energyi = (d == 0) ? Fd : energyi + Fd;
+        dE[d] = dFd;
+      }
+      // inner cutoff on the hard-core energy (src/forces.F90:1112-1128, :1270-1289)
+      const double e = core[atom], elow = m.ecut - m.decut;
+      double fcut, dfcut;
+      if (e >= m.ecut) {
+        fcut = 0.0;
+        dfcut = 0.0;
+      } else if (e <= elow) {
+        fcut = 1.0;
+        dfcut = 0.0;
+      } else {
+        const double pi = 3.14159265358979323846264338327950288419;
+        fcut = 0.5 * (1.0 + cos(pi * (e - elow) / m.decut));
+        dfcut = -0.5 * sin(pi * (e - elow) / m.decut) * pi / m.decut;
+      }
+      edf_out[atom] = dfcut * energyi + 1.0;
+      for (int d = 0; d < ND; ++d) {
+        dE[d] = fcut * dE[d];
+        s_dE[d] = dE[d];
+        dedrho_out[static_cast<size_t>(atom) * 2 + d] = dE[d];
+      }
+      energy[atom] = fcut * energyi + e;
+    }
+    __syncthreads();
+    C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    for (int s = threadIdx.x; s < m.nslot; s += blockDim.x) {
+      const int w = m.slot_weight[s];
+      if (w < 0) continue;
+      C<double> v = {0.0, 0.0};
+      for (int d = 0; d < ND; ++d) {
+        v.x += s_dE[d] * tot[s * ND + d].x;
+        v.y += s_dE[d] * tot[s * ND + d].y;
+      }
+      const double mu = m.slot_mult[s];
+      Wa[w] = {R(mu * v.x), R(mu * v.y)};
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// k_forces
+// Shared memory: Ws[nW] (complex R), then per-thread feature columns (SoA,
+// [feature][blockDim]) so that every thread's scratch is bank-conflict free.
+template <class R>
+__global__ void __launch_bounds__(kForceThreads)
+    k_forces(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
+             const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
+             const double* __restrict__ magi, const double* __restrict__ mhi, const C<R>* __restrict__ W,
+             const double* __restrict__ edf_in, const double* __restrict__ dedrho, double* __restrict__ fij,
+             double* __restrict__ tij, double* __restrict__ ti0, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int T = blockDim.x;
+  C<R>* Ws = reinterpret_cast<C<R>*>(smem);
+  C<R>* cY = Ws + ((m.nW + 1) & ~1);           // Ya full [lsa][T], then dYa [lsa][3][T]
+  C<R>* cdY = cY + m.lsa * T;
+  C<R>* cYm = cdY + m.lsa * 3 * T;              // Ym half [h2][T], dYm [h2][3][T]
+  C<R>* cdYm = cYm + m.h2 * T;
+  R* cg = reinterpret_cast<R*>(cdYm + m.h2 * 3 * T);  // g [nba][T], g' [nba][T]
+  R* cgd = cg + m.nba * T;
+  R* cR = cgd + m.nba * T;                      // R, R' [n3a*(l3a+1)][T]
+  R* cRd = cR + m.n3a * (m.l3a + 1) * T;
+  R* cM = cRd + m.n3a * (m.l3a + 1) * T;        // M, M' [n2m*(l2m+1)][T]
+  R* cMd = cM + m.n2m * (m.l2m + 1) * T;
+  const int t = threadIdx.x;
+  const int nRl = m.n3a * (m.l3a + 1), nMl = m.n2m * (m.l2m + 1);
+
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    for (int s = t; s < m.nW; s += T) Ws[s] = Wa[s];
+    __syncthreads();
+    const double edf = edf_in[atom];
+    const int b0 = off[atom], b1 = off[atom + 1];
+    for (int j = b0 + t; j < b1; j += T) {
+      const double r = rr[j];
+      const double ex = ee[3 * j], ey = ee[3 * j + 1], ez = ee[3 * j + 2];
+      const double mg = magj[j];
+      const double mx = mhj[3 * j], my = mhj[3 * j + 1], mz = mhj[3 * j + 2];
+      // radial features with derivatives
+      R tmpv[32], tmpd[32];
+      double wl = 0.0, cd = 0.0;
+      const int nla = atomic_bin(m, r, wl, err);
+      if (nla > 0) {
+        lut_eval<R, true>(m.lut_a, m.nfa, 0, m.nba, nla, wl, m.rscale_a, tmpv, tmpd);
+        for (int n = 0; n < m.nba; ++n) {
+          cg[n * T + t] = tmpv[n];
+          cgd[n * T + t] = tmpd[n];
+        }
+        lut_eval<R, true>(m.lut_a, m.nfa, m.nba, nRl, nla, wl, m.rscale_a, tmpv, tmpd);
+        for (int q = 0; q < nRl; ++q) {
+          cR[q * T + t] = tmpv[q];
+          cRd[q * T + t] = tmpd[q];
+        }
+        R cv[1], cdv[1];
+        lut_eval<R, true>(m.lut_a, m.nfa, m.nba + nRl, 1, nla, wl, m.rscale_a, cv, cdv);
+        cd = static_cast<double>(cdv[0]);
+      } else {
+        for (int n = 0; n < m.nba; ++n) cg[n * T + t] = cgd[n * T + t] = R(0);
+        for (int q = 0; q < nRl; ++q) cR[q * T + t] = cRd[q * T + t] = R(0);
+      }
+      double wm = 0.0;
+      const int nlm = magnetic_bin(m, mg, wm, err);
+      if (nlm > 0) {
+        lut_eval<R, true>(m.lut_m, m.nfm, 0, nMl, nlm, wm, m.rscale_m, tmpv, tmpd);
+        for (int q = 0; q < nMl; ++q) {
+          cM[q * T + t] = tmpv[q];
+          cMd[q * T + t] = tmpd[q];
+        }
+      } else {
+        for (int q = 0; q < nMl; ++q) {
+          cM[q * T + t] = R(nlm == 0 ? 1 : 0);
+          cMd[q * T + t] = R(0);
+        }
+      }
+      {
+        C<R> Yh[kMaxHalf], dYh[kMaxHalf][3];
+        ylm_half<R, true>(m.l3a, R(ex), R(ey), R(ez), Yh, dYh);
+        for (int l = 0; l <= m.l3a; ++l)
+          for (int mm = -l; mm <= l; ++mm) {
+            const int lm = l * l + l + mm;
+            cY[lm * T + t] = y_full(Yh, l, mm);
+            for (int c = 0; c < 3; ++c) {
+              C<R> d = dYh[ph(l, mm < 0 ? -mm : mm)][c];
+              if (mm < 0) {
+                const R s = R(parity(mm));
+                d = {d.x * s, -d.y * s};
+              }
+              cdY[(lm * 3 + c) * T + t] = d;
+            }
+          }
+        ylm_half<R, true>(m.l2m, R(mx), R(my), R(mz), Yh, dYh);
+        for (int h = 0; h < m.h2; ++h) {
+          cYm[h * T + t] = Yh[h];
+          for (int c = 0; c < 3; ++c) cdYm[(h * 3 + c) * T + t] = dYh[h][c];
+        }
+      }
+      // ---- force: dE_i / d(x_i - x_j)
+      double fr = edf * cd;  // radial (along e) part
+      double ft[3] = {0.0, 0.0, 0.0};
+      const double invr = 1.0 / r;
+      // pair part: sum_n g'_n sum_{nr,h} Re(W2[n][nr][h] Q[nr][h])
+      for (int nr = 0; nr < m.n2m; ++nr)
+        for (int l = 0; l <= m.l2m; ++l) {
+          const R Ml = cM[(nr * (m.l2m + 1) + l) * T + t];
+          for (int mm = 0; mm <= l; ++mm) {
+            const int h = ph(l, mm);
+            const C<R> q = cscale(cYm[h * T + t], Ml);
+            R s = R(0);
+            for (int n = 0; n < m.nba; ++n) s += cgd[n * T + t] * re_mul(Ws[m.offW2 + (n * m.n2m + nr) * m.h2 + h], q);
+            fr += static_cast<double>(s);
+          }
+        }
+      // many-body part via U[n1][lma] = sum_{n2,h} WA Q
+      for (int n1 = 0; n1 < m.n3a; ++n1)
+        for (int l1 = 0; l1 <= m.l3a; ++l1)
+          for (int m1 = -l1; m1 <= l1; ++m1) {
+            const int lma = l1 * l1 + l1 + m1;
+            const C<R>* wrow = Ws + (n1 * m.lsa + lma) * m.n3m * m.h3;
+            C<R> U = {R(0), R(0)};
+            for (int n2 = 0; n2 < m.n3m; ++n2)
+              for (int l2 = 0; l2 <= m.l3m; ++l2) {
+                const R Ml = cM[(n2 * (m.l2m + 1) + l2) * T + t];
+                for (int m2 = 0; m2 <= l2; ++m2) {
+                  const int h = ph(l2, m2);
+                  const C<R> q = cscale(cYm[h * T + t], Ml);
+                  const C<R> w = wrow[n2 * m.h3 + h];
+                  U.x += w.x * q.x - w.y * q.y;
+                  U.y += w.x * q.y + w.y * q.x;
+                }
+              }
+            const R Rv = cR[(n1 * (m.l3a + 1) + l1) * T + t];
+            const R Rd = cRd[(n1 * (m.l3a + 1) + l1) * T + t];
+            fr += static_cast<double>(Rd * re_mul(U, cY[lma * T + t]));
+            const R sc = R(invr) * Rv;
+            for (int c = 0; c < 3; ++c) ft[c] += static_cast<double>(sc * re_mul(U, cdY[(lma * 3 + c) * T + t]));
+          }
+      fij[3 * static_cast<size_t>(j) + 0] = fr * ex + ft[0];
+      fij[3 * static_cast<size_t>(j) + 1] = fr * ey + ft[1];
+      fij[3 * static_cast<size_t>(j) + 2] = fr * ez + ft[2];
+      // ---- magnetic force: dE_i / dm_j
+      double tr = 0.0, tt[3] = {0.0, 0.0, 0.0};
+      const double invm = 1.0 / mg;
+      for (int nr = 0; nr < m.n2m; ++nr)
+        for (int l = 0; l <= m.l2m; ++l)
+          for (int mm = 0; mm <= l; ++mm) {
+            const int h = ph(l, mm);
+            C<R> V = {R(0), R(0)};
+            for (int n = 0; n < m.nba; ++n) {
+              const C<R> w = Ws[m.offW2 + (n * m.n2m + nr) * m.h2 + h];
+              const R gv = cg[n * T + t];
+              V.x += gv * w.x;
+              V.y += gv * w.y;
+            }
+            if (nr < m.n3m && l <= m.l3m) {
+              for (int n1 = 0; n1 < m.n3a; ++n1)
+                for (int l1 = 0; l1 <= m.l3a; ++l1) {
+                  const R Rv = cR[(n1 * (m.l3a + 1) + l1) * T + t];
+                  for (int m1 = -l1; m1 <= l1; ++m1) {
+                    const int lma = l1 * l1 + l1 + m1;
+                    const C<R> ry = cscale(cY[lma * T + t], Rv);
+                    const C<R> w = Ws[((n1 * m.lsa + lma) * m.n3m + nr) * m.h3 + h];
+                    V.x += w.x * ry.x - w.y * ry.y;
+                    V.y += w.x * ry.y + w.y * ry.x;
+                  }
+                }
+            }
+            const int q = nr * (m.l2m + 1) + l;
+            tr += static_cast<double>(cMd[q * T + t] * re_mul(V, cYm[h * T + t]));
+            const R sc = R(invm) * cM[q * T + t];
+            for (int c = 0; c < 3; ++c) tt[c] += static_cast<double>(sc * re_mul(V, cdYm[(h * 3 + c) * T + t]));
+          }
+      tij[3 * static_cast<size_t>(j) + 0] = tr * mx + tt[0];
+      tij[3 * static_cast<size_t>(j) + 1] = tr * my + tt[1];
+      tij[3 * static_cast<size_t>(j) + 2] = tr * mz + tt[2];
+    }
+    if (t == 0) {
+      // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749)
+      const double mg = magi[atom];
+      const double mx = mhi[3 * atom], my = mhi[3 * atom + 1], mz = mhi[3 * atom + 2];
+      double wm = 0.0;
+      const int nl = magnetic_bin(m, mg, wm, err);
+      R Mv[32], Md[32], gm[32], gmd[32];
+      if (nl > 0) {
+        lut_eval<R, true>(m.lut_m, m.nfm, 0, nMl, nl, wm, m.rscale_m, Mv, Md);
+        lut_eval<R, true>(m.lut_m, m.nfm, nMl, m.nbm, nl, wm, m.rscale_m, gm, gmd);
+      } else {
+        for (int q = 0; q < nMl; ++q) {
+          Mv[q] = R(nl == 0 ? 1 : 0);
+          Md[q] = R(0);
+        }
+        for (int q = 0; q < m.nbm; ++q) gmd[q] = R(0);
+      }
+      C<R> Yh[kMaxHalf], dYh[kMaxHalf][3];
+      ylm_half<R, true>(m.l2m, R(mx), R(my), R(mz), Yh, dYh);
+      double tr = 0.0, tt[3] = {0.0, 0.0, 0.0};
+      for (int n = 0; n < m.nbm; ++n) {
+        double wf1 = 0.0;
+        for (int d = 0; d < m.nd; ++d) wf1 += dedrho[static_cast<size_t>(atom) * 2 + d] * m.c1[d * m.nbm + n];
+        tr += wf1 * static_cast<double>(gmd[n]);
+      }
+      const double invm = 1.0 / mg;
+      for (int nr = 0; nr < m.n2m; ++nr)
+        for (int l = 0; l <= m.l2m; ++l)
+          for (int mm = 0; mm <= l; ++mm) {
+            const int h = ph(l, mm);
+            const C<R> w = Ws[m.offW0 + nr * m.h2 + h];
+            const int q = nr * (m.l2m + 1) + l;
+            tr += static_cast<double>(Md[q] * re_mul(w, Yh[h]));
+            const R sc = R(invm) * Mv[q];
+            for (int c = 0; c < 3; ++c) tt[c] += static_cast<double>(sc * re_mul(w, dYh[h][c]));
+          }
+      ti0[3 * static_cast<size_t>(atom) + 0] = tr * mx + tt[0];
+      ti0[3 * static_cast<size_t>(atom) + 1] = tr * my + tt[1];
+      ti0[3 * static_cast<size_t>(atom) + 2] = tr * mz + tt[2];
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// host-side launch helpers
+
+void upload_ylm_constants(const double* alm, const double* blm, const double* cl, const double* dl) {
+  cudaMemcpyToSymbol(c_alm, alm, sizeof(double) * kMaxHalf);
+  cudaMemcpyToSymbol(c_blm, blm, sizeof(double) * kMaxHalf);
+  cudaMemcpyToSymbol(c_cl, cl, sizeof(double) * (kMaxL + 1));
+  cudaMemcpyToSymbol(c_dl, dl, sizeof(double) * (kMaxL + 1));
+}
+
+template <class R>
+size_t abasis_smem(const DeviceModel& m) {
+  const int TB = kAbasisTile;
+  const size_t nacc = static_cast<size_t>(m.nWA) + static_cast<size_t>(m.nba) * m.n2m * m.h2;
+  return sizeof(C<R>) * (nacc + static_cast<size_t>(m.n3a) * m.lsa * TB + static_cast<size_t>(m.n2m) * m.h2 * TB) +
+         sizeof(R) * static_cast<size_t>(m.nba) * TB + sizeof(double) * TB + 64;
+}
+
+template <class R>
+size_t density_smem(const DeviceModel& m) {
+  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((m.nseg * m.nd + 1) & ~1)) +
+         sizeof(C<double>) * static_cast<size_t>(m.nslot) * m.nd + 64;
+}
+
+template <class R>
+size_t forces_smem(const DeviceModel& m, int T) {
+  const size_t nc = static_cast<size_t>((m.nW + 1) & ~1) + static_cast<size_t>(T) * (m.lsa * 4 + m.h2 * 4);
+  const size_t nr = static_cast<size_t>(T) * (2 * m.nba + 2 * m.n3a * (m.l3a + 1) + 2 * m.n2m * (m.l2m + 1));
+  return sizeof(C<R>) * nc + sizeof(R) * nr + 64;
+}
+
+template <class R>
+int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap) {
+  const int natom = b.natom;
+  if (natom <= 0) return 0;
+  const int grid = natom < grid_cap ? natom : grid_cap;
+  const size_t s1 = abasis_smem<R>(m), s2 = density_smem<R>(m), s3 = forces_smem<R>(m, kForceThreads);
+  cudaFuncSetAttribute(k_abasis<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1));
+  k_abasis<R><<<grid, kAbasisThreads, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                 reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+  if (m.nd == 1) {
+    cudaFuncSetAttribute(k_density<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
+    k_density<R, 1><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
+                                                       reinterpret_cast<C<R>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
+  } else {
+    cudaFuncSetAttribute(k_density<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
+    k_density<R, 2><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
+                                                       reinterpret_cast<C<R>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
+  }
+  cudaFuncSetAttribute(k_forces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s3));
+  k_forces<R><<<grid, kForceThreads, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
+                                                b.ti0, b.err);
+  return 3;
+}
+
+size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
+  if (precision == 0) {
+    if (which == 0) return abasis_smem<double>(m);
+    if (which == 1) return density_smem<double>(m);
+    return forces_smem<double>(m, kForceThreads);
+  }
+  if (which == 0) return abasis_smem<float>(m);
+  if (which == 1) return density_smem<float>(m);
+  return forces_smem<float>(m, kForceThreads);
+}
+
+int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap) {
+  return launch_eval<double>(m, b, st, grid_cap);
+}
+
+}  // namespace magace
+
+namespace magace {
+int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap) {
+  return launch_eval<float>(m, b, st, grid_cap);
+}
+}  // namespace magace

@@ -1,0 +1,645 @@
+// Host-side model construction: basis enumeration, couplings, folded gather
+// tables and radial lookup tables.
+#include "model.hpp"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <map>
+
+#include "magace.h"
+
+namespace magace {
+namespace {
+
+const double kPi = 3.14159265358979323846264338327950288419;
+
+// ---------------------------------------------------------------------------
+// Clebsch-Gordan coefficients. Racah's closed formula with double-precision
+// factorials, the same evaluation the reference uses (src/util.F90:4149-4252)
+// so that coefficient values agree to the last bits.
+struct Factorials {
+  std::vector<double> f;
+  Factorials() {
+    f.resize(64);
+    f[0] = 1.0;
+    for (size_t i = 1; i < f.size(); ++i) f[i] = static_cast<double>(i) * f[i - 1];
+  }
+};
+const Factorials kFac;
+
+}  // namespace
+
+double clebsch_gordan(int j1, int j2, int J, int m1, int m2, int M) {
+  if (M != m1 + m2) return 0.0;
+  if (std::abs(m1) > j1 || std::abs(m2) > j2 || std::abs(M) > J) return 0.0;
+  if (J > j1 + j2 || J < std::abs(j1 - j2)) return 0.0;
+  const auto& f = kFac.f;
+  double pre = (static_cast<double>(2 * J + 1) * f[j1 + j2 - J] * f[j1 - j2 + J] * f[-j1 + j2 + J] /
+                f[j1 + j2 + J + 1]) *
+               (f[J + M] * f[J - M] * f[j1 + m1] * f[j1 - m1] * f[j2 + m2] * f[j2 - m2]);
+  pre = std::sqrt(pre);
+  double sum = 0.0;
+  for (int k = 0; k <= j1 + j2 + J; ++k) {
+    int a = j1 + j2 - J - k, b = j1 - m1 - k, c = j2 + m2 - k, d = J - j2 + m1 + k, e = J - j1 - m2 + k;
+    if (a < 0 || b < 0 || c < 0 || d < 0 || e < 0) continue;
+    sum += static_cast<double>(k % 2 ? -1 : 1) / (f[k] * f[a] * f[b] * f[c] * f[d] * f[e]);
+  }
+  return pre * sum;
+}
+
+int FactorLayout::A(int n1, int l1, int m1, int n2, int l2, int m2) const {
+  // A entries beyond (n3m, l3m) are never accumulated by the A pass and stay
+  // zero in the reference (src/a_basis.F90:248-291 loops only to
+  // nradial3_magnetic / l3max_magnetic)
+  if (n1 >= n3a || l1 > l3a || n2 >= n3m || l2 > l3m) return offZero;
+  return offA + ((n1 * lsa + l1 * l1 + l1 + m1) * n3m + n2) * ls3 + l2 * l2 + l2 + m2;
+}
+
+int FactorLayout::WA(int n1, int l1, int m1, int n2, int l2, int m2) const {
+  if (m2 < 0 || n1 >= n3a || l1 > l3a || n2 >= n3m || l2 > l3m) return -1;
+  return ((n1 * lsa + l1 * l1 + l1 + m1) * n3m + n2) * h3 + l2 * (l2 + 1) / 2 + m2;
+}
+
+namespace {
+
+bool triangle_even(int a, int b, int c) {
+  return a + b >= c && std::abs(a - b) <= c && (a + b + c) % 2 == 0;
+}
+
+// ---------------------------------------------------------------------------
+// Radial basis functions g_n(r) on [0, cutoff) and their r-derivatives
+// (src/radial.F90:430-606): Chebyshev polynomials of a scaled variable, with
+// optional cosine envelope, and a cosine taper over the last dcut.
+void chebyshev(int n, double x, std::vector<double>& T, std::vector<double>& dT) {
+  // T_k(x) and dT_k/dx = k U_{k-1}(x)
+  std::vector<double> U(n + 1);
+  T.assign(n + 1, 0.0);
+  dT.assign(n + 1, 0.0);
+  T[0] = 1.0;
+  U[0] = 1.0;
+  if (n == 0) return;
+  T[1] = x;
+  U[1] = 2.0 * x;
+  for (int k = 1; k < n; ++k) {
+    T[k + 1] = 2.0 * x * T[k] - T[k - 1];
+    U[k + 1] = 2.0 * x * U[k] - U[k - 1];
+  }
+  for (int k = 1; k <= n; ++k) dT[k] = static_cast<double>(k) * U[k - 1];
+}
+
+bool radial_basis(int type, double lam, int nb, double rc, double dc, double r, std::vector<double>& g,
+                  std::vector<double>& dg) {
+  g.assign(nb, 0.0);
+  dg.assign(nb, 0.0);
+  if (r >= rc) return true;
+  std::vector<double> T, dT;
+  const double x0 = r / rc;
+  switch (type) {
+    case 3:
+    case 4: {  // exponentially scaled Chebyshev, with (3) / without (4) envelope
+      double y1 = std::exp(-lam * x0), dy1 = -lam * y1 / rc, y2 = std::exp(-lam);
+      double x = 1.0 - 2.0 * (y1 - y2) / (1.0 - y2), dx = -2.0 * dy1 / (1.0 - y2);
+      chebyshev(nb - 1, x, T, dT);
+      g[0] = T[0];
+      dg[0] = dT[0] * dx;
+      for (int n = 1; n < nb; ++n) {
+        g[n] = 0.5 - 0.5 * T[n];
+        dg[n] = -0.5 * dT[n] * dx;
+      }
+      if (type == 3) {
+        double env = 0.5 * (1.0 + std::cos(kPi * x0)), denv = -0.5 * std::sin(kPi * x0) * kPi / rc;
+        for (int n = 0; n < nb; ++n) {
+          dg[n] = g[n] * denv + dg[n] * env;
+          g[n] = g[n] * env;
+        }
+      }
+      break;
+    }
+    case 5:
+    case 6: {  // power-law scaled Chebyshev, without (5) / with (6) envelope
+      double y0 = 1.0 - x0, dy1 = std::pow(y0, lam - 1.0);
+      double y1 = 1.0 - dy1 * y0;
+      dy1 = lam / rc * dy1;
+      double x = 2.0 * y1 - 1.0, dx = 2.0 * dy1;
+      if (type == 5) {
+        chebyshev(nb, x, T, dT);
+        for (int n = 0; n < nb; ++n) {
+          g[n] = 0.5 - 0.5 * T[n + 1];
+          dg[n] = -0.5 * dT[n + 1] * dx;
+        }
+      } else {
+        chebyshev(nb - 1, x, T, dT);
+        g[0] = T[0];
+        dg[0] = dT[0] * dx;
+        for (int n = 1; n < nb; ++n) {
+          g[n] = 0.5 - 0.5 * T[n];
+          dg[n] = -0.5 * dT[n] * dx;
+        }
+        double env = 0.5 * (1.0 + std::cos(kPi * x0)), denv = -0.5 * std::sin(kPi * x0) * kPi / rc;
+        for (int n = 0; n < nb; ++n) {
+          dg[n] = g[n] * denv + dg[n] * env;
+          g[n] = g[n] * env;
+        }
+      }
+      break;
+    }
+    case 7: {  // Chebyshev in 1 - 2 x^2
+      double x = 1.0 - 2.0 * x0 * x0, dx = -(4.0 / rc) * x0;
+      chebyshev(nb, x, T, dT);
+      for (int n = 0; n < nb; ++n) {
+        g[n] = T[n + 1];
+        dg[n] = dT[n + 1] * dx;
+      }
+      break;
+    }
+    case 8: {  // Chebyshev in 1 - 2 x, shifted to vanish at r = 0
+      double x = 1.0 - 2.0 * x0, dx = -2.0 / rc;
+      chebyshev(nb, x, T, dT);
+      for (int n = 0; n < nb; ++n) {
+        g[n] = T[n + 1] - 1.0;
+        dg[n] = dT[n + 1] * dx;
+      }
+      break;
+    }
+    default:
+      return false;
+  }
+  double rt = rc - dc;
+  if (r > rt) {
+    double fc = 0.5 * (1.0 + std::cos(kPi * (r - rt) / dc));
+    double dfc = -0.5 * std::sin(kPi * (r - rt) / dc) * kPi / dc;
+    for (int n = 0; n < nb; ++n) {
+      dg[n] = g[n] * dfc + dg[n] * fc;
+      g[n] = g[n] * fc;
+    }
+  }
+  return true;
+}
+
+// Hard-core repulsion pre*exp(-lambda r^2)/r with a cosine envelope
+// (src/radial.F90:630-668).
+void core_repulsion(double r, double pre, double lam, double rc, double& c, double& dc) {
+  c = dc = 0.0;
+  if (r >= rc) return;
+  pre = std::fabs(pre);
+  lam = std::fabs(lam);
+  double r2 = r * r, lr2 = lam * r2;
+  if (lr2 >= 50.0) return;
+  double y = std::exp(-lr2);
+  c = pre * y / r;
+  dc = -pre * y * (2.0 * lr2 + 1.0) / r2;
+  double x0 = r / rc, env = 0.5 * (1.0 + std::cos(kPi * x0)), denv = -0.5 * std::sin(kPi * x0) * kPi / rc;
+  dc = c * denv + dc * env;
+  c = c * env;
+}
+
+// Tabulates `nf` functions on the grid r_n = n / rscale (n = 1..nlut) as
+// cubic-Hermite segments over [r_n, r_{n+1}], in bin units: segment n holds
+// (f(r_n), f'(r_n) h, c2, c3) with the right end taken from segment n+1 and
+// zero beyond the last node. This is the construction of
+// src/radial.F90:223-296, swept downwards so each segment sees its right
+// neighbour already evaluated.
+template <class Eval>
+void tabulate(int nlut, double rscale, int nf, std::vector<double>& out, Eval eval) {
+  out.assign(static_cast<size_t>(nlut + 1) * nf * 4, 0.0);
+  const double h = 1.0 / rscale;
+  std::vector<double> v(nf), dv(nf), right(nf, 0.0), dright(nf, 0.0);
+  for (int n = nlut; n >= 1; --n) {
+    double x = h * static_cast<double>(n);
+    eval(x, v, dv);
+    for (int f = 0; f < nf; ++f) {
+      double f0 = v[f], f0d = dv[f] * h, f1 = right[f], f1d = dright[f];
+      double* c = &out[(static_cast<size_t>(n) * nf + f) * 4];
+      c[0] = f0;
+      c[1] = f0d;
+      c[2] = 3.0 * (f1 - f0) - f1d - 2.0 * f0d;
+      c[3] = -2.0 * (f1 - f0) + f1d + f0d;
+      right[f] = c[0];
+      dright[f] = c[1];
+    }
+  }
+}
+
+bool build_lut(const Model& mdl, RadialLUT& lut) {
+  const Potential& p = mdl.pot;
+  const BasisDims& d = p.dims;
+  const FactorLayout& L = mdl.L;
+  lut.nlut = 10000;  // bins per table (src/radial.F90:43)
+  lut.rscale_a = static_cast<double>(lut.nlut) / mdl.cutoff;
+  lut.rscale_m = static_cast<double>(lut.nlut) / mdl.cutoff_m;
+  // the reference steps the grid as (1/rscale)*n; use the same spacing
+  lut.rscale_a = 1.0 / (1.0 / lut.rscale_a) == lut.rscale_a ? lut.rscale_a : lut.rscale_a;
+  const int la = d.l3max_a + 1, lm = d.l2max_m + 1;
+  lut.nfa = d.nradbase_a + d.nradial3_a * la + 1;
+  lut.nfm = d.nradial2_m * lm + d.nradbase_m;
+  bool ok = true;
+  std::vector<double> g, dg;
+  tabulate(lut.nlut, lut.rscale_a, lut.nfa, lut.a, [&](double r, std::vector<double>& v, std::vector<double>& dv) {
+    if (!radial_basis(d.radtype_a, p.lambda[0], d.nradbase_a, p.cut[0], p.dcut[0], r, g, dg)) ok = false;
+    int k = 0;
+    for (int n = 0; n < d.nradbase_a; ++n, ++k) {
+      v[k] = g[n];
+      dv[k] = dg[n];
+    }
+    for (int nr = 0; nr < d.nradial3_a; ++nr)
+      for (int l = 0; l < la; ++l, ++k) {
+        double s = 0.0, ds = 0.0;
+        const double* c = &p.crad_a[(static_cast<size_t>(l) * d.nradial3_a + nr) * d.nradbase_a];
+        for (int n = 0; n < d.nradbase_a; ++n) {
+          s += c[n] * g[n];
+          ds += c[n] * dg[n];
+        }
+        v[k] = s;
+        dv[k] = ds;
+      }
+    core_repulsion(r, p.core_pre, p.core_lambda, p.cut[0], v[k], dv[k]);
+  });
+  tabulate(lut.nlut, lut.rscale_m, lut.nfm, lut.m, [&](double r, std::vector<double>& v, std::vector<double>& dv) {
+    if (!radial_basis(d.radtype_m, p.lambda[1], d.nradbase_m, p.cut[1], p.dcut[1], r, g, dg)) ok = false;
+    int k = 0;
+    for (int nr = 0; nr < d.nradial2_m; ++nr)
+      for (int l = 0; l < lm; ++l, ++k) {
+        double s = 0.0, ds = 0.0;
+        const double* c = &p.crad_m[(static_cast<size_t>(l) * d.nradial2_m + nr) * d.nradbase_m];
+        for (int n = 0; n < d.nradbase_m; ++n) {
+          s += c[n] * g[n];
+          ds += c[n] * dg[n];
+        }
+        v[k] = s;
+        dv[k] = ds;
+      }
+    for (int n = 0; n < d.nradbase_m; ++n, ++k) {
+      v[k] = g[n];
+      dv[k] = dg[n];
+    }
+  });
+  (void)L;
+  return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Basis enumeration, single element (the reference's C-ABI admits one,
+// src/ace.F90:46-49). Selection rules of setuptables/bcreate
+// (src/util.F90:1803-2582, :4673-4857): pair radial indices ordered n0' >= n1';
+// 3-body pairs (n1,l1,n1',l1') >= (n2,l1,n2',l2') in the packed key order and
+// (l0',l1',l2') a triangle with even sum; 4-body triples ordered the same way,
+// (l1,l2,l3) an even triangle, and for the magnetic quadruple every
+// intermediate L01' coupling (l0' l1')L (l2' l3')L allowed, odd L excluded
+// when a pair is identical, even total.
+void enumerate(const BasisDims& d, std::vector<std::vector<int>>* rows) {
+  for (int n = 1; n <= d.nradbase_m; ++n) rows[1].push_back({n});
+  for (int a = 1; a <= d.nradial2_m; ++a)
+    for (int b = 1; b <= d.nradial2_m; ++b)
+      for (int n = 1; n <= d.nradbase_a; ++n)
+        for (int l = 0; l <= d.l2max_m; ++l)
+          if (a >= b) rows[2].push_back({a, b, n, l});
+  {
+    const int na = d.nradial3_a, nm = d.nradial3_m;
+    const long kmm = static_cast<long>(nm) * (d.l3max_m + 1) + 1;
+    auto key = [&](int n, int l, int np, int lp) { return kmm * (na * l + n) + nm * lp + np; };
+    for (int n1 = 1; n1 <= na; ++n1)
+      for (int n2 = 1; n2 <= na; ++n2)
+        for (int p0 = 1; p0 <= nm; ++p0)
+          for (int p1 = 1; p1 <= nm; ++p1)
+            for (int p2 = 1; p2 <= nm; ++p2)
+              for (int l1 = 0; l1 <= d.l3max_a; ++l1)
+                for (int q0 = 0; q0 <= d.l3max_m; ++q0)
+                  for (int q1 = 0; q1 <= d.l3max_m; ++q1)
+                    for (int q2 = 0; q2 <= d.l3max_m; ++q2)
+                      if (key(n1, l1, p1, q1) >= key(n2, l1, p2, q2) && triangle_even(q0, q1, q2))
+                        rows[3].push_back({n1, n2, p0, p1, p2, l1, q0, q1, q2});
+  }
+  {
+    const int na = d.nradial4_a, nm = d.nradial4_m;
+    const long kmm = static_cast<long>(nm) * (d.l4max_m + 1) + 1;
+    auto key = [&](int n, int l, int np, int lp) { return kmm * (na * l + n) + nm * lp + np; };
+    for (int n1 = 1; n1 <= na; ++n1)
+      for (int n2 = 1; n2 <= na; ++n2)
+        for (int n3 = 1; n3 <= na; ++n3)
+          for (int p0 = 1; p0 <= nm; ++p0)
+            for (int p1 = 1; p1 <= nm; ++p1)
+              for (int p2 = 1; p2 <= nm; ++p2)
+                for (int p3 = 1; p3 <= nm; ++p3)
+                  for (int l1 = 0; l1 <= d.l4max_a; ++l1)
+                    for (int l2 = 0; l2 <= d.l4max_a; ++l2)
+                      for (int l3 = 0; l3 <= d.l4max_a; ++l3)
+                        for (int q0 = 0; q0 <= d.l4max_m; ++q0)
+                          for (int q1 = 0; q1 <= d.l4max_m; ++q1)
+                            for (int q2 = 0; q2 <= d.l4max_m; ++q2)
+                              for (int q3 = 0; q3 <= d.l4max_m; ++q3) {
+                                long k1 = key(n1, l1, p1, q1), k2 = key(n2, l2, p2, q2), k3 = key(n3, l3, p3, q3);
+                                if (!(k1 >= k2 && k2 >= k3)) continue;
+                                if (!triangle_even(l1, l2, l3)) continue;
+                                if ((q0 + q1 + q2 + q3) % 2) continue;
+                                const bool same01 = (p0 == p1 && q0 == q1), same23 = (p2 == p3 && q2 == q3);
+                                const int lmaxq = std::max(std::max(q0, q1), std::max(q2, q3));
+                                for (int L = 0; L <= 2 * lmaxq; ++L) {
+                                  if (L > q0 + q1 || L > q2 + q3) continue;
+                                  if (L < std::abs(q0 - q1) || L < std::abs(q2 - q3)) continue;
+                                  if ((same01 || same23) && L % 2) continue;
+                                  rows[4].push_back({n1, n2, n3, p0, p1, p2, p3, l1, l2, l3, q0, q1, q2, q3, L});
+                                }
+                              }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Gather-table construction. Every product term kappa * A0 * X1 * ... of the
+// density becomes one entry of the A0 slot it contains (all m), and one entry
+// of each weight slot (m' >= 0) of its other factors.
+struct TermSink {
+  const FactorLayout& L;
+  int nd;
+  std::vector<std::vector<Entry>> by_slot[4];  // [arity] -> slot -> entries
+  int nslot;
+  explicit TermSink(const FactorLayout& l, int ndens) : L(l), nd(ndens) {
+    nslot = l.n2m * l.ls2 + l.nWA + (l.offW0 - l.offW2);
+    for (int a = 1; a <= 3; ++a) by_slot[a].resize(nslot);
+  }
+  int g0_slot(int a0_factor) const { return a0_factor - L.offA0; }
+  int w_slot(int weight_index) const { return L.n2m * L.ls2 + weight_index; }  // WA and W2 only
+
+  void add(int slot, const double* k, const int* others, int arity) {
+    Entry e;
+    e.kappa[0] = k[0];
+    e.kappa[1] = nd > 1 ? k[1] : 0.0;
+    for (int q = 0; q < 3; ++q) e.o[q] = static_cast<uint16_t>(q < arity ? others[q] : L.offOne);
+    by_slot[arity][slot].push_back(e);
+  }
+};
+
+int build_gather(Model& M, std::string& msg) {
+  const FactorLayout& L = M.L;
+  const BasisDims& d = M.pot.dims;
+  const int nd = M.ndensity;
+  TermSink sink(L, nd);
+  long nterm[5] = {0, 0, 0, 0, 0};
+
+  // 2-body: kappa A0(n0',l,m) A2(n1,n1',l,-m), cg <l m l -m|0 0> (src/b_basis.F90:91-129)
+  for (size_t c = 0; c < M.rows[2].size(); ++c) {
+    const auto& r = M.rows[2][c];
+    const int n0 = r[0] - 1, n1p = r[1] - 1, n1 = r[2] - 1, l = r[3];
+    for (int m = -l; m <= l; ++m) {
+      double cf = clebsch_gordan(l, l, 0, m, -m, 0);
+      double k[2] = {M.coef[2][c][0] * cf, M.coef[2][c][1] * cf};
+      if (k[0] == 0.0 && k[1] == 0.0) continue;
+      ++nterm[2];
+      int a0 = L.A0(n0, l, m), a2 = L.A2(n1, n1p, l, -m);
+      sink.add(sink.g0_slot(a0), k, &a2, 1);
+      if (-m >= 0) sink.add(sink.w_slot(L.W2(n1, n1p, l, -m) - L.offW2 + L.nWA), k, &a0, 1);
+    }
+  }
+  // 3-body: kappa A0(n0',l0',m0') A(n1,l1,m1,n1',l1',m1') A(n2,l1,-m1,n2',l2',m2')
+  // with cg<l1 m1 l1 -m1|00> * cg<l0' m0' l1' m1'|l2' -m2'> cg<l2' m2' l2' -m2'|00>
+  // (src/b_basis.F90:142-212, src/util.F90:4297-4333)
+  for (size_t c = 0; c < M.rows[3].size(); ++c) {
+    const auto& r = M.rows[3][c];
+    const int n1 = r[0] - 1, n2 = r[1] - 1, p0 = r[2] - 1, p1 = r[3] - 1, p2 = r[4] - 1;
+    const int l1 = r[5], q0 = r[6], q1 = r[7], q2 = r[8];
+    for (int m1 = -l1; m1 <= l1; ++m1) {
+      double cfa = clebsch_gordan(l1, l1, 0, m1, -m1, 0);
+      for (int u0 = -q0; u0 <= q0; ++u0)
+        for (int u1 = -q1; u1 <= q1; ++u1) {
+          int u2 = -(u0 + u1);
+          if (std::abs(u2) > q2) continue;
+          double cfm = clebsch_gordan(q0, q1, q2, u0, u1, -u2) * clebsch_gordan(q2, q2, 0, u2, -u2, 0);
+          double cf = cfa * cfm;
+          double k[2] = {M.coef[3][c][0] * cf, M.coef[3][c][1] * cf};
+          if (k[0] == 0.0 && k[1] == 0.0) continue;
+          ++nterm[3];
+          int f0 = L.A0(p0, q0, u0), f1 = L.A(n1, l1, m1, p1, q1, u1), f2 = L.A(n2, l1, -m1, p2, q2, u2);
+          int o12[2] = {f1, f2};
+          sink.add(sink.g0_slot(f0), k, o12, 2);
+          int w1 = L.WA(n1, l1, m1, p1, q1, u1), w2 = L.WA(n2, l1, -m1, p2, q2, u2);
+          int o02[2] = {f0, f2}, o01[2] = {f0, f1};
+          if (w1 >= 0) sink.add(sink.w_slot(w1), k, o02, 2);
+          if (w2 >= 0) sink.add(sink.w_slot(w2), k, o01, 2);
+        }
+    }
+  }
+  // 4-body: kappa A0 A(1) A(2) A(3) with
+  // cg<l1 m1 l2 m2|l3 -m3> cg<l3 m3 l3 -m3|00> *
+  // cg<l0' m0' l1' m1'|L M> cg<l2' m2' l3' m3'|L -M> cg<L M L -M|00>
+  // (src/b_basis.F90:225-307, src/util.F90:4344-4388)
+  for (size_t c = 0; c < M.rows[4].size(); ++c) {
+    const auto& r = M.rows[4][c];
+    const int n1 = r[0] - 1, n2 = r[1] - 1, n3 = r[2] - 1;
+    const int p0 = r[3] - 1, p1 = r[4] - 1, p2 = r[5] - 1, p3 = r[6] - 1;
+    const int l1 = r[7], l2 = r[8], l3 = r[9], q0 = r[10], q1 = r[11], q2 = r[12], q3 = r[13], Lc = r[14];
+    for (int m1 = -l1; m1 <= l1; ++m1)
+      for (int m2 = -l2; m2 <= l2; ++m2) {
+        int m3 = -(m1 + m2);
+        if (std::abs(m3) > l3) continue;
+        double cfa = clebsch_gordan(l1, l2, l3, m1, m2, -m3) * clebsch_gordan(l3, l3, 0, m3, -m3, 0);
+        for (int Mc = -Lc; Mc <= Lc; ++Mc)
+          for (int u0 = -q0; u0 <= q0; ++u0) {
+            int u1 = Mc - u0;
+            if (std::abs(u1) > q1) continue;
+            for (int u2 = -q2; u2 <= q2; ++u2) {
+              int u3 = -Mc - u2;
+              if (std::abs(u3) > q3) continue;
+              double cfm = clebsch_gordan(q0, q1, Lc, u0, u1, Mc) * clebsch_gordan(q2, q3, Lc, u2, u3, -Mc) *
+                           clebsch_gordan(Lc, Lc, 0, Mc, -Mc, 0);
+              double cf = cfa * cfm;
+              double k[2] = {M.coef[4][c][0] * cf, M.coef[4][c][1] * cf};
+              if (k[0] == 0.0 && k[1] == 0.0) continue;
+              ++nterm[4];
+              int f0 = L.A0(p0, q0, u0), f1 = L.A(n1, l1, m1, p1, q1, u1), f2 = L.A(n2, l2, m2, p2, q2, u2),
+                  f3 = L.A(n3, l3, m3, p3, q3, u3);
+              int o123[3] = {f1, f2, f3};
+              sink.add(sink.g0_slot(f0), k, o123, 3);
+              int w1 = L.WA(n1, l1, m1, p1, q1, u1), w2 = L.WA(n2, l2, m2, p2, q2, u2),
+                  w3 = L.WA(n3, l3, m3, p3, q3, u3);
+              int o023[3] = {f0, f2, f3}, o013[3] = {f0, f1, f3}, o012[3] = {f0, f1, f2};
+              if (w1 >= 0) sink.add(sink.w_slot(w1), k, o023, 3);
+              if (w2 >= 0) sink.add(sink.w_slot(w2), k, o013, 3);
+              if (w3 >= 0) sink.add(sink.w_slot(w3), k, o012, 3);
+            }
+          }
+      }
+  }
+  for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
+
+  // flatten into segments
+  GatherTable& g = M.gt;
+  g = GatherTable();
+  g.nG0 = L.n2m * L.ls2;
+  g.nslot = sink.nslot;
+  g.slot_seg_begin.assign(g.nslot + 1, 0);
+  for (int s = 0; s < g.nslot; ++s) {
+    g.slot_seg_begin[s] = static_cast<int32_t>(g.seg_slot.size());
+    for (int a = 1; a <= 3; ++a) {
+      const auto& es = sink.by_slot[a][s];
+      for (size_t e0 = 0; e0 < es.size(); e0 += GatherTable::kSegLen) {
+        size_t cnt = std::min(es.size() - e0, static_cast<size_t>(GatherTable::kSegLen));
+        std::vector<double>* kk = a == 1 ? g.k1 : (a == 2 ? g.k2 : g.k3);
+        std::vector<uint16_t>& oo = a == 1 ? g.o1 : (a == 2 ? g.o2 : g.o3);
+        g.seg_arity.push_back(a);
+        g.seg_first.push_back(static_cast<int32_t>(kk[0].size()));
+        g.seg_count.push_back(static_cast<int32_t>(cnt));
+        g.seg_slot.push_back(s);
+        for (size_t e = e0; e < e0 + cnt; ++e) {
+          kk[0].push_back(es[e].kappa[0]);
+          kk[1].push_back(es[e].kappa[1]);
+          for (int q = 0; q < a; ++q) oo.push_back(es[e].o[q]);
+        }
+      }
+    }
+  }
+  g.slot_seg_begin[g.nslot] = static_cast<int32_t>(g.seg_slot.size());
+  // process long, high-arity segments first so warps see similar work
+  const int nseg = static_cast<int>(g.seg_slot.size());
+  g.order.resize(nseg);
+  for (int s = 0; s < nseg; ++s) g.order[s] = s;
+  std::stable_sort(g.order.begin(), g.order.end(), [&](int a, int b) {
+    long wa = static_cast<long>(g.seg_count[a]) * (g.seg_arity[a] + 1);
+    long wb = static_cast<long>(g.seg_count[b]) * (g.seg_arity[b] + 1);
+    return wa > wb;
+  });
+  // slot -> weight mapping and multiplicity
+  g.slot_factor.assign(g.nslot, -1);
+  g.slot_weight.assign(g.nslot, -1);
+  g.slot_mult.assign(g.nslot, 0.0);
+  for (int nr = 0; nr < L.n2m; ++nr)
+    for (int l = 0; l <= L.l2m; ++l)
+      for (int m = -l; m <= l; ++m) {
+        int s = L.A0(nr, l, m) - L.offA0;
+        g.slot_factor[s] = L.A0(nr, l, m);
+        if (m >= 0) {
+          g.slot_weight[s] = L.W0(nr, l, m);
+          g.slot_mult[s] = m == 0 ? 1.0 : 2.0;
+        }
+      }
+  for (int n1 = 0; n1 < L.n3a; ++n1)
+    for (int l1 = 0; l1 <= L.l3a; ++l1)
+      for (int m1 = -l1; m1 <= l1; ++m1)
+        for (int n2 = 0; n2 < L.n3m; ++n2)
+          for (int l2 = 0; l2 <= L.l3m; ++l2)
+            for (int m2 = 0; m2 <= l2; ++m2) {
+              int w = L.WA(n1, l1, m1, n2, l2, m2);
+              int s = sink.w_slot(w);
+              g.slot_weight[s] = w;
+              // force/torque loop multiplicities (src/forces.F90:509-614)
+              g.slot_mult[s] = m2 > 0 ? 2.0 : (m1 > 0 ? 2.0 : (m1 == 0 ? 1.0 : 0.0));
+            }
+  for (int n = 0; n < L.nba; ++n)
+    for (int nr = 0; nr < L.n2m; ++nr)
+      for (int l = 0; l <= L.l2m; ++l)
+        for (int m = 0; m <= l; ++m) {
+          int w = L.W2(n, nr, l, m);
+          int s = sink.w_slot(w - L.offW2 + L.nWA);
+          g.slot_weight[s] = w;
+          g.slot_mult[s] = m == 0 ? 1.0 : 2.0;
+        }
+  (void)d;
+  (void)nd;
+  (void)msg;
+  return MAGACE_OK;
+}
+
+}  // namespace
+
+int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& M, std::string& msg) {
+  M = Model();
+  M.pot = pot;
+  M.cutoff = rcut;
+  M.cutoff_m = rcut_magnetic;
+  const BasisDims& d = pot.dims;
+  if (d.nradial5_a || d.nradial5_m || d.nradial6_a || d.nradial6_m) {
+    msg = "5- and 6-body clusters are not supported by this build";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+  // limits of src/util.F90:234-272
+  if (d.l3max_a < d.l4max_a || d.l2max_m < d.l3max_m || d.l2max_m < d.l4max_m ||
+      d.nradial3_a < d.nradial4_a || d.nradial2_m < d.nradial3_m || d.nradial2_m < d.nradial4_m ||
+      d.nradial3_a > d.nradbase_a || d.nradial2_m > d.nradbase_m ||
+      std::max(d.nradial3_a, d.nradial2_m) > std::max(d.nradbase_a, d.nradbase_m)) {
+    msg = "basis dimensions violate the limits of the reference setup";
+    return MAGACE_ERR_FORMAT;
+  }
+  if (d.nradial2_m == 0 || d.nradial3_a == 0 || d.nradial3_m == 0) {
+    msg = "potentials without 2- or 3-body magnetic terms are not supported";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+  if (d.nfemb < 0 || d.nfemb > 2) {
+    msg = "embedding types 3 and 4 have no gradient (src/forces.F90:1234-1258)";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+  for (int t : {d.radtype_a, d.radtype_m})
+    if (t < 3 || t > 8) {
+      msg = "radial basis types 0-2 are not working in the reference either";
+      return MAGACE_ERR_UNSUPPORTED;
+    }
+  if (pot.cut[0] > rcut || pot.cut[1] > rcut_magnetic) {
+    msg = "global cutoff shorter than the potential's cutoff";
+    return MAGACE_ERR_FORMAT;
+  }
+  M.ndensity = d.ndensity;
+  M.nfemb = d.nfemb;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) M.par[a][b] = pot.par[a][b];
+  M.ecut = pot.ecut;
+  M.decut = pot.decut;
+  M.core_pre = pot.core_pre;
+  M.core_lambda = pot.core_lambda;
+
+  FactorLayout& L = M.L;
+  L.n3a = d.nradial3_a;
+  L.n3m = d.nradial3_m;
+  L.l3a = d.l3max_a;
+  L.l3m = d.l3max_m;
+  L.nba = d.nradbase_a;
+  L.nbm = d.nradbase_m;
+  L.n2m = d.nradial2_m;
+  L.l2m = d.l2max_m;
+  L.lsa = (L.l3a + 1) * (L.l3a + 1);
+  L.ls3 = (L.l3m + 1) * (L.l3m + 1);
+  L.ls2 = (L.l2m + 1) * (L.l2m + 1);
+  L.h3 = (L.l3m + 1) * (L.l3m + 2) / 2;
+  L.h2 = (L.l2m + 1) * (L.l2m + 2) / 2;
+  L.offA = 0;
+  L.offA2 = L.n3a * L.lsa * L.n3m * L.ls3;
+  L.offA0 = L.offA2 + L.nba * L.n2m * L.ls2;
+  L.offOne = L.offA0 + L.n2m * L.ls2;
+  L.offZero = L.offOne + 1;
+  L.nF = L.offZero + 1;
+  L.nWA = L.n3a * L.lsa * L.n3m * L.h3;
+  L.offW2 = L.nWA;
+  L.offW0 = L.offW2 + L.nba * L.n2m * L.h2;
+  L.nW = L.offW0 + L.n2m * L.h2;
+  if (L.nF > 65535) {
+    msg = "basis too large for 16-bit factor indices";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+
+  enumerate(d, M.rows);
+  // match the file's cluster records (src/util.F90:678-956)
+  std::map<std::vector<int>, size_t> index[5];
+  for (int r = 1; r <= 4; ++r) {
+    M.coef[r].assign(M.rows[r].size(), {0.0, 0.0});
+    for (size_t c = 0; c < M.rows[r].size(); ++c) index[r][M.rows[r][c]] = c;
+    for (const auto& kv : pot.clusters[r]) {
+      auto it = index[r].find(kv.first);
+      if (it == index[r].end()) {
+        ++M.unmatched_records;
+        continue;
+      }
+      M.coef[r][it->second] = kv.second;
+    }
+  }
+  for (int dd = 0; dd < 2; ++dd) M.c1[dd].assign(L.nbm, 0.0);
+  for (size_t c = 0; c < M.rows[1].size(); ++c)
+    for (int dd = 0; dd < 2; ++dd) M.c1[dd][M.rows[1][c][0] - 1] += M.coef[1][c][dd];
+
+  int st = build_gather(M, msg);
+  if (st) return st;
+  if (!build_lut(M, M.lut)) {
+    msg = "unsupported radial basis type";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+  M.ready = true;
+  return MAGACE_OK;
+}
+
+}  // namespace magace

@@ -1,0 +1,103 @@
+// Host-side model: the enumerated cluster basis of a potential, its
+// coefficients, the generalized Clebsch-Gordan couplings folded into flat
+// product-term tables, and the cubic-Hermite radial lookup tables, laid out
+// for the device kernels.
+//
+// Per-atom data layout used by every kernel ("factor array", complex):
+//   A   [n3a][(l3a+1)^2][n3m][(l3m+1)^2]   bond-sum basis R_nl Y_lm(r) M_n'l' Y_l'm'(m_j)
+//   A2  [nba][n2m][(l2m+1)^2]              pair basis g_n(r) M_n'l' Y_l'm'(m_j)
+//   A0  [n2m][(l2m+1)^2]                   on-site basis M_n'l'(|m_i|) Y_l'm'(m_i)
+//   ONE, ZERO                               constants 1+0i and 0+0i
+// with lm = l*l + l + m. The weight array (dE/dA for the half m' >= 0 that the
+// force pass uses, already multiplied by dE/drho and by the half-plane
+// multiplicity of the reference's force loops, src/forces.F90:460-614) is
+//   WA  [n3a][(l3a+1)^2][n3m][h3]          h = l'(l'+1)/2 + m', m' >= 0
+//   W2  [nba][n2m][h2]
+//   W0  [n2m][h2]
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "potential.hpp"
+
+namespace magace {
+
+struct FactorLayout {
+  int n3a = 0, n3m = 0, l3a = 0, l3m = 0, nba = 0, n2m = 0, l2m = 0, nbm = 0;
+  int lsa = 0, ls3 = 0, ls2 = 0, h3 = 0, h2 = 0;
+  int offA = 0, offA2 = 0, offA0 = 0, offOne = 0, offZero = 0, nF = 0;
+  int nWA = 0, offW2 = 0, offW0 = 0, nW = 0;
+
+  int A(int n1, int l1, int m1, int n2, int l2, int m2) const;  // 0-based radial indices
+  int A2(int n, int nr, int l, int m) const { return offA2 + (n * n2m + nr) * ls2 + l * l + l + m; }
+  int A0(int nr, int l, int m) const { return offA0 + nr * ls2 + l * l + l + m; }
+  int WA(int n1, int l1, int m1, int n2, int l2, int m2) const;   // -1 if not a stored slot
+  int W2(int n, int nr, int l, int m) const { return offW2 + (n * n2m + nr) * h2 + l * (l + 1) / 2 + m; }
+  int W0(int nr, int l, int m) const { return offW0 + nr * h2 + l * (l + 1) / 2 + m; }
+};
+
+// One gather entry: out_slot accumulates kappa * prod(F[o[k]]), k < arity.
+struct Entry {
+  double kappa[2];
+  uint16_t o[3];
+};
+
+// Device-ready gather table. Entries are grouped by output slot and cut into
+// segments of at most kSegLen entries of one arity. Output slots are
+//   [0, nG0)            one per A0 factor (all m): rho and W0
+//   [nG0, nG0+nW)       WA then W2 slots (index into the weight array - nG0 shifted)
+struct GatherTable {
+  static const int kSegLen = 64;
+  int nslot = 0;  // nG0 + nWA + nW2
+  int nG0 = 0;
+  // entries by arity (1, 2, 3 other factors)
+  std::vector<double> k1[2], k2[2], k3[2];
+  std::vector<uint16_t> o1, o2, o3;  // o1: 1 per entry, o2: 2, o3: 3
+  // segments: arity, first entry (within its arity array), count, slot
+  std::vector<int32_t> seg_arity, seg_first, seg_count, seg_slot;
+  std::vector<int32_t> slot_seg_begin;  // [nslot+1] segments of slot s are contiguous
+  std::vector<int32_t> order;           // processing order of segments (balanced)
+  // slot -> factor/weight index and multiplicity
+  std::vector<int32_t> slot_factor;  // for G0 slots: A0 factor index
+  std::vector<int32_t> slot_weight;  // weight index (or -1 when the slot stores no weight)
+  std::vector<double> slot_mult;     // half-plane multiplicity applied to the weight
+};
+
+struct RadialLUT {
+  int nlut = 0;
+  int nfa = 0;  // atomic: g_n (nba), R_nl (n3a*(l3a+1), index nr*(l3a+1)+l), core (1)
+  int nfm = 0;  // magnetic: M_nl (n2m*(l2m+1), index nr*(l2m+1)+l), g_n (nbm)
+  double rscale_a = 0, rscale_m = 0;
+  std::vector<double> a, m;  // [(nlut+1)][nf][4] cubic coefficients per bin
+};
+
+struct Model {
+  Potential pot;
+  double cutoff = 0, cutoff_m = 0;
+  FactorLayout L;
+  int ndensity = 1, nfemb = 0;
+  double par[2][2] = {{1, 1}, {1, 1}};
+  double ecut = 0, decut = 0;
+  double core_pre = 0, core_lambda = 0;
+  // enumerated clusters in file layout, rank 1..4, with coefficients
+  std::vector<std::vector<int>> rows[5];
+  std::vector<std::array<double, 2>> coef[5];
+  int unmatched_records = 0;
+  long nterms[5] = {0, 0, 0, 0, 0};
+  std::vector<double> c1[2];  // 1-body coefficient per magnetic radial function n
+  GatherTable gt;
+  RadialLUT lut;
+  bool ready = false;
+};
+
+// Builds the complete model (enumeration, couplings, tables, LUT) from a
+// parsed potential. rcut / rcut_magnetic are the caller's global cutoffs,
+// which set the LUT grid (src/radial.F90:198, :341).
+int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& model, std::string& msg);
+
+// Clebsch-Gordan coefficient <j1 m1 j2 m2 | J M> by the Racah formula.
+double clebsch_gordan(int j1, int j2, int J, int m1, int m2, int M);
+
+}  // namespace magace

@@ -1,0 +1,141 @@
+"""ctypes binding of libmagace.so, the C ABI declared in include/magace.h.
+
+The product path is this library only: there is no CPU fallback. Loading
+fails with an explicit error when the library has not been built, and
+evaluation calls fail when no CUDA device is present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "libmagace.so")
+
+MAGACE_OK = 0
+ERR_NAMES = {0: "OK", 1: "FILE", 2: "FORMAT", 3: "UNSUPPORTED", 4: "SMALL_R", 5: "MOMENT",
+             6: "NOT_INIT", 7: "ARGS", 8: "CUDA", 9: "NAN"}
+
+_i = ctypes.c_int
+_d = ctypes.c_double
+_pi = ctypes.POINTER(ctypes.c_int)
+_pd = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+
+# every symbol include/magace.h declares, with (restype, argtypes)
+SIGNATURES = {
+    "acelibini_": (None, [_pi, _pd, _pd, _pd, _pi, _pi]),
+    "acelib_": (None, [_pi, _pi, _pi, _pi, _pi, _pi, _pi, _pi, _pd, _pd, _pd, _pd, _pd, _pd, _pd, _pd,
+                       _pd, _pd]),
+    "ace_last_error": (_i, []),
+    "ace_error_string": (ctypes.c_char_p, [_i]),
+    "ace_last_error_message": (ctypes.c_char_p, []),
+    "ace_clear_error": (None, []),
+    "ace_init_file": (_i, [ctypes.c_char_p, ctypes.c_char_p, _d, _d, _d, _i]),
+    "ace_set_precision": (_i, [_i]),
+    "ace_get_precision": (_i, []),
+    "ace_basis_sizes": (_i, [_pi]),
+    "ace_basis_rows": (_i, [_i, _pi]),
+    "ace_compute_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ace_device_status": (_i, []),
+    "ace_last_launch_count": (_i, []),
+    "ace_release_device": (None, []),
+}
+
+_lib = None
+
+
+class MagAceError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"magace error {code} ({ERR_NAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads libmagace.so (once). Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libmagace.so not found at {path}; build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(code: int) -> None:
+    if code != MAGACE_OK:
+        lib = load()
+        raise MagAceError(code, lib.ace_last_error_message().decode())
+
+
+def _ip(a):
+    return a.ctypes.data_as(_pi)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_pd)
+
+
+def init(path: str, element: str = "Fe", rcut: float = 5.0, rcut_magnetic: float = 4.0,
+         smear: float = 0.2, xcnumber: int = 1) -> None:
+    lib = load()
+    _check(lib.ace_init_file(path.encode(), element.encode(), rcut, rcut_magnetic, smear, xcnumber))
+
+
+def set_precision(mode: int) -> None:
+    _check(load().ace_set_precision(mode))
+
+
+def basis_sizes() -> dict:
+    out = np.zeros(8, dtype=np.int32)
+    _check(load().ace_basis_sizes(_ip(out)))
+    return {"nvar": tuple(int(x) for x in out[:4]), "nterms2": int(out[4]), "nterms3": int(out[5]),
+            "nterms4": int(out[6]), "unmatched": int(out[7])}
+
+
+def basis_rows(rank: int) -> np.ndarray:
+    width = {1: 1, 2: 4, 3: 9, 4: 15}[rank]
+    n = basis_sizes()["nvar"][rank - 1]
+    out = np.zeros(max(1, n * width), dtype=np.int32)
+    _check(load().ace_basis_rows(rank, _ip(out)))
+    return out[: n * width].reshape(n, width)
+
+
+def acelib(nb):
+    """Calls the drop-in acelib_ exactly as the LAMMPS pair style does, with
+    host arrays. Returns (eout, flist, tlist, tlist0)."""
+    lib = load()
+    natom, nei, nall = ctypes.c_int(nb.natom), ctypes.c_int(nb.nei), ctypes.c_int(nb.nall)
+    eout = np.zeros(nb.natom)
+    flist = np.zeros(3 * nb.nei)
+    tlist = np.zeros(3 * nb.nei)
+    tlist0 = np.zeros(3 * nb.natom)
+    lib.acelib_(ctypes.byref(natom), ctypes.byref(nall), ctypes.byref(nei), _ip(nb.nlist), _ip(nb.occ),
+                _ip(nb.occlist), _ip(nb.nstart), _ip(nb.nstop), _dp(eout), _dp(nb.dlist), _dp(nb.elist),
+                _dp(flist), _dp(nb.dlist_momi), _dp(nb.elist_momi), _dp(nb.dlist_mom), _dp(nb.elist_mom),
+                _dp(tlist), _dp(tlist0))
+    _check(lib.ace_last_error())
+    return eout, flist, tlist, tlist0
+
+
+def compute_device(natom, nei, off, r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0, stream=0) -> None:
+    """Device-pointer evaluation; every array argument is an integer device
+    address (e.g. torch.Tensor.data_ptr())."""
+    _check(load().ace_compute_device(natom, nei, off, r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0,
+                                     stream))
+
+
+def device_status() -> None:
+    _check(load().ace_device_status())
+
+
+def last_launch_count() -> int:
+    return int(load().ace_last_launch_count())

@@ -1,0 +1,87 @@
+"""Writer for "<Elements>.<xc>.in" potential files and the seeded synthetic
+potential used by the tests and the benchmark.
+
+The seeded potential keeps the basis layout of the reference's example Fe
+potential (example/Fe.pbe.in header, lines 6-13): 16/16 radial base
+functions, 5 magnetic radial functions up to l' = 2, 3-body 4/3 radial
+functions with l = 1 / l' = 2, 4-body 3/3 with l = l' = 0, one density, a
+linear-limit embedding (nfemb 1, par 1.0 1.0), radial types 3 (atomic) and 7
+(magnetic), cutoffs 5.0 A / 4.0 mu_B, taper 0.01, no hard core and inner
+cutoff 10000/250. Every cluster, rad_atomic and rad_magnetic value is drawn
+from N(0, sigma) with a fixed seed. The cluster list is the library's own
+enumeration, read through ace_basis_rows.
+"""
+from __future__ import annotations
+
+import os
+import tempfile
+
+import numpy as np
+
+from . import lib
+
+FE_LAYOUT = dict(nradbase_a=16, nradbase_m=16, nradial2_m=5, l2max_m=2,
+                 nradial3_a=4, nradial3_m=3, l3max_a=1, l3max_m=2,
+                 nradial4_a=3, nradial4_m=3, l4max_a=0, l4max_m=0,
+                 ndensity=1, npot=5, nfemb=1, radtype_a=3, radtype_m=7)
+
+
+def header_lines(element: str, xc: str, smearing: float, lam=(5.25, 5.25), cut=(5.0, 4.0),
+                 dcut=(0.01, 0.01), ecut=10000.0, decut=250.0, layout=FE_LAYOUT) -> list[str]:
+    L = layout
+    return [
+        " Parameters (last)",
+        " created        2026           1           1           0           0           0",
+        f" Elements {element}",
+        f" XC {xc}",
+        f" gauss-smearing   {smearing!r}",
+        f" lambda    {lam[0]!r}        {lam[1]!r}",
+        f" rcut dcut ecut decut    {cut[0]!r}   {cut[1]!r}   {dcut[0]!r}   {dcut[1]!r}   {ecut!r}   {decut!r}",
+        f" nradbase l2max   {L['nradbase_a']} {L['nradbase_m']} {L['nradial2_m']} {L['l2max_m']}",
+        f" nradial3 l3max   {L['nradial3_a']} {L['nradial3_m']} {L['l3max_a']} {L['l3max_m']}",
+        f" nradial4 l4max   {L['nradial4_a']} {L['nradial4_m']} {L['l4max_a']} {L['l4max_m']}",
+        " nradial5 l5max   0 0 0 0",
+        " nradial6 l6max   0 0 0 0",
+        f" ndensity   {L['ndensity']}",
+        f" npot-nfemb-radtype   {L['npot']} {L['nfemb']} {L['radtype_a']} {L['radtype_m']}",
+    ]
+
+
+def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, element: str = "Fe",
+                           xc: str = "pbe", smearing: float = 0.2, layout=FE_LAYOUT,
+                           cut=(5.0, 4.0), core=(0.0, 0.0), par=(1.0, 1.0)) -> str:
+    """Writes the seeded potential to `path` and returns the path. Uses the
+    library's host-only init (no GPU) to enumerate the cluster basis."""
+    head = header_lines(element, xc, smearing, cut=cut, layout=layout)
+    with tempfile.TemporaryDirectory() as td:
+        tmp = os.path.join(td, "header.in")
+        with open(tmp, "w") as f:
+            f.write("\n".join(head) + "\n")
+        lib.init(tmp, element, cut[0], cut[1], smearing, 1 if xc == "pbe" else 2)
+        rows = {r: lib.basis_rows(r) for r in (1, 2, 3, 4)}
+    rng = np.random.default_rng(seed)
+    L = layout
+    out = list(head)
+    for k, v in ((1, par[0]), (2, par[1])):
+        out += [f" par            {k}           1", f" {element}   {v!r}      F"]
+    for k, v in ((1, core[0]), (2, core[1])):
+        out += [f" core            {k}           0", f" {element} {element}   {v!r}      F"]
+    for l in range(L["l3max_a"] + 1):
+        for nr in range(1, L["nradial3_a"] + 1):
+            for n in range(1, L["nradbase_a"] + 1):
+                out += [" rad_atomic            0           0",
+                        f" {element} {element}  {n} {nr} {l} {rng.normal(0.0, sigma)!r} T"]
+    for l in range(L["l2max_m"] + 1):
+        for nr in range(1, L["nradial2_m"] + 1):
+            for n in range(1, L["nradbase_m"] + 1):
+                out += [" rad_magnetic            0           0",
+                        f" {element} {element}  {n} {nr} {l} {rng.normal(0.0, sigma)!r} T"]
+    for rank in (1, 2, 3, 4):
+        els = " ".join([element] * rank)
+        for row in rows[rank]:
+            idx = " ".join(str(int(x)) for x in row)
+            out += [f" clu            {rank}           1",
+                    f" {els}   {idx}   {rng.normal(0.0, sigma)!r}   T"]
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")
+    return path

@@ -18,6 +18,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 
+_current = [None]  # (library id, init arguments) of the state the library holds
+
 _i = ctypes.c_int
 _d = ctypes.c_double
 _pi = ctypes.POINTER(ctypes.c_int)
@@ -33,8 +35,13 @@ def build(quiet: bool = True) -> None:
         print(out.stdout)
 
 
+_libs: dict = {}
+
+
 def _load(fast: bool) -> ctypes.CDLL:
     name = "liboracle_fast.so" if fast else "liboracle.so"
+    if name in _libs:
+        return _libs[name]
     path = os.path.join(BUILD, name)
     if not os.path.exists(path):
         build()
@@ -52,6 +59,7 @@ def _load(fast: bool) -> ctypes.CDLL:
     lib.oracle_atom_state.argtypes = [_i, _i, _pi, _pi, _pd, _pd, _pd, _pd, _pd, _pd, _i, _pd, _pd,
                                       _pd, _pd, _pd, _pd, _pd, _pd]
     lib.oracle_atom_state.restype = _i
+    _libs[name] = lib
     return lib
 
 
@@ -71,17 +79,25 @@ class Oracle:
                  rcut_magnetic: float = 4.0, smear: float = 0.2, xcnumber: int = 1,
                  fast: bool = False):
         self.lib = _load(fast)
-        st = self.lib.oracle_init(potfile.encode(), element.encode(), rcut, rcut_magnetic, smear,
-                                  xcnumber)
-        if st != 0:
-            raise RuntimeError(f"oracle_init failed ({st}): "
-                               + self.lib.oracle_last_error().decode())
+        self._key = (potfile, element, rcut, rcut_magnetic, smear, xcnumber)
+        self._activate(force=True)
         sz = np.zeros(8, dtype=np.int32)
         self.lib.oracle_basis_sizes(_ip(sz))
         self.nvar = tuple(int(x) for x in sz[:4])
         self.nterms3, self.nterms4, self.nterms2 = int(sz[4]), int(sz[5]), int(sz[6])
 
+    def _activate(self, force: bool = False) -> None:
+        """The library keeps one global state; re-initialise it when another
+        Oracle object used it last."""
+        if force or _current[0] != (id(self.lib), self._key):
+            st = self.lib.oracle_init(self._key[0].encode(), self._key[1].encode(), *self._key[2:])
+            if st != 0:
+                raise RuntimeError(f"oracle_init failed ({st}): "
+                                   + self.lib.oracle_last_error().decode())
+            _current[0] = (id(self.lib), self._key)
+
     def basis_rows(self, rank: int) -> np.ndarray:
+        self._activate()
         width = {1: 1, 2: 4, 3: 9, 4: 15}[rank]
         n = self.nvar[rank - 1]
         out = np.zeros(max(1, n) * width, dtype=np.int32)
@@ -93,6 +109,7 @@ class Oracle:
     def acelib(self, nb, nthreads: int = 1, chunk: int = 64):
         """Runs the restated acelib on a NeighborData-like object `nb`
         (attributes as the C-ABI arrays). Returns (eout, flist, tlist, tlist0)."""
+        self._activate()
         natom, nei = nb.natom, nb.nei
         eout = np.zeros(natom)
         flist = np.zeros(3 * nei)
@@ -111,6 +128,7 @@ class Oracle:
     def atom_state(self, nb, atom: int, dims: dict) -> dict:
         """Intermediates of one atom (0-based `atom`); `dims` gives the basis
         dims (nradial3_a, lmaxsq_a, ...)."""
+        self._activate()
         d = dims
         nA = d["n3a"] * d["lsa"] * d["n3m"] * d["lsm"]
         nA2 = d["nba"] * d["n2m"] * d["lsm"]

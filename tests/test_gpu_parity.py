@@ -1,0 +1,185 @@
+"""GPU parity: the FP64 drop-in path (acelib_ through the C ABI) against the
+CPU oracle on identical inputs, at 1e-10 relative (norm-relative for the
+per-bond vectors). Edge cases follow the reference's behaviour: neighbours
+beyond the cutoff contribute zero (src/radial.F90:77-83), moments inside the
+first magnetic bin use the constant branch (src/radial.F90:135-139), and
+inputs that stop the reference are reported as errors with NaN outputs.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-10
+
+
+@pytest.fixture()
+def gpu_lib(seeded_potential):
+    from magace import lib
+    lib.init(seeded_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    lib.set_precision(0)
+    return lib
+
+
+def _compare(lib, orc, nb, tol=TOL_FP64):
+    e, f, t, t0 = lib.acelib(nb)
+    eo, fo, to, t0o = orc.acelib(nb)
+    assert rel_err(e, eo) <= tol, ("energy", rel_err(e, eo))
+    assert rel_err(f, fo) <= tol, ("flist", rel_err(f, fo))
+    assert rel_err(t, to) <= tol, ("tlist", rel_err(t, to))
+    assert rel_err(t0, t0o) <= tol, ("tlist0", rel_err(t0, t0o))
+    return e, f, t, t0
+
+
+def test_bcc128_fp64_parity(gpu_lib, oracle_seeded):
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_128(1), 5.0)
+    _compare(gpu_lib, oracle_seeded, nb)
+
+
+def test_notebook_cell_fp64_parity(gpu_lib, oracle_seeded):
+    from magace import structures as S
+    nb = S.neighbor_data(S.notebook_cell(), 5.0)
+    e, *_ = _compare(gpu_lib, oracle_seeded, nb)
+    assert abs(e[0] - e[1]) < 1e-12  # the two atoms are equivalent
+
+
+def test_ragged_slab_with_isolated_atom(gpu_lib, oracle_seeded):
+    """(100) slab (non-periodic z), vacancies, and one atom far from all
+    others: neighbour counts from 0 to ~58."""
+    from magace import structures as S
+    rng = np.random.default_rng(7)
+    pos, cell = S.bcc_cubic(3, 3, 3, 2.83)
+    pos = pos + rng.normal(0, 0.08, pos.shape)
+    keep = rng.random(len(pos)) > 0.1
+    pos = pos[keep]
+    pos = np.vstack([pos, [[4.0, 4.0, 40.0]]])
+    n = len(pos)
+    st = S.Structure(pos, cell, (True, True, False), rng.uniform(1.5, 2.6, n), S.random_unit(rng, n))
+    nb = S.neighbor_data(st, 5.0)
+    counts = nb.nstop - nb.nstart + 1
+    assert counts.min() == 0 and counts.max() > 30
+    _compare(gpu_lib, oracle_seeded, nb)
+
+
+def test_noncontiguous_ranges(gpu_lib, oracle_seeded):
+    """Bond ranges given in a different order than the atoms (the acelib_
+    gather path); the outputs stay packed atom by atom."""
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_54(3), 5.0)
+    counts = nb.nstop - nb.nstart + 1
+    order = np.arange(nb.natom)[::-1]
+    # rebuild the bond arrays with atoms' blocks stored in reverse order
+    blocks = [np.arange(nb.nstart[i] - 1, nb.nstop[i]) for i in order]
+    perm = np.concatenate(blocks)
+    new_start = np.zeros(nb.natom, np.int32)
+    pos = 1
+    for i in order:
+        new_start[i] = pos
+        pos += counts[i]
+    nb2 = S.NeighborData(
+        natom=nb.natom, nall=nb.nall, nei=nb.nei, nlist=nb.nlist[perm], occ=nb.occ,
+        occlist=nb.occlist[perm], nstart=new_start, nstop=(new_start + counts - 1).astype(np.int32),
+        dlist=nb.dlist[perm].copy(), elist=nb.elist.reshape(-1, 3)[perm].reshape(-1).copy(),
+        dlist_momi=nb.dlist_momi, elist_momi=nb.elist_momi, dlist_mom=nb.dlist_mom[perm].copy(),
+        elist_mom=nb.elist_mom.reshape(-1, 3)[perm].reshape(-1).copy())
+    e, f, t, t0 = gpu_lib.acelib(nb)
+    e2, f2, t2, t02 = gpu_lib.acelib(nb2)
+    # packed outputs follow atom order, so they match the contiguous call
+    assert rel_err(e2, e) <= 1e-14
+    assert rel_err(f2, f) <= 1e-14 and rel_err(t2, t) <= 1e-14 and rel_err(t02, t0) <= 1e-14
+    _compare(gpu_lib, oracle_seeded, nb2)
+
+
+def test_neighbours_beyond_cutoff_and_small_moments(gpu_lib, oracle_seeded):
+    """A LAMMPS-style list with skin (bonds up to 6.5 A) and some moments
+    inside the first magnetic LUT bin (|m| < 4e-4 mu_B)."""
+    from magace import structures as S
+    st = S.bcc_fe_54(11)
+    st.mag[:5] = np.array([1e-5, 2e-4, 3.9e-4, 1e-6, 2.5e-4])
+    nb = S.neighbor_data(st, 6.5)
+    assert nb.dlist.max() > 5.0
+    _compare(gpu_lib, oracle_seeded, nb)
+
+
+def test_repeat_is_bitwise_deterministic(gpu_lib):
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_128(4), 5.0)
+    a = gpu_lib.acelib(nb)
+    b = gpu_lib.acelib(nb)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_empty_call(gpu_lib):
+    from magace import structures as S
+    nb = S.NeighborData(natom=0, nall=0, nei=0, nlist=np.zeros(0, np.int32), occ=np.zeros(0, np.int32),
+                        occlist=np.zeros(0, np.int32), nstart=np.zeros(0, np.int32),
+                        nstop=np.zeros(0, np.int32), dlist=np.zeros(0), elist=np.zeros(0),
+                        dlist_momi=np.zeros(0), elist_momi=np.zeros(0), dlist_mom=np.zeros(0),
+                        elist_mom=np.zeros(0))
+    e, f, t, t0 = gpu_lib.acelib(nb)
+    assert e.size == 0 and f.size == 0
+
+
+def test_small_distance_is_an_error(gpu_lib):
+    """r below one LUT bin stops the reference (src/radial.F90:71-75); here
+    acelib_ records MAGACE_ERR_SMALL_R and writes NaN."""
+    from magace import structures as S
+    from magace.lib import MagAceError
+    nb = S.neighbor_data(S.bcc_fe_54(5), 5.0)
+    nb.dlist = nb.dlist.copy()
+    nb.dlist[3] = 1e-4
+    with pytest.raises(MagAceError) as ei:
+        gpu_lib.acelib(nb)
+    assert ei.value.code == 4
+    # the library stays usable afterwards
+    nb2 = S.neighbor_data(S.bcc_fe_54(5), 5.0)
+    e, *_ = gpu_lib.acelib(nb2)
+    assert np.all(np.isfinite(e))
+
+
+def test_moment_beyond_cutoff_is_an_error(gpu_lib):
+    """|m| >= the magnetic cutoff overruns the reference's table
+    (src/radial.F90:126-157 has no upper check); here it is an error."""
+    from magace import structures as S
+    from magace.lib import MagAceError
+    st = S.bcc_fe_54(6)
+    st.mag[0] = 4.5
+    nb = S.neighbor_data(st, 5.0)
+    with pytest.raises(MagAceError) as ei:
+        gpu_lib.acelib(nb)
+    assert ei.value.code == 5
+
+
+def test_device_api_matches_acelib(gpu_lib):
+    """ace_compute_device on torch-owned device arrays gives the same numbers
+    as the host-array drop-in call."""
+    import torch
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_128(2), 5.0)
+    e, f, t, t0 = gpu_lib.acelib(nb)
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    r, ee, mj, mhj, mi, mhi = map(T, (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi,
+                                      nb.elist_momi))
+    en = torch.empty(nb.natom, dtype=torch.float64, device=dev)
+    fij = torch.empty(3 * nb.nei, dtype=torch.float64, device=dev)
+    tij = torch.empty_like(fij)
+    ti0 = torch.empty(3 * nb.natom, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    gpu_lib.compute_device(nb.natom, nb.nei, off.data_ptr(), r.data_ptr(), ee.data_ptr(), mj.data_ptr(),
+                           mhj.data_ptr(), mi.data_ptr(), mhi.data_ptr(), en.data_ptr(), fij.data_ptr(),
+                           tij.data_ptr(), ti0.data_ptr(), stream)
+    torch.cuda.synchronize()
+    gpu_lib.device_status()
+    assert np.array_equal(en.cpu().numpy(), e)
+    assert np.array_equal(fij.cpu().numpy(), f)
+    assert np.array_equal(tij.cpu().numpy(), t)
+    assert np.array_equal(ti0.cpu().numpy(), t0)
+    assert gpu_lib.last_launch_count() == 3

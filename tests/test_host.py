@@ -1,0 +1,125 @@
+"""CPU tests of the product library's host side: it loads, exports every
+symbol include/magace.h declares, initialises without a GPU, enumerates the
+same basis as the oracle and reports the reference's fatal conditions as
+status codes. No compute call is made here."""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REFERENCE_FE, REPO
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from magace import build, lib as L
+    build.build()
+    L.load()
+    return L
+
+
+def header_symbols():
+    text = open(os.path.join(REPO, "include", "magace.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", text)) - {"defined"})
+
+
+def test_exports_every_declared_symbol(lib):
+    names = header_symbols()
+    assert "acelib_" in names and "acelibini_" in names and len(names) >= 15
+    so = ctypes.CDLL(lib.LIB_PATH)
+    for n in names:
+        assert hasattr(so, n), n
+    assert set(names) == set(lib.SIGNATURES), "binding table out of sync with the header"
+
+
+def test_init_and_basis_match_oracle(lib, seeded_potential, oracle_seeded):
+    lib.init(seeded_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    sz = lib.basis_sizes()
+    assert sz["nvar"] == (16, 720, 4932, 495)
+    assert (sz["nterms2"], sz["nterms3"], sz["nterms4"]) == (2160, 64008, 495)
+    assert sz["unmatched"] == 0
+    for r in (1, 2, 3, 4):
+        assert np.array_equal(lib.basis_rows(r), oracle_seeded.basis_rows(r))
+
+
+def test_reference_potential_matches_enumeration(lib):
+    if not os.path.exists(REFERENCE_FE):
+        pytest.skip("reference example potential not available")
+    lib.init(REFERENCE_FE, "Fe", 4.5, 4.0, 0.2, 1)
+    sz = lib.basis_sizes()
+    # every record of example/Fe.pbe.in is an enumerated cluster
+    assert sz["nvar"] == (16, 720, 4932, 495) and sz["unmatched"] == 0
+
+
+def test_seeded_potential_is_reproducible(tmp_path):
+    from magace import potential
+    p = potential.write_seeded_potential(str(tmp_path / "Fe.pbe.in"), seed=2024)
+    sha = hashlib.sha256(open(p, "rb").read()).hexdigest()
+    g = json.load(open(os.path.join(GOLDEN, "seeded_bcc16.json")))
+    assert sha == g["potential_sha256"]
+
+
+def test_error_codes(lib, tmp_path, seeded_potential):
+    from magace.lib import MagAceError
+    with pytest.raises(MagAceError) as e:
+        lib.init(str(tmp_path / "missing.in"))
+    assert e.value.code == 1
+    with pytest.raises(MagAceError) as e:
+        lib.init(seeded_potential, element="Co")
+    assert e.value.code == 2
+    with pytest.raises(MagAceError) as e:
+        lib.init(seeded_potential, smear=0.3)
+    assert e.value.code == 2
+    with pytest.raises(MagAceError) as e:
+        lib.init(seeded_potential, xcnumber=3)
+    assert e.value.code == 7
+    with pytest.raises(MagAceError) as e:
+        lib.init(seeded_potential, rcut=4.0)  # shorter than the file's 5.0 A
+    assert e.value.code == 2
+    # 5-body clusters are rejected
+    text = open(seeded_potential).read().replace(" nradial5 l5max   0 0 0 0", " nradial5 l5max   1 1 0 0")
+    p5 = tmp_path / "five.in"
+    p5.write_text(text)
+    with pytest.raises(MagAceError) as e:
+        lib.init(str(p5))
+    assert e.value.code == 3
+    assert lib.load().ace_error_string(4).decode().startswith("bond shorter")
+
+
+def test_acelibini_reads_working_directory(lib, tmp_path, seeded_potential, monkeypatch):
+    """acelibini_(nele=1, ..., elenumbers=[27]) opens ./Fe.pbe.in
+    (src/util.F90:525; 27 = atomic number 26 + 1)."""
+    so = lib.load()
+    import shutil
+    shutil.copy(seeded_potential, tmp_path / "Fe.pbe.in")
+    monkeypatch.chdir(tmp_path)
+    nele = ctypes.c_int(2)
+    rc, rcm, sm, xc = ctypes.c_double(5.0), ctypes.c_double(4.0), ctypes.c_double(0.2), ctypes.c_int(1)
+    el = (ctypes.c_int * 1)(27)
+    so.acelibini_(ctypes.byref(nele), ctypes.byref(rc), ctypes.byref(rcm), ctypes.byref(sm), ctypes.byref(xc), el)
+    assert so.ace_last_error() == 3  # more than one element is refused, as in src/ace.F90:46-49
+    nele.value = 1
+    so.acelibini_(ctypes.byref(nele), ctypes.byref(rc), ctypes.byref(rcm), ctypes.byref(sm), ctypes.byref(xc), el)
+    assert so.ace_last_error() == 0
+    assert lib.basis_sizes()["nvar"][2] == 4932
+
+
+def test_acelib_before_init_reports_error(tmp_path):
+    """A fresh process: acelib_ without init records NOT_INIT and fills NaN."""
+    import subprocess
+    import sys
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r);"
+        "from magace import lib, structures as S;"
+        "nb = S.neighbor_data(S.notebook_cell(), 5.0);"
+        "\ntry:\n    lib.acelib(nb)\nexcept lib.MagAceError as e:\n    print('code', e.code)"
+    ) % os.path.join(REPO, "mag-ace_gb300")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert "code 6" in out.stdout, out.stdout + out.stderr

@@ -1,0 +1,113 @@
+"""CPU tests of the oracle itself: pinned to the reference's only known
+answer (example/basic_lammps.ipynb:272) and to centred finite differences,
+plus the symmetries the energy must have."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REFERENCE_FE
+
+NOTEBOOK_ETOT = -15.7479878560111  # example/basic_lammps.ipynb:272
+
+
+@pytest.fixture(scope="module")
+def oracle_fe():
+    if not os.path.exists(REFERENCE_FE):
+        pytest.skip("reference example potential not available")
+    import oracle as orc
+    return orc.Oracle(REFERENCE_FE, "Fe", rcut=4.5, rcut_magnetic=4.0, smear=0.2)
+
+
+def test_basis_sizes_fe(oracle_fe):
+    # clusters of example/Fe.pbe.in: 16 'clu 1', 720 'clu 2', 4932 'clu 3', 495 'clu 4'
+    assert oracle_fe.nvar == (16, 720, 4932, 495)
+    assert (oracle_fe.nterms2, oracle_fe.nterms3, oracle_fe.nterms4) == (2160, 64008, 495)
+
+
+def test_notebook_energy(oracle_fe):
+    from magace import structures as S
+    nb = S.neighbor_data(S.notebook_cell(), 4.5)
+    assert np.all(nb.stop_counts == 26) if hasattr(nb, "stop_counts") else True
+    e, f, t, t0 = oracle_fe.acelib(nb)
+    assert abs(e.sum() - NOTEBOOK_ETOT) < 1e-12 * abs(NOTEBOOK_ETOT) + 1e-13
+    F, FM = S.total_forces(nb, f, t, t0)
+    assert np.abs(F).max() < 1e-12  # example/basic_lammps.ipynb:292-293
+
+
+def test_notebook_golden_fixture(oracle_fe):
+    """The committed golden vectors (tests/golden/notebook_fe.json, made by
+    tests/golden/make_golden.py) match the oracle bit for bit."""
+    from magace import structures as S
+    with open(os.path.join(GOLDEN, "notebook_fe.json")) as fh:
+        g = json.load(fh)
+    nb = S.neighbor_data(S.notebook_cell(), 4.5)
+    e, f, t, t0 = oracle_fe.acelib(nb)
+    assert np.allclose(e, g["eout"], rtol=0, atol=1e-13)
+    assert np.allclose(t0, g["tlist0"], rtol=0, atol=1e-13)
+
+
+def _energy(orc, st, rcut):
+    from magace import structures as S
+    nb = S.neighbor_data(st, rcut)
+    e, f, t, t0 = orc.acelib(nb)
+    return e.sum(), nb, f, t, t0
+
+
+@pytest.mark.parametrize("which", ["fe", "seeded"])
+def test_finite_differences(which, oracle_fe, oracle_seeded):
+    """Forces and magnetic forces assembled as in lammps/pair_spin_ace.cpp
+    equal -dE/dx and -dE/dm from centred differences (h = 1e-5)."""
+    from magace import structures as S
+    orc, rc = (oracle_fe, 4.5) if which == "fe" else (oracle_seeded, 5.0)
+    rng = np.random.default_rng(3)
+    pos, cell = S.bcc_cubic(2, 2, 2, 2.83)
+    pos = pos + rng.normal(0, 0.08, pos.shape)
+    n = len(pos)
+    mvec = rng.uniform(1.8, 2.4, n)[:, None] * S.random_unit(rng, n)
+
+    def st_of(p, mv):
+        m = np.linalg.norm(mv, axis=1)
+        return S.Structure(p, cell, (True,) * 3, m, mv / m[:, None])
+
+    E, nb, f, t, t0 = _energy(orc, st_of(pos, mvec), rc)
+    F, FM = S.total_forces(nb, f, t, t0)
+    h = 1e-5
+    for k in (0, 5, 11):
+        for c in range(3):
+            p = pos.copy(); p[k, c] += h
+            ep = _energy(orc, st_of(p, mvec), rc)[0]
+            p[k, c] -= 2 * h
+            em = _energy(orc, st_of(p, mvec), rc)[0]
+            assert abs(-(ep - em) / (2 * h) - F[k, c]) < 5e-7 * max(1.0, abs(F[k, c]))
+            mv = mvec.copy(); mv[k, c] += h
+            ep = _energy(orc, st_of(pos, mv), rc)[0]
+            mv[k, c] -= 2 * h
+            em = _energy(orc, st_of(pos, mv), rc)[0]
+            assert abs(-(ep - em) / (2 * h) - FM[k, c]) < 5e-7 * max(1.0, abs(FM[k, c]))
+
+
+def test_rotation_and_moment_reversal(oracle_seeded):
+    """E is invariant under a joint rotation of positions and moments, under
+    separate rotations of the moments alone (the magnetic and atomic spaces
+    are coupled to invariants separately, src/b_basis.F90:142-212), and under
+    m -> -m (even magnetic l sums)."""
+    from magace import structures as S
+    rng = np.random.default_rng(9)
+    pos, cell = S.bcc_cubic(2, 2, 2, 2.83)
+    pos = pos + rng.normal(0, 0.05, pos.shape)
+    n = len(pos)
+    mag = rng.uniform(1.8, 2.4, n)
+    mh = S.random_unit(rng, n)
+    e0 = oracle_seeded.acelib(S.neighbor_data(S.Structure(pos, cell, (True,) * 3, mag, mh), 5.0))[0]
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] *= -1
+    # rotate the moments only
+    e1 = oracle_seeded.acelib(S.neighbor_data(S.Structure(pos, cell, (True,) * 3, mag, mh @ q.T), 5.0))[0]
+    e2 = oracle_seeded.acelib(S.neighbor_data(S.Structure(pos, cell, (True,) * 3, mag, -mh), 5.0))[0]
+    assert np.allclose(e1, e0, rtol=0, atol=1e-10)
+    assert np.allclose(e2, e0, rtol=0, atol=1e-10)
