@@ -1,0 +1,382 @@
+"""Benchmark of the mag-ace potential evaluation on GB300.
+
+Metric: atom-evals/s, one atom-eval = the atom's energy E_i, its per-bond
+forces dE_i/d(x_i - x_j) and magnetic forces dE_i/dm_j, and dE_i/dm_i.
+
+Workload (one step = one evaluation of the whole system): 20x20x20 cubic bcc
+Fe cells (16,000 sites, a = 2.83 A) with 1% random vacancies, jitter
+N(0, 0.1 A), paramagnetic moments uniform on the sphere with
+|m| ~ U(1.5, 2.6) mu_B, cutoff 5.0 A, the seeded potential in the reference's
+example Fe layout. Synthetic, seeded data; no dataset is involved.
+
+  value   device-resident inputs, CUDA-event time of the three kernels per step
+  e2e     the drop-in acelib_ with host arrays (copies in and out inside the
+          timed region), wall clock per call
+
+With --gpus N > 1 (torchrun), every rank evaluates its own replica of the
+workload (weak scaling, no collective in the data path); value = total atoms
+over the slowest rank's time.
+
+--impl reference times the CPU oracle port (the reference algorithm restated
+in C++, all host threads) on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "mag-ace_gb300"))
+
+METRIC = "atom-evals/s (E+F+magF)"
+UNIT = "atom-evals/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--precision", default="auto", choices=["auto", "fp64", "split"])
+    p.add_argument("--ncell", type=int, default=20)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(ncell: int, tmpdir: str):
+    from magace import potential, structures as S
+    pot = potential.write_seeded_potential(os.path.join(tmpdir, "Fe.pbe.in"), seed=2024)
+    st = S.bcc_fe_vacancies(ncell=ncell, seed=2)
+    nb = S.neighbor_data(st, 5.0)
+    desc = (f"bcc Fe {ncell}x{ncell}x{ncell} cubic cells, 1% vacancies ({nb.natom} atoms, {nb.nei} bonds), "
+            "rcut 5.0 A, seeded potential in the example Fe.pbe.in layout")
+    return pot, nb, desc
+
+
+def flop_model(stats: dict, natom: int, nbond: int) -> dict:
+    """Algorithmic FLOPs of one evaluation, per kernel, from the basis tables
+    ('FLOP model'). One complex multiply = 6, a complex MAC = 8,
+    a complex-by-real MAC = 4, a cubic LUT evaluation = 6 (+6 with derivative)."""
+    s = stats
+    nM = s["n2m"] * (s["l2m"] + 1)          # magnetic radial functions per bond
+    nRY = s["n3a"] * (s["l3a"] + 1) ** 2    # R_nl Y_lm products
+    nQ = s["n2m"] * s["h2"]                 # M_n'l' Y_l'm' products (m' >= 0)
+    nQ3 = s["n3m"] * s["h3"]
+    nfa, nWA, nA2h = s["nfa"], s["nWA"], s["nA2h"]
+    ab_bond = 6 * (nfa + nM) + 2 * nRY + 2 * nQ + 8 * nWA + 4 * nA2h
+    dens_atom = 4 * s["ne1"] + 10 * s["ne2"] + 16 * s["ne3"] + 4 * s["n2m"] * (s["l2m"] + 1) ** 2
+    f_bond = (12 * (nfa + nM)                       # radial values and derivatives
+              + nQ * (2 + 5 * s["nba"])             # pair force
+              + nRY * nQ3 * 10 + nRY * 20           # many-body force via U
+              + nQ * s["nba"] * 4                   # pair magnetic force
+              + nQ3 * nRY * 10 + nQ * 18)           # many-body magnetic force via V
+    return {"k_abasis": ab_bond * nbond, "k_density": dens_atom * natom, "k_forces": f_bond * nbond}
+
+
+def measure_peaks(torch):
+    """FP64 and FP32 (CUDA-core, TF32 off) GEMM throughput measured in-run with
+    cuBLAS; the basis of the FP pipe rooflines."""
+    out = {}
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n in (("fp64", torch.float64, 4096), ("fp32", torch.float32, 8192)):
+        a = torch.randn(n, n, device="cuda", dtype=dt)
+        b = torch.randn(n, n, device="cuda", dtype=dt)
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            a @ b
+            e.record()
+            torch.cuda.synchronize()
+            best = min(best, s.elapsed_time(e) / 1e3)
+        out[name] = 2.0 * n ** 3 / best / 1e12
+        del a, b
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    torch.cuda.empty_cache()
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_arm(args, rank, world, local_rank):
+    import torch
+    from magace import build as mbuild, lib
+    if not os.path.exists(mbuild.LIB):
+        mbuild.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    tmp = tempfile.mkdtemp(prefix="magace_bench_")
+    pot, nb, desc = workload(args.ncell, tmp)
+    lib.init(pot, "Fe", 5.0, 4.0, 0.2, 1)
+    stats = lib.table_stats()
+    counts = (nb.nstop - nb.nstart + 1)
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    T = lambda a, dt=torch.float64: torch.tensor(a, dtype=dt, device=dev)
+    d_off = T(off, torch.int32)
+    d_r, d_e, d_mj, d_mhj, d_mi, d_mhi = map(T, (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom,
+                                                  nb.dlist_momi, nb.elist_momi))
+    out = {k: torch.empty(n, dtype=torch.float64, device=dev)
+           for k, n in (("e", nb.natom), ("f", 3 * nb.nei), ("t", 3 * nb.nei), ("t0", 3 * nb.natom))}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    def step():
+        lib.compute_device(nb.natom, nb.nei, d_off.data_ptr(), d_r.data_ptr(), d_e.data_ptr(), d_mj.data_ptr(),
+                           d_mhj.data_ptr(), d_mi.data_ptr(), d_mhi.data_ptr(), out["e"].data_ptr(),
+                           out["f"].data_ptr(), out["t"].data_ptr(), out["t0"].data_ptr(), stream)
+
+    peaks = measure_peaks(torch) if rank == 0 else {}
+    flops = flop_model(stats, nb.natom, nb.nei)
+
+    def run_path(mode):
+        lib.set_precision(mode)
+        lib.set_kernel_timing(True)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        lib.device_status()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        step_ms, ktimes = [], []
+        with ClockSampler(local_rank) as clk:
+            wall0 = time.perf_counter()
+            for _ in range(args.steps):
+                flush.zero_()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record()
+                step()
+                e.record()
+                e.synchronize()
+                step_ms.append(s.elapsed_time(e))
+                ktimes.append(lib.kernel_times())
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - wall0
+        if world > 1:
+            torch.distributed.barrier()
+        lib.device_status()
+        res = {k: v.detach().cpu().numpy().copy() for k, v in out.items()}
+        return {"ms": float(np.mean(step_ms)), "ms_all": step_ms, "kernel_ms": np.mean(ktimes, axis=0).tolist(),
+                "wall_s": wall, "clocks": clk.summary(), "out": res}
+
+    paths = {}
+    want = ["fp64", "split"] if args.precision == "auto" else [args.precision]
+    for name in want:
+        paths[name] = run_path(0 if name == "fp64" else 1)
+
+    # accuracy of the split path against the FP64 path (which equals the oracle to 1e-10)
+    acc = None
+    if "split" in paths and "fp64" in paths:
+        a, b = paths["split"]["out"], paths["fp64"]["out"]
+        acc = {"energy_meV_per_atom": float(np.abs(a["e"] - b["e"]).max() * 1e3),
+               "force_meV_per_A": float(np.abs(a["f"] - b["f"]).max() * 1e3),
+               "magforce_meV_per_muB": float(max(np.abs(a["t"] - b["t"]).max(), np.abs(a["t0"] - b["t0"]).max()) * 1e3)}
+    split_ok = acc is not None and acc["energy_meV_per_atom"] <= 1.0 and acc["force_meV_per_A"] <= 10.0
+    headline = "split" if (("split" in paths) and (split_ok or args.precision == "split")) else "fp64"
+    P = paths[headline]
+
+    # slowest rank defines the step time
+    ms = P["ms"]
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nb.natom / (ms / 1e3)
+
+    # end-to-end through the drop-in acelib_ with host arrays
+    lib.set_precision(0 if headline == "fp64" else 1)
+    lib.set_kernel_timing(False)
+    for _ in range(max(1, args.warmup)):
+        lib.acelib(nb)
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        lib.acelib(nb)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e_t))
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = (nb.natom + 1) * 4 + nb.nei * 8 * 8 + nb.natom * 8 * 4
+    d2h = nb.natom * 8 * 4 + nb.nei * 8 * 6 + 4
+
+    if rank != 0:
+        return None
+    kms = P["kernel_ms"]
+    names = ["k_abasis", "k_density", "k_forces"]
+    dom = int(np.argmax(kms))
+    fp_peak = peaks.get("fp64" if headline == "fp64" else "fp32")
+    achieved = flops[names[dom]] / (kms[dom] / 1e3) / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if headline == "fp64" else "f32/f64-split",
+        "data": "synthetic (seeded potential and structure)",
+        "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": headline,
+                   "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * nb.natom / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": 3 * args.steps,
+        "roofline": {"bound": "fp64" if headline == "fp64" else "fp32", "kernel": names[dom],
+                     "achieved": achieved, "peak": fp_peak, "unit": "TFLOP/s",
+                     "frac": (achieved / fp_peak) if fp_peak else None, "traffic": None,
+                     "peak_source": "measured in this run: cuBLAS %s GEMM (TF32 off)" % ("DGEMM" if headline == "fp64" else "SGEMM"),
+                     "flops_per_launch": flops[names[dom]]},
+        "kernel_ms": dict(zip(names, kms)),
+        "clocks": P["clocks"],
+        "paths": {k: {"ms_per_step": v["ms"], "atom_evals_per_s": world * nb.natom / (v["ms"] / 1e3),
+                      "kernel_ms": dict(zip(names, v["kernel_ms"]))} for k, v in paths.items()},
+        "split_error_vs_fp64": acc,
+        "peaks_measured_tflops": peaks,
+    }
+    return line, nb, pot
+
+
+def cpu_baseline(nb, pot, budget_s: float, steps: int = 1):
+    """The oracle port (reference algorithm, -Ofast, all host threads) on a
+    contiguous sample of the workload's atoms, sized to about budget_s."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as orc
+    from magace import structures as S
+    threads = os.cpu_count() or 1
+    o = orc.Oracle(pot, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2, fast=True)
+
+    def sample(n):
+        n = min(n, nb.natom)
+        b1 = int(nb.nstop[n - 1])
+        sub = S.NeighborData(natom=n, nall=n, nei=b1, nlist=nb.nlist[:b1], occ=nb.occ[:n],
+                             occlist=nb.occlist[:b1], nstart=nb.nstart[:n], nstop=nb.nstop[:n],
+                             dlist=nb.dlist[:b1], elist=nb.elist[:3 * b1], dlist_momi=nb.dlist_momi[:n],
+                             elist_momi=nb.elist_momi[:3 * n], dlist_mom=nb.dlist_mom[:b1],
+                             elist_mom=nb.elist_mom[:3 * b1])
+        t0 = time.perf_counter()
+        o.acelib(sub, nthreads=threads, chunk=32)
+        return n, time.perf_counter() - t0
+
+    n, dt = sample(min(nb.natom, 4 * threads))
+    rate = n / dt
+    n = int(max(threads, min(nb.natom, rate * budget_s / max(1, steps))))
+    rates = []
+    for _ in range(steps):
+        n2, dt2 = sample(n)
+        rates.append(n2 / dt2)
+    return {"value": float(np.mean(rates)), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} atoms of the workload per step (contiguous block), oracle port -Ofast, "
+                      f"{threads} threads, chunk 32 atoms"}
+
+
+def reference_arm(args, rank):
+    if rank != 0:
+        return
+    tmp = tempfile.mkdtemp(prefix="magace_ref_")
+    pot, nb, desc = workload(args.ncell, tmp)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as orc
+    orc.build()
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline(nb, pot, budget_s=2.0)
+    cb = cpu_baseline(nb, pot, budget_s=args.cpu_seconds * max(1, args.steps) / 2, steps=args.steps)
+    line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded potential and structure)",
+            "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": "reference-port"},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank)
+        return
+    import torch
+    if world > 1:
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    res = gpu_arm(args, rank, world, local_rank)
+    if rank == 0 and res is not None:
+        line, nb, pot = res
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(nb, pot, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

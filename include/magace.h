@@ -113,6 +113,22 @@ int ace_device_status(void);
 /* Number of kernel launches issued by the last evaluation call. */
 int ace_last_launch_count(void);
 
+/* Kernel timing: when on, the boundaries of the three kernels of every
+ * evaluation are recorded with CUDA events on the evaluation stream;
+ * ace_kernel_times writes the last evaluation's per-kernel durations in ms
+ * (k_abasis, k_density, k_forces), synchronising on the last event. */
+int ace_set_kernel_timing(int on);
+int ace_kernel_times(float* ms);
+
+/* Gather-table statistics: out[0..2] entries with 1/2/3 other factors,
+ * out[3] segments, out[4] output slots, out[5] factors per atom (nF),
+ * out[6] weights per atom (nW), out[7] A weight slots, out[8] A2 half slots,
+ * out[9] atomic LUT functions, out[10] magnetic LUT functions, out[11..20]
+ * the basis dims nradbase_a, nradbase_m, nradial2_m, l2max_m, nradial3_a,
+ * nradial3_m, l3max_a, l3max_m, and the half-plane sizes h2, h3
+ * (21 entries). */
+int ace_table_stats(long long* out);
+
 /* Releases every device buffer held by the library (tables stay on the host). */
 void ace_release_device(void);
 

@@ -85,6 +85,11 @@ struct Runtime {
   DevBuf<double> r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0, rho1, core, edf, dedrho;
   DevBuf<unsigned char> F, W;
   std::vector<int> h_off;
+
+  // optional kernel-boundary events of the last evaluation
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ev_recorded = false;
 };
 
 Runtime& rt() {
@@ -254,8 +259,15 @@ int run_eval(EvalBuffers& b, cudaStream_t st) {
   b.dedrho = R.dedrho.p;
   b.err = R.err.p;
   CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), st));
-  R.last_launches = R.precision == 0 ? launch_eval_fp64(R.dm, b, st, R.grid_cap)
-                                     : launch_eval_fp32(R.dm, b, st, R.grid_cap);
+  cudaEvent_t* ev = nullptr;
+  if (R.timing) {
+    for (auto& e : R.ev)
+      if (!e) CUDA_TRY(cudaEventCreate(&e));
+    ev = R.ev;
+  }
+  R.last_launches = R.precision == 0 ? launch_eval_fp64(R.dm, b, st, R.grid_cap, ev)
+                                     : launch_eval_fp32(R.dm, b, st, R.grid_cap, ev);
+  R.ev_recorded = ev != nullptr && R.last_launches == 3;
   CUDA_TRY(cudaGetLastError());
   return MAGACE_OK;
 }
@@ -380,6 +392,40 @@ int ace_basis_rows(int rank, int* out) {
 }
 
 int ace_last_launch_count(void) { return rt().last_launches; }
+
+int ace_set_kernel_timing(int on) {
+  rt().timing = on != 0;
+  return MAGACE_OK;
+}
+
+int ace_kernel_times(float* ms) {
+  Runtime& R = rt();
+  if (!R.ev_recorded) return set_error(MAGACE_ERR_ARGS, "no timed evaluation recorded");
+  CUDA_TRY(cudaEventSynchronize(R.ev[3]));
+  for (int k = 0; k < 3; ++k) CUDA_TRY(cudaEventElapsedTime(&ms[k], R.ev[k], R.ev[k + 1]));
+  return MAGACE_OK;
+}
+
+int ace_table_stats(long long* out) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  const GatherTable& g = R.model.gt;
+  const FactorLayout& L = R.model.L;
+  out[0] = static_cast<long long>(g.k1[0].size());
+  out[1] = static_cast<long long>(g.k2[0].size());
+  out[2] = static_cast<long long>(g.k3[0].size());
+  out[3] = static_cast<long long>(g.seg_slot.size());
+  out[4] = g.nslot;
+  out[5] = L.nF;
+  out[6] = L.nW;
+  out[7] = L.nWA;
+  out[8] = static_cast<long long>(L.nba) * L.n2m * L.h2;  // A2 half slots
+  out[9] = R.model.lut.nfa;
+  out[10] = R.model.lut.nfm;
+  const int dims[10] = {L.nba, L.nbm, L.n2m, L.l2m, L.n3a, L.n3m, L.l3a, L.l3m, L.h2, L.h3};
+  for (int k = 0; k < 10; ++k) out[11 + k] = dims[k];
+  return MAGACE_OK;
+}
 
 int ace_compute_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
                        const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,

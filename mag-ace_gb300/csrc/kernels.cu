@@ -766,14 +766,16 @@ size_t forces_smem(const DeviceModel& m, int T) {
 }
 
 template <class R>
-int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap) {
+int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
   const int natom = b.natom;
   if (natom <= 0) return 0;
   const int grid = natom < grid_cap ? natom : grid_cap;
   const size_t s1 = abasis_smem<R>(m), s2 = density_smem<R>(m), s3 = forces_smem<R>(m, kForceThreads);
+  if (ev) cudaEventRecord(ev[0], st);
   cudaFuncSetAttribute(k_abasis<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1));
   k_abasis<R><<<grid, kAbasisThreads, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
                                                  reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+  if (ev) cudaEventRecord(ev[1], st);
   if (m.nd == 1) {
     cudaFuncSetAttribute(k_density<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
     k_density<R, 1><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
@@ -783,10 +785,12 @@ int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int
     k_density<R, 2><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
                                                        reinterpret_cast<C<R>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
   }
+  if (ev) cudaEventRecord(ev[2], st);
   cudaFuncSetAttribute(k_forces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s3));
   k_forces<R><<<grid, kForceThreads, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
                                                 reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
                                                 b.ti0, b.err);
+  if (ev) cudaEventRecord(ev[3], st);
   return 3;
 }
 
@@ -801,14 +805,14 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
   return forces_smem<float>(m, kForceThreads);
 }
 
-int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap) {
-  return launch_eval<double>(m, b, st, grid_cap);
+int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
+  return launch_eval<double>(m, b, st, grid_cap, ev);
 }
 
 }  // namespace magace
 
 namespace magace {
-int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap) {
-  return launch_eval<float>(m, b, st, grid_cap);
+int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
+  return launch_eval<float>(m, b, st, grid_cap, ev);
 }
 }  // namespace magace

@@ -41,8 +41,9 @@ struct EvalBuffers {
 
 void upload_ylm_constants(const double* alm, const double* blm, const double* cl, const double* dl);
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which);
-// returns the number of kernels launched
-int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap);
-int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap);
+// Launches k_abasis, k_density and k_forces on `st`; returns the number of
+// kernels launched. With `ev` (4 events) the kernel boundaries are recorded.
+int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
+int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
 
 }  // namespace magace

@@ -42,6 +42,9 @@ SIGNATURES = {
     "ace_device_status": (_i, []),
     "ace_last_launch_count": (_i, []),
     "ace_release_device": (None, []),
+    "ace_set_kernel_timing": (_i, [_i]),
+    "ace_kernel_times": (_i, [ctypes.POINTER(ctypes.c_float)]),
+    "ace_table_stats": (_i, [ctypes.POINTER(ctypes.c_longlong)]),
 }
 
 _lib = None
@@ -139,3 +142,22 @@ def device_status() -> None:
 
 def last_launch_count() -> int:
     return int(load().ace_last_launch_count())
+
+
+def set_kernel_timing(on: bool) -> None:
+    _check(load().ace_set_kernel_timing(1 if on else 0))
+
+
+def kernel_times() -> list:
+    """Per-kernel durations (ms) of the last evaluation: [k_abasis, k_density, k_forces]."""
+    out = (ctypes.c_float * 3)()
+    _check(load().ace_kernel_times(out))
+    return [float(x) for x in out]
+
+
+def table_stats() -> dict:
+    out = (ctypes.c_longlong * 21)()
+    _check(load().ace_table_stats(out))
+    keys = ["ne1", "ne2", "ne3", "nseg", "nslot", "nF", "nW", "nWA", "nA2h", "nfa", "nfm",
+            "nba", "nbm", "n2m", "l2m", "n3a", "n3m", "l3a", "l3m", "h2", "h3"]
+    return {k: int(v) for k, v in zip(keys, out)}
