@@ -187,7 +187,11 @@ def gpu_arm(args, rank, world, local_rank):
     out = {k: torch.empty(n, dtype=torch.float64, device=dev)
            for k, n in (("e", nb.natom), ("f", 3 * nb.nei), ("t", 3 * nb.nei), ("t0", 3 * nb.natom))}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
-    stream = torch.cuda.current_stream(dev).cuda_stream
+    # an explicit stream: the library treats a NULL stream as its own stream,
+    # so the kernels and the timing events must share a non-default stream
+    work_stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(work_stream)
+    stream = work_stream.cuda_stream
 
     def step():
         lib.compute_device(nb.natom, nb.nei, d_off.data_ptr(), d_r.data_ptr(), d_e.data_ptr(), d_mj.data_ptr(),

@@ -72,11 +72,13 @@ struct Runtime {
   bool dev_tables = false;
   int device = -1;
   cudaStream_t stream = nullptr;
-  DevBuf<double> lut_a, lut_m, c1, k1, k2, k3, slot_mult;
-  DevBuf<float> lut_a32, lut_m32, k1f, k2f, k3f;
-  DevBuf<uint16_t> o1, o2, o3;
-  DevBuf<SegmentInfo> seg;
-  DevBuf<int32_t> order, slot_seg, slot_factor, slot_weight;
+  DevBuf<double> lut_a, lut_m, c1, slot_mult;
+  DevBuf<double> kap[4];
+  DevBuf<float> lut_a32, lut_m32;
+  DevBuf<float> kapf[4];
+  DevBuf<uint32_t> o12[4];
+  DevBuf<uint16_t> o3;
+  DevBuf<int32_t> grp_arity, grp_len, grp_first, grp_seg, slot_seg, slot_factor, slot_weight;
   DeviceModel dm{};
   int grid_cap = 0;
 
@@ -154,25 +156,18 @@ int upload_tables() {
   for (int d = 0; d < 2; ++d)
     for (int n = 0; n < M.L.nbm; ++n) c1[d * M.L.nbm + n] = M.c1[d][n];
   CUDA_TRY(R.c1.upload(c1));
-  auto cat = [](const std::vector<double>* k) {
-    std::vector<double> v(k[0]);
-    v.insert(v.end(), k[1].begin(), k[1].end());
-    return v;
-  };
-  std::vector<double> k1 = cat(g.k1), k2 = cat(g.k2), k3 = cat(g.k3);
-  CUDA_TRY(R.k1.upload(k1));
-  CUDA_TRY(R.k2.upload(k2));
-  CUDA_TRY(R.k3.upload(k3));
-  CUDA_TRY(R.k1f.upload(to_float(k1)));
-  CUDA_TRY(R.k2f.upload(to_float(k2)));
-  CUDA_TRY(R.k3f.upload(to_float(k3)));
-  CUDA_TRY(R.o1.upload(g.o1));
-  CUDA_TRY(R.o2.upload(g.o2));
+  for (int a = 1; a <= 3; ++a) {
+    std::vector<double> k(g.kap[a][0]);
+    k.insert(k.end(), g.kap[a][1].begin(), g.kap[a][1].end());
+    CUDA_TRY(R.kap[a].upload(k));
+    CUDA_TRY(R.kapf[a].upload(to_float(k)));
+    CUDA_TRY(R.o12[a].upload(g.o12[a]));
+  }
   CUDA_TRY(R.o3.upload(g.o3));
-  std::vector<SegmentInfo> seg(g.seg_slot.size());
-  for (size_t s = 0; s < seg.size(); ++s) seg[s] = {g.seg_arity[s], g.seg_first[s], g.seg_count[s], g.seg_slot[s]};
-  CUDA_TRY(R.seg.upload(seg));
-  CUDA_TRY(R.order.upload(g.order));
+  CUDA_TRY(R.grp_arity.upload(g.grp_arity));
+  CUDA_TRY(R.grp_len.upload(g.grp_len));
+  CUDA_TRY(R.grp_first.upload(g.grp_first));
+  CUDA_TRY(R.grp_seg.upload(g.grp_seg));
   CUDA_TRY(R.slot_seg.upload(g.slot_seg_begin));
   CUDA_TRY(R.slot_factor.upload(g.slot_factor));
   CUDA_TRY(R.slot_weight.upload(g.slot_weight));
@@ -206,15 +201,23 @@ int upload_tables() {
   d.c1 = R.c1.p;
   d.nslot = g.nslot;
   d.nG0 = g.nG0;
-  d.nseg = static_cast<int>(g.seg_slot.size());
-  d.ne1 = static_cast<int>(g.k1[0].size());
-  d.ne2 = static_cast<int>(g.k2[0].size());
-  d.ne3 = static_cast<int>(g.k3[0].size());
-  d.k1 = R.k1.p; d.k2 = R.k2.p; d.k3 = R.k3.p;
-  d.k1f = R.k1f.p; d.k2f = R.k2f.p; d.k3f = R.k3f.p;
-  d.o1 = R.o1.p; d.o2 = R.o2.p; d.o3 = R.o3.p;
-  d.seg = R.seg.p;
-  d.order = R.order.p;
+  d.nseg = g.nseg;
+  d.ngroup = g.ngroup;
+  d.grp_arity = R.grp_arity.p;
+  d.grp_len = R.grp_len.p;
+  d.grp_first = R.grp_first.p;
+  d.grp_seg = R.grp_seg.p;
+  d.kap[0] = nullptr;
+  d.kapf[0] = nullptr;
+  d.o12[0] = nullptr;
+  d.kstride[0] = 0;
+  for (int a = 1; a <= 3; ++a) {
+    d.kap[a] = R.kap[a].p;
+    d.kapf[a] = R.kapf[a].p;
+    d.o12[a] = R.o12[a].p;
+    d.kstride[a] = static_cast<int>(g.kap[a][0].size());
+  }
+  d.o3 = R.o3.p;
   d.slot_seg = R.slot_seg.p;
   d.slot_factor = R.slot_factor.p;
   d.slot_weight = R.slot_weight.p;
@@ -411,10 +414,10 @@ int ace_table_stats(long long* out) {
   if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
   const GatherTable& g = R.model.gt;
   const FactorLayout& L = R.model.L;
-  out[0] = static_cast<long long>(g.k1[0].size());
-  out[1] = static_cast<long long>(g.k2[0].size());
-  out[2] = static_cast<long long>(g.k3[0].size());
-  out[3] = static_cast<long long>(g.seg_slot.size());
+  out[0] = g.entries[1];
+  out[1] = g.entries[2];
+  out[2] = g.entries[3];
+  out[3] = g.nseg;
   out[4] = g.nslot;
   out[5] = L.nF;
   out[6] = L.nW;
@@ -465,13 +468,18 @@ int ace_device_status(void) {
 
 void ace_release_device(void) {
   Runtime& R = rt();
-  for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.k1, &R.k2, &R.k3, &R.slot_mult, &R.r, &R.e, &R.magj, &R.mhj,
-                  &R.magi, &R.mhi, &R.energy, &R.fij, &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
+  for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.slot_mult, &R.r, &R.e, &R.magj, &R.mhj, &R.magi, &R.mhi,
+                  &R.energy, &R.fij, &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
     b->release();
-  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.k1f, &R.k2f, &R.k3f}) b->release();
-  for (auto* b : {&R.o1, &R.o2, &R.o3}) b->release();
-  for (auto* b : {&R.order, &R.slot_seg, &R.slot_factor, &R.slot_weight}) b->release();
-  R.seg.release();
+  for (int a = 0; a < 4; ++a) {
+    R.kap[a].release();
+    R.kapf[a].release();
+    R.o12[a].release();
+  }
+  for (auto* b : {&R.lut_a32, &R.lut_m32}) b->release();
+  R.o3.release();
+  for (auto* b : {&R.grp_arity, &R.grp_len, &R.grp_first, &R.grp_seg, &R.slot_seg, &R.slot_factor, &R.slot_weight})
+    b->release();
   R.off.release();
   R.err.release();
   R.F.release();

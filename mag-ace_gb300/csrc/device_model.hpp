@@ -20,13 +20,6 @@ enum DeviceError : int {
   kDevShape = 4,   // more bonds than a tile index can address
 };
 
-struct SegmentInfo {
-  int32_t arity;  // number of other factors (1..3)
-  int32_t first;  // first entry in the arity's arrays
-  int32_t count;  // entries in this segment
-  int32_t slot;   // output slot
-};
-
 struct DeviceModel {
   // basis dims (see model.hpp for the layouts)
   int n3a, n3m, l3a, l3m, nba, n2m, l2m, nbm;
@@ -45,21 +38,19 @@ struct DeviceModel {
   const float* lut_m32;
   // 1-body coefficients c1[d * nbm + n]
   const double* c1;
-  // gather table
-  int nslot, nG0, nseg;
-  int ne1, ne2, ne3;        // entries per arity (stride of the second density)
-  const double* k1;          // [nd][ne1]
-  const double* k2;
-  const double* k3;
-  const float* k1f;          // FP32 copies (split path)
-  const float* k2f;
-  const float* k3f;
-  const uint16_t* o1;        // [ne1]
-  const uint16_t* o2;        // [2*ne2]
-  const uint16_t* o3;        // [3*ne3]
-  const SegmentInfo* seg;    // [nseg]
-  const int32_t* order;      // [nseg] processing order
-  const int32_t* slot_seg;   // [nslot+1]
+  // gather table in warp groups (see model.hpp): group g has arity
+  // grp_arity[g], length grp_len[g] and its entries at grp_first[g] + e*32 + lane
+  int nslot, nG0, nseg, ngroup;
+  const int32_t* grp_arity;
+  const int32_t* grp_len;
+  const int32_t* grp_first;
+  const int32_t* grp_seg;      // [ngroup*32] segment id per lane, -1 padding
+  const double* kap[4];        // [arity][density * kstride[arity] + slot] FP64
+  const float* kapf[4];        // FP32 copies (split path)
+  int kstride[4];
+  const uint32_t* o12[4];      // o1 | o2 << 16
+  const uint16_t* o3;          // third factor of arity-3 entries
+  const int32_t* slot_seg;     // [nslot+1]
   const int32_t* slot_factor;  // [nslot] (G0 slots only)
   const int32_t* slot_weight;  // [nslot]
   const double* slot_mult;     // [nslot]

@@ -142,17 +142,39 @@ __device__ __forceinline__ C<R> y_full(const C<R>* Yh, int l, int m) {
 }
 
 // Cubic-Hermite lookup of `count` consecutive functions starting at `f0` of a
-// table with `nf` functions per bin (src/radial.F90:85-105).
-template <class R, bool GRAD>
+// table with `nf` functions per bin (src/radial.F90:85-105). FP64 tables for
+// the drop-in path, FP32 copies for the split path.
+template <bool GRAD>
 __device__ __forceinline__ void lut_eval(const double* __restrict__ lut, int nf, int f0, int count, int nl,
-                                         double wl, double rscale, R* v, R* dv) {
+                                         double wl, double rscale, double* v, double* dv) {
   const double wl2 = wl * wl, wl3 = wl2 * wl, w2 = 2.0 * wl, w3 = 3.0 * wl2;
   const double2* c2 = reinterpret_cast<const double2*>(lut) + 2 * (static_cast<size_t>(nl) * nf + f0);
   for (int f = 0; f < count; ++f) {
     const double2 a = __ldg(c2 + 2 * f), b = __ldg(c2 + 2 * f + 1);
-    v[f] = R(a.x + a.y * wl + b.x * wl2 + b.y * wl3);
-    if (GRAD) dv[f] = R((a.y + b.x * w2 + b.y * w3) * rscale);
+    v[f] = a.x + a.y * wl + b.x * wl2 + b.y * wl3;
+    if (GRAD) dv[f] = (a.y + b.x * w2 + b.y * w3) * rscale;
   }
+}
+template <bool GRAD>
+__device__ __forceinline__ void lut_eval(const float* __restrict__ lut, int nf, int f0, int count, int nl,
+                                         float wl, float rscale, float* v, float* dv) {
+  const float wl2 = wl * wl, wl3 = wl2 * wl, w2 = 2.0f * wl, w3 = 3.0f * wl2;
+  const float4* c4 = reinterpret_cast<const float4*>(lut) + static_cast<size_t>(nl) * nf + f0;
+  for (int f = 0; f < count; ++f) {
+    const float4 c = __ldg(c4 + f);
+    v[f] = c.x + c.y * wl + c.z * wl2 + c.w * wl3;
+    if (GRAD) dv[f] = (c.y + c.z * w2 + c.w * w3) * rscale;
+  }
+}
+template <class R>
+__device__ __forceinline__ const R* pick(const double* d, const float* f);
+template <>
+__device__ __forceinline__ const double* pick<double>(const double* d, const float*) {
+  return d;
+}
+template <>
+__device__ __forceinline__ const float* pick<float>(const double*, const float* f) {
+  return f;
 }
 
 // bins of the atomic table: returns false (features zero) beyond the cutoff
@@ -217,9 +239,9 @@ __global__ void __launch_bounds__(kAbasisThreads)
         double wl = 0.0;
         const int nla = atomic_bin(m, r, wl, err);
         if (nla > 0) {
-          lut_eval<R, false>(m.lut_a, m.nfa, 0, m.nba, nla, wl, m.rscale_a, g, dummy);
-          lut_eval<R, false>(m.lut_a, m.nfa, m.nba, m.n3a * (m.l3a + 1), nla, wl, m.rscale_a, Rv, dummy);
-          lut_eval<R, false>(m.lut_a, m.nfa, m.nba + m.n3a * (m.l3a + 1), 1, nla, wl, m.rscale_a, cv, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, 0, m.nba, nla, R(wl), R(m.rscale_a), g, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba, m.n3a * (m.l3a + 1), nla, R(wl), R(m.rscale_a), Rv, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba + m.n3a * (m.l3a + 1), 1, nla, R(wl), R(m.rscale_a), cv, dummy);
         } else {
           for (int q = 0; q < m.nba; ++q) g[q] = R(0);
           for (int q = 0; q < m.n3a * (m.l3a + 1); ++q) Rv[q] = R(0);
@@ -229,7 +251,7 @@ __global__ void __launch_bounds__(kAbasisThreads)
         const int nlm = magnetic_bin(m, magj[j], wm, err);
         const int nM = m.n2m * (m.l2m + 1);
         if (nlm > 0) {
-          lut_eval<R, false>(m.lut_m, m.nfm, 0, nM, nlm, wm, m.rscale_m, Mv, dummy);
+          lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nM, nlm, R(wm), R(m.rscale_m), Mv, dummy);
         } else {
           for (int q = 0; q < nM; ++q) Mv[q] = R(nlm == 0 ? 1 : 0);
         }
@@ -331,8 +353,8 @@ __global__ void __launch_bounds__(kAbasisThreads)
       R Mv[32], gm[32], dummy[1];
       const int nM = m.n2m * (m.l2m + 1);
       if (nl > 0) {
-        lut_eval<R, false>(m.lut_m, m.nfm, 0, nM, nl, wl, m.rscale_m, Mv, dummy);
-        lut_eval<R, false>(m.lut_m, m.nfm, nM, m.nbm, nl, wl, m.rscale_m, gm, dummy);
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nM, nl, R(wl), R(m.rscale_m), Mv, dummy);
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, nM, m.nbm, nl, R(wl), R(m.rscale_m), gm, dummy);
       } else {
         for (int q = 0; q < nM; ++q) Mv[q] = R(nl == 0 ? 1 : 0);
         for (int q = 0; q < m.nbm; ++q) gm[q] = R(nl == 0 ? 1 : 0);
@@ -385,8 +407,38 @@ __device__ void embed(int nfemb, double rho, double wpre, double mexp, double& F
 
 // ===========================================================================
 // k_density
+// One CTA per atom. Warps walk the warp groups of the gather table (lane l of
+// group g owns segment grp_seg[g*32+l]); each lane accumulates its segment's
+// entries kappa * prod F[o] into a partial sum. Slot totals then add a slot's
+// partials in segment order (compensated in FP32 for the split path), the
+// density is rho = rho1 + sum over A0 slots of Re(A0 * total) in FP64, and the
+// weights are dE/drho * multiplicity * total.
 // Shared memory: Fs[nF] (complex R), part[nseg][ND] (complex R),
-// tot[nslot][ND] (complex double).
+// tot[nslot][ND] (complex R, hi) and, for FP32, the low words.
+template <class R>
+__device__ __forceinline__ const R* kap_ptr(const DeviceModel& m, int a);
+template <>
+__device__ __forceinline__ const double* kap_ptr<double>(const DeviceModel& m, int a) {
+  return m.kap[a];
+}
+template <>
+__device__ __forceinline__ const float* kap_ptr<float>(const DeviceModel& m, int a) {
+  return m.kapf[a];
+}
+
+// running sum with an error term: exact for double, two-float for float
+template <class R>
+struct CSum {
+  R hi = R(0), lo = R(0);
+  __device__ __forceinline__ void add(R b) {
+    const R s = hi + b;
+    const R bb = s - hi;
+    lo += (hi - (s - bb)) + (b - bb);
+    hi = s;
+  }
+  __device__ __forceinline__ double value() const { return static_cast<double>(hi) + static_cast<double>(lo); }
+};
+
 template <class R, int ND>
 __global__ void __launch_bounds__(kDensityThreads)
     k_density(DeviceModel m, int natom, const C<R>* __restrict__ F, const double* __restrict__ rho1,
@@ -395,50 +447,58 @@ __global__ void __launch_bounds__(kDensityThreads)
   extern __shared__ __align__(16) unsigned char smem[];
   C<R>* Fs = reinterpret_cast<C<R>*>(smem);
   C<R>* part = Fs + ((m.nF + 1) & ~1);
-  C<double>* tot = reinterpret_cast<C<double>*>(part + ((m.nseg * ND + 1) & ~1));
+  C<R>* tot = part + ((m.nseg * ND + 1) & ~1);
   __shared__ double s_red[kDensityThreads / 32][ND];
   __shared__ double s_dE[ND];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
 
   for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
     const C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
     for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
     __syncthreads();
-    for (int i = threadIdx.x; i < m.nseg; i += blockDim.x) {
-      const int sid = m.order[i];
-      const SegmentInfo sg = m.seg[sid];
+    for (int g = warp; g < m.ngroup; g += nwarp) {
+      const int a = m.grp_arity[g], len = m.grp_len[g], base = m.grp_first[g] + lane;
+      const int seg = m.grp_seg[g * 32 + lane];
+      const R* kp = kap_ptr<R>(m, a) + base;
+      const uint32_t* op = m.o12[a] + base;
+      const int ks = m.kstride[a];
       C<R> acc[ND];
       for (int d = 0; d < ND; ++d) acc[d] = {R(0), R(0)};
-      const int e0 = sg.first, e1 = sg.first + sg.count;
-      if (sg.arity == 2) {
-        for (int e = e0; e < e1; ++e) {
-          const C<R> p = cmul(Fs[m.o2[2 * e]], Fs[m.o2[2 * e + 1]]);
+      if (a == 2) {
+#pragma unroll 4
+        for (int e = 0; e < len; ++e) {
+          const uint32_t o = __ldg(op + e * 32);
+          const C<R> p = cmul(Fs[o & 0xffffu], Fs[o >> 16]);
           for (int d = 0; d < ND; ++d) {
-            const R k = R(m.k2[d * m.ne2 + e]);
+            const R k = __ldg(kp + d * ks + e * 32);
             acc[d].x += k * p.x;
             acc[d].y += k * p.y;
           }
         }
-      } else if (sg.arity == 1) {
-        for (int e = e0; e < e1; ++e) {
-          const C<R> p = Fs[m.o1[e]];
+      } else if (a == 1) {
+        for (int e = 0; e < len; ++e) {
+          const uint32_t o = __ldg(op + e * 32);
+          const C<R> p = Fs[o & 0xffffu];
           for (int d = 0; d < ND; ++d) {
-            const R k = R(m.k1[d * m.ne1 + e]);
+            const R k = __ldg(kp + d * ks + e * 32);
             acc[d].x += k * p.x;
             acc[d].y += k * p.y;
           }
         }
       } else {
-        for (int e = e0; e < e1; ++e) {
-          const C<R> p = cmul(cmul(Fs[m.o3[3 * e]], Fs[m.o3[3 * e + 1]]), Fs[m.o3[3 * e + 2]]);
+        const uint16_t* o3p = m.o3 + base;
+        for (int e = 0; e < len; ++e) {
+          const uint32_t o = __ldg(op + e * 32);
+          const C<R> p = cmul(cmul(Fs[o & 0xffffu], Fs[o >> 16]), Fs[__ldg(o3p + e * 32)]);
           for (int d = 0; d < ND; ++d) {
-            const R k = R(m.k3[d * m.ne3 + e]);
+            const R k = __ldg(kp + d * ks + e * 32);
             acc[d].x += k * p.x;
             acc[d].y += k * p.y;
           }
         }
       }
-      for (int d = 0; d < ND; ++d) part[sid * ND + d] = acc[d];
+      if (seg >= 0)
+        for (int d = 0; d < ND; ++d) part[seg * ND + d] = acc[d];
     }
     __syncthreads();
     double rloc[ND];
@@ -446,15 +506,15 @@ __global__ void __launch_bounds__(kDensityThreads)
     for (int s = threadIdx.x; s < m.nslot; s += blockDim.x) {
       const int q0 = m.slot_seg[s], q1 = m.slot_seg[s + 1];
       for (int d = 0; d < ND; ++d) {
-        C<double> t = {0.0, 0.0};
+        CSum<R> tx, ty;
         for (int q = q0; q < q1; ++q) {
-          t.x += static_cast<double>(part[q * ND + d].x);
-          t.y += static_cast<double>(part[q * ND + d].y);
+          tx.add(part[q * ND + d].x);
+          ty.add(part[q * ND + d].y);
         }
-        tot[s * ND + d] = t;
+        tot[s * ND + d] = {tx.hi + tx.lo, ty.hi + ty.lo};
         if (s < m.nG0) {
           const C<R> f = Fs[m.slot_factor[s]];
-          rloc[d] += static_cast<double>(f.x) * t.x - static_cast<double>(f.y) * t.y;
+          rloc[d] += static_cast<double>(f.x) * tx.value() - static_cast<double>(f.y) * ty.value();
         }
       }
     }
@@ -503,13 +563,14 @@ __global__ void __launch_bounds__(kDensityThreads)
     for (int s = threadIdx.x; s < m.nslot; s += blockDim.x) {
       const int w = m.slot_weight[s];
       if (w < 0) continue;
-      C<double> v = {0.0, 0.0};
+      const R mu = R(m.slot_mult[s]);
+      C<R> v = {R(0), R(0)};
       for (int d = 0; d < ND; ++d) {
-        v.x += s_dE[d] * tot[s * ND + d].x;
-        v.y += s_dE[d] * tot[s * ND + d].y;
+        const R sc = mu * R(s_dE[d]);
+        v.x += sc * tot[s * ND + d].x;
+        v.y += sc * tot[s * ND + d].y;
       }
-      const double mu = m.slot_mult[s];
-      Wa[w] = {R(mu * v.x), R(mu * v.y)};
+      Wa[w] = v;
     }
     __syncthreads();
   }
@@ -555,22 +616,23 @@ __global__ void __launch_bounds__(kForceThreads)
       const double mx = mhj[3 * j], my = mhj[3 * j + 1], mz = mhj[3 * j + 2];
       // radial features with derivatives
       R tmpv[32], tmpd[32];
-      double wl = 0.0, cd = 0.0;
+      double wl = 0.0;
+      R cd = R(0);
       const int nla = atomic_bin(m, r, wl, err);
       if (nla > 0) {
-        lut_eval<R, true>(m.lut_a, m.nfa, 0, m.nba, nla, wl, m.rscale_a, tmpv, tmpd);
+        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, 0, m.nba, nla, R(wl), R(m.rscale_a), tmpv, tmpd);
         for (int n = 0; n < m.nba; ++n) {
           cg[n * T + t] = tmpv[n];
           cgd[n * T + t] = tmpd[n];
         }
-        lut_eval<R, true>(m.lut_a, m.nfa, m.nba, nRl, nla, wl, m.rscale_a, tmpv, tmpd);
+        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba, nRl, nla, R(wl), R(m.rscale_a), tmpv, tmpd);
         for (int q = 0; q < nRl; ++q) {
           cR[q * T + t] = tmpv[q];
           cRd[q * T + t] = tmpd[q];
         }
         R cv[1], cdv[1];
-        lut_eval<R, true>(m.lut_a, m.nfa, m.nba + nRl, 1, nla, wl, m.rscale_a, cv, cdv);
-        cd = static_cast<double>(cdv[0]);
+        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba + nRl, 1, nla, R(wl), R(m.rscale_a), cv, cdv);
+        cd = cdv[0];
       } else {
         for (int n = 0; n < m.nba; ++n) cg[n * T + t] = cgd[n * T + t] = R(0);
         for (int q = 0; q < nRl; ++q) cR[q * T + t] = cRd[q * T + t] = R(0);
@@ -578,7 +640,7 @@ __global__ void __launch_bounds__(kForceThreads)
       double wm = 0.0;
       const int nlm = magnetic_bin(m, mg, wm, err);
       if (nlm > 0) {
-        lut_eval<R, true>(m.lut_m, m.nfm, 0, nMl, nlm, wm, m.rscale_m, tmpv, tmpd);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nMl, nlm, R(wm), R(m.rscale_m), tmpv, tmpd);
         for (int q = 0; q < nMl; ++q) {
           cM[q * T + t] = tmpv[q];
           cMd[q * T + t] = tmpd[q];
@@ -612,9 +674,9 @@ __global__ void __launch_bounds__(kForceThreads)
         }
       }
       // ---- force: dE_i / d(x_i - x_j)
-      double fr = edf * cd;  // radial (along e) part
-      double ft[3] = {0.0, 0.0, 0.0};
-      const double invr = 1.0 / r;
+      R fr = R(edf) * cd;  // radial (along e) part
+      R ft[3] = {R(0), R(0), R(0)};
+      const R invr = R(1.0 / r);
       // pair part: sum_n g'_n sum_{nr,h} Re(W2[n][nr][h] Q[nr][h])
       for (int nr = 0; nr < m.n2m; ++nr)
         for (int l = 0; l <= m.l2m; ++l) {
@@ -624,7 +686,7 @@ __global__ void __launch_bounds__(kForceThreads)
             const C<R> q = cscale(cYm[h * T + t], Ml);
             R s = R(0);
             for (int n = 0; n < m.nba; ++n) s += cgd[n * T + t] * re_mul(Ws[m.offW2 + (n * m.n2m + nr) * m.h2 + h], q);
-            fr += static_cast<double>(s);
+            fr += s;
           }
         }
       // many-body part via U[n1][lma] = sum_{n2,h} WA Q
@@ -647,16 +709,16 @@ __global__ void __launch_bounds__(kForceThreads)
               }
             const R Rv = cR[(n1 * (m.l3a + 1) + l1) * T + t];
             const R Rd = cRd[(n1 * (m.l3a + 1) + l1) * T + t];
-            fr += static_cast<double>(Rd * re_mul(U, cY[lma * T + t]));
-            const R sc = R(invr) * Rv;
-            for (int c = 0; c < 3; ++c) ft[c] += static_cast<double>(sc * re_mul(U, cdY[(lma * 3 + c) * T + t]));
+            fr += Rd * re_mul(U, cY[lma * T + t]);
+            const R sc = invr * Rv;
+            for (int c = 0; c < 3; ++c) ft[c] += sc * re_mul(U, cdY[(lma * 3 + c) * T + t]);
           }
-      fij[3 * static_cast<size_t>(j) + 0] = fr * ex + ft[0];
-      fij[3 * static_cast<size_t>(j) + 1] = fr * ey + ft[1];
-      fij[3 * static_cast<size_t>(j) + 2] = fr * ez + ft[2];
+      fij[3 * static_cast<size_t>(j) + 0] = static_cast<double>(fr * R(ex) + ft[0]);
+      fij[3 * static_cast<size_t>(j) + 1] = static_cast<double>(fr * R(ey) + ft[1]);
+      fij[3 * static_cast<size_t>(j) + 2] = static_cast<double>(fr * R(ez) + ft[2]);
       // ---- magnetic force: dE_i / dm_j
-      double tr = 0.0, tt[3] = {0.0, 0.0, 0.0};
-      const double invm = 1.0 / mg;
+      R tr = R(0), tt[3] = {R(0), R(0), R(0)};
+      const R invm = R(1.0 / mg);
       for (int nr = 0; nr < m.n2m; ++nr)
         for (int l = 0; l <= m.l2m; ++l)
           for (int mm = 0; mm <= l; ++mm) {
@@ -682,13 +744,13 @@ __global__ void __launch_bounds__(kForceThreads)
                 }
             }
             const int q = nr * (m.l2m + 1) + l;
-            tr += static_cast<double>(cMd[q * T + t] * re_mul(V, cYm[h * T + t]));
-            const R sc = R(invm) * cM[q * T + t];
-            for (int c = 0; c < 3; ++c) tt[c] += static_cast<double>(sc * re_mul(V, cdYm[(h * 3 + c) * T + t]));
+            tr += cMd[q * T + t] * re_mul(V, cYm[h * T + t]);
+            const R sc = invm * cM[q * T + t];
+            for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(V, cdYm[(h * 3 + c) * T + t]);
           }
-      tij[3 * static_cast<size_t>(j) + 0] = tr * mx + tt[0];
-      tij[3 * static_cast<size_t>(j) + 1] = tr * my + tt[1];
-      tij[3 * static_cast<size_t>(j) + 2] = tr * mz + tt[2];
+      tij[3 * static_cast<size_t>(j) + 0] = static_cast<double>(tr * R(mx) + tt[0]);
+      tij[3 * static_cast<size_t>(j) + 1] = static_cast<double>(tr * R(my) + tt[1]);
+      tij[3 * static_cast<size_t>(j) + 2] = static_cast<double>(tr * R(mz) + tt[2]);
     }
     if (t == 0) {
       // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749)
@@ -698,8 +760,8 @@ __global__ void __launch_bounds__(kForceThreads)
       const int nl = magnetic_bin(m, mg, wm, err);
       R Mv[32], Md[32], gm[32], gmd[32];
       if (nl > 0) {
-        lut_eval<R, true>(m.lut_m, m.nfm, 0, nMl, nl, wm, m.rscale_m, Mv, Md);
-        lut_eval<R, true>(m.lut_m, m.nfm, nMl, m.nbm, nl, wm, m.rscale_m, gm, gmd);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nMl, nl, R(wm), R(m.rscale_m), Mv, Md);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, nMl, m.nbm, nl, R(wm), R(m.rscale_m), gm, gmd);
       } else {
         for (int q = 0; q < nMl; ++q) {
           Mv[q] = R(nl == 0 ? 1 : 0);
@@ -754,8 +816,8 @@ size_t abasis_smem(const DeviceModel& m) {
 
 template <class R>
 size_t density_smem(const DeviceModel& m) {
-  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((m.nseg * m.nd + 1) & ~1)) +
-         sizeof(C<double>) * static_cast<size_t>(m.nslot) * m.nd + 64;
+  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((m.nseg * m.nd + 1) & ~1) +
+                         static_cast<size_t>(m.nslot) * m.nd) + 64;
 }
 
 template <class R>

@@ -461,42 +461,68 @@ int build_gather(Model& M, std::string& msg) {
   }
   for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
 
-  // flatten into segments
+  // flatten into segments, then pack segments into warp groups
   GatherTable& g = M.gt;
   g = GatherTable();
   g.nG0 = L.n2m * L.ls2;
   g.nslot = sink.nslot;
   g.slot_seg_begin.assign(g.nslot + 1, 0);
+  struct Seg {
+    int arity, slot;
+    const Entry* e;
+    int count;
+  };
+  std::vector<Seg> segs;
   for (int s = 0; s < g.nslot; ++s) {
-    g.slot_seg_begin[s] = static_cast<int32_t>(g.seg_slot.size());
+    g.slot_seg_begin[s] = static_cast<int32_t>(segs.size());
     for (int a = 1; a <= 3; ++a) {
       const auto& es = sink.by_slot[a][s];
+      g.entries[a] += static_cast<long>(es.size());
       for (size_t e0 = 0; e0 < es.size(); e0 += GatherTable::kSegLen) {
-        size_t cnt = std::min(es.size() - e0, static_cast<size_t>(GatherTable::kSegLen));
-        std::vector<double>* kk = a == 1 ? g.k1 : (a == 2 ? g.k2 : g.k3);
-        std::vector<uint16_t>& oo = a == 1 ? g.o1 : (a == 2 ? g.o2 : g.o3);
-        g.seg_arity.push_back(a);
-        g.seg_first.push_back(static_cast<int32_t>(kk[0].size()));
-        g.seg_count.push_back(static_cast<int32_t>(cnt));
-        g.seg_slot.push_back(s);
-        for (size_t e = e0; e < e0 + cnt; ++e) {
-          kk[0].push_back(es[e].kappa[0]);
-          kk[1].push_back(es[e].kappa[1]);
-          for (int q = 0; q < a; ++q) oo.push_back(es[e].o[q]);
-        }
+        int cnt = static_cast<int>(std::min(es.size() - e0, static_cast<size_t>(GatherTable::kSegLen)));
+        segs.push_back({a, s, es.data() + e0, cnt});
       }
     }
   }
-  g.slot_seg_begin[g.nslot] = static_cast<int32_t>(g.seg_slot.size());
-  // process long, high-arity segments first so warps see similar work
-  const int nseg = static_cast<int>(g.seg_slot.size());
-  g.order.resize(nseg);
-  for (int s = 0; s < nseg; ++s) g.order[s] = s;
-  std::stable_sort(g.order.begin(), g.order.end(), [&](int a, int b) {
-    long wa = static_cast<long>(g.seg_count[a]) * (g.seg_arity[a] + 1);
-    long wb = static_cast<long>(g.seg_count[b]) * (g.seg_arity[b] + 1);
-    return wa > wb;
+  g.slot_seg_begin[g.nslot] = static_cast<int32_t>(segs.size());
+  g.nseg = static_cast<int>(segs.size());
+  g.seg_slot.resize(g.nseg);
+  for (int i = 0; i < g.nseg; ++i) g.seg_slot[i] = segs[i].slot;
+  std::vector<int> order(g.nseg);
+  for (int i = 0; i < g.nseg; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (segs[a].arity != segs[b].arity) return segs[a].arity > segs[b].arity;
+    return segs[a].count > segs[b].count;
   });
+  const int W = GatherTable::kLanes;
+  for (size_t i = 0; i < order.size();) {
+    const int a = segs[order[i]].arity;
+    size_t j = i;
+    while (j < order.size() && j - i < static_cast<size_t>(W) && segs[order[j]].arity == a) ++j;
+    const int len = segs[order[i]].count;  // sorted descending
+    g.grp_arity.push_back(a);
+    g.grp_len.push_back(len);
+    g.grp_first.push_back(static_cast<int32_t>(g.o12[a].size()));
+    for (int lane = 0; lane < W; ++lane) g.grp_seg.push_back(i + lane < j ? order[i + lane] : -1);
+    for (int e = 0; e < len; ++e)
+      for (int lane = 0; lane < W; ++lane) {
+        const Seg* sg = (i + lane < j) ? &segs[order[i + lane]] : nullptr;
+        if (sg && e < sg->count) {
+          const Entry& en = sg->e[e];
+          g.kap[a][0].push_back(en.kappa[0]);
+          g.kap[a][1].push_back(en.kappa[1]);
+          g.o12[a].push_back(static_cast<uint32_t>(en.o[0]) | (static_cast<uint32_t>(a >= 2 ? en.o[1] : 0) << 16));
+          if (a == 3) g.o3.push_back(en.o[2]);
+        } else {
+          g.kap[a][0].push_back(0.0);
+          g.kap[a][1].push_back(0.0);
+          g.o12[a].push_back(static_cast<uint32_t>(L.offZero) | (static_cast<uint32_t>(L.offZero) << 16));
+          if (a == 3) g.o3.push_back(static_cast<uint16_t>(L.offZero));
+        }
+      }
+    i = j;
+  }
+  g.ngroup = static_cast<int>(g.grp_arity.size());
   // slot -> weight mapping and multiplicity
   g.slot_factor.assign(g.nslot, -1);
   g.slot_weight.assign(g.nslot, -1);

@@ -47,18 +47,30 @@ struct Entry {
 // Device-ready gather table. Entries are grouped by output slot and cut into
 // segments of at most kSegLen entries of one arity. Output slots are
 //   [0, nG0)            one per A0 factor (all m): rho and W0
-//   [nG0, nG0+nW)       WA then W2 slots (index into the weight array - nG0 shifted)
+//   [nG0, nslot)        WA then W2 weight slots
+// Segments of one slot have consecutive ids (slot_seg_begin). For the device,
+// segments are packed 32 at a time into warp groups of one arity, sorted by
+// length, and their entries interleaved so that entry e of lane l of group g
+// sits at grp_first[g] + e*32 + l: one warp-wide load per entry is fully
+// coalesced. Short segments are padded with kappa = 0 entries that point at
+// the ZERO factor.
 struct GatherTable {
   static const int kSegLen = 64;
-  int nslot = 0;  // nG0 + nWA + nW2
+  static const int kLanes = 32;
+  int nslot = 0;
   int nG0 = 0;
-  // entries by arity (1, 2, 3 other factors)
-  std::vector<double> k1[2], k2[2], k3[2];
-  std::vector<uint16_t> o1, o2, o3;  // o1: 1 per entry, o2: 2, o3: 3
-  // segments: arity, first entry (within its arity array), count, slot
-  std::vector<int32_t> seg_arity, seg_first, seg_count, seg_slot;
-  std::vector<int32_t> slot_seg_begin;  // [nslot+1] segments of slot s are contiguous
-  std::vector<int32_t> order;           // processing order of segments (balanced)
+  int nseg = 0;
+  std::vector<int32_t> seg_slot;        // [nseg]
+  std::vector<int32_t> slot_seg_begin;  // [nslot+1]
+  int ngroup = 0;
+  std::vector<int32_t> grp_arity, grp_len, grp_first;  // [ngroup]
+  std::vector<int32_t> grp_seg;         // [ngroup*32], -1 for padding lanes
+  // interleaved entries per arity (index 1..3): kappa per density, packed
+  // factor indices o1 | o2 << 16, and the third index for arity 3
+  std::vector<double> kap[4][2];
+  std::vector<uint32_t> o12[4];
+  std::vector<uint16_t> o3;
+  long entries[4] = {0, 0, 0, 0};       // real (unpadded) entries per arity
   // slot -> factor/weight index and multiplicity
   std::vector<int32_t> slot_factor;  // for G0 slots: A0 factor index
   std::vector<int32_t> slot_weight;  // weight index (or -1 when the slot stores no weight)

@@ -172,14 +172,32 @@ def test_device_api_matches_acelib(gpu_lib):
     fij = torch.empty(3 * nb.nei, dtype=torch.float64, device=dev)
     tij = torch.empty_like(fij)
     ti0 = torch.empty(3 * nb.natom, dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream().cuda_stream
+    st = torch.cuda.Stream()
+    stream = st.cuda_stream
     gpu_lib.compute_device(nb.natom, nb.nei, off.data_ptr(), r.data_ptr(), ee.data_ptr(), mj.data_ptr(),
                            mhj.data_ptr(), mi.data_ptr(), mhi.data_ptr(), en.data_ptr(), fij.data_ptr(),
                            tij.data_ptr(), ti0.data_ptr(), stream)
-    torch.cuda.synchronize()
+    st.synchronize()
     gpu_lib.device_status()
     assert np.array_equal(en.cpu().numpy(), e)
     assert np.array_equal(fij.cpu().numpy(), f)
     assert np.array_equal(tij.cpu().numpy(), t)
     assert np.array_equal(ti0.cpu().numpy(), t0)
     assert gpu_lib.last_launch_count() == 3
+
+
+def test_split_precision_accuracy(gpu_lib, oracle_seeded):
+    """The split path (FP32 features, products and weights; FP64 density,
+    energy and embedding) stays within 1 meV/atom and 10 meV/A of the FP64
+    oracle on the 128-atom cell."""
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_128(1), 5.0)
+    gpu_lib.set_precision(1)
+    try:
+        e, f, t, t0 = gpu_lib.acelib(nb)
+    finally:
+        gpu_lib.set_precision(0)
+    eo, fo, to, t0o = oracle_seeded.acelib(nb)
+    assert np.abs(e - eo).max() * 1e3 < 1.0
+    assert np.abs(f - fo).max() * 1e3 < 10.0
+    assert np.abs(t - to).max() * 1e3 < 10.0 and np.abs(t0 - t0o).max() * 1e3 < 10.0
