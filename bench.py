@@ -190,6 +190,7 @@ def gpu_arm(args, rank, world, local_rank):
     # an explicit stream: the library treats a NULL stream as its own stream,
     # so the kernels and the timing events must share a non-default stream
     work_stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize()
     torch.cuda.set_stream(work_stream)
     stream = work_stream.cuda_stream
 

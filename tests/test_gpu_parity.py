@@ -173,6 +173,7 @@ def test_device_api_matches_acelib(gpu_lib):
     tij = torch.empty_like(fij)
     ti0 = torch.empty(3 * nb.natom, dtype=torch.float64, device=dev)
     st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
     stream = st.cuda_stream
     gpu_lib.compute_device(nb.natom, nb.nei, off.data_ptr(), r.data_ptr(), ee.data_ptr(), mj.data_ptr(),
                            mhj.data_ptr(), mi.data_ptr(), mhi.data_ptr(), en.data_ptr(), fij.data_ptr(),
