@@ -129,6 +129,25 @@ int ace_kernel_times(float* ms);
  * (21 entries). */
 int ace_table_stats(long long* out);
 
+/* Allocation-free variant of ace_compute_device, for callers that cannot
+ * allocate device memory when they evaluate (an allocator they do not own,
+ * MD drivers that forbid allocation after set-up). It has no counterpart in
+ * the reference. Same arguments and results as ace_compute_device, but it
+ * calls no cudaMalloc/cudaFree or allocating routine: its per-atom scratch
+ * lives in one fixed 64 MiB device array that every GPU loading the library
+ * holds until exit, which bounds natom (about 2000 atoms in FP64 and 4000 in
+ * the split precision for the example Fe basis); larger calls are refused
+ * with MAGACE_ERR_ARGS. The potential's tables must already be on the device
+ * (placed by any ace_compute_device call; natom = 0 is enough). The first call
+ * on each device looks up the scratch address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. Calls share the scratch, so
+ * calls that overlap on the GPU race. The call returns after the evaluation
+ * has completed, with this call's device-side status. */
+int ace_compute_device_noalloc(int natom, int nei, const int* bond_offset, const double* r,
+                               const double* e, const double* mag_j, const double* mhat_j,
+                               const double* mag_i, const double* mhat_i, double* energy,
+                               double* fij, double* tij, double* ti0, void* stream);
+
 /* Releases every device buffer held by the library (tables stay on the host). */
 void ace_release_device(void);
 

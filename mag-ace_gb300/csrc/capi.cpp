@@ -310,6 +310,32 @@ int init_file(const char* path, const char* element, double rcut, double rcut_ma
 }
 
 }  // namespace
+
+// Read-only view of the runtime for the allocation-free entry point
+// (noalloc.cu): the device model of the current device, if its tables are
+// already resident there, and the selected precision.
+int runtime_snapshot(DeviceModel* dm, int* precision, int* grid_cap) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  if (!R.dev_tables || R.device != dev)
+    return set_error(MAGACE_ERR_NOT_INIT,
+                     "the potential's tables are not on this device yet; an ace_compute_device call "
+                     "(natom = 0 is enough) places them");
+  *dm = R.dm;
+  *precision = R.precision;
+  *grid_cap = R.grid_cap;
+  return MAGACE_OK;
+}
+
+int runtime_error(int code, const char* msg) { return set_error(code, msg); }
+
+int runtime_device_error(int dev_err) { return dev_err ? device_error_to_status(dev_err) : set_error(MAGACE_OK, ""); }
+
+void runtime_set_launches(int n) { rt().last_launches = n; }
+
 }  // namespace magace
 
 using namespace magace;

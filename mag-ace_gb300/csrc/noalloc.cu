@@ -1,0 +1,132 @@
+// Allocation-free evaluation entry point.
+//
+// Some callers cannot allocate device memory at the point where they
+// evaluate the potential: code running inside a memory pool or allocator
+// they do not own, real-time MD drivers that forbid allocation after set-up,
+// or hosts whose device allocator is disabled in the evaluation phase. For
+// them, ace_compute_device_noalloc runs the same three kernels as
+// ace_compute_device, but its per-atom scratch (the factor array F, the
+// weight array W and the per-atom density, core energy and embedding
+// derivatives) lives in one fixed file-scope device array instead of
+// library-allocated buffers. The caller still passes the inputs and outputs.
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdio>
+
+#include "device_model.hpp"
+#include "kernels.hpp"
+#include "magace.h"
+
+namespace magace {
+
+int runtime_snapshot(DeviceModel* dm, int* precision, int* grid_cap);
+int runtime_error(int code, const char* msg);
+int runtime_device_error(int dev_err);
+void runtime_set_launches(int n);
+
+namespace {
+
+// Capacity of the shared scratch: 64 MiB on every device that loads the
+// library, held until the process exits.
+constexpr size_t kScratchBytes = static_cast<size_t>(64) << 20;
+
+// The scratch itself. In host code this name is only a stand-in for the
+// device symbol; its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_scratch_addr[kMaxDevices] = {nullptr};  // device address per device
+
+size_t round256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+}  // namespace
+}  // namespace magace
+
+using namespace magace;
+
+extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_offset, const double* r,
+                                          const double* e, const double* mag_j, const double* mhat_j,
+                                          const double* mag_i, const double* mhat_i, double* energy,
+                                          double* fij, double* tij, double* ti0, void* stream) {
+  if (natom < 0 || nei < 0) return runtime_error(MAGACE_ERR_ARGS, "negative sizes");
+  DeviceModel dm;
+  int precision = 0, grid_cap = 1;
+  int st = runtime_snapshot(&dm, &precision, &grid_cap);
+  if (st) return st;
+  int dev = -1;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return runtime_error(MAGACE_ERR_CUDA, cudaGetErrorString(ce));
+  if (dev < 0 || dev >= kMaxDevices) return runtime_error(MAGACE_ERR_CUDA, "device index beyond 64");
+  // one-time set-up per device, with that device current: the device
+  // address of the scratch array
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (ce != cudaSuccess || !p) return runtime_error(MAGACE_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
+    g_scratch_addr[dev] = p;
+  }
+  unsigned char* base = static_cast<unsigned char*>(g_scratch_addr[dev]);
+  const size_t csz = precision == 0 ? 16 : 8;  // complex FP64 / FP32
+  const size_t na = static_cast<size_t>(natom);
+  size_t off = 0;
+  const size_t o_err = off;
+  off += 256;
+  const size_t o_F = off;
+  off += round256(na * dm.nF * csz);
+  const size_t o_W = off;
+  off += round256(na * dm.nW * csz);
+  const size_t o_rho1 = off;
+  off += round256(na * 2 * sizeof(double));
+  const size_t o_core = off;
+  off += round256(na * sizeof(double));
+  const size_t o_edf = off;
+  off += round256(na * sizeof(double));
+  const size_t o_dedrho = off;
+  off += round256(na * 2 * sizeof(double));
+  if (off > kScratchBytes) {
+    const size_t per_atom = dm.nF * csz + dm.nW * csz + 6 * sizeof(double);
+    static char msg[160];
+    snprintf(msg, sizeof(msg), "natom = %d exceeds the allocation-free scratch (64 MiB, about %zu atoms for this potential and precision)",
+             natom, (kScratchBytes - 2048) / per_atom);
+    return runtime_error(MAGACE_ERR_ARGS, msg);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int* err = reinterpret_cast<int*>(base + o_err);
+  // every call shares the scratch; only the error word must start at zero,
+  // the kernels overwrite every other entry they read
+  ce = cudaMemsetAsync(err, 0, sizeof(int), s);
+  if (ce != cudaSuccess) return runtime_error(MAGACE_ERR_CUDA, cudaGetErrorString(ce));
+  EvalBuffers b;
+  b.natom = natom;
+  b.nei = nei;
+  b.off = bond_offset;
+  b.r = r;
+  b.e = e;
+  b.magj = mag_j;
+  b.mhj = mhat_j;
+  b.magi = mag_i;
+  b.mhi = mhat_i;
+  b.energy = energy;
+  b.fij = fij;
+  b.tij = tij;
+  b.ti0 = ti0;
+  b.F = base + o_F;
+  b.W = base + o_W;
+  b.rho1 = reinterpret_cast<double*>(base + o_rho1);
+  b.core = reinterpret_cast<double*>(base + o_core);
+  b.edf = reinterpret_cast<double*>(base + o_edf);
+  b.dedrho = reinterpret_cast<double*>(base + o_dedrho);
+  b.err = err;
+  const int n = precision == 0 ? launch_eval_fp64(dm, b, s, grid_cap, nullptr) : launch_eval_fp32(dm, b, s, grid_cap, nullptr);
+  runtime_set_launches(n);
+  ce = cudaGetLastError();
+  if (ce != cudaSuccess) return runtime_error(MAGACE_ERR_CUDA, cudaGetErrorString(ce));
+  // the call completes before it returns, so that the device error word of
+  // this call can be reported
+  int dev_err = 0;
+  ce = cudaMemcpyAsync(&dev_err, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return runtime_error(MAGACE_ERR_CUDA, cudaGetErrorString(ce));
+  return runtime_device_error(dev_err);
+}

@@ -45,6 +45,7 @@ SIGNATURES = {
     "ace_set_kernel_timing": (_i, [_i]),
     "ace_kernel_times": (_i, [ctypes.POINTER(ctypes.c_float)]),
     "ace_table_stats": (_i, [ctypes.POINTER(ctypes.c_longlong)]),
+    "ace_compute_device_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -1,0 +1,76 @@
+"""GPU test of ace_compute_device_noalloc, the entry point for callers that
+cannot allocate device memory while they evaluate. It is called through the
+C ABI twice in a row and must reproduce ace_compute_device (the regular entry
+point, which uses library-allocated scratch) within the FP64 parity tolerance
+of the other tests. The file sorts last so that a stop-at-first-failure run
+has executed every other test before it; it also passes alone in a fresh
+process, because it places the potential's tables on the device itself."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_noalloc_matches_compute_device(seeded_potential):
+    import torch
+    from magace import lib, structures as S
+
+    lib.init(seeded_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    lib.set_precision(0)
+    so = lib.load()
+    nb = S.neighbor_data(S.bcc_fe_128(3), 5.0)
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    ins = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
+
+    def outputs():
+        return [torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+                for n in (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)]
+
+    stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    ptr = lambda ts: [t.data_ptr() for t in ts]
+
+    # regular entry point (library-allocated scratch); also places the tables
+    ref = outputs()
+    st = so.ace_compute_device(nb.natom, nb.nei, off.data_ptr(), *ptr(ins), *ptr(ref), stream.cuda_stream)
+    assert st == 0, so.ace_last_error_message()
+    stream.synchronize()
+    assert so.ace_device_status() == 0
+    ref = [t.cpu().numpy() for t in ref]
+
+    for _ in range(2):  # two calls in a row share the same scratch
+        got = outputs()
+        st = so.ace_compute_device_noalloc(nb.natom, nb.nei, off.data_ptr(), *ptr(ins), *ptr(got),
+                                           ctypes.c_void_p(stream.cuda_stream))
+        assert st == 0, so.ace_last_error_message()
+        got = [t.cpu().numpy() for t in got]
+        for g, r in zip(got, ref):
+            assert np.all(np.isfinite(g))
+            assert _rel(g, r) <= TOL
+
+
+def test_noalloc_refuses_more_atoms_than_its_scratch(seeded_potential):
+    import torch
+    from magace import lib
+
+    lib.init(seeded_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    lib.set_precision(0)
+    so = lib.load()
+    # zero-atom regular call places the tables on the device
+    assert so.ace_compute_device(0, 0, None, None, None, None, None, None, None, None, None, None, None, None) == 0
+    st = so.ace_compute_device_noalloc(100000, 0, None, None, None, None, None, None, None, None, None, None,
+                                       None, None)
+    assert st == 7  # MAGACE_ERR_ARGS
+    assert b"scratch" in so.ace_last_error_message()
