@@ -257,17 +257,23 @@ def gpu_arm(args, rank, world, local_rank):
         ms = float(t.item())
     value = world * nb.natom / (ms / 1e3)
 
-    # end-to-end through the drop-in acelib_ with host arrays
+    # end-to-end through the drop-in acelib_ with host arrays, for each way of
+    # reaching host memory; "auto" is the library default
     lib.set_precision(0 if headline == "fp64" else 1)
     lib.set_kernel_timing(False)
-    for _ in range(max(1, args.warmup)):
-        lib.acelib(nb)
-    e2e_t = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        lib.acelib(nb)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_s = float(np.mean(e2e_t))
+    e2e_modes = {}
+    for mode in ("copy", "pinned", "auto"):
+        os.environ["MAGACE_HOST_ACCESS"] = mode
+        for _ in range(max(1, args.warmup)):
+            lib.acelib(nb)
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            lib.acelib(nb)
+            ts.append(time.perf_counter() - t0)
+        e2e_modes[mode] = float(np.mean(ts))
+    os.environ.pop("MAGACE_HOST_ACCESS", None)
+    e2e_s = e2e_modes["auto"]
     if world > 1:
         t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -290,7 +296,8 @@ def gpu_arm(args, rank, world, local_rank):
         "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": headline,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * nb.natom / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "host_access": lib.host_access(),
+                "ms_per_call": {k: v * 1e3 for k, v in e2e_modes.items()}},
         "gpu_launches": 3 * args.steps,
         "roofline": {"bound": "fp64" if headline == "fp64" else "fp32", "kernel": names[dom],
                      "achieved": achieved, "peak": fp_peak, "unit": "TFLOP/s",

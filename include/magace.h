@@ -110,6 +110,14 @@ int ace_compute_device(int natom, int nei, const int* bond_offset, const double*
  * call; synchronises the library stream. */
 int ace_device_status(void);
 
+/* How acelib_ reaches the caller's host arrays on the current device:
+ * 0 = pageable copies, 1 = staged through pinned memory, 2 = the kernels read
+ * and write the caller's memory directly (the GPU uses the host page tables,
+ * as with NVLink-C2C on Grace). The environment variable MAGACE_HOST_ACCESS
+ * (copy | pinned | direct | auto) chooses; "auto" (default) takes 2 when the
+ * device supports it, else 1. Returns -1 when no tables could be placed. */
+int ace_host_access_mode(void);
+
 /* Number of kernel launches issued by the last evaluation call. */
 int ace_last_launch_count(void);
 

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -87,6 +88,12 @@ struct Runtime {
   DevBuf<double> r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0, rho1, core, edf, dedrho;
   DevBuf<unsigned char> F, W;
   std::vector<int> h_off;
+
+  // pinned staging for host transfers, and whether the GPU reads pageable
+  // host memory directly (Grace: NVLink-C2C with the host page tables)
+  unsigned char* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  int pageable_access = -1;  // -1 unknown, 0 no, 1 yes
 
   // optional kernel-boundary events of the last evaluation
   bool timing = false;
@@ -285,6 +292,41 @@ int device_error_to_status(int dev) {
   }
 }
 
+enum HostAccess { kHostCopy = 0, kHostPinned = 1, kHostDirect = 2 };
+
+// How acelib_ moves the caller's host arrays. MAGACE_HOST_ACCESS selects
+// "direct" (kernels read and write the caller's pageable memory, possible
+// when the GPU uses the host page tables, as on Grace with NVLink-C2C),
+// "pinned" (staged through a pinned buffer) or "copy" (plain pageable
+// copies); the default "auto" takes direct when available, else pinned.
+int host_access_mode() {
+  Runtime& R = rt();
+  if (R.pageable_access < 0) {
+    int a = 0, b = 0;
+    if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, R.device) != cudaSuccess) a = 0;
+    if (cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, R.device) != cudaSuccess) b = 0;
+    R.pageable_access = (a && b) ? 1 : 0;
+  }
+  const char* env = std::getenv("MAGACE_HOST_ACCESS");
+  const std::string m = env ? env : "auto";
+  if (m == "copy") return kHostCopy;
+  if (m == "pinned") return kHostPinned;
+  if (m == "direct" && R.pageable_access == 1) return kHostDirect;
+  return R.pageable_access == 1 ? kHostDirect : kHostPinned;
+}
+
+int reserve_pinned(size_t bytes) {
+  Runtime& R = rt();
+  if (bytes <= R.pinned_bytes && R.pinned) return MAGACE_OK;
+  if (R.pinned) cudaFreeHost(R.pinned);
+  R.pinned = nullptr;
+  R.pinned_bytes = 0;
+  size_t want = bytes + bytes / 4;
+  CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&R.pinned), want, cudaHostAllocDefault));
+  R.pinned_bytes = want;
+  return MAGACE_OK;
+}
+
 int init_file(const char* path, const char* element, double rcut, double rcut_magnetic, double smear,
               int xcnumber) {
   Runtime& R = rt();
@@ -422,6 +464,12 @@ int ace_basis_rows(int rank, int* out) {
 
 int ace_last_launch_count(void) { return rt().last_launches; }
 
+int ace_host_access_mode(void) {
+  int st = upload_tables();
+  if (st) return -1;
+  return host_access_mode();
+}
+
 int ace_set_kernel_timing(int on) {
   rt().timing = on != 0;
   return MAGACE_OK;
@@ -512,6 +560,9 @@ void ace_release_device(void) {
   R.W.release();
   if (R.stream) cudaStreamDestroy(R.stream);
   R.stream = nullptr;
+  if (R.pinned) cudaFreeHost(R.pinned);
+  R.pinned = nullptr;
+  R.pinned_bytes = 0;
   R.dev_tables = false;
 }
 
@@ -557,11 +608,6 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
   if (st) return fail(st, R.last_msg.c_str(), npacked);
   const size_t na = natom, nb = npacked;
   cudaStream_t s = R.stream;
-  auto res = [&](DevBuf<double>& b, size_t n) { return b.reserve(n) == cudaSuccess; };
-  if (!(res(R.r, nb) && res(R.e, 3 * nb) && res(R.magj, nb) && res(R.mhj, 3 * nb) && res(R.magi, na) &&
-        res(R.mhi, 3 * na) && res(R.fij, 3 * nb) && res(R.tij, 3 * nb) && res(R.ti0, 3 * na)) ||
-      R.off.reserve(na + 1) != cudaSuccess)
-    return fail(MAGACE_ERR_CUDA, "device allocation failed", npacked);
   // inputs; non-contiguous ranges are gathered into atom order first
   std::vector<double> gr, ge, gm, gmh;
   const double *pr = dlist, *pe = elist, *pm = dlist_mom, *pmh = elist_mom;
@@ -585,42 +631,97 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
     pm = gm.data();
     pmh = gmh.data();
   }
+  const int mode = host_access_mode();
   cudaError_t ce = cudaSuccess;
-  auto h2d = [&](void* d, const void* h, size_t bytes) {
-    if (ce == cudaSuccess && bytes) ce = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
-  };
-  h2d(R.off.p, off.data(), (na + 1) * sizeof(int));
-  h2d(R.r.p, pr, nb * sizeof(double));
-  h2d(R.e.p, pe, 3 * nb * sizeof(double));
-  h2d(R.magj.p, pm, nb * sizeof(double));
-  h2d(R.mhj.p, pmh, 3 * nb * sizeof(double));
-  h2d(R.magi.p, dlist_momi, na * sizeof(double));
-  h2d(R.mhi.p, elist_momi, 3 * na * sizeof(double));
-  if (ce != cudaSuccess) return fail(MAGACE_ERR_CUDA, cudaGetErrorString(ce), npacked);
   EvalBuffers b;
   b.natom = natom;
   b.nei = static_cast<int>(npacked);
-  b.off = R.off.p;
-  b.r = R.r.p;
-  b.e = R.e.p;
-  b.magj = R.magj.p;
-  b.mhj = R.mhj.p;
-  b.magi = R.magi.p;
-  b.mhi = R.mhi.p;
-  b.energy = R.energy.p;
-  b.fij = R.fij.p;
-  b.tij = R.tij.p;
-  b.ti0 = R.ti0.p;
-  if (run_eval(b, s)) return fail(R.last_error, R.last_msg.c_str(), npacked);
+  if (mode == kHostDirect) {
+    // the kernels read the caller's arrays and write its outputs in place
+    b.off = off.data();
+    b.r = pr;
+    b.e = pe;
+    b.magj = pm;
+    b.mhj = pmh;
+    b.magi = dlist_momi;
+    b.mhi = elist_momi;
+    b.energy = eout;
+    b.fij = flist;
+    b.tij = tlist;
+    b.ti0 = tlist0;
+    if (run_eval(b, s)) return fail(R.last_error, R.last_msg.c_str(), npacked);
+  } else {
+    auto res = [&](DevBuf<double>& bb, size_t n) { return bb.reserve(n) == cudaSuccess; };
+    if (!(res(R.r, nb) && res(R.e, 3 * nb) && res(R.magj, nb) && res(R.mhj, 3 * nb) && res(R.magi, na) &&
+          res(R.mhi, 3 * na) && res(R.fij, 3 * nb) && res(R.tij, 3 * nb) && res(R.ti0, 3 * na)) ||
+        R.off.reserve(na + 1) != cudaSuccess)
+      return fail(MAGACE_ERR_CUDA, "device allocation failed", npacked);
+    // host side of every transfer: the caller's memory, or a pinned copy of it
+    struct Xfer {
+      void* dev;
+      const void* host;
+      size_t bytes;
+    };
+    const Xfer in[] = {{R.off.p, off.data(), (na + 1) * sizeof(int)},
+                       {R.r.p, pr, nb * sizeof(double)},
+                       {R.e.p, pe, 3 * nb * sizeof(double)},
+                       {R.magj.p, pm, nb * sizeof(double)},
+                       {R.mhj.p, pmh, 3 * nb * sizeof(double)},
+                       {R.magi.p, dlist_momi, na * sizeof(double)},
+                       {R.mhi.p, elist_momi, 3 * na * sizeof(double)}};
+    const Xfer out[] = {{R.energy.p, eout, na * sizeof(double)},
+                        {R.fij.p, flist, 3 * nb * sizeof(double)},
+                        {R.tij.p, tlist, 3 * nb * sizeof(double)},
+                        {R.ti0.p, tlist0, 3 * na * sizeof(double)}};
+    size_t in_bytes = 0, out_bytes = 0;
+    for (const auto& x : in) in_bytes += (x.bytes + 255) & ~static_cast<size_t>(255);
+    for (const auto& x : out) out_bytes += (x.bytes + 255) & ~static_cast<size_t>(255);
+    bool pinned = mode == kHostPinned && reserve_pinned(std::max(in_bytes, out_bytes)) == MAGACE_OK;
+    size_t o = 0;
+    for (const auto& x : in) {
+      const void* src = x.host;
+      if (pinned && x.bytes) {
+        std::memcpy(R.pinned + o, x.host, x.bytes);
+        src = R.pinned + o;
+        o += (x.bytes + 255) & ~static_cast<size_t>(255);
+      }
+      if (ce == cudaSuccess && x.bytes) ce = cudaMemcpyAsync(x.dev, src, x.bytes, cudaMemcpyHostToDevice, s);
+    }
+    if (ce != cudaSuccess) return fail(MAGACE_ERR_CUDA, cudaGetErrorString(ce), npacked);
+    b.off = R.off.p;
+    b.r = R.r.p;
+    b.e = R.e.p;
+    b.magj = R.magj.p;
+    b.mhj = R.mhj.p;
+    b.magi = R.magi.p;
+    b.mhi = R.mhi.p;
+    b.energy = R.energy.p;
+    b.fij = R.fij.p;
+    b.tij = R.tij.p;
+    b.ti0 = R.ti0.p;
+    if (run_eval(b, s)) return fail(R.last_error, R.last_msg.c_str(), npacked);
+    o = 0;
+    for (const auto& x : out) {
+      void* dst = const_cast<void*>(x.host);
+      if (pinned && x.bytes) {
+        dst = R.pinned + o;
+        o += (x.bytes + 255) & ~static_cast<size_t>(255);
+      }
+      if (ce == cudaSuccess && x.bytes) ce = cudaMemcpyAsync(dst, x.dev, x.bytes, cudaMemcpyDeviceToHost, s);
+    }
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return fail(MAGACE_ERR_CUDA, cudaGetErrorString(ce), npacked);
+    if (pinned) {
+      o = 0;
+      for (const auto& x : out)
+        if (x.bytes) {
+          std::memcpy(const_cast<void*>(x.host), R.pinned + o, x.bytes);
+          o += (x.bytes + 255) & ~static_cast<size_t>(255);
+        }
+    }
+  }
   int dev_err = 0;
-  auto d2h = [&](void* h, const void* d, size_t bytes) {
-    if (ce == cudaSuccess && bytes) ce = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, s);
-  };
-  d2h(eout, R.energy.p, na * sizeof(double));
-  d2h(flist, R.fij.p, 3 * nb * sizeof(double));
-  d2h(tlist, R.tij.p, 3 * nb * sizeof(double));
-  d2h(tlist0, R.ti0.p, 3 * na * sizeof(double));
-  d2h(&dev_err, R.err.p, sizeof(int));
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&dev_err, R.err.p, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
   if (ce != cudaSuccess) return fail(MAGACE_ERR_CUDA, cudaGetErrorString(ce), npacked);
   if (dev_err) {

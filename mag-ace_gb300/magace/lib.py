@@ -46,6 +46,7 @@ SIGNATURES = {
     "ace_kernel_times": (_i, [ctypes.POINTER(ctypes.c_float)]),
     "ace_table_stats": (_i, [ctypes.POINTER(ctypes.c_longlong)]),
     "ace_compute_device_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ace_host_access_mode": (_i, []),
 }
 
 _lib = None
@@ -162,3 +163,8 @@ def table_stats() -> dict:
     keys = ["ne1", "ne2", "ne3", "nseg", "nslot", "nF", "nW", "nWA", "nA2h", "nfa", "nfm",
             "nba", "nbm", "n2m", "l2m", "n3a", "n3m", "l3a", "l3m", "h2", "h3"]
     return {k: int(v) for k, v in zip(keys, out)}
+
+
+def host_access() -> str:
+    """How acelib_ reaches host arrays under the current MAGACE_HOST_ACCESS."""
+    return {0: "copy", 1: "pinned", 2: "direct"}.get(int(load().ace_host_access_mode()), "unavailable")

@@ -202,3 +202,18 @@ def test_split_precision_accuracy(gpu_lib, oracle_seeded):
     assert np.abs(e - eo).max() * 1e3 < 1.0
     assert np.abs(f - fo).max() * 1e3 < 10.0
     assert np.abs(t - to).max() * 1e3 < 10.0 and np.abs(t0 - t0o).max() * 1e3 < 10.0
+
+
+@pytest.mark.parametrize("mode", ["copy", "pinned", "direct"])
+def test_host_access_modes_agree(gpu_lib, monkeypatch, mode):
+    """acelib_ gives bit-identical results whether it copies pageable memory,
+    stages through pinned memory, or lets the kernels read and write the
+    caller's arrays directly (where the GPU uses the host page tables)."""
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_128(5), 5.0)
+    monkeypatch.setenv("MAGACE_HOST_ACCESS", "copy")
+    ref = gpu_lib.acelib(nb)
+    monkeypatch.setenv("MAGACE_HOST_ACCESS", mode)
+    got = gpu_lib.acelib(nb)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
