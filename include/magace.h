@@ -121,10 +121,13 @@ int ace_host_access_mode(void);
 /* Number of kernel launches issued by the last evaluation call. */
 int ace_last_launch_count(void);
 
-/* Kernel timing: when on, the boundaries of the three kernels of every
- * evaluation are recorded with CUDA events on the evaluation stream;
- * ace_kernel_times writes the last evaluation's per-kernel durations in ms
- * (k_abasis, k_density, k_forces), synchronising on the last event. */
+/* Kernel timing: when on, the boundaries of the kernels of every evaluation
+ * are recorded with CUDA events on the evaluation stream; ace_kernel_times
+ * writes the last evaluation's per-kernel durations in ms into ms[0..3],
+ * synchronising on the last event: k_abasis, k_density, k_forces (3
+ * kernels), or k_abasis, k_b3, k_density, k_forces when the split-precision
+ * path runs its 3-body terms as a kernel of their own (4 kernels, see
+ * ace_last_launch_count). Entries beyond the kernel count are 0. */
 int ace_set_kernel_timing(int on);
 int ace_kernel_times(float* ms);
 
@@ -133,8 +136,12 @@ int ace_kernel_times(float* ms);
  * out[6] weights per atom (nW), out[7] A weight slots, out[8] A2 half slots,
  * out[9] atomic LUT functions, out[10] magnetic LUT functions, out[11..20]
  * the basis dims nradbase_a, nradbase_m, nradial2_m, l2max_m, nradial3_a,
- * nradial3_m, l3max_a, l3max_m, and the half-plane sizes h2, h3
- * (21 entries). */
+ * nradial3_m, l3max_a, l3max_m, and the half-plane sizes h2, h3;
+ * out[21..25] the dense 3-body tables of the specialised kernels: tasks,
+ * angular combinations, half-plane elements, and the segments and entries of
+ * the remaining (non-3-body) gather table; out[26..28] that table's entries
+ * by arity 1..3; out[29] the coefficient pairs the dense 3-body contraction
+ * visits per atom (30 entries). */
 int ace_table_stats(long long* out);
 
 /* Allocation-free variant of ace_compute_device, for callers that cannot

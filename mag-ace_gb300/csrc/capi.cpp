@@ -73,20 +73,35 @@ struct Runtime {
   bool dev_tables = false;
   int device = -1;
   cudaStream_t stream = nullptr;
-  DevBuf<double> lut_a, lut_m, c1, slot_mult;
-  DevBuf<double> kap[4];
+  DevBuf<double> lut_a, lut_m, c1;
   DevBuf<float> lut_a32, lut_m32;
-  DevBuf<float> kapf[4];
-  DevBuf<uint32_t> o12[4];
-  DevBuf<uint16_t> o3;
-  DevBuf<int32_t> grp_arity, grp_len, grp_first, grp_seg, slot_seg, slot_factor, slot_weight;
+  struct GatherBufs {
+    DevBuf<double> kap[4], slot_mult;
+    DevBuf<float> kapf[4];
+    DevBuf<uint32_t> o12[4];
+    DevBuf<uint16_t> o3;
+    DevBuf<int32_t> grp_arity, grp_len, grp_first, grp_seg, slot_seg, slot_factor, slot_weight;
+    void release() {
+      for (int a = 0; a < 4; ++a) {
+        kap[a].release();
+        kapf[a].release();
+        o12[a].release();
+      }
+      slot_mult.release();
+      o3.release();
+      for (auto* b : {&grp_arity, &grp_len, &grp_first, &grp_seg, &slot_seg, &slot_factor, &slot_weight}) b->release();
+    }
+  } gb1, gb2;
+  DevBuf<float> b3_Cf, b3_cff;
+  DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
+  DevBuf<uint16_t> b3_code;
   DeviceModel dm{};
   int grid_cap = 0;
 
   // work buffers
   DevBuf<int> off, err;
   DevBuf<double> r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0, rho1, core, edf, dedrho;
-  DevBuf<unsigned char> F, W;
+  DevBuf<unsigned char> F, W, aux;
   std::vector<int> h_off;
 
   // pinned staging for host transfers, and whether the GPU reads pageable
@@ -97,7 +112,7 @@ struct Runtime {
 
   // optional kernel-boundary events of the last evaluation
   bool timing = false;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[kMaxLaunches + 1] = {};
   bool ev_recorded = false;
 };
 
@@ -145,6 +160,49 @@ std::vector<float> to_float(const std::vector<T>& v) {
   return std::vector<float>(v.begin(), v.end());
 }
 
+int upload_gather(const GatherTable& g, Runtime::GatherBufs& B, GatherView& v) {
+  for (int a = 1; a <= 3; ++a) {
+    std::vector<double> k(g.kap[a][0]);
+    k.insert(k.end(), g.kap[a][1].begin(), g.kap[a][1].end());
+    CUDA_TRY(B.kap[a].upload(k));
+    CUDA_TRY(B.kapf[a].upload(to_float(k)));
+    CUDA_TRY(B.o12[a].upload(g.o12[a]));
+  }
+  CUDA_TRY(B.o3.upload(g.o3));
+  CUDA_TRY(B.grp_arity.upload(g.grp_arity));
+  CUDA_TRY(B.grp_len.upload(g.grp_len));
+  CUDA_TRY(B.grp_first.upload(g.grp_first));
+  CUDA_TRY(B.grp_seg.upload(g.grp_seg));
+  CUDA_TRY(B.slot_seg.upload(g.slot_seg_begin));
+  CUDA_TRY(B.slot_factor.upload(g.slot_factor));
+  CUDA_TRY(B.slot_weight.upload(g.slot_weight));
+  CUDA_TRY(B.slot_mult.upload(g.slot_mult));
+  v.nslot = g.nslot;
+  v.nG0 = g.nG0;
+  v.nseg = g.nseg;
+  v.ngroup = g.ngroup;
+  v.grp_arity = B.grp_arity.p;
+  v.grp_len = B.grp_len.p;
+  v.grp_first = B.grp_first.p;
+  v.grp_seg = B.grp_seg.p;
+  v.kap[0] = nullptr;
+  v.kapf[0] = nullptr;
+  v.o12[0] = nullptr;
+  v.kstride[0] = 0;
+  for (int a = 1; a <= 3; ++a) {
+    v.kap[a] = B.kap[a].p;
+    v.kapf[a] = B.kapf[a].p;
+    v.o12[a] = B.o12[a].p;
+    v.kstride[a] = static_cast<int>(g.kap[a][0].size());
+  }
+  v.o3 = B.o3.p;
+  v.slot_seg = B.slot_seg.p;
+  v.slot_factor = B.slot_factor.p;
+  v.slot_weight = B.slot_weight.p;
+  v.slot_mult = B.slot_mult.p;
+  return MAGACE_OK;
+}
+
 int upload_tables() {
   Runtime& R = rt();
   if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
@@ -163,22 +221,24 @@ int upload_tables() {
   for (int d = 0; d < 2; ++d)
     for (int n = 0; n < M.L.nbm; ++n) c1[d * M.L.nbm + n] = M.c1[d][n];
   CUDA_TRY(R.c1.upload(c1));
-  for (int a = 1; a <= 3; ++a) {
-    std::vector<double> k(g.kap[a][0]);
-    k.insert(k.end(), g.kap[a][1].begin(), g.kap[a][1].end());
-    CUDA_TRY(R.kap[a].upload(k));
-    CUDA_TRY(R.kapf[a].upload(to_float(k)));
-    CUDA_TRY(R.o12[a].upload(g.o12[a]));
+  {
+    int st = upload_gather(M.gt, R.gb1, R.dm.g);
+    if (st) return st;
+    if (M.ndensity == 1) {
+      st = upload_gather(M.gt_nob3, R.gb2, R.dm.g2);
+      if (st) return st;
+      const DenseB3& D = M.db3;
+      CUDA_TRY(R.b3_Cf.upload(to_float(D.C)));
+      CUDA_TRY(R.b3_cff.upload(to_float(D.task_cf)));
+      CUDA_TRY(R.b3_pattern.upload(D.pattern));
+      CUDA_TRY(R.b3_combo.upload(D.task_combo));
+      CUDA_TRY(R.b3_code.upload(D.code));
+      CUDA_TRY(R.b3_factor.upload(D.factor_of));
+      CUDA_TRY(R.b3_cw.upload(D.compact_of_weight));
+    } else {
+      R.dm.g2 = R.dm.g;
+    }
   }
-  CUDA_TRY(R.o3.upload(g.o3));
-  CUDA_TRY(R.grp_arity.upload(g.grp_arity));
-  CUDA_TRY(R.grp_len.upload(g.grp_len));
-  CUDA_TRY(R.grp_first.upload(g.grp_first));
-  CUDA_TRY(R.grp_seg.upload(g.grp_seg));
-  CUDA_TRY(R.slot_seg.upload(g.slot_seg_begin));
-  CUDA_TRY(R.slot_factor.upload(g.slot_factor));
-  CUDA_TRY(R.slot_weight.upload(g.slot_weight));
-  CUDA_TRY(R.slot_mult.upload(g.slot_mult));
   double alm[kMaxHalf], blm[kMaxHalf], cl[kMaxL + 1], dl[kMaxL + 1];
   ylm_constants(alm, blm, cl, dl);
   upload_ylm_constants(alm, blm, cl, dl);
@@ -206,29 +266,16 @@ int upload_tables() {
   d.lut_a32 = R.lut_a32.p;
   d.lut_m32 = R.lut_m32.p;
   d.c1 = R.c1.p;
-  d.nslot = g.nslot;
-  d.nG0 = g.nG0;
-  d.nseg = g.nseg;
-  d.ngroup = g.ngroup;
-  d.grp_arity = R.grp_arity.p;
-  d.grp_len = R.grp_len.p;
-  d.grp_first = R.grp_first.p;
-  d.grp_seg = R.grp_seg.p;
-  d.kap[0] = nullptr;
-  d.kapf[0] = nullptr;
-  d.o12[0] = nullptr;
-  d.kstride[0] = 0;
-  for (int a = 1; a <= 3; ++a) {
-    d.kap[a] = R.kap[a].p;
-    d.kapf[a] = R.kapf[a].p;
-    d.o12[a] = R.o12[a].p;
-    d.kstride[a] = static_cast<int>(g.kap[a][0].size());
-  }
-  d.o3 = R.o3.p;
-  d.slot_seg = R.slot_seg.p;
-  d.slot_factor = R.slot_factor.p;
-  d.slot_weight = R.slot_weight.p;
-  d.slot_mult = R.slot_mult.p;
+  d.b3_ntask = M.db3.ntask;
+  d.b3_ncombo = M.db3.ncombo;
+  d.b3_nc = M.db3.nc;
+  d.b3_Cf = R.b3_Cf.p;
+  d.b3_pattern = R.b3_pattern.p;
+  d.b3_combo = R.b3_combo.p;
+  d.b3_cff = R.b3_cff.p;
+  d.b3_code = R.b3_code.p;
+  d.b3_factor = R.b3_factor.p;
+  d.b3_cw = R.b3_cw.p;
   int sms = 0;
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   R.grid_cap = std::max(1, sms) * 64;
@@ -255,6 +302,7 @@ int reserve_work(int natom, int nei) {
   CUDA_TRY(R.dedrho.reserve(2 * na));
   CUDA_TRY(R.F.reserve(na * R.dm.nF * csz));
   CUDA_TRY(R.W.reserve(na * R.dm.nW * csz));
+  CUDA_TRY(R.aux.reserve(eval_aux_bytes(R.dm, R.precision, natom)));
   (void)nb;
   return MAGACE_OK;
 }
@@ -268,6 +316,7 @@ int run_eval(EvalBuffers& b, cudaStream_t st) {
   b.edf = R.edf.p;
   b.dedrho = R.dedrho.p;
   b.err = R.err.p;
+  b.aux = R.aux.p;
   CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), st));
   cudaEvent_t* ev = nullptr;
   if (R.timing) {
@@ -277,7 +326,7 @@ int run_eval(EvalBuffers& b, cudaStream_t st) {
   }
   R.last_launches = R.precision == 0 ? launch_eval_fp64(R.dm, b, st, R.grid_cap, ev)
                                      : launch_eval_fp32(R.dm, b, st, R.grid_cap, ev);
-  R.ev_recorded = ev != nullptr && R.last_launches == 3;
+  R.ev_recorded = ev != nullptr && R.last_launches >= 3;
   CUDA_TRY(cudaGetLastError());
   return MAGACE_OK;
 }
@@ -478,8 +527,12 @@ int ace_set_kernel_timing(int on) {
 int ace_kernel_times(float* ms) {
   Runtime& R = rt();
   if (!R.ev_recorded) return set_error(MAGACE_ERR_ARGS, "no timed evaluation recorded");
-  CUDA_TRY(cudaEventSynchronize(R.ev[3]));
-  for (int k = 0; k < 3; ++k) CUDA_TRY(cudaEventElapsedTime(&ms[k], R.ev[k], R.ev[k + 1]));
+  const int n = R.last_launches;
+  CUDA_TRY(cudaEventSynchronize(R.ev[n]));
+  for (int k = 0; k < kMaxLaunches; ++k) {
+    ms[k] = 0.0f;
+    if (k < n) CUDA_TRY(cudaEventElapsedTime(&ms[k], R.ev[k], R.ev[k + 1]));
+  }
   return MAGACE_OK;
 }
 
@@ -501,6 +554,21 @@ int ace_table_stats(long long* out) {
   out[10] = R.model.lut.nfm;
   const int dims[10] = {L.nba, L.nbm, L.n2m, L.l2m, L.n3a, L.n3m, L.l3a, L.l3m, L.h2, L.h3};
   for (int k = 0; k < 10; ++k) out[11 + k] = dims[k];
+  out[21] = R.model.db3.ntask;
+  out[22] = R.model.db3.ncombo;
+  out[23] = R.model.db3.nc;
+  out[24] = R.model.gt_nob3.nseg;
+  out[25] = R.model.gt_nob3.entries[1] + R.model.gt_nob3.entries[2] + R.model.gt_nob3.entries[3];
+  for (int a = 1; a <= 3; ++a) out[25 + a] = R.model.gt_nob3.entries[a];
+  // (i, j) coefficient pairs the dense 3-body contraction visits per atom
+  const DenseB3& D = R.model.db3;
+  long long pairs = 0;
+  for (int t = 0; t < D.ntask; ++t) {
+    const int pat = D.pattern[D.task_combo[t]];
+    for (int i = 0; i < D.I; ++i)
+      pairs += D.NM * (pat == 0 ? i + 1 : (pat == 1 ? (i / D.NM + 1) * D.NM : (i / D.NM) * D.NM));
+  }
+  out[29] = pairs;
   return MAGACE_OK;
 }
 
@@ -542,21 +610,18 @@ int ace_device_status(void) {
 
 void ace_release_device(void) {
   Runtime& R = rt();
-  for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.slot_mult, &R.r, &R.e, &R.magj, &R.mhj, &R.magi, &R.mhi,
-                  &R.energy, &R.fij, &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
+  for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.r, &R.e, &R.magj, &R.mhj, &R.magi, &R.mhi, &R.energy, &R.fij,
+                  &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
     b->release();
-  for (int a = 0; a < 4; ++a) {
-    R.kap[a].release();
-    R.kapf[a].release();
-    R.o12[a].release();
-  }
-  for (auto* b : {&R.lut_a32, &R.lut_m32}) b->release();
-  R.o3.release();
-  for (auto* b : {&R.grp_arity, &R.grp_len, &R.grp_first, &R.grp_seg, &R.slot_seg, &R.slot_factor, &R.slot_weight})
-    b->release();
+  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff}) b->release();
+  for (auto* b : {&R.b3_pattern, &R.b3_combo, &R.b3_factor, &R.b3_cw}) b->release();
+  R.b3_code.release();
+  R.gb1.release();
+  R.gb2.release();
   R.off.release();
   R.err.release();
   R.F.release();
+  R.aux.release();
   R.W.release();
   if (R.stream) cudaStreamDestroy(R.stream);
   R.stream = nullptr;

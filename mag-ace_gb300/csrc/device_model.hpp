@@ -20,6 +20,25 @@ enum DeviceError : int {
   kDevShape = 4,   // more bonds than a tile index can address
 };
 
+// one gather table: group g has arity grp_arity[g], length grp_len[g] and its
+// entries at grp_first[g] + e*32 + lane
+struct GatherView {
+  int nslot, nG0, nseg, ngroup;
+  const int32_t* grp_arity;
+  const int32_t* grp_len;
+  const int32_t* grp_first;
+  const int32_t* grp_seg;      // [ngroup*32] segment id per lane, -1 padding
+  const double* kap[4];        // [arity][density * kstride[arity] + slot] FP64
+  const float* kapf[4];        // FP32 copies (split path)
+  int kstride[4];
+  const uint32_t* o12[4];      // o1 | o2 << 16
+  const uint16_t* o3;          // third factor of arity-3 entries
+  const int32_t* slot_seg;     // [nslot+1]
+  const int32_t* slot_factor;  // [nslot] (G0 slots only)
+  const int32_t* slot_weight;  // [nslot]
+  const double* slot_mult;     // [nslot]
+};
+
 struct DeviceModel {
   // basis dims (see model.hpp for the layouts)
   int n3a, n3m, l3a, l3m, nba, n2m, l2m, nbm;
@@ -38,22 +57,18 @@ struct DeviceModel {
   const float* lut_m32;
   // 1-body coefficients c1[d * nbm + n]
   const double* c1;
-  // gather table in warp groups (see model.hpp): group g has arity
-  // grp_arity[g], length grp_len[g] and its entries at grp_first[g] + e*32 + lane
-  int nslot, nG0, nseg, ngroup;
-  const int32_t* grp_arity;
-  const int32_t* grp_len;
-  const int32_t* grp_first;
-  const int32_t* grp_seg;      // [ngroup*32] segment id per lane, -1 padding
-  const double* kap[4];        // [arity][density * kstride[arity] + slot] FP64
-  const float* kapf[4];        // FP32 copies (split path)
-  int kstride[4];
-  const uint32_t* o12[4];      // o1 | o2 << 16
-  const uint16_t* o3;          // third factor of arity-3 entries
-  const int32_t* slot_seg;     // [nslot+1]
-  const int32_t* slot_factor;  // [nslot] (G0 slots only)
-  const int32_t* slot_weight;  // [nslot]
-  const double* slot_mult;     // [nslot]
+  // gather tables in warp groups (see model.hpp): g holds every term (generic
+  // kernels), g2 every term except the 3-body ones (specialised kernels)
+  GatherView g, g2;
+  // dense 3-body tables of the specialised kernels (see model.hpp DenseB3)
+  int b3_ntask, b3_ncombo, b3_nc;
+  const float* b3_Cf;         // [combo][NM][I][I]
+  const int32_t* b3_pattern;  // [combo]
+  const int32_t* b3_combo;    // [task]
+  const float* b3_cff;        // [task]
+  const uint16_t* b3_code;    // [task][NM + 2I] compact element | sign bits
+  const int32_t* b3_factor;   // [nc] factor index of each compact element
+  const int32_t* b3_cw;       // [nW] compact element of each weight, or -1
 };
 
 }  // namespace magace

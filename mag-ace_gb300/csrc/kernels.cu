@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 
 #include "device_model.hpp"
 #include "kernels.hpp"
@@ -60,12 +61,57 @@ __device__ __forceinline__ void raise_error(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
 
+// Double <-> float conversions on the integer pipes. A hardware conversion
+// issues on the FP64 pipe, which GB300 runs at 1/64 of the FP32 rate; the
+// split path converts every input and output, so it uses these instead.
+// d2f rounds half away from zero (|error| <= 1/2 float ulp), flushes values
+// below the float normal range to signed zero, maps overflow to infinity and
+// keeps NaN; f2d is exact for normal floats and flushes float subnormals.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long b0 = static_cast<unsigned long long>(__double_as_longlong(x));
+  const int e0 = static_cast<int>((b0 >> 52) & 0x7ffu);
+  const unsigned long long b = b0 + (1ull << 28);  // half a float ulp
+  const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
+  const unsigned sign = hi & 0x80000000u;
+  const int fe = static_cast<int>((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  unsigned f = sign | (static_cast<unsigned>(fe) << 23) | mant;
+  if (fe <= 0) f = sign;
+  if (fe >= 255) f = sign | 0x7f800000u;
+  if (e0 == 0x7ff) f = (b0 << 12) ? 0x7fc00000u : (sign | 0x7f800000u);
+  return __uint_as_float(f);
+}
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned f = __float_as_uint(x);
+  const unsigned long long sign = static_cast<unsigned long long>(f & 0x80000000u) << 32;
+  const unsigned e = (f >> 23) & 0xffu;
+  const unsigned long long mant = static_cast<unsigned long long>(f & 0x7fffffu) << 29;
+  unsigned long long d = sign | (static_cast<unsigned long long>(e + 1023 - 127) << 52) | mant;
+  if (e == 0) d = sign;
+  if (e == 0xff) d = sign | (0x7ffull << 52) | mant;
+  return __longlong_as_double(static_cast<long long>(d));
+}
+template <class R>
+__device__ __forceinline__ R to_r(double x);
+template <>
+__device__ __forceinline__ double to_r<double>(double x) {
+  return x;
+}
+template <>
+__device__ __forceinline__ float to_r<float>(double x) {
+  return d2f(x);
+}
+__device__ __forceinline__ double to_d(double x) { return x; }
+__device__ __forceinline__ double to_d(float x) { return f2d(x); }
+__device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
+
 // Spherical harmonics Y_lm (m >= 0 half, packed by ph) of a unit vector and,
 // optionally, their tangential gradients dY = grad Y - (r . grad Y) r, in the
 // normalisation and recurrence of src/spherical.F90:55-260 (Y_00 = 1,
 // Condon-Shortley phase through cl).
 template <class R, bool GRAD>
-__device__ void ylm_half(int L, R rx, R ry, R rz, C<R>* Y, C<R> (*dY)[3]) {
+__device__ __forceinline__ void ylm_half(int L, R rx, R ry, R rz, C<R>* Y, C<R> (*dY)[3]) {
   R plm[kMaxHalf], dplm[kMaxHalf];
   const R sq3 = R(1.73205080756887719318), sq3o2 = R(1.22474487139158894067);
   plm[0] = R(1);
@@ -187,6 +233,32 @@ __device__ __forceinline__ int atomic_bin(const DeviceModel& m, double r, double
   if (x >= static_cast<double>(m.nlut)) return 0;  // zero features (src/radial.F90:77-83)
   const int nl = static_cast<int>(floor(x));
   wl = x - static_cast<double>(nl);
+  return nl;
+}
+
+// the same in the working precision of the split path (the bin position
+// carries ~1e-7 relative error, far inside the interpolant's own)
+template <class R>
+__device__ __forceinline__ int atomic_bin_r(const DeviceModel& m, R r, R& wl, int* err) {
+  const R x = r * R(m.rscale_a);
+  if (!(x >= R(1))) {
+    raise_error(err, kDevSmallR);
+    return -1;
+  }
+  if (x >= R(m.nlut)) return 0;
+  const int nl = static_cast<int>(floor(x));
+  wl = x - R(nl);
+  return nl;
+}
+template <class R>
+__device__ __forceinline__ int magnetic_bin_r(const DeviceModel& m, R mag, R& wl, int* err) {
+  const R x = mag * R(m.rscale_m);
+  if (!(x >= R(0)) || x >= R(m.nlut)) {
+    raise_error(err, kDevMoment);
+    return -1;
+  }
+  const int nl = static_cast<int>(floor(x));
+  wl = x - R(nl);
   return nl;
 }
 
@@ -416,13 +488,13 @@ __device__ void embed(int nfemb, double rho, double wpre, double mexp, double& F
 // Shared memory: Fs[nF] (complex R), part[nseg][ND] (complex R),
 // tot[nslot][ND] (complex R, hi) and, for FP32, the low words.
 template <class R>
-__device__ __forceinline__ const R* kap_ptr(const DeviceModel& m, int a);
+__device__ __forceinline__ const R* kap_ptr(const GatherView& m, int a);
 template <>
-__device__ __forceinline__ const double* kap_ptr<double>(const DeviceModel& m, int a) {
+__device__ __forceinline__ const double* kap_ptr<double>(const GatherView& m, int a) {
   return m.kap[a];
 }
 template <>
-__device__ __forceinline__ const float* kap_ptr<float>(const DeviceModel& m, int a) {
+__device__ __forceinline__ const float* kap_ptr<float>(const GatherView& m, int a) {
   return m.kapf[a];
 }
 
@@ -447,7 +519,7 @@ __global__ void __launch_bounds__(kDensityThreads)
   extern __shared__ __align__(16) unsigned char smem[];
   C<R>* Fs = reinterpret_cast<C<R>*>(smem);
   C<R>* part = Fs + ((m.nF + 1) & ~1);
-  C<R>* tot = part + ((m.nseg * ND + 1) & ~1);
+  C<R>* tot = part + ((m.g.nseg * ND + 1) & ~1);
   __shared__ double s_red[kDensityThreads / 32][ND];
   __shared__ double s_dE[ND];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -456,12 +528,12 @@ __global__ void __launch_bounds__(kDensityThreads)
     const C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
     for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
     __syncthreads();
-    for (int g = warp; g < m.ngroup; g += nwarp) {
-      const int a = m.grp_arity[g], len = m.grp_len[g], base = m.grp_first[g] + lane;
-      const int seg = m.grp_seg[g * 32 + lane];
-      const R* kp = kap_ptr<R>(m, a) + base;
-      const uint32_t* op = m.o12[a] + base;
-      const int ks = m.kstride[a];
+    for (int g = warp; g < m.g.ngroup; g += nwarp) {
+      const int a = m.g.grp_arity[g], len = m.g.grp_len[g], base = m.g.grp_first[g] + lane;
+      const int seg = m.g.grp_seg[g * 32 + lane];
+      const R* kp = kap_ptr<R>(m.g, a) + base;
+      const uint32_t* op = m.g.o12[a] + base;
+      const int ks = m.g.kstride[a];
       C<R> acc[ND];
       for (int d = 0; d < ND; ++d) acc[d] = {R(0), R(0)};
       if (a == 2) {
@@ -486,7 +558,7 @@ __global__ void __launch_bounds__(kDensityThreads)
           }
         }
       } else {
-        const uint16_t* o3p = m.o3 + base;
+        const uint16_t* o3p = m.g.o3 + base;
         for (int e = 0; e < len; ++e) {
           const uint32_t o = __ldg(op + e * 32);
           const C<R> p = cmul(cmul(Fs[o & 0xffffu], Fs[o >> 16]), Fs[__ldg(o3p + e * 32)]);
@@ -503,8 +575,8 @@ __global__ void __launch_bounds__(kDensityThreads)
     __syncthreads();
     double rloc[ND];
     for (int d = 0; d < ND; ++d) rloc[d] = 0.0;
-    for (int s = threadIdx.x; s < m.nslot; s += blockDim.x) {
-      const int q0 = m.slot_seg[s], q1 = m.slot_seg[s + 1];
+    for (int s = threadIdx.x; s < m.g.nslot; s += blockDim.x) {
+      const int q0 = m.g.slot_seg[s], q1 = m.g.slot_seg[s + 1];
       for (int d = 0; d < ND; ++d) {
         CSum<R> tx, ty;
         for (int q = q0; q < q1; ++q) {
@@ -512,8 +584,8 @@ __global__ void __launch_bounds__(kDensityThreads)
           ty.add(part[q * ND + d].y);
         }
         tot[s * ND + d] = {tx.hi + tx.lo, ty.hi + ty.lo};
-        if (s < m.nG0) {
-          const C<R> f = Fs[m.slot_factor[s]];
+        if (s < m.g.nG0) {
+          const C<R> f = Fs[m.g.slot_factor[s]];
           rloc[d] += static_cast<double>(f.x) * tx.value() - static_cast<double>(f.y) * ty.value();
         }
       }
@@ -560,10 +632,10 @@ __global__ void __launch_bounds__(kDensityThreads)
     }
     __syncthreads();
     C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
-    for (int s = threadIdx.x; s < m.nslot; s += blockDim.x) {
-      const int w = m.slot_weight[s];
+    for (int s = threadIdx.x; s < m.g.nslot; s += blockDim.x) {
+      const int w = m.g.slot_weight[s];
       if (w < 0) continue;
-      const R mu = R(m.slot_mult[s]);
+      const R mu = R(m.g.slot_mult[s]);
       C<R> v = {R(0), R(0)};
       for (int d = 0; d < ND; ++d) {
         const R sc = mu * R(s_dE[d]);
@@ -796,6 +868,8 @@ __global__ void __launch_bounds__(kForceThreads)
   }
 }
 
+#include "kernels_fe.inl"
+
 // ===========================================================================
 // host-side launch helpers
 
@@ -816,8 +890,8 @@ size_t abasis_smem(const DeviceModel& m) {
 
 template <class R>
 size_t density_smem(const DeviceModel& m) {
-  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((m.nseg * m.nd + 1) & ~1) +
-                         static_cast<size_t>(m.nslot) * m.nd) + 64;
+  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((m.g.nseg * m.nd + 1) & ~1) +
+                         static_cast<size_t>(m.g.nslot) * m.nd) + 64;
 }
 
 template <class R>
@@ -827,17 +901,51 @@ size_t forces_smem(const DeviceModel& m, int T) {
   return sizeof(C<R>) * nc + sizeof(R) * nr + 64;
 }
 
+// k_b3_fe's outputs in EvalBuffers::aux: G3 [natom][nc] complex float, then
+// rho3 [natom] double at the next 256-byte boundary
+size_t b3_g3_bytes(const DeviceModel& m, int natom) {
+  const size_t g = sizeof(C<float>) * static_cast<size_t>(m.b3_nc) * static_cast<size_t>(natom);
+  return (g + 255) & ~static_cast<size_t>(255);
+}
+
+// Whether the compile-time specialised kernels apply: the basis has the Fe
+// layout and one density, and MAGACE_GENERIC is not set.
+bool use_specialised(const DeviceModel& m) {
+  static const bool forced_generic = [] {
+    const char* e = std::getenv("MAGACE_GENERIC");
+    return e && e[0] == '1';
+  }();
+  return !forced_generic && m.nd == 1 && dims_match<FeDims>(m);
+}
+
+// The density phase: in split precision with the specialised layout, k_b3_fe
+// (3-body terms, 32 atoms per CTA) and then k_density_fe (the rest, the
+// embedding and the weights); otherwise one generic k_density. Returns the
+// number of kernels launched.
 template <class R>
-int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
+int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid, int grid_cap, bool fe,
+                   cudaEvent_t ev_between) {
   const int natom = b.natom;
-  if (natom <= 0) return 0;
-  const int grid = natom < grid_cap ? natom : grid_cap;
-  const size_t s1 = abasis_smem<R>(m), s2 = density_smem<R>(m), s3 = forces_smem<R>(m, kForceThreads);
-  if (ev) cudaEventRecord(ev[0], st);
-  cudaFuncSetAttribute(k_abasis<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1));
-  k_abasis<R><<<grid, kAbasisThreads, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                 reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
-  if (ev) cudaEventRecord(ev[1], st);
+  if constexpr (sizeof(R) == 4) {
+    if (fe) {
+      C<float>* G3 = static_cast<C<float>*>(b.aux);
+      double* rho3 = reinterpret_cast<double*>(static_cast<unsigned char*>(b.aux) + b3_g3_bytes(m, natom));
+      const size_t sb = b3_fe_smem(m);
+      cudaFuncSetAttribute(k_b3_fe<FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb));
+      const int nblk = (natom + 31) / 32;
+      k_b3_fe<FeDims><<<nblk < grid_cap ? nblk : grid_cap, kB3Warps * 32, sb, st>>>(
+          m, natom, reinterpret_cast<const C<float>*>(b.F), G3, rho3);
+      if (ev_between) cudaEventRecord(ev_between, st);
+      const size_t s2 = density_fe_smem<float, FeDims>(m);
+      cudaFuncSetAttribute(k_density_fe<float, FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(s2));
+      k_density_fe<float, FeDims><<<grid, kDensityFeThreads, s2, st>>>(
+          m, natom, reinterpret_cast<const C<float>*>(b.F), b.rho1, b.core, G3, rho3,
+          reinterpret_cast<C<float>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
+      return 2;
+    }
+  }
+  const size_t s2 = density_smem<R>(m);
   if (m.nd == 1) {
     cudaFuncSetAttribute(k_density<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
     k_density<R, 1><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
@@ -847,16 +955,67 @@ int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int
     k_density<R, 2><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
                                                        reinterpret_cast<C<R>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
   }
-  if (ev) cudaEventRecord(ev[2], st);
-  cudaFuncSetAttribute(k_forces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s3));
-  k_forces<R><<<grid, kForceThreads, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
-                                                b.ti0, b.err);
-  if (ev) cudaEventRecord(ev[3], st);
-  return 3;
+  return 1;
+}
+
+template <class R>
+int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
+  const int natom = b.natom;
+  if (natom <= 0) return 0;
+  const int grid = natom < grid_cap ? natom : grid_cap;
+  const bool fe = use_specialised(m);
+  if (ev) cudaEventRecord(ev[0], st);
+  if (fe) {
+    const size_t s1 = abasis_fe_smem<R, FeDims>();
+    cudaFuncSetAttribute(k_abasis_fe<R, FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1));
+    k_abasis_fe<R, FeDims><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                 reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+  } else {
+    const size_t s1 = abasis_smem<R>(m);
+    cudaFuncSetAttribute(k_abasis<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1));
+    k_abasis<R><<<grid, kAbasisThreads, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                   reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+  }
+  if (ev) cudaEventRecord(ev[1], st);
+  const int nd = launch_density<R>(m, b, st, grid, grid_cap, fe, ev ? ev[2] : nullptr);
+  const int nlaunch = 2 + nd;
+  if (ev) cudaEventRecord(ev[1 + nd], st);
+  if (fe) {
+    const size_t s3 = forces_fe_smem<R, FeDims>();
+    cudaFuncSetAttribute(k_forces_fe<R, FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s3));
+    k_forces_fe<R, FeDims><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                 reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
+                                                 b.ti0, b.err);
+  } else {
+    const size_t s3 = forces_smem<R>(m, kForceThreads);
+    cudaFuncSetAttribute(k_forces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s3));
+    k_forces<R><<<grid, kForceThreads, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                  reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
+                                                  b.ti0, b.err);
+  }
+  if (ev) cudaEventRecord(ev[nlaunch], st);
+  return nlaunch;
+}
+
+size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom) {
+  if (precision == 0 || !use_specialised(m) || natom <= 0) return 0;
+  return b3_g3_bytes(m, natom) + sizeof(double) * static_cast<size_t>(natom);
 }
 
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
+  if (use_specialised(m)) {
+    if (precision == 0) {
+      if (which == 0) return abasis_fe_smem<double, FeDims>();
+      if (which == 1) return density_smem<double>(m);
+      return forces_fe_smem<double, FeDims>();
+    }
+    if (which == 0) return abasis_fe_smem<float, FeDims>();
+    if (which == 1) {
+      const size_t a = density_fe_smem<float, FeDims>(m), b = b3_fe_smem(m);
+      return a > b ? a : b;
+    }
+    return forces_fe_smem<float, FeDims>();
+  }
   if (precision == 0) {
     if (which == 0) return abasis_smem<double>(m);
     if (which == 1) return density_smem<double>(m);

@@ -12,8 +12,10 @@ namespace magace {
 constexpr int kAbasisThreads = 128;
 constexpr int kAbasisTile = 64;  // bonds per feature tile
 constexpr int kDensityThreads = 256;
+constexpr int kDensityFeThreads = 128;
 constexpr int kForceThreads = 64;
 constexpr int kMaxFeat = 32;     // per-bond radial functions of one kind
+constexpr int kMaxLaunches = 4;  // kernels of one evaluation
 
 // Device arrays of one evaluation. F and W are complex arrays of the selected
 // precision (FP64: 16 bytes per entry, FP32: 8 bytes).
@@ -37,12 +39,17 @@ struct EvalBuffers {
   double* tij = nullptr;      // [3*nei]
   double* ti0 = nullptr;      // [3*natom]
   int* err = nullptr;         // device error word
+  void* aux = nullptr;        // [eval_aux_bytes] scratch of the specialised split-precision kernels
 };
 
 void upload_ylm_constants(const double* alm, const double* blm, const double* cl, const double* dl);
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which);
-// Launches k_abasis, k_density and k_forces on `st`; returns the number of
-// kernels launched. With `ev` (4 events) the kernel boundaries are recorded.
+// Size of EvalBuffers::aux for natom atoms (0 when the kernels need none).
+size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom);
+// Launches the A-basis, density and force phases on `st` (3 kernels, or 4
+// when the split-precision density runs its 3-body part as a kernel of its
+// own); returns the number of kernels launched n. With `ev` (kMaxLaunches + 1
+// events) ev[k] is recorded before kernel k and ev[n] after the last one.
 int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
 int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
 

@@ -1,0 +1,723 @@
+// Kernels specialised at compile time for one basis layout: the layout of
+// the reference's example Fe potential (example/Fe.pbe.in:6-13; 16/16 base
+// functions, 4 atomic x 3 magnetic radial functions up to l = 1 / l' = 2,
+// 5 magnetic pair functions up to l' = 2). Included by kernels.cu; the
+// generic kernels there serve every other layout.
+//
+// With the dims known to the compiler, the per-bond and per-task loops fully
+// unroll and their operands stay in registers:
+//   k_abasis_fe  the bond sums A and A2 are small GEMMs over the bonds of an
+//                atom; warp 0 owns 1 x 9 tiles of A, warp 1 1 x 15 tiles of A2.
+//   k_density_fe the 3-body density and weights as dense contractions per
+//                (angular combination, m-term) task, C[n0'][i][j] a X Y,
+//                exploiting the triangular cluster order; the 2- and 4-body
+//                terms go through the gather table.
+//   k_forces_fe  per bond, U = W_A Q and V = W2 g + W_A^T RY with the
+//                weights transposed in shared memory for 16-byte loads.
+
+template <int NA_, int LA_, int NM_, int LM_, int NB_, int N2_, int L2_, int NBM_>
+struct Dims {
+  static constexpr int NA = NA_, LA = LA_, NM = NM_, LM = LM_, NB = NB_, N2 = N2_, L2 = L2_, NBM = NBM_;
+  static constexpr int LSA = (LA + 1) * (LA + 1), LS3 = (LM + 1) * (LM + 1), LS2 = (L2 + 1) * (L2 + 1);
+  static constexpr int HA = (LA + 1) * (LA + 2) / 2, H3 = (LM + 1) * (LM + 2) / 2, H2 = (L2 + 1) * (L2 + 2) / 2;
+  static constexpr int NR = NA * (LA + 1);  // atomic radial functions R_nl
+  static constexpr int NMF = N2 * (L2 + 1); // magnetic radial functions M_nl
+  static constexpr int NRY = NA * LSA;      // R_nl Y_lm products (rows of A)
+  static constexpr int NQ = N2 * H2;        // M_nl Y_lm (m >= 0) products
+  static constexpr int NQ3 = NM * H3;       // the subset used by A
+  static constexpr int NWA = NRY * NQ3;
+  static constexpr int NA2H = NB * NQ;
+  static constexpr int I = NA * NM;         // dense 3-body index (n, n')
+  static constexpr int NPOS = NM + 2 * I;   // outputs of one 3-body task
+  static constexpr int NFA = NB + NR + 1;
+  static constexpr int NFM = NMF + NBM;
+};
+using FeDims = Dims<4, 1, 3, 2, 16, 5, 2, 16>;
+
+template <class D>
+bool dims_match(const DeviceModel& m) {
+  return m.n3a == D::NA && m.l3a == D::LA && m.n3m == D::NM && m.l3m == D::LM && m.nba == D::NB &&
+         m.n2m == D::N2 && m.l2m == D::L2 && m.nbm == D::NBM && m.nfa == D::NFA && m.nfm == D::NFM;
+}
+
+__host__ __device__ constexpr int l_of_h(int h) { return h == 0 ? 0 : (h < 3 ? 1 : (h < 6 ? 2 : (h < 10 ? 3 : 4))); }
+__host__ __device__ constexpr int l_of_lm(int lm) { return lm == 0 ? 0 : (lm < 4 ? 1 : (lm < 9 ? 2 : (lm < 16 ? 3 : 4))); }
+
+// ===========================================================================
+template <class R, class D>
+__global__ void __launch_bounds__(64)
+    k_abasis_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
+                const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
+                const double* __restrict__ magi, const double* __restrict__ mhi, C<R>* __restrict__ F,
+                double* __restrict__ rho1, double* __restrict__ core_out, int* err) {
+  constexpr int TB = 64;
+  static_assert(D::NRY == 16 && D::NB == 16 && D::NQ3 == 18 && D::NQ == 30, "tile shapes assume the Fe layout");
+  extern __shared__ __align__(16) unsigned char smem[];
+  C<R>* sRY = reinterpret_cast<C<R>*>(smem);             // [TB][NRY]
+  C<R>* sQ = sRY + TB * D::NRY;                           // [TB][NQ]
+  R* sg = reinterpret_cast<R*>(sQ + TB * D::NQ);          // [TB][NB]
+  double* score = reinterpret_cast<double*>(sg + TB * D::NB);  // [TB]
+  C<R>* accA = sRY;                                       // reuse after the tiles: [NRY][NQ3]
+  C<R>* accA2 = accA + D::NWA;                            // [NB][NQ]
+  __shared__ double s_core;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int row = lane >> 1, cb = lane & 1;
+
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    C<R> acc[15];
+#pragma unroll
+    for (int c = 0; c < 15; ++c) acc[c] = {R(0), R(0)};
+    if (t == 0) s_core = 0.0;
+    const int b0 = off[atom], b1 = off[atom + 1];
+    for (int t0 = b0; t0 < b1; t0 += TB) {
+      const int nb = min(TB, b1 - t0);
+      __syncthreads();
+      if (t < nb) {
+        const int j = t0 + t;
+        R g[D::NB], Rv[D::NR], Mv[D::NMF], cv[1], dummy[1];
+        R wl = R(0);
+        const int nla = atomic_bin_r<R>(m, to_r<R>(rr[j]), wl, err);
+        if (nla > 0) {
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, R(m.rscale_a), g, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, R(m.rscale_a), Rv, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, R(m.rscale_a), cv, dummy);
+        } else {
+#pragma unroll
+          for (int q = 0; q < D::NB; ++q) g[q] = R(0);
+#pragma unroll
+          for (int q = 0; q < D::NR; ++q) Rv[q] = R(0);
+          cv[0] = R(0);
+        }
+        R wm = R(0);
+        const int nlm = magnetic_bin_r<R>(m, to_r<R>(magj[j]), wm, err);
+        if (nlm > 0) {
+          lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, R(m.rscale_m), Mv, dummy);
+        } else {
+#pragma unroll
+          for (int q = 0; q < D::NMF; ++q) Mv[q] = R(nlm == 0 ? 1 : 0);
+        }
+        C<R> Ya[D::HA], Ym[D::H2];
+        ylm_half<R, false>(D::LA, to_r<R>(ee[3 * j]), to_r<R>(ee[3 * j + 1]), to_r<R>(ee[3 * j + 2]), Ya, nullptr);
+        ylm_half<R, false>(D::L2, to_r<R>(mhj[3 * j]), to_r<R>(mhj[3 * j + 1]), to_r<R>(mhj[3 * j + 2]), Ym, nullptr);
+#pragma unroll
+        for (int n1 = 0; n1 < D::NA; ++n1)
+#pragma unroll
+          for (int lm = 0; lm < D::LSA; ++lm) {
+            const int l = l_of_lm(lm), mm = lm - l * l - l;
+            sRY[t * D::NRY + n1 * D::LSA + lm] = cscale(y_full(Ya, l, mm), Rv[n1 * (D::LA + 1) + l]);
+          }
+#pragma unroll
+        for (int nr = 0; nr < D::N2; ++nr)
+#pragma unroll
+          for (int h = 0; h < D::H2; ++h) sQ[t * D::NQ + nr * D::H2 + h] = cscale(Ym[h], Mv[nr * (D::L2 + 1) + l_of_h(h)]);
+#pragma unroll
+        for (int n = 0; n < D::NB; ++n) sg[t * D::NB + n] = g[n];
+        score[t] = to_d(cv[0]);
+      }
+      __syncthreads();
+      if (warp == 0) {
+        // A[row][9cb .. 9cb+8], row = (n1, l1 m1), column = (n2, l2 m2 >= 0)
+        for (int b = 0; b < nb; ++b) {
+          const C<R> ry = sRY[b * D::NRY + row];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) {
+            const int k3 = 9 * cb + c;
+            const C<R> q = sQ[b * D::NQ + (k3 / D::H3) * D::H2 + k3 % D::H3];
+            acc[c].x += ry.x * q.x - ry.y * q.y;
+            acc[c].y += ry.x * q.y + ry.y * q.x;
+          }
+        }
+      } else {
+        // A2[row][15cb .. 15cb+14], row = n, column = (n', l' m' >= 0)
+        for (int b = 0; b < nb; ++b) {
+          const R gv = sg[b * D::NB + row];
+#pragma unroll
+          for (int c = 0; c < 15; ++c) {
+            const C<R> q = sQ[b * D::NQ + 15 * cb + c];
+            acc[c].x += gv * q.x;
+            acc[c].y += gv * q.y;
+          }
+        }
+      }
+      if (t == 0)
+        for (int b = 0; b < nb; ++b) s_core += score[b];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+      for (int c = 0; c < 9; ++c) accA[row * D::NQ3 + 9 * cb + c] = acc[c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 15; ++c) accA2[row * D::NQ + 15 * cb + c] = acc[c];
+    }
+    __syncthreads();
+    // complete the m' < 0 half by A(m1,m2) = (-1)^(m1+m2) conj A(-m1,-m2) and write F
+    C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
+    constexpr int nA = D::NRY * D::NM * D::LS3;
+    for (int s = t; s < nA; s += blockDim.x) {
+      const int lmm = s % D::LS3, q = s / D::LS3, n2 = q % D::NM, ia = q / D::NM;
+      const int lma = ia % D::LSA;
+      const int l2 = l_of_lm(lmm), m2 = lmm - l2 * l2 - l2;
+      const int l1 = l_of_lm(lma), m1 = lma - l1 * l1 - l1;
+      C<R> v;
+      if (m2 >= 0) {
+        v = accA[ia * D::NQ3 + n2 * D::H3 + ph(l2, m2)];
+      } else {
+        const int ib = ia - lma + (l1 * l1 + l1 - m1);
+        const C<R> w = accA[ib * D::NQ3 + n2 * D::H3 + ph(l2, -m2)];
+        const R sgn = R(parity(m1 + m2));
+        v = {w.x * sgn, -w.y * sgn};
+      }
+      Fa[m.offA + s] = v;
+    }
+    constexpr int nA2 = D::NB * D::N2 * D::LS2;
+    for (int s = t; s < nA2; s += blockDim.x) {
+      const int lm = s % D::LS2, q = s / D::LS2;  // q = n*N2 + nr
+      const int l = l_of_lm(lm), mm = lm - l * l - l;
+      const C<R> w = accA2[(q / D::N2) * D::NQ + (q % D::N2) * D::H2 + ph(l, mm < 0 ? -mm : mm)];
+      C<R> v = w;
+      if (mm < 0) {
+        const R sgn = R(parity(mm));
+        v = {w.x * sgn, -w.y * sgn};
+      }
+      Fa[m.offA2 + s] = v;
+    }
+    if (t == 0) {
+      double wl = 0.0;
+      const int nl = magnetic_bin(m, magi[atom], wl, err);
+      R Mv[D::NMF], gm[D::NBM], dummy[1];
+      if (nl > 0) {
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, R(wl), R(m.rscale_m), Mv, dummy);
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, R(wl), R(m.rscale_m), gm, dummy);
+      } else {
+        for (int q = 0; q < D::NMF; ++q) Mv[q] = R(nl == 0 ? 1 : 0);
+        for (int q = 0; q < D::NBM; ++q) gm[q] = R(nl == 0 ? 1 : 0);
+      }
+      C<R> Yi[D::H2];
+      ylm_half<R, false>(D::L2, R(mhi[3 * atom]), R(mhi[3 * atom + 1]), R(mhi[3 * atom + 2]), Yi, nullptr);
+      for (int nr = 0; nr < D::N2; ++nr)
+        for (int l = 0; l <= D::L2; ++l)
+          for (int mm = -l; mm <= l; ++mm)
+            Fa[m.offA0 + nr * D::LS2 + l * l + l + mm] = cscale(y_full(Yi, l, mm), Mv[nr * (D::L2 + 1) + l]);
+      Fa[m.offOne] = {R(1), R(0)};
+      Fa[m.offZero] = {R(0), R(0)};
+      for (int d = 0; d < m.nd; ++d) {
+        double s = 0.0;
+        for (int n = 0; n < D::NBM; ++n) s += m.c1[d * D::NBM + n] * (static_cast<double>(gm[n]) - 1.0);
+        rho1[static_cast<size_t>(atom) * 2 + d] = s;
+      }
+      core_out[atom] = s_core;
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// k_b3_fe: the 3-body density and its gradient, split precision only.
+//
+// One CTA holds 32 atoms, one per lane, and its warps share out the
+// (combination, m-term) tasks; every lane of a warp runs the same task on its
+// own atom, so all table reads are warp-uniform broadcasts and no lane
+// diverges. The CTA stages the compact half-plane factors of its atoms in
+// shared memory as Xs[element][atom] and accumulates the density gradient in
+// Gs[element][atom]. Tasks of different warps add into the same elements, so
+// the adds are shared-memory atomics: the result carries FP32 rounding that
+// depends on the order in which warps arrive (the FP64 path is bitwise
+// reproducible; this one is reproducible to FP32 rounding). The density is
+// summed per lane in FP64 and its per-warp partials in a fixed order.
+// Outputs: G3[atom][element] (unscaled dRho/dF) and rho3[atom].
+
+constexpr int kB3Warps = 12;
+constexpr int kB3Stride = 33;  // row stride of Xs/Gs in complex elements
+
+// Z[i] = sum_{j allowed} C[i][j] Y[j] and gY[j] += sum_{i allowed} C[i][j] aX[i]
+// over the cluster pairs the enumeration keeps for pattern PAT (0: l1' == l2'
+// keeps (n1,n1') >= (n2,n2'); 1: l1' > l2' keeps n1 >= n2; 2: keeps n1 > n2).
+template <int PAT, int I, int NM>
+__device__ __forceinline__ constexpr int jmax_of(int i) {
+  return PAT == 0 ? i + 1 : (PAT == 1 ? (i / NM + 1) * NM : (i / NM) * NM);
+}
+
+// C rows are I floats, 16-byte aligned when I % 4 == 0: four coefficients per
+// load (a row's trailing coefficients beyond jmax are loaded and not used)
+template <int PAT, class D>
+__device__ __forceinline__ void dense_pass(const float* __restrict__ Cp, const C<float>* Y, const C<float>* X,
+                                           C<float> a, C<float>* aZ, C<float>& ga, C<float>* gY) {
+  constexpr int I = D::I;
+  static_assert(I % 4 == 0, "rows of C are read as float4");
+#pragma unroll
+  for (int i = 0; i < I; ++i) {
+    C<float> z = {0.f, 0.f};
+    const C<float> ax = cmul(a, X[i]);
+    const int jm = jmax_of<PAT, I, D::NM>(i);
+#pragma unroll
+    for (int j4 = 0; j4 < (jm + 3) / 4; ++j4) {
+      const float4 c4 = __ldg(reinterpret_cast<const float4*>(Cp + i * I) + j4);
+      const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = 4 * j4 + u;
+        if (j < jm) {
+          z.x += cv[u] * Y[j].x;
+          z.y += cv[u] * Y[j].y;
+          gY[j].x += cv[u] * ax.x;
+          gY[j].y += cv[u] * ax.y;
+        }
+      }
+    }
+    const C<float> az = cmul(a, z);
+    aZ[i].x += az.x;
+    aZ[i].y += az.y;
+    const C<float> xz = cmul(X[i], z);
+    ga.x += xz.x;
+    ga.y += xz.y;
+  }
+}
+
+// factor of a task position: the compact element with its sign bits applied
+__device__ __forceinline__ C<float> b3_load(const C<float>* Xs, unsigned code, int lane) {
+  const C<float> v = Xs[(code & 0x3fffu) * kB3Stride + lane];
+  return {__uint_as_float(__float_as_uint(v.x) ^ ((code & 0x8000u) << 16)),
+          __uint_as_float(__float_as_uint(v.y) ^ ((code & 0x4000u) << 17))};
+}
+__device__ __forceinline__ void b3_add(C<float>* Gs, unsigned code, int lane, C<float> v, float cf) {
+  if (code & 0xc000u) return;  // mirrored factor: its gradient belongs to the mirror's weight
+  C<float>* g = Gs + code * kB3Stride + lane;
+  atomicAdd(&g->x, cf * v.x);
+  atomicAdd(&g->y, cf * v.y);
+}
+
+template <class D>
+__global__ void __launch_bounds__(kB3Warps * 32, 1)
+    k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ G3,
+            double* __restrict__ rho3) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nc = m.b3_nc;
+  C<float>* Xs = reinterpret_cast<C<float>*>(smem);
+  C<float>* Gs = Xs + nc * kB3Stride;
+  double* rpart = reinterpret_cast<double*>(Gs + nc * kB3Stride);  // [kB3Warps][32]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
+  const int nblk = (natom + 31) / 32;
+
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int a0 = blk * 32;
+    const int na = min(32, natom - a0);
+    // stage: consecutive threads read consecutive elements of one atom
+    for (int t = threadIdx.x; t < 32 * nc; t += blockDim.x) {
+      const int a = t / nc, c = t - a * nc;
+      C<float> v = {0.f, 0.f};
+      if (a < na) v = F[static_cast<size_t>(a0 + a) * m.nF + __ldg(m.b3_factor + c)];
+      Xs[c * kB3Stride + a] = v;
+      Gs[c * kB3Stride + a] = {0.f, 0.f};
+    }
+    __syncthreads();
+    double rloc = 0.0;
+#pragma unroll 1
+    for (int tk = warp; tk < m.b3_ntask; tk += kB3Warps) {
+      const int k = __ldg(m.b3_combo + tk);
+      const int pat = __ldg(m.b3_pattern + k);
+      const float cf = __ldg(m.b3_cff + tk);
+      const uint16_t* code = m.b3_code + tk * NPOS;
+      C<float> X[I], Y[I], aZ[I], gY[I];
+#pragma unroll
+      for (int i = 0; i < I; ++i) {
+        X[i] = b3_load(Xs, __ldg(code + NM + i), lane);
+        Y[i] = b3_load(Xs, __ldg(code + NM + I + i), lane);
+        aZ[i] = {0.f, 0.f};
+        gY[i] = {0.f, 0.f};
+      }
+      const float* Ck = m.b3_Cf + static_cast<size_t>(k) * NM * I * I;
+#pragma unroll 1
+      for (int p = 0; p < NM; ++p) {
+        const unsigned cp = __ldg(code + p);
+        const C<float> a = b3_load(Xs, cp, lane);
+        C<float> ga = {0.f, 0.f};
+        if (pat == 0) dense_pass<0, D>(Ck + p * I * I, Y, X, a, aZ, ga, gY);
+        else if (pat == 1) dense_pass<1, D>(Ck + p * I * I, Y, X, a, aZ, ga, gY);
+        else dense_pass<2, D>(Ck + p * I * I, Y, X, a, aZ, ga, gY);
+        b3_add(Gs, cp, lane, ga, cf);
+      }
+      float rt = 0.f;
+#pragma unroll
+      for (int i = 0; i < I; ++i) {
+        rt += re_mul(X[i], aZ[i]);
+        b3_add(Gs, __ldg(code + NM + i), lane, aZ[i], cf);
+        b3_add(Gs, __ldg(code + NM + I + i), lane, gY[i], cf);
+      }
+      rloc += f2d(cf * rt);
+    }
+    rpart[warp * 32 + lane] = rloc;
+    __syncthreads();
+    for (int t = threadIdx.x; t < 32 * nc; t += blockDim.x) {
+      const int a = t / nc, c = t - a * nc;
+      if (a < na) G3[static_cast<size_t>(a0 + a) * nc + c] = Gs[c * kB3Stride + a];
+    }
+    if (threadIdx.x < na) {
+      double r = 0.0;
+      for (int w = 0; w < kB3Warps; ++w) r += rpart[w * 32 + threadIdx.x];
+      rho3[a0 + threadIdx.x] = r;
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// k_density_fe: one CTA per atom for the 2- and 4-body terms (gather table
+// g2), the density, the embedding, and the weights W = dE/drho * mult *
+// (gather slot totals + the 3-body gradient of k_b3_fe).
+// Shared memory: Fs[nF], part[g2.nseg], tot[g2.nslot] (complex R).
+
+template <class R, class D>
+__global__ void __launch_bounds__(kDensityFeThreads)
+    k_density_fe(DeviceModel m, int natom, const C<R>* __restrict__ F, const double* __restrict__ rho1,
+                 const double* __restrict__ core, const C<R>* __restrict__ G3, const double* __restrict__ rho3,
+                 C<R>* __restrict__ W, double* __restrict__ energy, double* __restrict__ edf_out,
+                 double* __restrict__ dedrho_out, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const GatherView& g = m.g2;
+  C<R>* Fs = reinterpret_cast<C<R>*>(smem);
+  C<R>* part = Fs + ((m.nF + 1) & ~1);
+  C<R>* tot = part + ((g.nseg + 1) & ~1);
+  __shared__ double s_red[kDensityFeThreads / 32];
+  __shared__ double s_dE;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int nc = m.b3_nc;
+
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    const C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
+    for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
+    __syncthreads();
+    // 2- and 4-body terms: segment partials of the gather table
+    for (int gi = warp; gi < g.ngroup; gi += nwarp) {
+      const int a = g.grp_arity[gi], len = g.grp_len[gi], base = g.grp_first[gi] + lane;
+      const int seg = g.grp_seg[gi * 32 + lane];
+      const R* kp = kap_ptr<R>(g, a) + base;
+      const uint32_t* op = g.o12[a] + base;
+      C<R> acc = {R(0), R(0)};
+      for (int e = 0; e < len; ++e) {
+        const uint32_t o = __ldg(op + e * 32);
+        C<R> p = Fs[o & 0xffffu];
+        if (a >= 2) p = cmul(p, Fs[o >> 16]);
+        if (a == 3) p = cmul(p, Fs[__ldg(g.o3 + base + e * 32)]);
+        const R k = __ldg(kp + e * 32);
+        acc.x += k * p.x;
+        acc.y += k * p.y;
+      }
+      if (seg >= 0) part[seg] = acc;
+    }
+    __syncthreads();
+    // slot totals; the A0 slots add to rho
+    double rloc = 0.0;
+    for (int s = threadIdx.x; s < g.nslot; s += blockDim.x) {
+      const int q0 = g.slot_seg[s], q1 = g.slot_seg[s + 1];
+      CSum<R> tx, ty;
+      for (int q = q0; q < q1; ++q) {
+        tx.add(part[q].x);
+        ty.add(part[q].y);
+      }
+      tot[s] = {tx.hi + tx.lo, ty.hi + ty.lo};
+      if (s < g.nG0) {
+        const C<R> f = Fs[g.slot_factor[s]];
+        rloc += to_d(f.x) * tx.value() - to_d(f.y) * ty.value();
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) rloc += __shfl_xor_sync(0xffffffffu, rloc, o);
+    if (lane == 0) s_red[warp] = rloc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double rho = rho1[static_cast<size_t>(atom) * 2] + rho3[atom];
+      for (int w = 0; w < nwarp; ++w) rho += s_red[w];
+      if (!isfinite(rho)) raise_error(err, kDevNaN);
+      double Fd, dFd;
+      embed(m.nfemb, rho, m.par[0][0], m.par[1][0], Fd, dFd);
+      const double e = core[atom], elow = m.ecut - m.decut;
+      double fcut, dfcut;
+      if (e >= m.ecut) {
+        fcut = 0.0;
+        dfcut = 0.0;
+      } else if (e <= elow) {
+        fcut = 1.0;
+        dfcut = 0.0;
+      } else {
+        const double pi = 3.14159265358979323846264338327950288419;
+        fcut = 0.5 * (1.0 + cos(pi * (e - elow) / m.decut));
+        dfcut = -0.5 * sin(pi * (e - elow) / m.decut) * pi / m.decut;
+      }
+      edf_out[atom] = dfcut * Fd + 1.0;
+      s_dE = fcut * dFd;
+      dedrho_out[static_cast<size_t>(atom) * 2] = fcut * dFd;
+      energy[atom] = fcut * Fd + e;
+    }
+    __syncthreads();
+    C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    const C<R>* Ga = G3 + static_cast<size_t>(atom) * nc;
+    const double dE = s_dE;
+    for (int s = threadIdx.x; s < g.nslot; s += blockDim.x) {
+      const int w = g.slot_weight[s];
+      if (w < 0) continue;
+      C<R> v = tot[s];
+      const int c = __ldg(m.b3_cw + w);
+      if (c >= 0) {
+        const C<R> t = Ga[c];
+        v.x += t.x;
+        v.y += t.y;
+      }
+      const R sc = to_r<R>(g.slot_mult[s] * dE);
+      Wa[w] = {v.x * sc, v.y * sc};
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// k_forces_fe: one thread per bond. Weights transposed into shared memory:
+// W2T[k][n] and WAT[k3][i], so the inner loops read 16-byte pairs.
+template <class R, class D>
+__global__ void __launch_bounds__(64)
+    k_forces_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
+                const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
+                const double* __restrict__ magi, const double* __restrict__ mhi, const C<R>* __restrict__ W,
+                const double* __restrict__ edf_in, const double* __restrict__ dedrho, double* __restrict__ fij,
+                double* __restrict__ tij, double* __restrict__ ti0, int* err) {
+  constexpr int T = 64;
+  extern __shared__ __align__(16) unsigned char smem[];
+  C<R>* W2T = reinterpret_cast<C<R>*>(smem);   // [NQ][NB]
+  C<R>* WAT = W2T + D::NQ * D::NB;             // [NQ3][NRY]
+  C<R>* W0s = WAT + D::NQ3 * D::NRY;           // [N2*H2]
+  // per-thread feature columns [feature][T]
+  R* cgd = reinterpret_cast<R*>(W0s + D::NQ + 2);
+  R* cR = cgd + D::NB * T;
+  R* cRd = cR + D::NR * T;
+  R* cM = cRd + D::NR * T;
+  R* cMd = cM + D::NMF * T;
+  C<R>* cYa = reinterpret_cast<C<R>*>(cMd + D::NMF * T);  // full [LSA]
+  C<R>* cdYa = cYa + D::LSA * T;                         // [LSA][3]
+  C<R>* cYm = cdYa + D::LSA * 3 * T;                     // half [H2]
+  const int t = threadIdx.x;
+
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    for (int s = t; s < D::NA2H; s += T) {  // W2[n][k] -> W2T[k][n]
+      const int n = s / D::NQ, k = s % D::NQ;
+      W2T[k * D::NB + n] = Wa[m.offW2 + s];
+    }
+    for (int s = t; s < D::NWA; s += T) {   // WA[i][k3] -> WAT[k3][i]
+      const int i = s / D::NQ3, k3 = s % D::NQ3;
+      WAT[k3 * D::NRY + i] = Wa[s];
+    }
+    for (int s = t; s < D::NQ; s += T) W0s[s] = Wa[m.offW0 + s];
+    __syncthreads();
+    const double edf = edf_in[atom];
+    const int b0 = off[atom], b1 = off[atom + 1];
+    for (int j = b0 + t; j < b1; j += T) {
+      const R r = to_r<R>(rr[j]);
+      const R ex = to_r<R>(ee[3 * j]), ey = to_r<R>(ee[3 * j + 1]), ez = to_r<R>(ee[3 * j + 2]);
+      const R mg = to_r<R>(magj[j]);
+      const R mx = to_r<R>(mhj[3 * j]), my = to_r<R>(mhj[3 * j + 1]), mz = to_r<R>(mhj[3 * j + 2]);
+      R g[D::NB];
+      R cdv = R(0);
+      {
+        R tv[D::NR], td[D::NR], gd[D::NB], cv[1];
+        R wl = R(0);
+        const int nla = atomic_bin_r<R>(m, r, wl, err);
+        if (nla > 0) {
+          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, R(m.rscale_a), g, gd);
+          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, R(m.rscale_a), tv, td);
+          R cd1[1];
+          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, R(m.rscale_a), cv, cd1);
+          cdv = cd1[0];
+        } else {
+#pragma unroll
+          for (int q = 0; q < D::NB; ++q) g[q] = gd[q] = R(0);
+#pragma unroll
+          for (int q = 0; q < D::NR; ++q) tv[q] = td[q] = R(0);
+        }
+#pragma unroll
+        for (int q = 0; q < D::NB; ++q) cgd[q * T + t] = gd[q];
+#pragma unroll
+        for (int q = 0; q < D::NR; ++q) {
+          cR[q * T + t] = tv[q];
+          cRd[q * T + t] = td[q];
+        }
+      }
+      {
+        R mv[D::NMF], Md[D::NMF];
+        R wm = R(0);
+        const int nlm = magnetic_bin_r<R>(m, mg, wm, err);
+        if (nlm > 0) {
+          lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, R(m.rscale_m), mv, Md);
+        } else {
+#pragma unroll
+          for (int q = 0; q < D::NMF; ++q) {
+            mv[q] = R(nlm == 0 ? 1 : 0);
+            Md[q] = R(0);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < D::NMF; ++q) {
+          cM[q * T + t] = mv[q];
+          cMd[q * T + t] = Md[q];
+        }
+      }
+      C<R> Ym[D::H2], dYm[D::H2][3];
+      {
+        C<R> Ya[D::HA], dYa[D::HA][3];
+        ylm_half<R, true>(D::LA, ex, ey, ez, Ya, dYa);
+#pragma unroll
+        for (int lm = 0; lm < D::LSA; ++lm) {
+          const int l = l_of_lm(lm), mm = lm - l * l - l;
+          cYa[lm * T + t] = y_full(Ya, l, mm);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            C<R> d = dYa[ph(l, mm < 0 ? -mm : mm)][c];
+            if (mm < 0) {
+              const R s = R(parity(mm));
+              d = {d.x * s, -d.y * s};
+            }
+            cdYa[(lm * 3 + c) * T + t] = d;
+          }
+        }
+        ylm_half<R, true>(D::L2, mx, my, mz, Ym, dYm);
+#pragma unroll
+        for (int h = 0; h < D::H2; ++h) cYm[h * T + t] = Ym[h];
+      }
+      // ---- force
+      R fr = R(edf) * cdv, ft[3] = {R(0), R(0), R(0)};
+      {
+        R sp[D::NB];
+        C<R> U[D::NRY];
+#pragma unroll
+        for (int n = 0; n < D::NB; ++n) sp[n] = R(0);
+#pragma unroll
+        for (int i = 0; i < D::NRY; ++i) U[i] = {R(0), R(0)};
+#pragma unroll 1
+        for (int nr = 0; nr < D::N2; ++nr)
+#pragma unroll
+          for (int h = 0; h < D::H2; ++h) {
+            const int k = nr * D::H2 + h;
+            const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
+            const C<R>* w2 = W2T + k * D::NB;
+#pragma unroll
+            for (int n = 0; n < D::NB; ++n) sp[n] += re_mul(w2[n], q);
+            if (nr < D::NM && h < D::H3) {
+              const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
+#pragma unroll
+              for (int i = 0; i < D::NRY; ++i) {
+                const C<R> w = wa[i];
+                U[i].x += w.x * q.x - w.y * q.y;
+                U[i].y += w.x * q.y + w.y * q.x;
+              }
+            }
+          }
+#pragma unroll
+        for (int n = 0; n < D::NB; ++n) fr += cgd[n * T + t] * sp[n];
+        const R invr = rcp(r);
+#pragma unroll
+        for (int i = 0; i < D::NRY; ++i) {
+          const int n1 = i / D::LSA, lma = i % D::LSA, l1 = l_of_lm(lma);
+          fr += cRd[(n1 * (D::LA + 1) + l1) * T + t] * re_mul(U[i], cYa[lma * T + t]);
+          const R sc = invr * cR[(n1 * (D::LA + 1) + l1) * T + t];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) ft[c] += sc * re_mul(U[i], cdYa[(lma * 3 + c) * T + t]);
+        }
+      }
+      fij[3 * static_cast<size_t>(j) + 0] = to_d(fr * ex + ft[0]);
+      fij[3 * static_cast<size_t>(j) + 1] = to_d(fr * ey + ft[1]);
+      fij[3 * static_cast<size_t>(j) + 2] = to_d(fr * ez + ft[2]);
+      // ---- magnetic force
+      R tr = R(0), tt[3] = {R(0), R(0), R(0)};
+      {
+        C<R> RY[D::NRY];
+#pragma unroll
+        for (int i = 0; i < D::NRY; ++i) {
+          const int n1 = i / D::LSA, lma = i % D::LSA;
+          RY[i] = cscale(cYa[lma * T + t], cR[(n1 * (D::LA + 1) + l_of_lm(lma)) * T + t]);
+        }
+        const R invm = rcp(mg);
+#pragma unroll 1
+        for (int nr = 0; nr < D::N2; ++nr)
+#pragma unroll
+          for (int h = 0; h < D::H2; ++h) {
+          const int k = nr * D::H2 + h;
+          const C<R>* w2 = W2T + k * D::NB;
+          C<R> V = {R(0), R(0)};
+#pragma unroll
+          for (int n = 0; n < D::NB; ++n) {
+            V.x += g[n] * w2[n].x;
+            V.y += g[n] * w2[n].y;
+          }
+          if (nr < D::NM && h < D::H3) {
+            const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
+#pragma unroll
+            for (int i = 0; i < D::NRY; ++i) {
+              const C<R> w = wa[i];
+              V.x += w.x * RY[i].x - w.y * RY[i].y;
+              V.y += w.x * RY[i].y + w.y * RY[i].x;
+            }
+          }
+          const int q = nr * (D::L2 + 1) + l_of_h(h);
+          tr += cMd[q * T + t] * re_mul(V, Ym[h]);
+          const R sc = invm * cM[q * T + t];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(V, dYm[h][c]);
+        }
+      }
+      tij[3 * static_cast<size_t>(j) + 0] = to_d(tr * mx + tt[0]);
+      tij[3 * static_cast<size_t>(j) + 1] = to_d(tr * my + tt[1]);
+      tij[3 * static_cast<size_t>(j) + 2] = to_d(tr * mz + tt[2]);
+    }
+    if (t == 0) {
+      // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749)
+      const double mg = magi[atom];
+      const double mx = mhi[3 * atom], my = mhi[3 * atom + 1], mz = mhi[3 * atom + 2];
+      double wm = 0.0;
+      const int nl = magnetic_bin(m, mg, wm, err);
+      R Mv[D::NMF], Md[D::NMF], gm[D::NBM], gmd[D::NBM];
+      if (nl > 0) {
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, R(wm), R(m.rscale_m), Mv, Md);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, R(wm), R(m.rscale_m), gm, gmd);
+      } else {
+        for (int q = 0; q < D::NMF; ++q) {
+          Mv[q] = R(nl == 0 ? 1 : 0);
+          Md[q] = R(0);
+        }
+        for (int q = 0; q < D::NBM; ++q) gmd[q] = R(0);
+      }
+      C<R> Yh[D::H2], dYh[D::H2][3];
+      ylm_half<R, true>(D::L2, R(mx), R(my), R(mz), Yh, dYh);
+      double tr = 0.0, tt[3] = {0.0, 0.0, 0.0};
+      const double dE = dedrho[static_cast<size_t>(atom) * 2];
+      for (int n = 0; n < D::NBM; ++n) tr += dE * m.c1[n] * static_cast<double>(gmd[n]);
+      const double invm = 1.0 / mg;
+      for (int k = 0; k < D::NQ; ++k) {
+        const int nr = k / D::H2, h = k % D::H2, q = nr * (D::L2 + 1) + l_of_h(h);
+        const C<R> w = W0s[k];
+        tr += static_cast<double>(Md[q] * re_mul(w, Yh[h]));
+        const R sc = R(invm) * Mv[q];
+        for (int c = 0; c < 3; ++c) tt[c] += static_cast<double>(sc * re_mul(w, dYh[h][c]));
+      }
+      ti0[3 * static_cast<size_t>(atom) + 0] = tr * mx + tt[0];
+      ti0[3 * static_cast<size_t>(atom) + 1] = tr * my + tt[1];
+      ti0[3 * static_cast<size_t>(atom) + 2] = tr * mz + tt[2];
+    }
+    __syncthreads();
+  }
+}
+
+template <class R, class D>
+size_t abasis_fe_smem() {
+  return sizeof(C<R>) * 64 * (D::NRY + D::NQ) + sizeof(R) * 64 * D::NB + sizeof(double) * 64 + 64;
+}
+template <class R, class D>
+size_t density_fe_smem(const DeviceModel& m) {
+  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + ((m.g2.nseg + 1) & ~1) + ((m.g2.nslot + 1) & ~1)) + 64;
+}
+inline size_t b3_fe_smem(const DeviceModel& m) {
+  return sizeof(C<float>) * 2 * static_cast<size_t>(m.b3_nc) * kB3Stride + sizeof(double) * kB3Warps * 32;
+}
+template <class R, class D>
+size_t forces_fe_smem() {
+  return sizeof(C<R>) * (D::NQ * D::NB + D::NQ3 * D::NRY + D::NQ + 2) +
+         sizeof(R) * 64 * (D::NB + 2 * D::NR + 2 * D::NMF) + sizeof(C<R>) * 64 * (D::LSA * 4 + D::H2) + 64;
+}

@@ -369,7 +369,7 @@ struct TermSink {
   }
 };
 
-int build_gather(Model& M, std::string& msg) {
+int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg) {
   const FactorLayout& L = M.L;
   const BasisDims& d = M.pot.dims;
   const int nd = M.ndensity;
@@ -393,7 +393,7 @@ int build_gather(Model& M, std::string& msg) {
   // 3-body: kappa A0(n0',l0',m0') A(n1,l1,m1,n1',l1',m1') A(n2,l1,-m1,n2',l2',m2')
   // with cg<l1 m1 l1 -m1|00> * cg<l0' m0' l1' m1'|l2' -m2'> cg<l2' m2' l2' -m2'|00>
   // (src/b_basis.F90:142-212, src/util.F90:4297-4333)
-  for (size_t c = 0; c < M.rows[3].size(); ++c) {
+  for (size_t c = 0; with_b3 && c < M.rows[3].size(); ++c) {
     const auto& r = M.rows[3][c];
     const int n1 = r[0] - 1, n2 = r[1] - 1, p0 = r[2] - 1, p1 = r[3] - 1, p2 = r[4] - 1;
     const int l1 = r[5], q0 = r[6], q1 = r[7], q2 = r[8];
@@ -459,10 +459,10 @@ int build_gather(Model& M, std::string& msg) {
           }
       }
   }
-  for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
+  if (with_b3)
+    for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
 
   // flatten into segments, then pack segments into warp groups
-  GatherTable& g = M.gt;
   g = GatherTable();
   g.nG0 = L.n2m * L.ls2;
   g.nslot = sink.nslot;
@@ -564,6 +564,99 @@ int build_gather(Model& M, std::string& msg) {
   return MAGACE_OK;
 }
 
+
+// Dense form of the 3-body density (the term of src/b_basis.F90:142-212).
+// For one angular combination (l1, l0', l1', l2') and one m-term
+// (m1, m0', m1', m2'), the 3-body density is
+//   cf * sum_{n0', i, j} C[n0'][i][j] a[n0'] X[i] Y[j]
+// with a = A0(., l0', m0'), X[i] = A(n1, l1, m1, n1', l1', m1'),
+// Y[j] = A(n2, l1, -m1, n2', l2', m2'), i = n1*n3m + n1', j = n2*n3m + n2',
+// and C the cluster coefficients (zero for pairs the enumeration excludes).
+// Every (combination, m-term) is one task of the density kernel.
+void build_dense_b3(Model& M) {
+  const FactorLayout& L = M.L;
+  DenseB3& D = M.db3;
+  D = DenseB3();
+  const int I = L.n3a * L.n3m, NM = L.n3m;
+  D.I = I;
+  D.NM = NM;
+  // combos in order of first appearance in the enumeration
+  std::map<std::array<int, 4>, int> combo_id;
+  for (const auto& r : M.rows[3]) {
+    std::array<int, 4> key{r[5], r[6], r[7], r[8]};
+    if (!combo_id.count(key)) {
+      combo_id[key] = static_cast<int>(D.combo_l.size());
+      D.combo_l.push_back(key);
+    }
+  }
+  D.ncombo = static_cast<int>(D.combo_l.size());
+  D.C.assign(static_cast<size_t>(D.ncombo) * NM * I * I, 0.0);
+  D.pattern.assign(D.ncombo, 0);
+  for (int k = 0; k < D.ncombo; ++k) {
+    const int q1 = D.combo_l[k][2], q2 = D.combo_l[k][3];
+    D.pattern[k] = q1 == q2 ? 0 : (q1 > q2 ? 1 : 2);
+  }
+  for (size_t c = 0; c < M.rows[3].size(); ++c) {
+    const auto& r = M.rows[3][c];
+    const int k = combo_id[{r[5], r[6], r[7], r[8]}];
+    const int i = (r[0] - 1) * NM + (r[3] - 1), j = (r[1] - 1) * NM + (r[4] - 1), p0 = r[2] - 1;
+    D.C[((static_cast<size_t>(k) * NM + p0) * I + i) * I + j] = M.coef[3][c][0];
+  }
+  // compact elements: A half-plane in weight order, then A0(n' < n3m, m' >= 0)
+  D.nc = L.nWA + NM * L.h3;
+  D.factor_of.assign(D.nc, 0);
+  D.compact_of_weight.assign(L.nW, -1);
+  for (int n = 0; n < L.n3a; ++n)
+    for (int l = 0; l <= L.l3a; ++l)
+      for (int m = -l; m <= l; ++m)
+        for (int p = 0; p < NM; ++p)
+          for (int q = 0; q <= L.l3m; ++q)
+            for (int u = 0; u <= q; ++u) {
+              const int c = L.WA(n, l, m, p, q, u);
+              D.factor_of[c] = L.A(n, l, m, p, q, u);
+              D.compact_of_weight[c] = c;
+            }
+  for (int p = 0; p < NM; ++p)
+    for (int q = 0; q <= L.l3m; ++q)
+      for (int u = 0; u <= q; ++u) {
+        const int c = L.nWA + p * L.h3 + q * (q + 1) / 2 + u;
+        D.factor_of[c] = L.A0(p, q, u);
+        D.compact_of_weight[L.W0(p, q, u)] = c;
+      }
+  // (-1)^k conj(mirror) as sign bits: negate real part if odd k, else imaginary
+  const auto mirrored = [](int c, int k) {
+    return static_cast<uint16_t>(c | ((k & 1) ? 0x8000 : 0x4000));
+  };
+  const auto code_A = [&](int n, int l, int m, int p, int q, int u) {
+    return u >= 0 ? static_cast<uint16_t>(L.WA(n, l, m, p, q, u)) : mirrored(L.WA(n, l, -m, p, q, -u), m + u);
+  };
+  const auto code_A0 = [&](int p, int q, int u) {
+    const int c = L.nWA + p * L.h3 + q * (q + 1) / 2 + std::abs(u);
+    return u >= 0 ? static_cast<uint16_t>(c) : mirrored(c, u);
+  };
+  for (int k = 0; k < D.ncombo; ++k) {
+    const int l1 = D.combo_l[k][0], q0 = D.combo_l[k][1], q1 = D.combo_l[k][2], q2 = D.combo_l[k][3];
+    for (int m1 = -l1; m1 <= l1; ++m1) {
+      const double cfa = clebsch_gordan(l1, l1, 0, m1, -m1, 0);
+      for (int u0 = -q0; u0 <= q0; ++u0)
+        for (int u1 = -q1; u1 <= q1; ++u1) {
+          const int u2 = -(u0 + u1);
+          if (std::abs(u2) > q2) continue;
+          const double cf = cfa * (clebsch_gordan(q0, q1, q2, u0, u1, -u2) * clebsch_gordan(q2, q2, 0, u2, -u2, 0));
+          if (cf == 0.0) continue;
+          ++D.ntask;
+          D.task_combo.push_back(k);
+          D.task_cf.push_back(cf);
+          for (int p = 0; p < NM; ++p) D.code.push_back(code_A0(p, q0, u0));
+          for (int n = 0; n < L.n3a; ++n)
+            for (int p = 0; p < NM; ++p) D.code.push_back(code_A(n, l1, m1, p, q1, u1));
+          for (int n = 0; n < L.n3a; ++n)
+            for (int p = 0; p < NM; ++p) D.code.push_back(code_A(n, l1, -m1, p, q2, u2));
+        }
+    }
+  }
+}
+
 }  // namespace
 
 int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& M, std::string& msg) {
@@ -658,8 +751,15 @@ int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& 
   for (size_t c = 0; c < M.rows[1].size(); ++c)
     for (int dd = 0; dd < 2; ++dd) M.c1[dd][M.rows[1][c][0] - 1] += M.coef[1][c][dd];
 
-  int st = build_gather(M, msg);
+  int st = build_gather(M, true, M.gt, msg);
   if (st) return st;
+  // tables of the specialised kernels: 3-body terms as dense per-(combo, m)
+  // contractions, everything else through the gather table without them
+  if (M.ndensity == 1) {
+    st = build_gather(M, false, M.gt_nob3, msg);
+    if (st) return st;
+    build_dense_b3(M);
+  }
   if (!build_lut(M, M.lut)) {
     msg = "unsupported radial basis type";
     return MAGACE_ERR_UNSUPPORTED;

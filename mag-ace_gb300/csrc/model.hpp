@@ -16,6 +16,7 @@
 //   W0  [n2m][h2]
 #pragma once
 
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -77,6 +78,29 @@ struct GatherTable {
   std::vector<double> slot_mult;     // half-plane multiplicity applied to the weight
 };
 
+// Dense tables of the 3-body density for the specialised kernels (see
+// build_dense_b3 in model.cpp). C is [combo][n0'][i][j], tasks are
+// (combination, m-term) pairs with their coupling cf. The kernel keeps the
+// half-plane factors the 3-body terms read (A with m' >= 0, then A0 with
+// n' < n3m and m' >= 0: `nc` "compact" elements) and accumulates the
+// gradient of the density with respect to the same elements. code[task][pos]
+// addresses the factor a[NM], X[I], Y[I] of each task position: bits 0-13
+// the compact element, bit 15 negates its real part and bit 14 its imaginary
+// part (a factor with m' < 0 is (-1)^(m+m') times the conjugate of its
+// mirror). Positions whose code has no sign bits are half-plane elements
+// themselves and receive their gradient.
+struct DenseB3 {
+  int I = 0, NM = 0, ncombo = 0, ntask = 0, nc = 0;
+  std::vector<std::array<int, 4>> combo_l;  // (l1, l0', l1', l2')
+  std::vector<int32_t> pattern;             // 0: l1' == l2', 1: l1' > l2', 2: l1' < l2'
+  std::vector<double> C;
+  std::vector<int32_t> task_combo;
+  std::vector<double> task_cf;
+  std::vector<uint16_t> code;               // [ntask][NM + 2I]
+  std::vector<int32_t> factor_of;           // [nc] factor index of each compact element
+  std::vector<int32_t> compact_of_weight;   // [nW] compact element of each weight, or -1
+};
+
 struct RadialLUT {
   int nlut = 0;
   int nfa = 0;  // atomic: g_n (nba), R_nl (n3a*(l3a+1), index nr*(l3a+1)+l), core (1)
@@ -99,7 +123,9 @@ struct Model {
   int unmatched_records = 0;
   long nterms[5] = {0, 0, 0, 0, 0};
   std::vector<double> c1[2];  // 1-body coefficient per magnetic radial function n
-  GatherTable gt;
+  GatherTable gt;        // every term (generic kernels)
+  GatherTable gt_nob3;   // every term except the 3-body ones (specialised kernels)
+  DenseB3 db3;           // 3-body terms in dense form (specialised kernels)
   RadialLUT lut;
   bool ready = false;
 };

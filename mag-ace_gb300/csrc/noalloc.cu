@@ -4,10 +4,10 @@
 // evaluate the potential: code running inside a memory pool or allocator
 // they do not own, real-time MD drivers that forbid allocation after set-up,
 // or hosts whose device allocator is disabled in the evaluation phase. For
-// them, ace_compute_device_noalloc runs the same three kernels as
+// them, ace_compute_device_noalloc runs the same kernels as
 // ace_compute_device, but its per-atom scratch (the factor array F, the
-// weight array W and the per-atom density, core energy and embedding
-// derivatives) lives in one fixed file-scope device array instead of
+// weight array W, the per-atom density, core energy and embedding
+// derivatives, and the 3-body scratch of the split-precision kernels) lives in one fixed file-scope device array instead of
 // library-allocated buffers. The caller still passes the inputs and outputs.
 #include <cuda_runtime.h>
 
@@ -84,8 +84,11 @@ extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_of
   off += round256(na * sizeof(double));
   const size_t o_dedrho = off;
   off += round256(na * 2 * sizeof(double));
+  const size_t o_aux = off;
+  const size_t aux_bytes = eval_aux_bytes(dm, precision, natom);
+  off += round256(aux_bytes);
   if (off > kScratchBytes) {
-    const size_t per_atom = dm.nF * csz + dm.nW * csz + 6 * sizeof(double);
+    const size_t per_atom = dm.nF * csz + dm.nW * csz + 6 * sizeof(double) + (na ? aux_bytes / na : 0);
     static char msg[160];
     snprintf(msg, sizeof(msg), "natom = %d exceeds the allocation-free scratch (64 MiB, about %zu atoms for this potential and precision)",
              natom, (kScratchBytes - 2048) / per_atom);
@@ -118,6 +121,7 @@ extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_of
   b.edf = reinterpret_cast<double*>(base + o_edf);
   b.dedrho = reinterpret_cast<double*>(base + o_dedrho);
   b.err = err;
+  b.aux = aux_bytes ? base + o_aux : nullptr;
   const int n = precision == 0 ? launch_eval_fp64(dm, b, s, grid_cap, nullptr) : launch_eval_fp32(dm, b, s, grid_cap, nullptr);
   runtime_set_launches(n);
   ce = cudaGetLastError();

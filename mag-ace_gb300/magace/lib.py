@@ -150,18 +150,26 @@ def set_kernel_timing(on: bool) -> None:
     _check(load().ace_set_kernel_timing(1 if on else 0))
 
 
+def kernel_names(n: int) -> list:
+    """Names of the kernels of an evaluation that launched n of them."""
+    return ["k_abasis", "k_b3", "k_density", "k_forces"] if n == 4 else ["k_abasis", "k_density", "k_forces"]
+
+
 def kernel_times() -> list:
-    """Per-kernel durations (ms) of the last evaluation: [k_abasis, k_density, k_forces]."""
-    out = (ctypes.c_float * 3)()
+    """Per-kernel durations (ms) of the last evaluation, in launch order
+    (kernel_names(last_launch_count()))."""
+    out = (ctypes.c_float * 4)()
     _check(load().ace_kernel_times(out))
-    return [float(x) for x in out]
+    return [float(x) for x in out][:last_launch_count()]
 
 
 def table_stats() -> dict:
-    out = (ctypes.c_longlong * 21)()
+    out = (ctypes.c_longlong * 30)()
     _check(load().ace_table_stats(out))
     keys = ["ne1", "ne2", "ne3", "nseg", "nslot", "nF", "nW", "nWA", "nA2h", "nfa", "nfm",
-            "nba", "nbm", "n2m", "l2m", "n3a", "n3m", "l3a", "l3m", "h2", "h3"]
+            "nba", "nbm", "n2m", "l2m", "n3a", "n3m", "l3a", "l3m", "h2", "h3",
+            "b3_tasks", "b3_combos", "b3_elements", "rest_segments", "rest_entries",
+            "rest_ne1", "rest_ne2", "rest_ne3", "b3_pairs"]
     return {k: int(v) for k, v in zip(keys, out)}
 
 

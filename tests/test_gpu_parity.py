@@ -187,21 +187,41 @@ def test_device_api_matches_acelib(gpu_lib):
     assert gpu_lib.last_launch_count() == 3
 
 
-def test_split_precision_accuracy(gpu_lib, oracle_seeded):
+def _ragged_slab():
+    from magace import structures as S
+    rng = np.random.default_rng(7)
+    pos, cell = S.bcc_cubic(3, 3, 3, 2.83)
+    pos = pos + rng.normal(0, 0.08, pos.shape)
+    pos = pos[rng.random(len(pos)) > 0.1]
+    pos = np.vstack([pos, [[4.0, 4.0, 40.0]]])
+    n = len(pos)
+    return S.Structure(pos, cell, (True, True, False), rng.uniform(1.5, 2.6, n), S.random_unit(rng, n))
+
+
+@pytest.mark.parametrize("case", ["bcc128", "bcc54", "slab"])
+def test_split_precision_accuracy(gpu_lib, oracle_seeded, case):
     """The split path (FP32 features, products and weights; FP64 density,
     energy and embedding) stays within 1 meV/atom and 10 meV/A of the FP64
-    oracle on the 128-atom cell."""
+    oracle; atom counts that are not multiples of the 32-atom tiles of the
+    3-body kernel and an atom without neighbours included. The norm-relative
+    bounds (1e-5) are far below those limits and catch a wrong sign or a
+    missing term in any one part of the basis."""
     from magace import structures as S
-    nb = S.neighbor_data(S.bcc_fe_128(1), 5.0)
+    st = {"bcc128": lambda: S.bcc_fe_128(1), "bcc54": lambda: S.bcc_fe_54(2), "slab": _ragged_slab}[case]()
+    nb = S.neighbor_data(st, 5.0)
     gpu_lib.set_precision(1)
     try:
         e, f, t, t0 = gpu_lib.acelib(nb)
     finally:
         gpu_lib.set_precision(0)
     eo, fo, to, t0o = oracle_seeded.acelib(nb)
+    print(case, "max |dE| meV/atom", np.abs(e - eo).max() * 1e3, "max |dF| meV/A", np.abs(f - fo).max() * 1e3,
+          "rel", rel_err(e, eo), rel_err(f, fo), rel_err(t, to), rel_err(t0, t0o))
     assert np.abs(e - eo).max() * 1e3 < 1.0
     assert np.abs(f - fo).max() * 1e3 < 10.0
     assert np.abs(t - to).max() * 1e3 < 10.0 and np.abs(t0 - t0o).max() * 1e3 < 10.0
+    for got, ref in ((e, eo), (f, fo), (t, to), (t0, t0o)):
+        assert rel_err(got, ref) < 1e-5
 
 
 @pytest.mark.parametrize("mode", ["copy", "pinned", "direct"])
