@@ -125,7 +125,7 @@ int ace_last_launch_count(void);
  * are recorded with CUDA events on the evaluation stream; ace_kernel_times
  * writes the last evaluation's per-kernel durations in ms into ms[0..3],
  * synchronising on the last event: k_abasis, k_density, k_forces (3
- * kernels), or k_abasis, k_b3, k_density, k_forces when the split-precision
+ * kernels), or k_abasis, k_density, k_b3, k_forces when the split-precision
  * path runs its 3-body terms as a kernel of their own (4 kernels, see
  * ace_last_launch_count). Entries beyond the kernel count are 0. */
 int ace_set_kernel_timing(int on);

@@ -92,7 +92,7 @@ struct Runtime {
       for (auto* b : {&grp_arity, &grp_len, &grp_first, &grp_seg, &slot_seg, &slot_factor, &slot_weight}) b->release();
     }
   } gb1, gb2;
-  DevBuf<float> b3_Cf, b3_cff;
+  DevBuf<float> b3_Cf, b3_cff, b3_mult;
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
   DevBuf<uint16_t> b3_code;
   DeviceModel dm{};
@@ -235,6 +235,7 @@ int upload_tables() {
       CUDA_TRY(R.b3_code.upload(D.code));
       CUDA_TRY(R.b3_factor.upload(D.factor_of));
       CUDA_TRY(R.b3_cw.upload(D.compact_of_weight));
+      CUDA_TRY(R.b3_mult.upload(to_float(D.mult)));
     } else {
       R.dm.g2 = R.dm.g;
     }
@@ -276,6 +277,7 @@ int upload_tables() {
   d.b3_code = R.b3_code.p;
   d.b3_factor = R.b3_factor.p;
   d.b3_cw = R.b3_cw.p;
+  d.b3_mult = R.b3_mult.p;
   int sms = 0;
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   R.grid_cap = std::max(1, sms) * 64;
@@ -613,7 +615,7 @@ void ace_release_device(void) {
   for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.r, &R.e, &R.magj, &R.mhj, &R.magi, &R.mhi, &R.energy, &R.fij,
                   &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
     b->release();
-  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff}) b->release();
+  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult}) b->release();
   for (auto* b : {&R.b3_pattern, &R.b3_combo, &R.b3_factor, &R.b3_cw}) b->release();
   R.b3_code.release();
   R.gb1.release();

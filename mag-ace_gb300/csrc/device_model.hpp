@@ -69,6 +69,7 @@ struct DeviceModel {
   const uint16_t* b3_code;    // [task][NM + 2I] compact element | sign bits
   const int32_t* b3_factor;   // [nc] factor index of each compact element
   const int32_t* b3_cw;       // [nW] compact element of each weight, or -1
+  const float* b3_mult;       // [nc] half-plane multiplicity of each element's weight
 };
 
 }  // namespace magace

@@ -901,13 +901,6 @@ size_t forces_smem(const DeviceModel& m, int T) {
   return sizeof(C<R>) * nc + sizeof(R) * nr + 64;
 }
 
-// k_b3_fe's outputs in EvalBuffers::aux: G3 [natom][nc] complex float, then
-// rho3 [natom] double at the next 256-byte boundary
-size_t b3_g3_bytes(const DeviceModel& m, int natom) {
-  const size_t g = sizeof(C<float>) * static_cast<size_t>(m.b3_nc) * static_cast<size_t>(natom);
-  return (g + 255) & ~static_cast<size_t>(255);
-}
-
 // Whether the compile-time specialised kernels apply: the basis has the Fe
 // layout and one density, and MAGACE_GENERIC is not set.
 bool use_specialised(const DeviceModel& m) {
@@ -918,30 +911,28 @@ bool use_specialised(const DeviceModel& m) {
   return !forced_generic && m.nd == 1 && dims_match<FeDims>(m);
 }
 
-// The density phase: in split precision with the specialised layout, k_b3_fe
-// (3-body terms, 32 atoms per CTA) and then k_density_fe (the rest, the
-// embedding and the weights); otherwise one generic k_density. Returns the
-// number of kernels launched.
+// The density phase: in split precision with the specialised layout,
+// k_density_fe (2- and 4-body terms, one CTA per atom) and then k_b3_fe
+// (3-body terms, 32 atoms per CTA; embedding and weights); otherwise one
+// generic k_density. Returns the number of kernels launched.
 template <class R>
 int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid, int grid_cap, bool fe,
                    cudaEvent_t ev_between) {
   const int natom = b.natom;
   if constexpr (sizeof(R) == 4) {
     if (fe) {
-      C<float>* G3 = static_cast<C<float>*>(b.aux);
-      double* rho3 = reinterpret_cast<double*>(static_cast<unsigned char*>(b.aux) + b3_g3_bytes(m, natom));
-      const size_t sb = b3_fe_smem(m);
+      double* rho_rest = static_cast<double*>(b.aux);
+      const size_t s2 = density_fe_smem(m);
+      cudaFuncSetAttribute(k_density_fe<FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
+      k_density_fe<FeDims><<<grid, kDensityFeThreads, s2, st>>>(m, natom, reinterpret_cast<const C<float>*>(b.F),
+                                                                reinterpret_cast<C<float>*>(b.W), rho_rest);
+      if (ev_between) cudaEventRecord(ev_between, st);
+      const size_t sb = b3_fe_smem<FeDims>(m);
       cudaFuncSetAttribute(k_b3_fe<FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb));
       const int nblk = (natom + 31) / 32;
       k_b3_fe<FeDims><<<nblk < grid_cap ? nblk : grid_cap, kB3Warps * 32, sb, st>>>(
-          m, natom, reinterpret_cast<const C<float>*>(b.F), G3, rho3);
-      if (ev_between) cudaEventRecord(ev_between, st);
-      const size_t s2 = density_fe_smem<float, FeDims>(m);
-      cudaFuncSetAttribute(k_density_fe<float, FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(s2));
-      k_density_fe<float, FeDims><<<grid, kDensityFeThreads, s2, st>>>(
-          m, natom, reinterpret_cast<const C<float>*>(b.F), b.rho1, b.core, G3, rho3,
-          reinterpret_cast<C<float>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
+          m, natom, reinterpret_cast<const C<float>*>(b.F), reinterpret_cast<C<float>*>(b.W), b.rho1, rho_rest,
+          b.core, b.energy, b.edf, b.dedrho, b.err);
       return 2;
     }
   }
@@ -998,8 +989,9 @@ int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int
 }
 
 size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom) {
+  // k_density_fe's per-atom 2- and 4-body density, read by k_b3_fe
   if (precision == 0 || !use_specialised(m) || natom <= 0) return 0;
-  return b3_g3_bytes(m, natom) + sizeof(double) * static_cast<size_t>(natom);
+  return sizeof(double) * static_cast<size_t>(natom);
 }
 
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
@@ -1011,7 +1003,7 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
     }
     if (which == 0) return abasis_fe_smem<float, FeDims>();
     if (which == 1) {
-      const size_t a = density_fe_smem<float, FeDims>(m), b = b3_fe_smem(m);
+      const size_t a = density_fe_smem(m), b = b3_fe_smem<FeDims>(m);
       return a > b ? a : b;
     }
     return forces_fe_smem<float, FeDims>();

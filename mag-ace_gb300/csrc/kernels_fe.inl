@@ -8,10 +8,13 @@
 // unroll and their operands stay in registers:
 //   k_abasis_fe  the bond sums A and A2 are small GEMMs over the bonds of an
 //                atom; warp 0 owns 1 x 9 tiles of A, warp 1 1 x 15 tiles of A2.
-//   k_density_fe the 3-body density and weights as dense contractions per
+//   k_density_fe the 2- and 4-body terms through the gather table (split
+//                precision; FP64 uses the generic k_density).
+//   k_b3_fe      the 3-body density and weights as dense contractions per
 //                (angular combination, m-term) task, C[n0'][i][j] a X Y,
-//                exploiting the triangular cluster order; the 2- and 4-body
-//                terms go through the gather table.
+//                exploiting the triangular cluster order, with 32 atoms
+//                in the lanes of each warp; then the embedding and the
+//                final weights of those atoms.
 //   k_forces_fe  per bond, U = W_A Q and V = W2 g + W_A^T RY with the
 //                weights transposed in shared memory for 16-byte loads.
 
@@ -213,65 +216,116 @@ __global__ void __launch_bounds__(64)
 }
 
 // ===========================================================================
-// k_b3_fe: the 3-body density and its gradient, split precision only.
+// The split-precision density phase of the specialised layout, two kernels:
 //
-// One CTA holds 32 atoms, one per lane, and its warps share out the
-// (combination, m-term) tasks; every lane of a warp runs the same task on its
-// own atom, so all table reads are warp-uniform broadcasts and no lane
-// diverges. The CTA stages the compact half-plane factors of its atoms in
-// shared memory as Xs[element][atom] and accumulates the density gradient in
-// Gs[element][atom]. Tasks of different warps add into the same elements, so
-// the adds are shared-memory atomics: the result carries FP32 rounding that
-// depends on the order in which warps arrive (the FP64 path is bitwise
-// reproducible; this one is reproducible to FP32 rounding). The density is
-// summed per lane in FP64 and its per-warp partials in a fixed order.
-// Outputs: G3[atom][element] (unscaled dRho/dF) and rho3[atom].
+// k_density_fe (one CTA per atom) evaluates the 2- and 4-body terms through
+// the gather table g2 and writes, per atom, their density rho_rest and the
+// unscaled weights mult * dRho_rest/dF into W.
+//
+// k_b3_fe (32 atoms per CTA, one per lane) evaluates the 3-body terms as
+// dense contractions per (angular combination, m-term) task, then finishes
+// each atom in its lane: rho = rho1 + rho_rest + rho3, the embedding and
+// energy in FP64 (a full warp of atoms per FP64 instruction), and the final
+// weights W = dE/drho * (W + mult * dRho3/dF).
 
-constexpr int kB3Warps = 12;
+// Global loads of the staging and weight loops are issued kBatch at a time,
+// so that each thread has that many in flight.
+constexpr int kBatch = 8;
+
+// k_density_fe. Shared memory: Fs[nF], part[g2.nseg] (complex float).
+template <class D>
+__global__ void __launch_bounds__(kDensityFeThreads)
+    k_density_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
+                 double* __restrict__ rho_rest) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const GatherView& g = m.g2;
+  C<float>* Fs = reinterpret_cast<C<float>*>(smem);
+  C<float>* part = Fs + ((m.nF + 1) & ~1);
+  __shared__ double s_red[kDensityFeThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+
+  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+    const C<float>* Fa = F + static_cast<size_t>(atom) * m.nF;
+    for (int s0 = 0; s0 < m.nF; s0 += kBatch * kDensityFeThreads) {
+      C<float> v[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int s = s0 + b * kDensityFeThreads + threadIdx.x;
+        if (s < m.nF) v[b] = Fa[s];
+      }
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int s = s0 + b * kDensityFeThreads + threadIdx.x;
+        if (s < m.nF) Fs[s] = v[b];
+      }
+    }
+    __syncthreads();
+    // segment partials of the gather table
+    for (int gi = warp; gi < g.ngroup; gi += nwarp) {
+      const int a = g.grp_arity[gi], len = g.grp_len[gi], base = g.grp_first[gi] + lane;
+      const int seg = g.grp_seg[gi * 32 + lane];
+      const float* kp = g.kapf[a] + base;
+      const uint32_t* op = g.o12[a] + base;
+      C<float> acc = {0.f, 0.f};
+      for (int e = 0; e < len; ++e) {
+        const uint32_t o = __ldg(op + e * 32);
+        C<float> p = Fs[o & 0xffffu];
+        if (a >= 2) p = cmul(p, Fs[o >> 16]);
+        if (a == 3) p = cmul(p, Fs[__ldg(g.o3 + base + e * 32)]);
+        const float k = __ldg(kp + e * 32);
+        acc.x += k * p.x;
+        acc.y += k * p.y;
+      }
+      if (seg >= 0) part[seg] = acc;
+    }
+    __syncthreads();
+    // slot totals (compensated, in segment order): unscaled weights, and the
+    // A0 slots' density terms
+    CSum<float> rs;
+    C<float>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    for (int s = threadIdx.x; s < g.nslot; s += blockDim.x) {
+      const int q0 = g.slot_seg[s], q1 = g.slot_seg[s + 1];
+      CSum<float> tx, ty;
+      for (int q = q0; q < q1; ++q) {
+        tx.add(part[q].x);
+        ty.add(part[q].y);
+      }
+      const float vx = tx.hi + tx.lo, vy = ty.hi + ty.lo;
+      if (s < g.nG0) {
+        const C<float> f = Fs[g.slot_factor[s]];
+        rs.add(f.x * vx);
+        rs.add(-f.y * vy);
+      }
+      const int w = g.slot_weight[s];
+      if (w >= 0) {
+        const float mu = static_cast<float>(g.slot_mult[s]);
+        Wa[w] = {vx * mu, vy * mu};
+      }
+    }
+    double rloc = f2d(rs.hi) + f2d(rs.lo);
+    if (warp * 32 < g.nG0) {  // only these warps hold density terms
+      for (int o = 16; o > 0; o >>= 1) rloc += __shfl_xor_sync(0xffffffffu, rloc, o);
+    }
+    if (lane == 0) s_red[warp] = rloc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double r = 0.0;
+      for (int w = 0; w * 32 < g.nG0 && w < nwarp; ++w) r += s_red[w];
+      rho_rest[atom] = r;
+    }
+    __syncthreads();
+  }
+}
+
+constexpr int kB3Warps = 16;
 constexpr int kB3Stride = 33;  // row stride of Xs/Gs in complex elements
 
-// Z[i] = sum_{j allowed} C[i][j] Y[j] and gY[j] += sum_{i allowed} C[i][j] aX[i]
-// over the cluster pairs the enumeration keeps for pattern PAT (0: l1' == l2'
-// keeps (n1,n1') >= (n2,n2'); 1: l1' > l2' keeps n1 >= n2; 2: keeps n1 > n2).
+// pairs (i, j) the enumeration keeps for pattern PAT (0: l1' == l2' keeps
+// (n1,n1') >= (n2,n2'); 1: l1' > l2' keeps n1 >= n2; 2: keeps n1 > n2),
+// as the j bound of row i
 template <int PAT, int I, int NM>
 __device__ __forceinline__ constexpr int jmax_of(int i) {
   return PAT == 0 ? i + 1 : (PAT == 1 ? (i / NM + 1) * NM : (i / NM) * NM);
-}
-
-// C rows are I floats, 16-byte aligned when I % 4 == 0: four coefficients per
-// load (a row's trailing coefficients beyond jmax are loaded and not used)
-template <int PAT, class D>
-__device__ __forceinline__ void dense_pass(const float* __restrict__ Cp, const C<float>* Y, const C<float>* X,
-                                           C<float> a, C<float>* aZ, C<float>& ga, C<float>* gY) {
-  constexpr int I = D::I;
-  static_assert(I % 4 == 0, "rows of C are read as float4");
-#pragma unroll
-  for (int i = 0; i < I; ++i) {
-    C<float> z = {0.f, 0.f};
-    const C<float> ax = cmul(a, X[i]);
-    const int jm = jmax_of<PAT, I, D::NM>(i);
-#pragma unroll
-    for (int j4 = 0; j4 < (jm + 3) / 4; ++j4) {
-      const float4 c4 = __ldg(reinterpret_cast<const float4*>(Cp + i * I) + j4);
-      const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int j = 4 * j4 + u;
-        if (j < jm) {
-          z.x += cv[u] * Y[j].x;
-          z.y += cv[u] * Y[j].y;
-          gY[j].x += cv[u] * ax.x;
-          gY[j].y += cv[u] * ax.y;
-        }
-      }
-    }
-    const C<float> az = cmul(a, z);
-    aZ[i].x += az.x;
-    aZ[i].y += az.y;
-    const C<float> xz = cmul(X[i], z);
-    ga.x += xz.x;
-    ga.y += xz.y;
-  }
 }
 
 // factor of a task position: the compact element with its sign bits applied
@@ -280,36 +334,135 @@ __device__ __forceinline__ C<float> b3_load(const C<float>* Xs, unsigned code, i
   return {__uint_as_float(__float_as_uint(v.x) ^ ((code & 0x8000u) << 16)),
           __uint_as_float(__float_as_uint(v.y) ^ ((code & 0x4000u) << 17))};
 }
+// gradient of a task position; a mirrored factor's gradient belongs to the
+// mirror's weight and is dropped, as the half-plane multiplicities count it
 __device__ __forceinline__ void b3_add(C<float>* Gs, unsigned code, int lane, C<float> v, float cf) {
-  if (code & 0xc000u) return;  // mirrored factor: its gradient belongs to the mirror's weight
+  if (code & 0xc000u) return;
   C<float>* g = Gs + code * kB3Stride + lane;
   atomicAdd(&g->x, cf * v.x);
   atomicAdd(&g->y, cf * v.y);
 }
 
+// One task on the lane's atom: the density term cf * sum C[p][i][j] a_p X_i Y_j
+// (returned) and its gradient, added into Gs. Cs points at the combination's
+// coefficients [NM][I][I] in shared memory; rows are read four at a time.
+template <int PAT, class D>
+__device__ __forceinline__ float b3_task(const float* __restrict__ Cs, const C<float>* Xs, C<float>* Gs,
+                                         const uint16_t* __restrict__ code, float cf, int lane) {
+  constexpr int I = D::I, NM = D::NM;
+  static_assert(I % 4 == 0, "rows of C are read as float4");
+  constexpr int JUSED = jmax_of<PAT, I, NM>(I - 1);  // largest j bound (rows grow with i)
+  C<float> Y[I], gY[I], a[NM], ga[NM];
+#pragma unroll
+  for (int j = 0; j < I; ++j) {
+    Y[j] = j < JUSED ? b3_load(Xs, __ldg(code + NM + I + j), lane) : C<float>{0.f, 0.f};
+    gY[j] = {0.f, 0.f};
+  }
+#pragma unroll
+  for (int p = 0; p < NM; ++p) {
+    a[p] = b3_load(Xs, __ldg(code + p), lane);
+    ga[p] = {0.f, 0.f};
+  }
+  float rt = 0.f;
+#pragma unroll
+  for (int i = 0; i < I; ++i) {
+    const int jm = jmax_of<PAT, I, NM>(i);
+    if (jm == 0) continue;
+    const unsigned cx = __ldg(code + NM + i);
+    const C<float> x = b3_load(Xs, cx, lane);
+    C<float> az = {0.f, 0.f};
+#pragma unroll
+    for (int p = 0; p < NM; ++p) {
+      C<float> z = {0.f, 0.f};
+      const C<float> ax = cmul(a[p], x);
+      const float4* crow = reinterpret_cast<const float4*>(Cs + (p * I + i) * I);
+#pragma unroll
+      for (int j4 = 0; j4 < (jm + 3) / 4; ++j4) {
+        const float4 c4 = crow[j4];
+        const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = 4 * j4 + u;
+          if (j < jm) {
+            z.x += cv[u] * Y[j].x;
+            z.y += cv[u] * Y[j].y;
+            gY[j].x += cv[u] * ax.x;
+            gY[j].y += cv[u] * ax.y;
+          }
+        }
+      }
+      const C<float> t = cmul(a[p], z);
+      az.x += t.x;
+      az.y += t.y;
+      const C<float> u = cmul(x, z);
+      ga[p].x += u.x;
+      ga[p].y += u.y;
+    }
+    rt += re_mul(x, az);
+    b3_add(Gs, cx, lane, az, cf);
+  }
+#pragma unroll
+  for (int j = 0; j < JUSED; ++j) b3_add(Gs, __ldg(code + NM + I + j), lane, gY[j], cf);
+#pragma unroll
+  for (int p = 0; p < NM; ++p) b3_add(Gs, __ldg(code + p), lane, ga[p], cf);
+  return cf * rt;
+}
+
+// k_b3_fe. Shared memory: Cs (all combinations' coefficients), Xs[nc][33]
+// (the CTA's factors, element-major), Gs[nc][33] (their density gradient),
+// the per-warp density partials, the atoms' dE/drho, and the element and
+// weight maps.
+
 template <class D>
 __global__ void __launch_bounds__(kB3Warps * 32, 1)
-    k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ G3,
-            double* __restrict__ rho3) {
+    k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
+            const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
+            double* __restrict__ energy, double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int nc = m.b3_nc;
-  C<float>* Xs = reinterpret_cast<C<float>*>(smem);
+  constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
+  const int nc = m.b3_nc, nW = m.nW;
+  const int ncoef = m.b3_ncombo * NM * I * I;
+  float* Cs = reinterpret_cast<float*>(smem);
+  C<float>* Xs = reinterpret_cast<C<float>*>(Cs + ((ncoef + 3) & ~3));
   C<float>* Gs = Xs + nc * kB3Stride;
   double* rpart = reinterpret_cast<double*>(Gs + nc * kB3Stride);  // [kB3Warps][32]
+  float* s_dE = reinterpret_cast<float*>(rpart + kB3Warps * 32);  // [32]
+  float* s_mult = s_dE + 32;                                       // [nc]
+  int* s_fac = reinterpret_cast<int*>(s_mult + nc);                // [nc]
+  int* s_cw = s_fac + nc;                                          // [nW]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
   const int nblk = (natom + 31) / 32;
 
+  for (int t = threadIdx.x; t < ncoef / 4; t += blockDim.x)
+    reinterpret_cast<float4*>(Cs)[t] = __ldg(reinterpret_cast<const float4*>(m.b3_Cf) + t);
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    s_mult[c] = __ldg(m.b3_mult + c);
+    s_fac[c] = __ldg(m.b3_factor + c);
+  }
+  for (int w = threadIdx.x; w < nW; w += blockDim.x) s_cw[w] = __ldg(m.b3_cw + w);
+  __syncthreads();
   for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
     const int a0 = blk * 32;
     const int na = min(32, natom - a0);
     // stage: consecutive threads read consecutive elements of one atom
-    for (int t = threadIdx.x; t < 32 * nc; t += blockDim.x) {
-      const int a = t / nc, c = t - a * nc;
-      C<float> v = {0.f, 0.f};
-      if (a < na) v = F[static_cast<size_t>(a0 + a) * m.nF + __ldg(m.b3_factor + c)];
-      Xs[c * kB3Stride + a] = v;
-      Gs[c * kB3Stride + a] = {0.f, 0.f};
+    for (int t0 = 0; t0 < 32 * nc; t0 += kBatch * blockDim.x) {
+      C<float> v[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int t = t0 + b * blockDim.x + threadIdx.x;
+        const int a = t / nc, c = t - a * nc;
+        v[b] = {0.f, 0.f};
+        if (t < 32 * nc && a < na) v[b] = F[static_cast<size_t>(a0 + a) * m.nF + s_fac[c]];
+      }
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int t = t0 + b * blockDim.x + threadIdx.x;
+        const int a = t / nc, c = t - a * nc;
+        if (t < 32 * nc) {
+          Xs[c * kB3Stride + a] = v[b];
+          Gs[c * kB3Stride + a] = {0.f, 0.f};
+        }
+      }
     }
     __syncthreads();
     double rloc = 0.0;
@@ -319,152 +472,62 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
       const int pat = __ldg(m.b3_pattern + k);
       const float cf = __ldg(m.b3_cff + tk);
       const uint16_t* code = m.b3_code + tk * NPOS;
-      C<float> X[I], Y[I], aZ[I], gY[I];
-#pragma unroll
-      for (int i = 0; i < I; ++i) {
-        X[i] = b3_load(Xs, __ldg(code + NM + i), lane);
-        Y[i] = b3_load(Xs, __ldg(code + NM + I + i), lane);
-        aZ[i] = {0.f, 0.f};
-        gY[i] = {0.f, 0.f};
-      }
-      const float* Ck = m.b3_Cf + static_cast<size_t>(k) * NM * I * I;
-#pragma unroll 1
-      for (int p = 0; p < NM; ++p) {
-        const unsigned cp = __ldg(code + p);
-        const C<float> a = b3_load(Xs, cp, lane);
-        C<float> ga = {0.f, 0.f};
-        if (pat == 0) dense_pass<0, D>(Ck + p * I * I, Y, X, a, aZ, ga, gY);
-        else if (pat == 1) dense_pass<1, D>(Ck + p * I * I, Y, X, a, aZ, ga, gY);
-        else dense_pass<2, D>(Ck + p * I * I, Y, X, a, aZ, ga, gY);
-        b3_add(Gs, cp, lane, ga, cf);
-      }
-      float rt = 0.f;
-#pragma unroll
-      for (int i = 0; i < I; ++i) {
-        rt += re_mul(X[i], aZ[i]);
-        b3_add(Gs, __ldg(code + NM + i), lane, aZ[i], cf);
-        b3_add(Gs, __ldg(code + NM + I + i), lane, gY[i], cf);
-      }
-      rloc += f2d(cf * rt);
+      const float* Ck = Cs + k * NM * I * I;
+      float r;
+      if (pat == 0) r = b3_task<0, D>(Ck, Xs, Gs, code, cf, lane);
+      else if (pat == 1) r = b3_task<1, D>(Ck, Xs, Gs, code, cf, lane);
+      else r = b3_task<2, D>(Ck, Xs, Gs, code, cf, lane);
+      rloc += f2d(r);
     }
     rpart[warp * 32 + lane] = rloc;
     __syncthreads();
-    for (int t = threadIdx.x; t < 32 * nc; t += blockDim.x) {
-      const int a = t / nc, c = t - a * nc;
-      if (a < na) G3[static_cast<size_t>(a0 + a) * nc + c] = Gs[c * kB3Stride + a];
-    }
-    if (threadIdx.x < na) {
-      double r = 0.0;
-      for (int w = 0; w < kB3Warps; ++w) r += rpart[w * 32 + threadIdx.x];
-      rho3[a0 + threadIdx.x] = r;
-    }
-    __syncthreads();
-  }
-}
-
-// ===========================================================================
-// k_density_fe: one CTA per atom for the 2- and 4-body terms (gather table
-// g2), the density, the embedding, and the weights W = dE/drho * mult *
-// (gather slot totals + the 3-body gradient of k_b3_fe).
-// Shared memory: Fs[nF], part[g2.nseg], tot[g2.nslot] (complex R).
-
-template <class R, class D>
-__global__ void __launch_bounds__(kDensityFeThreads)
-    k_density_fe(DeviceModel m, int natom, const C<R>* __restrict__ F, const double* __restrict__ rho1,
-                 const double* __restrict__ core, const C<R>* __restrict__ G3, const double* __restrict__ rho3,
-                 C<R>* __restrict__ W, double* __restrict__ energy, double* __restrict__ edf_out,
-                 double* __restrict__ dedrho_out, int* err) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const GatherView& g = m.g2;
-  C<R>* Fs = reinterpret_cast<C<R>*>(smem);
-  C<R>* part = Fs + ((m.nF + 1) & ~1);
-  C<R>* tot = part + ((g.nseg + 1) & ~1);
-  __shared__ double s_red[kDensityFeThreads / 32];
-  __shared__ double s_dE;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const int nc = m.b3_nc;
-
-  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
-    const C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
-    for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
-    __syncthreads();
-    // 2- and 4-body terms: segment partials of the gather table
-    for (int gi = warp; gi < g.ngroup; gi += nwarp) {
-      const int a = g.grp_arity[gi], len = g.grp_len[gi], base = g.grp_first[gi] + lane;
-      const int seg = g.grp_seg[gi * 32 + lane];
-      const R* kp = kap_ptr<R>(g, a) + base;
-      const uint32_t* op = g.o12[a] + base;
-      C<R> acc = {R(0), R(0)};
-      for (int e = 0; e < len; ++e) {
-        const uint32_t o = __ldg(op + e * 32);
-        C<R> p = Fs[o & 0xffffu];
-        if (a >= 2) p = cmul(p, Fs[o >> 16]);
-        if (a == 3) p = cmul(p, Fs[__ldg(g.o3 + base + e * 32)]);
-        const R k = __ldg(kp + e * 32);
-        acc.x += k * p.x;
-        acc.y += k * p.y;
-      }
-      if (seg >= 0) part[seg] = acc;
-    }
-    __syncthreads();
-    // slot totals; the A0 slots add to rho
-    double rloc = 0.0;
-    for (int s = threadIdx.x; s < g.nslot; s += blockDim.x) {
-      const int q0 = g.slot_seg[s], q1 = g.slot_seg[s + 1];
-      CSum<R> tx, ty;
-      for (int q = q0; q < q1; ++q) {
-        tx.add(part[q].x);
-        ty.add(part[q].y);
-      }
-      tot[s] = {tx.hi + tx.lo, ty.hi + ty.lo};
-      if (s < g.nG0) {
-        const C<R> f = Fs[g.slot_factor[s]];
-        rloc += to_d(f.x) * tx.value() - to_d(f.y) * ty.value();
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) rloc += __shfl_xor_sync(0xffffffffu, rloc, o);
-    if (lane == 0) s_red[warp] = rloc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double rho = rho1[static_cast<size_t>(atom) * 2] + rho3[atom];
-      for (int w = 0; w < nwarp; ++w) rho += s_red[w];
+    // finish the atoms, one per lane of warp 0
+    if (warp == 0 && lane < na) {
+      const int atom = a0 + lane;
+      double rho = rho1[static_cast<size_t>(atom) * 2] + rho_rest[atom];
+      for (int w = 0; w < kB3Warps; ++w) rho += rpart[w * 32 + lane];
       if (!isfinite(rho)) raise_error(err, kDevNaN);
       double Fd, dFd;
       embed(m.nfemb, rho, m.par[0][0], m.par[1][0], Fd, dFd);
       const double e = core[atom], elow = m.ecut - m.decut;
-      double fcut, dfcut;
+      double fcut = 1.0, dfcut = 0.0;
       if (e >= m.ecut) {
         fcut = 0.0;
-        dfcut = 0.0;
-      } else if (e <= elow) {
-        fcut = 1.0;
-        dfcut = 0.0;
-      } else {
+      } else if (e > elow) {
         const double pi = 3.14159265358979323846264338327950288419;
         fcut = 0.5 * (1.0 + cos(pi * (e - elow) / m.decut));
         dfcut = -0.5 * sin(pi * (e - elow) / m.decut) * pi / m.decut;
       }
       edf_out[atom] = dfcut * Fd + 1.0;
-      s_dE = fcut * dFd;
       dedrho_out[static_cast<size_t>(atom) * 2] = fcut * dFd;
       energy[atom] = fcut * Fd + e;
+      s_dE[lane] = d2f(fcut * dFd);
     }
     __syncthreads();
-    C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
-    const C<R>* Ga = G3 + static_cast<size_t>(atom) * nc;
-    const double dE = s_dE;
-    for (int s = threadIdx.x; s < g.nslot; s += blockDim.x) {
-      const int w = g.slot_weight[s];
-      if (w < 0) continue;
-      C<R> v = tot[s];
-      const int c = __ldg(m.b3_cw + w);
-      if (c >= 0) {
-        const C<R> t = Ga[c];
-        v.x += t.x;
-        v.y += t.y;
+    // final weights, consecutive threads on consecutive weights of one atom
+    const int nwt = na * nW;
+    for (int t0 = 0; t0 < nwt; t0 += kBatch * blockDim.x) {
+      C<float> v[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int t = t0 + b * blockDim.x + threadIdx.x;
+        if (t < nwt) v[b] = W[static_cast<size_t>(a0) * nW + t];
       }
-      const R sc = to_r<R>(g.slot_mult[s] * dE);
-      Wa[w] = {v.x * sc, v.y * sc};
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int t = t0 + b * blockDim.x + threadIdx.x;
+        if (t < nwt) {
+          const int a = t / nW, w = t - a * nW;
+          const int c = s_cw[w];
+          if (c >= 0) {
+            const C<float> gv = Gs[c * kB3Stride + a];
+            v[b].x += s_mult[c] * gv.x;
+            v[b].y += s_mult[c] * gv.y;
+          }
+          const float sc = s_dE[a];
+          W[static_cast<size_t>(a0) * nW + t] = {v[b].x * sc, v[b].y * sc};
+        }
+      }
     }
     __syncthreads();
   }
@@ -709,12 +772,15 @@ template <class R, class D>
 size_t abasis_fe_smem() {
   return sizeof(C<R>) * 64 * (D::NRY + D::NQ) + sizeof(R) * 64 * D::NB + sizeof(double) * 64 + 64;
 }
-template <class R, class D>
-size_t density_fe_smem(const DeviceModel& m) {
-  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + ((m.g2.nseg + 1) & ~1) + ((m.g2.nslot + 1) & ~1)) + 64;
+inline size_t density_fe_smem(const DeviceModel& m) {
+  return sizeof(C<float>) * (static_cast<size_t>((m.nF + 1) & ~1) + ((m.g2.nseg + 1) & ~1)) + 64;
 }
-inline size_t b3_fe_smem(const DeviceModel& m) {
-  return sizeof(C<float>) * 2 * static_cast<size_t>(m.b3_nc) * kB3Stride + sizeof(double) * kB3Warps * 32;
+template <class D>
+size_t b3_fe_smem(const DeviceModel& m) {
+  const size_t ncoef = static_cast<size_t>(m.b3_ncombo) * D::NM * D::I * D::I;
+  return sizeof(float) * ((ncoef + 3) & ~static_cast<size_t>(3)) +
+         sizeof(C<float>) * 2 * static_cast<size_t>(m.b3_nc) * kB3Stride + sizeof(double) * kB3Warps * 32 +
+         sizeof(float) * 32 + sizeof(float) * m.b3_nc + sizeof(int) * (m.b3_nc + m.nW);
 }
 template <class R, class D>
 size_t forces_fe_smem() {

@@ -655,6 +655,25 @@ void build_dense_b3(Model& M) {
         }
     }
   }
+  // tasks grouped by pattern (stable): warps that take consecutive tasks then
+  // run the same unrolled code at the same time
+  const int npos = NM + 2 * I;
+  std::vector<int> order(D.ntask);
+  for (int t = 0; t < D.ntask; ++t) order[t] = t;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return D.pattern[D.task_combo[x]] < D.pattern[D.task_combo[y]]; });
+  std::vector<int32_t> combo(D.ntask);
+  std::vector<double> cf(D.ntask);
+  std::vector<uint16_t> code(D.code.size());
+  for (int t = 0; t < D.ntask; ++t) {
+    combo[t] = D.task_combo[order[t]];
+    cf[t] = D.task_cf[order[t]];
+    std::copy(D.code.begin() + static_cast<size_t>(order[t]) * npos,
+              D.code.begin() + static_cast<size_t>(order[t] + 1) * npos, code.begin() + static_cast<size_t>(t) * npos);
+  }
+  D.task_combo.swap(combo);
+  D.task_cf.swap(cf);
+  D.code.swap(code);
 }
 
 }  // namespace
@@ -759,6 +778,14 @@ int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& 
     st = build_gather(M, false, M.gt_nob3, msg);
     if (st) return st;
     build_dense_b3(M);
+    // multiplicity of each compact element's weight, from the gather table's
+    // slots (every weight has a slot there, with or without entries)
+    DenseB3& D = M.db3;
+    D.mult.assign(D.nc, 0.0);
+    for (int s = 0; s < M.gt_nob3.nslot; ++s) {
+      const int w = M.gt_nob3.slot_weight[s];
+      if (w >= 0 && D.compact_of_weight[w] >= 0) D.mult[D.compact_of_weight[w]] = M.gt_nob3.slot_mult[s];
+    }
   }
   if (!build_lut(M, M.lut)) {
     msg = "unsupported radial basis type";

@@ -99,6 +99,7 @@ struct DenseB3 {
   std::vector<uint16_t> code;               // [ntask][NM + 2I]
   std::vector<int32_t> factor_of;           // [nc] factor index of each compact element
   std::vector<int32_t> compact_of_weight;   // [nW] compact element of each weight, or -1
+  std::vector<double> mult;                 // [nc] half-plane multiplicity of each element's weight
 };
 
 struct RadialLUT {
