@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--ncell", type=int, default=20)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--batch", type=int, default=1, help="also measure the 256-configuration uneven batch")
+    p.add_argument("--md-steps", type=int, default=100, help="spin-lattice MD steps in split precision (0: skip)")
+    p.add_argument("--md-steps-fp64", type=int, default=3, help="spin-lattice MD steps in plain FP64")
+    p.add_argument("--md-ncell", type=int, default=80, help="bcc cells per edge of the MD system")
     return p.parse_args()
 
 
@@ -302,6 +306,8 @@ def gpu_arm(args, rank, world, local_rank):
 
     if rank != 0:
         return None
+    batch = batch_measure(lib, torch, dev, args.steps, args.warmup) if args.batch else None
+    mdres = md_measure(lib, args.md_ncell, args.md_steps, args.md_steps_fp64) if args.md_steps > 0 else None
     kms = P["kernel_ms"]
     names = P["names"]
     kflops = dict(flops)
@@ -331,9 +337,98 @@ def gpu_arm(args, rank, world, local_rank):
         "paths": {k: {"ms_per_step": v["ms"], "atom_evals_per_s": whole_job_rate(total_atoms, v["ms"] / 1e3),
                       "kernel_ms": dict(zip(v["names"], v["kernel_ms"]))} for k, v in paths.items()},
         "split_error_vs_fp64": acc,
+        "uneven_batch": batch,
+        "spin_lattice_md": mdres,
         "peaks_measured_tflops": peaks,
     }
     return line, nb, pot
+
+
+def batch_measure(lib, torch, dev, steps: int, warmup: int) -> dict:
+    """The uneven batch: 256 independent configurations of 16-432 atoms (bcc
+    and fcc bulk, vacancy cells, (100)/(110) slabs with 10 A vacuum) in one
+    split-precision evaluation; natural order vs the neighbour-count-sorted
+    work queue, each launched directly and replayed from a CUDA graph. Inputs
+    resident on the device, L2 flushed between steps."""
+    from magace import structures as S
+    confs = S.uneven_batch(256, seed=3)
+    nb = S.concat_neighbor_data([S.neighbor_data(c, 5.0) for c in confs])
+    counts = nb.nstop - nb.nstart + 1
+    T = lambda a, dt=torch.float64: torch.tensor(a, dtype=dt, device=dev)
+    off = T(np.concatenate([[0], np.cumsum(counts)]).astype(np.int32), torch.int32)
+    ins = [T(x) for x in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
+    outs = [torch.empty(n, dtype=torch.float64, device=dev) for n in (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    lib.set_precision(1)
+
+    def call():
+        lib.compute_device(nb.natom, nb.nei, off.data_ptr(), *[x.data_ptr() for x in ins],
+                           *[y.data_ptr() for y in outs], s.cuda_stream)
+
+    res = {"configs": len(confs), "atoms": nb.natom, "bonds": nb.nei,
+           "neighbours_min_max": [int(counts.min()), int(counts.max())], "path": "split"}
+    for queue in (False, True):
+        lib.set_work_queue(queue)
+        with torch.cuda.stream(s):
+            for _ in range(max(1, warmup)):
+                call()
+        s.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            call()
+        for mode in ("launch", "graph"):
+            ts = []
+            for _ in range(steps):
+                with torch.cuda.stream(s):
+                    flush.zero_()
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(s)
+                    call() if mode == "launch" else g.replay()
+                    b.record(s)
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+            ms = float(np.mean(ts))
+            res[f"{'queue' if queue else 'natural'}_{mode}"] = {"ms": ms, "atom_evals_per_s": nb.natom / (ms / 1e3)}
+        del g
+    lib.set_work_queue(False)
+    lib.device_status()
+    return res
+
+
+def md_measure(lib, ncell: int, steps_split: int, steps_fp64: int) -> dict:
+    """Spin-lattice MD on the device: ncell^3 cubic bcc cells (80^3 gives
+    1,024,000 atoms), 300 K Maxwell velocities, random spins with
+    |m| ~ U(1.5, 2.6) mu_B, dt = 1 fs, neighbour list (5.0 + 0.5 A skin)
+    rebuilt every 10 steps, steps between rebuilds replayed from a CUDA
+    graph. Split precision for steps_split steps, plain FP64 for steps_fp64;
+    wall time of ace_md_run (list rebuilds and graph set-up included)."""
+    from magace import md, structures as S
+    rng = np.random.default_rng(5)
+    pos, cell = S.bcc_cubic(ncell, ncell, ncell, 2.83)
+    n = len(pos)
+    st = S.Structure(pos, cell, (True, True, True), rng.uniform(1.5, 2.6, n), S.random_unit(rng, n))
+    out = {"atoms": n, "dt_fs": 1.0, "rebuild_every": 10, "skin_A": 0.5, "temperature_K": 300.0}
+    for name, prec, k in (("split", 1, steps_split), ("fp64", 0, steps_fp64)):
+        if k <= 0:
+            continue
+        lib.set_precision(prec)
+        sim = md.SpinLatticeMD(st, temperature=300.0, seed=7)
+        sim.run(1)  # warm-up: buffers, tables, first graph
+        t0 = time.perf_counter()
+        log = sim.run(k)
+        wall = time.perf_counter() - t0
+        tot = log.sum(axis=1)
+        out[name] = {"steps": k, "wall_s": wall, "ms_per_step": wall / k * 1e3,
+                     "atom_steps_per_s": n * k / wall,
+                     "energy_drift_meV_per_atom": float((tot[-1] - tot[0]) / n * 1e3),
+                     "kinetic_range_meV_per_atom": float(np.ptp(log[:, 1]) / n * 1e3)}
+        sim.close()
+    lib.set_precision(0)
+    if "split" in out and "fp64" in out:
+        out["split_over_fp64"] = out["split"]["atom_steps_per_s"] / out["fp64"]["atom_steps_per_s"]
+    return out
 
 
 def cpu_baseline(nb, pot, budget_s: float, steps: int = 1):

@@ -98,7 +98,10 @@ int ace_basis_rows(int rank, int* out);
  * bond_offset[i] .. bond_offset[i+1]-1 (0-based CSR, natom+1 entries).
  * r[nei], e[3*nei] = (x_i - x_j)/r, mag_j[nei], mhat_j[3*nei], mag_i[natom],
  * mhat_i[3*natom]; outputs energy[natom], fij[3*nei], tij[3*nei], ti0[3*natom].
- * `stream` is a cudaStream_t or NULL for the library stream; the call is
+ * `stream` is a cudaStream_t or NULL for the library's own stream, which is
+ * non-blocking: it does not wait for work on other streams, so a caller
+ * whose inputs are still being written on another stream passes that stream
+ * (cudaStreamLegacy for the legacy default stream) or synchronises first. The call is
  * asynchronous with respect to the host. Check ace_device_status() after the
  * stream has completed. */
 int ace_compute_device(int natom, int nei, const int* bond_offset, const double* r,
@@ -162,6 +165,65 @@ int ace_compute_device_noalloc(int natom, int nei, const int* bond_offset, const
                                const double* e, const double* mag_j, const double* mhat_j,
                                const double* mag_i, const double* mhat_i, double* energy,
                                double* fij, double* tij, double* ti0, void* stream);
+
+/* Work queue (no counterpart in the reference): with on != 0, every
+ * evaluation first sorts its atoms by decreasing bond count on the device
+ * (three small kernels) and the persistent kernels take the atoms in that
+ * order: a longest-first schedule for batches of configurations of uneven
+ * size and neighbour count. Results do not change. Off by default;
+ * ace_compute_device_noalloc always uses the natural order. */
+int ace_set_work_queue(int on);
+
+/* ---- Differentiation and fitting (no counterpart in the reference's
+ * acelib_; they expose what src/forces.F90:976-1289 computes internally). ----
+ *
+ * The expansion coefficients as one vector c[ndensity][ncoef]: the 'clu'
+ * records of ranks 1..4 in the file's order (ace_basis_rows). The density
+ * of atom i is rho_d = sum_k c[d][k] B_k(i). */
+int ace_num_coefficients(int* ncoef, int* ndensity);
+int ace_get_coefficients(double* c);
+/* Replaces the coefficients and rebuilds the tables that fold them in; the
+ * next device call uploads them. */
+int ace_set_coefficients(const double* c);
+
+/* Descriptors B[natom][ncoef] (FP64) of the atoms described by the same
+ * device arrays as ace_compute_device: rank 1, g_n(|m_i|) - 1; ranks 2..4,
+ * the basis functions of src/b_basis.F90:91-307 without their coefficients.
+ * Asynchronous on `stream`. With dE_i/drho_d from
+ * ace_density_gradient_device, dE_i/dc[d][k] = dE_i/drho_d * B_k(i). */
+int ace_descriptors_device(int natom, int nei, const int* bond_offset, const double* r,
+                           const double* e, const double* mag_j, const double* mhat_j,
+                           const double* mag_i, const double* mhat_i, double* B, void* stream);
+
+/* Copies dE_i/drho_d [natom][2] (d = 0, 1; the second is 0 for one density)
+ * of the last ace_compute_device or acelib_ evaluation into a device array,
+ * on `stream`. */
+int ace_density_gradient_device(int natom, double* dedrho, void* stream);
+
+/* ---- Spin-lattice molecular dynamics on the device (no counterpart in
+ * the reference, which is driven by LAMMPS fix nve/spin). ----
+ *
+ * One configuration of natom atoms: positions x[3*natom] (A), velocities
+ * v[3*natom] (A/ps), moments m[3*natom] (mu_B, Cartesian), cell[9] (rows are
+ * lattice vectors, A), pbc[3]; mass in amu; bonds listed within rcut + skin.
+ * A periodic axis must be at least 3 (rcut + skin) wide. Returns a handle. */
+int ace_md_create(int natom, const double* x, const double* v, const double* m, const double* cell,
+                  const int* pbc, double mass_amu, double rcut, double skin, int* handle);
+/* nsteps steps of dt_ps: v += dt/2 F/m; x += dt v; every moment turns about
+ * its field fm = -(mub/hbar) dE/dm by |fm| dt (|m| kept); forces and fields
+ * at the new state; v += dt/2 F/m. The neighbour list is rebuilt every
+ * rebuild_every steps; with use_graph the steps in between replay one
+ * captured CUDA graph. log[2*(nsteps+1)] (may be NULL) receives the total
+ * potential and kinetic energy (eV) of the start and after every step. The
+ * evaluation uses the current precision (ace_set_precision). */
+int ace_md_run(int handle, int nsteps, double dt_ps, int rebuild_every, int use_graph, double* log);
+/* Copies the state to host arrays of 3*natom doubles (any may be NULL):
+ * positions, velocities, moments, forces -dE/dx and fields fm. */
+int ace_md_state(int handle, double* x, double* v, double* m, double* F, double* fm);
+/* The current neighbour list: nbond, off[natom+1], j[nbond], image shift
+ * (three bytes biased by 128) and the index of each bond's reverse. */
+int ace_md_bonds(int handle, int* nbond, int* off, int* j, int* shift, int* rev);
+int ace_md_destroy(int handle);
 
 /* Releases every device buffer held by the library (tables stay on the host). */
 void ace_release_device(void);

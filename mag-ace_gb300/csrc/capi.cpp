@@ -68,6 +68,9 @@ struct Runtime {
   int last_error = MAGACE_OK;
   std::string last_msg;
   int last_launches = 0;
+  int last_natom = -1;  // atoms of the last evaluation (ace_density_gradient_device)
+  bool work_queue = false;  // neighbour-count-sorted work queue
+  DevBuf<int> order, queue_bins;
 
   // device tables
   bool dev_tables = false;
@@ -95,6 +98,9 @@ struct Runtime {
   DevBuf<float> b3_Cf, b3_cff, b3_mult;
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
   DevBuf<uint16_t> b3_code;
+  DevBuf<int32_t> d_rank1_n, d_begin;
+  DevBuf<double> d_cf;
+  DevBuf<uint16_t> d_o;
   DeviceModel dm{};
   int grid_cap = 0;
 
@@ -240,6 +246,13 @@ int upload_tables() {
       R.dm.g2 = R.dm.g;
     }
   }
+  {
+    const DescriptorTable& T = M.desc;
+    CUDA_TRY(R.d_rank1_n.upload(T.rank1_n));
+    CUDA_TRY(R.d_begin.upload(T.begin));
+    CUDA_TRY(R.d_cf.upload(T.cf));
+    CUDA_TRY(R.d_o.upload(T.o));
+  }
   double alm[kMaxHalf], blm[kMaxHalf], cl[kMaxL + 1], dl[kMaxL + 1];
   ylm_constants(alm, blm, cl, dl);
   upload_ylm_constants(alm, blm, cl, dl);
@@ -278,6 +291,12 @@ int upload_tables() {
   d.b3_factor = R.b3_factor.p;
   d.b3_cw = R.b3_cw.p;
   d.b3_mult = R.b3_mult.p;
+  d.d_n1 = M.desc.n1;
+  d.d_nB = M.desc.nB;
+  d.d_rank1_n = R.d_rank1_n.p;
+  d.d_begin = R.d_begin.p;
+  d.d_cf = R.d_cf.p;
+  d.d_o = R.d_o.p;
   int sms = 0;
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   R.grid_cap = std::max(1, sms) * 64;
@@ -291,10 +310,10 @@ int upload_tables() {
   return MAGACE_OK;
 }
 
-int reserve_work(int natom, int nei) {
+int reserve_work(int natom, int nei, int precision) {
   Runtime& R = rt();
   const size_t na = static_cast<size_t>(natom), nb = static_cast<size_t>(nei);
-  const size_t csz = R.precision == 0 ? 16 : 8;
+  const size_t csz = precision == 0 ? 16 : 8;
   CUDA_TRY(R.off.reserve(na + 1));
   CUDA_TRY(R.err.reserve(1));
   CUDA_TRY(R.energy.reserve(na));
@@ -304,7 +323,7 @@ int reserve_work(int natom, int nei) {
   CUDA_TRY(R.dedrho.reserve(2 * na));
   CUDA_TRY(R.F.reserve(na * R.dm.nF * csz));
   CUDA_TRY(R.W.reserve(na * R.dm.nW * csz));
-  CUDA_TRY(R.aux.reserve(eval_aux_bytes(R.dm, R.precision, natom)));
+  CUDA_TRY(R.aux.reserve(eval_aux_bytes(R.dm, precision, natom)));
   (void)nb;
   return MAGACE_OK;
 }
@@ -320,6 +339,12 @@ int run_eval(EvalBuffers& b, cudaStream_t st) {
   b.err = R.err.p;
   b.aux = R.aux.p;
   CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), st));
+  if (R.work_queue && b.natom > 0) {
+    CUDA_TRY(R.order.reserve(static_cast<size_t>(b.natom)));
+    CUDA_TRY(R.queue_bins.reserve(2 * kQueueBins));
+    launch_work_queue(b.natom, b.off, R.order.p, R.queue_bins.p, st);
+    b.order = R.order.p;
+  }
   cudaEvent_t* ev = nullptr;
   if (R.timing) {
     for (auto& e : R.ev)
@@ -329,6 +354,7 @@ int run_eval(EvalBuffers& b, cudaStream_t st) {
   R.last_launches = R.precision == 0 ? launch_eval_fp64(R.dm, b, st, R.grid_cap, ev)
                                      : launch_eval_fp32(R.dm, b, st, R.grid_cap, ev);
   R.ev_recorded = ev != nullptr && R.last_launches >= 3;
+  R.last_natom = b.natom;
   CUDA_TRY(cudaGetLastError());
   return MAGACE_OK;
 }
@@ -581,7 +607,7 @@ int ace_compute_device(int natom, int nei, const int* bond_offset, const double*
   if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
   int st = upload_tables();
   if (st) return st;
-  st = reserve_work(natom, nei);
+  st = reserve_work(natom, nei, R.precision);
   if (st) return st;
   EvalBuffers b;
   b.natom = natom;
@@ -598,6 +624,78 @@ int ace_compute_device(int natom, int nei, const int* bond_offset, const double*
   b.tij = tij;
   b.ti0 = ti0;
   return run_eval(b, stream ? static_cast<cudaStream_t>(stream) : R.stream);
+}
+
+int ace_set_work_queue(int on) {
+  rt().work_queue = on != 0;
+  return set_error(MAGACE_OK, "");
+}
+
+int ace_num_coefficients(int* ncoef, int* ndensity) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  *ncoef = num_coefficients(R.model);
+  *ndensity = R.model.ndensity;
+  return set_error(MAGACE_OK, "");
+}
+
+int ace_get_coefficients(double* c) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  get_coefficients(R.model, c);
+  return set_error(MAGACE_OK, "");
+}
+
+int ace_set_coefficients(const double* c) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  std::string msg;
+  const int st = set_coefficients(R.model, c, msg);
+  if (st) return set_error(st, msg);
+  R.dev_tables = false;  // the next device call uploads the new tables
+  return set_error(MAGACE_OK, "");
+}
+
+int ace_descriptors_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
+                           const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
+                           double* B, void* stream) {
+  Runtime& R = rt();
+  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
+  int st = upload_tables();
+  if (st) return st;
+  st = reserve_work(natom, nei, 0);
+  if (st) return st;
+  EvalBuffers b;
+  b.natom = natom;
+  b.nei = nei;
+  b.off = bond_offset;
+  b.r = r;
+  b.e = e;
+  b.magj = mag_j;
+  b.mhj = mhat_j;
+  b.magi = mag_i;
+  b.mhi = mhat_i;
+  b.F = R.F.p;
+  b.rho1 = R.rho1.p;
+  b.core = R.core.p;
+  b.err = R.err.p;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : R.stream;
+  CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), s));
+  R.last_launches = launch_descriptors(R.dm, b, B, s, R.grid_cap);
+  R.ev_recorded = false;
+  CUDA_TRY(cudaGetLastError());
+  return set_error(MAGACE_OK, "");
+}
+
+int ace_density_gradient_device(int natom, double* dedrho, void* stream) {
+  Runtime& R = rt();
+  if (natom < 0 || natom > R.last_natom)
+    return set_error(MAGACE_ERR_ARGS, "natom exceeds the atoms of the last evaluation");
+  if (natom == 0) return set_error(MAGACE_OK, "");
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : R.stream;
+  CUDA_TRY(cudaMemcpyAsync(dedrho, R.dedrho.p, sizeof(double) * 2 * static_cast<size_t>(natom),
+                           cudaMemcpyDeviceToDevice, s));
+  return set_error(MAGACE_OK, "");
 }
 
 int ace_device_status(void) {
@@ -618,12 +716,17 @@ void ace_release_device(void) {
   for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult}) b->release();
   for (auto* b : {&R.b3_pattern, &R.b3_combo, &R.b3_factor, &R.b3_cw}) b->release();
   R.b3_code.release();
+  for (auto* b : {&R.d_rank1_n, &R.d_begin}) b->release();
+  R.d_cf.release();
+  R.d_o.release();
   R.gb1.release();
   R.gb2.release();
   R.off.release();
   R.err.release();
   R.F.release();
   R.aux.release();
+  R.order.release();
+  R.queue_bins.release();
   R.W.release();
   if (R.stream) cudaStreamDestroy(R.stream);
   R.stream = nullptr;
@@ -671,7 +774,7 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
       if (occlist[j] != 1) return fail(MAGACE_ERR_ARGS, "neighbour element index other than 1", npacked);
   int st = upload_tables();
   if (st) return fail(st, R.last_msg.c_str(), npacked);
-  st = reserve_work(natom, static_cast<int>(npacked));
+  st = reserve_work(natom, static_cast<int>(npacked), R.precision);
   if (st) return fail(st, R.last_msg.c_str(), npacked);
   const size_t na = natom, nb = npacked;
   cudaStream_t s = R.stream;

@@ -70,6 +70,15 @@ struct DeviceModel {
   const int32_t* b3_factor;   // [nc] factor index of each compact element
   const int32_t* b3_cw;       // [nW] compact element of each weight, or -1
   const float* b3_mult;       // [nc] half-plane multiplicity of each element's weight
+  // work queue of this evaluation: atoms in order of decreasing bond count,
+  // or null for the natural order (set per launch)
+  const int32_t* order;
+  // descriptor tables (see model.hpp DescriptorTable)
+  int d_n1, d_nB;
+  const int32_t* d_rank1_n;
+  const int32_t* d_begin;
+  const double* d_cf;
+  const uint16_t* d_o;
 };
 
 }  // namespace magace

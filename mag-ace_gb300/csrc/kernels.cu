@@ -22,6 +22,8 @@
 
 #include <cstdint>
 #include <cstdlib>
+#include <map>
+#include <utility>
 
 #include "device_model.hpp"
 #include "kernels.hpp"
@@ -60,6 +62,10 @@ __device__ __forceinline__ double parity(int m) { return (m & 1) ? -1.0 : 1.0; }
 __device__ __forceinline__ void raise_error(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
+
+// The atom at position `it` of the work queue: the neighbour-count-sorted
+// order when the evaluation has one, else atom `it`.
+__device__ __forceinline__ int queue_atom(const DeviceModel& m, int it) { return m.order ? __ldg(m.order + it) : it; }
 
 // Double <-> float conversions on the integer pipes. A hardware conversion
 // issues on the FP64 pipe, which GB300 runs at 1/64 of the FP32 rate; the
@@ -297,7 +303,8 @@ __global__ void __launch_bounds__(kAbasisThreads)
   double* score = reinterpret_cast<double*>(sg + m.nba * TB);  // [TB]
   __shared__ double s_core;
 
-  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
     for (int s = threadIdx.x; s < nacc; s += blockDim.x) acc[s] = {R(0), R(0)};
     if (threadIdx.x == 0) s_core = 0.0;
     const int b0 = off[atom], b1 = off[atom + 1];
@@ -524,7 +531,8 @@ __global__ void __launch_bounds__(kDensityThreads)
   __shared__ double s_dE[ND];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
 
-  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
     const C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
     for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
     __syncthreads();
@@ -675,7 +683,8 @@ __global__ void __launch_bounds__(kForceThreads)
   const int t = threadIdx.x;
   const int nRl = m.n3a * (m.l3a + 1), nMl = m.n2m * (m.l2m + 1);
 
-  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
     const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
     for (int s = t; s < m.nW; s += T) Ws[s] = Wa[s];
     __syncthreads();
@@ -911,6 +920,38 @@ bool use_specialised(const DeviceModel& m) {
   return !forced_generic && m.nd == 1 && dims_match<FeDims>(m);
 }
 
+// Opts a kernel into `bytes` of dynamic shared memory, once per kernel,
+// device and size: the attribute call is skipped when a launch needs no more
+// than was already set, so evaluations captured into a CUDA graph issue none.
+template <class K>
+void set_smem(K* kernel, size_t bytes) {
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  size_t& cur = done[{reinterpret_cast<const void*>(kernel), dev}];
+  if (bytes > cur) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    cur = bytes;
+  }
+}
+
+// The A-basis phase: factors F, rank-1 density and core energy per atom.
+template <class R>
+void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid, bool fe) {
+  const int natom = b.natom;
+  if (fe) {
+    const size_t s1 = abasis_fe_smem<R, FeDims>();
+    set_smem(k_abasis_fe<R, FeDims>, s1);
+    k_abasis_fe<R, FeDims><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                 reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+  } else {
+    const size_t s1 = abasis_smem<R>(m);
+    set_smem(k_abasis<R>, s1);
+    k_abasis<R><<<grid, kAbasisThreads, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                   reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+  }
+}
+
 // The density phase: in split precision with the specialised layout,
 // k_density_fe (2- and 4-body terms, one CTA per atom) and then k_b3_fe
 // (3-body terms, 32 atoms per CTA; embedding and weights); otherwise one
@@ -923,12 +964,12 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
     if (fe) {
       double* rho_rest = static_cast<double*>(b.aux);
       const size_t s2 = density_fe_smem(m);
-      cudaFuncSetAttribute(k_density_fe<FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
+      set_smem(k_density_fe<FeDims>, s2);
       k_density_fe<FeDims><<<grid, kDensityFeThreads, s2, st>>>(m, natom, reinterpret_cast<const C<float>*>(b.F),
                                                                 reinterpret_cast<C<float>*>(b.W), rho_rest);
       if (ev_between) cudaEventRecord(ev_between, st);
       const size_t sb = b3_fe_smem<FeDims>(m);
-      cudaFuncSetAttribute(k_b3_fe<FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb));
+      set_smem(k_b3_fe<FeDims>, sb);
       const int nblk = (natom + 31) / 32;
       k_b3_fe<FeDims><<<nblk < grid_cap ? nblk : grid_cap, kB3Warps * 32, sb, st>>>(
           m, natom, reinterpret_cast<const C<float>*>(b.F), reinterpret_cast<C<float>*>(b.W), b.rho1, rho_rest,
@@ -938,11 +979,11 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
   }
   const size_t s2 = density_smem<R>(m);
   if (m.nd == 1) {
-    cudaFuncSetAttribute(k_density<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
+    set_smem(k_density<R, 1>, s2);
     k_density<R, 1><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
                                                        reinterpret_cast<C<R>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
   } else {
-    cudaFuncSetAttribute(k_density<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s2));
+    set_smem(k_density<R, 2>, s2);
     k_density<R, 2><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
                                                        reinterpret_cast<C<R>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
   }
@@ -950,36 +991,28 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
 }
 
 template <class R>
-int launch_eval(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
+int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
+  DeviceModel m = m0;
+  m.order = b.order;
   const int natom = b.natom;
   if (natom <= 0) return 0;
   const int grid = natom < grid_cap ? natom : grid_cap;
   const bool fe = use_specialised(m);
   if (ev) cudaEventRecord(ev[0], st);
-  if (fe) {
-    const size_t s1 = abasis_fe_smem<R, FeDims>();
-    cudaFuncSetAttribute(k_abasis_fe<R, FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1));
-    k_abasis_fe<R, FeDims><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                 reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
-  } else {
-    const size_t s1 = abasis_smem<R>(m);
-    cudaFuncSetAttribute(k_abasis<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s1));
-    k_abasis<R><<<grid, kAbasisThreads, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                   reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
-  }
+  launch_abasis<R>(m, b, st, grid, fe);
   if (ev) cudaEventRecord(ev[1], st);
   const int nd = launch_density<R>(m, b, st, grid, grid_cap, fe, ev ? ev[2] : nullptr);
   const int nlaunch = 2 + nd;
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
     const size_t s3 = forces_fe_smem<R, FeDims>();
-    cudaFuncSetAttribute(k_forces_fe<R, FeDims>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s3));
+    set_smem(k_forces_fe<R, FeDims>, s3);
     k_forces_fe<R, FeDims><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
                                                  reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
                                                  b.ti0, b.err);
   } else {
     const size_t s3 = forces_smem<R>(m, kForceThreads);
-    cudaFuncSetAttribute(k_forces<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s3));
+    set_smem(k_forces<R>, s3);
     k_forces<R><<<grid, kForceThreads, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
                                                   reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
                                                   b.ti0, b.err);
@@ -1016,6 +1049,105 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
   if (which == 0) return abasis_smem<float>(m);
   if (which == 1) return density_smem<float>(m);
   return forces_smem<float>(m, kForceThreads);
+}
+
+// ===========================================================================
+// Work queue: atoms in order of decreasing bond count, so that the
+// persistent CTAs, which take queue positions round-robin, meet the largest
+// atoms first and similar ones in each round (a longest-first schedule for
+// batches of uneven configurations). Counting sort; atoms of equal clipped
+// count keep no particular order (each atom's result does not depend on it).
+__global__ void k_queue_hist(int natom, const int* __restrict__ off, int* __restrict__ bins) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < natom; a += gridDim.x * blockDim.x) {
+    const int c = min(off[a + 1] - off[a], kQueueBins - 1);
+    atomicAdd(&bins[kQueueBins - 1 - c], 1);  // bin 0 holds the largest count
+  }
+}
+__global__ void k_queue_scan(int* __restrict__ bins) {
+  // one warp: exclusive prefix sum of kQueueBins counts into the cursors
+  __shared__ int s[kQueueBins];
+  for (int k = threadIdx.x; k < kQueueBins; k += blockDim.x) s[k] = bins[k];
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int k = 0; k < kQueueBins; ++k) {
+      const int c = s[k];
+      s[k] = run;
+      run += c;
+    }
+  }
+  __syncwarp();
+  for (int k = threadIdx.x; k < kQueueBins; k += blockDim.x) bins[kQueueBins + k] = s[k];
+}
+__global__ void k_queue_place(int natom, const int* __restrict__ off, int* __restrict__ bins, int* __restrict__ order) {
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < natom; a += gridDim.x * blockDim.x) {
+    const int c = min(off[a + 1] - off[a], kQueueBins - 1);
+    order[atomicAdd(&bins[kQueueBins + kQueueBins - 1 - c], 1)] = a;
+  }
+}
+
+void launch_work_queue(int natom, const int* off, int* order, int* bins, cudaStream_t st) {
+  if (natom <= 0) return;
+  cudaMemsetAsync(bins, 0, sizeof(int) * kQueueBins, st);
+  const int blocks = (natom + 255) / 256 < 1024 ? (natom + 255) / 256 : 1024;
+  k_queue_hist<<<blocks, 256, 0, st>>>(natom, off, bins);
+  k_queue_scan<<<1, 32, 0, st>>>(bins);
+  k_queue_place<<<blocks, 256, 0, st>>>(natom, off, bins, order);
+}
+
+// ===========================================================================
+// k_descriptors: one CTA per atom, FP64. B[atom][k] for every cluster in
+// coefficient order: rank 1, g_n(|m_i|) - 1 (src/b_basis.F90:74-83); ranks
+// 2..4, Re sum over the cluster's m-terms of cf * F[o0] F[o1] F[o2] F[o3]
+// (src/b_basis.F90:91-307 without the coefficients).
+constexpr int kDescThreads = 128;
+
+__global__ void __launch_bounds__(kDescThreads)
+    k_descriptors(DeviceModel m, int natom, const C<double>* __restrict__ F, const double* __restrict__ magi,
+                  double* __restrict__ B, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  C<double>* Fs = reinterpret_cast<C<double>*>(smem);
+  const int nB = m.d_nB, n1 = m.d_n1;
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
+    const C<double>* Fa = F + static_cast<size_t>(atom) * m.nF;
+    for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
+    __syncthreads();
+    double* Ba = B + static_cast<size_t>(atom) * nB;
+    for (int k = threadIdx.x; k < n1; k += blockDim.x) {
+      double wl = 0.0, g = 1.0, dummy[1];
+      const int nl = magnetic_bin(m, magi[atom], wl, err);
+      if (nl > 0) {
+        lut_eval<false>(m.lut_m, m.nfm, m.n2m * (m.l2m + 1) + m.d_rank1_n[k], 1, nl, wl, m.rscale_m, &g, dummy);
+      } else if (nl < 0) {
+        g = 0.0;
+      }
+      Ba[k] = g - 1.0;
+    }
+    for (int k = threadIdx.x; k < nB - n1; k += blockDim.x) {
+      double acc = 0.0;
+      for (int e = m.d_begin[k]; e < m.d_begin[k + 1]; ++e) {
+        const ushort4 o = *reinterpret_cast<const ushort4*>(m.d_o + 4 * static_cast<size_t>(e));
+        const C<double> p = cmul(cmul(Fs[o.x], Fs[o.y]), cmul(Fs[o.z], Fs[o.w]));
+        acc += m.d_cf[e] * p.x;
+      }
+      Ba[n1 + k] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+int launch_descriptors(const DeviceModel& m0, const EvalBuffers& b, double* B, cudaStream_t st, int grid_cap) {
+  DeviceModel m = m0;
+  m.order = b.order;
+  const int natom = b.natom;
+  if (natom <= 0) return 0;
+  const int grid = natom < grid_cap ? natom : grid_cap;
+  launch_abasis<double>(m, b, st, grid, use_specialised(m));
+  const size_t sd = sizeof(C<double>) * static_cast<size_t>(m.nF);
+  set_smem(k_descriptors, sd);
+  k_descriptors<<<grid, kDescThreads, sd, st>>>(m, natom, reinterpret_cast<const C<double>*>(b.F), b.magi, B, b.err);
+  return 2;
 }
 
 int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {

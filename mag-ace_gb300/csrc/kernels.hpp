@@ -40,7 +40,14 @@ struct EvalBuffers {
   double* ti0 = nullptr;      // [3*natom]
   int* err = nullptr;         // device error word
   void* aux = nullptr;        // [eval_aux_bytes] scratch of the specialised split-precision kernels
+  const int* order = nullptr; // [natom] work queue (atoms by decreasing bond count) or null
 };
+
+// Work queue of one evaluation: the atoms sorted by decreasing bond count
+// (counting sort over counts clipped to kQueueBins - 1), into order[natom];
+// scratch bins[2 * kQueueBins] ints. Three small kernels on `st`.
+constexpr int kQueueBins = 256;
+void launch_work_queue(int natom, const int* off, int* order, int* bins, cudaStream_t st);
 
 void upload_ylm_constants(const double* alm, const double* blm, const double* cl, const double* dl);
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which);
@@ -50,6 +57,9 @@ size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom);
 // when the split-precision density runs its 3-body part as a kernel of its
 // own); returns the number of kernels launched n. With `ev` (kMaxLaunches + 1
 // events) ev[k] is recorded before kernel k and ev[n] after the last one.
+// Descriptors: the FP64 A-basis phase into b.F, then B[natom][nB] (see
+// model.hpp DescriptorTable); returns the number of kernels launched.
+int launch_descriptors(const DeviceModel& m, const EvalBuffers& b, double* B, cudaStream_t st, int grid_cap);
 int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
 int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
 

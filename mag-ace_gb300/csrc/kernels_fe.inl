@@ -66,7 +66,8 @@ __global__ void __launch_bounds__(64)
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int row = lane >> 1, cb = lane & 1;
 
-  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
     C<R> acc[15];
 #pragma unroll
     for (int c = 0; c < 15; ++c) acc[c] = {R(0), R(0)};
@@ -244,7 +245,8 @@ __global__ void __launch_bounds__(kDensityFeThreads)
   __shared__ double s_red[kDensityFeThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
 
-  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
     const C<float>* Fa = F + static_cast<size_t>(atom) * m.nF;
     for (int s0 = 0; s0 < m.nF; s0 += kBatch * kDensityFeThreads) {
       C<float> v[kBatch];
@@ -430,6 +432,7 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
   float* s_mult = s_dE + 32;                                       // [nc]
   int* s_fac = reinterpret_cast<int*>(s_mult + nc);                // [nc]
   int* s_cw = s_fac + nc;                                          // [nW]
+  __shared__ int s_atom[32];                                       // the block's atoms
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (natom + 31) / 32;
 
@@ -444,6 +447,8 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
   for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
     const int a0 = blk * 32;
     const int na = min(32, natom - a0);
+    if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
+    __syncthreads();
     // stage: consecutive threads read consecutive elements of one atom
     for (int t0 = 0; t0 < 32 * nc; t0 += kBatch * blockDim.x) {
       C<float> v[kBatch];
@@ -452,7 +457,7 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
         const int t = t0 + b * blockDim.x + threadIdx.x;
         const int a = t / nc, c = t - a * nc;
         v[b] = {0.f, 0.f};
-        if (t < 32 * nc && a < na) v[b] = F[static_cast<size_t>(a0 + a) * m.nF + s_fac[c]];
+        if (t < 32 * nc && a < na) v[b] = F[static_cast<size_t>(s_atom[a]) * m.nF + s_fac[c]];
       }
 #pragma unroll
       for (int b = 0; b < kBatch; ++b) {
@@ -483,7 +488,7 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
     __syncthreads();
     // finish the atoms, one per lane of warp 0
     if (warp == 0 && lane < na) {
-      const int atom = a0 + lane;
+      const int atom = s_atom[lane];
       double rho = rho1[static_cast<size_t>(atom) * 2] + rho_rest[atom];
       for (int w = 0; w < kB3Warps; ++w) rho += rpart[w * 32 + lane];
       if (!isfinite(rho)) raise_error(err, kDevNaN);
@@ -511,7 +516,8 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
 #pragma unroll
       for (int b = 0; b < kBatch; ++b) {
         const int t = t0 + b * blockDim.x + threadIdx.x;
-        if (t < nwt) v[b] = W[static_cast<size_t>(a0) * nW + t];
+        const int a = t / nW, w = t - a * nW;
+        if (t < nwt) v[b] = W[static_cast<size_t>(s_atom[a]) * nW + w];
       }
 #pragma unroll
       for (int b = 0; b < kBatch; ++b) {
@@ -525,7 +531,7 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
             v[b].y += s_mult[c] * gv.y;
           }
           const float sc = s_dE[a];
-          W[static_cast<size_t>(a0) * nW + t] = {v[b].x * sc, v[b].y * sc};
+          W[static_cast<size_t>(s_atom[a]) * nW + w] = {v[b].x * sc, v[b].y * sc};
         }
       }
     }
@@ -559,7 +565,8 @@ __global__ void __launch_bounds__(64)
   C<R>* cYm = cdYa + D::LSA * 3 * T;                     // half [H2]
   const int t = threadIdx.x;
 
-  for (int atom = blockIdx.x; atom < natom; atom += gridDim.x) {
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
     const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
     for (int s = t; s < D::NA2H; s += T) {  // W2[n][k] -> W2T[k][n]
       const int n = s / D::NQ, k = s % D::NQ;

@@ -369,28 +369,28 @@ struct TermSink {
   }
 };
 
-int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg) {
+// Visits every m-term of the 2-, 3- (when with_b3) and 4-body clusters in
+// enumeration order as fn(rank, cluster, cf, f, w): cf is the coupling (the
+// product of Clebsch-Gordan coefficients), f[0] the A0 factor and f[1 ..
+// rank-1] the A2 (rank 2) or A factors, w[q] the weight index of factor q
+// (-1 where it has none: m' < 0; w[0] is unused). Terms with cf == 0 are
+// skipped.
+template <class Fn>
+void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
   const FactorLayout& L = M.L;
-  const BasisDims& d = M.pot.dims;
-  const int nd = M.ndensity;
-  TermSink sink(L, nd);
-  long nterm[5] = {0, 0, 0, 0, 0};
-
-  // 2-body: kappa A0(n0',l,m) A2(n1,n1',l,-m), cg <l m l -m|0 0> (src/b_basis.F90:91-129)
+  // 2-body: A0(n0',l,m) A2(n1,n1',l,-m), cg <l m l -m|0 0> (src/b_basis.F90:91-129)
   for (size_t c = 0; c < M.rows[2].size(); ++c) {
     const auto& r = M.rows[2][c];
     const int n0 = r[0] - 1, n1p = r[1] - 1, n1 = r[2] - 1, l = r[3];
     for (int m = -l; m <= l; ++m) {
-      double cf = clebsch_gordan(l, l, 0, m, -m, 0);
-      double k[2] = {M.coef[2][c][0] * cf, M.coef[2][c][1] * cf};
-      if (k[0] == 0.0 && k[1] == 0.0) continue;
-      ++nterm[2];
-      int a0 = L.A0(n0, l, m), a2 = L.A2(n1, n1p, l, -m);
-      sink.add(sink.g0_slot(a0), k, &a2, 1);
-      if (-m >= 0) sink.add(sink.w_slot(L.W2(n1, n1p, l, -m) - L.offW2 + L.nWA), k, &a0, 1);
+      const double cf = clebsch_gordan(l, l, 0, m, -m, 0);
+      if (cf == 0.0) continue;
+      const int f[4] = {L.A0(n0, l, m), L.A2(n1, n1p, l, -m), L.offOne, L.offOne};
+      const int w[4] = {-1, -m >= 0 ? L.W2(n1, n1p, l, -m) : -1, -1, -1};
+      fn(2, c, cf, f, w);
     }
   }
-  // 3-body: kappa A0(n0',l0',m0') A(n1,l1,m1,n1',l1',m1') A(n2,l1,-m1,n2',l2',m2')
+  // 3-body: A0(n0',l0',m0') A(n1,l1,m1,n1',l1',m1') A(n2,l1,-m1,n2',l2',m2')
   // with cg<l1 m1 l1 -m1|00> * cg<l0' m0' l1' m1'|l2' -m2'> cg<l2' m2' l2' -m2'|00>
   // (src/b_basis.F90:142-212, src/util.F90:4297-4333)
   for (size_t c = 0; with_b3 && c < M.rows[3].size(); ++c) {
@@ -398,27 +398,21 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg) {
     const int n1 = r[0] - 1, n2 = r[1] - 1, p0 = r[2] - 1, p1 = r[3] - 1, p2 = r[4] - 1;
     const int l1 = r[5], q0 = r[6], q1 = r[7], q2 = r[8];
     for (int m1 = -l1; m1 <= l1; ++m1) {
-      double cfa = clebsch_gordan(l1, l1, 0, m1, -m1, 0);
+      const double cfa = clebsch_gordan(l1, l1, 0, m1, -m1, 0);
       for (int u0 = -q0; u0 <= q0; ++u0)
         for (int u1 = -q1; u1 <= q1; ++u1) {
-          int u2 = -(u0 + u1);
+          const int u2 = -(u0 + u1);
           if (std::abs(u2) > q2) continue;
-          double cfm = clebsch_gordan(q0, q1, q2, u0, u1, -u2) * clebsch_gordan(q2, q2, 0, u2, -u2, 0);
-          double cf = cfa * cfm;
-          double k[2] = {M.coef[3][c][0] * cf, M.coef[3][c][1] * cf};
-          if (k[0] == 0.0 && k[1] == 0.0) continue;
-          ++nterm[3];
-          int f0 = L.A0(p0, q0, u0), f1 = L.A(n1, l1, m1, p1, q1, u1), f2 = L.A(n2, l1, -m1, p2, q2, u2);
-          int o12[2] = {f1, f2};
-          sink.add(sink.g0_slot(f0), k, o12, 2);
-          int w1 = L.WA(n1, l1, m1, p1, q1, u1), w2 = L.WA(n2, l1, -m1, p2, q2, u2);
-          int o02[2] = {f0, f2}, o01[2] = {f0, f1};
-          if (w1 >= 0) sink.add(sink.w_slot(w1), k, o02, 2);
-          if (w2 >= 0) sink.add(sink.w_slot(w2), k, o01, 2);
+          const double cfm = clebsch_gordan(q0, q1, q2, u0, u1, -u2) * clebsch_gordan(q2, q2, 0, u2, -u2, 0);
+          const double cf = cfa * cfm;
+          if (cf == 0.0) continue;
+          const int f[4] = {L.A0(p0, q0, u0), L.A(n1, l1, m1, p1, q1, u1), L.A(n2, l1, -m1, p2, q2, u2), L.offOne};
+          const int w[4] = {-1, L.WA(n1, l1, m1, p1, q1, u1), L.WA(n2, l1, -m1, p2, q2, u2), -1};
+          fn(3, c, cf, f, w);
         }
     }
   }
-  // 4-body: kappa A0 A(1) A(2) A(3) with
+  // 4-body: A0 A(1) A(2) A(3) with
   // cg<l1 m1 l2 m2|l3 -m3> cg<l3 m3 l3 -m3|00> *
   // cg<l0' m0' l1' m1'|L M> cg<l2' m2' l3' m3'|L -M> cg<L M L -M|00>
   // (src/b_basis.F90:225-307, src/util.F90:4344-4388)
@@ -429,36 +423,53 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg) {
     const int l1 = r[7], l2 = r[8], l3 = r[9], q0 = r[10], q1 = r[11], q2 = r[12], q3 = r[13], Lc = r[14];
     for (int m1 = -l1; m1 <= l1; ++m1)
       for (int m2 = -l2; m2 <= l2; ++m2) {
-        int m3 = -(m1 + m2);
+        const int m3 = -(m1 + m2);
         if (std::abs(m3) > l3) continue;
-        double cfa = clebsch_gordan(l1, l2, l3, m1, m2, -m3) * clebsch_gordan(l3, l3, 0, m3, -m3, 0);
+        const double cfa = clebsch_gordan(l1, l2, l3, m1, m2, -m3) * clebsch_gordan(l3, l3, 0, m3, -m3, 0);
         for (int Mc = -Lc; Mc <= Lc; ++Mc)
           for (int u0 = -q0; u0 <= q0; ++u0) {
-            int u1 = Mc - u0;
+            const int u1 = Mc - u0;
             if (std::abs(u1) > q1) continue;
             for (int u2 = -q2; u2 <= q2; ++u2) {
-              int u3 = -Mc - u2;
+              const int u3 = -Mc - u2;
               if (std::abs(u3) > q3) continue;
-              double cfm = clebsch_gordan(q0, q1, Lc, u0, u1, Mc) * clebsch_gordan(q2, q3, Lc, u2, u3, -Mc) *
-                           clebsch_gordan(Lc, Lc, 0, Mc, -Mc, 0);
-              double cf = cfa * cfm;
-              double k[2] = {M.coef[4][c][0] * cf, M.coef[4][c][1] * cf};
-              if (k[0] == 0.0 && k[1] == 0.0) continue;
-              ++nterm[4];
-              int f0 = L.A0(p0, q0, u0), f1 = L.A(n1, l1, m1, p1, q1, u1), f2 = L.A(n2, l2, m2, p2, q2, u2),
-                  f3 = L.A(n3, l3, m3, p3, q3, u3);
-              int o123[3] = {f1, f2, f3};
-              sink.add(sink.g0_slot(f0), k, o123, 3);
-              int w1 = L.WA(n1, l1, m1, p1, q1, u1), w2 = L.WA(n2, l2, m2, p2, q2, u2),
-                  w3 = L.WA(n3, l3, m3, p3, q3, u3);
-              int o023[3] = {f0, f2, f3}, o013[3] = {f0, f1, f3}, o012[3] = {f0, f1, f2};
-              if (w1 >= 0) sink.add(sink.w_slot(w1), k, o023, 3);
-              if (w2 >= 0) sink.add(sink.w_slot(w2), k, o013, 3);
-              if (w3 >= 0) sink.add(sink.w_slot(w3), k, o012, 3);
+              const double cfm = clebsch_gordan(q0, q1, Lc, u0, u1, Mc) * clebsch_gordan(q2, q3, Lc, u2, u3, -Mc) *
+                                 clebsch_gordan(Lc, Lc, 0, Mc, -Mc, 0);
+              const double cf = cfa * cfm;
+              if (cf == 0.0) continue;
+              const int f[4] = {L.A0(p0, q0, u0), L.A(n1, l1, m1, p1, q1, u1), L.A(n2, l2, m2, p2, q2, u2),
+                                L.A(n3, l3, m3, p3, q3, u3)};
+              const int w[4] = {-1, L.WA(n1, l1, m1, p1, q1, u1), L.WA(n2, l2, m2, p2, q2, u2),
+                                L.WA(n3, l3, m3, p3, q3, u3)};
+              fn(4, c, cf, f, w);
             }
           }
       }
   }
+}
+
+int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg) {
+  const FactorLayout& L = M.L;
+  const BasisDims& d = M.pot.dims;
+  const int nd = M.ndensity;
+  TermSink sink(L, nd);
+  long nterm[5] = {0, 0, 0, 0, 0};
+  // every term adds kappa * (product of the other factors) to the A0 factor's
+  // slot (density and W0) and to the weight slot of each other factor
+  for_each_term(M, with_b3, [&](int rank, size_t c, double cf, const int* f, const int* w) {
+    const double k[2] = {M.coef[rank][c][0] * cf, M.coef[rank][c][1] * cf};
+    if (k[0] == 0.0 && k[1] == 0.0) return;
+    ++nterm[rank];
+    const int arity = rank - 1;
+    sink.add(sink.g0_slot(f[0]), k, f + 1, arity);
+    for (int q = 1; q < rank; ++q) {
+      if (w[q] < 0) continue;
+      int others[3], n = 0;
+      for (int o = 0; o < rank; ++o)
+        if (o != q) others[n++] = f[o];
+      sink.add(sink.w_slot(w[q]), k, others, arity);
+    }
+  });
   if (with_b3)
     for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
 
@@ -676,7 +687,89 @@ void build_dense_b3(Model& M) {
   D.code.swap(code);
 }
 
+// Per-cluster m-terms of the descriptors, in coefficient order (ranks 1..4).
+void build_descriptors(Model& M) {
+  DescriptorTable& T = M.desc;
+  T = DescriptorTable();
+  T.n1 = static_cast<int>(M.rows[1].size());
+  const int n2 = static_cast<int>(M.rows[2].size()), n3 = static_cast<int>(M.rows[3].size());
+  T.nB = T.n1 + n2 + n3 + static_cast<int>(M.rows[4].size());
+  for (const auto& r : M.rows[1]) T.rank1_n.push_back(r[0] - 1);
+  std::vector<int32_t> count(T.nB - T.n1, 0);
+  std::vector<std::array<int, 5>> terms;  // cluster (0-based past rank 1), factors
+  std::vector<double> cfs;
+  for_each_term(M, true, [&](int rank, size_t c, double cf, const int* f, const int*) {
+    const int k = static_cast<int>(c) + (rank == 2 ? 0 : (rank == 3 ? n2 : n2 + n3));
+    ++count[k];
+    terms.push_back({k, f[0], f[1], f[2], f[3]});
+    cfs.push_back(cf);
+  });
+  T.begin.assign(T.nB - T.n1 + 1, 0);
+  for (int k = 0; k < T.nB - T.n1; ++k) T.begin[k + 1] = T.begin[k] + count[k];
+  T.cf.assign(cfs.size(), 0.0);
+  T.o.assign(4 * cfs.size(), 0);
+  std::vector<int32_t> fill(T.begin.begin(), T.begin.end() - 1);
+  for (size_t e = 0; e < terms.size(); ++e) {
+    const int pos = fill[terms[e][0]]++;
+    T.cf[pos] = cfs[e];
+    for (int q = 0; q < 4; ++q) T.o[4 * pos + q] = static_cast<uint16_t>(terms[e][1 + q]);
+  }
+}
+
 }  // namespace
+
+// The coefficient-dependent tables: 1-body coefficients, gather tables with
+// the coefficients folded in, and the dense 3-body tables.
+int build_tables(Model& M, std::string& msg) {
+  const FactorLayout& L = M.L;
+  for (int dd = 0; dd < 2; ++dd) M.c1[dd].assign(L.nbm, 0.0);
+  for (size_t c = 0; c < M.rows[1].size(); ++c)
+    for (int dd = 0; dd < 2; ++dd) M.c1[dd][M.rows[1][c][0] - 1] += M.coef[1][c][dd];
+
+  int st = build_gather(M, true, M.gt, msg);
+  if (st) return st;
+  // tables of the specialised kernels: 3-body terms as dense per-(combo, m)
+  // contractions, everything else through the gather table without them
+  if (M.ndensity == 1) {
+    st = build_gather(M, false, M.gt_nob3, msg);
+    if (st) return st;
+    build_dense_b3(M);
+    // multiplicity of each compact element's weight, from the gather table's
+    // slots (every weight has a slot there, with or without entries)
+    DenseB3& D = M.db3;
+    D.mult.assign(D.nc, 0.0);
+    for (int s = 0; s < M.gt_nob3.nslot; ++s) {
+      const int w = M.gt_nob3.slot_weight[s];
+      if (w >= 0 && D.compact_of_weight[w] >= 0) D.mult[D.compact_of_weight[w]] = M.gt_nob3.slot_mult[s];
+    }
+  }
+  return MAGACE_OK;
+}
+
+int num_coefficients(const Model& M) {
+  int n = 0;
+  for (int r = 1; r <= 4; ++r) n += static_cast<int>(M.rows[r].size());
+  return n;
+}
+
+void get_coefficients(const Model& M, double* c) {
+  const int nB = num_coefficients(M);
+  for (int d = 0; d < M.ndensity; ++d) {
+    int k = 0;
+    for (int r = 1; r <= 4; ++r)
+      for (size_t q = 0; q < M.rows[r].size(); ++q) c[d * nB + k++] = M.coef[r][q][d];
+  }
+}
+
+int set_coefficients(Model& M, const double* c, std::string& msg) {
+  const int nB = num_coefficients(M);
+  for (int d = 0; d < M.ndensity; ++d) {
+    int k = 0;
+    for (int r = 1; r <= 4; ++r)
+      for (size_t q = 0; q < M.rows[r].size(); ++q) M.coef[r][q][d] = c[d * nB + k++];
+  }
+  return build_tables(M, msg);
+}
 
 int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& M, std::string& msg) {
   M = Model();
@@ -766,27 +859,11 @@ int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& 
       M.coef[r][it->second] = kv.second;
     }
   }
-  for (int dd = 0; dd < 2; ++dd) M.c1[dd].assign(L.nbm, 0.0);
-  for (size_t c = 0; c < M.rows[1].size(); ++c)
-    for (int dd = 0; dd < 2; ++dd) M.c1[dd][M.rows[1][c][0] - 1] += M.coef[1][c][dd];
-
-  int st = build_gather(M, true, M.gt, msg);
-  if (st) return st;
-  // tables of the specialised kernels: 3-body terms as dense per-(combo, m)
-  // contractions, everything else through the gather table without them
-  if (M.ndensity == 1) {
-    st = build_gather(M, false, M.gt_nob3, msg);
+  {
+    const int st = build_tables(M, msg);
     if (st) return st;
-    build_dense_b3(M);
-    // multiplicity of each compact element's weight, from the gather table's
-    // slots (every weight has a slot there, with or without entries)
-    DenseB3& D = M.db3;
-    D.mult.assign(D.nc, 0.0);
-    for (int s = 0; s < M.gt_nob3.nslot; ++s) {
-      const int w = M.gt_nob3.slot_weight[s];
-      if (w >= 0 && D.compact_of_weight[w] >= 0) D.mult[D.compact_of_weight[w]] = M.gt_nob3.slot_mult[s];
-    }
   }
+  build_descriptors(M);
   if (!build_lut(M, M.lut)) {
     msg = "unsupported radial basis type";
     return MAGACE_ERR_UNSUPPORTED;

@@ -102,6 +102,19 @@ struct DenseB3 {
   std::vector<double> mult;                 // [nc] half-plane multiplicity of each element's weight
 };
 
+// Per-cluster m-terms of the descriptors B_k, the basis functions that the
+// expansion coefficients multiply (rho_d = sum_k c[d][k] B_k): for clusters
+// of rank 2..4, B = Re sum_e cf_e F[o0] F[o1] F[o2] F[o3] with missing factors
+// ONE; for rank 1, B = g_n(|m_i|) - 1. Clusters are in coefficient order
+// (the file's record order, ranks 1..4).
+struct DescriptorTable {
+  int n1 = 0, nB = 0;            // rank-1 clusters; all clusters
+  std::vector<int32_t> rank1_n;  // [n1] magnetic radial function of each rank-1 cluster
+  std::vector<int32_t> begin;    // [nB - n1 + 1] first term of cluster n1 + k
+  std::vector<double> cf;        // [terms] coupling
+  std::vector<uint16_t> o;       // [terms][4] factor indices
+};
+
 struct RadialLUT {
   int nlut = 0;
   int nfa = 0;  // atomic: g_n (nba), R_nl (n3a*(l3a+1), index nr*(l3a+1)+l), core (1)
@@ -127,6 +140,7 @@ struct Model {
   GatherTable gt;        // every term (generic kernels)
   GatherTable gt_nob3;   // every term except the 3-body ones (specialised kernels)
   DenseB3 db3;           // 3-body terms in dense form (specialised kernels)
+  DescriptorTable desc;  // per-cluster terms without coefficients (descriptors)
   RadialLUT lut;
   bool ready = false;
 };
@@ -135,6 +149,15 @@ struct Model {
 // parsed potential. rcut / rcut_magnetic are the caller's global cutoffs,
 // which set the LUT grid (src/radial.F90:198, :341).
 int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& model, std::string& msg);
+
+// Rebuilds the coefficient-dependent tables after M.coef changed.
+int build_tables(Model& model, std::string& msg);
+
+// Expansion coefficients as one vector [ndensity][num_coefficients], the
+// clusters of ranks 1..4 in the file's record order.
+int num_coefficients(const Model& model);
+void get_coefficients(const Model& model, double* c);
+int set_coefficients(Model& model, const double* c, std::string& msg);
 
 // Clebsch-Gordan coefficient <j1 m1 j2 m2 | J M> by the Racah formula.
 double clebsch_gordan(int j1, int j2, int J, int m1, int m2, int M);

@@ -20,7 +20,7 @@ LIB = os.path.join(OUT, "libmagace.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
-SOURCES = ["potential.cpp", "model.cpp", "capi.cpp", "kernels.cu", "noalloc.cu"]
+SOURCES = ["potential.cpp", "model.cpp", "capi.cpp", "kernels.cu", "noalloc.cu", "md.cu"]
 
 
 def _compile(src: str, extra: list[str]) -> str:

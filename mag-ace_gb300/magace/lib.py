@@ -47,6 +47,17 @@ SIGNATURES = {
     "ace_table_stats": (_i, [ctypes.POINTER(ctypes.c_longlong)]),
     "ace_compute_device_noalloc": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ace_host_access_mode": (_i, []),
+    "ace_num_coefficients": (_i, [_pi, _pi]),
+    "ace_set_work_queue": (_i, [_i]),
+    "ace_md_create": (_i, [_i, _pd, _pd, _pd, _pd, _pi, _d, _d, _d, _pi]),
+    "ace_md_run": (_i, [_i, _i, _d, _i, _i, _pd]),
+    "ace_md_state": (_i, [_i, _pd, _pd, _pd, _pd, _pd]),
+    "ace_md_bonds": (_i, [_i, _pi, _pi, _pi, _pi, _pi]),
+    "ace_md_destroy": (_i, [_i]),
+    "ace_get_coefficients": (_i, [_pd]),
+    "ace_set_coefficients": (_i, [_pd]),
+    "ace_descriptors_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ace_density_gradient_device": (_i, [_i, _vp, _vp]),
 }
 
 _lib = None
@@ -138,6 +149,42 @@ def compute_device(natom, nei, off, r, e, magj, mhj, magi, mhi, energy, fij, tij
     address (e.g. torch.Tensor.data_ptr())."""
     _check(load().ace_compute_device(natom, nei, off, r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0,
                                      stream))
+
+
+def set_work_queue(on: bool) -> None:
+    """Neighbour-count-sorted work queue for the following evaluations."""
+    _check(load().ace_set_work_queue(1 if on else 0))
+
+
+def num_coefficients() -> tuple:
+    """(coefficients per density, number of densities)."""
+    n, nd = ctypes.c_int(), ctypes.c_int()
+    _check(load().ace_num_coefficients(ctypes.byref(n), ctypes.byref(nd)))
+    return n.value, nd.value
+
+
+def get_coefficients() -> np.ndarray:
+    """The expansion coefficients [ndensity, ncoef] in the file's record order."""
+    n, nd = num_coefficients()
+    c = np.zeros((nd, n))
+    _check(load().ace_get_coefficients(_dp(c)))
+    return c
+
+
+def set_coefficients(c) -> None:
+    n, nd = num_coefficients()
+    c = np.ascontiguousarray(np.asarray(c, dtype=np.float64).reshape(nd, n))
+    _check(load().ace_set_coefficients(_dp(c)))
+
+
+def descriptors_device(natom, nei, off, r, e, magj, mhj, magi, mhi, B, stream=0) -> None:
+    """B[natom, ncoef] (FP64, device address) for the given device arrays."""
+    _check(load().ace_descriptors_device(natom, nei, off, r, e, magj, mhj, magi, mhi, B, stream))
+
+
+def density_gradient_device(natom, dedrho, stream=0) -> None:
+    """dE_i/drho_d [natom, 2] of the last evaluation into a device array."""
+    _check(load().ace_density_gradient_device(natom, dedrho, stream))
 
 
 def device_status() -> None:

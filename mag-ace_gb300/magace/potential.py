@@ -85,3 +85,51 @@ def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, elem
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
     return path
+
+
+_WIDTH = {1: 1, 2: 4, 3: 9, 4: 15}
+
+
+def write_coefficients(src: str, dst: str, coefs, rows: dict, element: str = "Fe") -> str:
+    """Copies the potential file `src` to `dst` with new expansion
+    coefficients: coefs[d][k] for the clusters rows[1..4] in coefficient
+    order (ace_basis_rows, the library's order). The value of every 'clu'
+    record (src/util.F90:678-956) is replaced; clusters without a record in
+    `src` and with a nonzero coefficient get one appended. Everything else is
+    copied unchanged. Returns dst."""
+    coefs = np.atleast_2d(np.asarray(coefs, dtype=np.float64))
+    index, k = {}, 0
+    for rank in (1, 2, 3, 4):
+        for row in rows[rank]:
+            index[(rank, tuple(int(x) for x in row))] = k
+            k += 1
+    if coefs.shape[1] != k:
+        raise ValueError(f"expected {k} coefficients per density, got {coefs.shape[1]}")
+    with open(src) as f:
+        lines = f.read().splitlines()
+    seen = set()
+    out, q = [], 0
+    while q < len(lines):
+        line = lines[q]
+        tok = line.split()
+        if len(tok) == 3 and tok[0] == "clu" and q + 1 < len(lines):
+            order, dens = int(tok[1]), int(tok[2])
+            vals = lines[q + 1].split()
+            if order in _WIDTH and 1 <= dens <= coefs.shape[0]:
+                key = (order, tuple(int(x) for x in vals[order:order + _WIDTH[order]]))
+                if key in index:
+                    vals[order + _WIDTH[order]] = repr(float(coefs[dens - 1, index[key]]))
+                    seen.add((dens, index[key]))
+            out += [line, " " + "   ".join(vals)]
+            q += 2
+            continue
+        out.append(line)
+        q += 1
+    for (rank, row), kk in index.items():
+        for d in range(coefs.shape[0]):
+            if (d + 1, kk) not in seen and coefs[d, kk] != 0.0:
+                out += [f" clu            {rank}           {d + 1}",
+                        f" {' '.join([element] * rank)}   {' '.join(str(x) for x in row)}   {float(coefs[d, kk])!r}   T"]
+    with open(dst, "w") as f:
+        f.write("\n".join(out) + "\n")
+    return dst

@@ -205,3 +205,74 @@ def total_forces(nb: NeighborData, flist: np.ndarray, tlist: np.ndarray, tlist0:
     np.add.at(f, nb.j_of_bond, fl)
     np.add.at(fm, nb.j_of_bond, -tl)
     return f, fm
+
+
+def bcc_110_slab(nx: int, ny: int, layers: int, a: float, vacuum: float) -> tuple[np.ndarray, np.ndarray]:
+    """bcc (110) slab in the orthogonal cell x || [1-10], y || [001],
+    z || [110] (lengths a*sqrt2, a, a*sqrt2 per repeat, 4 atoms), `layers`
+    repeats along z plus `vacuum` Angstrom of empty space on top."""
+    s2 = np.sqrt(2.0)
+    # the 4-atom orthogonal cell, fractional coordinates
+    base = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]])
+    lx, ly, lz = a * s2, a, a * s2
+    grid = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(layers), indexing="ij"), -1).reshape(-1, 1, 3)
+    pos = ((grid + base[None]) * np.array([lx, ly, lz])).reshape(-1, 3)
+    cell = np.diag([nx * lx, ny * ly, layers * lz + vacuum])
+    return pos, cell
+
+
+def uneven_batch(nconf: int = 256, seed: int = 3) -> list:
+    """Independent configurations of 16-432 atoms with 20-70 neighbours per
+    atom within 5 A: bcc and fcc Fe bulk, bcc cells with vacancies, and
+    (100) / (110) bcc slabs with 10 A of vacuum; jitter N(0, 0.1 A), random
+    spins with |m| ~ U(1.5, 2.6) mu_B."""
+    rng = np.random.default_rng(seed)
+    out = []
+    kinds = ("bcc", "fcc", "vac", "s100", "s110")
+    for c in range(nconf):
+        kind = kinds[c % len(kinds)]
+        pbc = (True, True, True)
+        if kind == "bcc":
+            n = int(rng.integers(2, 7))                     # 16 .. 432 atoms
+            pos, cell = bcc_cubic(n, n, n, 2.83)
+        elif kind == "fcc":
+            n = int(rng.integers(2, 5))                     # 32 .. 256 atoms
+            pos, cell = fcc_cubic(n, n, n, 3.59)
+        elif kind == "vac":
+            n = int(rng.integers(3, 7))
+            pos, cell = bcc_cubic(n, n, n, 2.83)
+            keep = rng.random(len(pos)) > 0.05
+            keep[0] = True
+            pos = pos[keep]
+        elif kind == "s100":
+            n, layers = int(rng.integers(2, 5)), int(rng.integers(2, 6))
+            pos, cell = bcc_cubic(n, n, layers, 2.83)
+            cell[2, 2] += 10.0
+            pbc = (True, True, False)
+        else:
+            n, layers = int(rng.integers(2, 4)), int(rng.integers(2, 5))
+            pos, cell = bcc_110_slab(n, 2 * n, layers, 2.83, 10.0)
+            pbc = (True, True, False)
+        pos = pos + rng.normal(0.0, 0.1, size=pos.shape)
+        m = len(pos)
+        out.append(Structure(pos, cell, pbc, rng.uniform(1.5, 2.6, m), random_unit(rng, m)))
+    return out
+
+
+def concat_neighbor_data(parts: list) -> NeighborData:
+    """One acelib_ input of independent configurations: atoms and bonds of
+    part k follow those of part k-1 (bond ranges and j indices shifted)."""
+    a_off = np.cumsum([0] + [p.natom for p in parts])
+    b_off = np.cumsum([0] + [p.nei for p in parts])
+    cat = lambda name: np.ascontiguousarray(np.concatenate([getattr(p, name) for p in parts]))
+    return NeighborData(
+        natom=int(a_off[-1]), nall=int(a_off[-1]), nei=int(b_off[-1]),
+        nlist=np.concatenate([p.nlist + a for p, a in zip(parts, a_off)]).astype(np.int32),
+        occ=cat("occ"), occlist=cat("occlist"),
+        nstart=np.concatenate([p.nstart + b for p, b in zip(parts, b_off)]).astype(np.int32),
+        nstop=np.concatenate([p.nstop + b for p, b in zip(parts, b_off)]).astype(np.int32),
+        dlist=cat("dlist"), elist=cat("elist"), dlist_momi=cat("dlist_momi"), elist_momi=cat("elist_momi"),
+        dlist_mom=cat("dlist_mom"), elist_mom=cat("elist_mom"),
+        i_of_bond=np.concatenate([p.i_of_bond + a for p, a in zip(parts, a_off)]),
+        j_of_bond=np.concatenate([p.j_of_bond + a for p, a in zip(parts, a_off)]),
+        shift=np.concatenate([p.shift for p in parts]))

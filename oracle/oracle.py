@@ -59,6 +59,8 @@ def _load(fast: bool) -> ctypes.CDLL:
     lib.oracle_atom_state.argtypes = [_i, _i, _pi, _pi, _pd, _pd, _pd, _pd, _pd, _pd, _i, _pd, _pd,
                                       _pd, _pd, _pd, _pd, _pd, _pd]
     lib.oracle_atom_state.restype = _i
+    lib.oracle_descriptors.argtypes = [_i, _i, _pi, _pi, _pd, _pd, _pd, _pd, _pd, _pd, _pd, _pd]
+    lib.oracle_descriptors.restype = _i
     _libs[name] = lib
     return lib
 
@@ -124,6 +126,19 @@ class Oracle:
             raise RuntimeError(f"oracle_acelib failed ({st}): "
                                + self.lib.oracle_last_error().decode())
         return eout, flist, tlist, tlist0
+
+    def descriptors(self, nb):
+        """(B [natom, nvar1+..+nvar4], dE/drho [natom, 2]) of every atom."""
+        self._activate()
+        nB = sum(self.nvar[:4])
+        B = np.zeros((max(1, nb.natom), nB))
+        dedrho = np.zeros((max(1, nb.natom), 2))
+        st = self.lib.oracle_descriptors(nb.natom, nb.nei, _ip(nb.nstart), _ip(nb.nstop), _dp(nb.dlist),
+                                         _dp(nb.elist), _dp(nb.dlist_momi), _dp(nb.elist_momi),
+                                         _dp(nb.dlist_mom), _dp(nb.elist_mom), _dp(B), _dp(dedrho))
+        if st:
+            raise RuntimeError(f"oracle_descriptors failed ({st}): " + self.lib.oracle_last_error().decode())
+        return B[: nb.natom], dedrho[: nb.natom]
 
     def atom_state(self, nb, atom: int, dims: dict) -> dict:
         """Intermediates of one atom (0-based `atom`); `dims` gives the basis

@@ -1124,4 +1124,64 @@ int oracle_atom_state(int natom, int nei, const int* nstart, const int* nstop, c
   return ORACLE_OK;
 }
 
+// Descriptors B[natom][nvar1 + nvar2 + nvar3 + nvar4] (the prepB packs,
+// src/b_basis.F90:6-536, in cluster order) and dE/drho [natom][2] (from the
+// embedding step of forceweights, src/forces.F90:976-1289). Not part of the
+// reference's interface: test support for the differentiation harness.
+int oracle_descriptors(int natom, int nei, const int* nstart, const int* nstop, const double* dlist,
+                       const double* elist, const double* dlist_momi, const double* elist_momi,
+                       const double* dlist_mom, const double* elist_mom, double* B, double* dedrho) {
+  const OracleState& s = g_state;
+  if (!s.initialized) return ORACLE_ERR_NOT_INIT;
+  int st = validate(natom, nei, nullptr, nullptr, nstart, nstop);
+  if (st) return st;
+  Inputs in;
+  in.natom = natom;
+  in.nei = nei;
+  in.nstart = nstart;
+  in.nstop = nstop;
+  in.dlist = dlist;
+  in.elist = elist;
+  in.dlist_momi = dlist_momi;
+  in.elist_momi = elist_momi;
+  in.dlist_mom = dlist_mom;
+  in.elist_mom = elist_mom;
+  const int nB = s.nvar1 + s.nvar2 + s.nvar3 + s.nvar4;
+  const int chunk = 32;
+  Chunk ch;
+  for (int c0 = 1; c0 <= natom; c0 += chunk) {
+    const int c1 = std::min(natom, c0 + chunk - 1);
+    const int na = c1 - c0 + 1;
+    int nb = 0;
+    for (int i = c0; i <= c1; ++i) nb += std::max(0, nstop[i - 1] - nstart[i - 1] + 1);
+    ch.alloc(s, na, nb);
+    ch.atom.assign(na + 1, 0);
+    ch.lbase.assign(na + 1, 1);
+    int run = 1;
+    for (int la = 1; la <= na; ++la) {
+      ch.atom[la] = c0 + la - 1;
+      ch.lbase[la] = run;
+      run += std::max(0, nstop[c0 + la - 2] - nstart[c0 + la - 2] + 1);
+    }
+    ch.na = na;
+    st = prepA(s, in, ch);
+    if (st) return st;
+    prepB(s, ch);
+    forceweights(s, ch);
+    for (int la = 1; la <= na; ++la) {
+      double* b = B + static_cast<size_t>(c0 + la - 2) * nB;
+      int k = 0;
+      for (int c = 1; c <= s.nvar1; ++c) b[k++] = ch.b1pack(c, la);
+      for (int c = 1; c <= s.nvar2; ++c) b[k++] = ch.b2pack(c, la);
+      for (int c = 1; c <= s.nvar3; ++c) b[k++] = ch.b3pack(c, la);
+      for (int c = 1; c <= s.nvar4; ++c) b[k++] = ch.b4pack(c, la);
+      if (dedrho) {
+        dedrho[2 * (c0 + la - 2)] = ch.dEdrho_out[2 * la];
+        dedrho[2 * (c0 + la - 2) + 1] = ch.dEdrho_out[2 * la + 1];
+      }
+    }
+  }
+  return ORACLE_OK;
+}
+
 }  // extern "C"
