@@ -144,7 +144,7 @@ int ace_kernel_times(float* ms);
  * angular combinations, half-plane elements, and the segments and entries of
  * the remaining (non-3-body) gather table; out[26..28] that table's entries
  * by arity 1..3; out[29] the coefficient pairs the dense 3-body contraction
- * visits per atom (30 entries). */
+ * visits per atom; out[30] the factors that table reads (31 entries). */
 int ace_table_stats(long long* out);
 
 /* Allocation-free variant of ace_compute_device, for callers that cannot

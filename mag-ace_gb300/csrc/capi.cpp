@@ -77,10 +77,11 @@ struct Runtime {
   int device = -1;
   cudaStream_t stream = nullptr;
   DevBuf<double> lut_a, lut_m, c1;
+  DevBuf<float> c1f;
   DevBuf<float> lut_a32, lut_m32;
   struct GatherBufs {
     DevBuf<double> kap[4], slot_mult;
-    DevBuf<float> kapf[4];
+    DevBuf<float> kapf[4], slot_multf;
     DevBuf<uint32_t> o12[4];
     DevBuf<uint16_t> o3;
     DevBuf<int32_t> grp_arity, grp_len, grp_first, grp_seg, slot_seg, slot_factor, slot_weight;
@@ -91,6 +92,7 @@ struct Runtime {
         o12[a].release();
       }
       slot_mult.release();
+      slot_multf.release();
       o3.release();
       for (auto* b : {&grp_arity, &grp_len, &grp_first, &grp_seg, &slot_seg, &slot_factor, &slot_weight}) b->release();
     }
@@ -99,6 +101,8 @@ struct Runtime {
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
   DevBuf<uint16_t> b3_code;
   DevBuf<int32_t> d_rank1_n, d_begin;
+  DevBuf<int32_t> r_factor, r_run, r_g0, r_warp_begin, r_warp_slots;
+  DevBuf<uint32_t> r_rec;
   DevBuf<double> d_cf;
   DevBuf<uint16_t> d_o;
   DeviceModel dm{};
@@ -183,6 +187,7 @@ int upload_gather(const GatherTable& g, Runtime::GatherBufs& B, GatherView& v) {
   CUDA_TRY(B.slot_factor.upload(g.slot_factor));
   CUDA_TRY(B.slot_weight.upload(g.slot_weight));
   CUDA_TRY(B.slot_mult.upload(g.slot_mult));
+  CUDA_TRY(B.slot_multf.upload(to_float(g.slot_mult)));
   v.nslot = g.nslot;
   v.nG0 = g.nG0;
   v.nseg = g.nseg;
@@ -206,6 +211,7 @@ int upload_gather(const GatherTable& g, Runtime::GatherBufs& B, GatherView& v) {
   v.slot_factor = B.slot_factor.p;
   v.slot_weight = B.slot_weight.p;
   v.slot_mult = B.slot_mult.p;
+  v.slot_multf = B.slot_multf.p;
   return MAGACE_OK;
 }
 
@@ -227,6 +233,7 @@ int upload_tables() {
   for (int d = 0; d < 2; ++d)
     for (int n = 0; n < M.L.nbm; ++n) c1[d * M.L.nbm + n] = M.c1[d][n];
   CUDA_TRY(R.c1.upload(c1));
+  CUDA_TRY(R.c1f.upload(to_float(c1)));
   {
     int st = upload_gather(M.gt, R.gb1, R.dm.g);
     if (st) return st;
@@ -242,6 +249,13 @@ int upload_tables() {
       CUDA_TRY(R.b3_factor.upload(D.factor_of));
       CUDA_TRY(R.b3_cw.upload(D.compact_of_weight));
       CUDA_TRY(R.b3_mult.upload(to_float(D.mult)));
+      const RestTable& T = M.rest;
+      CUDA_TRY(R.r_factor.upload(T.factor_of));
+      CUDA_TRY(R.r_run.upload(T.run));
+      CUDA_TRY(R.r_g0.upload(T.slot_g0));
+      CUDA_TRY(R.r_rec.upload(T.rec));
+      CUDA_TRY(R.r_warp_begin.upload(T.warp_begin));
+      CUDA_TRY(R.r_warp_slots.upload(T.warp_slots));
     } else {
       R.dm.g2 = R.dm.g;
     }
@@ -280,6 +294,9 @@ int upload_tables() {
   d.lut_a32 = R.lut_a32.p;
   d.lut_m32 = R.lut_m32.p;
   d.c1 = R.c1.p;
+  d.c1f = R.c1f.p;
+  d.rscale_a_f = static_cast<float>(d.rscale_a);
+  d.rscale_m_f = static_cast<float>(d.rscale_m);
   d.b3_ntask = M.db3.ntask;
   d.b3_ncombo = M.db3.ncombo;
   d.b3_nc = M.db3.nc;
@@ -291,6 +308,14 @@ int upload_tables() {
   d.b3_factor = R.b3_factor.p;
   d.b3_cw = R.b3_cw.p;
   d.b3_mult = R.b3_mult.p;
+  d.r_nfac = M.rest.nfac;
+  d.r_nslot = M.rest.nslot;
+  d.r_factor = R.r_factor.p;
+  d.r_run = R.r_run.p;
+  d.r_rec = R.r_rec.p;
+  d.r_g0 = R.r_g0.p;
+  d.r_warp_begin = R.r_warp_begin.p;
+  d.r_warp_slots = R.r_warp_slots.p;
   d.d_n1 = M.desc.n1;
   d.d_nB = M.desc.nB;
   d.d_rank1_n = R.d_rank1_n.p;
@@ -597,6 +622,7 @@ int ace_table_stats(long long* out) {
       pairs += D.NM * (pat == 0 ? i + 1 : (pat == 1 ? (i / D.NM + 1) * D.NM : (i / D.NM) * D.NM));
   }
   out[29] = pairs;
+  out[30] = R.model.rest.nfac;
   return MAGACE_OK;
 }
 
@@ -713,10 +739,12 @@ void ace_release_device(void) {
   for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.r, &R.e, &R.magj, &R.mhj, &R.magi, &R.mhi, &R.energy, &R.fij,
                   &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
     b->release();
-  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult}) b->release();
+  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult, &R.c1f}) b->release();
   for (auto* b : {&R.b3_pattern, &R.b3_combo, &R.b3_factor, &R.b3_cw}) b->release();
   R.b3_code.release();
-  for (auto* b : {&R.d_rank1_n, &R.d_begin}) b->release();
+  for (auto* b : {&R.d_rank1_n, &R.d_begin, &R.r_factor, &R.r_run, &R.r_g0, &R.r_warp_begin, &R.r_warp_slots})
+    b->release();
+  R.r_rec.release();
   R.d_cf.release();
   R.d_o.release();
   R.gb1.release();

@@ -11,6 +11,10 @@ constexpr int kMaxL = 4;
 constexpr int kMaxHalf = (kMaxL + 1) * (kMaxL + 2) / 2;  // packed (l, m >= 0)
 constexpr int kMaxFull = (kMaxL + 1) * (kMaxL + 1);      // packed (l, -l..l)
 
+// warps of the split-precision rest kernel; its slot schedule is built for
+// this many on the host
+constexpr int kRestTableWarps = 32;
+
 // device-side error codes (first one wins)
 enum DeviceError : int {
   kDevOk = 0,
@@ -37,6 +41,7 @@ struct GatherView {
   const int32_t* slot_factor;  // [nslot] (G0 slots only)
   const int32_t* slot_weight;  // [nslot]
   const double* slot_mult;     // [nslot]
+  const float* slot_multf;     // FP32 copy (split path)
 };
 
 struct DeviceModel {
@@ -57,6 +62,9 @@ struct DeviceModel {
   const float* lut_m32;
   // 1-body coefficients c1[d * nbm + n]
   const double* c1;
+  // FP32 copies of the scale factors and 1-body coefficients (split path)
+  float rscale_a_f, rscale_m_f;
+  const float* c1f;
   // gather tables in warp groups (see model.hpp): g holds every term (generic
   // kernels), g2 every term except the 3-body ones (specialised kernels)
   GatherView g, g2;
@@ -70,6 +78,14 @@ struct DeviceModel {
   const int32_t* b3_factor;   // [nc] factor index of each compact element
   const int32_t* b3_cw;       // [nW] compact element of each weight, or -1
   const float* b3_mult;       // [nc] half-plane multiplicity of each element's weight
+  // per-slot table of the 2- and 4-body terms (see model.hpp RestTable)
+  int r_nfac, r_nslot;
+  const int32_t* r_factor;
+  const int32_t* r_run;         // [3 * nslot + 1]
+  const uint32_t* r_rec;        // [entries][4]
+  const int32_t* r_g0;
+  const int32_t* r_warp_begin;  // [warps + 1]
+  const int32_t* r_warp_slots;
   // work queue of this evaluation: atoms in order of decreasing bond count,
   // or null for the natural order (set per launch)
   const int32_t* order;

@@ -67,6 +67,39 @@ __device__ __forceinline__ void raise_error(int* err, int code) {
 // order when the evaluation has one, else atom `it`.
 __device__ __forceinline__ int queue_atom(const DeviceModel& m, int it) { return m.order ? __ldg(m.order + it) : it; }
 
+// Model constants in the working precision (the split path reads FP32
+// copies made on the host instead of converting on the FP64 pipe).
+template <class R>
+__device__ __forceinline__ R rscale_a(const DeviceModel& m);
+template <>
+__device__ __forceinline__ double rscale_a<double>(const DeviceModel& m) {
+  return m.rscale_a;
+}
+template <>
+__device__ __forceinline__ float rscale_a<float>(const DeviceModel& m) {
+  return m.rscale_a_f;
+}
+template <class R>
+__device__ __forceinline__ R rscale_m(const DeviceModel& m);
+template <>
+__device__ __forceinline__ double rscale_m<double>(const DeviceModel& m) {
+  return m.rscale_m;
+}
+template <>
+__device__ __forceinline__ float rscale_m<float>(const DeviceModel& m) {
+  return m.rscale_m_f;
+}
+template <class R>
+__device__ __forceinline__ R c1_of(const DeviceModel& m, int k);
+template <>
+__device__ __forceinline__ double c1_of<double>(const DeviceModel& m, int k) {
+  return m.c1[k];
+}
+template <>
+__device__ __forceinline__ float c1_of<float>(const DeviceModel& m, int k) {
+  return __ldg(m.c1f + k);
+}
+
 // Double <-> float conversions on the integer pipes. A hardware conversion
 // issues on the FP64 pipe, which GB300 runs at 1/64 of the FP32 rate; the
 // split path converts every input and output, so it uses these instead.
@@ -246,7 +279,7 @@ __device__ __forceinline__ int atomic_bin(const DeviceModel& m, double r, double
 // carries ~1e-7 relative error, far inside the interpolant's own)
 template <class R>
 __device__ __forceinline__ int atomic_bin_r(const DeviceModel& m, R r, R& wl, int* err) {
-  const R x = r * R(m.rscale_a);
+  const R x = r * rscale_a<R>(m);
   if (!(x >= R(1))) {
     raise_error(err, kDevSmallR);
     return -1;
@@ -258,7 +291,7 @@ __device__ __forceinline__ int atomic_bin_r(const DeviceModel& m, R r, R& wl, in
 }
 template <class R>
 __device__ __forceinline__ int magnetic_bin_r(const DeviceModel& m, R mag, R& wl, int* err) {
-  const R x = mag * R(m.rscale_m);
+  const R x = mag * rscale_m<R>(m);
   if (!(x >= R(0)) || x >= R(m.nlut)) {
     raise_error(err, kDevMoment);
     return -1;
@@ -318,9 +351,9 @@ __global__ void __launch_bounds__(kAbasisThreads)
         double wl = 0.0;
         const int nla = atomic_bin(m, r, wl, err);
         if (nla > 0) {
-          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, 0, m.nba, nla, R(wl), R(m.rscale_a), g, dummy);
-          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba, m.n3a * (m.l3a + 1), nla, R(wl), R(m.rscale_a), Rv, dummy);
-          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba + m.n3a * (m.l3a + 1), 1, nla, R(wl), R(m.rscale_a), cv, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, 0, m.nba, nla, R(wl), rscale_a<R>(m), g, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba, m.n3a * (m.l3a + 1), nla, R(wl), rscale_a<R>(m), Rv, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba + m.n3a * (m.l3a + 1), 1, nla, R(wl), rscale_a<R>(m), cv, dummy);
         } else {
           for (int q = 0; q < m.nba; ++q) g[q] = R(0);
           for (int q = 0; q < m.n3a * (m.l3a + 1); ++q) Rv[q] = R(0);
@@ -330,7 +363,7 @@ __global__ void __launch_bounds__(kAbasisThreads)
         const int nlm = magnetic_bin(m, magj[j], wm, err);
         const int nM = m.n2m * (m.l2m + 1);
         if (nlm > 0) {
-          lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nM, nlm, R(wm), R(m.rscale_m), Mv, dummy);
+          lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nM, nlm, R(wm), rscale_m<R>(m), Mv, dummy);
         } else {
           for (int q = 0; q < nM; ++q) Mv[q] = R(nlm == 0 ? 1 : 0);
         }
@@ -432,8 +465,8 @@ __global__ void __launch_bounds__(kAbasisThreads)
       R Mv[32], gm[32], dummy[1];
       const int nM = m.n2m * (m.l2m + 1);
       if (nl > 0) {
-        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nM, nl, R(wl), R(m.rscale_m), Mv, dummy);
-        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, nM, m.nbm, nl, R(wl), R(m.rscale_m), gm, dummy);
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nM, nl, R(wl), rscale_m<R>(m), Mv, dummy);
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), m.nfm, nM, m.nbm, nl, R(wl), rscale_m<R>(m), gm, dummy);
       } else {
         for (int q = 0; q < nM; ++q) Mv[q] = R(nl == 0 ? 1 : 0);
         for (int q = 0; q < m.nbm; ++q) gm[q] = R(nl == 0 ? 1 : 0);
@@ -701,18 +734,18 @@ __global__ void __launch_bounds__(kForceThreads)
       R cd = R(0);
       const int nla = atomic_bin(m, r, wl, err);
       if (nla > 0) {
-        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, 0, m.nba, nla, R(wl), R(m.rscale_a), tmpv, tmpd);
+        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, 0, m.nba, nla, R(wl), rscale_a<R>(m), tmpv, tmpd);
         for (int n = 0; n < m.nba; ++n) {
           cg[n * T + t] = tmpv[n];
           cgd[n * T + t] = tmpd[n];
         }
-        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba, nRl, nla, R(wl), R(m.rscale_a), tmpv, tmpd);
+        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba, nRl, nla, R(wl), rscale_a<R>(m), tmpv, tmpd);
         for (int q = 0; q < nRl; ++q) {
           cR[q * T + t] = tmpv[q];
           cRd[q * T + t] = tmpd[q];
         }
         R cv[1], cdv[1];
-        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba + nRl, 1, nla, R(wl), R(m.rscale_a), cv, cdv);
+        lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), m.nfa, m.nba + nRl, 1, nla, R(wl), rscale_a<R>(m), cv, cdv);
         cd = cdv[0];
       } else {
         for (int n = 0; n < m.nba; ++n) cg[n * T + t] = cgd[n * T + t] = R(0);
@@ -721,7 +754,7 @@ __global__ void __launch_bounds__(kForceThreads)
       double wm = 0.0;
       const int nlm = magnetic_bin(m, mg, wm, err);
       if (nlm > 0) {
-        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nMl, nlm, R(wm), R(m.rscale_m), tmpv, tmpd);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nMl, nlm, R(wm), rscale_m<R>(m), tmpv, tmpd);
         for (int q = 0; q < nMl; ++q) {
           cM[q * T + t] = tmpv[q];
           cMd[q * T + t] = tmpd[q];
@@ -841,8 +874,8 @@ __global__ void __launch_bounds__(kForceThreads)
       const int nl = magnetic_bin(m, mg, wm, err);
       R Mv[32], Md[32], gm[32], gmd[32];
       if (nl > 0) {
-        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nMl, nl, R(wm), R(m.rscale_m), Mv, Md);
-        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, nMl, m.nbm, nl, R(wm), R(m.rscale_m), gm, gmd);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, 0, nMl, nl, R(wm), rscale_m<R>(m), Mv, Md);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), m.nfm, nMl, m.nbm, nl, R(wm), rscale_m<R>(m), gm, gmd);
       } else {
         for (int q = 0; q < nMl; ++q) {
           Mv[q] = R(nl == 0 ? 1 : 0);
@@ -965,12 +998,12 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       double* rho_rest = static_cast<double*>(b.aux);
       const size_t s2 = density_fe_smem(m);
       set_smem(k_density_fe<FeDims>, s2);
-      k_density_fe<FeDims><<<grid, kDensityFeThreads, s2, st>>>(m, natom, reinterpret_cast<const C<float>*>(b.F),
-                                                                reinterpret_cast<C<float>*>(b.W), rho_rest);
+      const int nblk = (natom + 31) / 32;
+      k_density_fe<FeDims><<<nblk < grid_cap ? nblk : grid_cap, kRestWarps * 32, s2, st>>>(
+          m, natom, reinterpret_cast<const C<float>*>(b.F), reinterpret_cast<C<float>*>(b.W), rho_rest);
       if (ev_between) cudaEventRecord(ev_between, st);
       const size_t sb = b3_fe_smem<FeDims>(m);
       set_smem(k_b3_fe<FeDims>, sb);
-      const int nblk = (natom + 31) / 32;
       k_b3_fe<FeDims><<<nblk < grid_cap ? nblk : grid_cap, kB3Warps * 32, sb, st>>>(
           m, natom, reinterpret_cast<const C<float>*>(b.F), reinterpret_cast<C<float>*>(b.W), b.rho1, rho_rest,
           b.core, b.energy, b.edf, b.dedrho, b.err);

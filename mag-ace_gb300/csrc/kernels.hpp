@@ -12,7 +12,6 @@ namespace magace {
 constexpr int kAbasisThreads = 128;
 constexpr int kAbasisTile = 64;  // bonds per feature tile
 constexpr int kDensityThreads = 256;
-constexpr int kDensityFeThreads = 128;
 constexpr int kForceThreads = 64;
 constexpr int kMaxFeat = 32;     // per-bond radial functions of one kind
 constexpr int kMaxLaunches = 4;  // kernels of one evaluation

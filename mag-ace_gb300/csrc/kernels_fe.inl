@@ -59,10 +59,10 @@ __global__ void __launch_bounds__(64)
   C<R>* sRY = reinterpret_cast<C<R>*>(smem);             // [TB][NRY]
   C<R>* sQ = sRY + TB * D::NRY;                           // [TB][NQ]
   R* sg = reinterpret_cast<R*>(sQ + TB * D::NQ);          // [TB][NB]
-  double* score = reinterpret_cast<double*>(sg + TB * D::NB);  // [TB]
+  R* score = sg + TB * D::NB;                             // [TB]
   C<R>* accA = sRY;                                       // reuse after the tiles: [NRY][NQ3]
   C<R>* accA2 = accA + D::NWA;                            // [NB][NQ]
-  __shared__ double s_core;
+  CSum<R> core_sum;  // thread 0: the atom's core energy, over its bond tiles
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int row = lane >> 1, cb = lane & 1;
 
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(64)
     C<R> acc[15];
 #pragma unroll
     for (int c = 0; c < 15; ++c) acc[c] = {R(0), R(0)};
-    if (t == 0) s_core = 0.0;
+    core_sum = CSum<R>();
     const int b0 = off[atom], b1 = off[atom + 1];
     for (int t0 = b0; t0 < b1; t0 += TB) {
       const int nb = min(TB, b1 - t0);
@@ -82,9 +82,9 @@ __global__ void __launch_bounds__(64)
         R wl = R(0);
         const int nla = atomic_bin_r<R>(m, to_r<R>(rr[j]), wl, err);
         if (nla > 0) {
-          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, R(m.rscale_a), g, dummy);
-          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, R(m.rscale_a), Rv, dummy);
-          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, R(m.rscale_a), cv, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, rscale_a<R>(m), g, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, rscale_a<R>(m), Rv, dummy);
+          lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, rscale_a<R>(m), cv, dummy);
         } else {
 #pragma unroll
           for (int q = 0; q < D::NB; ++q) g[q] = R(0);
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(64)
         R wm = R(0);
         const int nlm = magnetic_bin_r<R>(m, to_r<R>(magj[j]), wm, err);
         if (nlm > 0) {
-          lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, R(m.rscale_m), Mv, dummy);
+          lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, rscale_m<R>(m), Mv, dummy);
         } else {
 #pragma unroll
           for (int q = 0; q < D::NMF; ++q) Mv[q] = R(nlm == 0 ? 1 : 0);
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(64)
           for (int h = 0; h < D::H2; ++h) sQ[t * D::NQ + nr * D::H2 + h] = cscale(Ym[h], Mv[nr * (D::L2 + 1) + l_of_h(h)]);
 #pragma unroll
         for (int n = 0; n < D::NB; ++n) sg[t * D::NB + n] = g[n];
-        score[t] = to_d(cv[0]);
+        score[t] = cv[0];
       }
       __syncthreads();
       if (warp == 0) {
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(64)
         }
       }
       if (t == 0)
-        for (int b = 0; b < nb; ++b) s_core += score[b];
+        for (int b = 0; b < nb; ++b) core_sum.add(score[b]);
     }
     __syncthreads();
     if (warp == 0) {
@@ -187,18 +187,20 @@ __global__ void __launch_bounds__(64)
       Fa[m.offA2 + s] = v;
     }
     if (t == 0) {
-      double wl = 0.0;
-      const int nl = magnetic_bin(m, magi[atom], wl, err);
+      // on-site A0 and the 1-body density in the working precision
+      R wl = R(0);
+      const int nl = magnetic_bin_r<R>(m, to_r<R>(magi[atom]), wl, err);
       R Mv[D::NMF], gm[D::NBM], dummy[1];
       if (nl > 0) {
-        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, R(wl), R(m.rscale_m), Mv, dummy);
-        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, R(wl), R(m.rscale_m), gm, dummy);
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, wl, rscale_m<R>(m), Mv, dummy);
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, wl, rscale_m<R>(m), gm, dummy);
       } else {
         for (int q = 0; q < D::NMF; ++q) Mv[q] = R(nl == 0 ? 1 : 0);
         for (int q = 0; q < D::NBM; ++q) gm[q] = R(nl == 0 ? 1 : 0);
       }
       C<R> Yi[D::H2];
-      ylm_half<R, false>(D::L2, R(mhi[3 * atom]), R(mhi[3 * atom + 1]), R(mhi[3 * atom + 2]), Yi, nullptr);
+      ylm_half<R, false>(D::L2, to_r<R>(mhi[3 * atom]), to_r<R>(mhi[3 * atom + 1]), to_r<R>(mhi[3 * atom + 2]), Yi,
+                         nullptr);
       for (int nr = 0; nr < D::N2; ++nr)
         for (int l = 0; l <= D::L2; ++l)
           for (int mm = -l; mm <= l; ++mm)
@@ -206,11 +208,11 @@ __global__ void __launch_bounds__(64)
       Fa[m.offOne] = {R(1), R(0)};
       Fa[m.offZero] = {R(0), R(0)};
       for (int d = 0; d < m.nd; ++d) {
-        double s = 0.0;
-        for (int n = 0; n < D::NBM; ++n) s += m.c1[d * D::NBM + n] * (static_cast<double>(gm[n]) - 1.0);
-        rho1[static_cast<size_t>(atom) * 2 + d] = s;
+        CSum<R> s1;
+        for (int n = 0; n < D::NBM; ++n) s1.add(c1_of<R>(m, d * D::NBM + n) * (gm[n] - R(1)));
+        rho1[static_cast<size_t>(atom) * 2 + d] = s1.value();
       }
-      core_out[atom] = s_core;
+      core_out[atom] = core_sum.value();
     }
     __syncthreads();
   }
@@ -233,89 +235,91 @@ __global__ void __launch_bounds__(64)
 // so that each thread has that many in flight.
 constexpr int kBatch = 8;
 
-// k_density_fe. Shared memory: Fs[nF], part[g2.nseg] (complex float).
+
+// k_density_fe: 32 atoms per CTA, one per lane; every warp walks its share
+// of the output slots of the rest table (dealt longest first on the host).
+// All lanes of a warp read the same 16-byte entry records (uniform loads)
+// and apply them to their own atom's factors, staged in shared memory as
+// Fs[factor][atom]. Slot totals are FP32 sums in entry order; the density
+// terms of the A0 slots add up per lane in FP64, and the per-warp partials
+// in warp order.
+constexpr int kRestWarps = kRestTableWarps;
+constexpr int kRestStride = 33;  // row stride of Fs in complex elements
+
+template <int A>
+__device__ __forceinline__ void rest_run(const uint4* __restrict__ rec, int e0, int e1, const C<float>* Fs, int lane,
+                                         float& vx, float& vy) {
+  for (int e = e0; e < e1; ++e) {
+    const uint4 r = __ldg(rec + e);
+    const float k = __uint_as_float(r.x);
+    C<float> p = Fs[(r.y & 0xffffu) * kRestStride + lane];
+    if (A >= 2) p = cmul(p, Fs[(r.y >> 16) * kRestStride + lane]);
+    if (A >= 3) p = cmul(p, Fs[r.z * kRestStride + lane]);
+    vx += k * p.x;
+    vy += k * p.y;
+  }
+}
+
 template <class D>
-__global__ void __launch_bounds__(kDensityFeThreads)
+__global__ void __launch_bounds__(kRestWarps * 32, 1)
     k_density_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
                  double* __restrict__ rho_rest) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const GatherView& g = m.g2;
-  C<float>* Fs = reinterpret_cast<C<float>*>(smem);
-  C<float>* part = Fs + ((m.nF + 1) & ~1);
-  __shared__ double s_red[kDensityFeThreads / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int nf = m.r_nfac, nW = m.nW;
+  const GatherView& g = m.g2;  // slot weights and multiplicities (same slot numbering)
+  C<float>* Fs = reinterpret_cast<C<float>*>(smem);                   // [nf][33]
+  double* rpart = reinterpret_cast<double*>(Fs + nf * kRestStride);   // [kRestWarps][32]
+  __shared__ int s_atom[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (natom + 31) / 32;
+  const uint4* rec = reinterpret_cast<const uint4*>(m.r_rec);
+  const int w0 = __ldg(m.r_warp_begin + warp), w1 = __ldg(m.r_warp_begin + warp + 1);
 
-  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
-    const int atom = queue_atom(m, it);
-    const C<float>* Fa = F + static_cast<size_t>(atom) * m.nF;
-    for (int s0 = 0; s0 < m.nF; s0 += kBatch * kDensityFeThreads) {
-      C<float> v[kBatch];
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int a0 = blk * 32;
+    const int na = min(32, natom - a0);
+    __syncthreads();
+    if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
+    __syncthreads();
+    // stage: thread c takes factor c of every atom, kBatch atoms in flight
+    for (int c = threadIdx.x; c < nf; c += blockDim.x) {
+      const int fc = __ldg(m.r_factor + c);
+      for (int ab = 0; ab < 32; ab += kBatch) {
+        C<float> v[kBatch];
 #pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int s = s0 + b * kDensityFeThreads + threadIdx.x;
-        if (s < m.nF) v[b] = Fa[s];
-      }
+        for (int b = 0; b < kBatch; ++b)
+          v[b] = ab + b < na ? F[static_cast<size_t>(s_atom[ab + b]) * m.nF + fc] : C<float>{0.f, 0.f};
 #pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int s = s0 + b * kDensityFeThreads + threadIdx.x;
-        if (s < m.nF) Fs[s] = v[b];
+        for (int b = 0; b < kBatch; ++b) Fs[c * kRestStride + ab + b] = v[b];
       }
     }
     __syncthreads();
-    // segment partials of the gather table
-    for (int gi = warp; gi < g.ngroup; gi += nwarp) {
-      const int a = g.grp_arity[gi], len = g.grp_len[gi], base = g.grp_first[gi] + lane;
-      const int seg = g.grp_seg[gi * 32 + lane];
-      const float* kp = g.kapf[a] + base;
-      const uint32_t* op = g.o12[a] + base;
-      C<float> acc = {0.f, 0.f};
-      for (int e = 0; e < len; ++e) {
-        const uint32_t o = __ldg(op + e * 32);
-        C<float> p = Fs[o & 0xffffu];
-        if (a >= 2) p = cmul(p, Fs[o >> 16]);
-        if (a == 3) p = cmul(p, Fs[__ldg(g.o3 + base + e * 32)]);
-        const float k = __ldg(kp + e * 32);
-        acc.x += k * p.x;
-        acc.y += k * p.y;
+    const int atom = lane < na ? s_atom[lane] : -1;
+    double rloc = 0.0;
+    for (int q = w0; q < w1; ++q) {
+      const int s = __ldg(m.r_warp_slots + q);
+      float vx = 0.f, vy = 0.f;
+      rest_run<1>(rec, __ldg(m.r_run + 3 * s), __ldg(m.r_run + 3 * s + 1), Fs, lane, vx, vy);
+      rest_run<2>(rec, __ldg(m.r_run + 3 * s + 1), __ldg(m.r_run + 3 * s + 2), Fs, lane, vx, vy);
+      rest_run<3>(rec, __ldg(m.r_run + 3 * s + 2), __ldg(m.r_run + 3 * s + 3), Fs, lane, vx, vy);
+      const int g0 = __ldg(m.r_g0 + s);
+      if (g0 >= 0) {
+        const C<float> f = Fs[g0 * kRestStride + lane];
+        rloc += f2d(f.x * vx) - f2d(f.y * vy);
       }
-      if (seg >= 0) part[seg] = acc;
+      const int w = __ldg(g.slot_weight + s);
+      if (w >= 0 && atom >= 0) {
+        const float mu = __ldg(g.slot_multf + s);
+        W[static_cast<size_t>(atom) * nW + w] = {vx * mu, vy * mu};
+      }
     }
+    rpart[warp * 32 + lane] = rloc;
     __syncthreads();
-    // slot totals (compensated, in segment order): unscaled weights, and the
-    // A0 slots' density terms
-    CSum<float> rs;
-    C<float>* Wa = W + static_cast<size_t>(atom) * m.nW;
-    for (int s = threadIdx.x; s < g.nslot; s += blockDim.x) {
-      const int q0 = g.slot_seg[s], q1 = g.slot_seg[s + 1];
-      CSum<float> tx, ty;
-      for (int q = q0; q < q1; ++q) {
-        tx.add(part[q].x);
-        ty.add(part[q].y);
-      }
-      const float vx = tx.hi + tx.lo, vy = ty.hi + ty.lo;
-      if (s < g.nG0) {
-        const C<float> f = Fs[g.slot_factor[s]];
-        rs.add(f.x * vx);
-        rs.add(-f.y * vy);
-      }
-      const int w = g.slot_weight[s];
-      if (w >= 0) {
-        const float mu = static_cast<float>(g.slot_mult[s]);
-        Wa[w] = {vx * mu, vy * mu};
-      }
-    }
-    double rloc = f2d(rs.hi) + f2d(rs.lo);
-    if (warp * 32 < g.nG0) {  // only these warps hold density terms
-      for (int o = 16; o > 0; o >>= 1) rloc += __shfl_xor_sync(0xffffffffu, rloc, o);
-    }
-    if (lane == 0) s_red[warp] = rloc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    if (warp == 0 && lane < na) {
       double r = 0.0;
-      for (int w = 0; w * 32 < g.nG0 && w < nwarp; ++w) r += s_red[w];
+      for (int w = 0; w < kRestWarps; ++w) r += rpart[w * 32 + lane];
       rho_rest[atom] = r;
     }
-    __syncthreads();
   }
 }
 
@@ -449,23 +453,18 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
     const int na = min(32, natom - a0);
     if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
     __syncthreads();
-    // stage: consecutive threads read consecutive elements of one atom
-    for (int t0 = 0; t0 < 32 * nc; t0 += kBatch * blockDim.x) {
-      C<float> v[kBatch];
+    // stage: thread c takes element c of every atom, kBatch atoms in flight
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+      const int fc = s_fac[c];
+      for (int ab = 0; ab < 32; ab += kBatch) {
+        C<float> v[kBatch];
 #pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int t = t0 + b * blockDim.x + threadIdx.x;
-        const int a = t / nc, c = t - a * nc;
-        v[b] = {0.f, 0.f};
-        if (t < 32 * nc && a < na) v[b] = F[static_cast<size_t>(s_atom[a]) * m.nF + s_fac[c]];
-      }
+        for (int b = 0; b < kBatch; ++b)
+          v[b] = ab + b < na ? F[static_cast<size_t>(s_atom[ab + b]) * m.nF + fc] : C<float>{0.f, 0.f};
 #pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int t = t0 + b * blockDim.x + threadIdx.x;
-        const int a = t / nc, c = t - a * nc;
-        if (t < 32 * nc) {
-          Xs[c * kB3Stride + a] = v[b];
-          Gs[c * kB3Stride + a] = {0.f, 0.f};
+        for (int b = 0; b < kBatch; ++b) {
+          Xs[c * kB3Stride + ab + b] = v[b];
+          Gs[c * kB3Stride + ab + b] = {0.f, 0.f};
         }
       }
     }
@@ -509,29 +508,27 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
       s_dE[lane] = d2f(fcut * dFd);
     }
     __syncthreads();
-    // final weights, consecutive threads on consecutive weights of one atom
-    const int nwt = na * nW;
-    for (int t0 = 0; t0 < nwt; t0 += kBatch * blockDim.x) {
-      C<float> v[kBatch];
+    // final weights: thread w takes weight w of every atom, kBatch atoms in flight
+    for (int w = threadIdx.x; w < nW; w += blockDim.x) {
+      const int c = s_cw[w];
+      const float mu = c >= 0 ? s_mult[c] : 0.f;
+      for (int ab = 0; ab < na; ab += kBatch) {
+        C<float> v[kBatch];
 #pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int t = t0 + b * blockDim.x + threadIdx.x;
-        const int a = t / nW, w = t - a * nW;
-        if (t < nwt) v[b] = W[static_cast<size_t>(s_atom[a]) * nW + w];
-      }
+        for (int b = 0; b < kBatch; ++b)
+          if (ab + b < na) v[b] = W[static_cast<size_t>(s_atom[ab + b]) * nW + w];
 #pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int t = t0 + b * blockDim.x + threadIdx.x;
-        if (t < nwt) {
-          const int a = t / nW, w = t - a * nW;
-          const int c = s_cw[w];
-          if (c >= 0) {
-            const C<float> gv = Gs[c * kB3Stride + a];
-            v[b].x += s_mult[c] * gv.x;
-            v[b].y += s_mult[c] * gv.y;
+        for (int b = 0; b < kBatch; ++b) {
+          const int a = ab + b;
+          if (a < na) {
+            if (c >= 0) {
+              const C<float> gv = Gs[c * kB3Stride + a];
+              v[b].x += mu * gv.x;
+              v[b].y += mu * gv.y;
+            }
+            const float sc = s_dE[a];
+            W[static_cast<size_t>(s_atom[a]) * nW + w] = {v[b].x * sc, v[b].y * sc};
           }
-          const float sc = s_dE[a];
-          W[static_cast<size_t>(s_atom[a]) * nW + w] = {v[b].x * sc, v[b].y * sc};
         }
       }
     }
@@ -578,7 +575,7 @@ __global__ void __launch_bounds__(64)
     }
     for (int s = t; s < D::NQ; s += T) W0s[s] = Wa[m.offW0 + s];
     __syncthreads();
-    const double edf = edf_in[atom];
+    const R edf = to_r<R>(edf_in[atom]);
     const int b0 = off[atom], b1 = off[atom + 1];
     for (int j = b0 + t; j < b1; j += T) {
       const R r = to_r<R>(rr[j]);
@@ -592,10 +589,10 @@ __global__ void __launch_bounds__(64)
         R wl = R(0);
         const int nla = atomic_bin_r<R>(m, r, wl, err);
         if (nla > 0) {
-          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, R(m.rscale_a), g, gd);
-          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, R(m.rscale_a), tv, td);
+          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, rscale_a<R>(m), g, gd);
+          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, rscale_a<R>(m), tv, td);
           R cd1[1];
-          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, R(m.rscale_a), cv, cd1);
+          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, rscale_a<R>(m), cv, cd1);
           cdv = cd1[0];
         } else {
 #pragma unroll
@@ -616,7 +613,7 @@ __global__ void __launch_bounds__(64)
         R wm = R(0);
         const int nlm = magnetic_bin_r<R>(m, mg, wm, err);
         if (nlm > 0) {
-          lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, R(m.rscale_m), mv, Md);
+          lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, rscale_m<R>(m), mv, Md);
         } else {
 #pragma unroll
           for (int q = 0; q < D::NMF; ++q) {
@@ -653,7 +650,7 @@ __global__ void __launch_bounds__(64)
         for (int h = 0; h < D::H2; ++h) cYm[h * T + t] = Ym[h];
       }
       // ---- force
-      R fr = R(edf) * cdv, ft[3] = {R(0), R(0), R(0)};
+      R fr = edf * cdv, ft[3] = {R(0), R(0), R(0)};
       {
         R sp[D::NB];
         C<R> U[D::NRY];
@@ -738,15 +735,16 @@ __global__ void __launch_bounds__(64)
       tij[3 * static_cast<size_t>(j) + 2] = to_d(tr * mz + tt[2]);
     }
     if (t == 0) {
-      // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749)
-      const double mg = magi[atom];
-      const double mx = mhi[3 * atom], my = mhi[3 * atom + 1], mz = mhi[3 * atom + 2];
-      double wm = 0.0;
-      const int nl = magnetic_bin(m, mg, wm, err);
+      // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749), in the
+      // working precision
+      const R mg = to_r<R>(magi[atom]);
+      const R mx = to_r<R>(mhi[3 * atom]), my = to_r<R>(mhi[3 * atom + 1]), mz = to_r<R>(mhi[3 * atom + 2]);
+      R wm = R(0);
+      const int nl = magnetic_bin_r<R>(m, mg, wm, err);
       R Mv[D::NMF], Md[D::NMF], gm[D::NBM], gmd[D::NBM];
       if (nl > 0) {
-        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, R(wm), R(m.rscale_m), Mv, Md);
-        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, R(wm), R(m.rscale_m), gm, gmd);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, wm, rscale_m<R>(m), Mv, Md);
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, wm, rscale_m<R>(m), gm, gmd);
       } else {
         for (int q = 0; q < D::NMF; ++q) {
           Mv[q] = R(nl == 0 ? 1 : 0);
@@ -755,21 +753,21 @@ __global__ void __launch_bounds__(64)
         for (int q = 0; q < D::NBM; ++q) gmd[q] = R(0);
       }
       C<R> Yh[D::H2], dYh[D::H2][3];
-      ylm_half<R, true>(D::L2, R(mx), R(my), R(mz), Yh, dYh);
-      double tr = 0.0, tt[3] = {0.0, 0.0, 0.0};
-      const double dE = dedrho[static_cast<size_t>(atom) * 2];
-      for (int n = 0; n < D::NBM; ++n) tr += dE * m.c1[n] * static_cast<double>(gmd[n]);
-      const double invm = 1.0 / mg;
+      ylm_half<R, true>(D::L2, mx, my, mz, Yh, dYh);
+      R tr = R(0), tt[3] = {R(0), R(0), R(0)};
+      const R dE = to_r<R>(dedrho[static_cast<size_t>(atom) * 2]);
+      for (int n = 0; n < D::NBM; ++n) tr += dE * c1_of<R>(m, n) * gmd[n];
+      const R invm = rcp(mg);
       for (int k = 0; k < D::NQ; ++k) {
         const int nr = k / D::H2, h = k % D::H2, q = nr * (D::L2 + 1) + l_of_h(h);
         const C<R> w = W0s[k];
-        tr += static_cast<double>(Md[q] * re_mul(w, Yh[h]));
-        const R sc = R(invm) * Mv[q];
-        for (int c = 0; c < 3; ++c) tt[c] += static_cast<double>(sc * re_mul(w, dYh[h][c]));
+        tr += Md[q] * re_mul(w, Yh[h]);
+        const R sc = invm * Mv[q];
+        for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(w, dYh[h][c]);
       }
-      ti0[3 * static_cast<size_t>(atom) + 0] = tr * mx + tt[0];
-      ti0[3 * static_cast<size_t>(atom) + 1] = tr * my + tt[1];
-      ti0[3 * static_cast<size_t>(atom) + 2] = tr * mz + tt[2];
+      ti0[3 * static_cast<size_t>(atom) + 0] = to_d(tr * mx + tt[0]);
+      ti0[3 * static_cast<size_t>(atom) + 1] = to_d(tr * my + tt[1]);
+      ti0[3 * static_cast<size_t>(atom) + 2] = to_d(tr * mz + tt[2]);
     }
     __syncthreads();
   }
@@ -777,10 +775,10 @@ __global__ void __launch_bounds__(64)
 
 template <class R, class D>
 size_t abasis_fe_smem() {
-  return sizeof(C<R>) * 64 * (D::NRY + D::NQ) + sizeof(R) * 64 * D::NB + sizeof(double) * 64 + 64;
+  return sizeof(C<R>) * 64 * (D::NRY + D::NQ) + sizeof(R) * 64 * (D::NB + 1) + 64;
 }
 inline size_t density_fe_smem(const DeviceModel& m) {
-  return sizeof(C<float>) * (static_cast<size_t>((m.nF + 1) & ~1) + ((m.g2.nseg + 1) & ~1)) + 64;
+  return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * kRestWarps * 32;
 }
 template <class D>
 size_t b3_fe_smem(const DeviceModel& m) {

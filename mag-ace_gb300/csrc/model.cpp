@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstring>
 #include <map>
 
 #include "magace.h"
@@ -448,7 +449,62 @@ void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
   }
 }
 
-int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg) {
+// The same terms per output slot for kernels with one atom per lane: every
+// slot's entries contiguous (arity 1, then 2, then 3), factors renumbered
+// into the compact set the terms use, and the slots dealt to the kernel's
+// warps longest first onto the least loaded warp.
+void build_rest(const Model& M, const TermSink& sink, RestTable& T) {
+  const FactorLayout& L = M.L;
+  T = RestTable();
+  std::vector<int32_t> compact(L.nF, -1);
+  const auto use = [&](int f) {
+    if (compact[f] < 0) {
+      compact[f] = static_cast<int32_t>(T.factor_of.size());
+      T.factor_of.push_back(f);
+    }
+    return static_cast<uint32_t>(compact[f]);
+  };
+  T.nslot = sink.nslot;
+  T.run.assign(3 * T.nslot + 1, 0);
+  T.slot_g0.assign(T.nslot, -1);
+  std::vector<double> cost(T.nslot, 0.0);
+  for (int s = 0; s < T.nslot; ++s) {
+    if (s < L.n2m * L.ls2) T.slot_g0[s] = static_cast<int32_t>(use(L.offA0 + s));
+    for (int a = 1; a <= 3; ++a) {
+      T.run[3 * s + a - 1] = static_cast<int32_t>(T.rec.size() / 4);
+      for (const Entry& e : sink.by_slot[a][s]) {
+        const float k = static_cast<float>(e.kappa[0]);
+        uint32_t kb;
+        std::memcpy(&kb, &k, sizeof(kb));
+        const uint32_t o1 = use(e.o[0]), o2 = a >= 2 ? use(e.o[1]) : 0, o3 = a >= 3 ? use(e.o[2]) : 0;
+        T.rec.insert(T.rec.end(), {kb, o1 | (o2 << 16), o3, 0u});
+        cost[s] += 2.0 * a;
+      }
+    }
+    cost[s] += 8.0;  // per-slot work: totals, density term, weight store
+  }
+  T.run[3 * T.nslot] = static_cast<int32_t>(T.rec.size() / 4);
+  T.nfac = static_cast<int>(T.factor_of.size());
+  // longest first onto the least loaded warp
+  T.nwarp = kRestTableWarps;
+  std::vector<int> order(T.nslot);
+  for (int s = 0; s < T.nslot; ++s) order[s] = s;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  std::vector<double> load(T.nwarp, 0.0);
+  std::vector<std::vector<int32_t>> per(T.nwarp);
+  for (int s : order) {
+    const int w = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+    load[w] += cost[s];
+    per[w].push_back(s);
+  }
+  T.warp_begin.assign(T.nwarp + 1, 0);
+  for (int w = 0; w < T.nwarp; ++w) {
+    T.warp_begin[w + 1] = T.warp_begin[w] + static_cast<int32_t>(per[w].size());
+    T.warp_slots.insert(T.warp_slots.end(), per[w].begin(), per[w].end());
+  }
+}
+
+int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestTable* rest = nullptr) {
   const FactorLayout& L = M.L;
   const BasisDims& d = M.pot.dims;
   const int nd = M.ndensity;
@@ -472,6 +528,7 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg) {
   });
   if (with_b3)
     for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
+  if (rest) build_rest(M, sink, *rest);
 
   // flatten into segments, then pack segments into warp groups
   g = GatherTable();
@@ -731,7 +788,7 @@ int build_tables(Model& M, std::string& msg) {
   // tables of the specialised kernels: 3-body terms as dense per-(combo, m)
   // contractions, everything else through the gather table without them
   if (M.ndensity == 1) {
-    st = build_gather(M, false, M.gt_nob3, msg);
+    st = build_gather(M, false, M.gt_nob3, msg, &M.rest);
     if (st) return st;
     build_dense_b3(M);
     // multiplicity of each compact element's weight, from the gather table's

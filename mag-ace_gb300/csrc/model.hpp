@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "device_model.hpp"
 #include "potential.hpp"
 
 namespace magace {
@@ -115,6 +116,25 @@ struct DescriptorTable {
   std::vector<uint16_t> o;       // [terms][4] factor indices
 };
 
+// The 2- and 4-body terms per output slot, for the split-precision kernel
+// that holds 32 atoms in the lanes of a warp. Slot s (numbered as in
+// GatherTable) adds kappa * prod F[factor_of[o_q]] over its entries
+// [run[3s], run[3s+3]): arity 1 up to run[3s+1], arity 2 up to run[3s+2],
+// arity 3 up to run[3s+3] (= run[3(s+1)]). An entry is one 16-byte record
+// {kappa bits, o1 | o2 << 16, o3, 0}. Factors are renumbered into the `nfac`
+// the terms use; slot_g0 is the compact A0 factor of a density slot. The
+// slots are dealt to `nwarp` warps longest first: warp w takes
+// warp_slots[warp_begin[w] .. warp_begin[w+1]).
+struct RestTable {
+  int nfac = 0, nslot = 0, nwarp = 0;
+  std::vector<int32_t> factor_of;  // [nfac] factor index
+  std::vector<int32_t> run;        // [3 * nslot + 1]
+  std::vector<uint32_t> rec;       // [entries][4]
+  std::vector<int32_t> slot_g0;    // [nslot] compact A0 factor, or -1
+  std::vector<int32_t> warp_begin; // [nwarp + 1]
+  std::vector<int32_t> warp_slots; // [nslot]
+};
+
 struct RadialLUT {
   int nlut = 0;
   int nfa = 0;  // atomic: g_n (nba), R_nl (n3a*(l3a+1), index nr*(l3a+1)+l), core (1)
@@ -140,6 +160,7 @@ struct Model {
   GatherTable gt;        // every term (generic kernels)
   GatherTable gt_nob3;   // every term except the 3-body ones (specialised kernels)
   DenseB3 db3;           // 3-body terms in dense form (specialised kernels)
+  RestTable rest;        // the other terms per slot (specialised split kernels)
   DescriptorTable desc;  // per-cluster terms without coefficients (descriptors)
   RadialLUT lut;
   bool ready = false;

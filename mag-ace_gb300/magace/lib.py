@@ -213,12 +213,12 @@ def kernel_times() -> list:
 
 
 def table_stats() -> dict:
-    out = (ctypes.c_longlong * 30)()
+    out = (ctypes.c_longlong * 31)()
     _check(load().ace_table_stats(out))
     keys = ["ne1", "ne2", "ne3", "nseg", "nslot", "nF", "nW", "nWA", "nA2h", "nfa", "nfm",
             "nba", "nbm", "n2m", "l2m", "n3a", "n3m", "l3a", "l3m", "h2", "h3",
             "b3_tasks", "b3_combos", "b3_elements", "rest_segments", "rest_entries",
-            "rest_ne1", "rest_ne2", "rest_ne3", "b3_pairs"]
+            "rest_ne1", "rest_ne2", "rest_ne3", "b3_pairs", "rest_factors"]
     return {k: int(v) for k, v in zip(keys, out)}
 
 
