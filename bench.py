@@ -264,7 +264,14 @@ def gpu_arm(args, rank, world, local_rank):
 
     paths = {}
     want = ["fp64", "split"] if args.precision == "auto" else [args.precision]
+    tuned = None
     for name in want:
+        if name == "split":
+            # the library's autotuner picks the density kernels' CTA shapes on this workload
+            lib.set_precision(1)
+            tuned = lib.autotune_device(nb.natom, nb.nei, d_off.data_ptr(), d_r.data_ptr(), d_e.data_ptr(),
+                                        d_mj.data_ptr(), d_mhj.data_ptr(), d_mi.data_ptr(), d_mhi.data_ptr(),
+                                        work_stream.cuda_stream)
         paths[name] = run_path(0 if name == "fp64" else 1)
 
     # accuracy of the split path against the FP64 path (which equals the oracle to 1e-10)
@@ -322,6 +329,7 @@ def gpu_arm(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "f64" if headline == "fp64" else "f32/f64-split",
         "data": "synthetic (seeded potential and structure)",
         "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": headline,
+                   "tuned_warps": {"density": tuned[0], "b3": tuned[1]} if tuned else None,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": whole_job_rate(total_atoms, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "host_access": lib.host_access(),

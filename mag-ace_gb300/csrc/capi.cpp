@@ -70,6 +70,7 @@ struct Runtime {
   int last_launches = 0;
   int last_natom = -1;  // atoms of the last evaluation (ace_density_gradient_device)
   bool work_queue = false;  // neighbour-count-sorted work queue
+  int tune_rest = 0, tune_b3 = 0;  // density kernel variants (ace_autotune_device)
   DevBuf<int> order, queue_bins;
 
   // device tables
@@ -308,6 +309,8 @@ int upload_tables() {
   d.b3_factor = R.b3_factor.p;
   d.b3_cw = R.b3_cw.p;
   d.b3_mult = R.b3_mult.p;
+  d.tune_rest = R.tune_rest;
+  d.tune_b3 = R.tune_b3;
   d.r_nfac = M.rest.nfac;
   d.r_nslot = M.rest.nslot;
   d.r_factor = R.r_factor.p;
@@ -655,6 +658,74 @@ int ace_compute_device(int natom, int nei, const int* bond_offset, const double*
 int ace_set_work_queue(int on) {
   rt().work_queue = on != 0;
   return set_error(MAGACE_OK, "");
+}
+
+int ace_autotune_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
+                        const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
+                        void* stream, int* rest_warps, int* b3_warps) {
+  Runtime& R = rt();
+  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
+  int st = upload_tables();
+  if (st) return st;
+  st = reserve_work(natom, nei, R.precision);
+  if (st) return st;
+  CUDA_TRY(R.energy.reserve(natom));
+  CUDA_TRY(R.ti0.reserve(3 * static_cast<size_t>(natom)));
+  CUDA_TRY(R.fij.reserve(3 * static_cast<size_t>(nei)));
+  CUDA_TRY(R.tij.reserve(3 * static_cast<size_t>(nei)));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : R.stream;
+  EvalBuffers b;
+  b.natom = natom;
+  b.nei = nei;
+  b.off = bond_offset;
+  b.r = r;
+  b.e = e;
+  b.magj = mag_j;
+  b.mhj = mhat_j;
+  b.magi = mag_i;
+  b.mhi = mhat_i;
+  b.energy = R.energy.p;
+  b.fij = R.fij.p;
+  b.tij = R.tij.p;
+  b.ti0 = R.ti0.p;
+  // every variant once to warm up, then timed; the fastest is kept
+  const bool timing = R.timing;
+  R.timing = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_r = R.tune_rest, best_b = R.tune_b3;
+  const int nr = static_cast<int>(sizeof(kRestWarpChoices) / sizeof(int));
+  const int nbw = static_cast<int>(sizeof(kB3WarpChoices) / sizeof(int));
+  for (int ir = 0; ir < nr; ++ir)
+    for (int ib = 0; ib < nbw; ++ib) {
+      R.dm.tune_rest = ir;
+      R.dm.tune_b3 = ib;
+      st = run_eval(b, s);
+      if (st) break;
+      CUDA_TRY(cudaEventRecord(e0, s));
+      st = run_eval(b, s);
+      if (st) break;
+      CUDA_TRY(cudaEventRecord(e1, s));
+      CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        best_r = ir;
+        best_b = ib;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  R.timing = timing;
+  R.tune_rest = R.dm.tune_rest = best_r;
+  R.tune_b3 = R.dm.tune_b3 = best_b;
+  if (st) return st;
+  if (rest_warps) *rest_warps = kRestWarpChoices[best_r];
+  if (b3_warps) *b3_warps = kB3WarpChoices[best_b];
+  return ace_device_status();
 }
 
 int ace_num_coefficients(int* ncoef, int* ndensity) {

@@ -996,17 +996,33 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
   if constexpr (sizeof(R) == 4) {
     if (fe) {
       double* rho_rest = static_cast<double*>(b.aux);
-      const size_t s2 = density_fe_smem(m);
-      set_smem(k_density_fe<FeDims>, s2);
       const int nblk = (natom + 31) / 32;
-      k_density_fe<FeDims><<<nblk < grid_cap ? nblk : grid_cap, kRestWarps * 32, s2, st>>>(
-          m, natom, reinterpret_cast<const C<float>*>(b.F), reinterpret_cast<C<float>*>(b.W), rho_rest);
+      const int gb = nblk < grid_cap ? nblk : grid_cap;
+      const auto* Fp = reinterpret_cast<const C<float>*>(b.F);
+      auto* Wp = reinterpret_cast<C<float>*>(b.W);
+      const int rw = kRestWarpChoices[m.tune_rest], bw = kB3WarpChoices[m.tune_b3];
+      const size_t s2 = density_fe_smem(m, rw);
+      if (rw == 16) {
+        set_smem(k_density_fe<FeDims, 16>, s2);
+        k_density_fe<FeDims, 16><<<gb, 16 * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest);
+      } else {
+        set_smem(k_density_fe<FeDims, 32>, s2);
+        k_density_fe<FeDims, 32><<<gb, 32 * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest);
+      }
       if (ev_between) cudaEventRecord(ev_between, st);
-      const size_t sb = b3_fe_smem<FeDims>(m);
-      set_smem(k_b3_fe<FeDims>, sb);
-      k_b3_fe<FeDims><<<nblk < grid_cap ? nblk : grid_cap, kB3Warps * 32, sb, st>>>(
-          m, natom, reinterpret_cast<const C<float>*>(b.F), reinterpret_cast<C<float>*>(b.W), b.rho1, rho_rest,
-          b.core, b.energy, b.edf, b.dedrho, b.err);
+      const size_t sb = b3_fe_smem<FeDims>(m, bw);
+#define MAGACE_B3(NW)                                                                                        \
+  set_smem(k_b3_fe<FeDims, NW>, sb);                                                                         \
+  k_b3_fe<FeDims, NW><<<gb, NW * 32, sb, st>>>(m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy, b.edf, \
+                                               b.dedrho, b.err)
+      if (bw == 8) {
+        MAGACE_B3(8);
+      } else if (bw == 12) {
+        MAGACE_B3(12);
+      } else {
+        MAGACE_B3(16);
+      }
+#undef MAGACE_B3
       return 2;
     }
   }
@@ -1069,7 +1085,7 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
     }
     if (which == 0) return abasis_fe_smem<float, FeDims>();
     if (which == 1) {
-      const size_t a = density_fe_smem(m), b = b3_fe_smem<FeDims>(m);
+      const size_t a = density_fe_smem(m, 32), b = b3_fe_smem<FeDims>(m, 16);
       return a > b ? a : b;
     }
     return forces_fe_smem<float, FeDims>();

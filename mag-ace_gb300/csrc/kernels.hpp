@@ -15,6 +15,10 @@ constexpr int kDensityThreads = 256;
 constexpr int kForceThreads = 64;
 constexpr int kMaxFeat = 32;     // per-bond radial functions of one kind
 constexpr int kMaxLaunches = 4;  // kernels of one evaluation
+// warps per CTA of the split-precision density kernels, chosen by
+// DeviceModel::tune_rest / tune_b3 (ace_autotune_device picks them)
+constexpr int kRestWarpChoices[2] = {32, 16};
+constexpr int kB3WarpChoices[3] = {16, 12, 8};
 
 // Device arrays of one evaluation. F and W are complex arrays of the selected
 // precision (FP64: 16 bytes per entry, FP32: 8 bytes).

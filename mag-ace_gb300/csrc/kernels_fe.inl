@@ -243,12 +243,12 @@ constexpr int kBatch = 8;
 // Fs[factor][atom]. Slot totals are FP32 sums in entry order; the density
 // terms of the A0 slots add up per lane in FP64, and the per-warp partials
 // in warp order.
-constexpr int kRestWarps = kRestTableWarps;
 constexpr int kRestStride = 33;  // row stride of Fs in complex elements
 
 template <int A>
 __device__ __forceinline__ void rest_run(const uint4* __restrict__ rec, int e0, int e1, const C<float>* Fs, int lane,
                                          float& vx, float& vy) {
+#pragma unroll 4
   for (int e = e0; e < e1; ++e) {
     const uint4 r = __ldg(rec + e);
     const float k = __uint_as_float(r.x);
@@ -260,20 +260,22 @@ __device__ __forceinline__ void rest_run(const uint4* __restrict__ rec, int e0, 
   }
 }
 
-template <class D>
-__global__ void __launch_bounds__(kRestWarps * 32, 1)
+// NW warps per CTA (a divisor of kRestTableWarps): warp w walks the slots
+// the host schedule gave to warps w, w + NW, ...
+template <class D, int NW>
+__global__ void __launch_bounds__(NW * 32, 1)
     k_density_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
                  double* __restrict__ rho_rest) {
+  static_assert(kRestTableWarps % NW == 0, "the slot schedule is dealt to kRestTableWarps warps");
   extern __shared__ __align__(16) unsigned char smem[];
   const int nf = m.r_nfac, nW = m.nW;
   const GatherView& g = m.g2;  // slot weights and multiplicities (same slot numbering)
   C<float>* Fs = reinterpret_cast<C<float>*>(smem);                   // [nf][33]
-  double* rpart = reinterpret_cast<double*>(Fs + nf * kRestStride);   // [kRestWarps][32]
+  double* rpart = reinterpret_cast<double*>(Fs + nf * kRestStride);   // [NW][32]
   __shared__ int s_atom[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (natom + 31) / 32;
   const uint4* rec = reinterpret_cast<const uint4*>(m.r_rec);
-  const int w0 = __ldg(m.r_warp_begin + warp), w1 = __ldg(m.r_warp_begin + warp + 1);
 
   for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
     const int a0 = blk * 32;
@@ -296,7 +298,8 @@ __global__ void __launch_bounds__(kRestWarps * 32, 1)
     __syncthreads();
     const int atom = lane < na ? s_atom[lane] : -1;
     double rloc = 0.0;
-    for (int q = w0; q < w1; ++q) {
+    for (int sw = warp; sw < kRestTableWarps; sw += NW)
+    for (int q = __ldg(m.r_warp_begin + sw); q < __ldg(m.r_warp_begin + sw + 1); ++q) {
       const int s = __ldg(m.r_warp_slots + q);
       float vx = 0.f, vy = 0.f;
       rest_run<1>(rec, __ldg(m.r_run + 3 * s), __ldg(m.r_run + 3 * s + 1), Fs, lane, vx, vy);
@@ -317,13 +320,12 @@ __global__ void __launch_bounds__(kRestWarps * 32, 1)
     __syncthreads();
     if (warp == 0 && lane < na) {
       double r = 0.0;
-      for (int w = 0; w < kRestWarps; ++w) r += rpart[w * 32 + lane];
+      for (int w = 0; w < NW; ++w) r += rpart[w * 32 + lane];
       rho_rest[atom] = r;
     }
   }
 }
 
-constexpr int kB3Warps = 16;
 constexpr int kB3Stride = 33;  // row stride of Xs/Gs in complex elements
 
 // pairs (i, j) the enumeration keeps for pattern PAT (0: l1' == l2' keeps
@@ -419,8 +421,8 @@ __device__ __forceinline__ float b3_task(const float* __restrict__ Cs, const C<f
 // the per-warp density partials, the atoms' dE/drho, and the element and
 // weight maps.
 
-template <class D>
-__global__ void __launch_bounds__(kB3Warps * 32, 1)
+template <class D, int NW>
+__global__ void __launch_bounds__(NW * 32, 1)
     k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
             const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
             double* __restrict__ energy, double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err) {
@@ -431,8 +433,8 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
   float* Cs = reinterpret_cast<float*>(smem);
   C<float>* Xs = reinterpret_cast<C<float>*>(Cs + ((ncoef + 3) & ~3));
   C<float>* Gs = Xs + nc * kB3Stride;
-  double* rpart = reinterpret_cast<double*>(Gs + nc * kB3Stride);  // [kB3Warps][32]
-  float* s_dE = reinterpret_cast<float*>(rpart + kB3Warps * 32);  // [32]
+  double* rpart = reinterpret_cast<double*>(Gs + nc * kB3Stride);  // [NW][32]
+  float* s_dE = reinterpret_cast<float*>(rpart + NW * 32);        // [32]
   float* s_mult = s_dE + 32;                                       // [nc]
   int* s_fac = reinterpret_cast<int*>(s_mult + nc);                // [nc]
   int* s_cw = s_fac + nc;                                          // [nW]
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
     __syncthreads();
     double rloc = 0.0;
 #pragma unroll 1
-    for (int tk = warp; tk < m.b3_ntask; tk += kB3Warps) {
+    for (int tk = warp; tk < m.b3_ntask; tk += NW) {
       const int k = __ldg(m.b3_combo + tk);
       const int pat = __ldg(m.b3_pattern + k);
       const float cf = __ldg(m.b3_cff + tk);
@@ -489,7 +491,7 @@ __global__ void __launch_bounds__(kB3Warps * 32, 1)
     if (warp == 0 && lane < na) {
       const int atom = s_atom[lane];
       double rho = rho1[static_cast<size_t>(atom) * 2] + rho_rest[atom];
-      for (int w = 0; w < kB3Warps; ++w) rho += rpart[w * 32 + lane];
+      for (int w = 0; w < NW; ++w) rho += rpart[w * 32 + lane];
       if (!isfinite(rho)) raise_error(err, kDevNaN);
       double Fd, dFd;
       embed(m.nfemb, rho, m.par[0][0], m.par[1][0], Fd, dFd);
@@ -777,14 +779,14 @@ template <class R, class D>
 size_t abasis_fe_smem() {
   return sizeof(C<R>) * 64 * (D::NRY + D::NQ) + sizeof(R) * 64 * (D::NB + 1) + 64;
 }
-inline size_t density_fe_smem(const DeviceModel& m) {
-  return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * kRestWarps * 32;
+inline size_t density_fe_smem(const DeviceModel& m, int nw) {
+  return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * nw * 32;
 }
 template <class D>
-size_t b3_fe_smem(const DeviceModel& m) {
+size_t b3_fe_smem(const DeviceModel& m, int nw) {
   const size_t ncoef = static_cast<size_t>(m.b3_ncombo) * D::NM * D::I * D::I;
   return sizeof(float) * ((ncoef + 3) & ~static_cast<size_t>(3)) +
-         sizeof(C<float>) * 2 * static_cast<size_t>(m.b3_nc) * kB3Stride + sizeof(double) * kB3Warps * 32 +
+         sizeof(C<float>) * 2 * static_cast<size_t>(m.b3_nc) * kB3Stride + sizeof(double) * nw * 32 +
          sizeof(float) * 32 + sizeof(float) * m.b3_nc + sizeof(int) * (m.b3_nc + m.nW);
 }
 template <class R, class D>

@@ -237,3 +237,26 @@ def test_host_access_modes_agree(gpu_lib, monkeypatch, mode):
     got = gpu_lib.acelib(nb)
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
+
+
+def test_autotuner_keeps_results(gpu_lib, oracle_seeded):
+    """The autotuner times every density-kernel variant and keeps one; the
+    split results stay within the split tolerance of the oracle."""
+    import torch
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_128(3), 5.0)
+    gpu_lib.set_precision(1)
+    try:
+        dev = torch.device("cuda", 0)
+        off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+        T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+        arrs = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
+        torch.cuda.synchronize()
+        rw, bw = gpu_lib.autotune_device(nb.natom, nb.nei, off.data_ptr(), *[a.data_ptr() for a in arrs])
+        assert rw in (16, 32) and bw in (8, 12, 16)
+        e, f, t, t0 = gpu_lib.acelib(nb)
+    finally:
+        gpu_lib.set_precision(0)
+    eo, fo, to, t0o = oracle_seeded.acelib(nb)
+    for got, ref in ((e, eo), (f, fo), (t, to), (t0, t0o)):
+        assert rel_err(got, ref) < 1e-5
