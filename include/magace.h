@@ -175,15 +175,17 @@ int ace_compute_device_noalloc(int natom, int nei, const int* bond_offset, const
 int ace_set_work_queue(int on);
 
 /* Autotuner (no counterpart in the reference): evaluates the given system
- * (same arrays as ace_compute_device) once per variant of the split-precision
- * density kernels (warps per CTA of the 2-/4-body and the 3-body kernel),
- * times each with CUDA events and keeps the fastest for later evaluations.
- * Writes the chosen warp counts. Synchronous. Results do not change beyond
- * the FP32 rounding order of the 3-body kernel. Does nothing but report the
- * current choice for the FP64 path or another basis layout. */
+ * (same arrays as ace_compute_device) with every variant of the
+ * split-precision kernels' CTA shapes (warps per CTA of the 2-/4-body and the
+ * 3-body density kernels; CTAs per SM the force kernel's registers allow),
+ * times each kernel with CUDA events and keeps each kernel's fastest variant
+ * for later evaluations. Writes the choices. Synchronous. Results do not
+ * change beyond the FP32 rounding order of the 3-body kernel. For the FP64
+ * path or another basis layout it only reports the current choice. */
 int ace_autotune_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
                         const double* mag_j, const double* mhat_j, const double* mag_i,
-                        const double* mhat_i, void* stream, int* rest_warps, int* b3_warps);
+                        const double* mhat_i, void* stream, int* rest_warps, int* b3_warps,
+                        int* force_blocks);
 
 /* ---- Differentiation and fitting (no counterpart in the reference's
  * acelib_; they expose what src/forces.F90:976-1289 computes internally). ----

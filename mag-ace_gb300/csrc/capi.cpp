@@ -70,7 +70,7 @@ struct Runtime {
   int last_launches = 0;
   int last_natom = -1;  // atoms of the last evaluation (ace_density_gradient_device)
   bool work_queue = false;  // neighbour-count-sorted work queue
-  int tune_rest = 0, tune_b3 = 0;  // density kernel variants (ace_autotune_device)
+  int tune_rest = 0, tune_b3 = 0, tune_forces = 0;  // kernel variants (ace_autotune_device)
   DevBuf<int> order, queue_bins;
 
   // device tables
@@ -311,6 +311,7 @@ int upload_tables() {
   d.b3_mult = R.b3_mult.p;
   d.tune_rest = R.tune_rest;
   d.tune_b3 = R.tune_b3;
+  d.tune_forces = R.tune_forces;
   d.r_nfac = M.rest.nfac;
   d.r_nslot = M.rest.nslot;
   d.r_factor = R.r_factor.p;
@@ -662,7 +663,7 @@ int ace_set_work_queue(int on) {
 
 int ace_autotune_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
                         const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
-                        void* stream, int* rest_warps, int* b3_warps) {
+                        void* stream, int* rest_warps, int* b3_warps, int* force_blocks) {
   Runtime& R = rt();
   if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
   int st = upload_tables();
@@ -688,43 +689,47 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
   b.fij = R.fij.p;
   b.tij = R.tij.p;
   b.ti0 = R.ti0.p;
-  // every variant once to warm up, then timed; the fastest is kept
+  // variant v of every kernel at once (each kernel's own choice list,
+  // clamped), warmed up, then timed kernel by kernel; each kernel keeps its
+  // fastest variant
   const bool timing = R.timing;
-  R.timing = false;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  CUDA_TRY(cudaEventCreate(&e0));
-  CUDA_TRY(cudaEventCreate(&e1));
-  float best = 1e30f;
-  int best_r = R.tune_rest, best_b = R.tune_b3;
+  R.timing = true;
+  for (auto& ev : R.ev)
+    if (!ev) CUDA_TRY(cudaEventCreate(&ev));
   const int nr = static_cast<int>(sizeof(kRestWarpChoices) / sizeof(int));
   const int nbw = static_cast<int>(sizeof(kB3WarpChoices) / sizeof(int));
-  for (int ir = 0; ir < nr; ++ir)
-    for (int ib = 0; ib < nbw; ++ib) {
-      R.dm.tune_rest = ir;
-      R.dm.tune_b3 = ib;
-      st = run_eval(b, s);
-      if (st) break;
-      CUDA_TRY(cudaEventRecord(e0, s));
-      st = run_eval(b, s);
-      if (st) break;
-      CUDA_TRY(cudaEventRecord(e1, s));
-      CUDA_TRY(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms < best) {
-        best = ms;
-        best_r = ir;
-        best_b = ib;
+  const int nfv = static_cast<int>(sizeof(kForceMinBlocksChoices) / sizeof(int));
+  float best[3] = {1e30f, 1e30f, 1e30f};  // density, b3, forces
+  int pick[3] = {R.tune_rest, R.tune_b3, R.tune_forces};
+  for (int v = 0; v < std::max(nr, std::max(nbw, nfv)); ++v) {
+    R.dm.tune_rest = std::min(v, nr - 1);
+    R.dm.tune_b3 = std::min(v, nbw - 1);
+    R.dm.tune_forces = std::min(v, nfv - 1);
+    st = run_eval(b, s);
+    if (st) break;
+    st = run_eval(b, s);
+    if (st) break;
+    if (R.last_launches != 4) break;  // not the split-precision specialised path: nothing to tune
+    float ms[kMaxLaunches];
+    CUDA_TRY(cudaEventSynchronize(R.ev[R.last_launches]));
+    for (int k = 0; k < R.last_launches; ++k) CUDA_TRY(cudaEventElapsedTime(&ms[k], R.ev[k], R.ev[k + 1]));
+    const float t3[3] = {ms[1], ms[2], ms[3]};
+    const int idx[3] = {R.dm.tune_rest, R.dm.tune_b3, R.dm.tune_forces};
+    for (int q = 0; q < 3; ++q)
+      if (t3[q] < best[q]) {
+        best[q] = t3[q];
+        pick[q] = idx[q];
       }
-    }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  }
   R.timing = timing;
-  R.tune_rest = R.dm.tune_rest = best_r;
-  R.tune_b3 = R.dm.tune_b3 = best_b;
+  R.tune_rest = R.dm.tune_rest = pick[0];
+  R.tune_b3 = R.dm.tune_b3 = pick[1];
+  R.tune_forces = R.dm.tune_forces = pick[2];
+  const int best_r = pick[0], best_b = pick[1];
   if (st) return st;
   if (rest_warps) *rest_warps = kRestWarpChoices[best_r];
   if (b3_warps) *b3_warps = kB3WarpChoices[best_b];
+  if (force_blocks) *force_blocks = kForceMinBlocksChoices[pick[2]];
   return ace_device_status();
 }
 

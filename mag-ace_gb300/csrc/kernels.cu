@@ -1055,10 +1055,25 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
     const size_t s3 = forces_fe_smem<R, FeDims>();
-    set_smem(k_forces_fe<R, FeDims>, s3);
-    k_forces_fe<R, FeDims><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                 reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij,
-                                                 b.ti0, b.err);
+    const int mb = kForceMinBlocksChoices[m.tune_forces];
+#define MAGACE_FORCES(MB)                                                                                          \
+  set_smem(k_forces_fe<R, FeDims, MB>, s3);                                                                        \
+  k_forces_fe<R, FeDims, MB><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,         \
+                                                   reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij, \
+                                                   b.ti0, b.err)
+    if constexpr (sizeof(R) == 8) {
+      (void)mb;
+      MAGACE_FORCES(4);
+    } else {
+      if (mb == 4) {
+        MAGACE_FORCES(4);
+      } else if (mb == 6) {
+        MAGACE_FORCES(6);
+      } else {
+        MAGACE_FORCES(8);
+      }
+    }
+#undef MAGACE_FORCES
   } else {
     const size_t s3 = forces_smem<R>(m, kForceThreads);
     set_smem(k_forces<R>, s3);

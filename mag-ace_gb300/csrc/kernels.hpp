@@ -19,6 +19,9 @@ constexpr int kMaxLaunches = 4;  // kernels of one evaluation
 // DeviceModel::tune_rest / tune_b3 (ace_autotune_device picks them)
 constexpr int kRestWarpChoices[2] = {32, 16};
 constexpr int kB3WarpChoices[3] = {16, 12, 8};
+// CTAs per SM the split-precision force kernel's registers must allow
+// (DeviceModel::tune_forces)
+constexpr int kForceMinBlocksChoices[3] = {4, 6, 8};
 
 // Device arrays of one evaluation. F and W are complex arrays of the selected
 // precision (FP64: 16 bytes per entry, FP32: 8 bytes).

@@ -540,9 +540,10 @@ __global__ void __launch_bounds__(NW * 32, 1)
 
 // ===========================================================================
 // k_forces_fe: one thread per bond. Weights transposed into shared memory:
-// W2T[k][n] and WAT[k3][i], so the inner loops read 16-byte pairs.
-template <class R, class D>
-__global__ void __launch_bounds__(64)
+// W2T[k][n] and WAT[k3][i], so the inner loops read 16-byte pairs. MINB is
+// the CTAs per SM the register allocation must allow (a tuning variant).
+template <class R, class D, int MINB>
+__global__ void __launch_bounds__(64, MINB)
     k_forces_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
                 const double* __restrict__ magi, const double* __restrict__ mhi, const C<R>* __restrict__ W,

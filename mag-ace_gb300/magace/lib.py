@@ -49,7 +49,7 @@ SIGNATURES = {
     "ace_host_access_mode": (_i, []),
     "ace_num_coefficients": (_i, [_pi, _pi]),
     "ace_set_work_queue": (_i, [_i]),
-    "ace_autotune_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _pi, _pi]),
+    "ace_autotune_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _pi, _pi, _pi]),
     "ace_md_create": (_i, [_i, _pd, _pd, _pd, _pd, _pi, _d, _d, _d, _pi]),
     "ace_md_run": (_i, [_i, _i, _d, _i, _i, _pd]),
     "ace_md_state": (_i, [_i, _pd, _pd, _pd, _pd, _pd]),
@@ -158,12 +158,13 @@ def set_work_queue(on: bool) -> None:
 
 
 def autotune_device(natom, nei, off, r, e, magj, mhj, magi, mhi, stream=0) -> tuple:
-    """Times the density-kernel variants on these device arrays and keeps the
-    fastest; returns (warps of the 2-/4-body kernel, warps of the 3-body kernel)."""
-    rw, bw = ctypes.c_int(), ctypes.c_int()
+    """Times the split-precision kernel variants on these device arrays and
+    keeps each kernel's fastest; returns (warps of the 2-/4-body density
+    kernel, warps of the 3-body kernel, CTAs per SM of the force kernel)."""
+    rw, bw, fb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     _check(load().ace_autotune_device(natom, nei, off, r, e, magj, mhj, magi, mhi, stream, ctypes.byref(rw),
-                                      ctypes.byref(bw)))
-    return rw.value, bw.value
+                                      ctypes.byref(bw), ctypes.byref(fb)))
+    return rw.value, bw.value, fb.value
 
 
 def num_coefficients() -> tuple:

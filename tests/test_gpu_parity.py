@@ -252,8 +252,8 @@ def test_autotuner_keeps_results(gpu_lib, oracle_seeded):
         T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
         arrs = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
         torch.cuda.synchronize()
-        rw, bw = gpu_lib.autotune_device(nb.natom, nb.nei, off.data_ptr(), *[a.data_ptr() for a in arrs])
-        assert rw in (16, 32) and bw in (8, 12, 16)
+        rw, bw, fb = gpu_lib.autotune_device(nb.natom, nb.nei, off.data_ptr(), *[a.data_ptr() for a in arrs])
+        assert rw in (16, 32) and bw in (8, 12, 16) and fb in (4, 6, 8)
         e, f, t, t0 = gpu_lib.acelib(nb)
     finally:
         gpu_lib.set_precision(0)
