@@ -1001,6 +1001,7 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const auto* Fp = reinterpret_cast<const C<float>*>(b.F);
       auto* Wp = reinterpret_cast<C<float>*>(b.W);
       const int rw = kRestWarpChoices[m.tune_rest], bw = kB3WarpChoices[m.tune_b3];
+      (void)bw;
       const size_t s2 = density_fe_smem(m, rw);
       if (rw == 16) {
         set_smem(k_density_fe<FeDims, 16>, s2);
@@ -1011,16 +1012,17 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       }
       if (ev_between) cudaEventRecord(ev_between, st);
       const size_t sb = b3_fe_smem<FeDims>(m, bw);
-#define MAGACE_B3(NW)                                                                                        \
-  set_smem(k_b3_fe<FeDims, NW>, sb);                                                                         \
-  k_b3_fe<FeDims, NW><<<gb, NW * 32, sb, st>>>(m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy, b.edf, \
-                                               b.dedrho, b.err)
-      if (bw == 8) {
-        MAGACE_B3(8);
-      } else if (bw == 12) {
-        MAGACE_B3(12);
-      } else {
-        MAGACE_B3(16);
+#define MAGACE_B3(NW, LOOP)                                                                                  \
+  set_smem(k_b3_fe<FeDims, NW, LOOP>, sb);                                                                   \
+  k_b3_fe<FeDims, NW, LOOP><<<gb, NW * 32, sb, st>>>(m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy,   \
+                                                     b.edf, b.dedrho, b.err)
+      // variants: (16 warps, n0' innermost), (12, innermost), (8, innermost),
+      // (12, n0' outermost)
+      switch (m.tune_b3) {
+        case 1: MAGACE_B3(12, 0); break;
+        case 2: MAGACE_B3(8, 0); break;
+        case 3: MAGACE_B3(12, 1); break;
+        default: MAGACE_B3(16, 0); break;
       }
 #undef MAGACE_B3
       return 2;

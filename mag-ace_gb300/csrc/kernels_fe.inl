@@ -416,12 +416,75 @@ __device__ __forceinline__ float b3_task(const float* __restrict__ Cs, const C<f
   return cf * rt;
 }
 
+// The same task with the n0' loop outermost and not unrolled: X, Y, dX and
+// dY stay in registers across it (more registers, a third of the code).
+template <int PAT, class D>
+__device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const C<float>* Xs, C<float>* Gs,
+                                            const uint16_t* __restrict__ code, float cf, int lane) {
+  constexpr int I = D::I, NM = D::NM;
+  constexpr int JUSED = jmax_of<PAT, I, NM>(I - 1);
+  C<float> X[I], Y[I], aZ[I], gY[I];
+#pragma unroll
+  for (int i = 0; i < I; ++i) {
+    X[i] = b3_load(Xs, __ldg(code + NM + i), lane);
+    Y[i] = i < JUSED ? b3_load(Xs, __ldg(code + NM + I + i), lane) : C<float>{0.f, 0.f};
+    aZ[i] = {0.f, 0.f};
+    gY[i] = {0.f, 0.f};
+  }
+#pragma unroll 1
+  for (int p = 0; p < NM; ++p) {
+    const unsigned cp = __ldg(code + p);
+    const C<float> a = b3_load(Xs, cp, lane);
+    C<float> ga = {0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < I; ++i) {
+      const int jm = jmax_of<PAT, I, NM>(i);
+      if (jm == 0) continue;
+      C<float> z = {0.f, 0.f};
+      const C<float> ax = cmul(a, X[i]);
+      const float4* crow = reinterpret_cast<const float4*>(Cs + (p * I + i) * I);
+#pragma unroll
+      for (int j4 = 0; j4 < (jm + 3) / 4; ++j4) {
+        const float4 c4 = crow[j4];
+        const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = 4 * j4 + u;
+          if (j < jm) {
+            z.x += cv[u] * Y[j].x;
+            z.y += cv[u] * Y[j].y;
+            gY[j].x += cv[u] * ax.x;
+            gY[j].y += cv[u] * ax.y;
+          }
+        }
+      }
+      const C<float> t = cmul(a, z);
+      aZ[i].x += t.x;
+      aZ[i].y += t.y;
+      const C<float> u = cmul(X[i], z);
+      ga.x += u.x;
+      ga.y += u.y;
+    }
+    b3_add(Gs, cp, lane, ga, cf);
+  }
+  float rt = 0.f;
+#pragma unroll
+  for (int i = 0; i < I; ++i) {
+    if (jmax_of<PAT, I, NM>(i) == 0) continue;
+    rt += re_mul(X[i], aZ[i]);
+    b3_add(Gs, __ldg(code + NM + i), lane, aZ[i], cf);
+  }
+#pragma unroll
+  for (int j = 0; j < JUSED; ++j) b3_add(Gs, __ldg(code + NM + I + j), lane, gY[j], cf);
+  return cf * rt;
+}
+
 // k_b3_fe. Shared memory: Cs (all combinations' coefficients), Xs[nc][33]
 // (the CTA's factors, element-major), Gs[nc][33] (their density gradient),
 // the per-warp density partials, the atoms' dE/drho, and the element and
 // weight maps.
 
-template <class D, int NW>
+template <class D, int NW, int LOOP>
 __global__ void __launch_bounds__(NW * 32, 1)
     k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
             const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
@@ -480,9 +543,15 @@ __global__ void __launch_bounds__(NW * 32, 1)
       const uint16_t* code = m.b3_code + tk * NPOS;
       const float* Ck = Cs + k * NM * I * I;
       float r;
-      if (pat == 0) r = b3_task<0, D>(Ck, Xs, Gs, code, cf, lane);
-      else if (pat == 1) r = b3_task<1, D>(Ck, Xs, Gs, code, cf, lane);
-      else r = b3_task<2, D>(Ck, Xs, Gs, code, cf, lane);
+      if constexpr (LOOP == 0) {
+        if (pat == 0) r = b3_task<0, D>(Ck, Xs, Gs, code, cf, lane);
+        else if (pat == 1) r = b3_task<1, D>(Ck, Xs, Gs, code, cf, lane);
+        else r = b3_task<2, D>(Ck, Xs, Gs, code, cf, lane);
+      } else {
+        if (pat == 0) r = b3_task_po<0, D>(Ck, Xs, Gs, code, cf, lane);
+        else if (pat == 1) r = b3_task_po<1, D>(Ck, Xs, Gs, code, cf, lane);
+        else r = b3_task_po<2, D>(Ck, Xs, Gs, code, cf, lane);
+      }
       rloc += f2d(r);
     }
     rpart[warp * 32 + lane] = rloc;
