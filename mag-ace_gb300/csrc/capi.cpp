@@ -98,9 +98,9 @@ struct Runtime {
       for (auto* b : {&grp_arity, &grp_len, &grp_first, &grp_seg, &slot_seg, &slot_factor, &slot_weight}) b->release();
     }
   } gb1, gb2;
-  DevBuf<float> b3_Cf, b3_cff, b3_mult;
+  DevBuf<float> b3_Cf, b3_cff, b3_mult, b3_cfw;
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
-  DevBuf<uint16_t> b3_code;
+  DevBuf<uint16_t> b3_code, b3_code2;
   DevBuf<int32_t> d_rank1_n, d_begin;
   DevBuf<int32_t> r_factor, r_run, r_g0, r_warp_begin, r_warp_slots;
   DevBuf<uint32_t> r_rec;
@@ -247,6 +247,12 @@ int upload_tables() {
       CUDA_TRY(R.b3_pattern.upload(D.pattern));
       CUDA_TRY(R.b3_combo.upload(D.task_combo));
       CUDA_TRY(R.b3_code.upload(D.code));
+      CUDA_TRY(R.b3_code2.upload(D.code2));
+      {
+        std::vector<float> cfw(D.ntask);
+        for (int t = 0; t < D.ntask; ++t) cfw[t] = static_cast<float>(D.task_cf[t] * D.task_w[t]);
+        CUDA_TRY(R.b3_cfw.upload(cfw));
+      }
       CUDA_TRY(R.b3_factor.upload(D.factor_of));
       CUDA_TRY(R.b3_cw.upload(D.compact_of_weight));
       CUDA_TRY(R.b3_mult.upload(to_float(D.mult)));
@@ -306,6 +312,8 @@ int upload_tables() {
   d.b3_combo = R.b3_combo.p;
   d.b3_cff = R.b3_cff.p;
   d.b3_code = R.b3_code.p;
+  d.b3_code2 = R.b3_code2.p;
+  d.b3_cfw = R.b3_cfw.p;
   d.b3_factor = R.b3_factor.p;
   d.b3_cw = R.b3_cw.p;
   d.b3_mult = R.b3_mult.p;
@@ -818,6 +826,8 @@ void ace_release_device(void) {
   for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult, &R.c1f}) b->release();
   for (auto* b : {&R.b3_pattern, &R.b3_combo, &R.b3_factor, &R.b3_cw}) b->release();
   R.b3_code.release();
+  R.b3_code2.release();
+  R.b3_cfw.release();
   for (auto* b : {&R.d_rank1_n, &R.d_begin, &R.r_factor, &R.r_run, &R.r_g0, &R.r_warp_begin, &R.r_warp_slots})
     b->release();
   R.r_rec.release();

@@ -75,6 +75,8 @@ struct DeviceModel {
   const int32_t* b3_combo;    // [task]
   const float* b3_cff;        // [task]
   const uint16_t* b3_code;    // [task][NM + 2I] compact element | sign bits
+  const uint16_t* b3_code2;   // [task][NM + 2I] mirror-task gradient target, 0xffff for none
+  const float* b3_cfw;        // [task] density weight (2 or 1) times the coupling
   const int32_t* b3_factor;   // [nc] factor index of each compact element
   const int32_t* b3_cw;       // [nW] compact element of each weight, or -1
   const float* b3_mult;       // [nc] half-plane multiplicity of each element's weight

@@ -1017,11 +1017,13 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
   k_b3_fe<FeDims, NW, LOOP><<<gb, NW * 32, sb, st>>>(m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy,   \
                                                      b.edf, b.dedrho, b.err)
       // variants: (16 warps, n0' innermost), (12, innermost), (8, innermost),
-      // (12, n0' outermost)
+      // (12, n0' outermost), (16, packed FP32x2), (12, packed FP32x2)
       switch (m.tune_b3) {
         case 1: MAGACE_B3(12, 0); break;
         case 2: MAGACE_B3(8, 0); break;
         case 3: MAGACE_B3(12, 1); break;
+        case 4: MAGACE_B3(16, 2); break;
+        case 5: MAGACE_B3(12, 2); break;
         default: MAGACE_B3(16, 0); break;
       }
 #undef MAGACE_B3

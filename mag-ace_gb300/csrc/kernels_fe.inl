@@ -342,13 +342,25 @@ __device__ __forceinline__ C<float> b3_load(const C<float>* Xs, unsigned code, i
   return {__uint_as_float(__float_as_uint(v.x) ^ ((code & 0x8000u) << 16)),
           __uint_as_float(__float_as_uint(v.y) ^ ((code & 0x4000u) << 17))};
 }
-// gradient of a task position; a mirrored factor's gradient belongs to the
-// mirror's weight and is dropped, as the half-plane multiplicities count it
-__device__ __forceinline__ void b3_add(C<float>* Gs, unsigned code, int lane, C<float> v, float cf) {
-  if (code & 0xc000u) return;
-  C<float>* g = Gs + code * kB3Stride + lane;
-  atomicAdd(&g->x, cf * v.x);
-  atomicAdd(&g->y, cf * v.y);
+// gradient of task position `pos`: dRho_T/dF to the element read directly
+// there (a factor read through a mirror code gets nothing: its element's
+// weight collects the mirror task's gradient instead), and the mirror task's
+// gradient s conj(dRho_T/dF) to the element that task reads directly there
+__device__ __forceinline__ void b3_add(C<float>* Gs, const uint16_t* __restrict__ code,
+                                       const uint16_t* __restrict__ code2, int pos, int lane, C<float> v, float cf) {
+  const unsigned c = __ldg(code + pos);
+  if (!(c & 0xc000u)) {
+    C<float>* g = Gs + c * kB3Stride + lane;
+    atomicAdd(&g->x, cf * v.x);
+    atomicAdd(&g->y, cf * v.y);
+  }
+  const unsigned c2 = __ldg(code2 + pos);
+  if (c2 != 0xffffu) {
+    const float s = (c2 & 0x8000u) ? -cf : cf;
+    C<float>* g = Gs + (c2 & 0x3fffu) * kB3Stride + lane;
+    atomicAdd(&g->x, s * v.x);
+    atomicAdd(&g->y, -s * v.y);
+  }
 }
 
 // One task on the lane's atom: the density term cf * sum C[p][i][j] a_p X_i Y_j
@@ -356,7 +368,8 @@ __device__ __forceinline__ void b3_add(C<float>* Gs, unsigned code, int lane, C<
 // coefficients [NM][I][I] in shared memory; rows are read four at a time.
 template <int PAT, class D>
 __device__ __forceinline__ float b3_task(const float* __restrict__ Cs, const C<float>* Xs, C<float>* Gs,
-                                         const uint16_t* __restrict__ code, float cf, int lane) {
+                                         const uint16_t* __restrict__ code, const uint16_t* __restrict__ code2, float cf,
+                                         int lane) {
   constexpr int I = D::I, NM = D::NM;
   static_assert(I % 4 == 0, "rows of C are read as float4");
   constexpr int JUSED = jmax_of<PAT, I, NM>(I - 1);  // largest j bound (rows grow with i)
@@ -407,20 +420,106 @@ __device__ __forceinline__ float b3_task(const float* __restrict__ Cs, const C<f
       ga[p].y += u.y;
     }
     rt += re_mul(x, az);
-    b3_add(Gs, cx, lane, az, cf);
+    b3_add(Gs, code, code2, NM + i, lane, az, cf);
   }
 #pragma unroll
-  for (int j = 0; j < JUSED; ++j) b3_add(Gs, __ldg(code + NM + I + j), lane, gY[j], cf);
+  for (int j = 0; j < JUSED; ++j) b3_add(Gs, code, code2, NM + I + j, lane, gY[j], cf);
 #pragma unroll
-  for (int p = 0; p < NM; ++p) b3_add(Gs, __ldg(code + p), lane, ga[p], cf);
-  return cf * rt;
+  for (int p = 0; p < NM; ++p) b3_add(Gs, code, code2, p, lane, ga[p], cf);
+  return rt;
+}
+
+// The same task with packed FP32x2 arithmetic (__ffma2_rn, two FMAs per
+// instruction): Y and dY are held as pairs of consecutive j, (Y_j, Y_j+1) for
+// the real and the imaginary parts, so that a row of C multiplies two j at a
+// time, and z is summed in two halves. Row lengths round up to even; the
+// coefficient after a row's last allowed j is zero in C.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+template <int PAT, class D>
+__device__ __forceinline__ float b3_task_x2(const float* __restrict__ Cs, const C<float>* Xs, C<float>* Gs,
+                                            const uint16_t* __restrict__ code, const uint16_t* __restrict__ code2, float cf,
+                                         int lane) {
+  constexpr int I = D::I, NM = D::NM, H = I / 2;
+  static_assert(I % 4 == 0, "rows of C are read as float4");
+  constexpr int JUSED = jmax_of<PAT, I, NM>(I - 1);
+  constexpr int HUSED = (JUSED + 1) / 2;
+  float2 Yx[H], Yy[H], gYx[H], gYy[H];
+  C<float> a[NM], ga[NM];
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    C<float> y0 = {0.f, 0.f}, y1 = {0.f, 0.f};
+    if (h < HUSED) {
+      y0 = b3_load(Xs, __ldg(code + NM + I + 2 * h), lane);
+      y1 = b3_load(Xs, __ldg(code + NM + I + 2 * h + 1), lane);
+    }
+    Yx[h] = f2(y0.x, y1.x);
+    Yy[h] = f2(y0.y, y1.y);
+    gYx[h] = f2(0.f, 0.f);
+    gYy[h] = f2(0.f, 0.f);
+  }
+#pragma unroll
+  for (int p = 0; p < NM; ++p) {
+    a[p] = b3_load(Xs, __ldg(code + p), lane);
+    ga[p] = {0.f, 0.f};
+  }
+  float rt = 0.f;
+#pragma unroll
+  for (int i = 0; i < I; ++i) {
+    const int jm = jmax_of<PAT, I, NM>(i);
+    if (jm == 0) continue;
+    const int hm = (jm + 1) / 2;
+    const unsigned cx = __ldg(code + NM + i);
+    const C<float> x = b3_load(Xs, cx, lane);
+    C<float> az = {0.f, 0.f};
+#pragma unroll
+    for (int p = 0; p < NM; ++p) {
+      const C<float> ax = cmul(a[p], x);
+      const float2 axx = f2(ax.x, ax.x), axy = f2(ax.y, ax.y);
+      float2 zx = f2(0.f, 0.f), zy = f2(0.f, 0.f);
+      const float4* crow = reinterpret_cast<const float4*>(Cs + (p * I + i) * I);
+#pragma unroll
+      for (int h4 = 0; h4 < (hm + 1) / 2; ++h4) {
+        const float4 c4 = crow[h4];
+        const float2 cp[2] = {f2(c4.x, c4.y), f2(c4.z, c4.w)};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int h = 2 * h4 + u;
+          if (h < hm) {
+            zx = __ffma2_rn(cp[u], Yx[h], zx);
+            zy = __ffma2_rn(cp[u], Yy[h], zy);
+            gYx[h] = __ffma2_rn(cp[u], axx, gYx[h]);
+            gYy[h] = __ffma2_rn(cp[u], axy, gYy[h]);
+          }
+        }
+      }
+      const C<float> z = {zx.x + zx.y, zy.x + zy.y};
+      const C<float> t = cmul(a[p], z);
+      az.x += t.x;
+      az.y += t.y;
+      const C<float> u = cmul(x, z);
+      ga[p].x += u.x;
+      ga[p].y += u.y;
+    }
+    rt += re_mul(x, az);
+    b3_add(Gs, code, code2, NM + i, lane, az, cf);
+  }
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    if (2 * h < JUSED) b3_add(Gs, code, code2, NM + I + 2 * h, lane, C<float>{gYx[h].x, gYy[h].x}, cf);
+    if (2 * h + 1 < JUSED) b3_add(Gs, code, code2, NM + I + 2 * h + 1, lane, C<float>{gYx[h].y, gYy[h].y}, cf);
+  }
+#pragma unroll
+  for (int p = 0; p < NM; ++p) b3_add(Gs, code, code2, p, lane, ga[p], cf);
+  return rt;
 }
 
 // The same task with the n0' loop outermost and not unrolled: X, Y, dX and
 // dY stay in registers across it (more registers, a third of the code).
 template <int PAT, class D>
 __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const C<float>* Xs, C<float>* Gs,
-                                            const uint16_t* __restrict__ code, float cf, int lane) {
+                                            const uint16_t* __restrict__ code, const uint16_t* __restrict__ code2, float cf,
+                                         int lane) {
   constexpr int I = D::I, NM = D::NM;
   constexpr int JUSED = jmax_of<PAT, I, NM>(I - 1);
   C<float> X[I], Y[I], aZ[I], gY[I];
@@ -465,18 +564,18 @@ __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const 
       ga.x += u.x;
       ga.y += u.y;
     }
-    b3_add(Gs, cp, lane, ga, cf);
+    b3_add(Gs, code, code2, p, lane, ga, cf);
   }
   float rt = 0.f;
 #pragma unroll
   for (int i = 0; i < I; ++i) {
     if (jmax_of<PAT, I, NM>(i) == 0) continue;
     rt += re_mul(X[i], aZ[i]);
-    b3_add(Gs, __ldg(code + NM + i), lane, aZ[i], cf);
+    b3_add(Gs, code, code2, NM + i, lane, aZ[i], cf);
   }
 #pragma unroll
-  for (int j = 0; j < JUSED; ++j) b3_add(Gs, __ldg(code + NM + I + j), lane, gY[j], cf);
-  return cf * rt;
+  for (int j = 0; j < JUSED; ++j) b3_add(Gs, code, code2, NM + I + j, lane, gY[j], cf);
+  return rt;
 }
 
 // k_b3_fe. Shared memory: Cs (all combinations' coefficients), Xs[nc][33]
@@ -541,18 +640,23 @@ __global__ void __launch_bounds__(NW * 32, 1)
       const int pat = __ldg(m.b3_pattern + k);
       const float cf = __ldg(m.b3_cff + tk);
       const uint16_t* code = m.b3_code + tk * NPOS;
+      const uint16_t* code2 = m.b3_code2 + tk * NPOS;
       const float* Ck = Cs + k * NM * I * I;
       float r;
       if constexpr (LOOP == 0) {
-        if (pat == 0) r = b3_task<0, D>(Ck, Xs, Gs, code, cf, lane);
-        else if (pat == 1) r = b3_task<1, D>(Ck, Xs, Gs, code, cf, lane);
-        else r = b3_task<2, D>(Ck, Xs, Gs, code, cf, lane);
+        if (pat == 0) r = b3_task<0, D>(Ck, Xs, Gs, code, code2, cf, lane);
+        else if (pat == 1) r = b3_task<1, D>(Ck, Xs, Gs, code, code2, cf, lane);
+        else r = b3_task<2, D>(Ck, Xs, Gs, code, code2, cf, lane);
+      } else if constexpr (LOOP == 2) {
+        if (pat == 0) r = b3_task_x2<0, D>(Ck, Xs, Gs, code, code2, cf, lane);
+        else if (pat == 1) r = b3_task_x2<1, D>(Ck, Xs, Gs, code, code2, cf, lane);
+        else r = b3_task_x2<2, D>(Ck, Xs, Gs, code, code2, cf, lane);
       } else {
-        if (pat == 0) r = b3_task_po<0, D>(Ck, Xs, Gs, code, cf, lane);
-        else if (pat == 1) r = b3_task_po<1, D>(Ck, Xs, Gs, code, cf, lane);
-        else r = b3_task_po<2, D>(Ck, Xs, Gs, code, cf, lane);
+        if (pat == 0) r = b3_task_po<0, D>(Ck, Xs, Gs, code, code2, cf, lane);
+        else if (pat == 1) r = b3_task_po<1, D>(Ck, Xs, Gs, code, code2, cf, lane);
+        else r = b3_task_po<2, D>(Ck, Xs, Gs, code, code2, cf, lane);
       }
-      rloc += f2d(r);
+      rloc += f2d(__ldg(m.b3_cfw + tk) * r);
     }
     rpart[warp * 32 + lane] = rloc;
     __syncthreads();

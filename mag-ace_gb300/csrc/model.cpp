@@ -702,6 +702,19 @@ void build_dense_b3(Model& M) {
     const int c = L.nWA + p * L.h3 + q * (q + 1) / 2 + std::abs(u);
     return u >= 0 ? static_cast<uint16_t>(c) : mirrored(c, u);
   };
+  // Mirror pairs: negating every m of a task (m1, m0', m1', m2') leaves its
+  // coupling unchanged (each Clebsch-Gordan factor picks up (-1)^(j1+j2-J),
+  // +1 for these even triangles) and turns every factor into +-conj of
+  // itself with signs whose product is +1, so the mirror task's density is
+  // the conjugate of the task's. Only one task of each pair is evaluated:
+  // it contributes 2 Re rho_T (1 for a task that is its own mirror), and for
+  // every position it also adds the mirror task's gradient,
+  // s conj(dRho_T/dF), to the element the mirror task reads directly there
+  // (code2: compact element | bit 15 for s = -1; 0xffff where the mirror
+  // task reads that position through a mirror code itself, or is T).
+  const auto mirror_code = [&](int c, int k) {
+    return static_cast<uint16_t>(c | ((k & 1) ? 0x8000 : 0));
+  };
   for (int k = 0; k < D.ncombo; ++k) {
     const int l1 = D.combo_l[k][0], q0 = D.combo_l[k][1], q1 = D.combo_l[k][2], q2 = D.combo_l[k][3];
     for (int m1 = -l1; m1 <= l1; ++m1) {
@@ -712,14 +725,28 @@ void build_dense_b3(Model& M) {
           if (std::abs(u2) > q2) continue;
           const double cf = cfa * (clebsch_gordan(q0, q1, q2, u0, u1, -u2) * clebsch_gordan(q2, q2, 0, u2, -u2, 0));
           if (cf == 0.0) continue;
+          // keep the task whose (m1, m0', m1') is lexicographically >= its mirror's
+          const std::array<int, 3> me{m1, u0, u1}, mi{-m1, -u0, -u1};
+          if (me < mi) continue;
+          const bool self = me == mi;
           ++D.ntask;
           D.task_combo.push_back(k);
           D.task_cf.push_back(cf);
-          for (int p = 0; p < NM; ++p) D.code.push_back(code_A0(p, q0, u0));
+          D.task_w.push_back(self ? 1.0 : 2.0);
+          for (int p = 0; p < NM; ++p) {
+            D.code.push_back(code_A0(p, q0, u0));
+            D.code2.push_back(self || u0 > 0 ? 0xffff : mirror_code(L.nWA + p * L.h3 + q0 * (q0 + 1) / 2 - u0, u0));
+          }
           for (int n = 0; n < L.n3a; ++n)
-            for (int p = 0; p < NM; ++p) D.code.push_back(code_A(n, l1, m1, p, q1, u1));
+            for (int p = 0; p < NM; ++p) {
+              D.code.push_back(code_A(n, l1, m1, p, q1, u1));
+              D.code2.push_back(self || u1 > 0 ? 0xffff : mirror_code(L.WA(n, l1, -m1, p, q1, -u1), m1 + u1));
+            }
           for (int n = 0; n < L.n3a; ++n)
-            for (int p = 0; p < NM; ++p) D.code.push_back(code_A(n, l1, -m1, p, q2, u2));
+            for (int p = 0; p < NM; ++p) {
+              D.code.push_back(code_A(n, l1, -m1, p, q2, u2));
+              D.code2.push_back(self || u2 > 0 ? 0xffff : mirror_code(L.WA(n, l1, m1, p, q2, -u2), m1 + u2));
+            }
         }
     }
   }
@@ -731,17 +758,21 @@ void build_dense_b3(Model& M) {
   std::stable_sort(order.begin(), order.end(),
                    [&](int x, int y) { return D.pattern[D.task_combo[x]] < D.pattern[D.task_combo[y]]; });
   std::vector<int32_t> combo(D.ntask);
-  std::vector<double> cf(D.ntask);
-  std::vector<uint16_t> code(D.code.size());
+  std::vector<double> cf(D.ntask), w(D.ntask);
+  std::vector<uint16_t> code(D.code.size()), code2(D.code2.size());
   for (int t = 0; t < D.ntask; ++t) {
     combo[t] = D.task_combo[order[t]];
     cf[t] = D.task_cf[order[t]];
-    std::copy(D.code.begin() + static_cast<size_t>(order[t]) * npos,
-              D.code.begin() + static_cast<size_t>(order[t] + 1) * npos, code.begin() + static_cast<size_t>(t) * npos);
+    w[t] = D.task_w[order[t]];
+    const size_t src = static_cast<size_t>(order[t]) * npos, dst = static_cast<size_t>(t) * npos;
+    std::copy(D.code.begin() + src, D.code.begin() + src + npos, code.begin() + dst);
+    std::copy(D.code2.begin() + src, D.code2.begin() + src + npos, code2.begin() + dst);
   }
   D.task_combo.swap(combo);
   D.task_cf.swap(cf);
+  D.task_w.swap(w);
   D.code.swap(code);
+  D.code2.swap(code2);
 }
 
 // Per-cluster m-terms of the descriptors, in coefficient order (ranks 1..4).

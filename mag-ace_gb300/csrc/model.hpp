@@ -97,7 +97,9 @@ struct DenseB3 {
   std::vector<double> C;
   std::vector<int32_t> task_combo;
   std::vector<double> task_cf;
+  std::vector<double> task_w;               // density weight: 2, or 1 for a task that is its own mirror
   std::vector<uint16_t> code;               // [ntask][NM + 2I]
+  std::vector<uint16_t> code2;              // [ntask][NM + 2I] mirror-task gradient target (see build_dense_b3)
   std::vector<int32_t> factor_of;           // [nc] factor index of each compact element
   std::vector<int32_t> compact_of_weight;   // [nW] compact element of each weight, or -1
   std::vector<double> mult;                 // [nc] half-plane multiplicity of each element's weight
