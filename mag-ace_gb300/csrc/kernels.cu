@@ -1059,22 +1059,22 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
     const size_t s3 = forces_fe_smem<R, FeDims>();
-    const int mb = kForceMinBlocksChoices[m.tune_forces];
-#define MAGACE_FORCES(MB)                                                                                          \
-  set_smem(k_forces_fe<R, FeDims, MB>, s3);                                                                        \
-  k_forces_fe<R, FeDims, MB><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,         \
-                                                   reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij, b.tij, \
-                                                   b.ti0, b.err)
+#define MAGACE_FORCES(MB, PK)                                                                                       \
+  set_smem(k_forces_fe<R, FeDims, MB, PK>, s3);                                                                     \
+  k_forces_fe<R, FeDims, MB, PK><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,      \
+                                                       reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij,   \
+                                                       b.tij, b.ti0, b.err)
     if constexpr (sizeof(R) == 8) {
-      (void)mb;
-      MAGACE_FORCES(4);
+      MAGACE_FORCES(4, false);
     } else {
-      if (mb == 4) {
-        MAGACE_FORCES(4);
-      } else if (mb == 6) {
-        MAGACE_FORCES(6);
-      } else {
-        MAGACE_FORCES(8);
+      // variants: CTAs per SM 4 / 6 / 8, scalar then packed FP32x2
+      switch (m.tune_forces) {
+        case 1: MAGACE_FORCES(6, false); break;
+        case 2: MAGACE_FORCES(8, false); break;
+        case 3: MAGACE_FORCES(4, true); break;
+        case 4: MAGACE_FORCES(6, true); break;
+        case 5: MAGACE_FORCES(8, true); break;
+        default: MAGACE_FORCES(4, false); break;
       }
     }
 #undef MAGACE_FORCES

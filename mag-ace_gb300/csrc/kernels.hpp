@@ -20,9 +20,9 @@ constexpr int kMaxLaunches = 4;  // kernels of one evaluation
 constexpr int kRestWarpChoices[2] = {32, 16};
 // (b3 variants 3: n0' loop outermost; 4 and 5: packed FP32x2 arithmetic)
 constexpr int kB3WarpChoices[6] = {16, 12, 8, 12, 16, 12};
-// CTAs per SM the split-precision force kernel's registers must allow
-// (DeviceModel::tune_forces)
-constexpr int kForceMinBlocksChoices[3] = {4, 6, 8};
+// CTAs per SM the split-precision force kernel's registers must allow, for
+// its scalar (variants 0-2) and packed FP32x2 (3-5) forms (DeviceModel::tune_forces)
+constexpr int kForceMinBlocksChoices[6] = {4, 6, 8, 4, 6, 8};
 
 // Device arrays of one evaluation. F and W are complex arrays of the selected
 // precision (FP64: 16 bytes per entry, FP32: 8 bytes).

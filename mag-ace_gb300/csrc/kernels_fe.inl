@@ -715,7 +715,10 @@ __global__ void __launch_bounds__(NW * 32, 1)
 // k_forces_fe: one thread per bond. Weights transposed into shared memory:
 // W2T[k][n] and WAT[k3][i], so the inner loops read 16-byte pairs. MINB is
 // the CTAs per SM the register allocation must allow (a tuning variant).
-template <class R, class D, int MINB>
+// PACKED (split precision only) stores the transposed weights as separate
+// real and imaginary planes and runs the contractions two n (or i) at a
+// time with packed FP32x2 FMAs.
+template <class R, class D, int MINB, bool PACKED>
 __global__ void __launch_bounds__(64, MINB)
     k_forces_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
@@ -737,17 +740,36 @@ __global__ void __launch_bounds__(64, MINB)
   C<R>* cdYa = cYa + D::LSA * T;                         // [LSA][3]
   C<R>* cYm = cdYa + D::LSA * 3 * T;                     // half [H2]
   const int t = threadIdx.x;
+  static_assert(!PACKED || sizeof(R) == 4, "packed contractions are FP32");
+  static_assert(D::NB % 4 == 0 && D::NRY % 4 == 0, "planes are read four floats at a time");
+  // planar views of the same shared memory (PACKED): [k][n] real, then imaginary
+  float* W2x = reinterpret_cast<float*>(W2T);
+  float* W2y = W2x + D::NQ * D::NB;
+  float* WAx = reinterpret_cast<float*>(WAT);
+  float* WAy = WAx + D::NQ3 * D::NRY;
 
   for (int it = blockIdx.x; it < natom; it += gridDim.x) {
     const int atom = queue_atom(m, it);
     const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
     for (int s = t; s < D::NA2H; s += T) {  // W2[n][k] -> W2T[k][n]
       const int n = s / D::NQ, k = s % D::NQ;
-      W2T[k * D::NB + n] = Wa[m.offW2 + s];
+      const C<R> w = Wa[m.offW2 + s];
+      if constexpr (PACKED) {
+        W2x[k * D::NB + n] = w.x;
+        W2y[k * D::NB + n] = w.y;
+      } else {
+        W2T[k * D::NB + n] = w;
+      }
     }
     for (int s = t; s < D::NWA; s += T) {   // WA[i][k3] -> WAT[k3][i]
       const int i = s / D::NQ3, k3 = s % D::NQ3;
-      WAT[k3 * D::NRY + i] = Wa[s];
+      const C<R> w = Wa[s];
+      if constexpr (PACKED) {
+        WAx[k3 * D::NRY + i] = w.x;
+        WAy[k3 * D::NRY + i] = w.y;
+      } else {
+        WAT[k3 * D::NRY + i] = w;
+      }
     }
     for (int s = t; s < D::NQ; s += T) W0s[s] = Wa[m.offW0 + s];
     __syncthreads();
@@ -830,29 +852,80 @@ __global__ void __launch_bounds__(64, MINB)
       {
         R sp[D::NB];
         C<R> U[D::NRY];
+        if constexpr (PACKED) {
+          float2 sp2[D::NB / 2], Ux2[D::NRY / 2], Uy2[D::NRY / 2];
 #pragma unroll
-        for (int n = 0; n < D::NB; ++n) sp[n] = R(0);
+          for (int n = 0; n < D::NB / 2; ++n) sp2[n] = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int i = 0; i < D::NRY; ++i) U[i] = {R(0), R(0)};
+          for (int i = 0; i < D::NRY / 2; ++i) Ux2[i] = Uy2[i] = make_float2(0.f, 0.f);
 #pragma unroll 1
-        for (int nr = 0; nr < D::N2; ++nr)
+          for (int nr = 0; nr < D::N2; ++nr)
 #pragma unroll
-          for (int h = 0; h < D::H2; ++h) {
-            const int k = nr * D::H2 + h;
-            const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
-            const C<R>* w2 = W2T + k * D::NB;
+            for (int h = 0; h < D::H2; ++h) {
+              const int k = nr * D::H2 + h;
+              const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
+              const float2 qxx = make_float2(q.x, q.x), qyy = make_float2(q.y, q.y), qyn = make_float2(-q.y, -q.y);
+              const float4* w2x = reinterpret_cast<const float4*>(W2x + k * D::NB);
+              const float4* w2y = reinterpret_cast<const float4*>(W2y + k * D::NB);
 #pragma unroll
-            for (int n = 0; n < D::NB; ++n) sp[n] += re_mul(w2[n], q);
-            if (nr < D::NM && h < D::H3) {
-              const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
+              for (int n4 = 0; n4 < D::NB / 4; ++n4) {
+                const float4 a = w2x[n4], b = w2y[n4];
+                sp2[2 * n4] = __ffma2_rn(make_float2(a.x, a.y), qxx, sp2[2 * n4]);
+                sp2[2 * n4] = __ffma2_rn(make_float2(b.x, b.y), qyn, sp2[2 * n4]);
+                sp2[2 * n4 + 1] = __ffma2_rn(make_float2(a.z, a.w), qxx, sp2[2 * n4 + 1]);
+                sp2[2 * n4 + 1] = __ffma2_rn(make_float2(b.z, b.w), qyn, sp2[2 * n4 + 1]);
+              }
+              if (nr < D::NM && h < D::H3) {
+                const int k3 = nr * D::H3 + h;
+                const float4* wax = reinterpret_cast<const float4*>(WAx + k3 * D::NRY);
+                const float4* way = reinterpret_cast<const float4*>(WAy + k3 * D::NRY);
 #pragma unroll
-              for (int i = 0; i < D::NRY; ++i) {
-                const C<R> w = wa[i];
-                U[i].x += w.x * q.x - w.y * q.y;
-                U[i].y += w.x * q.y + w.y * q.x;
+                for (int i4 = 0; i4 < D::NRY / 4; ++i4) {
+                  const float4 a = wax[i4], b = way[i4];
+                  const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
+                  const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
+                  Ux2[2 * i4] = __ffma2_rn(b0, qyn, __ffma2_rn(a0, qxx, Ux2[2 * i4]));
+                  Uy2[2 * i4] = __ffma2_rn(b0, qxx, __ffma2_rn(a0, qyy, Uy2[2 * i4]));
+                  Ux2[2 * i4 + 1] = __ffma2_rn(b1, qyn, __ffma2_rn(a1, qxx, Ux2[2 * i4 + 1]));
+                  Uy2[2 * i4 + 1] = __ffma2_rn(b1, qxx, __ffma2_rn(a1, qyy, Uy2[2 * i4 + 1]));
+                }
               }
             }
+#pragma unroll
+          for (int n = 0; n < D::NB / 2; ++n) {
+            sp[2 * n] = sp2[n].x;
+            sp[2 * n + 1] = sp2[n].y;
           }
+#pragma unroll
+          for (int i = 0; i < D::NRY / 2; ++i) {
+            U[2 * i] = {Ux2[i].x, Uy2[i].x};
+            U[2 * i + 1] = {Ux2[i].y, Uy2[i].y};
+          }
+        } else {
+#pragma unroll
+          for (int n = 0; n < D::NB; ++n) sp[n] = R(0);
+#pragma unroll
+          for (int i = 0; i < D::NRY; ++i) U[i] = {R(0), R(0)};
+#pragma unroll 1
+          for (int nr = 0; nr < D::N2; ++nr)
+#pragma unroll
+            for (int h = 0; h < D::H2; ++h) {
+              const int k = nr * D::H2 + h;
+              const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
+              const C<R>* w2 = W2T + k * D::NB;
+#pragma unroll
+              for (int n = 0; n < D::NB; ++n) sp[n] += re_mul(w2[n], q);
+              if (nr < D::NM && h < D::H3) {
+                const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
+#pragma unroll
+                for (int i = 0; i < D::NRY; ++i) {
+                  const C<R> w = wa[i];
+                  U[i].x += w.x * q.x - w.y * q.y;
+                  U[i].y += w.x * q.y + w.y * q.x;
+                }
+              }
+            }
+        }
 #pragma unroll
         for (int n = 0; n < D::NB; ++n) fr += cgd[n * T + t] * sp[n];
         const R invr = rcp(r);
@@ -878,32 +951,81 @@ __global__ void __launch_bounds__(64, MINB)
           RY[i] = cscale(cYa[lma * T + t], cR[(n1 * (D::LA + 1) + l_of_lm(lma)) * T + t]);
         }
         const R invm = rcp(mg);
-#pragma unroll 1
-        for (int nr = 0; nr < D::N2; ++nr)
-#pragma unroll
-          for (int h = 0; h < D::H2; ++h) {
-          const int k = nr * D::H2 + h;
-          const C<R>* w2 = W2T + k * D::NB;
-          C<R> V = {R(0), R(0)};
-#pragma unroll
-          for (int n = 0; n < D::NB; ++n) {
-            V.x += g[n] * w2[n].x;
-            V.y += g[n] * w2[n].y;
-          }
-          if (nr < D::NM && h < D::H3) {
-            const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
-#pragma unroll
-            for (int i = 0; i < D::NRY; ++i) {
-              const C<R> w = wa[i];
-              V.x += w.x * RY[i].x - w.y * RY[i].y;
-              V.y += w.x * RY[i].y + w.y * RY[i].x;
-            }
-          }
+        // V[k] = sum_n g_n W2[n][k] + sum_i W_A[i][k] RY_i, contracted per k
+        const auto contract = [&](int nr, int h, C<R> V) {
           const int q = nr * (D::L2 + 1) + l_of_h(h);
           tr += cMd[q * T + t] * re_mul(V, Ym[h]);
           const R sc = invm * cM[q * T + t];
 #pragma unroll
           for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(V, dYm[h][c]);
+        };
+        if constexpr (PACKED) {
+          float2 g2[D::NB / 2], RYx2[D::NRY / 2], RYy2[D::NRY / 2], RYyn2[D::NRY / 2];
+#pragma unroll
+          for (int n = 0; n < D::NB / 2; ++n) g2[n] = make_float2(g[2 * n], g[2 * n + 1]);
+#pragma unroll
+          for (int i = 0; i < D::NRY / 2; ++i) {
+            RYx2[i] = make_float2(RY[2 * i].x, RY[2 * i + 1].x);
+            RYy2[i] = make_float2(RY[2 * i].y, RY[2 * i + 1].y);
+            RYyn2[i] = make_float2(-RY[2 * i].y, -RY[2 * i + 1].y);
+          }
+#pragma unroll 1
+          for (int nr = 0; nr < D::N2; ++nr)
+#pragma unroll
+            for (int h = 0; h < D::H2; ++h) {
+              const int k = nr * D::H2 + h;
+              float2 vx2 = make_float2(0.f, 0.f), vy2 = make_float2(0.f, 0.f);
+              const float4* w2x = reinterpret_cast<const float4*>(W2x + k * D::NB);
+              const float4* w2y = reinterpret_cast<const float4*>(W2y + k * D::NB);
+#pragma unroll
+              for (int n4 = 0; n4 < D::NB / 4; ++n4) {
+                const float4 a = w2x[n4], b = w2y[n4];
+                vx2 = __ffma2_rn(g2[2 * n4], make_float2(a.x, a.y), vx2);
+                vx2 = __ffma2_rn(g2[2 * n4 + 1], make_float2(a.z, a.w), vx2);
+                vy2 = __ffma2_rn(g2[2 * n4], make_float2(b.x, b.y), vy2);
+                vy2 = __ffma2_rn(g2[2 * n4 + 1], make_float2(b.z, b.w), vy2);
+              }
+              if (nr < D::NM && h < D::H3) {
+                const int k3 = nr * D::H3 + h;
+                const float4* wax = reinterpret_cast<const float4*>(WAx + k3 * D::NRY);
+                const float4* way = reinterpret_cast<const float4*>(WAy + k3 * D::NRY);
+#pragma unroll
+                for (int i4 = 0; i4 < D::NRY / 4; ++i4) {
+                  const float4 a = wax[i4], b = way[i4];
+                  const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
+                  const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
+                  vx2 = __ffma2_rn(b0, RYyn2[2 * i4], __ffma2_rn(a0, RYx2[2 * i4], vx2));
+                  vy2 = __ffma2_rn(b0, RYx2[2 * i4], __ffma2_rn(a0, RYy2[2 * i4], vy2));
+                  vx2 = __ffma2_rn(b1, RYyn2[2 * i4 + 1], __ffma2_rn(a1, RYx2[2 * i4 + 1], vx2));
+                  vy2 = __ffma2_rn(b1, RYx2[2 * i4 + 1], __ffma2_rn(a1, RYy2[2 * i4 + 1], vy2));
+                }
+              }
+              contract(nr, h, C<R>{vx2.x + vx2.y, vy2.x + vy2.y});
+            }
+        } else {
+#pragma unroll 1
+          for (int nr = 0; nr < D::N2; ++nr)
+#pragma unroll
+            for (int h = 0; h < D::H2; ++h) {
+              const int k = nr * D::H2 + h;
+              const C<R>* w2 = W2T + k * D::NB;
+              C<R> V = {R(0), R(0)};
+#pragma unroll
+              for (int n = 0; n < D::NB; ++n) {
+                V.x += g[n] * w2[n].x;
+                V.y += g[n] * w2[n].y;
+              }
+              if (nr < D::NM && h < D::H3) {
+                const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
+#pragma unroll
+                for (int i = 0; i < D::NRY; ++i) {
+                  const C<R> w = wa[i];
+                  V.x += w.x * RY[i].x - w.y * RY[i].y;
+                  V.y += w.x * RY[i].y + w.y * RY[i].x;
+                }
+              }
+              contract(nr, h, V);
+            }
         }
       }
       tij[3 * static_cast<size_t>(j) + 0] = to_d(tr * mx + tt[0]);
