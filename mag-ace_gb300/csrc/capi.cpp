@@ -70,7 +70,7 @@ struct Runtime {
   int last_launches = 0;
   int last_natom = -1;  // atoms of the last evaluation (ace_density_gradient_device)
   bool work_queue = false;  // neighbour-count-sorted work queue
-  int tune_rest = 0, tune_b3 = 0, tune_forces = 0;  // kernel variants (ace_autotune_device)
+  int tune_abasis = 0, tune_rest = 0, tune_b3 = 0, tune_forces = 0;  // kernel variants (ace_autotune_device)
   DevBuf<int> order, queue_bins;
 
   // device tables
@@ -317,6 +317,7 @@ int upload_tables() {
   d.b3_factor = R.b3_factor.p;
   d.b3_cw = R.b3_cw.p;
   d.b3_mult = R.b3_mult.p;
+  d.tune_abasis = R.tune_abasis;
   d.tune_rest = R.tune_rest;
   d.tune_b3 = R.tune_b3;
   d.tune_forces = R.tune_forces;
@@ -707,9 +708,10 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
   const int nr = static_cast<int>(sizeof(kRestWarpChoices) / sizeof(int));
   const int nbw = static_cast<int>(sizeof(kB3WarpChoices) / sizeof(int));
   const int nfv = static_cast<int>(sizeof(kForceMinBlocksChoices) / sizeof(int));
-  float best[3] = {1e30f, 1e30f, 1e30f};  // density, b3, forces
-  int pick[3] = {R.tune_rest, R.tune_b3, R.tune_forces};
+  float best[4] = {1e30f, 1e30f, 1e30f, 1e30f};  // A basis, density, b3, forces
+  int pick[4] = {R.tune_abasis, R.tune_rest, R.tune_b3, R.tune_forces};
   for (int v = 0; v < std::max(nr, std::max(nbw, nfv)); ++v) {
+    R.dm.tune_abasis = std::min(v, kAbasisVariants - 1);
     R.dm.tune_rest = std::min(v, nr - 1);
     R.dm.tune_b3 = std::min(v, nbw - 1);
     R.dm.tune_forces = std::min(v, nfv - 1);
@@ -721,23 +723,23 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
     float ms[kMaxLaunches];
     CUDA_TRY(cudaEventSynchronize(R.ev[R.last_launches]));
     for (int k = 0; k < R.last_launches; ++k) CUDA_TRY(cudaEventElapsedTime(&ms[k], R.ev[k], R.ev[k + 1]));
-    const float t3[3] = {ms[1], ms[2], ms[3]};
-    const int idx[3] = {R.dm.tune_rest, R.dm.tune_b3, R.dm.tune_forces};
-    for (int q = 0; q < 3; ++q)
-      if (t3[q] < best[q]) {
-        best[q] = t3[q];
+    const int idx[4] = {R.dm.tune_abasis, R.dm.tune_rest, R.dm.tune_b3, R.dm.tune_forces};
+    for (int q = 0; q < 4; ++q)
+      if (ms[q] < best[q]) {
+        best[q] = ms[q];
         pick[q] = idx[q];
       }
   }
   R.timing = timing;
-  R.tune_rest = R.dm.tune_rest = pick[0];
-  R.tune_b3 = R.dm.tune_b3 = pick[1];
-  R.tune_forces = R.dm.tune_forces = pick[2];
-  const int best_r = pick[0], best_b = pick[1];
+  R.tune_abasis = R.dm.tune_abasis = pick[0];
+  R.tune_rest = R.dm.tune_rest = pick[1];
+  R.tune_b3 = R.dm.tune_b3 = pick[2];
+  R.tune_forces = R.dm.tune_forces = pick[3];
+  const int best_r = pick[1], best_b = pick[2];
   if (st) return st;
   if (rest_warps) *rest_warps = kRestWarpChoices[best_r];
   if (b3_warps) *b3_warps = kB3WarpChoices[best_b];
-  if (force_blocks) *force_blocks = kForceMinBlocksChoices[pick[2]];
+  if (force_blocks) *force_blocks = kForceMinBlocksChoices[pick[3]];
   return ace_device_status();
 }
 

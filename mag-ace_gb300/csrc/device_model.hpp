@@ -90,7 +90,7 @@ struct DeviceModel {
   const int32_t* r_warp_slots;
   // variants of the split-precision density kernels (indices into the
   // kernels.hpp choice tables)
-  int tune_rest, tune_b3, tune_forces;
+  int tune_abasis, tune_rest, tune_b3, tune_forces;
   // work queue of this evaluation: atoms in order of decreasing bond count,
   // or null for the natural order (set per launch)
   const int32_t* order;

@@ -974,9 +974,19 @@ void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
   const int natom = b.natom;
   if (fe) {
     const size_t s1 = abasis_fe_smem<R, FeDims>();
-    set_smem(k_abasis_fe<R, FeDims>, s1);
-    k_abasis_fe<R, FeDims><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                 reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+    bool packed = false;
+    if constexpr (sizeof(R) == 4) packed = m.tune_abasis == 1;
+    if (packed) {
+      if constexpr (sizeof(R) == 4) {
+        set_smem(k_abasis_fe<R, FeDims, true>, s1);
+        k_abasis_fe<R, FeDims, true><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                           reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+      }
+    } else {
+      set_smem(k_abasis_fe<R, FeDims, false>, s1);
+      k_abasis_fe<R, FeDims, false><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
+                                                          reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+    }
   } else {
     const size_t s1 = abasis_smem<R>(m);
     set_smem(k_abasis<R>, s1);

@@ -15,6 +15,9 @@ constexpr int kDensityThreads = 256;
 constexpr int kForceThreads = 64;
 constexpr int kMaxFeat = 32;     // per-bond radial functions of one kind
 constexpr int kMaxLaunches = 4;  // kernels of one evaluation
+// variants of the split-precision A-basis kernel: scalar, packed FP32x2
+// (DeviceModel::tune_abasis)
+constexpr int kAbasisVariants = 2;
 // warps per CTA of the split-precision density kernels, chosen by
 // DeviceModel::tune_rest / tune_b3 (ace_autotune_device picks them)
 constexpr int kRestWarpChoices[2] = {32, 16};

@@ -47,7 +47,11 @@ __host__ __device__ constexpr int l_of_h(int h) { return h == 0 ? 0 : (h < 3 ? 1
 __host__ __device__ constexpr int l_of_lm(int lm) { return lm == 0 ? 0 : (lm < 4 ? 1 : (lm < 9 ? 2 : (lm < 16 ? 3 : 4))); }
 
 // ===========================================================================
-template <class R, class D>
+// PACKED (split precision only): the M Y tile is stored as real and
+// imaginary planes of 32 columns, and the lanes accumulate column pairs with
+// packed FP32x2 FMAs (warp 0: five pairs of the 18 A columns per half-row,
+// warp 1: eight pairs of the 30 A2 columns; padding pairs are discarded).
+template <class R, class D, bool PACKED>
 __global__ void __launch_bounds__(64)
     k_abasis_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
@@ -57,12 +61,16 @@ __global__ void __launch_bounds__(64)
   static_assert(D::NRY == 16 && D::NB == 16 && D::NQ3 == 18 && D::NQ == 30, "tile shapes assume the Fe layout");
   extern __shared__ __align__(16) unsigned char smem[];
   C<R>* sRY = reinterpret_cast<C<R>*>(smem);             // [TB][NRY]
-  C<R>* sQ = sRY + TB * D::NRY;                           // [TB][NQ]
-  R* sg = reinterpret_cast<R*>(sQ + TB * D::NQ);          // [TB][NB]
+  C<R>* sQ = sRY + TB * D::NRY;                           // [TB][NQ] (PACKED: 2 x [TB][32] floats)
+  constexpr size_t kQBytes = sizeof(C<R>) * D::NQ > sizeof(float) * 64 ? sizeof(C<R>) * D::NQ : sizeof(float) * 64;
+  R* sg = reinterpret_cast<R*>(reinterpret_cast<unsigned char*>(sQ) + TB * kQBytes);  // [TB][NB]
   R* score = sg + TB * D::NB;                             // [TB]
+  float* sQx = reinterpret_cast<float*>(sQ);              // PACKED: [TB][32] real, then imaginary
+  float* sQy = sQx + TB * 32;
   C<R>* accA = sRY;                                       // reuse after the tiles: [NRY][NQ3]
   C<R>* accA2 = accA + D::NWA;                            // [NB][NQ]
   CSum<R> core_sum;  // thread 0: the atom's core energy, over its bond tiles
+  static_assert(!PACKED || (sizeof(R) == 4 && D::H3 == D::H2 && D::NQ <= 32), "packed tiles: FP32, Fe layout");
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int row = lane >> 1, cb = lane & 1;
 
@@ -71,6 +79,9 @@ __global__ void __launch_bounds__(64)
     C<R> acc[15];
 #pragma unroll
     for (int c = 0; c < 15; ++c) acc[c] = {R(0), R(0)};
+    float2 accx[8], accy[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) accx[c] = accy[c] = make_float2(0.f, 0.f);
     core_sum = CSum<R>();
     const int b0 = off[atom], b1 = off[atom + 1];
     for (int t0 = b0; t0 < b1; t0 += TB) {
@@ -113,13 +124,54 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
         for (int nr = 0; nr < D::N2; ++nr)
 #pragma unroll
-          for (int h = 0; h < D::H2; ++h) sQ[t * D::NQ + nr * D::H2 + h] = cscale(Ym[h], Mv[nr * (D::L2 + 1) + l_of_h(h)]);
+          for (int h = 0; h < D::H2; ++h) {
+            const C<R> q = cscale(Ym[h], Mv[nr * (D::L2 + 1) + l_of_h(h)]);
+            if constexpr (PACKED) {
+              sQx[t * 32 + nr * D::H2 + h] = q.x;
+              sQy[t * 32 + nr * D::H2 + h] = q.y;
+            } else {
+              sQ[t * D::NQ + nr * D::H2 + h] = q;
+            }
+          }
+        if constexpr (PACKED) {
+          for (int k = D::NQ; k < 32; ++k) sQx[t * 32 + k] = sQy[t * 32 + k] = 0.f;
+        }
 #pragma unroll
         for (int n = 0; n < D::NB; ++n) sg[t * D::NB + n] = g[n];
         score[t] = cv[0];
       }
       __syncthreads();
-      if (warp == 0) {
+      if constexpr (PACKED) {
+        if (warp == 0) {
+          // A[row][10cb .. 10cb+9] (columns 18, 19 padding)
+          for (int b = 0; b < nb; ++b) {
+            const C<R> ry = sRY[b * D::NRY + row];
+            const float2 rxx = make_float2(ry.x, ry.x), ryy = make_float2(ry.y, ry.y),
+                         ryn = make_float2(-ry.y, -ry.y);
+            const float2* qx = reinterpret_cast<const float2*>(sQx + b * 32 + 10 * cb);
+            const float2* qy = reinterpret_cast<const float2*>(sQy + b * 32 + 10 * cb);
+#pragma unroll
+            for (int c = 0; c < 5; ++c) {
+              const float2 a = qx[c], d = qy[c];
+              accx[c] = __ffma2_rn(ryn, d, __ffma2_rn(rxx, a, accx[c]));
+              accy[c] = __ffma2_rn(ryy, a, __ffma2_rn(rxx, d, accy[c]));
+            }
+          }
+        } else {
+          // A2[row][16cb .. 16cb+15] (columns 30, 31 padding)
+          for (int b = 0; b < nb; ++b) {
+            const R gv = sg[b * D::NB + row];
+            const float2 gg = make_float2(gv, gv);
+            const float2* qx = reinterpret_cast<const float2*>(sQx + b * 32 + 16 * cb);
+            const float2* qy = reinterpret_cast<const float2*>(sQy + b * 32 + 16 * cb);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+              accx[c] = __ffma2_rn(gg, qx[c], accx[c]);
+              accy[c] = __ffma2_rn(gg, qy[c], accy[c]);
+            }
+          }
+        }
+      } else if (warp == 0) {
         // A[row][9cb .. 9cb+8], row = (n1, l1 m1), column = (n2, l2 m2 >= 0)
         for (int b = 0; b < nb; ++b) {
           const C<R> ry = sRY[b * D::NRY + row];
@@ -147,7 +199,23 @@ __global__ void __launch_bounds__(64)
         for (int b = 0; b < nb; ++b) core_sum.add(score[b]);
     }
     __syncthreads();
-    if (warp == 0) {
+    if constexpr (PACKED) {
+      if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < 10; ++c) {
+          const int k3 = 10 * cb + c;
+          const float2 x = accx[c / 2], y = accy[c / 2];
+          if (k3 < D::NQ3) accA[row * D::NQ3 + k3] = (c & 1) ? C<R>{x.y, y.y} : C<R>{x.x, y.x};
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const int k = 16 * cb + c;
+          const float2 x = accx[c / 2], y = accy[c / 2];
+          if (k < D::NQ) accA2[row * D::NQ + k] = (c & 1) ? C<R>{x.y, y.y} : C<R>{x.x, y.x};
+        }
+      }
+    } else if (warp == 0) {
 #pragma unroll
       for (int c = 0; c < 9; ++c) accA[row * D::NQ3 + 9 * cb + c] = acc[c];
     } else {
@@ -1073,7 +1141,9 @@ __global__ void __launch_bounds__(64, MINB)
 
 template <class R, class D>
 size_t abasis_fe_smem() {
-  return sizeof(C<R>) * 64 * (D::NRY + D::NQ) + sizeof(R) * 64 * (D::NB + 1) + 64;
+  // sQ holds NQ complex or, packed, 2 x 32 floats per bond
+  const size_t q = sizeof(C<R>) * D::NQ > sizeof(float) * 64 ? sizeof(C<R>) * D::NQ : sizeof(float) * 64;
+  return sizeof(C<R>) * 64 * D::NRY + q * 64 + sizeof(R) * 64 * (D::NB + 1) + 64;
 }
 inline size_t density_fe_smem(const DeviceModel& m, int nw) {
   return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * nw * 32;
