@@ -329,8 +329,7 @@ def gpu_arm(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "f64" if headline == "fp64" else "f32/f64-split",
         "data": "synthetic (seeded potential and structure)",
         "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": headline,
-                   "tuned": {"density_warps": tuned[0], "b3_warps": tuned[1], "force_ctas_per_sm": tuned[2]}
-                   if tuned else None,
+                   "tuned": lib.get_tuning() if tuned else None,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": whole_job_rate(total_atoms, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "host_access": lib.host_access(),

@@ -103,7 +103,8 @@ struct Runtime {
   DevBuf<uint16_t> b3_code, b3_code2;
   DevBuf<int32_t> d_rank1_n, d_begin;
   DevBuf<int32_t> r_factor, r_run, r_g0, r_warp_begin, r_warp_slots;
-  DevBuf<uint32_t> r_rec;
+  DevBuf<uint32_t> r_rec, r_stream;
+  DevBuf<int32_t> r_stream_begin;
   DevBuf<double> d_cf;
   DevBuf<uint16_t> d_o;
   DeviceModel dm{};
@@ -263,6 +264,8 @@ int upload_tables() {
       CUDA_TRY(R.r_rec.upload(T.rec));
       CUDA_TRY(R.r_warp_begin.upload(T.warp_begin));
       CUDA_TRY(R.r_warp_slots.upload(T.warp_slots));
+      CUDA_TRY(R.r_stream.upload(T.stream));
+      CUDA_TRY(R.r_stream_begin.upload(T.stream_begin));
     } else {
       R.dm.g2 = R.dm.g;
     }
@@ -329,6 +332,8 @@ int upload_tables() {
   d.r_g0 = R.r_g0.p;
   d.r_warp_begin = R.r_warp_begin.p;
   d.r_warp_slots = R.r_warp_slots.p;
+  d.r_stream = R.r_stream.p;
+  d.r_stream_begin = R.r_stream_begin.p;
   d.d_n1 = M.desc.n1;
   d.d_nB = M.desc.nB;
   d.d_rank1_n = R.d_rank1_n.p;
@@ -743,6 +748,15 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
   return ace_device_status();
 }
 
+int ace_get_tuning(int* variants) {
+  Runtime& R = rt();
+  variants[0] = R.tune_abasis;
+  variants[1] = R.tune_rest;
+  variants[2] = R.tune_b3;
+  variants[3] = R.tune_forces;
+  return set_error(MAGACE_OK, "");
+}
+
 int ace_num_coefficients(int* ncoef, int* ndensity) {
   Runtime& R = rt();
   if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
@@ -833,6 +847,8 @@ void ace_release_device(void) {
   for (auto* b : {&R.d_rank1_n, &R.d_begin, &R.r_factor, &R.r_run, &R.r_g0, &R.r_warp_begin, &R.r_warp_slots})
     b->release();
   R.r_rec.release();
+  R.r_stream.release();
+  R.r_stream_begin.release();
   R.d_cf.release();
   R.d_o.release();
   R.gb1.release();

@@ -14,6 +14,8 @@ constexpr int kMaxFull = (kMaxL + 1) * (kMaxL + 1);      // packed (l, -l..l)
 // warps of the split-precision rest kernel; its slot schedule is built for
 // this many on the host
 constexpr int kRestTableWarps = 32;
+// flag of a slot's end record in the rest kernel's record stream
+constexpr uint32_t kRestEnd = 0x80000000u;
 
 // device-side error codes (first one wins)
 enum DeviceError : int {
@@ -88,6 +90,8 @@ struct DeviceModel {
   const int32_t* r_g0;
   const int32_t* r_warp_begin;  // [warps + 1]
   const int32_t* r_warp_slots;
+  const uint32_t* r_stream;     // [records][4] per-warp record streams
+  const int32_t* r_stream_begin;  // [warps + 1]
   // variants of the split-precision density kernels (indices into the
   // kernels.hpp choice tables)
   int tune_abasis, tune_rest, tune_b3, tune_forces;

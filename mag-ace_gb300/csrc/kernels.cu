@@ -1013,13 +1013,17 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const int rw = kRestWarpChoices[m.tune_rest], bw = kB3WarpChoices[m.tune_b3];
       (void)bw;
       const size_t s2 = density_fe_smem(m, rw);
-      if (rw == 16) {
-        set_smem(k_density_fe<FeDims, 16>, s2);
-        k_density_fe<FeDims, 16><<<gb, 16 * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest);
-      } else {
-        set_smem(k_density_fe<FeDims, 32>, s2);
-        k_density_fe<FeDims, 32><<<gb, 32 * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest);
+#define MAGACE_REST(NW, SM)                         \
+  set_smem(k_density_fe<FeDims, NW, SM>, s2);       \
+  k_density_fe<FeDims, NW, SM><<<gb, NW * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest)
+      // variants: 32 or 16 warps; per-entry uniform loads, or record streams
+      switch (m.tune_rest) {
+        case 1: MAGACE_REST(16, false); break;
+        case 2: MAGACE_REST(32, true); break;
+        case 3: MAGACE_REST(16, true); break;
+        default: MAGACE_REST(32, false); break;
       }
+#undef MAGACE_REST
       if (ev_between) cudaEventRecord(ev_between, st);
       const size_t sb = b3_fe_smem<FeDims>(m, bw);
 #define MAGACE_B3(NW, LOOP)                                                                                  \

@@ -329,8 +329,11 @@ __device__ __forceinline__ void rest_run(const uint4* __restrict__ rec, int e0, 
 }
 
 // NW warps per CTA (a divisor of kRestTableWarps): warp w walks the slots
-// the host schedule gave to warps w, w + NW, ...
-template <class D, int NW>
+// the host schedule gave to warps w, w + NW, ... With STREAM the warp reads
+// its slots as one record stream, 32 records per coalesced load, and
+// broadcasts record q to every lane with warp shuffles, instead of one
+// warp-uniform load per entry.
+template <class D, int NW, bool STREAM>
 __global__ void __launch_bounds__(NW * 32, 1)
     k_density_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
                  double* __restrict__ rho_rest) {
@@ -366,23 +369,59 @@ __global__ void __launch_bounds__(NW * 32, 1)
     __syncthreads();
     const int atom = lane < na ? s_atom[lane] : -1;
     double rloc = 0.0;
-    for (int sw = warp; sw < kRestTableWarps; sw += NW)
-    for (int q = __ldg(m.r_warp_begin + sw); q < __ldg(m.r_warp_begin + sw + 1); ++q) {
-      const int s = __ldg(m.r_warp_slots + q);
-      float vx = 0.f, vy = 0.f;
-      rest_run<1>(rec, __ldg(m.r_run + 3 * s), __ldg(m.r_run + 3 * s + 1), Fs, lane, vx, vy);
-      rest_run<2>(rec, __ldg(m.r_run + 3 * s + 1), __ldg(m.r_run + 3 * s + 2), Fs, lane, vx, vy);
-      rest_run<3>(rec, __ldg(m.r_run + 3 * s + 2), __ldg(m.r_run + 3 * s + 3), Fs, lane, vx, vy);
-      const int g0 = __ldg(m.r_g0 + s);
-      if (g0 >= 0) {
-        const C<float> f = Fs[g0 * kRestStride + lane];
-        rloc += f2d(f.x * vx) - f2d(f.y * vy);
+    if constexpr (STREAM) {
+      const uint4* srec = reinterpret_cast<const uint4*>(m.r_stream);
+      for (int sw = warp; sw < kRestTableWarps; sw += NW) {
+        const int e0 = __ldg(m.r_stream_begin + sw), e1 = __ldg(m.r_stream_begin + sw + 1);
+        float vx = 0.f, vy = 0.f;
+        for (int base = e0; base < e1; base += 32) {
+          const uint4 mine = base + lane < e1 ? __ldg(srec + base + lane) : make_uint4(0u, 0u, 0u, 0u);
+          const int n = min(32, e1 - base);
+          for (int q = 0; q < n; ++q) {
+            const unsigned rx = __shfl_sync(0xffffffffu, mine.x, q), ry = __shfl_sync(0xffffffffu, mine.y, q);
+            const unsigned rz = __shfl_sync(0xffffffffu, mine.z, q), rw = __shfl_sync(0xffffffffu, mine.w, q);
+            if (rw & kRestEnd) {
+              // end of a slot: density term and unscaled weight
+              const int g0 = static_cast<int>(rz), w = static_cast<int>(ry);
+              if (g0 >= 0) {
+                const C<float> f = Fs[g0 * kRestStride + lane];
+                rloc += f2d(f.x * vx) - f2d(f.y * vy);
+              }
+              if (w >= 0 && atom >= 0) {
+                const float mu = __uint_as_float(rx);
+                W[static_cast<size_t>(atom) * nW + w] = {vx * mu, vy * mu};
+              }
+              vx = vy = 0.f;
+            } else {
+              const float k = __uint_as_float(rx);
+              C<float> p = Fs[(ry & 0xffffu) * kRestStride + lane];
+              if (rw >= 2u) p = cmul(p, Fs[(ry >> 16) * kRestStride + lane]);
+              if (rw == 3u) p = cmul(p, Fs[rz * kRestStride + lane]);
+              vx += k * p.x;
+              vy += k * p.y;
+            }
+          }
+        }
       }
-      const int w = __ldg(g.slot_weight + s);
-      if (w >= 0 && atom >= 0) {
-        const float mu = __ldg(g.slot_multf + s);
-        W[static_cast<size_t>(atom) * nW + w] = {vx * mu, vy * mu};
-      }
+    } else {
+      for (int sw = warp; sw < kRestTableWarps; sw += NW)
+        for (int q = __ldg(m.r_warp_begin + sw); q < __ldg(m.r_warp_begin + sw + 1); ++q) {
+          const int s = __ldg(m.r_warp_slots + q);
+          float vx = 0.f, vy = 0.f;
+          rest_run<1>(rec, __ldg(m.r_run + 3 * s), __ldg(m.r_run + 3 * s + 1), Fs, lane, vx, vy);
+          rest_run<2>(rec, __ldg(m.r_run + 3 * s + 1), __ldg(m.r_run + 3 * s + 2), Fs, lane, vx, vy);
+          rest_run<3>(rec, __ldg(m.r_run + 3 * s + 2), __ldg(m.r_run + 3 * s + 3), Fs, lane, vx, vy);
+          const int g0 = __ldg(m.r_g0 + s);
+          if (g0 >= 0) {
+            const C<float> f = Fs[g0 * kRestStride + lane];
+            rloc += f2d(f.x * vx) - f2d(f.y * vy);
+          }
+          const int w = __ldg(g.slot_weight + s);
+          if (w >= 0 && atom >= 0) {
+            const float mu = __ldg(g.slot_multf + s);
+            W[static_cast<size_t>(atom) * nW + w] = {vx * mu, vy * mu};
+          }
+        }
     }
     rpart[warp * 32 + lane] = rloc;
     __syncthreads();

@@ -453,7 +453,7 @@ void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
 // slot's entries contiguous (arity 1, then 2, then 3), factors renumbered
 // into the compact set the terms use, and the slots dealt to the kernel's
 // warps longest first onto the least loaded warp.
-void build_rest(const Model& M, const TermSink& sink, RestTable& T) {
+void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, RestTable& T) {
   const FactorLayout& L = M.L;
   T = RestTable();
   std::vector<int32_t> compact(L.nF, -1);
@@ -467,6 +467,9 @@ void build_rest(const Model& M, const TermSink& sink, RestTable& T) {
   T.nslot = sink.nslot;
   T.run.assign(3 * T.nslot + 1, 0);
   T.slot_g0.assign(T.nslot, -1);
+  T.slot_weight.assign(g.slot_weight.begin(), g.slot_weight.end());
+  T.slot_mult.assign(T.nslot, 0.0f);
+  for (int s = 0; s < T.nslot; ++s) T.slot_mult[s] = static_cast<float>(g.slot_mult[s]);
   std::vector<double> cost(T.nslot, 0.0);
   for (int s = 0; s < T.nslot; ++s) {
     if (s < L.n2m * L.ls2) T.slot_g0[s] = static_cast<int32_t>(use(L.offA0 + s));
@@ -502,6 +505,24 @@ void build_rest(const Model& M, const TermSink& sink, RestTable& T) {
     T.warp_begin[w + 1] = T.warp_begin[w] + static_cast<int32_t>(per[w].size());
     T.warp_slots.insert(T.warp_slots.end(), per[w].begin(), per[w].end());
   }
+  // record streams per warp: each slot's entries, then its end record
+  // {multiplicity bits, weight index, A0 factor, kRestEnd | slot}
+  T.stream_begin.assign(T.nwarp + 1, 0);
+  for (int w = 0; w < T.nwarp; ++w) {
+    for (int s : per[w]) {
+      for (int a = 1; a <= 3; ++a)
+        for (int e = T.run[3 * s + a - 1]; e < T.run[3 * s + a]; ++e) {
+          const uint32_t* r = &T.rec[4 * static_cast<size_t>(e)];
+          T.stream.insert(T.stream.end(), {r[0], r[1], r[2], static_cast<uint32_t>(a)});
+        }
+      const float mu = T.slot_mult[s];
+      uint32_t mb;
+      std::memcpy(&mb, &mu, sizeof(mb));
+      T.stream.insert(T.stream.end(), {mb, static_cast<uint32_t>(T.slot_weight[s]), static_cast<uint32_t>(T.slot_g0[s]),
+                                       kRestEnd | static_cast<uint32_t>(s)});
+    }
+    T.stream_begin[w + 1] = static_cast<int32_t>(T.stream.size() / 4);
+  }
 }
 
 int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestTable* rest = nullptr) {
@@ -528,7 +549,6 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
   });
   if (with_b3)
     for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
-  if (rest) build_rest(M, sink, *rest);
 
   // flatten into segments, then pack segments into warp groups
   g = GatherTable();
@@ -626,6 +646,7 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
           g.slot_weight[s] = w;
           g.slot_mult[s] = m == 0 ? 1.0 : 2.0;
         }
+  if (rest) build_rest(M, sink, g, *rest);
   (void)d;
   (void)nd;
   (void)msg;

@@ -49,6 +49,7 @@ SIGNATURES = {
     "ace_host_access_mode": (_i, []),
     "ace_num_coefficients": (_i, [_pi, _pi]),
     "ace_set_work_queue": (_i, [_i]),
+    "ace_get_tuning": (_i, [_pi]),
     "ace_autotune_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _pi, _pi, _pi]),
     "ace_md_create": (_i, [_i, _pd, _pd, _pd, _pd, _pi, _d, _d, _d, _pi]),
     "ace_md_run": (_i, [_i, _i, _d, _i, _i, _pd]),
@@ -165,6 +166,23 @@ def autotune_device(natom, nei, off, r, e, magj, mhj, magi, mhi, stream=0) -> tu
     _check(load().ace_autotune_device(natom, nei, off, r, e, magj, mhj, magi, mhi, stream, ctypes.byref(rw),
                                       ctypes.byref(bw), ctypes.byref(fb)))
     return rw.value, bw.value, fb.value
+
+
+TUNING_NAMES = {
+    "abasis": ["scalar", "packed FP32x2"],
+    "density": ["32 warps", "16 warps", "32 warps, record streams", "16 warps, record streams"],
+    "b3": ["16 warps", "12 warps", "8 warps", "12 warps, n0' outermost", "16 warps, packed FP32x2",
+           "12 warps, packed FP32x2"],
+    "forces": ["4 CTAs/SM", "6 CTAs/SM", "8 CTAs/SM", "4 CTAs/SM, packed FP32x2", "6 CTAs/SM, packed FP32x2",
+               "8 CTAs/SM, packed FP32x2"],
+}
+
+
+def get_tuning() -> dict:
+    """The split-precision kernel variants in use, by kernel."""
+    v = np.zeros(4, np.int32)
+    _check(load().ace_get_tuning(_ip(v)))
+    return {k: TUNING_NAMES[k][int(i)] for k, i in zip(("abasis", "density", "b3", "forces"), v)}
 
 
 def num_coefficients() -> tuple:
