@@ -113,7 +113,7 @@ struct Runtime {
   // work buffers
   DevBuf<int> off, err;
   DevBuf<double> r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0, rho1, core, edf, dedrho;
-  DevBuf<unsigned char> F, W, aux;
+  DevBuf<unsigned char> F, W, aux, bstage;
   std::vector<int> h_off;
 
   // pinned staging for host transfers, and whether the GPU reads pageable
@@ -367,7 +367,7 @@ int reserve_work(int natom, int nei, int precision) {
   CUDA_TRY(R.F.reserve(na * R.dm.nF * csz));
   CUDA_TRY(R.W.reserve(na * R.dm.nW * csz));
   CUDA_TRY(R.aux.reserve(eval_aux_bytes(R.dm, precision, natom)));
-  (void)nb;
+  CUDA_TRY(R.bstage.reserve(nb * 8 * (precision == 0 ? sizeof(double) : sizeof(float))));
   return MAGACE_OK;
 }
 
@@ -381,6 +381,7 @@ int run_eval(EvalBuffers& b, cudaStream_t st) {
   b.dedrho = R.dedrho.p;
   b.err = R.err.p;
   b.aux = R.aux.p;
+  b.stage = R.bstage.p;
   CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), st));
   if (R.work_queue && b.natom > 0) {
     CUDA_TRY(R.order.reserve(static_cast<size_t>(b.natom)));
@@ -857,6 +858,7 @@ void ace_release_device(void) {
   R.err.release();
   R.F.release();
   R.aux.release();
+  R.bstage.release();
   R.order.release();
   R.queue_bins.release();
   R.W.release();
@@ -901,9 +903,11 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
     off[i + 1] = off[i] + cnt;
   }
   const long npacked = off[natom];
-  if (occlist)
-    for (int j = 0; j < nei; ++j)
-      if (occlist[j] != 1) return fail(MAGACE_ERR_ARGS, "neighbour element index other than 1", npacked);
+  if (occlist) {
+    unsigned bad = 0;  // a branch-free scan the compiler vectorises
+    for (int j = 0; j < nei; ++j) bad |= static_cast<unsigned>(occlist[j] ^ 1);
+    if (bad) return fail(MAGACE_ERR_ARGS, "neighbour element index other than 1", npacked);
+  }
   int st = upload_tables();
   if (st) return fail(st, R.last_msg.c_str(), npacked);
   st = reserve_work(natom, static_cast<int>(npacked), R.precision);

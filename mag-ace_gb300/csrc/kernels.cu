@@ -980,12 +980,14 @@ void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       if constexpr (sizeof(R) == 4) {
         set_smem(k_abasis_fe<R, FeDims, true>, s1);
         k_abasis_fe<R, FeDims, true><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                           reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+                                                           reinterpret_cast<C<R>*>(b.F), b.rho1, b.core,
+                                                           static_cast<R*>(b.stage), b.err);
       }
     } else {
       set_smem(k_abasis_fe<R, FeDims, false>, s1);
       k_abasis_fe<R, FeDims, false><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                          reinterpret_cast<C<R>*>(b.F), b.rho1, b.core, b.err);
+                                                          reinterpret_cast<C<R>*>(b.F), b.rho1, b.core,
+                                                          static_cast<R*>(b.stage), b.err);
     }
   } else {
     const size_t s1 = abasis_smem<R>(m);
@@ -1077,7 +1079,7 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   set_smem(k_forces_fe<R, FeDims, MB, PK>, s3);                                                                     \
   k_forces_fe<R, FeDims, MB, PK><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,      \
                                                        reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij,   \
-                                                       b.tij, b.ti0, b.err)
+                                                       b.tij, b.ti0, static_cast<const R*>(b.stage), b.err)
     if constexpr (sizeof(R) == 8) {
       MAGACE_FORCES(4, false);
     } else {

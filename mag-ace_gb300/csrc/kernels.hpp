@@ -51,6 +51,7 @@ struct EvalBuffers {
   int* err = nullptr;         // device error word
   void* aux = nullptr;        // [eval_aux_bytes] scratch of the specialised split-precision kernels
   const int* order = nullptr; // [natom] work queue (atoms by decreasing bond count) or null
+  void* stage = nullptr;      // [nei][8] bond inputs in the working precision (specialised kernels), or null
 };
 
 // Work queue of one evaluation: the atoms sorted by decreasing bond count

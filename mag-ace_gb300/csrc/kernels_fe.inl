@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(64)
     k_abasis_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
                 const double* __restrict__ magi, const double* __restrict__ mhi, C<R>* __restrict__ F,
-                double* __restrict__ rho1, double* __restrict__ core_out, int* err) {
+                double* __restrict__ rho1, double* __restrict__ core_out, R* __restrict__ stage, int* err) {
   constexpr int TB = 64;
   static_assert(D::NRY == 16 && D::NB == 16 && D::NQ3 == 18 && D::NQ == 30, "tile shapes assume the Fe layout");
   extern __shared__ __align__(16) unsigned char smem[];
@@ -89,9 +89,26 @@ __global__ void __launch_bounds__(64)
       __syncthreads();
       if (t < nb) {
         const int j = t0 + t;
+        // the bond's inputs in the working precision; with `stage`, also
+        // kept in device memory for the force kernel (8 values per bond)
+        const R br = to_r<R>(rr[j]);
+        const R bex = to_r<R>(ee[3 * j]), bey = to_r<R>(ee[3 * j + 1]), bez = to_r<R>(ee[3 * j + 2]);
+        const R bmg = to_r<R>(magj[j]);
+        const R bmx = to_r<R>(mhj[3 * j]), bmy = to_r<R>(mhj[3 * j + 1]), bmz = to_r<R>(mhj[3 * j + 2]);
+        if (stage) {
+          R* sp = stage + 8 * static_cast<size_t>(j);
+          sp[0] = br;
+          sp[1] = bex;
+          sp[2] = bey;
+          sp[3] = bez;
+          sp[4] = bmg;
+          sp[5] = bmx;
+          sp[6] = bmy;
+          sp[7] = bmz;
+        }
         R g[D::NB], Rv[D::NR], Mv[D::NMF], cv[1], dummy[1];
         R wl = R(0);
-        const int nla = atomic_bin_r<R>(m, to_r<R>(rr[j]), wl, err);
+        const int nla = atomic_bin_r<R>(m, br, wl, err);
         if (nla > 0) {
           lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, rscale_a<R>(m), g, dummy);
           lut_eval<false>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, rscale_a<R>(m), Rv, dummy);
@@ -104,7 +121,7 @@ __global__ void __launch_bounds__(64)
           cv[0] = R(0);
         }
         R wm = R(0);
-        const int nlm = magnetic_bin_r<R>(m, to_r<R>(magj[j]), wm, err);
+        const int nlm = magnetic_bin_r<R>(m, bmg, wm, err);
         if (nlm > 0) {
           lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, rscale_m<R>(m), Mv, dummy);
         } else {
@@ -112,8 +129,8 @@ __global__ void __launch_bounds__(64)
           for (int q = 0; q < D::NMF; ++q) Mv[q] = R(nlm == 0 ? 1 : 0);
         }
         C<R> Ya[D::HA], Ym[D::H2];
-        ylm_half<R, false>(D::LA, to_r<R>(ee[3 * j]), to_r<R>(ee[3 * j + 1]), to_r<R>(ee[3 * j + 2]), Ya, nullptr);
-        ylm_half<R, false>(D::L2, to_r<R>(mhj[3 * j]), to_r<R>(mhj[3 * j + 1]), to_r<R>(mhj[3 * j + 2]), Ym, nullptr);
+        ylm_half<R, false>(D::LA, bex, bey, bez, Ya, nullptr);
+        ylm_half<R, false>(D::L2, bmx, bmy, bmz, Ym, nullptr);
 #pragma unroll
         for (int n1 = 0; n1 < D::NA; ++n1)
 #pragma unroll
@@ -831,7 +848,7 @@ __global__ void __launch_bounds__(64, MINB)
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
                 const double* __restrict__ magi, const double* __restrict__ mhi, const C<R>* __restrict__ W,
                 const double* __restrict__ edf_in, const double* __restrict__ dedrho, double* __restrict__ fij,
-                double* __restrict__ tij, double* __restrict__ ti0, int* err) {
+                double* __restrict__ tij, double* __restrict__ ti0, const R* __restrict__ stage, int* err) {
   constexpr int T = 64;
   extern __shared__ __align__(16) unsigned char smem[];
   C<R>* W2T = reinterpret_cast<C<R>*>(smem);   // [NQ][NB]
@@ -883,10 +900,27 @@ __global__ void __launch_bounds__(64, MINB)
     const R edf = to_r<R>(edf_in[atom]);
     const int b0 = off[atom], b1 = off[atom + 1];
     for (int j = b0 + t; j < b1; j += T) {
-      const R r = to_r<R>(rr[j]);
-      const R ex = to_r<R>(ee[3 * j]), ey = to_r<R>(ee[3 * j + 1]), ez = to_r<R>(ee[3 * j + 2]);
-      const R mg = to_r<R>(magj[j]);
-      const R mx = to_r<R>(mhj[3 * j]), my = to_r<R>(mhj[3 * j + 1]), mz = to_r<R>(mhj[3 * j + 2]);
+      R r, ex, ey, ez, mg, mx, my, mz;
+      if (stage) {  // the A-basis kernel's copy in device memory
+        const R* sp = stage + 8 * static_cast<size_t>(j);
+        r = sp[0];
+        ex = sp[1];
+        ey = sp[2];
+        ez = sp[3];
+        mg = sp[4];
+        mx = sp[5];
+        my = sp[6];
+        mz = sp[7];
+      } else {
+        r = to_r<R>(rr[j]);
+        ex = to_r<R>(ee[3 * j]);
+        ey = to_r<R>(ee[3 * j + 1]);
+        ez = to_r<R>(ee[3 * j + 2]);
+        mg = to_r<R>(magj[j]);
+        mx = to_r<R>(mhj[3 * j]);
+        my = to_r<R>(mhj[3 * j + 1]);
+        mz = to_r<R>(mhj[3 * j + 2]);
+      }
       R g[D::NB];
       R cdv = R(0);
       {
