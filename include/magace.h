@@ -189,7 +189,8 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
 
 /* The kernel variants in use, variants[4]: A basis (0 scalar, 1 packed
  * FP32x2), 2-/4-body density (0/1: 32/16 warps with per-entry loads, 2/3:
- * 32/16 warps reading record streams), 3-body (0-2: 16/12/8 warps, 3: 12
+ * 32/16 warps reading record streams by shuffles, 4/5: through shared
+ * memory), 3-body (0-2: 16/12/8 warps, 3: 12
  * warps with the n0' loop outermost, 4/5: 16/12 warps packed FP32x2), forces
  * (0-2: 4/6/8 CTAs per SM, 3-5: the same packed FP32x2). */
 int ace_get_tuning(int* variants);

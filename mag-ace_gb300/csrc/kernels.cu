@@ -1018,12 +1018,15 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
 #define MAGACE_REST(NW, SM)                         \
   set_smem(k_density_fe<FeDims, NW, SM>, s2);       \
   k_density_fe<FeDims, NW, SM><<<gb, NW * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest)
-      // variants: 32 or 16 warps; per-entry uniform loads, or record streams
+      // variants: 32 or 16 warps; per-entry uniform loads, record streams
+      // broadcast by shuffles, or record streams through shared memory
       switch (m.tune_rest) {
-        case 1: MAGACE_REST(16, false); break;
-        case 2: MAGACE_REST(32, true); break;
-        case 3: MAGACE_REST(16, true); break;
-        default: MAGACE_REST(32, false); break;
+        case 1: MAGACE_REST(16, 0); break;
+        case 2: MAGACE_REST(32, 1); break;
+        case 3: MAGACE_REST(16, 1); break;
+        case 4: MAGACE_REST(32, 2); break;
+        case 5: MAGACE_REST(16, 2); break;
+        default: MAGACE_REST(32, 0); break;
       }
 #undef MAGACE_REST
       if (ev_between) cudaEventRecord(ev_between, st);

@@ -20,7 +20,8 @@ constexpr int kMaxLaunches = 4;  // kernels of one evaluation
 constexpr int kAbasisVariants = 2;
 // warps per CTA of the split-precision density kernels, chosen by
 // DeviceModel::tune_rest / tune_b3 (ace_autotune_device picks them)
-constexpr int kRestWarpChoices[4] = {32, 16, 32, 16};  // (the last two read record streams)
+// (2/3: record streams broadcast by shuffles, 4/5: through shared memory)
+constexpr int kRestWarpChoices[6] = {32, 16, 32, 16, 32, 16};
 // (b3 variants 3: n0' loop outermost; 4 and 5: packed FP32x2 arithmetic)
 constexpr int kB3WarpChoices[6] = {16, 12, 8, 12, 16, 12};
 // CTAs per SM the split-precision force kernel's registers must allow, for

@@ -348,9 +348,11 @@ __device__ __forceinline__ void rest_run(const uint4* __restrict__ rec, int e0, 
 // NW warps per CTA (a divisor of kRestTableWarps): warp w walks the slots
 // the host schedule gave to warps w, w + NW, ... With STREAM the warp reads
 // its slots as one record stream, 32 records per coalesced load, and
-// broadcasts record q to every lane with warp shuffles, instead of one
-// warp-uniform load per entry.
-template <class D, int NW, bool STREAM>
+// broadcasts record q to every lane with warp shuffles (STREAM 1) or, 16
+// records at a time, through a per-warp shared-memory buffer read with one
+// uniform 16-byte load per record (STREAM 2), instead of one warp-uniform
+// global load per entry (STREAM 0).
+template <class D, int NW, int STREAM>
 __global__ void __launch_bounds__(NW * 32, 1)
     k_density_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
                  double* __restrict__ rho_rest) {
@@ -386,17 +388,35 @@ __global__ void __launch_bounds__(NW * 32, 1)
     __syncthreads();
     const int atom = lane < na ? s_atom[lane] : -1;
     double rloc = 0.0;
-    if constexpr (STREAM) {
+    if constexpr (STREAM > 0) {
       const uint4* srec = reinterpret_cast<const uint4*>(m.r_stream);
+      constexpr int CH = STREAM == 1 ? 32 : 16;  // records per load
+      uint4* rbuf = reinterpret_cast<uint4*>(rpart + NW * 32) + warp * 16;  // STREAM 2
       for (int sw = warp; sw < kRestTableWarps; sw += NW) {
         const int e0 = __ldg(m.r_stream_begin + sw), e1 = __ldg(m.r_stream_begin + sw + 1);
         float vx = 0.f, vy = 0.f;
-        for (int base = e0; base < e1; base += 32) {
-          const uint4 mine = base + lane < e1 ? __ldg(srec + base + lane) : make_uint4(0u, 0u, 0u, 0u);
-          const int n = min(32, e1 - base);
+        for (int base = e0; base < e1; base += CH) {
+          uint4 mine = make_uint4(0u, 0u, 0u, 0u);
+          if (lane < CH && base + lane < e1) mine = __ldg(srec + base + lane);
+          if constexpr (STREAM == 2) {
+            if (lane < 16) rbuf[lane] = mine;
+            __syncwarp();
+          }
+          const int n = min(CH, e1 - base);
           for (int q = 0; q < n; ++q) {
-            const unsigned rx = __shfl_sync(0xffffffffu, mine.x, q), ry = __shfl_sync(0xffffffffu, mine.y, q);
-            const unsigned rz = __shfl_sync(0xffffffffu, mine.z, q), rw = __shfl_sync(0xffffffffu, mine.w, q);
+            unsigned rx, ry, rz, rw;
+            if constexpr (STREAM == 2) {
+              const uint4 t = rbuf[q];
+              rx = t.x;
+              ry = t.y;
+              rz = t.z;
+              rw = t.w;
+            } else {
+              rx = __shfl_sync(0xffffffffu, mine.x, q);
+              ry = __shfl_sync(0xffffffffu, mine.y, q);
+              rz = __shfl_sync(0xffffffffu, mine.z, q);
+              rw = __shfl_sync(0xffffffffu, mine.w, q);
+            }
             if (rw & kRestEnd) {
               // end of a slot: density term and unscaled weight
               const int g0 = static_cast<int>(rz), w = static_cast<int>(ry);
@@ -418,6 +438,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
               vy += k * p.y;
             }
           }
+          if constexpr (STREAM == 2) __syncwarp();
         }
       }
     } else {
@@ -1219,7 +1240,9 @@ size_t abasis_fe_smem() {
   return sizeof(C<R>) * 64 * D::NRY + q * 64 + sizeof(R) * 64 * (D::NB + 1) + 64;
 }
 inline size_t density_fe_smem(const DeviceModel& m, int nw) {
-  return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * nw * 32;
+  // factors, per-warp density partials, per-warp 16-record buffers
+  return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * nw * 32 +
+         sizeof(uint4) * 16 * nw;
 }
 template <class D>
 size_t b3_fe_smem(const DeviceModel& m, int nw) {
