@@ -25,6 +25,15 @@ FE_LAYOUT = dict(nradbase_a=16, nradbase_m=16, nradial2_m=5, l2max_m=2,
                  nradial4_a=3, nradial4_m=3, l4max_a=0, l4max_m=0,
                  ndensity=1, npot=5, nfemb=1, radtype_a=3, radtype_m=7)
 
+# A second, smaller layout that exercises what FE_LAYOUT leaves out: two
+# densities with a non-linear embedding (nfemb 2), 4-body clusters with
+# l = l' = 1, other radial types, and radial counts that fit none of the
+# kernels specialised to FE_LAYOUT (so the generic kernels run).
+ALT_LAYOUT = dict(nradbase_a=8, nradbase_m=6, nradial2_m=3, l2max_m=2,
+                  nradial3_a=3, nradial3_m=2, l3max_a=2, l3max_m=1,
+                  nradial4_a=2, nradial4_m=2, l4max_a=1, l4max_m=1,
+                  ndensity=2, npot=5, nfemb=2, radtype_a=5, radtype_m=3)
+
 
 def header_lines(element: str, xc: str, smearing: float, lam=(5.25, 5.25), cut=(5.0, 4.0),
                  dcut=(0.01, 0.01), ecut=10000.0, decut=250.0, layout=FE_LAYOUT) -> list[str]:
@@ -49,9 +58,12 @@ def header_lines(element: str, xc: str, smearing: float, lam=(5.25, 5.25), cut=(
 
 def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, element: str = "Fe",
                            xc: str = "pbe", smearing: float = 0.2, layout=FE_LAYOUT,
-                           cut=(5.0, 4.0), core=(0.0, 0.0), par=(1.0, 1.0)) -> str:
+                           cut=(5.0, 4.0), core=(0.0, 0.0), par=(1.0, 1.0), par2=(1.0, 1.0)) -> str:
     """Writes the seeded potential to `path` and returns the path. Uses the
-    library's host-only init (no GPU) to enumerate the cluster basis."""
+    library's host-only init (no GPU) to enumerate the cluster basis. With
+    two densities, `par2` holds the second density's embedding parameters
+    and its cluster values come from a second generator (seed + 1), so the
+    first density's records do not depend on the layout's density count."""
     head = header_lines(element, xc, smearing, cut=cut, layout=layout)
     with tempfile.TemporaryDirectory() as td:
         tmp = os.path.join(td, "header.in")
@@ -64,6 +76,9 @@ def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, elem
     out = list(head)
     for k, v in ((1, par[0]), (2, par[1])):
         out += [f" par            {k}           1", f" {element}   {v!r}      F"]
+    if L["ndensity"] == 2:
+        for k, v in ((1, par2[0]), (2, par2[1])):
+            out += [f" par            {k}           2", f" {element}   {v!r}      F"]
     for k, v in ((1, core[0]), (2, core[1])):
         out += [f" core            {k}           0", f" {element} {element}   {v!r}      F"]
     for l in range(L["l3max_a"] + 1):
@@ -82,6 +97,14 @@ def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, elem
             idx = " ".join(str(int(x)) for x in row)
             out += [f" clu            {rank}           1",
                     f" {els}   {idx}   {rng.normal(0.0, sigma)!r}   T"]
+    if L["ndensity"] == 2:
+        rng2 = np.random.default_rng(seed + 1)
+        for rank in (1, 2, 3, 4):
+            els = " ".join([element] * rank)
+            for row in rows[rank]:
+                idx = " ".join(str(int(x)) for x in row)
+                out += [f" clu            {rank}           2",
+                        f" {els}   {idx}   {rng2.normal(0.0, sigma)!r}   T"]
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
     return path

@@ -43,6 +43,23 @@ def oracle_seeded(seeded_potential):
     return orc.Oracle(seeded_potential, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)
 
 
+@pytest.fixture(scope="session")
+def alt_potential(tmp_path_factory):
+    """A second seeded potential in a smaller layout with two densities, a
+    non-linear embedding and 4-body clusters with l = 1 (evaluated by the
+    generic kernels)."""
+    from magace import potential
+    path = str(tmp_path_factory.mktemp("alt") / "Fe.pbe.in")
+    potential.write_seeded_potential(path, seed=5, layout=potential.ALT_LAYOUT, par=(1.0, 0.5), par2=(0.7, 0.8))
+    return path
+
+
+@pytest.fixture(scope="session")
+def oracle_alt(alt_potential):
+    import oracle as orc
+    return orc.Oracle(alt_potential, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)
+
+
 def rel_err(a, b) -> float:
     """max |a-b| / max |b| (norm-relative, robust to components that vanish)."""
     a = np.asarray(a, dtype=np.float64)

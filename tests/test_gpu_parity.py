@@ -260,3 +260,64 @@ def test_autotuner_keeps_results(gpu_lib, oracle_seeded):
     eo, fo, to, t0o = oracle_seeded.acelib(nb)
     for got, ref in ((e, eo), (f, fo), (t, to), (t0, t0o)):
         assert rel_err(got, ref) < 1e-5
+
+
+# ---------------------------------------------------------------------------
+# A second layout: two densities with a non-linear embedding, 4-body clusters
+# with l = l' = 1, other radial types; evaluated by the generic kernels.
+
+
+@pytest.fixture()
+def alt_lib(alt_potential):
+    from magace import lib
+    lib.init(alt_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    lib.set_precision(0)
+    yield lib
+    lib.set_precision(0)
+
+
+@pytest.mark.parametrize("case", ["bcc128", "slab"])
+def test_second_layout_fp64_parity(alt_lib, oracle_alt, case):
+    from magace import structures as S
+    st = {"bcc128": lambda: S.bcc_fe_128(4), "slab": _ragged_slab}[case]()
+    _compare(alt_lib, oracle_alt, S.neighbor_data(st, 5.0))
+
+
+def test_second_layout_split_precision(alt_lib, oracle_alt):
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_54(6), 5.0)
+    alt_lib.set_precision(1)
+    e, f, t, t0 = alt_lib.acelib(nb)
+    eo, fo, to, t0o = oracle_alt.acelib(nb)
+    assert np.abs(e - eo).max() * 1e3 < 1.0
+    assert np.abs(f - fo).max() * 1e3 < 10.0
+    assert np.abs(t - to).max() * 1e3 < 10.0 and np.abs(t0 - t0o).max() * 1e3 < 10.0
+    for got, ref in ((e, eo), (f, fo), (t, to), (t0, t0o)):
+        assert rel_err(got, ref) < 1e-5
+
+
+def test_second_layout_descriptors_and_density_gradients(alt_lib, oracle_alt):
+    """Per-atom basis functions B and dE/drho of both densities through the
+    device API, against the oracle's prepB packs."""
+    import torch
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_54(8), 5.0)
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    arrs = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
+    ncoef, nd = alt_lib.num_coefficients()
+    assert nd == 2
+    B = torch.zeros(nb.natom, ncoef, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    alt_lib.descriptors_device(nb.natom, nb.nei, off.data_ptr(), *[a.data_ptr() for a in arrs], B.data_ptr(), 1)
+    outs = [torch.empty(n, dtype=torch.float64, device=dev) for n in (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)]
+    alt_lib.compute_device(nb.natom, nb.nei, off.data_ptr(), *[a.data_ptr() for a in arrs],
+                           *[o.data_ptr() for o in outs], 1)
+    dedrho = torch.empty(nb.natom, 2, dtype=torch.float64, device=dev)
+    alt_lib.density_gradient_device(nb.natom, dedrho.data_ptr(), 1)
+    torch.cuda.synchronize()
+    alt_lib.device_status()
+    Bo, dedrho_o = oracle_alt.descriptors(nb)
+    assert rel_err(B.cpu().numpy(), Bo) < 1e-10
+    assert rel_err(dedrho.cpu().numpy(), dedrho_o) < 1e-10

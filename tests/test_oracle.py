@@ -57,12 +57,15 @@ def _energy(orc, st, rcut):
     return e.sum(), nb, f, t, t0
 
 
-@pytest.mark.parametrize("which", ["fe", "seeded"])
-def test_finite_differences(which, oracle_fe, oracle_seeded):
+@pytest.mark.parametrize("which", ["fe", "seeded", "alt"])
+def test_finite_differences(which, request):
     """Forces and magnetic forces assembled as in lammps/pair_spin_ace.cpp
-    equal -dE/dx and -dE/dm from centred differences (h = 1e-5)."""
+    equal -dE/dx and -dE/dm from centred differences (h = 1e-5), for the
+    example Fe potential and both seeded layouts (the second one with two
+    densities and a non-linear embedding)."""
     from magace import structures as S
-    orc, rc = (oracle_fe, 4.5) if which == "fe" else (oracle_seeded, 5.0)
+    orc = request.getfixturevalue({"fe": "oracle_fe", "seeded": "oracle_seeded", "alt": "oracle_alt"}[which])
+    rc = 4.5 if which == "fe" else 5.0
     rng = np.random.default_rng(3)
     pos, cell = S.bcc_cubic(2, 2, 2, 2.83)
     pos = pos + rng.normal(0, 0.08, pos.shape)
