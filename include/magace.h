@@ -188,12 +188,20 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
                         int* force_blocks);
 
 /* The kernel variants in use, variants[4]: A basis (0 scalar, 1 packed
- * FP32x2), 2-/4-body density (0/1: 32/16 warps with per-entry loads, 2/3:
+ * FP32x2, 2/3 the same with the bond tiles staged into shared memory by TMA
+ * bulk copies on a persistent grid; 2/3 run only when the bond arrays are
+ * device memory and otherwise fall back to 0/1), 2-/4-body density (0/1: 32/16 warps with per-entry loads, 2/3:
  * 32/16 warps reading record streams by shuffles, 4/5: through shared
  * memory), 3-body (0-2: 16/12/8 warps, 3: 12
  * warps with the n0' loop outermost, 4/5: 16/12 warps packed FP32x2), forces
  * (0-2: 4/6/8 CTAs per SM, 3-5: the same packed FP32x2). */
 int ace_get_tuning(int* variants);
+
+/* Selects the kernel variants directly (no counterpart in the reference):
+ * variants[4] as ace_get_tuning reports them; an index out of a kernel's
+ * range is an error (MAGACE_ERR_ARGS). Results do not change beyond the FP32
+ * rounding order of the 3-body kernel. */
+int ace_set_tuning(const int* variants);
 
 /* ---- Differentiation and fitting (no counterpart in the reference's
  * acelib_; they expose what src/forces.F90:976-1289 computes internally). ----

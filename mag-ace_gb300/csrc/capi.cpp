@@ -4,9 +4,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <limits>
 #include <string>
 #include <vector>
@@ -409,6 +411,7 @@ int device_error_to_status(int dev) {
     case kDevSmallR: return set_error(MAGACE_ERR_SMALL_R, "encountered a very small distance");
     case kDevMoment: return set_error(MAGACE_ERR_MOMENT, "moment magnitude negative, NaN or beyond the magnetic cutoff");
     case kDevNaN: return set_error(MAGACE_ERR_NAN, "non-finite density");
+    case kDevTimeout: return set_error(MAGACE_ERR_CUDA, "a bulk copy of bond inputs did not complete");
     default: return set_error(MAGACE_ERR_ARGS, "inconsistent bond tile");
   }
 }
@@ -645,6 +648,22 @@ int ace_table_stats(long long* out) {
   return MAGACE_OK;
 }
 
+// True when every non-null pointer is device memory, 8-byte aligned: the
+// bond arrays the TMA-staged A-basis variants read with bulk copies.
+static bool device_resident(std::initializer_list<const void*> ptrs) {
+  for (const void* p : ptrs) {
+    if (!p) continue;
+    if (reinterpret_cast<uintptr_t>(p) & 7u) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (a.type != cudaMemoryTypeDevice) return false;
+  }
+  return true;
+}
+
 int ace_compute_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
                        const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
                        double* energy, double* fij, double* tij, double* ti0, void* stream) {
@@ -668,6 +687,7 @@ int ace_compute_device(int natom, int nei, const int* bond_offset, const double*
   b.fij = fij;
   b.tij = tij;
   b.ti0 = ti0;
+  b.dev_inputs = device_resident({r, e, mag_j, mhat_j});
   return run_eval(b, stream ? static_cast<cudaStream_t>(stream) : R.stream);
 }
 
@@ -704,6 +724,7 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
   b.fij = R.fij.p;
   b.tij = R.tij.p;
   b.ti0 = R.ti0.p;
+  b.dev_inputs = device_resident({r, e, mag_j, mhat_j});
   // variant v of every kernel at once (each kernel's own choice list,
   // clamped), warmed up, then timed kernel by kernel; each kernel keeps its
   // fastest variant
@@ -755,6 +776,21 @@ int ace_get_tuning(int* variants) {
   variants[1] = R.tune_rest;
   variants[2] = R.tune_b3;
   variants[3] = R.tune_forces;
+  return set_error(MAGACE_OK, "");
+}
+
+int ace_set_tuning(const int* variants) {
+  Runtime& R = rt();
+  const int count[4] = {kAbasisVariants, static_cast<int>(sizeof(kRestWarpChoices) / sizeof(int)),
+                        static_cast<int>(sizeof(kB3WarpChoices) / sizeof(int)),
+                        static_cast<int>(sizeof(kForceMinBlocksChoices) / sizeof(int))};
+  if (!variants) return set_error(MAGACE_ERR_ARGS, "null variants");
+  for (int k = 0; k < 4; ++k)
+    if (variants[k] < 0 || variants[k] >= count[k]) return set_error(MAGACE_ERR_ARGS, "kernel variant out of range");
+  R.tune_abasis = R.dm.tune_abasis = variants[0];
+  R.tune_rest = R.dm.tune_rest = variants[1];
+  R.tune_b3 = R.dm.tune_b3 = variants[2];
+  R.tune_forces = R.dm.tune_forces = variants[3];
   return set_error(MAGACE_OK, "");
 }
 
@@ -999,6 +1035,7 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
     b.e = R.e.p;
     b.magj = R.magj.p;
     b.mhj = R.mhj.p;
+    b.dev_inputs = true;  // the library's own device buffers
     b.magi = R.magi.p;
     b.mhi = R.mhi.p;
     b.energy = R.energy.p;

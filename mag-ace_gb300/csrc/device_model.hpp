@@ -24,6 +24,7 @@ enum DeviceError : int {
   kDevMoment = 2,  // |m| negative, NaN or beyond the magnetic cutoff
   kDevNaN = 3,     // non-finite density
   kDevShape = 4,   // more bonds than a tile index can address
+  kDevTimeout = 5, // a bulk copy of bond inputs did not complete within the wait limit
 };
 
 // one gather table: group g has arity grp_arity[g], length grp_len[g] and its

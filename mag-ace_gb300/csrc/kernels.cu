@@ -968,27 +968,60 @@ void set_smem(K* kernel, size_t bytes) {
   }
 }
 
+// Resident CTAs of `kernel` on this device (a persistent grid), computed
+// once per kernel and device so that captured evaluations make no query.
+template <class K>
+int resident_grid(K* kernel, int threads, size_t smem_bytes) {
+  static std::map<std::pair<const void*, int>, int> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int& g = done[{reinterpret_cast<const void*>(kernel), dev}];
+  if (g == 0) {
+    int per_sm = 0, nsm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem_bytes);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    g = (per_sm > 0 ? per_sm : 1) * (nsm > 0 ? nsm : 1);
+  }
+  return g;
+}
+
 // The A-basis phase: factors F, rank-1 density and core energy per atom.
+// Split-precision variants (DeviceModel::tune_abasis): 0 scalar, 1 packed
+// FP32x2, 2 and 3 the same with the bond tiles staged by TMA on a persistent
+// grid; 2 and 3 run only when the bond inputs are device memory
+// (EvalBuffers::dev_inputs), else they fall back to 0 and 1.
 template <class R>
 void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid, bool fe) {
   const int natom = b.natom;
   if (fe) {
     const size_t s1 = abasis_fe_smem<R, FeDims>();
-    bool packed = false;
-    if constexpr (sizeof(R) == 4) packed = m.tune_abasis == 1;
-    if (packed) {
-      if constexpr (sizeof(R) == 4) {
-        set_smem(k_abasis_fe<R, FeDims, true>, s1);
-        k_abasis_fe<R, FeDims, true><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                           reinterpret_cast<C<R>*>(b.F), b.rho1, b.core,
-                                                           static_cast<R*>(b.stage), b.err);
+    int v = 0;
+    if constexpr (sizeof(R) == 4) v = m.tune_abasis;
+    if (v >= 2 && !b.dev_inputs) v -= 2;
+#define MAGACE_ABASIS(PK, TMA)                                                                                     \
+  {                                                                                                                 \
+    const size_t sm = TMA ? ((s1 + 15) & ~static_cast<size_t>(15)) + kTileBytes : s1;                              \
+    set_smem(k_abasis_fe<R, FeDims, PK, TMA>, sm);                                                                 \
+    int g = grid;                                                                                                   \
+    if (TMA) {                                                                                                      \
+      const int rg = resident_grid(k_abasis_fe<R, FeDims, PK, TMA>, 64, sm);                                        \
+      g = natom < rg ? natom : rg;                                                                                  \
+    }                                                                                                               \
+    k_abasis_fe<R, FeDims, PK, TMA><<<g, 64, sm, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,     \
+                                                       reinterpret_cast<C<R>*>(b.F), b.rho1, b.core,               \
+                                                       static_cast<R*>(b.stage), b.err);                            \
+  }
+    if constexpr (sizeof(R) == 4) {
+      switch (v) {
+        case 1: MAGACE_ABASIS(true, false); break;
+        case 2: MAGACE_ABASIS(false, true); break;
+        case 3: MAGACE_ABASIS(true, true); break;
+        default: MAGACE_ABASIS(false, false); break;
       }
     } else {
-      set_smem(k_abasis_fe<R, FeDims, false>, s1);
-      k_abasis_fe<R, FeDims, false><<<grid, 64, s1, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,
-                                                          reinterpret_cast<C<R>*>(b.F), b.rho1, b.core,
-                                                          static_cast<R*>(b.stage), b.err);
+      MAGACE_ABASIS(false, false);
     }
+#undef MAGACE_ABASIS
   } else {
     const size_t s1 = abasis_smem<R>(m);
     set_smem(k_abasis<R>, s1);

@@ -15,9 +15,9 @@ constexpr int kDensityThreads = 256;
 constexpr int kForceThreads = 64;
 constexpr int kMaxFeat = 32;     // per-bond radial functions of one kind
 constexpr int kMaxLaunches = 4;  // kernels of one evaluation
-// variants of the split-precision A-basis kernel: scalar, packed FP32x2
-// (DeviceModel::tune_abasis)
-constexpr int kAbasisVariants = 2;
+// variants of the split-precision A-basis kernel: scalar, packed FP32x2,
+// and both with TMA-staged bond tiles (DeviceModel::tune_abasis)
+constexpr int kAbasisVariants = 4;
 // warps per CTA of the split-precision density kernels, chosen by
 // DeviceModel::tune_rest / tune_b3 (ace_autotune_device picks them)
 // (2/3: record streams broadcast by shuffles, 4/5: through shared memory)
@@ -53,6 +53,7 @@ struct EvalBuffers {
   void* aux = nullptr;        // [eval_aux_bytes] scratch of the specialised split-precision kernels
   const int* order = nullptr; // [natom] work queue (atoms by decreasing bond count) or null
   void* stage = nullptr;      // [nei][8] bond inputs in the working precision (specialised kernels), or null
+  bool dev_inputs = false;    // r, e, magj, mhj are device memory (bulk copies may read them)
 };
 
 // Work queue of one evaluation: the atoms sorted by decreasing bond count

@@ -46,12 +46,131 @@ bool dims_match(const DeviceModel& m) {
 __host__ __device__ constexpr int l_of_h(int h) { return h == 0 ? 0 : (h < 3 ? 1 : (h < 6 ? 2 : (h < 10 ? 3 : 4))); }
 __host__ __device__ constexpr int l_of_lm(int lm) { return lm == 0 ? 0 : (lm < 4 ? 1 : (lm < 9 ? 2 : (lm < 16 ? 3 : 4))); }
 
+// dynamic shared memory of k_abasis_fe without the staged tile
+template <class R, class D>
+__host__ __device__ constexpr size_t abasis_fe_smem() {
+  // sQ holds NQ complex or, packed, 2 x 32 floats per bond
+  const size_t q = sizeof(C<R>) * D::NQ > sizeof(float) * 64 ? sizeof(C<R>) * D::NQ : sizeof(float) * 64;
+  return sizeof(C<R>) * 64 * D::NRY + q * 64 + sizeof(R) * 64 * (D::NB + 1) + 64;
+}
+
+// ===========================================================================
+// Bond tiles staged by the Tensor Memory Accelerator. One thread issues, per
+// input array, a bulk copy (cp.async.bulk) of a tile's bond segment into
+// shared memory; the copies signal one mbarrier with their byte count and
+// the CTA waits on its phase. A bulk copy needs 16-byte aligned addresses
+// and a multiple of 16 bytes, and the caller's arrays are only 8-byte
+// aligned, so each copy covers the 16-byte aligned interior of the segment
+// and the at most two FP64 elements outside it are read from global memory
+// by the threads that use them. An element g of the segment [e0, e1) sits
+// at shared index g - e0 + h (h = 1 when element e0 starts 8 bytes past a
+// 16-byte boundary), which keeps the interior's start 16-byte aligned.
+// Every wait is bounded: after ~2^32 SM cycles it returns false and the
+// kernel reports kDevTimeout instead of hanging.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const long long end = clock64() + (1ll << 32);
+  while (!mbar_test(bar, parity))
+    if (clock64() > end) return false;
+  return true;
+}
+
+// the part of the segment [e0, e1) of array g that one bulk copy moves
+struct TileWindow {
+  int lo, hi, h;
+};
+__device__ __forceinline__ TileWindow tile_window(const double* g, int e0, int e1) {
+  TileWindow w;
+  w.h = (reinterpret_cast<uintptr_t>(g + e0) & 8u) ? 1 : 0;
+  w.lo = e0 + w.h;
+  w.hi = e1 - ((reinterpret_cast<uintptr_t>(g + e1) & 8u) ? 1 : 0);
+  if (w.hi < w.lo) w.hi = w.lo;
+  return w;
+}
+__device__ __forceinline__ double tile_value(const double* sbuf, const double* g, const TileWindow& w, int e0, int idx) {
+  return (idx >= w.lo && idx < w.hi) ? sbuf[idx - e0 + w.h] : g[idx];
+}
+
+// shared-memory layout of one staged tile of up to 64 bonds: r, e[3], |m|,
+// m-hat[3] as FP64, each array padded to keep the next one 16-byte aligned
+constexpr int kTileR = 66, kTileE = 194;
+constexpr int kTileDoubles = 2 * kTileR + 2 * kTileE;
+constexpr size_t kTileBytes = sizeof(double) * kTileDoubles + 16;  // + the mbarrier and the tile's first bond
+
+struct BondTile {
+  double* r;
+  double* e;
+  double* mg;
+  double* mh;
+  uint64_t* bar;
+  int* first;
+  __device__ explicit BondTile(unsigned char* p)
+      : r(reinterpret_cast<double*>(p)), e(r + kTileR), mg(e + kTileE), mh(mg + kTileR),
+        bar(reinterpret_cast<uint64_t*>(mh + kTileE)), first(reinterpret_cast<int*>(bar + 1)) {}
+  // issues the copies of bonds [j0, j0 + nb) (one thread)
+  __device__ void issue(const double* rr, const double* ee, const double* magj, const double* mhj, int j0, int nb) {
+    const TileWindow w0 = tile_window(rr, j0, j0 + nb), w1 = tile_window(ee, 3 * j0, 3 * (j0 + nb)),
+                     w2 = tile_window(magj, j0, j0 + nb), w3 = tile_window(mhj, 3 * j0, 3 * (j0 + nb));
+    const uint32_t b0 = 8u * (w0.hi - w0.lo), b1 = 8u * (w1.hi - w1.lo), b2 = 8u * (w2.hi - w2.lo),
+                   b3 = 8u * (w3.hi - w3.lo);
+    *first = j0;
+    mbar_expect_tx(bar, b0 + b1 + b2 + b3);
+    if (b0) bulk_to_smem(r + 2 * w0.h, rr + w0.lo, b0, bar);
+    if (b1) bulk_to_smem(e + 2 * w1.h, ee + w1.lo, b1, bar);
+    if (b2) bulk_to_smem(mg + 2 * w2.h, magj + w2.lo, b2, bar);
+    if (b3) bulk_to_smem(mh + 2 * w3.h, mhj + w3.lo, b3, bar);
+  }
+};
+
+// the first tile of the first atom with bonds at queue position it, it +
+// gridDim.x, ...: (j0, nb), nb = 0 when there is none
+__device__ __forceinline__ int2 next_atom_tile(const DeviceModel& m, const int* __restrict__ off, int it, int natom,
+                                               int tb) {
+  for (; it < natom; it += gridDim.x) {
+    const int a = queue_atom(m, it);
+    const int c0 = off[a], c1 = off[a + 1];
+    if (c1 > c0) return make_int2(c0, c1 - c0 < tb ? c1 - c0 : tb);
+  }
+  return make_int2(0, 0);
+}
+
 // ===========================================================================
 // PACKED (split precision only): the M Y tile is stored as real and
 // imaginary planes of 32 columns, and the lanes accumulate column pairs with
 // packed FP32x2 FMAs (warp 0: five pairs of the 18 A columns per half-row,
 // warp 1: eight pairs of the 30 A2 columns; padding pairs are discarded).
-template <class R, class D, bool PACKED>
+//
+// TMA (device-resident inputs only): a persistent grid, each CTA's bond
+// tiles staged into shared memory by bulk copies (BondTile); the copy of the
+// next tile is issued as soon as the current tile's features are computed,
+// so that it overlaps the bond sums and the completion of A.
+template <class R, class D, bool PACKED, bool TMA = false>
 __global__ void __launch_bounds__(64)
     k_abasis_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
@@ -73,6 +192,20 @@ __global__ void __launch_bounds__(64)
   static_assert(!PACKED || (sizeof(R) == 4 && D::H3 == D::H2 && D::NQ <= 32), "packed tiles: FP32, Fe layout");
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int row = lane >> 1, cb = lane & 1;
+  // TMA: the staged tile after the other buffers (16-byte aligned)
+  BondTile tile(smem + ((abasis_fe_smem<R, D>() + 15) & ~static_cast<size_t>(15)));
+  constexpr int kIssuer = 32;  // lane 0 of warp 1 issues the copies
+  uint32_t phase = 0;
+  bool timed_out = false;
+  uint32_t timeout_parity = 0;
+  if constexpr (TMA) {
+    if (t == kIssuer) {
+      mbar_init(tile.bar, 1);
+      const int2 first = next_atom_tile(m, off, blockIdx.x, natom, TB);
+      if (first.y > 0) tile.issue(rr, ee, magj, mhj, first.x, first.y);
+    }
+    __syncthreads();
+  }
 
   for (int it = blockIdx.x; it < natom; it += gridDim.x) {
     const int atom = queue_atom(m, it);
@@ -87,14 +220,46 @@ __global__ void __launch_bounds__(64)
     for (int t0 = b0; t0 < b1; t0 += TB) {
       const int nb = min(TB, b1 - t0);
       __syncthreads();
+      if constexpr (TMA) {
+        if (!mbar_wait(tile.bar, phase)) {
+          raise_error(err, kDevTimeout);
+          timed_out = true;
+          timeout_parity = phase;
+        }
+        phase ^= 1u;
+      }
       if (t < nb) {
         const int j = t0 + t;
         // the bond's inputs in the working precision; with `stage`, also
         // kept in device memory for the force kernel (8 values per bond)
-        const R br = to_r<R>(rr[j]);
-        const R bex = to_r<R>(ee[3 * j]), bey = to_r<R>(ee[3 * j + 1]), bez = to_r<R>(ee[3 * j + 2]);
-        const R bmg = to_r<R>(magj[j]);
-        const R bmx = to_r<R>(mhj[3 * j]), bmy = to_r<R>(mhj[3 * j + 1]), bmz = to_r<R>(mhj[3 * j + 2]);
+        double dr, dex, dey, dez, dmg, dmx, dmy, dmz;
+        if constexpr (TMA) {
+          if (*tile.first != t0) raise_error(err, kDevShape);  // the staged tile is always this one
+          const int e0 = 3 * t0, e1 = 3 * (t0 + nb);
+          const TileWindow w0 = tile_window(rr, t0, t0 + nb), w1 = tile_window(ee, e0, e1),
+                           w2 = tile_window(magj, t0, t0 + nb), w3 = tile_window(mhj, e0, e1);
+          dr = tile_value(tile.r, rr, w0, t0, j);
+          dex = tile_value(tile.e, ee, w1, e0, 3 * j);
+          dey = tile_value(tile.e, ee, w1, e0, 3 * j + 1);
+          dez = tile_value(tile.e, ee, w1, e0, 3 * j + 2);
+          dmg = tile_value(tile.mg, magj, w2, t0, j);
+          dmx = tile_value(tile.mh, mhj, w3, e0, 3 * j);
+          dmy = tile_value(tile.mh, mhj, w3, e0, 3 * j + 1);
+          dmz = tile_value(tile.mh, mhj, w3, e0, 3 * j + 2);
+        } else {
+          dr = rr[j];
+          dex = ee[3 * j];
+          dey = ee[3 * j + 1];
+          dez = ee[3 * j + 2];
+          dmg = magj[j];
+          dmx = mhj[3 * j];
+          dmy = mhj[3 * j + 1];
+          dmz = mhj[3 * j + 2];
+        }
+        const R br = to_r<R>(dr);
+        const R bex = to_r<R>(dex), bey = to_r<R>(dey), bez = to_r<R>(dez);
+        const R bmg = to_r<R>(dmg);
+        const R bmx = to_r<R>(dmx), bmy = to_r<R>(dmy), bmz = to_r<R>(dmz);
         if (stage) {
           R* sp = stage + 8 * static_cast<size_t>(j);
           sp[0] = br;
@@ -158,6 +323,15 @@ __global__ void __launch_bounds__(64)
         score[t] = cv[0];
       }
       __syncthreads();
+      if constexpr (TMA) {
+        // the tile's inputs are in registers: stage the next tile
+        if (t == kIssuer) {
+          int2 nx;
+          if (t0 + TB < b1) nx = make_int2(t0 + TB, min(TB, b1 - t0 - TB));
+          else nx = next_atom_tile(m, off, it + gridDim.x, natom, TB);
+          if (nx.y > 0) tile.issue(rr, ee, magj, mhj, nx.x, nx.y);
+        }
+      }
       if constexpr (PACKED) {
         if (warp == 0) {
           // A[row][10cb .. 10cb+9] (columns 18, 19 padding)
@@ -300,6 +474,9 @@ __global__ void __launch_bounds__(64)
       core_out[atom] = core_sum.value();
     }
     __syncthreads();
+  }
+  if constexpr (TMA) {
+    if (timed_out) mbar_wait(tile.bar, timeout_parity);  // a copy still in flight: wait once more, bounded
   }
 }
 
@@ -1233,12 +1410,6 @@ __global__ void __launch_bounds__(64, MINB)
   }
 }
 
-template <class R, class D>
-size_t abasis_fe_smem() {
-  // sQ holds NQ complex or, packed, 2 x 32 floats per bond
-  const size_t q = sizeof(C<R>) * D::NQ > sizeof(float) * 64 ? sizeof(C<R>) * D::NQ : sizeof(float) * 64;
-  return sizeof(C<R>) * 64 * D::NRY + q * 64 + sizeof(R) * 64 * (D::NB + 1) + 64;
-}
 inline size_t density_fe_smem(const DeviceModel& m, int nw) {
   // factors, per-warp density partials, per-warp 16-record buffers
   return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * nw * 32 +

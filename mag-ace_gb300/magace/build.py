@@ -26,7 +26,7 @@ SOURCES = ["potential.cpp", "model.cpp", "capi.cpp", "kernels.cu", "noalloc.cu",
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
-    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".hpp", ".cuh"))]
+    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".hpp", ".cuh", ".inl"))]
     deps.append(os.path.join(INCLUDE, "magace.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj

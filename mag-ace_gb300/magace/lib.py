@@ -50,6 +50,7 @@ SIGNATURES = {
     "ace_num_coefficients": (_i, [_pi, _pi]),
     "ace_set_work_queue": (_i, [_i]),
     "ace_get_tuning": (_i, [_pi]),
+    "ace_set_tuning": (_i, [_pi]),
     "ace_autotune_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _pi, _pi, _pi]),
     "ace_md_create": (_i, [_i, _pd, _pd, _pd, _pd, _pi, _d, _d, _d, _pi]),
     "ace_md_run": (_i, [_i, _i, _d, _i, _i, _pd]),
@@ -169,7 +170,7 @@ def autotune_device(natom, nei, off, r, e, magj, mhj, magi, mhi, stream=0) -> tu
 
 
 TUNING_NAMES = {
-    "abasis": ["scalar", "packed FP32x2"],
+    "abasis": ["scalar", "packed FP32x2", "scalar, TMA-staged bond tiles", "packed FP32x2, TMA-staged bond tiles"],
     "density": ["32 warps", "16 warps", "32 warps, record streams", "16 warps, record streams",
                 "32 warps, record streams via shared memory", "16 warps, record streams via shared memory"],
     "b3": ["16 warps", "12 warps", "8 warps", "12 warps, n0' outermost", "16 warps, packed FP32x2",
@@ -184,6 +185,19 @@ def get_tuning() -> dict:
     v = np.zeros(4, np.int32)
     _check(load().ace_get_tuning(_ip(v)))
     return {k: TUNING_NAMES[k][int(i)] for k, i in zip(("abasis", "density", "b3", "forces"), v)}
+
+
+def get_tuning_indices() -> list:
+    """The variant indices in use: [A basis, density, 3-body, forces]."""
+    v = np.zeros(4, np.int32)
+    _check(load().ace_get_tuning(_ip(v)))
+    return [int(x) for x in v]
+
+
+def set_tuning(variants) -> None:
+    """Selects the variant indices [A basis, density, 3-body, forces]."""
+    v = np.ascontiguousarray(np.asarray(variants, dtype=np.int32).reshape(4))
+    _check(load().ace_set_tuning(_ip(v)))
 
 
 def num_coefficients() -> tuple:

@@ -321,3 +321,58 @@ def test_second_layout_descriptors_and_density_gradients(alt_lib, oracle_alt):
     Bo, dedrho_o = oracle_alt.descriptors(nb)
     assert rel_err(B.cpu().numpy(), Bo) < 1e-10
     assert rel_err(dedrho.cpu().numpy(), dedrho_o) < 1e-10
+
+
+def _device_eval(lib, nb, shift=0):
+    """Split evaluation through ace_compute_device on device arrays; with
+    shift = 1 every bond array starts 8 bytes past its allocation's start."""
+    import torch
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+
+    def T(a):
+        buf = torch.zeros(len(a) + shift, dtype=torch.float64, device=dev)
+        buf[shift:] = torch.tensor(a, dtype=torch.float64, device=dev)
+        return buf[shift:]
+    ins = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
+    outs = [torch.empty(n, dtype=torch.float64, device=dev) for n in (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)]
+    torch.cuda.synchronize()
+    lib.compute_device(nb.natom, nb.nei, off.data_ptr(), *[x.data_ptr() for x in ins], *[o.data_ptr() for o in outs], 1)
+    torch.cuda.synchronize()
+    lib.device_status()
+    return [o.cpu().numpy() for o in outs]
+
+
+@pytest.mark.parametrize("shift", [0, 1])
+def test_abasis_variants_on_device_inputs(gpu_lib, oracle_seeded, shift):
+    """Every A-basis variant on device-resident bond arrays, the TMA-staged
+    ones included: arrays that start on and 8 bytes past a 16-byte boundary,
+    atoms of two 64-bond tiles (neighbours listed out to 8.4 A,
+    beyond the cutoff) and an atom without neighbours. Split results stay
+    within the split tolerance of the oracle and within 1e-6 of the scalar
+    variant."""
+    from magace import structures as S
+    st = _ragged_slab()
+    st = S.Structure(np.vstack([st.positions, [[1.0, 1.0, 90.0]]]), st.cell, st.pbc, np.append(st.mag, 2.0),
+                     np.vstack([st.mhat, [[0.0, 0.0, 1.0]]]))
+    nb = S.neighbor_data(st, 8.4)
+    counts = nb.nstop - nb.nstart + 1
+    assert counts.max() > 64 and counts.min() == 0
+    gpu_lib.set_precision(1)
+    try:
+        res = []
+        for v in range(4):
+            gpu_lib.set_tuning([v, 0, 0, 0])
+            res.append(_device_eval(gpu_lib, nb, shift))
+    finally:
+        gpu_lib.set_tuning([0, 0, 0, 0])
+        gpu_lib.set_precision(0)
+    eo, fo, to, t0o = oracle_seeded.acelib(nb)
+    for got in res:
+        e, f, t, t0 = got
+        assert np.abs(e - eo).max() * 1e3 < 1.0 and np.abs(f - fo).max() * 1e3 < 10.0
+        for x, y in zip(got, (eo, fo, to, t0o)):
+            assert rel_err(x, y) < 1e-5
+        for x, y in zip(got, res[0]):
+            assert rel_err(x, y) < 1e-6
+

@@ -91,6 +91,17 @@ def test_error_codes(lib, tmp_path, seeded_potential):
         lib.init(str(p5))
     assert e.value.code == 3
     assert lib.load().ace_error_string(4).decode().startswith("bond shorter")
+    # kernel variants: indices outside a kernel's range are refused, valid ones kept
+    before = lib.get_tuning_indices()
+    for bad in ([4, 0, 0, 0], [0, 6, 0, 0], [0, 0, -1, 0], [0, 0, 0, 6]):
+        with pytest.raises(MagAceError) as e:
+            lib.set_tuning(bad)
+        assert e.value.code == 7
+    assert lib.get_tuning_indices() == before
+    lib.set_tuning([3, 5, 5, 5])
+    assert lib.get_tuning_indices() == [3, 5, 5, 5]
+    assert lib.get_tuning()["abasis"] == "packed FP32x2, TMA-staged bond tiles"
+    lib.set_tuning(before)
 
 
 def test_acelibini_reads_working_directory(lib, tmp_path, seeded_potential, monkeypatch):
