@@ -85,6 +85,10 @@ __device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_
                "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
 }
+// a bulk prefetch of [src, src + bytes) into L2 (16-byte aligned, 16-byte multiple)
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
@@ -923,8 +927,18 @@ __global__ void __launch_bounds__(NW * 32, 1)
   int* s_fac = reinterpret_cast<int*>(s_mult + nc);                // [nc]
   int* s_cw = s_fac + nc;                                          // [nW]
   __shared__ int s_atom[32];                                       // the block's atoms
+  __shared__ int s_next;                                           // next task to take
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (natom + 31) / 32;
+  // bulk L2 prefetch of the rows of atom slot `a` of block `b` (whole
+  // 16-byte units inside the row, so that nothing past the array is touched)
+  const auto prefetch_rows = [&](const void* base, size_t row_bytes, int b, int a) {
+    if (b * 32 + a >= natom) return;
+    const int atom = queue_atom(m, b * 32 + a);
+    const uintptr_t p0 = reinterpret_cast<uintptr_t>(base) + row_bytes * static_cast<size_t>(atom);
+    const uintptr_t lo = (p0 + 15) & ~static_cast<uintptr_t>(15), hi = (p0 + row_bytes) & ~static_cast<uintptr_t>(15);
+    if (hi > lo) bulk_prefetch_l2(reinterpret_cast<const void*>(lo), static_cast<uint32_t>(hi - lo));
+  };
 
   for (int t = threadIdx.x; t < ncoef / 4; t += blockDim.x)
     reinterpret_cast<float4*>(Cs)[t] = __ldg(reinterpret_cast<const float4*>(m.b3_Cf) + t);
@@ -938,6 +952,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
     const int a0 = blk * 32;
     const int na = min(32, natom - a0);
     if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
+    if (threadIdx.x == 0) s_next = NW;
     __syncthreads();
     // stage: thread c takes element c of every atom, kBatch atoms in flight
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
@@ -955,9 +970,17 @@ __global__ void __launch_bounds__(NW * 32, 1)
       }
     }
     __syncthreads();
+    // while the tasks run: this block's weights (read by the final phase)
+    // and the factors of this CTA's next block, if any, into L2
+    if (warp == NW - 1) {
+      prefetch_rows(W, sizeof(C<float>) * nW, blk, lane);
+      prefetch_rows(F, sizeof(C<float>) * m.nF, blk + gridDim.x, lane);
+    }
     double rloc = 0.0;
+    // tasks from a shared counter (dynamic balance between the warps)
+    int tk = warp;
 #pragma unroll 1
-    for (int tk = warp; tk < m.b3_ntask; tk += NW) {
+    while (tk < m.b3_ntask) {
       const int k = __ldg(m.b3_combo + tk);
       const int pat = __ldg(m.b3_pattern + k);
       const float cf = __ldg(m.b3_cff + tk);
@@ -979,6 +1002,9 @@ __global__ void __launch_bounds__(NW * 32, 1)
         else r = b3_task_po<2, D>(Ck, Xs, Gs, code, code2, cf, lane);
       }
       rloc += f2d(__ldg(m.b3_cfw + tk) * r);
+      int nx = 0;
+      if (lane == 0) nx = atomicAdd(&s_next, 1);
+      tk = __shfl_sync(0xffffffffu, nx, 0);
     }
     rpart[warp * 32 + lane] = rloc;
     __syncthreads();

@@ -771,8 +771,9 @@ void build_dense_b3(Model& M) {
         }
     }
   }
-  // tasks grouped by pattern (stable): warps that take consecutive tasks then
-  // run the same unrolled code at the same time
+  // tasks grouped by pattern (stable): warps that take consecutive tasks
+  // from the kernel's shared task counter then run the same unrolled code at
+  // the same time (a longest-pattern-first order measured ~2 % slower)
   const int npos = NM + 2 * I;
   std::vector<int> order(D.ntask);
   for (int t = 0; t < D.ntask; ++t) order[t] = t;
