@@ -20,6 +20,7 @@
 // per-atom density, energy and output sums stay in double).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdlib>
 #include <map>
@@ -968,6 +969,55 @@ void set_smem(K* kernel, size_t bytes) {
   }
 }
 
+// Multiprocessors of the current device (queried once per device).
+int sm_count() {
+  static std::map<int, int> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int& n = done[dev];
+  if (n == 0) {
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+// How k_b3_fe splits the last, partial wave of its 32-atom blocks (one CTA
+// per SM): with every block on its own CTA, the blocks beyond the last whole
+// wave are each divided among `parts` CTAs (2 to 8, as many as the idle SMs
+// allow), unless that wave is more than half full.
+struct B3Split {
+  int nfull, ntail, parts;
+};
+B3Split b3_split(int nblk, int grid_cap) {
+  B3Split s{nblk, 0, 1};
+  if (nblk > grid_cap) return s;
+  const int nsm = sm_count();
+  const int nfull = nblk / nsm * nsm, ntail = nblk - nfull;
+  const int parts = ntail > 0 ? std::min(8, nsm / ntail) : 1;
+  if (parts >= 2) s = {nfull, ntail, parts};
+  return s;
+}
+
+// The split-precision scratch (EvalBuffers::aux): rho_rest[natom] doubles,
+// then the 3-body split tail's accumulators for up to min(blocks, SMs) tail
+// blocks: rho3[tail][32] doubles, tickets[tail] ints, g[tail][nc][32][2]
+// floats (each part 256-byte aligned).
+struct AuxLayout {
+  size_t rho3, tickets, gacc, end;
+};
+AuxLayout aux_layout(const DeviceModel& m, int natom) {
+  const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
+  const int nblk = (natom + 31) / 32;
+  const size_t ntail = static_cast<size_t>(std::min(nblk, sm_count()));
+  AuxLayout L;
+  L.rho3 = up(sizeof(double) * static_cast<size_t>(natom));
+  L.tickets = L.rho3 + up(sizeof(double) * 32 * ntail);
+  L.gacc = L.tickets + up(sizeof(int) * ntail);
+  L.end = L.gacc + up(sizeof(float) * 64 * static_cast<size_t>(m.b3_nc) * ntail);
+  return L;
+}
+
 // Resident CTAs of `kernel` on this device (a persistent grid), computed
 // once per kernel and device so that captured evaluations make no query.
 template <class K>
@@ -1064,10 +1114,19 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
 #undef MAGACE_REST
       if (ev_between) cudaEventRecord(ev_between, st);
       const size_t sb = b3_fe_smem<FeDims>(m, bw);
+      // the last partial wave split by task range (B3Split); its
+      // accumulators and tickets start at zero
+      const B3Split sp = b3_split(nblk, grid_cap);
+      const AuxLayout al = aux_layout(m, natom);
+      unsigned char* auxb = static_cast<unsigned char*>(b.aux);
+      if (sp.parts > 1) cudaMemsetAsync(auxb + al.rho3, 0, al.end - al.rho3, st);
+      const int g3 = sp.parts > 1 ? sp.nfull + sp.ntail * sp.parts : gb;
 #define MAGACE_B3(NW, LOOP)                                                                                  \
   set_smem(k_b3_fe<FeDims, NW, LOOP>, sb);                                                                   \
-  k_b3_fe<FeDims, NW, LOOP><<<gb, NW * 32, sb, st>>>(m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy,   \
-                                                     b.edf, b.dedrho, b.err)
+  k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(                                                        \
+      m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy, b.edf, b.dedrho, b.err, sp.nfull, sp.parts,      \
+      reinterpret_cast<double*>(auxb + al.rho3), reinterpret_cast<float*>(auxb + al.gacc),                   \
+      reinterpret_cast<int*>(auxb + al.tickets))
       // variants: (16 warps, n0' innermost), (12, innermost), (8, innermost),
       // (12, n0' outermost), (16, packed FP32x2), (12, packed FP32x2)
       switch (m.tune_b3) {
@@ -1142,9 +1201,10 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
 }
 
 size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom) {
-  // k_density_fe's per-atom 2- and 4-body density, read by k_b3_fe
+  // k_density_fe's per-atom 2- and 4-body density, read by k_b3_fe, and
+  // k_b3_fe's split-tail accumulators (aux_layout)
   if (precision == 0 || !use_specialised(m) || natom <= 0) return 0;
-  return sizeof(double) * static_cast<size_t>(natom);
+  return aux_layout(m, natom).end;
 }
 
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {

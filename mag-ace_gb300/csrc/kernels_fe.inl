@@ -908,12 +908,21 @@ __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const 
 // (the CTA's factors, element-major), Gs[nc][33] (their density gradient),
 // the per-warp density partials, the atoms' dE/drho, and the element and
 // weight maps.
-
+//
+// Split tail (parts > 1, one CTA per block): CTAs below `nfull` evaluate
+// their block whole. The remaining blocks, the last partial wave of one CTA
+// per SM, are each divided among `parts` CTAs by task range. Each such CTA
+// adds its 3-body density into rho3_acc[tail][32] and its gradients into
+// g_acc[tail][nc][32] (re, im) with global atomics, then takes a ticket; the
+// CTA that takes the last ticket loads the totals and completes the block
+// (embedding, final weights). No CTA waits on another. The accumulators and
+// tickets are zeroed before the launch.
 template <class D, int NW, int LOOP>
 __global__ void __launch_bounds__(NW * 32, 1)
     k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
             const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
-            double* __restrict__ energy, double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err) {
+            double* __restrict__ energy, double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err,
+            int nfull, int parts, double* __restrict__ rho3_acc, float* __restrict__ g_acc, int* __restrict__ tickets) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
   const int nc = m.b3_nc, nW = m.nW;
@@ -928,8 +937,21 @@ __global__ void __launch_bounds__(NW * 32, 1)
   int* s_cw = s_fac + nc;                                          // [nW]
   __shared__ int s_atom[32];                                       // the block's atoms
   __shared__ int s_next;                                           // next task to take
+  __shared__ int s_last;                                           // split tail: this CTA completes the block
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (natom + 31) / 32;
+  // this CTA's blocks and task range
+  int blk_first = blockIdx.x, blk_stride = gridDim.x, task0 = 0, task1 = m.b3_ntask, tail = -1;
+  if (parts > 1) {
+    blk_stride = nblk;  // one block per CTA
+    if (static_cast<int>(blockIdx.x) >= nfull) {
+      const int q = (blockIdx.x - nfull) / parts, p = (blockIdx.x - nfull) % parts;
+      tail = q;
+      blk_first = nfull + q;
+      task0 = m.b3_ntask * p / parts;
+      task1 = m.b3_ntask * (p + 1) / parts;
+    }
+  }
   // bulk L2 prefetch of the rows of atom slot `a` of block `b` (whole
   // 16-byte units inside the row, so that nothing past the array is touched)
   const auto prefetch_rows = [&](const void* base, size_t row_bytes, int b, int a) {
@@ -948,11 +970,11 @@ __global__ void __launch_bounds__(NW * 32, 1)
   }
   for (int w = threadIdx.x; w < nW; w += blockDim.x) s_cw[w] = __ldg(m.b3_cw + w);
   __syncthreads();
-  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+  for (int blk = blk_first; blk < nblk; blk += blk_stride) {
     const int a0 = blk * 32;
     const int na = min(32, natom - a0);
     if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
-    if (threadIdx.x == 0) s_next = NW;
+    if (threadIdx.x == 0) s_next = task0 + NW;
     __syncthreads();
     // stage: thread c takes element c of every atom, kBatch atoms in flight
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
@@ -978,9 +1000,9 @@ __global__ void __launch_bounds__(NW * 32, 1)
     }
     double rloc = 0.0;
     // tasks from a shared counter (dynamic balance between the warps)
-    int tk = warp;
+    int tk = task0 + warp;
 #pragma unroll 1
-    while (tk < m.b3_ntask) {
+    while (tk < task1) {
       const int k = __ldg(m.b3_combo + tk);
       const int pat = __ldg(m.b3_pattern + k);
       const float cf = __ldg(m.b3_cff + tk);
@@ -1008,6 +1030,37 @@ __global__ void __launch_bounds__(NW * 32, 1)
     }
     rpart[warp * 32 + lane] = rloc;
     __syncthreads();
+    if (tail >= 0) {
+      // split tail: add this part into the block's accumulators
+      if (warp == 0 && lane < na) {
+        double r3 = 0.0;
+        for (int w = 0; w < NW; ++w) r3 += rpart[w * 32 + lane];
+        atomicAdd(rho3_acc + tail * 32 + lane, r3);
+      }
+      float* ga = g_acc + static_cast<size_t>(tail) * nc * 64;
+      for (int q = threadIdx.x; q < nc * 32; q += blockDim.x) {
+        const int c = q >> 5, a = q & 31;
+        if (a < na) {
+          const C<float> g = Gs[c * kB3Stride + a];
+          atomicAdd(ga + 2 * q, g.x);
+          atomicAdd(ga + 2 * q + 1, g.y);
+        }
+      }
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) s_last = atomicAdd(tickets + tail, 1) == parts - 1;
+      __syncthreads();
+      if (!s_last) break;  // another part completes the block
+      __threadfence();
+      // the last part: the block's totals replace this part's own
+      for (int q = threadIdx.x; q < nc * 32; q += blockDim.x) {
+        const int c = q >> 5, a = q & 31;
+        Gs[c * kB3Stride + a] = {__ldcg(ga + 2 * q), __ldcg(ga + 2 * q + 1)};
+      }
+      for (int q = threadIdx.x; q < NW * 32; q += blockDim.x)
+        rpart[q] = q < 32 ? __ldcg(rho3_acc + tail * 32 + q) : 0.0;
+      __syncthreads();
+    }
     // finish the atoms, one per lane of warp 0
     if (warp == 0 && lane < na) {
       const int atom = s_atom[lane];
