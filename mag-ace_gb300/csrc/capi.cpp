@@ -939,11 +939,15 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
     off[i + 1] = off[i] + cnt;
   }
   const long npacked = off[natom];
-  if (occlist) {
+  // the neighbour elements must all be 1; the scan runs on the host while
+  // the GPU evaluates, and a failure is reported once the stream is idle
+  const auto occlist_bad = [&]() {
     unsigned bad = 0;  // a branch-free scan the compiler vectorises
-    for (int j = 0; j < nei; ++j) bad |= static_cast<unsigned>(occlist[j] ^ 1);
-    if (bad) return fail(MAGACE_ERR_ARGS, "neighbour element index other than 1", npacked);
-  }
+    if (occlist)
+      for (int j = 0; j < nei; ++j) bad |= static_cast<unsigned>(occlist[j] ^ 1);
+    return bad != 0;
+  };
+  const char* occ_msg = "neighbour element index other than 1";
   int st = upload_tables();
   if (st) return fail(st, R.last_msg.c_str(), npacked);
   st = reserve_work(natom, static_cast<int>(npacked), R.precision);
@@ -991,7 +995,12 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
     b.fij = flist;
     b.tij = tlist;
     b.ti0 = tlist0;
+    b.host_outputs = true;
     if (run_eval(b, s)) return fail(R.last_error, R.last_msg.c_str(), npacked);
+    if (occlist_bad()) {
+      cudaStreamSynchronize(s);
+      return fail(MAGACE_ERR_ARGS, occ_msg, npacked);
+    }
   } else {
     auto res = [&](DevBuf<double>& bb, size_t n) { return bb.reserve(n) == cudaSuccess; };
     if (!(res(R.r, nb) && res(R.e, 3 * nb) && res(R.magj, nb) && res(R.mhj, 3 * nb) && res(R.magi, na) &&
@@ -1052,7 +1061,9 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
       }
       if (ce == cudaSuccess && x.bytes) ce = cudaMemcpyAsync(dst, x.dev, x.bytes, cudaMemcpyDeviceToHost, s);
     }
+    const bool bad_elements = occlist_bad();
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+    if (bad_elements) return fail(MAGACE_ERR_ARGS, occ_msg, npacked);
     if (ce != cudaSuccess) return fail(MAGACE_ERR_CUDA, cudaGetErrorString(ce), npacked);
     if (pinned) {
       o = 0;

@@ -1170,11 +1170,19 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
     const size_t s3 = forces_fe_smem<R, FeDims>();
-#define MAGACE_FORCES(MB, PK)                                                                                       \
-  set_smem(k_forces_fe<R, FeDims, MB, PK>, s3);                                                                     \
-  k_forces_fe<R, FeDims, MB, PK><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,      \
-                                                       reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho, b.fij,   \
-                                                       b.tij, b.ti0, static_cast<const R*>(b.stage), b.err)
+    // outputs in host memory (acelib_ writing the caller's arrays directly):
+    // the variants that store each tile's outputs as whole lines
+#define MAGACE_FORCES_SO(MB, PK, SO)                                                                                \
+  set_smem(k_forces_fe<R, FeDims, MB, PK, SO>, s3);                                                                 \
+  k_forces_fe<R, FeDims, MB, PK, SO><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,  \
+                                                           reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho,      \
+                                                           b.fij, b.tij, b.ti0, static_cast<const R*>(b.stage), b.err)
+#define MAGACE_FORCES(MB, PK)                 \
+  if (b.host_outputs) {                       \
+    MAGACE_FORCES_SO(MB, PK, true);           \
+  } else {                                    \
+    MAGACE_FORCES_SO(MB, PK, false);          \
+  }
     if constexpr (sizeof(R) == 8) {
       MAGACE_FORCES(4, false);
     } else {
@@ -1189,6 +1197,7 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
       }
     }
 #undef MAGACE_FORCES
+#undef MAGACE_FORCES_SO
   } else {
     const size_t s3 = forces_smem<R>(m, kForceThreads);
     set_smem(k_forces<R>, s3);

@@ -54,6 +54,7 @@ struct EvalBuffers {
   const int* order = nullptr; // [natom] work queue (atoms by decreasing bond count) or null
   void* stage = nullptr;      // [nei][8] bond inputs in the working precision (specialised kernels), or null
   bool dev_inputs = false;    // r, e, magj, mhj are device memory (bulk copies may read them)
+  bool host_outputs = false;  // fij, tij are host memory (written as whole lines)
 };
 
 // Work queue of one evaluation: the atoms sorted by decreasing bond count

@@ -1112,6 +1112,19 @@ __global__ void __launch_bounds__(NW * 32, 1)
   }
 }
 
+// Writes v[0 .. 3n) to dst[3 j0 .. 3 (j0 + n)) with 16-byte stores wherever
+// the destination is 16-byte aligned (the CTA's threads in turn).
+__device__ __forceinline__ void store_tile(double* __restrict__ dst, const double* v, int j0, int n) {
+  double* d = dst + 3 * static_cast<size_t>(j0);
+  const int cnt = 3 * n;
+  const int h = (reinterpret_cast<uintptr_t>(d) & 8u) ? 1 : 0;
+  const int np = (cnt - h) >> 1;
+  double2* d2 = reinterpret_cast<double2*>(d + h);
+  for (int q = threadIdx.x; q < np; q += blockDim.x) d2[q] = make_double2(v[h + 2 * q], v[h + 2 * q + 1]);
+  if (threadIdx.x == 0 && h) d[0] = v[0];
+  if (threadIdx.x == blockDim.x - 1 && ((cnt - h) & 1)) d[cnt - 1] = v[cnt - 1];
+}
+
 // ===========================================================================
 // k_forces_fe: one thread per bond. Weights transposed into shared memory:
 // W2T[k][n] and WAT[k3][i], so the inner loops read 16-byte pairs. MINB is
@@ -1119,7 +1132,12 @@ __global__ void __launch_bounds__(NW * 32, 1)
 // PACKED (split precision only) stores the transposed weights as separate
 // real and imaginary planes and runs the contractions two n (or i) at a
 // time with packed FP32x2 FMAs.
-template <class R, class D, int MINB, bool PACKED>
+//
+// SOUT: each tile's f_ij and t_ij go through shared memory and are written
+// as contiguous 16-byte stores (whole lines); chosen when the outputs are
+// host memory read over NVLink-C2C, where scattered 8-byte stores cost far
+// more than in device memory.
+template <class R, class D, int MINB, bool PACKED, bool SOUT = false>
 __global__ void __launch_bounds__(64, MINB)
     k_forces_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
@@ -1140,6 +1158,7 @@ __global__ void __launch_bounds__(64, MINB)
   C<R>* cYa = reinterpret_cast<C<R>*>(cMd + D::NMF * T);  // full [LSA]
   C<R>* cdYa = cYa + D::LSA * T;                         // [LSA][3]
   C<R>* cYm = cdYa + D::LSA * 3 * T;                     // half [H2]
+  double* sOut = reinterpret_cast<double*>(cYm + D::H2 * T);  // the tile's f_ij [T][3], then t_ij [T][3]
   const int t = threadIdx.x;
   static_assert(!PACKED || sizeof(R) == 4, "packed contractions are FP32");
   static_assert(D::NB % 4 == 0 && D::NRY % 4 == 0, "planes are read four floats at a time");
@@ -1176,279 +1195,290 @@ __global__ void __launch_bounds__(64, MINB)
     __syncthreads();
     const R edf = to_r<R>(edf_in[atom]);
     const int b0 = off[atom], b1 = off[atom + 1];
-    for (int j = b0 + t; j < b1; j += T) {
-      R r, ex, ey, ez, mg, mx, my, mz;
-      if (stage) {  // the A-basis kernel's copy in device memory
-        const R* sp = stage + 8 * static_cast<size_t>(j);
-        r = sp[0];
-        ex = sp[1];
-        ey = sp[2];
-        ez = sp[3];
-        mg = sp[4];
-        mx = sp[5];
-        my = sp[6];
-        mz = sp[7];
-      } else {
-        r = to_r<R>(rr[j]);
-        ex = to_r<R>(ee[3 * j]);
-        ey = to_r<R>(ee[3 * j + 1]);
-        ez = to_r<R>(ee[3 * j + 2]);
-        mg = to_r<R>(magj[j]);
-        mx = to_r<R>(mhj[3 * j]);
-        my = to_r<R>(mhj[3 * j + 1]);
-        mz = to_r<R>(mhj[3 * j + 2]);
-      }
-      R g[D::NB];
-      R cdv = R(0);
-      {
-        R tv[D::NR], td[D::NR], gd[D::NB], cv[1];
-        R wl = R(0);
-        const int nla = atomic_bin_r<R>(m, r, wl, err);
-        if (nla > 0) {
-          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, rscale_a<R>(m), g, gd);
-          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, rscale_a<R>(m), tv, td);
-          R cd1[1];
-          lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, rscale_a<R>(m), cv, cd1);
-          cdv = cd1[0];
+    // bonds in tiles of T, uniform over the CTA (SOUT: each tile's outputs
+    // are written from shared memory after the tile)
+    for (int jt = b0; jt < b1; jt += T) {
+      const int j = jt + t;
+      if (j < b1) {
+        R r, ex, ey, ez, mg, mx, my, mz;
+        if (stage) {  // the A-basis kernel's copy in device memory
+          const R* sp = stage + 8 * static_cast<size_t>(j);
+          r = sp[0];
+          ex = sp[1];
+          ey = sp[2];
+          ez = sp[3];
+          mg = sp[4];
+          mx = sp[5];
+          my = sp[6];
+          mz = sp[7];
         } else {
-#pragma unroll
-          for (int q = 0; q < D::NB; ++q) g[q] = gd[q] = R(0);
-#pragma unroll
-          for (int q = 0; q < D::NR; ++q) tv[q] = td[q] = R(0);
+          r = to_r<R>(rr[j]);
+          ex = to_r<R>(ee[3 * j]);
+          ey = to_r<R>(ee[3 * j + 1]);
+          ez = to_r<R>(ee[3 * j + 2]);
+          mg = to_r<R>(magj[j]);
+          mx = to_r<R>(mhj[3 * j]);
+          my = to_r<R>(mhj[3 * j + 1]);
+          mz = to_r<R>(mhj[3 * j + 2]);
         }
-#pragma unroll
-        for (int q = 0; q < D::NB; ++q) cgd[q * T + t] = gd[q];
-#pragma unroll
-        for (int q = 0; q < D::NR; ++q) {
-          cR[q * T + t] = tv[q];
-          cRd[q * T + t] = td[q];
+        R g[D::NB];
+        R cdv = R(0);
+        {
+          R tv[D::NR], td[D::NR], gd[D::NB], cv[1];
+          R wl = R(0);
+          const int nla = atomic_bin_r<R>(m, r, wl, err);
+          if (nla > 0) {
+            lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, 0, D::NB, nla, wl, rscale_a<R>(m), g, gd);
+            lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB, D::NR, nla, wl, rscale_a<R>(m), tv, td);
+            R cd1[1];
+            lut_eval<true>(pick<R>(m.lut_a, m.lut_a32), D::NFA, D::NB + D::NR, 1, nla, wl, rscale_a<R>(m), cv, cd1);
+            cdv = cd1[0];
+          } else {
+  #pragma unroll
+            for (int q = 0; q < D::NB; ++q) g[q] = gd[q] = R(0);
+  #pragma unroll
+            for (int q = 0; q < D::NR; ++q) tv[q] = td[q] = R(0);
+          }
+  #pragma unroll
+          for (int q = 0; q < D::NB; ++q) cgd[q * T + t] = gd[q];
+  #pragma unroll
+          for (int q = 0; q < D::NR; ++q) {
+            cR[q * T + t] = tv[q];
+            cRd[q * T + t] = td[q];
+          }
         }
-      }
-      {
-        R mv[D::NMF], Md[D::NMF];
-        R wm = R(0);
-        const int nlm = magnetic_bin_r<R>(m, mg, wm, err);
-        if (nlm > 0) {
-          lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, rscale_m<R>(m), mv, Md);
-        } else {
-#pragma unroll
+        {
+          R mv[D::NMF], Md[D::NMF];
+          R wm = R(0);
+          const int nlm = magnetic_bin_r<R>(m, mg, wm, err);
+          if (nlm > 0) {
+            lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nlm, wm, rscale_m<R>(m), mv, Md);
+          } else {
+  #pragma unroll
+            for (int q = 0; q < D::NMF; ++q) {
+              mv[q] = R(nlm == 0 ? 1 : 0);
+              Md[q] = R(0);
+            }
+          }
+  #pragma unroll
           for (int q = 0; q < D::NMF; ++q) {
-            mv[q] = R(nlm == 0 ? 1 : 0);
-            Md[q] = R(0);
+            cM[q * T + t] = mv[q];
+            cMd[q * T + t] = Md[q];
           }
         }
-#pragma unroll
-        for (int q = 0; q < D::NMF; ++q) {
-          cM[q * T + t] = mv[q];
-          cMd[q * T + t] = Md[q];
-        }
-      }
-      C<R> Ym[D::H2], dYm[D::H2][3];
-      {
-        C<R> Ya[D::HA], dYa[D::HA][3];
-        ylm_half<R, true>(D::LA, ex, ey, ez, Ya, dYa);
-#pragma unroll
-        for (int lm = 0; lm < D::LSA; ++lm) {
-          const int l = l_of_lm(lm), mm = lm - l * l - l;
-          cYa[lm * T + t] = y_full(Ya, l, mm);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            C<R> d = dYa[ph(l, mm < 0 ? -mm : mm)][c];
-            if (mm < 0) {
-              const R s = R(parity(mm));
-              d = {d.x * s, -d.y * s};
-            }
-            cdYa[(lm * 3 + c) * T + t] = d;
-          }
-        }
-        ylm_half<R, true>(D::L2, mx, my, mz, Ym, dYm);
-#pragma unroll
-        for (int h = 0; h < D::H2; ++h) cYm[h * T + t] = Ym[h];
-      }
-      // ---- force
-      R fr = edf * cdv, ft[3] = {R(0), R(0), R(0)};
-      {
-        R sp[D::NB];
-        C<R> U[D::NRY];
-        if constexpr (PACKED) {
-          float2 sp2[D::NB / 2], Ux2[D::NRY / 2], Uy2[D::NRY / 2];
-#pragma unroll
-          for (int n = 0; n < D::NB / 2; ++n) sp2[n] = make_float2(0.f, 0.f);
-#pragma unroll
-          for (int i = 0; i < D::NRY / 2; ++i) Ux2[i] = Uy2[i] = make_float2(0.f, 0.f);
-#pragma unroll 1
-          for (int nr = 0; nr < D::N2; ++nr)
-#pragma unroll
-            for (int h = 0; h < D::H2; ++h) {
-              const int k = nr * D::H2 + h;
-              const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
-              const float2 qxx = make_float2(q.x, q.x), qyy = make_float2(q.y, q.y), qyn = make_float2(-q.y, -q.y);
-              const float4* w2x = reinterpret_cast<const float4*>(W2x + k * D::NB);
-              const float4* w2y = reinterpret_cast<const float4*>(W2y + k * D::NB);
-#pragma unroll
-              for (int n4 = 0; n4 < D::NB / 4; ++n4) {
-                const float4 a = w2x[n4], b = w2y[n4];
-                sp2[2 * n4] = __ffma2_rn(make_float2(a.x, a.y), qxx, sp2[2 * n4]);
-                sp2[2 * n4] = __ffma2_rn(make_float2(b.x, b.y), qyn, sp2[2 * n4]);
-                sp2[2 * n4 + 1] = __ffma2_rn(make_float2(a.z, a.w), qxx, sp2[2 * n4 + 1]);
-                sp2[2 * n4 + 1] = __ffma2_rn(make_float2(b.z, b.w), qyn, sp2[2 * n4 + 1]);
+        C<R> Ym[D::H2], dYm[D::H2][3];
+        {
+          C<R> Ya[D::HA], dYa[D::HA][3];
+          ylm_half<R, true>(D::LA, ex, ey, ez, Ya, dYa);
+  #pragma unroll
+          for (int lm = 0; lm < D::LSA; ++lm) {
+            const int l = l_of_lm(lm), mm = lm - l * l - l;
+            cYa[lm * T + t] = y_full(Ya, l, mm);
+  #pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              C<R> d = dYa[ph(l, mm < 0 ? -mm : mm)][c];
+              if (mm < 0) {
+                const R s = R(parity(mm));
+                d = {d.x * s, -d.y * s};
               }
-              if (nr < D::NM && h < D::H3) {
-                const int k3 = nr * D::H3 + h;
-                const float4* wax = reinterpret_cast<const float4*>(WAx + k3 * D::NRY);
-                const float4* way = reinterpret_cast<const float4*>(WAy + k3 * D::NRY);
-#pragma unroll
-                for (int i4 = 0; i4 < D::NRY / 4; ++i4) {
-                  const float4 a = wax[i4], b = way[i4];
-                  const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
-                  const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
-                  Ux2[2 * i4] = __ffma2_rn(b0, qyn, __ffma2_rn(a0, qxx, Ux2[2 * i4]));
-                  Uy2[2 * i4] = __ffma2_rn(b0, qxx, __ffma2_rn(a0, qyy, Uy2[2 * i4]));
-                  Ux2[2 * i4 + 1] = __ffma2_rn(b1, qyn, __ffma2_rn(a1, qxx, Ux2[2 * i4 + 1]));
-                  Uy2[2 * i4 + 1] = __ffma2_rn(b1, qxx, __ffma2_rn(a1, qyy, Uy2[2 * i4 + 1]));
+              cdYa[(lm * 3 + c) * T + t] = d;
+            }
+          }
+          ylm_half<R, true>(D::L2, mx, my, mz, Ym, dYm);
+  #pragma unroll
+          for (int h = 0; h < D::H2; ++h) cYm[h * T + t] = Ym[h];
+        }
+        // ---- force
+        R fr = edf * cdv, ft[3] = {R(0), R(0), R(0)};
+        {
+          R sp[D::NB];
+          C<R> U[D::NRY];
+          if constexpr (PACKED) {
+            float2 sp2[D::NB / 2], Ux2[D::NRY / 2], Uy2[D::NRY / 2];
+  #pragma unroll
+            for (int n = 0; n < D::NB / 2; ++n) sp2[n] = make_float2(0.f, 0.f);
+  #pragma unroll
+            for (int i = 0; i < D::NRY / 2; ++i) Ux2[i] = Uy2[i] = make_float2(0.f, 0.f);
+  #pragma unroll 1
+            for (int nr = 0; nr < D::N2; ++nr)
+  #pragma unroll
+              for (int h = 0; h < D::H2; ++h) {
+                const int k = nr * D::H2 + h;
+                const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
+                const float2 qxx = make_float2(q.x, q.x), qyy = make_float2(q.y, q.y), qyn = make_float2(-q.y, -q.y);
+                const float4* w2x = reinterpret_cast<const float4*>(W2x + k * D::NB);
+                const float4* w2y = reinterpret_cast<const float4*>(W2y + k * D::NB);
+  #pragma unroll
+                for (int n4 = 0; n4 < D::NB / 4; ++n4) {
+                  const float4 a = w2x[n4], b = w2y[n4];
+                  sp2[2 * n4] = __ffma2_rn(make_float2(a.x, a.y), qxx, sp2[2 * n4]);
+                  sp2[2 * n4] = __ffma2_rn(make_float2(b.x, b.y), qyn, sp2[2 * n4]);
+                  sp2[2 * n4 + 1] = __ffma2_rn(make_float2(a.z, a.w), qxx, sp2[2 * n4 + 1]);
+                  sp2[2 * n4 + 1] = __ffma2_rn(make_float2(b.z, b.w), qyn, sp2[2 * n4 + 1]);
+                }
+                if (nr < D::NM && h < D::H3) {
+                  const int k3 = nr * D::H3 + h;
+                  const float4* wax = reinterpret_cast<const float4*>(WAx + k3 * D::NRY);
+                  const float4* way = reinterpret_cast<const float4*>(WAy + k3 * D::NRY);
+  #pragma unroll
+                  for (int i4 = 0; i4 < D::NRY / 4; ++i4) {
+                    const float4 a = wax[i4], b = way[i4];
+                    const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
+                    const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
+                    Ux2[2 * i4] = __ffma2_rn(b0, qyn, __ffma2_rn(a0, qxx, Ux2[2 * i4]));
+                    Uy2[2 * i4] = __ffma2_rn(b0, qxx, __ffma2_rn(a0, qyy, Uy2[2 * i4]));
+                    Ux2[2 * i4 + 1] = __ffma2_rn(b1, qyn, __ffma2_rn(a1, qxx, Ux2[2 * i4 + 1]));
+                    Uy2[2 * i4 + 1] = __ffma2_rn(b1, qxx, __ffma2_rn(a1, qyy, Uy2[2 * i4 + 1]));
+                  }
                 }
               }
+  #pragma unroll
+            for (int n = 0; n < D::NB / 2; ++n) {
+              sp[2 * n] = sp2[n].x;
+              sp[2 * n + 1] = sp2[n].y;
             }
-#pragma unroll
-          for (int n = 0; n < D::NB / 2; ++n) {
-            sp[2 * n] = sp2[n].x;
-            sp[2 * n + 1] = sp2[n].y;
-          }
-#pragma unroll
-          for (int i = 0; i < D::NRY / 2; ++i) {
-            U[2 * i] = {Ux2[i].x, Uy2[i].x};
-            U[2 * i + 1] = {Ux2[i].y, Uy2[i].y};
-          }
-        } else {
-#pragma unroll
-          for (int n = 0; n < D::NB; ++n) sp[n] = R(0);
-#pragma unroll
-          for (int i = 0; i < D::NRY; ++i) U[i] = {R(0), R(0)};
-#pragma unroll 1
-          for (int nr = 0; nr < D::N2; ++nr)
-#pragma unroll
-            for (int h = 0; h < D::H2; ++h) {
-              const int k = nr * D::H2 + h;
-              const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
-              const C<R>* w2 = W2T + k * D::NB;
-#pragma unroll
-              for (int n = 0; n < D::NB; ++n) sp[n] += re_mul(w2[n], q);
-              if (nr < D::NM && h < D::H3) {
-                const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
-#pragma unroll
-                for (int i = 0; i < D::NRY; ++i) {
-                  const C<R> w = wa[i];
-                  U[i].x += w.x * q.x - w.y * q.y;
-                  U[i].y += w.x * q.y + w.y * q.x;
+  #pragma unroll
+            for (int i = 0; i < D::NRY / 2; ++i) {
+              U[2 * i] = {Ux2[i].x, Uy2[i].x};
+              U[2 * i + 1] = {Ux2[i].y, Uy2[i].y};
+            }
+          } else {
+  #pragma unroll
+            for (int n = 0; n < D::NB; ++n) sp[n] = R(0);
+  #pragma unroll
+            for (int i = 0; i < D::NRY; ++i) U[i] = {R(0), R(0)};
+  #pragma unroll 1
+            for (int nr = 0; nr < D::N2; ++nr)
+  #pragma unroll
+              for (int h = 0; h < D::H2; ++h) {
+                const int k = nr * D::H2 + h;
+                const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
+                const C<R>* w2 = W2T + k * D::NB;
+  #pragma unroll
+                for (int n = 0; n < D::NB; ++n) sp[n] += re_mul(w2[n], q);
+                if (nr < D::NM && h < D::H3) {
+                  const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
+  #pragma unroll
+                  for (int i = 0; i < D::NRY; ++i) {
+                    const C<R> w = wa[i];
+                    U[i].x += w.x * q.x - w.y * q.y;
+                    U[i].y += w.x * q.y + w.y * q.x;
+                  }
                 }
               }
+          }
+  #pragma unroll
+          for (int n = 0; n < D::NB; ++n) fr += cgd[n * T + t] * sp[n];
+          const R invr = rcp(r);
+  #pragma unroll
+          for (int i = 0; i < D::NRY; ++i) {
+            const int n1 = i / D::LSA, lma = i % D::LSA, l1 = l_of_lm(lma);
+            fr += cRd[(n1 * (D::LA + 1) + l1) * T + t] * re_mul(U[i], cYa[lma * T + t]);
+            const R sc = invr * cR[(n1 * (D::LA + 1) + l1) * T + t];
+  #pragma unroll
+            for (int c = 0; c < 3; ++c) ft[c] += sc * re_mul(U[i], cdYa[(lma * 3 + c) * T + t]);
+          }
+        }
+        *(SOUT ? sOut + 3 * t + 0 : fij + 3 * static_cast<size_t>(j) + 0) = to_d(fr * ex + ft[0]);
+        *(SOUT ? sOut + 3 * t + 1 : fij + 3 * static_cast<size_t>(j) + 1) = to_d(fr * ey + ft[1]);
+        *(SOUT ? sOut + 3 * t + 2 : fij + 3 * static_cast<size_t>(j) + 2) = to_d(fr * ez + ft[2]);
+        // ---- magnetic force
+        R tr = R(0), tt[3] = {R(0), R(0), R(0)};
+        {
+          C<R> RY[D::NRY];
+  #pragma unroll
+          for (int i = 0; i < D::NRY; ++i) {
+            const int n1 = i / D::LSA, lma = i % D::LSA;
+            RY[i] = cscale(cYa[lma * T + t], cR[(n1 * (D::LA + 1) + l_of_lm(lma)) * T + t]);
+          }
+          const R invm = rcp(mg);
+          // V[k] = sum_n g_n W2[n][k] + sum_i W_A[i][k] RY_i, contracted per k
+          const auto contract = [&](int nr, int h, C<R> V) {
+            const int q = nr * (D::L2 + 1) + l_of_h(h);
+            tr += cMd[q * T + t] * re_mul(V, Ym[h]);
+            const R sc = invm * cM[q * T + t];
+  #pragma unroll
+            for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(V, dYm[h][c]);
+          };
+          if constexpr (PACKED) {
+            float2 g2[D::NB / 2], RYx2[D::NRY / 2], RYy2[D::NRY / 2], RYyn2[D::NRY / 2];
+  #pragma unroll
+            for (int n = 0; n < D::NB / 2; ++n) g2[n] = make_float2(g[2 * n], g[2 * n + 1]);
+  #pragma unroll
+            for (int i = 0; i < D::NRY / 2; ++i) {
+              RYx2[i] = make_float2(RY[2 * i].x, RY[2 * i + 1].x);
+              RYy2[i] = make_float2(RY[2 * i].y, RY[2 * i + 1].y);
+              RYyn2[i] = make_float2(-RY[2 * i].y, -RY[2 * i + 1].y);
             }
+  #pragma unroll 1
+            for (int nr = 0; nr < D::N2; ++nr)
+  #pragma unroll
+              for (int h = 0; h < D::H2; ++h) {
+                const int k = nr * D::H2 + h;
+                float2 vx2 = make_float2(0.f, 0.f), vy2 = make_float2(0.f, 0.f);
+                const float4* w2x = reinterpret_cast<const float4*>(W2x + k * D::NB);
+                const float4* w2y = reinterpret_cast<const float4*>(W2y + k * D::NB);
+  #pragma unroll
+                for (int n4 = 0; n4 < D::NB / 4; ++n4) {
+                  const float4 a = w2x[n4], b = w2y[n4];
+                  vx2 = __ffma2_rn(g2[2 * n4], make_float2(a.x, a.y), vx2);
+                  vx2 = __ffma2_rn(g2[2 * n4 + 1], make_float2(a.z, a.w), vx2);
+                  vy2 = __ffma2_rn(g2[2 * n4], make_float2(b.x, b.y), vy2);
+                  vy2 = __ffma2_rn(g2[2 * n4 + 1], make_float2(b.z, b.w), vy2);
+                }
+                if (nr < D::NM && h < D::H3) {
+                  const int k3 = nr * D::H3 + h;
+                  const float4* wax = reinterpret_cast<const float4*>(WAx + k3 * D::NRY);
+                  const float4* way = reinterpret_cast<const float4*>(WAy + k3 * D::NRY);
+  #pragma unroll
+                  for (int i4 = 0; i4 < D::NRY / 4; ++i4) {
+                    const float4 a = wax[i4], b = way[i4];
+                    const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
+                    const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
+                    vx2 = __ffma2_rn(b0, RYyn2[2 * i4], __ffma2_rn(a0, RYx2[2 * i4], vx2));
+                    vy2 = __ffma2_rn(b0, RYx2[2 * i4], __ffma2_rn(a0, RYy2[2 * i4], vy2));
+                    vx2 = __ffma2_rn(b1, RYyn2[2 * i4 + 1], __ffma2_rn(a1, RYx2[2 * i4 + 1], vx2));
+                    vy2 = __ffma2_rn(b1, RYx2[2 * i4 + 1], __ffma2_rn(a1, RYy2[2 * i4 + 1], vy2));
+                  }
+                }
+                contract(nr, h, C<R>{vx2.x + vx2.y, vy2.x + vy2.y});
+              }
+          } else {
+  #pragma unroll 1
+            for (int nr = 0; nr < D::N2; ++nr)
+  #pragma unroll
+              for (int h = 0; h < D::H2; ++h) {
+                const int k = nr * D::H2 + h;
+                const C<R>* w2 = W2T + k * D::NB;
+                C<R> V = {R(0), R(0)};
+  #pragma unroll
+                for (int n = 0; n < D::NB; ++n) {
+                  V.x += g[n] * w2[n].x;
+                  V.y += g[n] * w2[n].y;
+                }
+                if (nr < D::NM && h < D::H3) {
+                  const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
+  #pragma unroll
+                  for (int i = 0; i < D::NRY; ++i) {
+                    const C<R> w = wa[i];
+                    V.x += w.x * RY[i].x - w.y * RY[i].y;
+                    V.y += w.x * RY[i].y + w.y * RY[i].x;
+                  }
+                }
+                contract(nr, h, V);
+              }
+          }
         }
-#pragma unroll
-        for (int n = 0; n < D::NB; ++n) fr += cgd[n * T + t] * sp[n];
-        const R invr = rcp(r);
-#pragma unroll
-        for (int i = 0; i < D::NRY; ++i) {
-          const int n1 = i / D::LSA, lma = i % D::LSA, l1 = l_of_lm(lma);
-          fr += cRd[(n1 * (D::LA + 1) + l1) * T + t] * re_mul(U[i], cYa[lma * T + t]);
-          const R sc = invr * cR[(n1 * (D::LA + 1) + l1) * T + t];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) ft[c] += sc * re_mul(U[i], cdYa[(lma * 3 + c) * T + t]);
-        }
+        *(SOUT ? sOut + 3 * T + 3 * t + 0 : tij + 3 * static_cast<size_t>(j) + 0) = to_d(tr * mx + tt[0]);
+        *(SOUT ? sOut + 3 * T + 3 * t + 1 : tij + 3 * static_cast<size_t>(j) + 1) = to_d(tr * my + tt[1]);
+        *(SOUT ? sOut + 3 * T + 3 * t + 2 : tij + 3 * static_cast<size_t>(j) + 2) = to_d(tr * mz + tt[2]);
       }
-      fij[3 * static_cast<size_t>(j) + 0] = to_d(fr * ex + ft[0]);
-      fij[3 * static_cast<size_t>(j) + 1] = to_d(fr * ey + ft[1]);
-      fij[3 * static_cast<size_t>(j) + 2] = to_d(fr * ez + ft[2]);
-      // ---- magnetic force
-      R tr = R(0), tt[3] = {R(0), R(0), R(0)};
-      {
-        C<R> RY[D::NRY];
-#pragma unroll
-        for (int i = 0; i < D::NRY; ++i) {
-          const int n1 = i / D::LSA, lma = i % D::LSA;
-          RY[i] = cscale(cYa[lma * T + t], cR[(n1 * (D::LA + 1) + l_of_lm(lma)) * T + t]);
-        }
-        const R invm = rcp(mg);
-        // V[k] = sum_n g_n W2[n][k] + sum_i W_A[i][k] RY_i, contracted per k
-        const auto contract = [&](int nr, int h, C<R> V) {
-          const int q = nr * (D::L2 + 1) + l_of_h(h);
-          tr += cMd[q * T + t] * re_mul(V, Ym[h]);
-          const R sc = invm * cM[q * T + t];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(V, dYm[h][c]);
-        };
-        if constexpr (PACKED) {
-          float2 g2[D::NB / 2], RYx2[D::NRY / 2], RYy2[D::NRY / 2], RYyn2[D::NRY / 2];
-#pragma unroll
-          for (int n = 0; n < D::NB / 2; ++n) g2[n] = make_float2(g[2 * n], g[2 * n + 1]);
-#pragma unroll
-          for (int i = 0; i < D::NRY / 2; ++i) {
-            RYx2[i] = make_float2(RY[2 * i].x, RY[2 * i + 1].x);
-            RYy2[i] = make_float2(RY[2 * i].y, RY[2 * i + 1].y);
-            RYyn2[i] = make_float2(-RY[2 * i].y, -RY[2 * i + 1].y);
-          }
-#pragma unroll 1
-          for (int nr = 0; nr < D::N2; ++nr)
-#pragma unroll
-            for (int h = 0; h < D::H2; ++h) {
-              const int k = nr * D::H2 + h;
-              float2 vx2 = make_float2(0.f, 0.f), vy2 = make_float2(0.f, 0.f);
-              const float4* w2x = reinterpret_cast<const float4*>(W2x + k * D::NB);
-              const float4* w2y = reinterpret_cast<const float4*>(W2y + k * D::NB);
-#pragma unroll
-              for (int n4 = 0; n4 < D::NB / 4; ++n4) {
-                const float4 a = w2x[n4], b = w2y[n4];
-                vx2 = __ffma2_rn(g2[2 * n4], make_float2(a.x, a.y), vx2);
-                vx2 = __ffma2_rn(g2[2 * n4 + 1], make_float2(a.z, a.w), vx2);
-                vy2 = __ffma2_rn(g2[2 * n4], make_float2(b.x, b.y), vy2);
-                vy2 = __ffma2_rn(g2[2 * n4 + 1], make_float2(b.z, b.w), vy2);
-              }
-              if (nr < D::NM && h < D::H3) {
-                const int k3 = nr * D::H3 + h;
-                const float4* wax = reinterpret_cast<const float4*>(WAx + k3 * D::NRY);
-                const float4* way = reinterpret_cast<const float4*>(WAy + k3 * D::NRY);
-#pragma unroll
-                for (int i4 = 0; i4 < D::NRY / 4; ++i4) {
-                  const float4 a = wax[i4], b = way[i4];
-                  const float2 a0 = make_float2(a.x, a.y), a1 = make_float2(a.z, a.w);
-                  const float2 b0 = make_float2(b.x, b.y), b1 = make_float2(b.z, b.w);
-                  vx2 = __ffma2_rn(b0, RYyn2[2 * i4], __ffma2_rn(a0, RYx2[2 * i4], vx2));
-                  vy2 = __ffma2_rn(b0, RYx2[2 * i4], __ffma2_rn(a0, RYy2[2 * i4], vy2));
-                  vx2 = __ffma2_rn(b1, RYyn2[2 * i4 + 1], __ffma2_rn(a1, RYx2[2 * i4 + 1], vx2));
-                  vy2 = __ffma2_rn(b1, RYx2[2 * i4 + 1], __ffma2_rn(a1, RYy2[2 * i4 + 1], vy2));
-                }
-              }
-              contract(nr, h, C<R>{vx2.x + vx2.y, vy2.x + vy2.y});
-            }
-        } else {
-#pragma unroll 1
-          for (int nr = 0; nr < D::N2; ++nr)
-#pragma unroll
-            for (int h = 0; h < D::H2; ++h) {
-              const int k = nr * D::H2 + h;
-              const C<R>* w2 = W2T + k * D::NB;
-              C<R> V = {R(0), R(0)};
-#pragma unroll
-              for (int n = 0; n < D::NB; ++n) {
-                V.x += g[n] * w2[n].x;
-                V.y += g[n] * w2[n].y;
-              }
-              if (nr < D::NM && h < D::H3) {
-                const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
-#pragma unroll
-                for (int i = 0; i < D::NRY; ++i) {
-                  const C<R> w = wa[i];
-                  V.x += w.x * RY[i].x - w.y * RY[i].y;
-                  V.y += w.x * RY[i].y + w.y * RY[i].x;
-                }
-              }
-              contract(nr, h, V);
-            }
-        }
+      if constexpr (SOUT) {
+        __syncthreads();
+        store_tile(fij, sOut, jt, min(T, b1 - jt));
+        store_tile(tij, sOut + 3 * T, jt, min(T, b1 - jt));
+        __syncthreads();
       }
-      tij[3 * static_cast<size_t>(j) + 0] = to_d(tr * mx + tt[0]);
-      tij[3 * static_cast<size_t>(j) + 1] = to_d(tr * my + tt[1]);
-      tij[3 * static_cast<size_t>(j) + 2] = to_d(tr * mz + tt[2]);
     }
     if (t == 0) {
       // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749), in the
@@ -1504,5 +1534,6 @@ size_t b3_fe_smem(const DeviceModel& m, int nw) {
 template <class R, class D>
 size_t forces_fe_smem() {
   return sizeof(C<R>) * (D::NQ * D::NB + D::NQ3 * D::NRY + D::NQ + 2) +
-         sizeof(R) * 64 * (D::NB + 2 * D::NR + 2 * D::NMF) + sizeof(C<R>) * 64 * (D::LSA * 4 + D::H2) + 64;
+         sizeof(R) * 64 * (D::NB + 2 * D::NR + 2 * D::NMF) + sizeof(C<R>) * 64 * (D::LSA * 4 + D::H2) +
+         sizeof(double) * 6 * 64 + 64;
 }

@@ -143,6 +143,28 @@ def test_small_distance_is_an_error(gpu_lib):
     assert np.all(np.isfinite(e))
 
 
+@pytest.mark.parametrize("mode", ["direct", "copy"])
+def test_neighbour_element_other_than_one_is_an_error(gpu_lib, monkeypatch, mode):
+    """The C entry serves one element (src/ace.F90:46-49): a neighbour element
+    index other than 1 is refused with MAGACE_ERR_ARGS and NaN outputs in
+    every host-access mode (the check runs while the GPU evaluates), and the
+    library stays usable."""
+    from magace import structures as S
+    from magace.lib import MagAceError
+    monkeypatch.setenv("MAGACE_HOST_ACCESS", mode)
+    nb = S.neighbor_data(S.bcc_fe_54(5), 5.0)
+    nb.occlist = nb.occlist.copy()
+    nb.occlist[7] = 2
+    out = (np.zeros(nb.natom), np.zeros(3 * nb.nei), np.zeros(3 * nb.nei), np.zeros(3 * nb.natom))
+    with pytest.raises(MagAceError) as ei:
+        gpu_lib.acelib(nb, out)
+    assert ei.value.code == 7
+    assert all(np.isnan(x).all() for x in out)
+    nb.occlist[7] = 1
+    e, *_ = gpu_lib.acelib(nb)
+    assert np.all(np.isfinite(e))
+
+
 def test_moment_beyond_cutoff_is_an_error(gpu_lib):
     """|m| >= the magnetic cutoff overruns the reference's table
     (src/radial.F90:126-157 has no upper check); here it is an error."""
