@@ -188,9 +188,9 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
                         int* force_blocks);
 
 /* The kernel variants in use, variants[4]: A basis (0 scalar, 1 packed
- * FP32x2, 2/3 the same with the bond tiles staged into shared memory by TMA
- * bulk copies on a persistent grid; 2/3 run only when the bond arrays are
- * device memory and otherwise fall back to 0/1), 2-/4-body density (0/1: 32/16 warps with per-entry loads, 2/3:
+ * FP32x2, 2 scalar with the bond tiles staged into shared memory by TMA bulk
+ * copies, 3 the same on a persistent grid; 2/3 run only when the bond arrays
+ * are device memory and otherwise fall back to 0), 2-/4-body density (0/1: 32/16 warps with per-entry loads, 2/3:
  * 32/16 warps reading record streams by shuffles, 4/5: through shared
  * memory), 3-body (0-2: 16/12/8 warps, 3: 12
  * warps with the n0' loop outermost, 4/5: 16/12 warps packed FP32x2), forces

@@ -1037,9 +1037,9 @@ int resident_grid(K* kernel, int threads, size_t smem_bytes) {
 
 // The A-basis phase: factors F, rank-1 density and core energy per atom.
 // Split-precision variants (DeviceModel::tune_abasis): 0 scalar, 1 packed
-// FP32x2, 2 and 3 the same with the bond tiles staged by TMA on a persistent
-// grid; 2 and 3 run only when the bond inputs are device memory
-// (EvalBuffers::dev_inputs), else they fall back to 0 and 1.
+// FP32x2, 2 scalar with the bond tiles staged by TMA, 3 the same on a
+// persistent grid; 2 and 3 run only when the bond inputs are device memory
+// (EvalBuffers::dev_inputs), else variant 0 runs.
 template <class R>
 void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid, bool fe) {
   const int natom = b.natom;
@@ -1047,13 +1047,13 @@ void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
     const size_t s1 = abasis_fe_smem<R, FeDims>();
     int v = 0;
     if constexpr (sizeof(R) == 4) v = m.tune_abasis;
-    if (v >= 2 && !b.dev_inputs) v -= 2;
-#define MAGACE_ABASIS(PK, TMA)                                                                                     \
+    if (v >= 2 && !b.dev_inputs) v = 0;
+#define MAGACE_ABASIS(PK, TMA, PERSIST)                                                                            \
   {                                                                                                                 \
-    const size_t sm = TMA ? ((s1 + 15) & ~static_cast<size_t>(15)) + kTileBytes : s1;                              \
+    const size_t sm = TMA ? ((s1 + 15) & ~static_cast<size_t>(15)) + kTileBarBytes : s1;                           \
     set_smem(k_abasis_fe<R, FeDims, PK, TMA>, sm);                                                                 \
     int g = grid;                                                                                                   \
-    if (TMA) {                                                                                                      \
+    if (PERSIST) {                                                                                                  \
       const int rg = resident_grid(k_abasis_fe<R, FeDims, PK, TMA>, 64, sm);                                        \
       g = natom < rg ? natom : rg;                                                                                  \
     }                                                                                                               \
@@ -1063,13 +1063,13 @@ void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
   }
     if constexpr (sizeof(R) == 4) {
       switch (v) {
-        case 1: MAGACE_ABASIS(true, false); break;
-        case 2: MAGACE_ABASIS(false, true); break;
-        case 3: MAGACE_ABASIS(true, true); break;
-        default: MAGACE_ABASIS(false, false); break;
+        case 1: MAGACE_ABASIS(true, false, false); break;
+        case 2: MAGACE_ABASIS(false, true, false); break;
+        case 3: MAGACE_ABASIS(false, true, true); break;
+        default: MAGACE_ABASIS(false, false, false); break;
       }
     } else {
-      MAGACE_ABASIS(false, false);
+      MAGACE_ABASIS(false, false, false);
     }
 #undef MAGACE_ABASIS
   } else {

@@ -16,7 +16,8 @@ constexpr int kForceThreads = 64;
 constexpr int kMaxFeat = 32;     // per-bond radial functions of one kind
 constexpr int kMaxLaunches = 4;  // kernels of one evaluation
 // variants of the split-precision A-basis kernel: scalar, packed FP32x2,
-// and both with TMA-staged bond tiles (DeviceModel::tune_abasis)
+// scalar with TMA-staged bond tiles, the same on a persistent grid
+// (DeviceModel::tune_abasis)
 constexpr int kAbasisVariants = 4;
 // warps per CTA of the split-precision density kernels, chosen by
 // DeviceModel::tune_rest / tune_b3 (ace_autotune_device picks them)

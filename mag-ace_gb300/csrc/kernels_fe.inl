@@ -125,7 +125,8 @@ __device__ __forceinline__ double tile_value(const double* sbuf, const double* g
 // m-hat[3] as FP64, each array padded to keep the next one 16-byte aligned
 constexpr int kTileR = 66, kTileE = 194;
 constexpr int kTileDoubles = 2 * kTileR + 2 * kTileE;
-constexpr size_t kTileBytes = sizeof(double) * kTileDoubles + 16;  // + the mbarrier and the tile's first bond
+constexpr size_t kTileBytes = sizeof(double) * kTileDoubles;
+constexpr size_t kTileBarBytes = 16;  // the mbarrier and the staged tile's first bond
 
 struct BondTile {
   double* r;
@@ -134,9 +135,10 @@ struct BondTile {
   double* mh;
   uint64_t* bar;
   int* first;
-  __device__ explicit BondTile(unsigned char* p)
+  // p: kTileBytes, 16-byte aligned; q: kTileBarBytes, 8-byte aligned
+  __device__ BondTile(unsigned char* p, unsigned char* q)
       : r(reinterpret_cast<double*>(p)), e(r + kTileR), mg(e + kTileE), mh(mg + kTileR),
-        bar(reinterpret_cast<uint64_t*>(mh + kTileE)), first(reinterpret_cast<int*>(bar + 1)) {}
+        bar(reinterpret_cast<uint64_t*>(q)), first(reinterpret_cast<int*>(bar + 1)) {}
   // issues the copies of bonds [j0, j0 + nb) (one thread)
   __device__ void issue(const double* rr, const double* ee, const double* magj, const double* mhj, int j0, int nb) {
     const TileWindow w0 = tile_window(rr, j0, j0 + nb), w1 = tile_window(ee, 3 * j0, 3 * (j0 + nb)),
@@ -144,6 +146,10 @@ struct BondTile {
     const uint32_t b0 = 8u * (w0.hi - w0.lo), b1 = 8u * (w1.hi - w1.lo), b2 = 8u * (w2.hi - w2.lo),
                    b3 = 8u * (w3.hi - w3.lo);
     *first = j0;
+    // the buffer was last written and read through the generic proxy (the
+    // caller passed a CTA barrier since): order those accesses before the
+    // bulk copies' writes
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(bar, b0 + b1 + b2 + b3);
     if (b0) bulk_to_smem(r + 2 * w0.h, rr + w0.lo, b0, bar);
     if (b1) bulk_to_smem(e + 2 * w1.h, ee + w1.lo, b1, bar);
@@ -170,10 +176,11 @@ __device__ __forceinline__ int2 next_atom_tile(const DeviceModel& m, const int* 
 // packed FP32x2 FMAs (warp 0: five pairs of the 18 A columns per half-row,
 // warp 1: eight pairs of the 30 A2 columns; padding pairs are discarded).
 //
-// TMA (device-resident inputs only): a persistent grid, each CTA's bond
-// tiles staged into shared memory by bulk copies (BondTile); the copy of the
-// next tile is issued as soon as the current tile's features are computed,
-// so that it overlaps the bond sums and the completion of A.
+// TMA (device-resident inputs only): each CTA's bond tiles staged into
+// shared memory by bulk copies (BondTile); the copy of the CTA's next tile
+// is issued as soon as the current tile's features are computed, so that it
+// overlaps the bond sums and the completion of A (on a persistent grid every
+// tile after a CTA's first arrives this way).
 template <class R, class D, bool PACKED, bool TMA = false>
 __global__ void __launch_bounds__(64)
     k_abasis_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
@@ -192,12 +199,16 @@ __global__ void __launch_bounds__(64)
   float* sQy = sQx + TB * 32;
   C<R>* accA = sRY;                                       // reuse after the tiles: [NRY][NQ3]
   C<R>* accA2 = accA + D::NWA;                            // [NB][NQ]
-  CSum<R> core_sum;  // thread 0: the atom's core energy, over its bond tiles
+  double core_acc = 0.0;  // warp 1: the atom's core energy, over its bond tiles
   static_assert(!PACKED || (sizeof(R) == 4 && D::H3 == D::H2 && D::NQ <= 32), "packed tiles: FP32, Fe layout");
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int row = lane >> 1, cb = lane & 1;
-  // TMA: the staged tile after the other buffers (16-byte aligned)
-  BondTile tile(smem + ((abasis_fe_smem<R, D>() + 15) & ~static_cast<size_t>(15)));
+  // TMA: the staged tile lives in the M Y tile's space (sQ), which is not
+  // read between the end of a tile's bond sums and the next tile's
+  // features; its mbarrier after the other buffers
+  static_assert(sizeof(C<R>) * D::NQ * 64 >= kTileBytes || sizeof(float) * 64 * 64 >= kTileBytes,
+                "the staged tile fits in the M Y tile");
+  BondTile tile(reinterpret_cast<unsigned char*>(sQ), smem + ((abasis_fe_smem<R, D>() + 15) & ~static_cast<size_t>(15)));
   constexpr int kIssuer = 32;  // lane 0 of warp 1 issues the copies
   uint32_t phase = 0;
   bool timed_out = false;
@@ -219,12 +230,14 @@ __global__ void __launch_bounds__(64)
     float2 accx[8], accy[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) accx[c] = accy[c] = make_float2(0.f, 0.f);
-    core_sum = CSum<R>();
+    core_acc = 0.0;
     const int b0 = off[atom], b1 = off[atom + 1];
     for (int t0 = b0; t0 < b1; t0 += TB) {
       const int nb = min(TB, b1 - t0);
       __syncthreads();
       if constexpr (TMA) {
+        // a later tile of this atom: the previous tile's bond sums are done
+        if (t0 > b0 && t == kIssuer) tile.issue(rr, ee, magj, mhj, t0, nb);
         if (!mbar_wait(tile.bar, phase)) {
           raise_error(err, kDevTimeout);
           timed_out = true;
@@ -232,11 +245,10 @@ __global__ void __launch_bounds__(64)
         }
         phase ^= 1u;
       }
+      // the bond's inputs
+      double dr = 0.0, dex = 0.0, dey = 0.0, dez = 0.0, dmg = 0.0, dmx = 0.0, dmy = 0.0, dmz = 0.0;
       if (t < nb) {
         const int j = t0 + t;
-        // the bond's inputs in the working precision; with `stage`, also
-        // kept in device memory for the force kernel (8 values per bond)
-        double dr, dex, dey, dez, dmg, dmx, dmy, dmz;
         if constexpr (TMA) {
           if (*tile.first != t0) raise_error(err, kDevShape);  // the staged tile is always this one
           const int e0 = 3 * t0, e1 = 3 * (t0 + nb);
@@ -260,6 +272,12 @@ __global__ void __launch_bounds__(64)
           dmy = mhj[3 * j + 1];
           dmz = mhj[3 * j + 2];
         }
+      }
+      if constexpr (TMA) __syncthreads();  // the staged tile is read: sQ may be written
+      if (t < nb) {
+        const int j = t0 + t;
+        // the bond's inputs in the working precision; with `stage`, also
+        // kept in device memory for the force kernel (8 values per bond)
         const R br = to_r<R>(dr);
         const R bex = to_r<R>(dex), bey = to_r<R>(dey), bez = to_r<R>(dez);
         const R bmg = to_r<R>(dmg);
@@ -327,15 +345,6 @@ __global__ void __launch_bounds__(64)
         score[t] = cv[0];
       }
       __syncthreads();
-      if constexpr (TMA) {
-        // the tile's inputs are in registers: stage the next tile
-        if (t == kIssuer) {
-          int2 nx;
-          if (t0 + TB < b1) nx = make_int2(t0 + TB, min(TB, b1 - t0 - TB));
-          else nx = next_atom_tile(m, off, it + gridDim.x, natom, TB);
-          if (nx.y > 0) tile.issue(rr, ee, magj, mhj, nx.x, nx.y);
-        }
-      }
       if constexpr (PACKED) {
         if (warp == 0) {
           // A[row][10cb .. 10cb+9] (columns 18, 19 padding)
@@ -390,10 +399,23 @@ __global__ void __launch_bounds__(64)
           }
         }
       }
-      if (t == 0)
-        for (int b = 0; b < nb; ++b) core_sum.add(score[b]);
+      if (warp == 1) {
+        double cs = (lane < nb ? static_cast<double>(score[lane]) : 0.0) +
+                    (lane + 32 < nb ? static_cast<double>(score[lane + 32]) : 0.0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cs += __shfl_xor_sync(0xffffffffu, cs, o);
+        core_acc += cs;
+      }
     }
     __syncthreads();
+    if constexpr (TMA) {
+      // the bond sums are done (sQ is free): stage the CTA's next atom's
+      // first tile while A is completed and written
+      if (b1 > b0 && t == kIssuer) {
+        const int2 nx = next_atom_tile(m, off, it + gridDim.x, natom, TB);
+        if (nx.y > 0) tile.issue(rr, ee, magj, mhj, nx.x, nx.y);
+      }
+    }
     if constexpr (PACKED) {
       if (warp == 0) {
 #pragma unroll
@@ -449,33 +471,38 @@ __global__ void __launch_bounds__(64)
       }
       Fa[m.offA2 + s] = v;
     }
-    if (t == 0) {
-      // on-site A0 and the 1-body density in the working precision
+    if (warp == 1) {
+      // on-site A0 and the 1-body density in the working precision, one
+      // magnetic function per lane: lane q < NMF holds M_q, lane NMF + n the
+      // 1-body function g_n
+      static_assert(D::NMF + D::NBM <= 32 && D::N2 * D::LS2 <= 64, "one function per lane");
       R wl = R(0);
       const int nl = magnetic_bin_r<R>(m, to_r<R>(magi[atom]), wl, err);
-      R Mv[D::NMF], gm[D::NBM], dummy[1];
-      if (nl > 0) {
-        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, wl, rscale_m<R>(m), Mv, dummy);
-        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, wl, rscale_m<R>(m), gm, dummy);
-      } else {
-        for (int q = 0; q < D::NMF; ++q) Mv[q] = R(nl == 0 ? 1 : 0);
-        for (int q = 0; q < D::NBM; ++q) gm[q] = R(nl == 0 ? 1 : 0);
-      }
+      R v = R(nl == 0 ? 1 : 0), dummy[1];
+      if (nl > 0 && lane < D::NMF + D::NBM)
+        lut_eval<false>(pick<R>(m.lut_m, m.lut_m32), D::NFM, lane, 1, nl, wl, rscale_m<R>(m), &v, dummy);
       C<R> Yi[D::H2];
       ylm_half<R, false>(D::L2, to_r<R>(mhi[3 * atom]), to_r<R>(mhi[3 * atom + 1]), to_r<R>(mhi[3 * atom + 2]), Yi,
                          nullptr);
-      for (int nr = 0; nr < D::N2; ++nr)
-        for (int l = 0; l <= D::L2; ++l)
-          for (int mm = -l; mm <= l; ++mm)
-            Fa[m.offA0 + nr * D::LS2 + l * l + l + mm] = cscale(y_full(Yi, l, mm), Mv[nr * (D::L2 + 1) + l]);
-      Fa[m.offOne] = {R(1), R(0)};
-      Fa[m.offZero] = {R(0), R(0)};
-      for (int d = 0; d < m.nd; ++d) {
-        CSum<R> s1;
-        for (int n = 0; n < D::NBM; ++n) s1.add(c1_of<R>(m, d * D::NBM + n) * (gm[n] - R(1)));
-        rho1[static_cast<size_t>(atom) * 2 + d] = s1.value();
+#pragma unroll
+      for (int k0 = 0; k0 < D::N2 * D::LS2; k0 += 32) {
+        const int k = k0 + lane;
+        const int nr = k / D::LS2, lm = k % D::LS2, l = l_of_lm(lm), mm = lm - l * l - l;
+        const R mv = __shfl_sync(0xffffffffu, v, k < D::N2 * D::LS2 ? nr * (D::L2 + 1) + l : 0);
+        if (k < D::N2 * D::LS2) Fa[m.offA0 + k] = cscale(y_full(Yi, l, mm), mv);
       }
-      core_out[atom] = core_sum.value();
+      if (lane == 0) {
+        Fa[m.offOne] = {R(1), R(0)};
+        Fa[m.offZero] = {R(0), R(0)};
+        core_out[atom] = core_acc;
+      }
+      for (int d = 0; d < m.nd; ++d) {
+        const int n = lane - D::NMF;
+        double s1 = n >= 0 && n < D::NBM ? static_cast<double>(c1_of<R>(m, d * D::NBM + n) * (v - R(1))) : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        if (lane == 0) rho1[static_cast<size_t>(atom) * 2 + d] = s1;
+      }
     }
     __syncthreads();
   }
@@ -1480,40 +1507,47 @@ __global__ void __launch_bounds__(64, MINB)
         __syncthreads();
       }
     }
-    if (t == 0) {
+    if (t >= 32) {
       // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749), in the
-      // working precision
+      // working precision, on warp 1: lane q < NMF evaluates M_q, lane
+      // NMF + n the 1-body function g_n (values and derivatives); lane k <
+      // NQ takes the on-site weight W0[k]; the terms are summed by shuffles
+      static_assert(D::NMF + D::NBM <= 32 && D::NQ <= 32, "one function and one weight per lane");
+      const int lane = t - 32;
       const R mg = to_r<R>(magi[atom]);
       const R mx = to_r<R>(mhi[3 * atom]), my = to_r<R>(mhi[3 * atom + 1]), mz = to_r<R>(mhi[3 * atom + 2]);
       R wm = R(0);
       const int nl = magnetic_bin_r<R>(m, mg, wm, err);
-      R Mv[D::NMF], Md[D::NMF], gm[D::NBM], gmd[D::NBM];
-      if (nl > 0) {
-        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, 0, D::NMF, nl, wm, rscale_m<R>(m), Mv, Md);
-        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, D::NMF, D::NBM, nl, wm, rscale_m<R>(m), gm, gmd);
-      } else {
-        for (int q = 0; q < D::NMF; ++q) {
-          Mv[q] = R(nl == 0 ? 1 : 0);
-          Md[q] = R(0);
-        }
-        for (int q = 0; q < D::NBM; ++q) gmd[q] = R(0);
-      }
+      R v = R(nl == 0 ? 1 : 0), dv = R(0);
+      if (nl > 0 && lane < D::NMF + D::NBM)
+        lut_eval<true>(pick<R>(m.lut_m, m.lut_m32), D::NFM, lane, 1, nl, wm, rscale_m<R>(m), &v, &dv);
       C<R> Yh[D::H2], dYh[D::H2][3];
       ylm_half<R, true>(D::L2, mx, my, mz, Yh, dYh);
       R tr = R(0), tt[3] = {R(0), R(0), R(0)};
-      const R dE = to_r<R>(dedrho[static_cast<size_t>(atom) * 2]);
-      for (int n = 0; n < D::NBM; ++n) tr += dE * c1_of<R>(m, n) * gmd[n];
-      const R invm = rcp(mg);
-      for (int k = 0; k < D::NQ; ++k) {
-        const int nr = k / D::H2, h = k % D::H2, q = nr * (D::L2 + 1) + l_of_h(h);
+      const int n = lane - D::NMF;
+      if (n >= 0 && n < D::NBM) tr = to_r<R>(dedrho[static_cast<size_t>(atom) * 2]) * c1_of<R>(m, n) * dv;
+      const int k = lane < D::NQ ? lane : 0;
+      const int nr = k / D::H2, h = k % D::H2, q = nr * (D::L2 + 1) + l_of_h(h);
+      const R Mq = __shfl_sync(0xffffffffu, v, q), Mdq = __shfl_sync(0xffffffffu, dv, q);
+      if (lane < D::NQ) {
         const C<R> w = W0s[k];
-        tr += Md[q] * re_mul(w, Yh[h]);
-        const R sc = invm * Mv[q];
+        const R invm = rcp(mg);
+        tr += Mdq * re_mul(w, Yh[h]);
+        const R sc = invm * Mq;
+#pragma unroll
         for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(w, dYh[h][c]);
       }
-      ti0[3 * static_cast<size_t>(atom) + 0] = to_d(tr * mx + tt[0]);
-      ti0[3 * static_cast<size_t>(atom) + 1] = to_d(tr * my + tt[1]);
-      ti0[3 * static_cast<size_t>(atom) + 2] = to_d(tr * mz + tt[2]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        tr += __shfl_xor_sync(0xffffffffu, tr, o);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) tt[c] += __shfl_xor_sync(0xffffffffu, tt[c], o);
+      }
+      if (lane == 0) {
+        ti0[3 * static_cast<size_t>(atom) + 0] = to_d(tr * mx + tt[0]);
+        ti0[3 * static_cast<size_t>(atom) + 1] = to_d(tr * my + tt[1]);
+        ti0[3 * static_cast<size_t>(atom) + 2] = to_d(tr * mz + tt[2]);
+      }
     }
     __syncthreads();
   }

@@ -100,7 +100,7 @@ def test_error_codes(lib, tmp_path, seeded_potential):
     assert lib.get_tuning_indices() == before
     lib.set_tuning([3, 5, 5, 5])
     assert lib.get_tuning_indices() == [3, 5, 5, 5]
-    assert lib.get_tuning()["abasis"] == "packed FP32x2, TMA-staged bond tiles"
+    assert lib.get_tuning()["abasis"] == "scalar, TMA-staged bond tiles, persistent grid"
     lib.set_tuning(before)
 
 
