@@ -1000,21 +1000,22 @@ B3Split b3_split(int nblk, int grid_cap) {
 }
 
 // The split-precision scratch (EvalBuffers::aux): rho_rest[natom] doubles,
-// then the 3-body split tail's accumulators for up to min(blocks, SMs) tail
-// blocks: rho3[tail][32] doubles, tickets[tail] ints, g[tail][nc][32][2]
-// floats (each part 256-byte aligned).
+// then one record per tail block of the 3-body kernel's split tail (up to
+// min(blocks, SMs) records, 256-byte aligned): rho3[32] doubles, a ticket
+// (padded to 16 bytes) and the gradients g[nc][32][2] floats. The records in
+// use are zeroed before each evaluation that splits.
 struct AuxLayout {
-  size_t rho3, tickets, gacc, end;
+  size_t tail0, rec;  // first record, bytes per record
+  size_t end;
 };
 AuxLayout aux_layout(const DeviceModel& m, int natom) {
   const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
   const int nblk = (natom + 31) / 32;
   const size_t ntail = static_cast<size_t>(std::min(nblk, sm_count()));
   AuxLayout L;
-  L.rho3 = up(sizeof(double) * static_cast<size_t>(natom));
-  L.tickets = L.rho3 + up(sizeof(double) * 32 * ntail);
-  L.gacc = L.tickets + up(sizeof(int) * ntail);
-  L.end = L.gacc + up(sizeof(float) * 64 * static_cast<size_t>(m.b3_nc) * ntail);
+  L.tail0 = up(sizeof(double) * static_cast<size_t>(natom));
+  L.rec = up(kTailG + sizeof(float) * 64 * static_cast<size_t>(m.b3_nc));
+  L.end = L.tail0 + L.rec * ntail;
   return L;
 }
 
@@ -1098,8 +1099,8 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const int rw = kRestWarpChoices[m.tune_rest], bw = kB3WarpChoices[m.tune_b3];
       (void)bw;
       const size_t s2 = density_fe_smem(m, rw);
-#define MAGACE_REST(NW, SM)                         \
-  set_smem(k_density_fe<FeDims, NW, SM>, s2);       \
+#define MAGACE_REST(NW, SM)                                                                                   \
+  set_smem(k_density_fe<FeDims, NW, SM>, s2);                                                                 \
   k_density_fe<FeDims, NW, SM><<<gb, NW * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest)
       // variants: 32 or 16 warps; per-entry uniform loads, record streams
       // broadcast by shuffles, or record streams through shared memory
@@ -1114,19 +1115,18 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
 #undef MAGACE_REST
       if (ev_between) cudaEventRecord(ev_between, st);
       const size_t sb = b3_fe_smem<FeDims>(m, bw);
-      // the last partial wave split by task range (B3Split); its
-      // accumulators and tickets start at zero
+      // the last partial wave split by task range (B3Split); the records of
+      // the tail blocks start at zero
       const B3Split sp = b3_split(nblk, grid_cap);
       const AuxLayout al = aux_layout(m, natom);
-      unsigned char* auxb = static_cast<unsigned char*>(b.aux);
-      if (sp.parts > 1) cudaMemsetAsync(auxb + al.rho3, 0, al.end - al.rho3, st);
+      unsigned char* tails = static_cast<unsigned char*>(b.aux) + al.tail0;
+      if (sp.parts > 1) cudaMemsetAsync(tails, 0, al.rec * sp.ntail, st);
       const int g3 = sp.parts > 1 ? sp.nfull + sp.ntail * sp.parts : gb;
 #define MAGACE_B3(NW, LOOP)                                                                                  \
   set_smem(k_b3_fe<FeDims, NW, LOOP>, sb);                                                                   \
   k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(                                                        \
-      m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy, b.edf, b.dedrho, b.err, sp.nfull, sp.parts,      \
-      reinterpret_cast<double*>(auxb + al.rho3), reinterpret_cast<float*>(auxb + al.gacc),                   \
-      reinterpret_cast<int*>(auxb + al.tickets))
+      m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy, b.edf, b.dedrho, b.err, sp.nfull, sp.parts, tails, \
+      al.rec)
       // variants: (16 warps, n0' innermost), (12, innermost), (8, innermost),
       // (12, n0' outermost), (16, packed FP32x2), (12, packed FP32x2)
       switch (m.tune_b3) {

@@ -18,6 +18,10 @@
 //   k_forces_fe  per bond, U = W_A Q and V = W2 g + W_A^T RY with the
 //                weights transposed in shared memory for 16-byte loads.
 
+// byte offsets in a split tail block's record of accumulators (aux_layout):
+// 3-body density [32] doubles, ticket, 3-body gradients [nc][32][2] floats
+constexpr size_t kTailRho3 = 0, kTailTickets = 256, kTailG = 272;
+
 template <int NA_, int LA_, int NM_, int LM_, int NB_, int N2_, int L2_, int NBM_>
 struct Dims {
   static constexpr int NA = NA_, LA = LA_, NM = NM_, LM = LM_, NB = NB_, N2 = N2_, L2 = L2_, NBM = NBM_;
@@ -939,17 +943,17 @@ __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const 
 // Split tail (parts > 1, one CTA per block): CTAs below `nfull` evaluate
 // their block whole. The remaining blocks, the last partial wave of one CTA
 // per SM, are each divided among `parts` CTAs by task range. Each such CTA
-// adds its 3-body density into rho3_acc[tail][32] and its gradients into
-// g_acc[tail][nc][32] (re, im) with global atomics, then takes a ticket; the
-// CTA that takes the last ticket loads the totals and completes the block
-// (embedding, final weights). No CTA waits on another. The accumulators and
-// tickets are zeroed before the launch.
+// adds its 3-body density and its gradients [nc][32] (re, im) into the tail
+// block's record in `tails` (tail_rec bytes per block) with global atomics,
+// then takes a ticket; the CTA that takes the last ticket loads the totals
+// and completes the block (embedding, final weights). No CTA waits on
+// another. The records are zeroed before the launch.
 template <class D, int NW, int LOOP>
 __global__ void __launch_bounds__(NW * 32, 1)
     k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
             const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
             double* __restrict__ energy, double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err,
-            int nfull, int parts, double* __restrict__ rho3_acc, float* __restrict__ g_acc, int* __restrict__ tickets) {
+            int nfull, int parts, unsigned char* __restrict__ tails, size_t tail_rec) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
   const int nc = m.b3_nc, nW = m.nW;
@@ -1059,12 +1063,14 @@ __global__ void __launch_bounds__(NW * 32, 1)
     __syncthreads();
     if (tail >= 0) {
       // split tail: add this part into the block's accumulators
+      unsigned char* rec = tails + tail * tail_rec;
+      double* rho3_acc = reinterpret_cast<double*>(rec + kTailRho3);
       if (warp == 0 && lane < na) {
         double r3 = 0.0;
         for (int w = 0; w < NW; ++w) r3 += rpart[w * 32 + lane];
-        atomicAdd(rho3_acc + tail * 32 + lane, r3);
+        atomicAdd(rho3_acc + lane, r3);
       }
-      float* ga = g_acc + static_cast<size_t>(tail) * nc * 64;
+      float* ga = reinterpret_cast<float*>(rec + kTailG);
       for (int q = threadIdx.x; q < nc * 32; q += blockDim.x) {
         const int c = q >> 5, a = q & 31;
         if (a < na) {
@@ -1075,7 +1081,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
       }
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) s_last = atomicAdd(tickets + tail, 1) == parts - 1;
+      if (threadIdx.x == 0) s_last = atomicAdd(reinterpret_cast<int*>(rec + kTailTickets), 1) == parts - 1;
       __syncthreads();
       if (!s_last) break;  // another part completes the block
       __threadfence();
@@ -1085,7 +1091,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
         Gs[c * kB3Stride + a] = {__ldcg(ga + 2 * q), __ldcg(ga + 2 * q + 1)};
       }
       for (int q = threadIdx.x; q < NW * 32; q += blockDim.x)
-        rpart[q] = q < 32 ? __ldcg(rho3_acc + tail * 32 + q) : 0.0;
+        rpart[q] = q < 32 ? __ldcg(rho3_acc + q) : 0.0;
       __syncthreads();
     }
     // finish the atoms, one per lane of warp 0
