@@ -1000,8 +1000,8 @@ B3Split b3_split(int nblk, int grid_cap) {
 }
 
 // The split-precision scratch (EvalBuffers::aux): rho_rest[natom] doubles,
-// then one record per tail block of the 3-body kernel's split tail (up to
-// min(blocks, SMs) records, 256-byte aligned): rho3[32] doubles, a ticket
+// then one record per tail block of the 3-body kernel's split tail (the
+// blocks B3Split divides, 256-byte aligned): rho3[32] doubles, a ticket
 // (padded to 16 bytes) and the gradients g[nc][32][2] floats. The records in
 // use are zeroed before each evaluation that splits.
 struct AuxLayout {
@@ -1011,7 +1011,8 @@ struct AuxLayout {
 AuxLayout aux_layout(const DeviceModel& m, int natom) {
   const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
   const int nblk = (natom + 31) / 32;
-  const size_t ntail = static_cast<size_t>(std::min(nblk, sm_count()));
+  const B3Split sp = b3_split(nblk, nblk);  // as if every block had its own CTA
+  const size_t ntail = sp.parts > 1 ? static_cast<size_t>(sp.ntail) : 0;
   AuxLayout L;
   L.tail0 = up(sizeof(double) * static_cast<size_t>(natom));
   L.rec = up(kTailG + sizeof(float) * 64 * static_cast<size_t>(m.b3_nc));
