@@ -89,6 +89,65 @@ __device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_
                "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
 }
+// L2 eviction priorities for single loads and stores: the weights the
+// 3-body kernel writes are kept (evict-last) for the force kernel, which
+// reads them once (evict-first), as does the 3-body kernel its factors
+__device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_l2(C<float>* a, C<float> v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(__cvta_generic_to_global(a)), "f"(v.x),
+               "f"(v.y), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ C<float> ld_l2(const C<float>* a, uint64_t pol) {
+  C<float> v;
+  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+               : "=f"(v.x), "=f"(v.y)
+               : "l"(__cvta_generic_to_global(a)), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ C<double> ld_l2(const C<double>* a, uint64_t pol) {
+  C<double> v;
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y)
+               : "l"(__cvta_generic_to_global(a)), "l"(pol));
+  return v;
+}
+
+// one bond's 8 inputs in the working precision, with an L2 policy
+__device__ __forceinline__ void st8_l2(float* a, const float* v, uint64_t pol) {
+  const size_t g = __cvta_generic_to_global(a);
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(g), "f"(v[0]), "f"(v[1]),
+               "f"(v[2]), "f"(v[3]), "l"(pol)
+               : "memory");
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(g + 16), "f"(v[4]), "f"(v[5]),
+               "f"(v[6]), "f"(v[7]), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st8_l2(double* a, const double* v, uint64_t) {
+  for (int q = 0; q < 8; ++q) a[q] = v[q];
+}
+__device__ __forceinline__ void ld8_l2(const float* a, float* v, uint64_t pol) {
+  const size_t g = __cvta_generic_to_global(a);
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+               : "l"(g), "l"(pol));
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+               : "l"(g + 16), "l"(pol));
+}
+__device__ __forceinline__ void ld8_l2(const double* a, double* v, uint64_t) {
+  for (int q = 0; q < 8; ++q) v[q] = a[q];
+}
+
 // a bulk prefetch of [src, src + bytes) into L2 (16-byte aligned, 16-byte multiple)
 __device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
@@ -287,15 +346,8 @@ __global__ void __launch_bounds__(64)
         const R bmg = to_r<R>(dmg);
         const R bmx = to_r<R>(dmx), bmy = to_r<R>(dmy), bmz = to_r<R>(dmz);
         if (stage) {
-          R* sp = stage + 8 * static_cast<size_t>(j);
-          sp[0] = br;
-          sp[1] = bex;
-          sp[2] = bey;
-          sp[3] = bez;
-          sp[4] = bmg;
-          sp[5] = bmx;
-          sp[6] = bmy;
-          sp[7] = bmz;
+          const R sv[8] = {br, bex, bey, bez, bmg, bmx, bmy, bmz};
+          st8_l2(stage + 8 * static_cast<size_t>(j), sv, l2_evict_last());  // kept in L2 for the force kernel
         }
         R g[D::NB], Rv[D::NR], Mv[D::NMF], cv[1], dummy[1];
         R wl = R(0);
@@ -969,6 +1021,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
   __shared__ int s_atom[32];                                       // the block's atoms
   __shared__ int s_next;                                           // next task to take
   __shared__ int s_last;                                           // split tail: this CTA completes the block
+  const uint64_t pol_first = l2_evict_first(), pol_last = l2_evict_last();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (natom + 31) / 32;
   // this CTA's blocks and task range
@@ -1014,7 +1067,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
         C<float> v[kBatch];
 #pragma unroll
         for (int b = 0; b < kBatch; ++b)
-          v[b] = ab + b < na ? F[static_cast<size_t>(s_atom[ab + b]) * m.nF + fc] : C<float>{0.f, 0.f};
+          v[b] = ab + b < na ? ld_l2(F + static_cast<size_t>(s_atom[ab + b]) * m.nF + fc, pol_first) : C<float>{0.f, 0.f};
 #pragma unroll
         for (int b = 0; b < kBatch; ++b) {
           Xs[c * kB3Stride + ab + b] = v[b];
@@ -1136,7 +1189,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
               v[b].y += mu * gv.y;
             }
             const float sc = s_dE[a];
-            W[static_cast<size_t>(s_atom[a]) * nW + w] = {v[b].x * sc, v[b].y * sc};
+            st_l2(W + static_cast<size_t>(s_atom[a]) * nW + w, {v[b].x * sc, v[b].y * sc}, pol_last);
           }
         }
       }
@@ -1200,13 +1253,14 @@ __global__ void __launch_bounds__(64, MINB)
   float* W2y = W2x + D::NQ * D::NB;
   float* WAx = reinterpret_cast<float*>(WAT);
   float* WAy = WAx + D::NQ3 * D::NRY;
+  const uint64_t pol_first = l2_evict_first();  // the weights are read once
 
   for (int it = blockIdx.x; it < natom; it += gridDim.x) {
     const int atom = queue_atom(m, it);
     const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
     for (int s = t; s < D::NA2H; s += T) {  // W2[n][k] -> W2T[k][n]
       const int n = s / D::NQ, k = s % D::NQ;
-      const C<R> w = Wa[m.offW2 + s];
+      const C<R> w = ld_l2(Wa + m.offW2 + s, pol_first);
       if constexpr (PACKED) {
         W2x[k * D::NB + n] = w.x;
         W2y[k * D::NB + n] = w.y;
@@ -1216,7 +1270,7 @@ __global__ void __launch_bounds__(64, MINB)
     }
     for (int s = t; s < D::NWA; s += T) {   // WA[i][k3] -> WAT[k3][i]
       const int i = s / D::NQ3, k3 = s % D::NQ3;
-      const C<R> w = Wa[s];
+      const C<R> w = ld_l2(Wa + s, pol_first);
       if constexpr (PACKED) {
         WAx[k3 * D::NRY + i] = w.x;
         WAy[k3 * D::NRY + i] = w.y;
@@ -1224,7 +1278,7 @@ __global__ void __launch_bounds__(64, MINB)
         WAT[k3 * D::NRY + i] = w;
       }
     }
-    for (int s = t; s < D::NQ; s += T) W0s[s] = Wa[m.offW0 + s];
+    for (int s = t; s < D::NQ; s += T) W0s[s] = ld_l2(Wa + m.offW0 + s, pol_first);
     __syncthreads();
     const R edf = to_r<R>(edf_in[atom]);
     const int b0 = off[atom], b1 = off[atom + 1];
@@ -1235,7 +1289,8 @@ __global__ void __launch_bounds__(64, MINB)
       if (j < b1) {
         R r, ex, ey, ez, mg, mx, my, mz;
         if (stage) {  // the A-basis kernel's copy in device memory
-          const R* sp = stage + 8 * static_cast<size_t>(j);
+          R sp[8];
+          ld8_l2(stage + 8 * static_cast<size_t>(j), sp, pol_first);
           r = sp[0];
           ex = sp[1];
           ey = sp[2];
