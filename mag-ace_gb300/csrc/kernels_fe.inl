@@ -152,6 +152,24 @@ __device__ __forceinline__ void ld8_l2(const double* a, double* v, uint64_t) {
 __device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
+// L2 prefetch of atom slot `a` of 32-atom block `b`'s row of an [atom][row]
+// array (the row's whole 16-byte units, so nothing past the array is touched)
+__device__ __forceinline__ void prefetch_row(const DeviceModel& m, int natom, const void* base, size_t row_bytes, int b,
+                                             int a) {
+  if (b * 32 + a >= natom) return;
+  const int atom = queue_atom(m, b * 32 + a);
+  const uintptr_t p0 = reinterpret_cast<uintptr_t>(base) + row_bytes * static_cast<size_t>(atom);
+  const uintptr_t lo = (p0 + 15) & ~static_cast<uintptr_t>(15), hi = (p0 + row_bytes) & ~static_cast<uintptr_t>(15);
+  if (hi > lo) bulk_prefetch_l2(reinterpret_cast<const void*>(lo), static_cast<uint32_t>(hi - lo));
+}
+// Blocks between this CTA's block and the next one to start on this SM, for
+// a kernel of one CTA per SM: the grid stride on a persistent grid, else
+// the SM count (CTAs start in block order as SMs free up)
+__device__ __forceinline__ int next_stride() {
+  unsigned nsm;
+  asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+  return gridDim.x <= nsm ? static_cast<int>(gridDim.x) : static_cast<int>(nsm);
+}
 __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   uint32_t done;
   asm volatile(
@@ -650,6 +668,8 @@ __global__ void __launch_bounds__(NW * 32, 1)
       }
     }
     __syncthreads();
+    // the factors of the block that follows this one on the SM, into L2
+    if (warp == NW - 1) prefetch_row(m, natom, F, sizeof(C<float>) * m.nF, blk + next_stride(), lane);
     const int atom = lane < na ? s_atom[lane] : -1;
     double rloc = 0.0;
     if constexpr (STREAM > 0) {
@@ -1036,16 +1056,6 @@ __global__ void __launch_bounds__(NW * 32, 1)
       task1 = m.b3_ntask * (p + 1) / parts;
     }
   }
-  // bulk L2 prefetch of the rows of atom slot `a` of block `b` (whole
-  // 16-byte units inside the row, so that nothing past the array is touched)
-  const auto prefetch_rows = [&](const void* base, size_t row_bytes, int b, int a) {
-    if (b * 32 + a >= natom) return;
-    const int atom = queue_atom(m, b * 32 + a);
-    const uintptr_t p0 = reinterpret_cast<uintptr_t>(base) + row_bytes * static_cast<size_t>(atom);
-    const uintptr_t lo = (p0 + 15) & ~static_cast<uintptr_t>(15), hi = (p0 + row_bytes) & ~static_cast<uintptr_t>(15);
-    if (hi > lo) bulk_prefetch_l2(reinterpret_cast<const void*>(lo), static_cast<uint32_t>(hi - lo));
-  };
-
   for (int t = threadIdx.x; t < ncoef / 4; t += blockDim.x)
     reinterpret_cast<float4*>(Cs)[t] = __ldg(reinterpret_cast<const float4*>(m.b3_Cf) + t);
   for (int c = threadIdx.x; c < nc; c += blockDim.x) {
@@ -1077,11 +1087,8 @@ __global__ void __launch_bounds__(NW * 32, 1)
     }
     __syncthreads();
     // while the tasks run: this block's weights (read by the final phase)
-    // and the factors of this CTA's next block, if any, into L2
-    if (warp == NW - 1) {
-      prefetch_rows(W, sizeof(C<float>) * nW, blk, lane);
-      prefetch_rows(F, sizeof(C<float>) * m.nF, blk + gridDim.x, lane);
-    }
+    // into L2 (prefetching the next block's factors as well measured slower)
+    if (warp == NW - 1) prefetch_row(m, natom, W, sizeof(C<float>) * nW, blk, lane);
     double rloc = 0.0;
     // tasks from a shared counter (dynamic balance between the warps)
     int tk = task0 + warp;
