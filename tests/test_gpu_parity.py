@@ -261,6 +261,38 @@ def test_host_access_modes_agree(gpu_lib, monkeypatch, mode):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_direct_mode_outputs_at_any_alignment(gpu_lib, monkeypatch, precision):
+    """acelib_ writing the caller's arrays directly stores each bond tile's
+    outputs as 16-byte lines: output arrays that start 8 bytes past a 16-byte
+    boundary, atoms of two 64-bond tiles and an atom without bonds give the
+    same results as plain copies, bit for bit."""
+    from magace import structures as S
+    st = _ragged_slab()
+    st = S.Structure(np.vstack([st.positions, [[1.0, 1.0, 90.0]]]), st.cell, st.pbc, np.append(st.mag, 2.0),
+                     np.vstack([st.mhat, [[0.0, 0.0, 1.0]]]))
+    nb = S.neighbor_data(st, 8.4)
+    gpu_lib.set_precision(precision)
+    try:
+        monkeypatch.setenv("MAGACE_HOST_ACCESS", "copy")
+        ref = gpu_lib.acelib(nb)
+        monkeypatch.setenv("MAGACE_HOST_ACCESS", "direct")
+        for shift in (0, 1):
+            bufs = [np.full(n + 1, 7.0) for n in (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)]
+            out = tuple(b[shift:shift + n] for b, n in zip(bufs, (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)))
+            got = gpu_lib.acelib(nb, out)
+            for x, y in zip(got, ref):
+                if precision == 0:
+                    assert np.array_equal(x, y)
+                else:
+                    assert rel_err(x, y) < 1e-6
+            for b, n in zip(bufs, (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)):
+                # nothing outside the caller's arrays is written
+                assert b[n if shift == 0 else 0] == 7.0
+    finally:
+        gpu_lib.set_precision(0)
+
+
 def test_autotuner_keeps_results(gpu_lib, oracle_seeded):
     """The autotuner times every density-kernel variant and keeps one; the
     split results stay within the split tolerance of the oracle."""
