@@ -1096,6 +1096,7 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const int nblk = (natom + 31) / 32;
       const int gb = nblk < grid_cap ? nblk : grid_cap;
       const auto* Fp = reinterpret_cast<const C<float>*>(b.F);
+      auto* Fw = reinterpret_cast<C<float>*>(b.F);  // the 3-body kernel leaves its gradients there
       auto* Wp = reinterpret_cast<C<float>*>(b.W);
       const int rw = kRestWarpChoices[m.tune_rest], bw = kB3WarpChoices[m.tune_b3];
       (void)bw;
@@ -1125,9 +1126,8 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const int g3 = sp.parts > 1 ? sp.nfull + sp.ntail * sp.parts : gb;
 #define MAGACE_B3(NW, LOOP)                                                                                  \
   set_smem(k_b3_fe<FeDims, NW, LOOP>, sb);                                                                   \
-  k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(                                                        \
-      m, natom, Fp, Wp, b.rho1, rho_rest, b.core, b.energy, b.edf, b.dedrho, b.err, sp.nfull, sp.parts, tails, \
-      al.rec)
+  k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(m, natom, Fw, b.rho1, rho_rest, b.core, b.energy, b.edf,    \
+                                                     b.dedrho, b.err, sp.nfull, sp.parts, tails, al.rec)
       // variants: (16 warps, n0' innermost), (12, innermost), (8, innermost),
       // (12, n0' outermost), (16, packed FP32x2), (12, packed FP32x2)
       switch (m.tune_b3) {
@@ -1171,13 +1171,16 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
     const size_t s3 = forces_fe_smem<R, FeDims>();
+    // split precision: the 3-body kernel left its part of the weights in F
+    const C<float>* g3 = sizeof(R) == 4 ? reinterpret_cast<const C<float>*>(b.F) : nullptr;
     // outputs in host memory (acelib_ writing the caller's arrays directly):
     // the variants that store each tile's outputs as whole lines
 #define MAGACE_FORCES_SO(MB, PK, SO)                                                                                \
   set_smem(k_forces_fe<R, FeDims, MB, PK, SO>, s3);                                                                 \
   k_forces_fe<R, FeDims, MB, PK, SO><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,  \
                                                            reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho,      \
-                                                           b.fij, b.tij, b.ti0, static_cast<const R*>(b.stage), b.err)
+                                                           b.fij, b.tij, b.ti0, static_cast<const R*>(b.stage), b.err, \
+                                                           g3)
 #define MAGACE_FORCES(MB, PK)                 \
   if (b.host_outputs) {                       \
     MAGACE_FORCES_SO(MB, PK, true);           \

@@ -641,6 +641,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
   static_assert(kRestTableWarps % NW == 0, "the slot schedule is dealt to kRestTableWarps warps");
   extern __shared__ __align__(16) unsigned char smem[];
   const int nf = m.r_nfac, nW = m.nW;
+  const uint64_t pol_last = l2_evict_last();  // the weights are read by the force kernel
   const GatherView& g = m.g2;  // slot weights and multiplicities (same slot numbering)
   C<float>* Fs = reinterpret_cast<C<float>*>(smem);                   // [nf][33]
   double* rpart = reinterpret_cast<double*>(Fs + nf * kRestStride);   // [NW][32]
@@ -710,7 +711,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
               }
               if (w >= 0 && atom >= 0) {
                 const float mu = __uint_as_float(rx);
-                W[static_cast<size_t>(atom) * nW + w] = {vx * mu, vy * mu};
+                st_l2(W + static_cast<size_t>(atom) * nW + w, {vx * mu, vy * mu}, pol_last);
               }
               vx = vy = 0.f;
             } else {
@@ -741,7 +742,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
           const int w = __ldg(g.slot_weight + s);
           if (w >= 0 && atom >= 0) {
             const float mu = __ldg(g.slot_multf + s);
-            W[static_cast<size_t>(atom) * nW + w] = {vx * mu, vy * mu};
+            st_l2(W + static_cast<size_t>(atom) * nW + w, {vx * mu, vy * mu}, pol_last);
           }
         }
     }
@@ -1022,22 +1023,19 @@ __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const 
 // another. The records are zeroed before the launch.
 template <class D, int NW, int LOOP>
 __global__ void __launch_bounds__(NW * 32, 1)
-    k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ W,
-            const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
+    k_b3_fe(DeviceModel m, int natom, C<float>* F, const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
             double* __restrict__ energy, double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err,
             int nfull, int parts, unsigned char* __restrict__ tails, size_t tail_rec) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
-  const int nc = m.b3_nc, nW = m.nW;
+  const int nc = m.b3_nc;
   const int ncoef = m.b3_ncombo * NM * I * I;
   float* Cs = reinterpret_cast<float*>(smem);
   C<float>* Xs = reinterpret_cast<C<float>*>(Cs + ((ncoef + 3) & ~3));
   C<float>* Gs = Xs + nc * kB3Stride;
   double* rpart = reinterpret_cast<double*>(Gs + nc * kB3Stride);  // [NW][32]
-  float* s_dE = reinterpret_cast<float*>(rpart + NW * 32);        // [32]
-  float* s_mult = s_dE + 32;                                       // [nc]
+  float* s_mult = reinterpret_cast<float*>(rpart + NW * 32);      // [nc]
   int* s_fac = reinterpret_cast<int*>(s_mult + nc);                // [nc]
-  int* s_cw = s_fac + nc;                                          // [nW]
   __shared__ int s_atom[32];                                       // the block's atoms
   __shared__ int s_next;                                           // next task to take
   __shared__ int s_last;                                           // split tail: this CTA completes the block
@@ -1062,7 +1060,6 @@ __global__ void __launch_bounds__(NW * 32, 1)
     s_mult[c] = __ldg(m.b3_mult + c);
     s_fac[c] = __ldg(m.b3_factor + c);
   }
-  for (int w = threadIdx.x; w < nW; w += blockDim.x) s_cw[w] = __ldg(m.b3_cw + w);
   __syncthreads();
   for (int blk = blk_first; blk < nblk; blk += blk_stride) {
     const int a0 = blk * 32;
@@ -1086,9 +1083,6 @@ __global__ void __launch_bounds__(NW * 32, 1)
       }
     }
     __syncthreads();
-    // while the tasks run: this block's weights (read by the final phase)
-    // into L2 (prefetching the next block's factors as well measured slower)
-    if (warp == NW - 1) prefetch_row(m, natom, W, sizeof(C<float>) * nW, blk, lane);
     double rloc = 0.0;
     // tasks from a shared counter (dynamic balance between the warps)
     int tk = task0 + warp;
@@ -1174,31 +1168,18 @@ __global__ void __launch_bounds__(NW * 32, 1)
       edf_out[atom] = dfcut * Fd + 1.0;
       dedrho_out[static_cast<size_t>(atom) * 2] = fcut * dFd;
       energy[atom] = fcut * Fd + e;
-      s_dE[lane] = d2f(fcut * dFd);
     }
     __syncthreads();
-    // final weights: thread w takes weight w of every atom, kBatch atoms in flight
-    for (int w = threadIdx.x; w < nW; w += blockDim.x) {
-      const int c = s_cw[w];
-      const float mu = c >= 0 ? s_mult[c] : 0.f;
-      for (int ab = 0; ab < na; ab += kBatch) {
-        C<float> v[kBatch];
-#pragma unroll
-        for (int b = 0; b < kBatch; ++b)
-          if (ab + b < na) v[b] = W[static_cast<size_t>(s_atom[ab + b]) * nW + w];
-#pragma unroll
-        for (int b = 0; b < kBatch; ++b) {
-          const int a = ab + b;
-          if (a < na) {
-            if (c >= 0) {
-              const C<float> gv = Gs[c * kB3Stride + a];
-              v[b].x += mu * gv.x;
-              v[b].y += mu * gv.y;
-            }
-            const float sc = s_dE[a];
-            st_l2(W + static_cast<size_t>(s_atom[a]) * nW + w, {v[b].x * sc, v[b].y * sc}, pol_last);
-          }
-        }
+    // the block's 3-body gradients times their multiplicities, into the
+    // factor rows of its atoms (nothing reads F after this kernel): the
+    // force kernel assembles W = dE/drho (W_rest + g3) from them; atom-major,
+    // so that consecutive threads store consecutive elements of one row
+    for (int q = threadIdx.x; q < nc * 32; q += blockDim.x) {
+      const int a = q / nc, c = q - a * nc;
+      if (a < na) {
+        const C<float> gv = Gs[c * kB3Stride + a];
+        const float mu = s_mult[c];
+        st_l2(F + static_cast<size_t>(s_atom[a]) * m.nF + c, {mu * gv.x, mu * gv.y}, pol_last);
       }
     }
     __syncthreads();
@@ -1236,7 +1217,8 @@ __global__ void __launch_bounds__(64, MINB)
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
                 const double* __restrict__ magi, const double* __restrict__ mhi, const C<R>* __restrict__ W,
                 const double* __restrict__ edf_in, const double* __restrict__ dedrho, double* __restrict__ fij,
-                double* __restrict__ tij, double* __restrict__ ti0, const R* __restrict__ stage, int* err) {
+                double* __restrict__ tij, double* __restrict__ ti0, const R* __restrict__ stage, int* err,
+                const C<float>* __restrict__ g3) {
   constexpr int T = 64;
   extern __shared__ __align__(16) unsigned char smem[];
   C<R>* W2T = reinterpret_cast<C<R>*>(smem);   // [NQ][NB]
@@ -1265,9 +1247,32 @@ __global__ void __launch_bounds__(64, MINB)
   for (int it = blockIdx.x; it < natom; it += gridDim.x) {
     const int atom = queue_atom(m, it);
     const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    // with g3 (split path, Fe layout): W holds the 2-/4-body part of the
+    // unscaled weights and g3 the 3-body part per compact element (the
+    // 3-body kernel's output in F's rows); the weight is dE/drho (W + g3)
+    const C<float>* Ga = g3 ? g3 + static_cast<size_t>(atom) * m.nF : nullptr;
+    const R sc = g3 ? to_r<R>(dedrho[static_cast<size_t>(atom) * 2]) : R(1);
+    // weight w with its 3-body element c (-1: none); the A weights are the
+    // first compact elements in the same order (c = w), the 2-body weights
+    // have none, the on-site ones are looked up
+    const auto weight = [&](int w, int c) {
+      C<R> v = ld_l2(Wa + w, pol_first);
+      if constexpr (sizeof(R) == 4) {
+        if (Ga) {
+          if (c >= 0) {
+            const C<float> gv = ld_l2(Ga + c, pol_first);
+            v.x += gv.x;
+            v.y += gv.y;
+          }
+          v.x *= sc;
+          v.y *= sc;
+        }
+      }
+      return v;
+    };
     for (int s = t; s < D::NA2H; s += T) {  // W2[n][k] -> W2T[k][n]
       const int n = s / D::NQ, k = s % D::NQ;
-      const C<R> w = ld_l2(Wa + m.offW2 + s, pol_first);
+      const C<R> w = weight(m.offW2 + s, -1);
       if constexpr (PACKED) {
         W2x[k * D::NB + n] = w.x;
         W2y[k * D::NB + n] = w.y;
@@ -1277,7 +1282,7 @@ __global__ void __launch_bounds__(64, MINB)
     }
     for (int s = t; s < D::NWA; s += T) {   // WA[i][k3] -> WAT[k3][i]
       const int i = s / D::NQ3, k3 = s % D::NQ3;
-      const C<R> w = ld_l2(Wa + s, pol_first);
+      const C<R> w = weight(s, s);
       if constexpr (PACKED) {
         WAx[k3 * D::NRY + i] = w.x;
         WAy[k3 * D::NRY + i] = w.y;
@@ -1285,7 +1290,7 @@ __global__ void __launch_bounds__(64, MINB)
         WAT[k3 * D::NRY + i] = w;
       }
     }
-    for (int s = t; s < D::NQ; s += T) W0s[s] = ld_l2(Wa + m.offW0 + s, pol_first);
+    for (int s = t; s < D::NQ; s += T) W0s[s] = weight(m.offW0 + s, Ga ? __ldg(m.b3_cw + m.offW0 + s) : -1);
     __syncthreads();
     const R edf = to_r<R>(edf_in[atom]);
     const int b0 = off[atom], b1 = off[atom + 1];
@@ -1631,7 +1636,7 @@ size_t b3_fe_smem(const DeviceModel& m, int nw) {
   const size_t ncoef = static_cast<size_t>(m.b3_ncombo) * D::NM * D::I * D::I;
   return sizeof(float) * ((ncoef + 3) & ~static_cast<size_t>(3)) +
          sizeof(C<float>) * 2 * static_cast<size_t>(m.b3_nc) * kB3Stride + sizeof(double) * nw * 32 +
-         sizeof(float) * 32 + sizeof(float) * m.b3_nc + sizeof(int) * (m.b3_nc + m.nW);
+         sizeof(float) * m.b3_nc + sizeof(int) * m.b3_nc;
 }
 template <class R, class D>
 size_t forces_fe_smem() {
