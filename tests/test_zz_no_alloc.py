@@ -1,8 +1,8 @@
 """GPU test of ace_compute_device_noalloc, the entry point for callers that
 cannot allocate device memory while they evaluate. It is called through the
 C ABI twice in a row and must reproduce ace_compute_device (the regular entry
-point, which uses library-allocated scratch) within the FP64 parity tolerance
-of the other tests. The file sorts last so that a stop-at-first-failure run
+point, which uses library-allocated scratch): in FP64 within the parity
+tolerance of the other tests, in split precision within 1e-6. The file sorts last so that a stop-at-first-failure run
 has executed every other test before it; it also passes alone in a fresh
 process, because it places the potential's tables on the device itself."""
 from __future__ import annotations
@@ -21,12 +21,17 @@ def _rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-def test_noalloc_matches_compute_device(seeded_potential):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_noalloc_matches_compute_device(seeded_potential, precision):
+    """FP64 at the parity tolerance; split precision within 1e-6 (the 3-body
+    kernel adds gradients with shared-memory atomics, so two split runs agree
+    to FP32 rounding, not bit for bit)."""
     import torch
     from magace import lib, structures as S
 
     lib.init(seeded_potential, "Fe", 5.0, 4.0, 0.2, 1)
-    lib.set_precision(0)
+    lib.set_precision(precision)
+    tol = TOL if precision == 0 else 1e-6
     so = lib.load()
     nb = S.neighbor_data(S.bcc_fe_128(3), 5.0)
     dev = torch.device("cuda", 0)
@@ -58,7 +63,8 @@ def test_noalloc_matches_compute_device(seeded_potential):
         got = [t.cpu().numpy() for t in got]
         for g, r in zip(got, ref):
             assert np.all(np.isfinite(g))
-            assert _rel(g, r) <= TOL
+            assert _rel(g, r) <= tol
+    lib.set_precision(0)
 
 
 def test_noalloc_refuses_more_atoms_than_its_scratch(seeded_potential):
