@@ -531,6 +531,45 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
   const int nd = M.ndensity;
   TermSink sink(L, nd);
   long nterm[5] = {0, 0, 0, 0, 0};
+  // mirror of every factor: negating all its m gives (-1)^(sum of the m)
+  // times the conjugate (A(m1,m2) = (-1)^(m1+m2) conj A(-m1,-m2), likewise
+  // A2 and A0)
+  std::vector<int> mir(L.nF), sgn(L.nF, 1);
+  for (int f = 0; f < L.nF; ++f) mir[f] = f;
+  for (int n1 = 0; n1 < L.n3a; ++n1)
+    for (int l1 = 0; l1 <= L.l3a; ++l1)
+      for (int m1 = -l1; m1 <= l1; ++m1)
+        for (int n2 = 0; n2 < L.n3m; ++n2)
+          for (int l2 = 0; l2 <= L.l3m; ++l2)
+            for (int m2 = -l2; m2 <= l2; ++m2) {
+              const int f = L.A(n1, l1, m1, n2, l2, m2);
+              mir[f] = L.A(n1, l1, -m1, n2, l2, -m2);
+              sgn[f] = ((m1 + m2) & 1) ? -1 : 1;
+            }
+  for (int n = 0; n < L.nba; ++n)
+    for (int nr = 0; nr < L.n2m; ++nr)
+      for (int l = 0; l <= L.l2m; ++l)
+        for (int m = -l; m <= l; ++m) {
+          const int f = L.A2(n, nr, l, m);
+          mir[f] = L.A2(n, nr, l, -m);
+          sgn[f] = (m & 1) ? -1 : 1;
+        }
+  for (int nr = 0; nr < L.n2m; ++nr)
+    for (int l = 0; l <= L.l2m; ++l)
+      for (int m = -l; m <= l; ++m) {
+        const int f = L.A0(nr, l, m);
+        mir[f] = L.A0(nr, l, -m);
+        sgn[f] = (m & 1) ? -1 : 1;
+      }
+  // density (A0-slot) terms, summed per factor set {A0, sorted others}
+  using G0Key = std::array<int, 5>;  // arity, A0 factor, three others (ONE-padded)
+  std::map<G0Key, std::array<double, 2>> g0;
+  const auto g0_key = [&](int arity, int a0, const int* o) {
+    G0Key key{arity, a0, L.offOne, L.offOne, L.offOne};
+    for (int q = 0; q < arity; ++q) key[2 + q] = o[q];
+    std::sort(key.begin() + 2, key.begin() + 2 + arity);
+    return key;
+  };
   // every term adds kappa * (product of the other factors) to the A0 factor's
   // slot (density and W0) and to the weight slot of each other factor
   for_each_term(M, with_b3, [&](int rank, size_t c, double cf, const int* f, const int* w) {
@@ -538,7 +577,9 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
     if (k[0] == 0.0 && k[1] == 0.0) return;
     ++nterm[rank];
     const int arity = rank - 1;
-    sink.add(sink.g0_slot(f[0]), k, f + 1, arity);
+    auto& kk = g0[g0_key(arity, f[0], f + 1)];
+    kk[0] += k[0];
+    kk[1] += k[1];
     for (int q = 1; q < rank; ++q) {
       if (w[q] < 0) continue;
       int others[3], n = 0;
@@ -549,6 +590,41 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
   });
   if (with_b3)
     for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
+  // Density entries folded over mirror pairs. A term's mirror (every m
+  // negated) has the conjugate product times s = the product of its factors'
+  // signs, so the pair adds (kappa + s kappa') Re(prod) to rho. The member
+  // whose key is larger (its A0 has m' > 0, or m' = 0 and larger others)
+  // takes 2 kappa, and the other only the remainder kappa' - s kappa, which is
+  // zero for the pairs of a mirror-symmetric basis (all of the Fe layout's).
+  // Self-mirror terms keep kappa. The W0 slots of m' > 0 then hold twice the
+  // terms' gradient, so their multiplicity is 1 (slot_mult below).
+  for (const auto& kv : g0) {
+    const G0Key& key = kv.first;
+    const int arity = key[0];
+    int mo[3];
+    int s = sgn[key[1]];
+    for (int q = 0; q < arity; ++q) {
+      mo[q] = mir[key[2 + q]];
+      s *= sgn[key[2 + q]];
+    }
+    const G0Key mkey = g0_key(arity, mir[key[1]], mo);
+    const auto emit = [&](const G0Key& at, double k0, double k1) {
+      if (k0 == 0.0 && k1 == 0.0) return;
+      const double k[2] = {k0, k1};
+      const int others[3] = {at[2], at[3], at[4]};
+      sink.add(sink.g0_slot(at[1]), k, others, arity);
+    };
+    const auto mit = g0.find(mkey);
+    if (mkey == key) {
+      emit(key, kv.second[0], kv.second[1]);
+    } else if (mkey < key) {
+      const double m0 = mit == g0.end() ? 0.0 : mit->second[0], m1 = mit == g0.end() ? 0.0 : mit->second[1];
+      emit(key, 2.0 * kv.second[0], 2.0 * kv.second[1]);
+      emit(mkey, m0 - s * kv.second[0], m1 - s * kv.second[1]);
+    } else if (mit == g0.end()) {
+      emit(key, kv.second[0], kv.second[1]);  // no partner: the pair is this term alone
+    }
+  }
 
   // flatten into segments, then pack segments into warp groups
   g = GatherTable();
@@ -622,7 +698,7 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
         g.slot_factor[s] = L.A0(nr, l, m);
         if (m >= 0) {
           g.slot_weight[s] = L.W0(nr, l, m);
-          g.slot_mult[s] = m == 0 ? 1.0 : 2.0;
+          g.slot_mult[s] = 1.0;  // m' > 0: the folded slot already holds both mirror halves
         }
       }
   for (int n1 = 0; n1 < L.n3a; ++n1)
@@ -845,12 +921,22 @@ int build_tables(Model& M, std::string& msg) {
     if (st) return st;
     build_dense_b3(M);
     // multiplicity of each compact element's weight, from the gather table's
-    // slots (every weight has a slot there, with or without entries)
+    // slots (every weight has a slot there, with or without entries); the
+    // A0 slots there hold folded mirror pairs (multiplicity 1), while the
+    // 3-body gradients of an A0 element with m' > 0 take the half-plane
+    // multiplicity 2 (src/forces.F90:690-749)
     DenseB3& D = M.db3;
+    const FactorLayout& L = M.L;
     D.mult.assign(D.nc, 0.0);
     for (int s = 0; s < M.gt_nob3.nslot; ++s) {
       const int w = M.gt_nob3.slot_weight[s];
-      if (w >= 0 && D.compact_of_weight[w] >= 0) D.mult[D.compact_of_weight[w]] = M.gt_nob3.slot_mult[s];
+      if (w < 0 || D.compact_of_weight[w] < 0) continue;
+      double mu = M.gt_nob3.slot_mult[s];
+      if (s < M.gt_nob3.nG0) {
+        const int lm = s % L.ls2, l = static_cast<int>(std::sqrt(static_cast<double>(lm)) + 1e-9);
+        mu = lm - l * l - l == 0 ? 1.0 : 2.0;
+      }
+      D.mult[D.compact_of_weight[w]] = mu;
     }
   }
   return MAGACE_OK;
