@@ -232,7 +232,10 @@ def gpu_arm(args, rank, world, local_rank):
 
     def run_path(mode):
         lib.set_precision(mode)
-        lib.set_kernel_timing(True)
+        # the timed steps run as a caller's would: without the library's
+        # per-kernel events, which would keep the split path's two density
+        # kernels from running side by side
+        lib.set_kernel_timing(False)
         for _ in range(args.warmup):
             step()
         torch.cuda.synchronize()
@@ -240,7 +243,7 @@ def gpu_arm(args, rank, world, local_rank):
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
-        step_ms, ktimes = [], []
+        step_ms = []
         with ClockSampler(local_rank) as clk:
             wall0 = time.perf_counter()
             for _ in range(args.steps):
@@ -251,12 +254,20 @@ def gpu_arm(args, rank, world, local_rank):
                 e.record()
                 e.synchronize()
                 step_ms.append(s.elapsed_time(e))
-                ktimes.append(lib.kernel_times())
             torch.cuda.synchronize()
             wall = time.perf_counter() - wall0
         if world > 1:
             torch.distributed.barrier()
         lib.device_status()
+        # per-kernel durations (roofline): further steps with kernel timing on
+        lib.set_kernel_timing(True)
+        ktimes = []
+        for _ in range(max(3, min(args.steps, 10))):
+            flush.zero_()
+            step()
+            torch.cuda.synchronize()
+            ktimes.append(lib.kernel_times())
+        lib.set_kernel_timing(False)
         res = {k: v.detach().cpu().numpy().copy() for k, v in out.items()}
         nl = lib.last_launch_count()
         return {"ms": float(np.mean(step_ms)), "ms_all": step_ms, "kernel_ms": np.mean(ktimes, axis=0).tolist(),

@@ -121,16 +121,19 @@ int ace_device_status(void);
  * device supports it, else 1. Returns -1 when no tables could be placed. */
 int ace_host_access_mode(void);
 
-/* Number of kernel launches issued by the last evaluation call. */
+/* Number of kernels launched by the last evaluation call: 3 for the FP64
+ * path, 5 for the split path of the specialised layout (A basis, 2-/4-body
+ * density, 3-body density, k_finish_fe, forces). */
 int ace_last_launch_count(void);
 
 /* Kernel timing: when on, the boundaries of the kernels of every evaluation
- * are recorded with CUDA events on the evaluation stream; ace_kernel_times
+ * are recorded with CUDA events on the evaluation stream, and every kernel
+ * runs on that stream (the split path otherwise runs its 2-/4-body and
+ * 3-body density kernels side by side on two streams); ace_kernel_times
  * writes the last evaluation's per-kernel durations in ms into ms[0..3],
- * synchronising on the last event: k_abasis, k_density, k_forces (3
- * kernels), or k_abasis, k_density, k_b3, k_forces when the split-precision
- * path runs its 3-body terms as a kernel of their own (4 kernels, see
- * ace_last_launch_count). Entries beyond the kernel count are 0. */
+ * synchronising on the last event: k_abasis, k_density, k_forces (FP64), or
+ * k_abasis, k_density, k_b3 (with k_finish_fe), k_forces (split path of the
+ * specialised layout). Entries beyond those are 0. */
 int ace_set_kernel_timing(int on);
 int ace_kernel_times(float* ms);
 

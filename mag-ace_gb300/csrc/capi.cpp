@@ -69,7 +69,12 @@ struct Runtime {
   int precision = 0;
   int last_error = MAGACE_OK;
   std::string last_msg;
-  int last_launches = 0;
+  int last_launches = 0;  // timed slots of the last evaluation (ace_kernel_times)
+  int last_kernels = 0;   // kernels it launched
+  // the side stream and fork/join events of the density kernels (EvalBuffers::side)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool overlap = true;  // MAGACE_OVERLAP=0 keeps every kernel on the launch stream
   int last_natom = -1;  // atoms of the last evaluation (ace_density_gradient_device)
   bool work_queue = false;  // neighbour-count-sorted work queue
   int tune_abasis = 0, tune_rest = 0, tune_b3 = 0, tune_forces = 0;  // kernel variants (ace_autotune_device)
@@ -227,6 +232,13 @@ int upload_tables() {
   if (R.dev_tables && R.device == dev) return MAGACE_OK;
   R.device = dev;
   if (!R.stream) CUDA_TRY(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
+  if (!R.side) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&R.side, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&R.ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&R.ev_join, cudaEventDisableTiming));
+    const char* e = std::getenv("MAGACE_OVERLAP");
+    R.overlap = !(e && e[0] == '0');
+  }
   const Model& M = R.model;
   const GatherTable& g = M.gt;
   CUDA_TRY(R.lut_a.upload(M.lut.a));
@@ -397,8 +409,13 @@ int run_eval(EvalBuffers& b, cudaStream_t st) {
       if (!e) CUDA_TRY(cudaEventCreate(&e));
     ev = R.ev;
   }
-  R.last_launches = R.precision == 0 ? launch_eval_fp64(R.dm, b, st, R.grid_cap, ev)
-                                     : launch_eval_fp32(R.dm, b, st, R.grid_cap, ev);
+  if (!ev && R.overlap && R.side) {
+    b.side = R.side;
+    b.ev_fork = R.ev_fork;
+    b.ev_join = R.ev_join;
+  }
+  R.last_launches = R.precision == 0 ? launch_eval_fp64(R.dm, b, st, R.grid_cap, ev, &R.last_kernels)
+                                     : launch_eval_fp32(R.dm, b, st, R.grid_cap, ev, &R.last_kernels);
   R.ev_recorded = ev != nullptr && R.last_launches >= 3;
   R.last_natom = b.natom;
   CUDA_TRY(cudaGetLastError());
@@ -500,7 +517,10 @@ int runtime_error(int code, const char* msg) { return set_error(code, msg); }
 
 int runtime_device_error(int dev_err) { return dev_err ? device_error_to_status(dev_err) : set_error(MAGACE_OK, ""); }
 
-void runtime_set_launches(int n) { rt().last_launches = n; }
+void runtime_set_launches(int slots, int kernels) {
+  rt().last_launches = slots;
+  rt().last_kernels = kernels;
+}
 
 }  // namespace magace
 
@@ -586,7 +606,7 @@ int ace_basis_rows(int rank, int* out) {
   return MAGACE_OK;
 }
 
-int ace_last_launch_count(void) { return rt().last_launches; }
+int ace_last_launch_count(void) { return rt().last_kernels; }
 
 int ace_host_access_mode(void) {
   int st = upload_tables();
@@ -844,7 +864,7 @@ int ace_descriptors_device(int natom, int nei, const int* bond_offset, const dou
   b.err = R.err.p;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : R.stream;
   CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), s));
-  R.last_launches = launch_descriptors(R.dm, b, B, s, R.grid_cap);
+  R.last_launches = R.last_kernels = launch_descriptors(R.dm, b, B, s, R.grid_cap);
   R.ev_recorded = false;
   CUDA_TRY(cudaGetLastError());
   return set_error(MAGACE_OK, "");
@@ -900,6 +920,11 @@ void ace_release_device(void) {
   R.W.release();
   if (R.stream) cudaStreamDestroy(R.stream);
   R.stream = nullptr;
+  if (R.side) cudaStreamDestroy(R.side);
+  if (R.ev_fork) cudaEventDestroy(R.ev_fork);
+  if (R.ev_join) cudaEventDestroy(R.ev_join);
+  R.side = nullptr;
+  R.ev_fork = R.ev_join = nullptr;
   if (R.pinned) cudaFreeHost(R.pinned);
   R.pinned = nullptr;
   R.pinned_bytes = 0;

@@ -999,12 +999,13 @@ B3Split b3_split(int nblk, int grid_cap) {
   return s;
 }
 
-// The split-precision scratch (EvalBuffers::aux): rho_rest[natom] doubles,
-// then one record per tail block of the 3-body kernel's split tail (the
+// The split-precision scratch (EvalBuffers::aux): rho_rest[natom] and
+// rho3[natom] doubles, then one record per tail block of the 3-body kernel's split tail (the
 // blocks B3Split divides, 256-byte aligned): rho3[32] doubles, a ticket
 // (padded to 16 bytes) and the gradients g[nc][32][2] floats. The records in
 // use are zeroed before each evaluation that splits.
 struct AuxLayout {
+  size_t rho3;        // the 3-body density per atom
   size_t tail0, rec;  // first record, bytes per record
   size_t end;
 };
@@ -1014,7 +1015,8 @@ AuxLayout aux_layout(const DeviceModel& m, int natom) {
   const B3Split sp = b3_split(nblk, nblk);  // as if every block had its own CTA
   const size_t ntail = sp.parts > 1 ? static_cast<size_t>(sp.ntail) : 0;
   AuxLayout L;
-  L.tail0 = up(sizeof(double) * static_cast<size_t>(natom));
+  L.rho3 = up(sizeof(double) * static_cast<size_t>(natom));
+  L.tail0 = L.rho3 + up(sizeof(double) * static_cast<size_t>(natom));
   L.rec = up(kTailG + sizeof(float) * 64 * static_cast<size_t>(m.b3_nc));
   L.end = L.tail0 + L.rec * ntail;
   return L;
@@ -1088,7 +1090,7 @@ void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
 // generic k_density. Returns the number of kernels launched.
 template <class R>
 int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid, int grid_cap, bool fe,
-                   cudaEvent_t ev_between) {
+                   cudaEvent_t ev_between, int* kernels) {
   const int natom = b.natom;
   if constexpr (sizeof(R) == 4) {
     if (fe) {
@@ -1101,9 +1103,21 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const int rw = kRestWarpChoices[m.tune_rest], bw = kB3WarpChoices[m.tune_b3];
       (void)bw;
       const size_t s2 = density_fe_smem(m, rw);
+      const AuxLayout al = aux_layout(m, natom);
+      double* rho3 = reinterpret_cast<double*>(static_cast<unsigned char*>(b.aux) + al.rho3);
+      // the 2-/4-body kernel and the 3-body kernel are independent: with a
+      // side stream (EvalBuffers::side) the first runs there, forked from and
+      // joined back into `st` by events, so that either fills the SMs the
+      // other's last wave leaves idle; k_finish_fe then adds their densities
+      const bool fork = b.side != nullptr;
+      cudaStream_t sr = fork ? b.side : st;
+      if (fork) {
+        cudaEventRecord(b.ev_fork, st);
+        cudaStreamWaitEvent(sr, b.ev_fork, 0);
+      }
 #define MAGACE_REST(NW, SM)                                                                                   \
   set_smem(k_density_fe<FeDims, NW, SM>, s2);                                                                 \
-  k_density_fe<FeDims, NW, SM><<<gb, NW * 32, s2, st>>>(m, natom, Fp, Wp, rho_rest)
+  k_density_fe<FeDims, NW, SM><<<gb, NW * 32, s2, sr>>>(m, natom, Fp, Wp, rho_rest)
       // variants: 32 or 16 warps; per-entry uniform loads, record streams
       // broadcast by shuffles, or record streams through shared memory
       switch (m.tune_rest) {
@@ -1120,14 +1134,12 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       // the last partial wave split by task range (B3Split); the records of
       // the tail blocks start at zero
       const B3Split sp = b3_split(nblk, grid_cap);
-      const AuxLayout al = aux_layout(m, natom);
       unsigned char* tails = static_cast<unsigned char*>(b.aux) + al.tail0;
       if (sp.parts > 1) cudaMemsetAsync(tails, 0, al.rec * sp.ntail, st);
       const int g3 = sp.parts > 1 ? sp.nfull + sp.ntail * sp.parts : gb;
 #define MAGACE_B3(NW, LOOP)                                                                                  \
   set_smem(k_b3_fe<FeDims, NW, LOOP>, sb);                                                                   \
-  k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(m, natom, Fw, b.rho1, rho_rest, b.core, b.energy, b.edf,    \
-                                                     b.dedrho, b.err, sp.nfull, sp.parts, tails, al.rec)
+  k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(m, natom, Fw, rho3, b.err, sp.nfull, sp.parts, tails, al.rec)
       // variants: (16 warps, n0' innermost), (12, innermost), (8, innermost),
       // (12, n0' outermost), (16, packed FP32x2), (12, packed FP32x2)
       switch (m.tune_b3) {
@@ -1139,6 +1151,13 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
         default: MAGACE_B3(16, 0); break;
       }
 #undef MAGACE_B3
+      if (fork) {
+        cudaEventRecord(b.ev_join, sr);
+        cudaStreamWaitEvent(st, b.ev_join, 0);
+      }
+      const int gf = (natom + 255) / 256;
+      k_finish_fe<<<gf, 256, 0, st>>>(m, natom, b.rho1, rho_rest, rho3, b.core, b.energy, b.edf, b.dedrho, b.err);
+      if (kernels) *kernels += 3;
       return 2;
     }
   }
@@ -1152,11 +1171,13 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
     k_density<R, 2><<<grid, kDensityThreads, s2, st>>>(m, natom, reinterpret_cast<const C<R>*>(b.F), b.rho1, b.core,
                                                        reinterpret_cast<C<R>*>(b.W), b.energy, b.edf, b.dedrho, b.err);
   }
+  if (kernels) *kernels += 1;
   return 1;
 }
 
 template <class R>
-int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
+int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,
+                int* kernels) {
   DeviceModel m = m0;
   m.order = b.order;
   const int natom = b.natom;
@@ -1166,8 +1187,10 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   if (ev) cudaEventRecord(ev[0], st);
   launch_abasis<R>(m, b, st, grid, fe);
   if (ev) cudaEventRecord(ev[1], st);
-  const int nd = launch_density<R>(m, b, st, grid, grid_cap, fe, ev ? ev[2] : nullptr);
+  int nk = 2;  // the A-basis and force kernels
+  const int nd = launch_density<R>(m, b, st, grid, grid_cap, fe, ev ? ev[2] : nullptr, &nk);
   const int nlaunch = 2 + nd;
+  if (kernels) *kernels = nk;
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
     const size_t s3 = forces_fe_smem<R, FeDims>();
@@ -1343,14 +1366,16 @@ int launch_descriptors(const DeviceModel& m0, const EvalBuffers& b, double* B, c
   return 2;
 }
 
-int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
-  return launch_eval<double>(m, b, st, grid_cap, ev);
+int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,
+                     int* kernels) {
+  return launch_eval<double>(m, b, st, grid_cap, ev, kernels);
 }
 
 }  // namespace magace
 
 namespace magace {
-int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev) {
-  return launch_eval<float>(m, b, st, grid_cap, ev);
+int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,
+                     int* kernels) {
+  return launch_eval<float>(m, b, st, grid_cap, ev, kernels);
 }
 }  // namespace magace

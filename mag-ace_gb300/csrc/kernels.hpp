@@ -56,6 +56,11 @@ struct EvalBuffers {
   void* stage = nullptr;      // [nei][8] bond inputs in the working precision (specialised kernels), or null
   bool dev_inputs = false;    // r, e, magj, mhj are device memory (bulk copies may read them)
   bool host_outputs = false;  // fij, tij are host memory (written as whole lines)
+  // a second stream for the 2-/4-body density kernel beside the 3-body one,
+  // with the events that fork it from and join it back into the launch
+  // stream; null: everything runs on the launch stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 // Work queue of one evaluation: the atoms sorted by decreasing bond count
@@ -68,14 +73,19 @@ void upload_ylm_constants(const double* alm, const double* blm, const double* cl
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which);
 // Size of EvalBuffers::aux for natom atoms (0 when the kernels need none).
 size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom);
-// Launches the A-basis, density and force phases on `st` (3 kernels, or 4
-// when the split-precision density runs its 3-body part as a kernel of its
-// own); returns the number of kernels launched n. With `ev` (kMaxLaunches + 1
-// events) ev[k] is recorded before kernel k and ev[n] after the last one.
+// Launches the A-basis, density and force phases on `st` and returns the
+// number n of timed slots: 3 (A basis, density, forces) or, when the
+// split-precision density runs its 3-body part in kernels of its own, 4 (the
+// third slot is the 3-body kernel and k_finish_fe). With `ev` (kMaxLaunches +
+// 1 events) ev[k] is recorded before slot k and ev[n] after the last one;
+// callers that time pass no side stream, so that the slots do not overlap.
+// `kernels` receives the number of kernels launched.
 // Descriptors: the FP64 A-basis phase into b.F, then B[natom][nB] (see
 // model.hpp DescriptorTable); returns the number of kernels launched.
 int launch_descriptors(const DeviceModel& m, const EvalBuffers& b, double* B, cudaStream_t st, int grid_cap);
-int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
-int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev);
+int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,
+                     int* kernels = nullptr);
+int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,
+                     int* kernels = nullptr);
 
 }  // namespace magace

@@ -586,17 +586,20 @@ __global__ void __launch_bounds__(64)
 }
 
 // ===========================================================================
-// The split-precision density phase of the specialised layout, two kernels:
+// The split-precision density phase of the specialised layout, three
+// kernels; the first two are independent and may run side by side:
 //
-// k_density_fe (one CTA per atom) evaluates the 2- and 4-body terms through
-// the gather table g2 and writes, per atom, their density rho_rest and the
-// unscaled weights mult * dRho_rest/dF into W.
+// k_density_fe (32 atoms per CTA, one per lane) evaluates the 2- and 4-body
+// terms through the rest table and writes, per atom, their density rho_rest
+// and the unscaled weights mult * dRho_rest/dF into W.
 //
 // k_b3_fe (32 atoms per CTA, one per lane) evaluates the 3-body terms as
-// dense contractions per (angular combination, m-term) task, then finishes
-// each atom in its lane: rho = rho1 + rho_rest + rho3, the embedding and
-// energy in FP64 (a full warp of atoms per FP64 instruction), and the final
-// weights W = dE/drho * (W + mult * dRho3/dF).
+// dense contractions per (angular combination, m-term) task and writes, per
+// atom, their density rho3 and the gradients mult * dRho3/dF into F's rows.
+//
+// k_finish_fe (one atom per thread) adds rho = rho1 + rho_rest + rho3 and
+// evaluates the embedding and energy in FP64; the force kernel then forms
+// the weights W = dE/drho * (W + g3).
 
 // Global loads of the staging and weight loops are issued kBatch at a time,
 // so that each thread has that many in flight.
@@ -1023,9 +1026,8 @@ __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const 
 // another. The records are zeroed before the launch.
 template <class D, int NW, int LOOP>
 __global__ void __launch_bounds__(NW * 32, 1)
-    k_b3_fe(DeviceModel m, int natom, C<float>* F, const double* __restrict__ rho1, const double* __restrict__ rho_rest, const double* __restrict__ core,
-            double* __restrict__ energy, double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err,
-            int nfull, int parts, unsigned char* __restrict__ tails, size_t tail_rec) {
+    k_b3_fe(DeviceModel m, int natom, C<float>* F, double* __restrict__ rho3, int* err, int nfull, int parts,
+            unsigned char* __restrict__ tails, size_t tail_rec) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
   const int nc = m.b3_nc;
@@ -1148,28 +1150,12 @@ __global__ void __launch_bounds__(NW * 32, 1)
         rpart[q] = q < 32 ? __ldcg(rho3_acc + q) : 0.0;
       __syncthreads();
     }
-    // finish the atoms, one per lane of warp 0
+    // the 3-body density of the block's atoms (k_finish_fe adds the parts)
     if (warp == 0 && lane < na) {
-      const int atom = s_atom[lane];
-      double rho = rho1[static_cast<size_t>(atom) * 2] + rho_rest[atom];
-      for (int w = 0; w < NW; ++w) rho += rpart[w * 32 + lane];
-      if (!isfinite(rho)) raise_error(err, kDevNaN);
-      double Fd, dFd;
-      embed(m.nfemb, rho, m.par[0][0], m.par[1][0], Fd, dFd);
-      const double e = core[atom], elow = m.ecut - m.decut;
-      double fcut = 1.0, dfcut = 0.0;
-      if (e >= m.ecut) {
-        fcut = 0.0;
-      } else if (e > elow) {
-        const double pi = 3.14159265358979323846264338327950288419;
-        fcut = 0.5 * (1.0 + cos(pi * (e - elow) / m.decut));
-        dfcut = -0.5 * sin(pi * (e - elow) / m.decut) * pi / m.decut;
-      }
-      edf_out[atom] = dfcut * Fd + 1.0;
-      dedrho_out[static_cast<size_t>(atom) * 2] = fcut * dFd;
-      energy[atom] = fcut * Fd + e;
+      double r3 = 0.0;
+      for (int w = 0; w < NW; ++w) r3 += rpart[w * 32 + lane];
+      rho3[s_atom[lane]] = r3;
     }
-    __syncthreads();
     // the block's 3-body gradients times their multiplicities, into the
     // factor rows of its atoms (nothing reads F after this kernel): the
     // force kernel assembles W = dE/drho (W_rest + g3) from them; atom-major,
@@ -1183,6 +1169,34 @@ __global__ void __launch_bounds__(NW * 32, 1)
       }
     }
     __syncthreads();
+  }
+}
+
+// k_finish_fe: per atom (one per thread) rho = rho1 + rho_rest + rho3, the
+// FP64 embedding and the inner cutoff on the core energy; the energy, edf and
+// dE/drho outputs (the two density kernels before it may run side by side).
+__global__ void __launch_bounds__(256) k_finish_fe(DeviceModel m, int natom, const double* __restrict__ rho1,
+                                                   const double* __restrict__ rho_rest,
+                                                   const double* __restrict__ rho3, const double* __restrict__ core,
+                                                   double* __restrict__ energy, double* __restrict__ edf_out,
+                                                   double* __restrict__ dedrho_out, int* err) {
+  for (int atom = blockIdx.x * blockDim.x + threadIdx.x; atom < natom; atom += gridDim.x * blockDim.x) {
+    const double rho = rho1[static_cast<size_t>(atom) * 2] + rho_rest[atom] + rho3[atom];
+    if (!isfinite(rho)) raise_error(err, kDevNaN);
+    double Fd, dFd;
+    embed(m.nfemb, rho, m.par[0][0], m.par[1][0], Fd, dFd);
+    const double e = core[atom], elow = m.ecut - m.decut;
+    double fcut = 1.0, dfcut = 0.0;
+    if (e >= m.ecut) {
+      fcut = 0.0;
+    } else if (e > elow) {
+      const double pi = 3.14159265358979323846264338327950288419;
+      fcut = 0.5 * (1.0 + cos(pi * (e - elow) / m.decut));
+      dfcut = -0.5 * sin(pi * (e - elow) / m.decut) * pi / m.decut;
+    }
+    edf_out[atom] = dfcut * Fd + 1.0;
+    dedrho_out[static_cast<size_t>(atom) * 2] = fcut * dFd;
+    energy[atom] = fcut * Fd + e;
   }
 }
 

@@ -23,7 +23,7 @@ namespace magace {
 int runtime_snapshot(DeviceModel* dm, int* precision, int* grid_cap);
 int runtime_error(int code, const char* msg);
 int runtime_device_error(int dev_err);
-void runtime_set_launches(int n);
+void runtime_set_launches(int slots, int kernels);
 
 namespace {
 
@@ -122,8 +122,10 @@ extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_of
   b.dedrho = reinterpret_cast<double*>(base + o_dedrho);
   b.err = err;
   b.aux = aux_bytes ? base + o_aux : nullptr;
-  const int n = precision == 0 ? launch_eval_fp64(dm, b, s, grid_cap, nullptr) : launch_eval_fp32(dm, b, s, grid_cap, nullptr);
-  runtime_set_launches(n);
+  int nk = 0;
+  const int n = precision == 0 ? launch_eval_fp64(dm, b, s, grid_cap, nullptr, &nk)
+                               : launch_eval_fp32(dm, b, s, grid_cap, nullptr, &nk);
+  runtime_set_launches(n, nk);
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return runtime_error(MAGACE_ERR_CUDA, cudaGetErrorString(ce));
   // the call completes before it returns, so that the device error word of

@@ -245,16 +245,17 @@ def set_kernel_timing(on: bool) -> None:
 
 
 def kernel_names(n: int) -> list:
-    """Names of the kernels of an evaluation that launched n of them."""
-    return ["k_abasis", "k_density", "k_b3", "k_forces"] if n == 4 else ["k_abasis", "k_density", "k_forces"]
+    """Names of the timed kernels of an evaluation that launched n kernels
+    (the split path's "k_b3" slot includes its k_finish_fe)."""
+    return ["k_abasis", "k_density", "k_b3", "k_forces"] if n >= 4 else ["k_abasis", "k_density", "k_forces"]
 
 
 def kernel_times() -> list:
-    """Per-kernel durations (ms) of the last evaluation, in launch order
-    (kernel_names(last_launch_count()))."""
+    """Per-kernel durations (ms) of the last timed evaluation, in launch
+    order (kernel_names(last_launch_count()))."""
     out = (ctypes.c_float * 4)()
     _check(load().ace_kernel_times(out))
-    return [float(x) for x in out][:last_launch_count()]
+    return [float(x) for x in out][:len(kernel_names(last_launch_count()))]
 
 
 def table_stats() -> dict:
