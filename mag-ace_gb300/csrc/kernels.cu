@@ -1000,12 +1000,15 @@ B3Split b3_split(int nblk, int grid_cap) {
 }
 
 // The split-precision scratch (EvalBuffers::aux): rho_rest[natom] and
-// rho3[natom] doubles, then one record per tail block of the 3-body kernel's split tail (the
+// rho3[natom] doubles, the 3-body gradients g3[natom][nc] (FP32 complex; a
+// buffer of their own, because the 2-/4-body kernel may still be reading the
+// factors F while the 3-body kernel finishes), then one record per tail block of the 3-body kernel's split tail (the
 // blocks B3Split divides, 256-byte aligned): rho3[32] doubles, a ticket
 // (padded to 16 bytes) and the gradients g[nc][32][2] floats. The records in
 // use are zeroed before each evaluation that splits.
 struct AuxLayout {
   size_t rho3;        // the 3-body density per atom
+  size_t g3;          // the 3-body gradients [natom][nc], FP32 complex
   size_t tail0, rec;  // first record, bytes per record
   size_t end;
 };
@@ -1016,7 +1019,8 @@ AuxLayout aux_layout(const DeviceModel& m, int natom) {
   const size_t ntail = sp.parts > 1 ? static_cast<size_t>(sp.ntail) : 0;
   AuxLayout L;
   L.rho3 = up(sizeof(double) * static_cast<size_t>(natom));
-  L.tail0 = L.rho3 + up(sizeof(double) * static_cast<size_t>(natom));
+  L.g3 = L.rho3 + up(sizeof(double) * static_cast<size_t>(natom));
+  L.tail0 = L.g3 + up(sizeof(float) * 2 * static_cast<size_t>(m.b3_nc) * static_cast<size_t>(natom));
   L.rec = up(kTailG + sizeof(float) * 64 * static_cast<size_t>(m.b3_nc));
   L.end = L.tail0 + L.rec * ntail;
   return L;
@@ -1098,13 +1102,13 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const int nblk = (natom + 31) / 32;
       const int gb = nblk < grid_cap ? nblk : grid_cap;
       const auto* Fp = reinterpret_cast<const C<float>*>(b.F);
-      auto* Fw = reinterpret_cast<C<float>*>(b.F);  // the 3-body kernel leaves its gradients there
       auto* Wp = reinterpret_cast<C<float>*>(b.W);
       const int rw = kRestWarpChoices[m.tune_rest], bw = kB3WarpChoices[m.tune_b3];
       (void)bw;
       const size_t s2 = density_fe_smem(m, rw);
       const AuxLayout al = aux_layout(m, natom);
       double* rho3 = reinterpret_cast<double*>(static_cast<unsigned char*>(b.aux) + al.rho3);
+      auto* G3 = reinterpret_cast<C<float>*>(static_cast<unsigned char*>(b.aux) + al.g3);
       // the 2-/4-body kernel and the 3-body kernel are independent: with a
       // side stream (EvalBuffers::side) the first runs there, forked from and
       // joined back into `st` by events, so that either fills the SMs the
@@ -1139,7 +1143,8 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const int g3 = sp.parts > 1 ? sp.nfull + sp.ntail * sp.parts : gb;
 #define MAGACE_B3(NW, LOOP)                                                                                  \
   set_smem(k_b3_fe<FeDims, NW, LOOP>, sb);                                                                   \
-  k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(m, natom, Fw, rho3, b.err, sp.nfull, sp.parts, tails, al.rec)
+  k_b3_fe<FeDims, NW, LOOP><<<g3, NW * 32, sb, st>>>(m, natom, Fp, G3, rho3, b.err, sp.nfull, sp.parts, tails,  \
+                                                     al.rec)
       // variants: (16 warps, n0' innermost), (12, innermost), (8, innermost),
       // (12, n0' outermost), (16, packed FP32x2), (12, packed FP32x2)
       switch (m.tune_b3) {
@@ -1194,8 +1199,11 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
     const size_t s3 = forces_fe_smem<R, FeDims>();
-    // split precision: the 3-body kernel left its part of the weights in F
-    const C<float>* g3 = sizeof(R) == 4 ? reinterpret_cast<const C<float>*>(b.F) : nullptr;
+    // split precision: the 3-body kernel's part of the weights (g3 in aux)
+    const C<float>* g3 =
+        sizeof(R) == 4 ? reinterpret_cast<const C<float>*>(static_cast<unsigned char*>(b.aux) +
+                                                           aux_layout(m, natom).g3)
+                       : nullptr;
     // outputs in host memory (acelib_ writing the caller's arrays directly):
     // the variants that store each tile's outputs as whole lines
 #define MAGACE_FORCES_SO(MB, PK, SO)                                                                                \

@@ -1026,8 +1026,9 @@ __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const 
 // another. The records are zeroed before the launch.
 template <class D, int NW, int LOOP>
 __global__ void __launch_bounds__(NW * 32, 1)
-    k_b3_fe(DeviceModel m, int natom, C<float>* F, double* __restrict__ rho3, int* err, int nfull, int parts,
-            unsigned char* __restrict__ tails, size_t tail_rec) {
+    k_b3_fe(DeviceModel m, int natom, const C<float>* __restrict__ F, C<float>* __restrict__ G3,
+            double* __restrict__ rho3, int* err, int nfull, int parts, unsigned char* __restrict__ tails,
+            size_t tail_rec) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
   const int nc = m.b3_nc;
@@ -1156,16 +1157,15 @@ __global__ void __launch_bounds__(NW * 32, 1)
       for (int w = 0; w < NW; ++w) r3 += rpart[w * 32 + lane];
       rho3[s_atom[lane]] = r3;
     }
-    // the block's 3-body gradients times their multiplicities, into the
-    // factor rows of its atoms (nothing reads F after this kernel): the
-    // force kernel assembles W = dE/drho (W_rest + g3) from them; atom-major,
-    // so that consecutive threads store consecutive elements of one row
+    // the block's 3-body gradients times their multiplicities, g3[atom][c]:
+    // the force kernel assembles W = dE/drho (W_rest + g3) from them;
+    // atom-major, so that consecutive threads store consecutive elements
     for (int q = threadIdx.x; q < nc * 32; q += blockDim.x) {
       const int a = q / nc, c = q - a * nc;
       if (a < na) {
         const C<float> gv = Gs[c * kB3Stride + a];
         const float mu = s_mult[c];
-        st_l2(F + static_cast<size_t>(s_atom[a]) * m.nF + c, {mu * gv.x, mu * gv.y}, pol_last);
+        st_l2(G3 + static_cast<size_t>(s_atom[a]) * nc + c, {mu * gv.x, mu * gv.y}, pol_last);
       }
     }
     __syncthreads();
@@ -1262,9 +1262,9 @@ __global__ void __launch_bounds__(64, MINB)
     const int atom = queue_atom(m, it);
     const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
     // with g3 (split path, Fe layout): W holds the 2-/4-body part of the
-    // unscaled weights and g3 the 3-body part per compact element (the
-    // 3-body kernel's output in F's rows); the weight is dE/drho (W + g3)
-    const C<float>* Ga = g3 ? g3 + static_cast<size_t>(atom) * m.nF : nullptr;
+    // unscaled weights and g3 [atom][nc] the 3-body part per compact element;
+    // the weight is dE/drho (W + g3)
+    const C<float>* Ga = g3 ? g3 + static_cast<size_t>(atom) * m.b3_nc : nullptr;
     const R sc = g3 ? to_r<R>(dedrho[static_cast<size_t>(atom) * 2]) : R(1);
     // weight w with its 3-body element c (-1: none); the A weights are the
     // first compact elements in the same order (c = w), the 2-body weights

@@ -111,3 +111,41 @@ def test_cuda_graph_replay(gpu_lib, batch, queue):
     ref = gpu_lib.acelib(nb2)
     for y, r in zip(outs, ref):
         assert rel_err(y.cpu().numpy(), r) < 1e-6
+
+
+def test_side_by_side_density_kernels_match_one_stream(gpu_lib):
+    """The split path runs its 2-/4-body and 3-body density kernels side by
+    side on two streams; with kernel timing on, every kernel runs on one
+    stream. On a 54,000-site system (about 1,700 blocks of 32 atoms, many
+    waves of both kernels, so that either may run far ahead of the other)
+    both give the same results up to the 3-body kernel's atomic order."""
+    import torch
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_vacancies(ncell=30, seed=3), 5.0)
+    gpu_lib.set_precision(1)
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    ins = [T(nb.dlist), T(nb.elist), T(nb.dlist_mom), T(nb.elist_mom), T(nb.dlist_momi), T(nb.elist_momi)]
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+
+    def run():
+        outs = [torch.empty(n, dtype=torch.float64, device=dev)
+                for n in (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)]
+        gpu_lib.compute_device(nb.natom, nb.nei, off.data_ptr(), *[x.data_ptr() for x in ins],
+                               *[y.data_ptr() for y in outs], s.cuda_stream)
+        s.synchronize()
+        gpu_lib.device_status()
+        return [y.cpu().numpy() for y in outs]
+
+    try:
+        gpu_lib.set_kernel_timing(False)
+        side = [run() for _ in range(3)]
+        gpu_lib.set_kernel_timing(True)
+        one = run()
+    finally:
+        gpu_lib.set_kernel_timing(False)
+    for got in side:
+        for x, y in zip(got, one):
+            assert rel_err(x, y) < 1e-6
