@@ -561,6 +561,18 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
         mir[f] = L.A0(nr, l, -m);
         sgn[f] = (m & 1) ? -1 : 1;
       }
+  // multiplicity of every WA weight in the force and torque loops
+  // (src/forces.F90:509-614): a weight with multiplicity 0 is never used, so
+  // its slot needs no entries
+  std::vector<char> wa_used(L.nW, 1);
+  for (int n1 = 0; n1 < L.n3a; ++n1)
+    for (int l1 = 0; l1 <= L.l3a; ++l1)
+      for (int m1 = -l1; m1 <= l1; ++m1)
+        for (int n2 = 0; n2 < L.n3m; ++n2)
+          for (int l2 = 0; l2 <= L.l3m; ++l2) {
+            const int w = L.WA(n1, l1, m1, n2, l2, 0);
+            if (w >= 0 && m1 < 0) wa_used[w] = 0;
+          }
   // density (A0-slot) terms, summed per factor set {A0, sorted others}
   using G0Key = std::array<int, 5>;  // arity, A0 factor, three others (ONE-padded)
   std::map<G0Key, std::array<double, 2>> g0;
@@ -581,7 +593,7 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
     kk[0] += k[0];
     kk[1] += k[1];
     for (int q = 1; q < rank; ++q) {
-      if (w[q] < 0) continue;
+      if (w[q] < 0 || (rank >= 3 && !wa_used[w[q]])) continue;
       int others[3], n = 0;
       for (int o = 0; o < rank; ++o)
         if (o != q) others[n++] = f[o];
