@@ -769,9 +769,11 @@ __device__ __forceinline__ constexpr int jmax_of(int i) {
   return PAT == 0 ? i + 1 : (PAT == 1 ? (i / NM + 1) * NM : (i / NM) * NM);
 }
 
-// factor of a task position: the compact element with its sign bits applied
+// factor of a task position: the compact element (low 13 bits) with its
+// sign bits (0x8000 real, 0x4000 imaginary) applied; 0x2000 marks a directly
+// read element whose gradient is not needed (weight multiplicity 0)
 __device__ __forceinline__ C<float> b3_load(const C<float>* Xs, unsigned code, int lane) {
-  const C<float> v = Xs[(code & 0x3fffu) * kB3Stride + lane];
+  const C<float> v = Xs[(code & 0x1fffu) * kB3Stride + lane];
   return {__uint_as_float(__float_as_uint(v.x) ^ ((code & 0x8000u) << 16)),
           __uint_as_float(__float_as_uint(v.y) ^ ((code & 0x4000u) << 17))};
 }
@@ -782,7 +784,7 @@ __device__ __forceinline__ C<float> b3_load(const C<float>* Xs, unsigned code, i
 __device__ __forceinline__ void b3_add(C<float>* Gs, const uint16_t* __restrict__ code,
                                        const uint16_t* __restrict__ code2, int pos, int lane, C<float> v, float cf) {
   const unsigned c = __ldg(code + pos);
-  if (!(c & 0xc000u)) {
+  if (!(c & 0xe000u)) {
     C<float>* g = Gs + c * kB3Stride + lane;
     atomicAdd(&g->x, cf * v.x);
     atomicAdd(&g->y, cf * v.y);

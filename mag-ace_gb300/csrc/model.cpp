@@ -950,6 +950,16 @@ int build_tables(Model& M, std::string& msg) {
       }
       D.mult[D.compact_of_weight[w]] = mu;
     }
+    // gradients of elements whose weight has multiplicity 0 are never used:
+    // such a direct read gets the 0x2000 flag (no gradient atomic), such a
+    // mirror target no mirror gradient
+    if (D.nc < 0x2000)
+      for (size_t q = 0; q < D.code.size(); ++q) {
+        uint16_t& c = D.code[q];
+        if (!(c & 0xc000) && D.mult[c & 0x1fff] == 0.0) c = static_cast<uint16_t>(c | 0x2000);
+        uint16_t& c2 = D.code2[q];
+        if (c2 != 0xffff && D.mult[c2 & 0x3fff] == 0.0) c2 = 0xffff;
+      }
   }
   return MAGACE_OK;
 }
