@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(64)
   static_assert(!PACKED || (sizeof(R) == 4 && D::H3 == D::H2 && D::NQ <= 32), "packed tiles: FP32, Fe layout");
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int row = lane >> 1, cb = lane & 1;
+  const uint64_t pol_f = l2_evict_first();  // split path: the factors are read once per density kernel
   // TMA: the staged tile lives in the M Y tile's space (sQ), which is not
   // read between the end of a tile's bond sums and the next tile's
   // features; its mbarrier after the other buffers
@@ -517,7 +518,22 @@ __global__ void __launch_bounds__(64)
     // complete the m' < 0 half by A(m1,m2) = (-1)^(m1+m2) conj A(-m1,-m2) and write F
     C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
     constexpr int nA = D::NRY * D::NM * D::LS3;
-    for (int s = t; s < nA; s += blockDim.x) {
+    if constexpr (sizeof(R) == 4) {
+      // split path: only the elements the density kernels read, A with
+      // m' >= 0 (the 3-body codes reach the other half as mirrors) and A2
+      // with m' <= 0 (the folded 2-body entries)
+      for (int q = t; q < D::NRY * D::NM * D::H3; q += blockDim.x) {
+        const int h = q % D::H3, l2 = l_of_h(h), m2 = h - l2 * (l2 + 1) / 2;
+        st_l2(Fa + m.offA + (q / D::H3) * D::LS3 + l2 * l2 + l2 + m2, accA[q], pol_f);
+      }
+      for (int q = t; q < D::NB * D::N2 * D::H2; q += blockDim.x) {
+        const int h = q % D::H2, l = l_of_h(h), mh = h - l * (l + 1) / 2;
+        const C<R> w = accA2[q];
+        const R sgn = R(parity(mh));
+        st_l2(Fa + m.offA2 + (q / D::H2) * D::LS2 + l * l + l - mh, mh ? C<R>{w.x * sgn, -w.y * sgn} : w, pol_f);
+      }
+    }
+    for (int s = t; s < (sizeof(R) == 4 ? 0 : nA); s += blockDim.x) {
       const int lmm = s % D::LS3, q = s / D::LS3, n2 = q % D::NM, ia = q / D::NM;
       const int lma = ia % D::LSA;
       const int l2 = l_of_lm(lmm), m2 = lmm - l2 * l2 - l2;
@@ -534,7 +550,7 @@ __global__ void __launch_bounds__(64)
       Fa[m.offA + s] = v;
     }
     constexpr int nA2 = D::NB * D::N2 * D::LS2;
-    for (int s = t; s < nA2; s += blockDim.x) {
+    for (int s = t; s < (sizeof(R) == 4 ? 0 : nA2); s += blockDim.x) {
       const int lm = s % D::LS2, q = s / D::LS2;  // q = n*N2 + nr
       const int l = l_of_lm(lm), mm = lm - l * l - l;
       const C<R> w = accA2[(q / D::N2) * D::NQ + (q % D::N2) * D::H2 + ph(l, mm < 0 ? -mm : mm)];
