@@ -8,15 +8,16 @@
 // unroll and their operands stay in registers:
 //   k_abasis_fe  the bond sums A and A2 are small GEMMs over the bonds of an
 //                atom; warp 0 owns 1 x 9 tiles of A, warp 1 1 x 15 tiles of A2.
-//   k_density_fe the 2- and 4-body terms through the gather table (split
+//   k_density_fe the 2- and 4-body terms through the rest table (split
 //                precision; FP64 uses the generic k_density).
-//   k_b3_fe      the 3-body density and weights as dense contractions per
-//                (angular combination, m-term) task, C[n0'][i][j] a X Y,
-//                exploiting the triangular cluster order, with 32 atoms
-//                in the lanes of each warp; then the embedding and the
-//                final weights of those atoms.
-//   k_forces_fe  per bond, U = W_A Q and V = W2 g + W_A^T RY with the
-//                weights transposed in shared memory for 16-byte loads.
+//   k_b3_fe      the 3-body density and its gradients as dense
+//                contractions per (angular combination, m-term) task,
+//                C[n0'][i][j] a X Y, exploiting the triangular cluster
+//                order, with 32 atoms in the lanes of each warp.
+//   k_finish_fe  per atom, the total density, the embedding and the energy.
+//   k_forces_fe  the weights dE/drho (W + g3), then per bond U = W_A Q and
+//                V = W2 g + W_A^T RY with the weights transposed in shared
+//                memory for 16-byte loads.
 
 // byte offsets in a split tail block's record of accumulators (aux_layout):
 // 3-body density [32] doubles, ticket, 3-body gradients [nc][32][2] floats
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(64)
 //
 // k_b3_fe (32 atoms per CTA, one per lane) evaluates the 3-body terms as
 // dense contractions per (angular combination, m-term) task and writes, per
-// atom, their density rho3 and the gradients mult * dRho3/dF into F's rows.
+// atom, their density rho3 and the gradients mult * dRho3/dF into g3.
 //
 // k_finish_fe (one atom per thread) adds rho = rho1 + rho_rest + rho3 and
 // evaluates the embedding and energy in FP64; the force kernel then forms
@@ -1040,7 +1041,7 @@ __device__ __forceinline__ float b3_task_po(const float* __restrict__ Cs, const 
 // adds its 3-body density and its gradients [nc][32] (re, im) into the tail
 // block's record in `tails` (tail_rec bytes per block) with global atomics,
 // then takes a ticket; the CTA that takes the last ticket loads the totals
-// and completes the block (embedding, final weights). No CTA waits on
+// and completes the block (its rho3 and g3). No CTA waits on
 // another. The records are zeroed before the launch.
 template <class D, int NW, int LOOP>
 __global__ void __launch_bounds__(NW * 32, 1)
