@@ -195,6 +195,28 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def profiled_traffic(kernel: str, path: str, ncell: int):
+    """DRAM bytes (read + write) of one launch of `kernel` from the committed
+    ncu summary of the same workload (profiles/*_split_16k.md, the default
+    20^3-cell workload in split precision), or None when there is none."""
+    if path != "split" or ncell != 20:
+        return None
+    name = {"k_abasis": "k_abasis_fe", "k_density": "k_density_fe", "k_b3": "k_b3_fe",
+            "k_forces": "k_forces_fe"}.get(kernel)
+    f = os.path.join(REPO, "profiles", f"{name}_split_16k.md") if name else None
+    if not f or not os.path.exists(f):
+        return None
+    total, found = 0.0, 0
+    scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    for line in open(f):
+        for metric in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            if f"`{metric}`" in line:
+                parts = line.strip().strip("|").split("|")[-1].split()
+                total += float(parts[0]) * scale.get(parts[1], 1.0)
+                found += 1
+    return (total, os.path.relpath(f, REPO)) if found == 2 else None
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     from magace import build as mbuild, lib
@@ -329,9 +351,10 @@ def gpu_arm(args, rank, world, local_rank):
     kms = P["kernel_ms"]
     names = P["names"]
     kflops = dict(flops)
-    if P["launches"] == 4:
+    if P["launches"] >= 4:  # split path of the specialised layout: the density kernel has the rest terms only
         kflops["k_density"] = flops["k_density_rest"]
     dom = int(np.argmax(kms))
+    traffic = profiled_traffic(names[dom], headline, args.ncell)
     fp_peak = peaks.get("fp64" if headline == "fp64" else "fp32")
     achieved = kflops[names[dom]] / (kms[dom] / 1e3) / 1e12
     line = {
@@ -348,7 +371,10 @@ def gpu_arm(args, rank, world, local_rank):
         "gpu_launches": P["launches"] * args.steps,
         "roofline": {"bound": "fp64" if headline == "fp64" else "fp32", "kernel": names[dom],
                      "achieved": achieved, "peak": fp_peak, "unit": "TFLOP/s",
-                     "frac": (achieved / fp_peak) if fp_peak else None, "traffic": None,
+                     "frac": (achieved / fp_peak) if fp_peak else None,
+                     "traffic": traffic[0] if traffic else None,
+                     "traffic_source": ("DRAM bytes read + written per launch, ncu summary " + traffic[1])
+                     if traffic else None,
                      "peak_source": "measured in this run: cuBLAS %s GEMM (TF32 off)" % ("DGEMM" if headline == "fp64" else "SGEMM"),
                      "flops_per_launch": kflops[names[dom]]},
         "kernel_ms": dict(zip(names, kms)),
