@@ -1280,6 +1280,22 @@ __global__ void __launch_bounds__(64, MINB)
   for (int it = blockIdx.x; it < natom; it += gridDim.x) {
     const int atom = queue_atom(m, it);
     const C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    if constexpr (sizeof(R) == 4) {
+      // the weights of the atom a CTA starting about one CTA lifetime later
+      // takes (MINB CTAs per SM resident), into L2
+      if (t == 0) {
+        unsigned nsm;
+        asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+        const int ahead = it + MINB * static_cast<int>(nsm);
+        if (ahead < natom) {
+          const int a2 = queue_atom(m, ahead);
+          const size_t wb = sizeof(C<R>) * static_cast<size_t>(m.nW);
+          if (wb % 16 == 0) bulk_prefetch_l2(W + static_cast<size_t>(a2) * m.nW, static_cast<uint32_t>(wb));
+          const size_t gb = sizeof(C<float>) * static_cast<size_t>(m.b3_nc);
+          if (g3 && gb % 16 == 0) bulk_prefetch_l2(g3 + static_cast<size_t>(a2) * m.b3_nc, static_cast<uint32_t>(gb));
+        }
+      }
+    }
     // with g3 (split path, Fe layout): W holds the 2-/4-body part of the
     // unscaled weights and g3 [atom][nc] the 3-body part per compact element;
     // the weight is dE/drho (W + g3)
