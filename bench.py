@@ -86,7 +86,7 @@ def workload(ncell: int, tmpdir: str, rank: int = 0):
 
 def flop_model(stats: dict, natom: int, nbond: int) -> dict:
     """Algorithmic FLOPs of one evaluation, per kernel, from the basis tables
-    ('FLOP model'). One complex multiply = 6, a complex MAC = 8,
+    as built at init for this potential. One complex multiply = 6, a complex MAC = 8,
     a complex-by-real MAC = 4, a cubic LUT evaluation = 6 (+6 with derivative)."""
     s = stats
     nM = s["n2m"] * (s["l2m"] + 1)          # magnetic radial functions per bond

@@ -1198,7 +1198,6 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   if (kernels) *kernels = nk;
   if (ev) cudaEventRecord(ev[1 + nd], st);
   if (fe) {
-    const size_t s3 = forces_fe_smem<R, FeDims>();
     // split precision: the 3-body kernel's part of the weights (g3 in aux)
     const C<float>* g3 =
         sizeof(R) == 4 ? reinterpret_cast<const C<float>*>(static_cast<unsigned char*>(b.aux) +
@@ -1207,11 +1206,14 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
     // outputs in host memory (acelib_ writing the caller's arrays directly):
     // the variants that store each tile's outputs as whole lines
 #define MAGACE_FORCES_SO(MB, PK, SO)                                                                                \
-  set_smem(k_forces_fe<R, FeDims, MB, PK, SO>, s3);                                                                 \
-  k_forces_fe<R, FeDims, MB, PK, SO><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,  \
-                                                           reinterpret_cast<const C<R>*>(b.W), b.edf, b.dedrho,      \
-                                                           b.fij, b.tij, b.ti0, static_cast<const R*>(b.stage), b.err, \
-                                                           g3)
+  {                                                                                                                 \
+    const size_t s3 = forces_fe_smem<R, FeDims>(SO);                                                                \
+    set_smem(k_forces_fe<R, FeDims, MB, PK, SO>, s3);                                                               \
+    k_forces_fe<R, FeDims, MB, PK, SO><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi,       \
+                                                             b.mhi, reinterpret_cast<const C<R>*>(b.W), b.edf,      \
+                                                             b.dedrho, b.fij, b.tij, b.ti0,                         \
+                                                             static_cast<const R*>(b.stage), b.err, g3);            \
+  }
 #define MAGACE_FORCES(MB, PK)                 \
   if (b.host_outputs) {                       \
     MAGACE_FORCES_SO(MB, PK, true);           \
@@ -1256,14 +1258,14 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
     if (precision == 0) {
       if (which == 0) return abasis_fe_smem<double, FeDims>();
       if (which == 1) return density_smem<double>(m);
-      return forces_fe_smem<double, FeDims>();
+      return forces_fe_smem<double, FeDims>(true);
     }
     if (which == 0) return abasis_fe_smem<float, FeDims>();
     if (which == 1) {
       const size_t a = density_fe_smem(m, 32), b = b3_fe_smem<FeDims>(m, 16);
       return a > b ? a : b;
     }
-    return forces_fe_smem<float, FeDims>();
+    return forces_fe_smem<float, FeDims>(true);
   }
   if (precision == 0) {
     if (which == 0) return abasis_smem<double>(m);

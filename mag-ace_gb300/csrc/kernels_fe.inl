@@ -1265,8 +1265,7 @@ __global__ void __launch_bounds__(64, MINB)
   R* cMd = cM + D::NMF * T;
   C<R>* cYa = reinterpret_cast<C<R>*>(cMd + D::NMF * T);  // full [LSA]
   C<R>* cdYa = cYa + D::LSA * T;                         // [LSA][3]
-  C<R>* cYm = cdYa + D::LSA * 3 * T;                     // half [H2]
-  double* sOut = reinterpret_cast<double*>(cYm + D::H2 * T);  // the tile's f_ij [T][3], then t_ij [T][3]
+  double* sOut = reinterpret_cast<double*>(cdYa + D::LSA * 3 * T);  // SOUT: the tile's f_ij [T][3], then t_ij [T][3]
   const int t = threadIdx.x;
   static_assert(!PACKED || sizeof(R) == 4, "packed contractions are FP32");
   static_assert(D::NB % 4 == 0 && D::NRY % 4 == 0, "planes are read four floats at a time");
@@ -1434,8 +1433,6 @@ __global__ void __launch_bounds__(64, MINB)
             }
           }
           ylm_half<R, true>(D::L2, mx, my, mz, Ym, dYm);
-  #pragma unroll
-          for (int h = 0; h < D::H2; ++h) cYm[h * T + t] = Ym[h];
         }
         // ---- force
         R fr = edf * cdv, ft[3] = {R(0), R(0), R(0)};
@@ -1688,8 +1685,8 @@ size_t b3_fe_smem(const DeviceModel& m, int nw) {
          sizeof(float) * m.b3_nc + sizeof(int) * m.b3_nc;
 }
 template <class R, class D>
-size_t forces_fe_smem() {
+size_t forces_fe_smem(bool sout) {
   return sizeof(C<R>) * (D::NQ * D::NB + D::NQ3 * D::NRY + D::NQ + 2) +
-         sizeof(R) * 64 * (D::NB + 2 * D::NR + 2 * D::NMF) + sizeof(C<R>) * 64 * (D::LSA * 4 + D::H2) +
-         sizeof(double) * 6 * 64 + 64;
+         sizeof(R) * 64 * (D::NB + 2 * D::NR + 2 * D::NMF) + sizeof(C<R>) * 64 * D::LSA * 4 +
+         (sout ? sizeof(double) * 6 * 64 : 0) + 64;
 }

@@ -430,3 +430,32 @@ def test_abasis_variants_on_device_inputs(gpu_lib, oracle_seeded, shift):
         for x, y in zip(got, res[0]):
             assert rel_err(x, y) < 1e-6
 
+
+def test_every_split_variant_matches_oracle(gpu_lib, oracle_seeded):
+    """Variant v of the 2-/4-body density, 3-body and force kernels together
+    (the A basis at min(v, 3)), on device arrays and through acelib_ with
+    host arrays (where the GPU writes host memory directly, the force
+    kernel's whole-line output form): every combination within the split
+    tolerance of the oracle and within 1e-6 of variant 0. Neighbours listed
+    out to 8.4 A give atoms of two 64-bond tiles."""
+    from magace import structures as S
+    nb = S.neighbor_data(_ragged_slab(), 8.4)
+    gpu_lib.set_precision(1)
+    try:
+        res = []
+        for v in range(6):
+            gpu_lib.set_tuning([min(v, 3), v, v, v])
+            res.append(_device_eval(gpu_lib, nb))
+            res.append(list(gpu_lib.acelib(nb)))
+    finally:
+        gpu_lib.set_tuning([0, 0, 0, 0])
+        gpu_lib.set_precision(0)
+    eo, fo, to, t0o = oracle_seeded.acelib(nb)
+    for got in res:
+        e, f, t, t0 = got
+        assert np.abs(e - eo).max() * 1e3 < 1.0 and np.abs(f - fo).max() * 1e3 < 10.0
+        for x, y in zip(got, (eo, fo, to, t0o)):
+            assert rel_err(x, y) < 1e-5
+        for x, y in zip(got, res[0]):
+            assert rel_err(x, y) < 1e-6
+
