@@ -9,9 +9,10 @@ N(0, 0.1 A), paramagnetic moments uniform on the sphere with
 |m| ~ U(1.5, 2.6) mu_B, cutoff 5.0 A, the seeded potential in the reference's
 example Fe layout. Synthetic, seeded data; no dataset is involved.
 
-  value   device-resident inputs, CUDA-event time of the three kernels per step
-  e2e     the drop-in acelib_ with host arrays (copies in and out inside the
-          timed region), wall clock per call
+  value   device-resident inputs, CUDA-event time of one whole evaluation per
+          step (all its kernels: three in FP64, five in split precision)
+  e2e     the drop-in acelib_ with host arrays (the host<->device transfers
+          inside the timed region), wall clock per call
 
 With --gpus N > 1 (torchrun), every rank evaluates its own configuration of
 the workload (same size, vacancies and moments seeded by rank; weak scaling,
@@ -500,10 +501,11 @@ def cpu_baseline(nb, pot, budget_s: float, steps: int = 1):
     n, dt = sample(min(nb.natom, 4 * threads))
     rate = n / dt
     n = int(max(threads, min(nb.natom, rate * budget_s / max(1, steps))))
-    rates = []
+    rates, step_s = [], []
     for _ in range(steps):
         n2, dt2 = sample(n)
         rates.append(n2 / dt2)
+        step_s.append(dt2)
     # one core, as the reference runs (single-threaded Fortran), on a sample
     # of about a fifth of the budget
     all_threads = threads
@@ -513,7 +515,8 @@ def cpu_baseline(nb, pot, budget_s: float, steps: int = 1):
     return {"value": float(np.mean(rates)), "unit": UNIT, "cores": all_threads, "kind": "port",
             "sample": f"{n} atoms of the workload per step (contiguous block), oracle port -Ofast, "
                       f"{all_threads} threads, chunk 32 atoms",
-            "serial": {"value": float(n1 / dt1), "cores": 1, "sample": f"{n1} atoms, one thread"}}
+            "serial": {"value": float(n1 / dt1), "cores": 1, "sample": f"{n1} atoms, one thread"},
+            "ms_per_sample_step": 1e3 * float(np.mean(step_s))}
 
 
 def reference_arm(args, rank):
@@ -528,7 +531,8 @@ def reference_arm(args, rank):
         cpu_baseline(nb, pot, budget_s=2.0)
     cb = cpu_baseline(nb, pot, budget_s=args.cpu_seconds * max(1, args.steps) / 2, steps=args.steps)
     line = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": cb["ms_per_sample_step"],
+            "ms_per_full_workload": 1e3 * nb.natom / cb["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded potential and structure)",
             "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": "reference-port"},
             "impl": "reference", "cpu_baseline": cb,
