@@ -103,7 +103,10 @@ int ace_basis_rows(int rank, int* out);
  * whose inputs are still being written on another stream passes that stream
  * (cudaStreamLegacy for the legacy default stream) or synchronises first. The call is
  * asynchronous with respect to the host. Check ace_device_status() after the
- * stream has completed. */
+ * stream has completed. One call (this one, ace_descriptors_device and acelib_)
+ * takes at most 715,827,882 bonds and atoms, since the kernels index the
+ * per-bond vectors as 3 j with 32-bit j; larger calls are refused with
+ * MAGACE_ERR_ARGS. */
 int ace_compute_device(int natom, int nei, const int* bond_offset, const double* r,
                        const double* e, const double* mag_j, const double* mhat_j,
                        const double* mag_i, const double* mhat_i, double* energy, double* fij,

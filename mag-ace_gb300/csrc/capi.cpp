@@ -152,6 +152,17 @@ int cuda_error(cudaError_t e, const char* what) {
   return set_error(MAGACE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// The kernels index the per-bond and per-atom vectors as 3 j with 32-bit j,
+// so one call takes at most INT_MAX / 3 = 715,827,882 bonds (and atoms).
+constexpr int kMaxCallSize = std::numeric_limits<int>::max() / 3;
+
+int check_sizes(int natom, int nei) {
+  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
+  if (natom > kMaxCallSize || nei > kMaxCallSize)
+    return set_error(MAGACE_ERR_ARGS, "more than 715,827,882 atoms or bonds in one call (32-bit indices): split the call");
+  return MAGACE_OK;
+}
+
 #define CUDA_TRY(call)                                \
   do {                                                \
     cudaError_t e_ = (call);                          \
@@ -688,7 +699,7 @@ int ace_compute_device(int natom, int nei, const int* bond_offset, const double*
                        const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
                        double* energy, double* fij, double* tij, double* ti0, void* stream) {
   Runtime& R = rt();
-  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
+  if (int st0 = check_sizes(natom, nei)) return st0;
   int st = upload_tables();
   if (st) return st;
   st = reserve_work(natom, nei, R.precision);
@@ -720,7 +731,7 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
                         const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
                         void* stream, int* rest_warps, int* b3_warps, int* force_blocks) {
   Runtime& R = rt();
-  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
+  if (int st0 = check_sizes(natom, nei)) return st0;
   int st = upload_tables();
   if (st) return st;
   st = reserve_work(natom, nei, R.precision);
@@ -843,7 +854,7 @@ int ace_descriptors_device(int natom, int nei, const int* bond_offset, const dou
                            const double* mag_j, const double* mhat_j, const double* mag_i, const double* mhat_i,
                            double* B, void* stream) {
   Runtime& R = rt();
-  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes");
+  if (int st0 = check_sizes(natom, nei)) return st0;
   int st = upload_tables();
   if (st) return st;
   st = reserve_work(natom, nei, 0);
@@ -951,7 +962,7 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
       std::fill(tlist, tlist + 3 * npacked, nan);
     }
   };
-  if (natom < 0 || nei < 0) return set_error(MAGACE_ERR_ARGS, "negative sizes"), void();
+  if (check_sizes(natom, nei)) return;
   if (!R.ready) return fail(MAGACE_ERR_NOT_INIT, "acelib_ called before a successful acelibini_", 0);
   std::vector<int>& off = R.h_off;
   off.assign(natom + 1, 0);
@@ -961,6 +972,7 @@ void acelib_(int* natom_p, int* nall, int* nei_p, int* nlist, int* occ, int* occ
     if (cnt > 0 && (nstart[i] < 1 || nstop[i] > nei)) return fail(MAGACE_ERR_ARGS, "bond range outside 1..nei", 0);
     if (occ && occ[i] != 1) return fail(MAGACE_ERR_ARGS, "element index other than 1 (single element)", 0);
     if (cnt > 0 && nstart[i] != off[i] + 1) contiguous = false;
+    if (cnt > kMaxCallSize - off[i]) return fail(MAGACE_ERR_ARGS, "the bond ranges hold more than 715,827,882 bonds", 0);
     off[i + 1] = off[i] + cnt;
   }
   const long npacked = off[natom];

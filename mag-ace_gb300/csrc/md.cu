@@ -22,6 +22,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <string>
@@ -41,6 +42,9 @@ constexpr double kMub = 5.78901e-5;         // eV/T (lammps/pair_spin_ace.cpp:57
 constexpr double kHbar = 6.582119569e-4;    // eV ps (metal units, hplanck / 2 pi)
 constexpr double kAccel = 9648.53321233100; // (eV/A)/amu -> A/ps^2
 constexpr int kMaxBondsPerAtom = 512;       // capacity guard of one atom's list
+// atoms of one system: with at most kMaxBondsPerAtom per atom the 32-bit
+// scan of the bond counts cannot overflow
+constexpr int kMaxMdAtoms = std::numeric_limits<int>::max() / kMaxBondsPerAtom;
 
 // --- small helpers -------------------------------------------------------
 struct Cell {
@@ -491,6 +495,9 @@ int build_list(MdState& S) {
   MD_CUDA(cudaMemcpyAsync(&flag, S.flags.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   MD_CUDA(cudaStreamSynchronize(st));
   if (flag) return runtime_error(MAGACE_ERR_ARGS, "more than 512 neighbours within rcut + skin for an atom");
+  // the evaluation indexes per-bond vectors as 3 j with 32-bit j
+  if (nb > std::numeric_limits<int>::max() / 3)
+    return runtime_error(MAGACE_ERR_ARGS, "more than 715,827,882 bonds within rcut + skin");
   S.nbond = nb;
   MD_CUDA(S.key.reserve(nb));
   for (auto* b : {&S.bi, &S.bj, &S.bsh, &S.rev}) MD_CUDA(b->reserve(nb));
@@ -559,6 +566,7 @@ int ace_md_create(int natom, const double* x, const double* v, const double* m, 
                   double mass_amu, double rcut, double skin, int* handle) {
   if (natom <= 0 || !x || !v || !m || !cell || !pbc || !handle || mass_amu <= 0 || rcut <= 0 || skin < 0)
     return runtime_error(MAGACE_ERR_ARGS, "invalid MD arguments");
+  if (natom > kMaxMdAtoms) return runtime_error(MAGACE_ERR_ARGS, "more than 4,194,303 atoms in one MD system");
   auto S = std::make_unique<MdState>();
   S->natom = natom;
   S->mass = mass_amu;

@@ -104,6 +104,19 @@ def test_error_codes(lib, tmp_path, seeded_potential):
     lib.set_tuning(before)
 
 
+def test_call_size_limits(lib):
+    """The kernels index per-bond vectors as 3 j with 32-bit j: a call with
+    more than 715,827,882 bonds or atoms is refused with MAGACE_ERR_ARGS
+    before any device work, like negative sizes."""
+    so = lib.load()
+    for natom, nei in ((0, 715_827_883), (715_827_883, 0), (-1, 0), (0, -5)):
+        assert so.ace_compute_device(natom, nei, *[None] * 12) == 7
+        assert so.ace_descriptors_device(natom, nei, *[None] * 9) == 7
+    n, big = ctypes.c_int(0), ctypes.c_int(715_827_883)
+    so.acelib_(ctypes.byref(n), ctypes.byref(n), ctypes.byref(big), *[None] * 15)
+    assert so.ace_last_error() == 7
+
+
 def test_acelibini_reads_working_directory(lib, tmp_path, seeded_potential, monkeypatch):
     """acelibini_(nele=1, ..., elenumbers=[27]) opens ./Fe.pbe.in
     (src/util.F90:525; 27 = atomic number 26 + 1)."""
