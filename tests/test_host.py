@@ -117,6 +117,39 @@ def test_call_size_limits(lib):
     assert so.ace_last_error() == 7
 
 
+def test_plain_c_caller_links(lib, tmp_path, seeded_potential):
+    """A C program that declares the two entry points by their argument lists
+    alone, as the pair style does (lammps/pair_spin_ace.cpp:59-62: every
+    argument by reference, gfortran naming), links against libmagace.so,
+    initialises from the working directory and gets a status code back."""
+    import shutil
+    import subprocess
+    src = tmp_path / "caller.c"
+    src.write_text(r"""
+extern void acelibini_(int*, double*, double*, double*, int*, int*);
+extern void acelib_(int*, int*, int*, int*, int*, int*, int*, int*, double*, double*, double*, double*,
+                    double*, double*, double*, double*, double*, double*);
+extern int ace_last_error(void);
+int main(void) {
+  int nele = 1, xc = 1, el[1] = {27}; /* Fe: atomic number + 1 */
+  double rcut = 5.0, rcut_mag = 4.0, smear = 0.2;
+  acelibini_(&nele, &rcut, &rcut_mag, &smear, &xc, el);
+  if (ace_last_error() != 0) return 1;
+  int natom = -1, nall = 0, nei = 0; /* refused before any device work */
+  acelib_(&natom, &nall, &nei, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0);
+  return ace_last_error() == 7 ? 0 : 2;
+}
+""")
+    libdir = os.path.dirname(lib.LIB_PATH)
+    exe = tmp_path / "caller"
+    cc = subprocess.run(["gcc", str(src), "-o", str(exe), "-L" + libdir, "-lmagace", "-Wl,-rpath," + libdir],
+                        capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr
+    shutil.copy(seeded_potential, tmp_path / "Fe.pbe.in")
+    run = subprocess.run([str(exe)], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
+
+
 def test_acelibini_reads_working_directory(lib, tmp_path, seeded_potential, monkeypatch):
     """acelibini_(nele=1, ..., elenumbers=[27]) opens ./Fe.pbe.in
     (src/util.F90:525; 27 = atomic number 26 + 1)."""
