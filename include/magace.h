@@ -159,9 +159,13 @@ int ace_table_stats(long long* out);
  * the reference. Same arguments and results as ace_compute_device, but it
  * calls no cudaMalloc/cudaFree or allocating routine: its per-atom scratch
  * lives in one fixed 64 MiB device array that every GPU loading the library
- * holds until exit, which bounds natom (about 2000 atoms in FP64 and 4000 in
- * the split precision for the example Fe basis); larger calls are refused
- * with MAGACE_ERR_ARGS. The potential's tables must already be on the device
+ * holds until exit, which bounds natom: for the example Fe basis on a
+ * 152-SM GB300, at most 2,097 atoms in FP64 and 3,305 in the split precision
+ * (the refusal's message gives the limit for the loaded potential). Larger
+ * calls, and calls beyond ace_compute_device's bond limit, are refused with
+ * MAGACE_ERR_ARGS. When the bond arrays are device memory, the A-basis
+ * kernel variants that stage bond tiles with bulk copies may run, as in
+ * ace_compute_device. The potential's tables must already be on the device
  * (placed by any ace_compute_device call; natom = 0 is enough). The first call
  * on each device looks up the scratch address (cudaGetSymbolAddress); make
  * that first call before any stream capture. Calls share the scratch, so

@@ -526,6 +526,10 @@ int runtime_snapshot(DeviceModel* dm, int* precision, int* grid_cap) {
 
 int runtime_error(int code, const char* msg) { return set_error(code, msg); }
 
+int runtime_check_sizes(int natom, int nei) { return check_sizes(natom, nei); }
+
+bool runtime_device_resident(const void* r, const void* e, const void* mag_j, const void* mhat_j);
+
 int runtime_device_error(int dev_err) { return dev_err ? device_error_to_status(dev_err) : set_error(MAGACE_OK, ""); }
 
 void runtime_set_launches(int slots, int kernels) {
@@ -536,6 +540,30 @@ void runtime_set_launches(int slots, int kernels) {
 }  // namespace magace
 
 using namespace magace;
+
+// True when every non-null pointer is device memory, 8-byte aligned: the
+// bond arrays the TMA-staged A-basis variants read with bulk copies.
+static bool device_resident(std::initializer_list<const void*> ptrs) {
+  for (const void* p : ptrs) {
+    if (!p) continue;
+    if (reinterpret_cast<uintptr_t>(p) & 7u) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (a.type != cudaMemoryTypeDevice) return false;
+  }
+  return true;
+}
+
+
+namespace magace {
+// The same check for the allocation-free entry point (noalloc.cu).
+bool runtime_device_resident(const void* r, const void* e, const void* mag_j, const void* mhat_j) {
+  return device_resident({r, e, mag_j, mhat_j});
+}
+}  // namespace magace
 
 extern "C" {
 
@@ -677,22 +705,6 @@ int ace_table_stats(long long* out) {
   out[29] = pairs;
   out[30] = R.model.rest.nfac;
   return MAGACE_OK;
-}
-
-// True when every non-null pointer is device memory, 8-byte aligned: the
-// bond arrays the TMA-staged A-basis variants read with bulk copies.
-static bool device_resident(std::initializer_list<const void*> ptrs) {
-  for (const void* p : ptrs) {
-    if (!p) continue;
-    if (reinterpret_cast<uintptr_t>(p) & 7u) return false;
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    if (a.type != cudaMemoryTypeDevice) return false;
-  }
-  return true;
 }
 
 int ace_compute_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,

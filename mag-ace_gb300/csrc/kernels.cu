@@ -1253,6 +1253,17 @@ size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom) {
   return aux_layout(m, natom).end;
 }
 
+size_t eval_aux_bytes_bound(const DeviceModel& m, int precision, int natom) {
+  // as eval_aux_bytes, with room for the most tail records any split can
+  // use (a split tail has at most half an SM count of blocks, and never more
+  // blocks than there are), so that the bound never falls as natom grows
+  if (precision == 0 || !use_specialised(m) || natom <= 0) return 0;
+  const AuxLayout L = aux_layout(m, natom);
+  const size_t nblk = (static_cast<size_t>(natom) + 31) / 32;
+  const size_t half = static_cast<size_t>(sm_count()) / 2;
+  return L.tail0 + L.rec * (nblk < half ? nblk : half);
+}
+
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
   if (use_specialised(m)) {
     if (precision == 0) {

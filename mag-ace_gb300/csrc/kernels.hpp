@@ -73,6 +73,8 @@ void upload_ylm_constants(const double* alm, const double* blm, const double* cl
 size_t eval_smem_bytes(const DeviceModel& m, int precision, int which);
 // Size of EvalBuffers::aux for natom atoms (0 when the kernels need none).
 size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom);
+// An upper bound of eval_aux_bytes that never decreases as natom grows.
+size_t eval_aux_bytes_bound(const DeviceModel& m, int precision, int natom);
 // Launches the A-basis, density and force phases on `st` and returns the
 // number n of timed slots: 3 (A basis, density, forces) or, when the
 // split-precision density runs its 3-body part in kernels of its own, 4 (the

@@ -21,6 +21,8 @@
 namespace magace {
 
 int runtime_snapshot(DeviceModel* dm, int* precision, int* grid_cap);
+int runtime_check_sizes(int natom, int nei);
+bool runtime_device_resident(const void* r, const void* e, const void* mag_j, const void* mhat_j);
 int runtime_error(int code, const char* msg);
 int runtime_device_error(int dev_err);
 void runtime_set_launches(int slots, int kernels);
@@ -40,6 +42,49 @@ void* g_scratch_addr[kMaxDevices] = {nullptr};  // device address per device
 
 size_t round256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
+// Byte offsets of one call's arrays in the scratch. Every size is an upper
+// bound that never falls as natom grows, so the atoms that fit form one
+// range 0..max_atoms().
+struct ScratchLayout {
+  size_t err, F, W, rho1, core, edf, dedrho, aux, aux_bytes, end;
+};
+ScratchLayout scratch_layout(const DeviceModel& dm, int precision, int natom) {
+  const size_t csz = precision == 0 ? 16 : 8;  // complex FP64 / FP32
+  const size_t na = static_cast<size_t>(natom);
+  ScratchLayout L;
+  size_t off = 0;
+  L.err = off;
+  off += 256;
+  L.F = off;
+  off += round256(na * dm.nF * csz);
+  L.W = off;
+  off += round256(na * dm.nW * csz);
+  L.rho1 = off;
+  off += round256(na * 2 * sizeof(double));
+  L.core = off;
+  off += round256(na * sizeof(double));
+  L.edf = off;
+  off += round256(na * sizeof(double));
+  L.dedrho = off;
+  off += round256(na * 2 * sizeof(double));
+  L.aux = off;
+  L.aux_bytes = eval_aux_bytes_bound(dm, precision, natom);
+  off += round256(L.aux_bytes);
+  L.end = off;
+  return L;
+}
+
+// The largest natom whose layout fits the scratch.
+int max_atoms(const DeviceModel& dm, int precision) {
+  int lo = 0, hi = 1;
+  while (scratch_layout(dm, precision, hi).end <= kScratchBytes) hi *= 2;
+  while (hi - lo > 1) {
+    const int mid = lo + (hi - lo) / 2;
+    (scratch_layout(dm, precision, mid).end <= kScratchBytes ? lo : hi) = mid;
+  }
+  return lo;
+}
+
 }  // namespace
 }  // namespace magace
 
@@ -49,7 +94,8 @@ extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_of
                                           const double* e, const double* mag_j, const double* mhat_j,
                                           const double* mag_i, const double* mhat_i, double* energy,
                                           double* fij, double* tij, double* ti0, void* stream) {
-  if (natom < 0 || nei < 0) return runtime_error(MAGACE_ERR_ARGS, "negative sizes");
+  // the same per-call limits as ace_compute_device (32-bit bond indexing)
+  if (int st0 = runtime_check_sizes(natom, nei)) return st0;
   DeviceModel dm;
   int precision = 0, grid_cap = 1;
   int st = runtime_snapshot(&dm, &precision, &grid_cap);
@@ -67,35 +113,17 @@ extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_of
     g_scratch_addr[dev] = p;
   }
   unsigned char* base = static_cast<unsigned char*>(g_scratch_addr[dev]);
-  const size_t csz = precision == 0 ? 16 : 8;  // complex FP64 / FP32
-  const size_t na = static_cast<size_t>(natom);
-  size_t off = 0;
-  const size_t o_err = off;
-  off += 256;
-  const size_t o_F = off;
-  off += round256(na * dm.nF * csz);
-  const size_t o_W = off;
-  off += round256(na * dm.nW * csz);
-  const size_t o_rho1 = off;
-  off += round256(na * 2 * sizeof(double));
-  const size_t o_core = off;
-  off += round256(na * sizeof(double));
-  const size_t o_edf = off;
-  off += round256(na * sizeof(double));
-  const size_t o_dedrho = off;
-  off += round256(na * 2 * sizeof(double));
-  const size_t o_aux = off;
-  const size_t aux_bytes = eval_aux_bytes(dm, precision, natom);
-  off += round256(aux_bytes);
-  if (off > kScratchBytes) {
-    const size_t per_atom = dm.nF * csz + dm.nW * csz + 6 * sizeof(double) + (na ? aux_bytes / na : 0);
-    static char msg[160];
-    snprintf(msg, sizeof(msg), "natom = %d exceeds the allocation-free scratch (64 MiB, about %zu atoms for this potential and precision)",
-             natom, (kScratchBytes - 2048) / per_atom);
+  const ScratchLayout L = scratch_layout(dm, precision, natom);
+  if (L.end > kScratchBytes) {
+    static char msg[200];
+    snprintf(msg, sizeof(msg),
+             "natom = %d exceeds the allocation-free scratch: at most %d atoms fit in its 64 MiB for this "
+             "potential and precision",
+             natom, max_atoms(dm, precision));
     return runtime_error(MAGACE_ERR_ARGS, msg);
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  int* err = reinterpret_cast<int*>(base + o_err);
+  int* err = reinterpret_cast<int*>(base + L.err);
   // every call shares the scratch; only the error word must start at zero,
   // the kernels overwrite every other entry they read
   ce = cudaMemsetAsync(err, 0, sizeof(int), s);
@@ -114,14 +142,17 @@ extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_of
   b.fij = fij;
   b.tij = tij;
   b.ti0 = ti0;
-  b.F = base + o_F;
-  b.W = base + o_W;
-  b.rho1 = reinterpret_cast<double*>(base + o_rho1);
-  b.core = reinterpret_cast<double*>(base + o_core);
-  b.edf = reinterpret_cast<double*>(base + o_edf);
-  b.dedrho = reinterpret_cast<double*>(base + o_dedrho);
+  b.F = base + L.F;
+  b.W = base + L.W;
+  b.rho1 = reinterpret_cast<double*>(base + L.rho1);
+  b.core = reinterpret_cast<double*>(base + L.core);
+  b.edf = reinterpret_cast<double*>(base + L.edf);
+  b.dedrho = reinterpret_cast<double*>(base + L.dedrho);
   b.err = err;
-  b.aux = aux_bytes ? base + o_aux : nullptr;
+  b.aux = L.aux_bytes ? base + L.aux : nullptr;
+  // device-memory bond arrays let the A-basis kernel variants that stage
+  // bond tiles with bulk copies run, as in ace_compute_device
+  b.dev_inputs = runtime_device_resident(r, e, mag_j, mhat_j);
   int nk = 0;
   const int n = precision == 0 ? launch_eval_fp64(dm, b, s, grid_cap, nullptr, &nk)
                                : launch_eval_fp32(dm, b, s, grid_cap, nullptr, &nk);

@@ -112,6 +112,7 @@ def test_call_size_limits(lib):
     for natom, nei in ((0, 715_827_883), (715_827_883, 0), (-1, 0), (0, -5)):
         assert so.ace_compute_device(natom, nei, *[None] * 12) == 7
         assert so.ace_descriptors_device(natom, nei, *[None] * 9) == 7
+        assert so.ace_compute_device_noalloc(natom, nei, *[None] * 12) == 7
     n, big = ctypes.c_int(0), ctypes.c_int(715_827_883)
     so.acelib_(ctypes.byref(n), ctypes.byref(n), ctypes.byref(big), *[None] * 15)
     assert so.ace_last_error() == 7

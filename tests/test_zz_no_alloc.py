@@ -67,16 +67,61 @@ def test_noalloc_matches_compute_device(seeded_potential, precision):
     lib.set_precision(0)
 
 
-def test_noalloc_refuses_more_atoms_than_its_scratch(seeded_potential):
+# limits of the 64 MiB scratch for the seeded Fe-layout potential on a
+# 152-SM GB300 (FP64, split precision)
+DOCUMENTED_LIMIT = {0: 2097, 1: 3305}
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_noalloc_takes_its_limit_and_refuses_one_more(seeded_potential, precision):
+    """The refusal message states the largest atom count the scratch holds;
+    a call with exactly that many atoms runs and matches ace_compute_device,
+    one more atom is refused with MAGACE_ERR_ARGS."""
+    import re
+
     import torch
-    from magace import lib
+    from magace import lib, structures as S
 
     lib.init(seeded_potential, "Fe", 5.0, 4.0, 0.2, 1)
-    lib.set_precision(0)
+    lib.set_precision(precision)
     so = lib.load()
-    # zero-atom regular call places the tables on the device
-    assert so.ace_compute_device(0, 0, None, None, None, None, None, None, None, None, None, None, None, None) == 0
-    st = so.ace_compute_device_noalloc(100000, 0, None, None, None, None, None, None, None, None, None, None,
-                                       None, None)
+    # a zero-atom regular call places the tables on the device
+    assert so.ace_compute_device(0, 0, *[None] * 12) == 0
+    st = so.ace_compute_device_noalloc(100000, 0, *[None] * 12)
     assert st == 7  # MAGACE_ERR_ARGS
-    assert b"scratch" in so.ace_last_error_message()
+    msg = so.ace_last_error_message().decode()
+    assert "scratch" in msg
+    limit = int(re.search(r"at most (\d+) atoms", msg).group(1))
+    if torch.cuda.get_device_properties(0).multi_processor_count == 152:
+        assert limit == DOCUMENTED_LIMIT[precision]
+    assert so.ace_compute_device_noalloc(limit + 1, 0, *[None] * 12) == 7
+
+    # exactly `limit` atoms: the first atoms of a larger bcc system
+    full = S.neighbor_data(S.bcc_fe_vacancies(ncell=12, seed=4), 5.0)
+    assert full.natom > limit
+    counts = (full.nstop - full.nstart + 1)[:limit]
+    nei = int(counts.sum())
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(counts)]).astype(np.int32), device=dev)
+    T = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    ins = [T(full.dlist[:nei]), T(full.elist[:3 * nei]), T(full.dlist_mom[:nei]), T(full.elist_mom[:3 * nei]),
+           T(full.dlist_momi[:limit]), T(full.elist_momi[:3 * limit])]
+    outs = lambda: [torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+                    for n in (limit, 3 * nei, 3 * nei, 3 * limit)]
+    ptr = lambda ts: [t.data_ptr() for t in ts]
+    stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    ref = outs()
+    assert so.ace_compute_device(limit, nei, off.data_ptr(), *ptr(ins), *ptr(ref), stream.cuda_stream) == 0
+    stream.synchronize()
+    assert so.ace_device_status() == 0
+    got = outs()
+    st = so.ace_compute_device_noalloc(limit, nei, off.data_ptr(), *ptr(ins), *ptr(got),
+                                       ctypes.c_void_p(stream.cuda_stream))
+    assert st == 0, so.ace_last_error_message()
+    tol = TOL if precision == 0 else 1e-6
+    for g, r in zip(got, ref):
+        g, r = g.cpu().numpy(), r.cpu().numpy()
+        assert np.all(np.isfinite(g))
+        assert _rel(g, r) <= tol
+    lib.set_precision(0)
