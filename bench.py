@@ -55,7 +55,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batch", type=int, default=1, help="also measure the 256-configuration uneven batch")
     p.add_argument("--md-steps", type=int, default=100, help="spin-lattice MD steps in split precision (0: skip)")
-    p.add_argument("--md-steps-fp64", type=int, default=3, help="spin-lattice MD steps in plain FP64")
+    p.add_argument("--md-steps-fp64", type=int, default=20, help="spin-lattice MD steps in plain FP64")
+    p.add_argument("--target-ncell", type=int, default=80,
+                   help="bcc cells per edge of the large evaluation (80: 1,024,000 atoms; 0: skip)")
+    p.add_argument("--target-steps-fp64", type=int, default=10, help="timed FP64 steps of the large evaluation")
     p.add_argument("--md-ncell", type=int, default=80, help="bcc cells per edge of the MD system")
     return p.parse_args()
 
@@ -70,14 +73,34 @@ def reduce_over_ranks(x: float, op: str, world: int, device) -> float:
     return float(t.item())
 
 
+def native_libraries() -> list:
+    """The shared libraries of this repository mapped into this process
+    (Linux /proc/self/maps), relative to the repository root."""
+    found = set()
+    try:
+        with open("/proc/self/maps") as fh:
+            for line in fh:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.endswith(".so") and path.startswith(REPO + os.sep):
+                    found.add(os.path.relpath(path, REPO))
+    except OSError:
+        pass
+    return sorted(found)
+
+
 def whole_job_rate(total_units: float, slowest_s: float) -> float:
     """Units of all ranks per second of the slowest rank."""
     return total_units / slowest_s
 
 
-def workload(ncell: int, tmpdir: str, rank: int = 0):
+def workload(ncell: int, tmpdir: str, rank: int = 0, enumerate_basis=None):
+    """The seeded potential and the bcc workload's neighbour data.
+    `enumerate_basis` lists the potential's cluster basis (default: the
+    library's host-only init; the reference arm passes the oracle's, so that
+    its process never loads the library)."""
     from magace import potential, structures as S
-    pot = potential.write_seeded_potential(os.path.join(tmpdir, "Fe.pbe.in"), seed=2024)
+    kw = {"enumerate_basis": enumerate_basis} if enumerate_basis else {}
+    pot = potential.write_seeded_potential(os.path.join(tmpdir, "Fe.pbe.in"), seed=2024, **kw)
     st = S.bcc_fe_vacancies(ncell=ncell, seed=2 + rank)
     nb = S.neighbor_data(st, 5.0)
     desc = (f"bcc Fe {ncell}x{ncell}x{ncell} cubic cells, 1% vacancies ({nb.natom} atoms, {nb.nei} bonds), "
@@ -324,30 +347,38 @@ def gpu_arm(args, rank, world, local_rank):
     total_atoms = reduce_over_ranks(nb.natom, "sum", world, dev)
     value = whole_job_rate(total_atoms, ms / 1e3)
 
-    # end-to-end through the drop-in acelib_ with host arrays, for each way of
-    # reaching host memory; "auto" is the library default
-    lib.set_precision(0 if headline == "fp64" else 1)
+    # end-to-end through the drop-in acelib_ with host arrays, in both
+    # precisions; for the headline path also each way of reaching host
+    # memory ("auto" is the library default)
     lib.set_kernel_timing(False)
-    e2e_modes = {}
     host_out = lib.acelib(nb)  # output arrays the caller keeps between steps
-    for mode in ("copy", "pinned", "auto"):
-        os.environ["MAGACE_HOST_ACCESS"] = mode
-        for _ in range(max(1, args.warmup)):
-            lib.acelib(nb, out=host_out)
-        ts = []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            lib.acelib(nb, out=host_out)
-            ts.append(time.perf_counter() - t0)
-        e2e_modes[mode] = float(np.mean(ts))
-    os.environ.pop("MAGACE_HOST_ACCESS", None)
-    e2e_s = reduce_over_ranks(e2e_modes["auto"], "max", world, dev)
+    e2e_path = {}
+    for name in paths:
+        lib.set_precision(0 if name == "fp64" else 1)
+        modes = ("copy", "pinned", "auto") if name == headline else ("auto",)
+        e2e_modes = {}
+        for mode in modes:
+            os.environ["MAGACE_HOST_ACCESS"] = mode
+            for _ in range(max(1, args.warmup)):
+                lib.acelib(nb, out=host_out)
+            ts = []
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                lib.acelib(nb, out=host_out)
+                ts.append(time.perf_counter() - t0)
+            e2e_modes[mode] = float(np.mean(ts))
+        os.environ.pop("MAGACE_HOST_ACCESS", None)
+        e2e_path[name] = e2e_modes
     h2d = (nb.natom + 1) * 4 + nb.nei * 8 * 8 + nb.natom * 8 * 4
     d2h = nb.natom * 8 * 4 + nb.nei * 8 * 6 + 4
+    e2e_s = {name: reduce_over_ranks(m["auto"], "max", world, dev) for name, m in e2e_path.items()}
+    lib.set_precision(0 if headline == "fp64" else 1)
 
     if rank != 0:
         return None
     batch = batch_measure(lib, torch, dev, args.steps, args.warmup) if args.batch else None
+    target = (target_measure(lib, torch, dev, args.target_ncell, args.target_steps_fp64, max(10, args.steps),
+                             args.warmup) if args.target_ncell > 0 else None)
     mdres = md_measure(lib, args.md_ncell, args.md_steps, args.md_steps_fp64) if args.md_steps > 0 else None
     kms = P["kernel_ms"]
     names = P["names"]
@@ -366,9 +397,9 @@ def gpu_arm(args, rank, world, local_rank):
         "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": headline,
                    "tuned": lib.get_tuning() if tuned else None,
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": whole_job_rate(total_atoms, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "host_access": lib.host_access(),
-                "ms_per_call": {k: v * 1e3 for k, v in e2e_modes.items()}},
+        "e2e": {"value": whole_job_rate(total_atoms, e2e_s[headline]), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "host_access": lib.host_access(), "path": headline,
+                "ms_per_call": {k: v * 1e3 for k, v in e2e_path[headline].items()}},
         "gpu_launches": P["launches"] * args.steps,
         "roofline": {"bound": "fp64" if headline == "fp64" else "fp32", "kernel": names[dom],
                      "achieved": achieved, "peak": fp_peak, "unit": "TFLOP/s",
@@ -381,11 +412,17 @@ def gpu_arm(args, rank, world, local_rank):
         "kernel_ms": dict(zip(names, kms)),
         "clocks": P["clocks"],
         "paths": {k: {"ms_per_step": v["ms"], "atom_evals_per_s": whole_job_rate(total_atoms, v["ms"] / 1e3),
-                      "kernel_ms": dict(zip(v["names"], v["kernel_ms"]))} for k, v in paths.items()},
+                      "kernel_ms": dict(zip(v["names"], v["kernel_ms"])),
+                      "e2e": {"value": whole_job_rate(total_atoms, e2e_s[k]), "unit": UNIT,
+                              "ms_per_call": e2e_s[k] * 1e3, "h2d_bytes_per_step": h2d,
+                              "d2h_bytes_per_step": d2h, "host_access": lib.host_access()}}
+                  for k, v in paths.items()},
         "split_error_vs_fp64": acc,
+        "target_config_eval": target,
         "uneven_batch": batch,
         "spin_lattice_md": mdres,
         "peaks_measured_tflops": peaks,
+        "native_libraries": native_libraries(),
     }
     return line, nb, pot
 
@@ -440,6 +477,90 @@ def batch_measure(lib, torch, dev, steps: int, warmup: int) -> dict:
         del g
     lib.set_work_queue(False)
     lib.device_status()
+    return res
+
+
+def target_measure(lib, torch, dev, ncell: int, steps_fp64: int, steps_split: int, warmup: int) -> dict:
+    """One evaluation of the large bcc system the benchmark spec's target is quoted
+    on (ncell^3 cubic cells; 80^3 = 1,024,000 atoms, a = 2.83 A), with
+    thermal-size jitter N(0, 0.05 A) and random spins |m| ~ U(1.5, 2.6) mu_B,
+    cutoff 5.0 A, device-resident inputs (the neighbour list from the
+    library's device builder), timed per step with CUDA events in both
+    precisions; the split results against the FP64 ones per result. The
+    inputs (about 64 bytes per bond) are far larger than L2, which is not
+    flushed."""
+    from magace import md, structures as S
+    rng = np.random.default_rng(11)
+    pos, cell = S.bcc_cubic(ncell, ncell, ncell, 2.83)
+    n = len(pos)
+    pos = pos + rng.normal(0.0, 0.05, pos.shape)
+    mag = rng.uniform(1.5, 2.6, n)
+    mhat = S.random_unit(rng, n)
+    st = S.Structure(pos, cell, (True, True, True), mag, mhat)
+    sim = md.SpinLatticeMD(st, temperature=0.0, seed=1, skin=0.0)
+    bl = sim.bonds()
+    sim.close()
+    T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    off = T(bl["off"], torch.int32)
+    nei = int(bl["off"][-1])
+    counts = np.diff(bl["off"])
+    ib = torch.repeat_interleave(torch.arange(n, device=dev), T(counts, torch.int64))
+    jb = T(bl["j"], torch.int64)
+    x, h = T(pos), T(cell)
+    d = x[ib] - x[jb] - T(bl["shift"]) @ h
+    del bl
+    r = torch.linalg.norm(d, dim=1)
+    e = (d / r[:, None]).reshape(-1).contiguous()
+    del d
+    mg, mh = T(mag), T(mhat)
+    ins = [r, e, mg[jb].contiguous(), mh[jb].reshape(-1).contiguous(), mg, mh.reshape(-1).contiguous()]
+    del ib, jb
+    outs = [torch.empty(k, dtype=torch.float64, device=dev) for k in (n, 3 * nei, 3 * nei, 3 * n)]
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+
+    def call():
+        lib.compute_device(n, nei, off.data_ptr(), *[t.data_ptr() for t in ins], *[t.data_ptr() for t in outs],
+                           s.cuda_stream)
+
+    res = {"workload": f"bcc Fe {ncell}x{ncell}x{ncell} cubic cells ({n} atoms, {nei} bonds), jitter N(0, 0.05 A), "
+                       "random spins |m| ~ U(1.5, 2.6) mu_B, rcut 5.0 A, seeded potential",
+           "atoms": n, "bonds": nei, "neighbours_min_max": [int(counts.min()), int(counts.max())],
+           "l2": "inputs of 64 B per bond, far larger than L2 (not flushed)"}
+    kept = {}
+    for name, prec, k in (("fp64", 0, steps_fp64), ("split", 1, steps_split)):
+        if k <= 0:
+            continue
+        lib.set_precision(prec)
+        with torch.cuda.stream(s):
+            for _ in range(max(1, warmup)):
+                call()
+        s.synchronize()
+        lib.device_status()
+        ts = []
+        with torch.cuda.stream(s):
+            for _ in range(k):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                call()
+                b.record(s)
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+        lib.device_status()
+        ms = float(np.mean(ts))
+        res[name] = {"steps": k, "ms_per_step": ms, "atom_evals_per_s": n / (ms / 1e3)}
+        kept[name] = [t.clone() for t in outs]
+    lib.set_precision(0)
+    if "fp64" in kept and "split" in kept:
+        a, b = kept["split"], kept["fp64"]
+        res["split_over_fp64"] = res["split"]["atom_evals_per_s"] / res["fp64"]["atom_evals_per_s"]
+        res["split_error_vs_fp64"] = {
+            "energy_meV_per_atom": float((a[0] - b[0]).abs().max()) * 1e3,
+            "force_meV_per_A": float((a[1] - b[1]).abs().max()) * 1e3,
+            "magforce_meV_per_muB": max(float((a[2] - b[2]).abs().max()), float((a[3] - b[3]).abs().max())) * 1e3,
+            "energy_rms_meV_per_atom": float(torch.sqrt(((a[0] - b[0]) ** 2).mean())) * 1e3}
+    del kept, outs, ins
+    torch.cuda.empty_cache()
     return res
 
 
@@ -523,10 +644,18 @@ def reference_arm(args, rank):
     if rank != 0:
         return
     tmp = tempfile.mkdtemp(prefix="magace_ref_")
-    pot, nb, desc = workload(args.ncell, tmp)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as orc
     orc.build()
+
+    def oracle_rows(header, element, rcut, rcut_magnetic, smearing, xcnumber):
+        o = orc.Oracle(header, element, rcut=rcut, rcut_magnetic=rcut_magnetic, smear=smearing,
+                       xcnumber=xcnumber, fast=True)
+        return {r: o.basis_rows(r) for r in (1, 2, 3, 4)}
+
+    # the potential's basis comes from the oracle: this process never loads
+    # the library (libmagace.so)
+    pot, nb, desc = workload(args.ncell, tmp, enumerate_basis=oracle_rows)
     for _ in range(min(args.warmup, 1)):
         cpu_baseline(nb, pot, budget_s=2.0)
     cb = cpu_baseline(nb, pot, budget_s=args.cpu_seconds * max(1, args.steps) / 2, steps=args.steps)
@@ -535,7 +664,7 @@ def reference_arm(args, rank):
             "ms_per_full_workload": 1e3 * nb.natom / cb["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded potential and structure)",
             "config": {"workload": desc, "atoms": nb.natom, "bonds": nb.nei, "path": "reference-port"},
-            "impl": "reference", "cpu_baseline": cb,
+            "impl": "reference", "cpu_baseline": cb, "native_libraries": native_libraries(),
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -56,21 +56,31 @@ def header_lines(element: str, xc: str, smearing: float, lam=(5.25, 5.25), cut=(
     ]
 
 
+def library_basis_rows(header: str, element: str, rcut: float, rcut_magnetic: float, smearing: float,
+                       xcnumber: int) -> dict:
+    """The cluster rows of ranks 1..4 that the library enumerates for the
+    potential file `header` (its host-only init; no GPU)."""
+    lib.init(header, element, rcut, rcut_magnetic, smearing, xcnumber)
+    return {r: lib.basis_rows(r) for r in (1, 2, 3, 4)}
+
+
 def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, element: str = "Fe",
                            xc: str = "pbe", smearing: float = 0.2, layout=FE_LAYOUT,
-                           cut=(5.0, 4.0), core=(0.0, 0.0), par=(1.0, 1.0), par2=(1.0, 1.0)) -> str:
-    """Writes the seeded potential to `path` and returns the path. Uses the
-    library's host-only init (no GPU) to enumerate the cluster basis. With
-    two densities, `par2` holds the second density's embedding parameters
-    and its cluster values come from a second generator (seed + 1), so the
-    first density's records do not depend on the layout's density count."""
+                           cut=(5.0, 4.0), core=(0.0, 0.0), par=(1.0, 1.0), par2=(1.0, 1.0),
+                           enumerate_basis=library_basis_rows) -> str:
+    """Writes the seeded potential to `path` and returns the path.
+    `enumerate_basis(header, element, rcut, rcut_magnetic, smearing,
+    xcnumber)` lists the cluster basis of the header-only file `header`;
+    by default the library's host-only init (no GPU). With two densities,
+    `par2` holds the second density's embedding parameters and its cluster
+    values come from a second generator (seed + 1), so the first density's
+    records do not depend on the layout's density count."""
     head = header_lines(element, xc, smearing, cut=cut, layout=layout)
     with tempfile.TemporaryDirectory() as td:
         tmp = os.path.join(td, "header.in")
         with open(tmp, "w") as f:
             f.write("\n".join(head) + "\n")
-        lib.init(tmp, element, cut[0], cut[1], smearing, 1 if xc == "pbe" else 2)
-        rows = {r: lib.basis_rows(r) for r in (1, 2, 3, 4)}
+        rows = enumerate_basis(tmp, element, cut[0], cut[1], smearing, 1 if xc == "pbe" else 2)
     rng = np.random.default_rng(seed)
     L = layout
     out = list(head)

@@ -223,34 +223,39 @@ def bcc_110_slab(nx: int, ny: int, layers: int, a: float, vacuum: float) -> tupl
 
 def uneven_batch(nconf: int = 256, seed: int = 3) -> list:
     """Independent configurations of 16-432 atoms with 20-70 neighbours per
-    atom within 5 A: bcc and fcc Fe bulk, bcc cells with vacancies, and
-    (100) / (110) bcc slabs with 10 A of vacuum; jitter N(0, 0.1 A), random
-    spins with |m| ~ U(1.5, 2.6) mu_B."""
+    atom within 5 A: bcc and fcc Fe bulk and bcc cells with vacancies, each
+    under a hydrostatic strain (lattice constant scaled by U(0.88, 1.02), so
+    that the compressed cells reach 60-70 neighbours), and (100) / (110) bcc
+    slabs of one or more cubic repeats with 10 A of vacuum (20-40 neighbours
+    at their surfaces); jitter N(0, 0.1 A), random spins with
+    |m| ~ U(1.5, 2.6) mu_B."""
     rng = np.random.default_rng(seed)
     out = []
     kinds = ("bcc", "fcc", "vac", "s100", "s110")
     for c in range(nconf):
         kind = kinds[c % len(kinds)]
         pbc = (True, True, True)
+        scale = float(rng.uniform(0.88, 1.02))
         if kind == "bcc":
             n = int(rng.integers(2, 7))                     # 16 .. 432 atoms
-            pos, cell = bcc_cubic(n, n, n, 2.83)
+            pos, cell = bcc_cubic(n, n, n, 2.83 * scale)
         elif kind == "fcc":
             n = int(rng.integers(2, 5))                     # 32 .. 256 atoms
-            pos, cell = fcc_cubic(n, n, n, 3.59)
+            pos, cell = fcc_cubic(n, n, n, 3.59 * scale)
         elif kind == "vac":
             n = int(rng.integers(3, 7))
-            pos, cell = bcc_cubic(n, n, n, 2.83)
+            pos, cell = bcc_cubic(n, n, n, 2.83 * scale)
             keep = rng.random(len(pos)) > 0.05
             keep[0] = True
             pos = pos[keep]
         elif kind == "s100":
-            n, layers = int(rng.integers(2, 5)), int(rng.integers(2, 6))
+            layers = int(rng.integers(1, 6))
+            n = int(rng.integers(3 if layers == 1 else 2, 5))  # at least 16 atoms
             pos, cell = bcc_cubic(n, n, layers, 2.83)
             cell[2, 2] += 10.0
             pbc = (True, True, False)
         else:
-            n, layers = int(rng.integers(2, 4)), int(rng.integers(2, 5))
+            n, layers = int(rng.integers(2, 4)), int(rng.integers(1, 5))
             pos, cell = bcc_110_slab(n, 2 * n, layers, 2.83, 10.0)
             pbc = (True, True, False)
         pos = pos + rng.normal(0.0, 0.1, size=pos.shape)

@@ -12,7 +12,6 @@ sys.path.insert(0, os.path.join(REPO, "mag-ace_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 sys.path.insert(0, REPO)
 
-REFERENCE_FE = "/root/reference/example/Fe.pbe.in"
 GOLDEN = os.path.join(REPO, "tests", "golden")
 
 
@@ -35,6 +34,29 @@ def seeded_potential(tmp_path_factory):
     path = str(tmp_path_factory.mktemp("pot") / "Fe.pbe.in")
     potential.write_seeded_potential(path, seed=2024)
     return path
+
+
+@pytest.fixture(scope="session")
+def reference_fe(tmp_path_factory):
+    """The reference's example potential example/Fe.pbe.in (cut 4.5 A /
+    4.0 mu_B), unpacked from the committed fixture tests/golden/Fe.pbe.in.gz
+    into a directory of its own and checked against its pinned sha256."""
+    import gzip
+    import hashlib
+    import json
+    meta = json.load(open(os.path.join(GOLDEN, "reference_fe.json")))
+    with gzip.open(os.path.join(GOLDEN, "Fe.pbe.in.gz"), "rb") as gz:
+        raw = gz.read()
+    assert hashlib.sha256(raw).hexdigest() == meta["sha256"], "Fe.pbe.in fixture does not match its pinned hash"
+    path = tmp_path_factory.mktemp("reference_fe") / "Fe.pbe.in"
+    path.write_bytes(raw)
+    return str(path)
+
+
+@pytest.fixture(scope="session")
+def oracle_fe(reference_fe):
+    import oracle as orc
+    return orc.Oracle(reference_fe, "Fe", rcut=4.5, rcut_magnetic=4.0, smear=0.2)
 
 
 @pytest.fixture(scope="session")

@@ -13,7 +13,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REFERENCE_FE, REPO
+from conftest import GOLDEN, REPO
 
 
 @pytest.fixture(scope="module")
@@ -49,10 +49,8 @@ def test_init_and_basis_match_oracle(lib, seeded_potential, oracle_seeded):
         assert np.array_equal(lib.basis_rows(r), oracle_seeded.basis_rows(r))
 
 
-def test_reference_potential_matches_enumeration(lib):
-    if not os.path.exists(REFERENCE_FE):
-        pytest.skip("reference example potential not available")
-    lib.init(REFERENCE_FE, "Fe", 4.5, 4.0, 0.2, 1)
+def test_reference_potential_matches_enumeration(lib, reference_fe):
+    lib.init(reference_fe, "Fe", 4.5, 4.0, 0.2, 1)
     sz = lib.basis_sizes()
     # every record of example/Fe.pbe.in is an enumerated cluster
     assert sz["nvar"] == (16, 720, 4932, 495) and sz["unmatched"] == 0

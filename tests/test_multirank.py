@@ -74,3 +74,19 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(bench, "workload", lambda *a, **k: called.append(a))
     bench.reference_arm(Args(), rank=1)
     assert called == [] and capsys.readouterr().out == ""
+
+
+def test_reference_arm_never_loads_the_library(tmp_path):
+    """The reference arm enumerates the seeded potential's basis with the
+    oracle: its process maps the oracle's library and never libmagace.so."""
+    import json
+    import subprocess
+    run = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--ncell", "2",
+                          "--steps", "1", "--warmup", "1", "--cpu-seconds", "0.2"],
+                         capture_output=True, text=True, timeout=600, cwd=tmp_path)
+    assert run.returncode == 0, run.stderr
+    line = json.loads(run.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    libs = line["native_libraries"]
+    assert any("oracle" in p for p in libs), libs
+    assert not any("libmagace" in p for p in libs), libs

@@ -9,17 +9,9 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REFERENCE_FE
+from conftest import GOLDEN
 
 NOTEBOOK_ETOT = -15.7479878560111  # example/basic_lammps.ipynb:272
-
-
-@pytest.fixture(scope="module")
-def oracle_fe():
-    if not os.path.exists(REFERENCE_FE):
-        pytest.skip("reference example potential not available")
-    import oracle as orc
-    return orc.Oracle(REFERENCE_FE, "Fe", rcut=4.5, rcut_magnetic=4.0, smear=0.2)
 
 
 def test_basis_sizes_fe(oracle_fe):
@@ -48,6 +40,25 @@ def test_notebook_golden_fixture(oracle_fe):
     e, f, t, t0 = oracle_fe.acelib(nb)
     assert np.allclose(e, g["eout"], rtol=0, atol=1e-13)
     assert np.allclose(t0, g["tlist0"], rtol=0, atol=1e-13)
+
+
+def test_reference_cells_golden_fixture(oracle_fe):
+    """The oracle on example/Fe.pbe.in for the two non-collinear cells
+    reproduces the committed per-atom summaries
+    (tests/golden/reference_fe_cells.json)."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden as mg
+    from magace import structures as S
+    with open(os.path.join(GOLDEN, "reference_fe_cells.json")) as fh:
+        g = json.load(fh)
+    for name, st in mg.reference_cells().items():
+        nb = S.neighbor_data(st, 4.5)
+        got = mg.per_atom_summary(nb, *oracle_fe.acelib(nb))
+        for k in ("eout", "tlist0", "fsum", "tsum"):
+            assert np.allclose(got[k], g[name][k], rtol=0, atol=1e-12), (name, k)
+        for k in ("f_sumsq", "t_sumsq"):
+            assert abs(got[k] - g[name][k]) <= 1e-12 * abs(g[name][k]), (name, k)
 
 
 def _energy(orc, st, rcut):
