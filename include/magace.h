@@ -124,19 +124,21 @@ int ace_device_status(void);
  * device supports it, else 1. Returns -1 when no tables could be placed. */
 int ace_host_access_mode(void);
 
-/* Number of kernels launched by the last evaluation call: 3 for the FP64
- * path, 5 for the split path of the specialised layout (A basis, 2-/4-body
- * density, 3-body density, k_finish_fe, forces). */
+/* Number of kernels launched by the last evaluation call: 5 for the
+ * specialised (example Fe) layout in either precision (A basis, 2-/4-body
+ * density, 3-body density, k_finish_fe, forces), 3 for the generic kernels
+ * of other layouts (A basis, density, forces). */
 int ace_last_launch_count(void);
 
 /* Kernel timing: when on, the boundaries of the kernels of every evaluation
  * are recorded with CUDA events on the evaluation stream, and every kernel
- * runs on that stream (the split path otherwise runs its 2-/4-body and
- * 3-body density kernels side by side on two streams); ace_kernel_times
+ * runs on that stream (the specialised layout otherwise runs its 2-/4-body
+ * and 3-body density kernels side by side on two streams); ace_kernel_times
  * writes the last evaluation's per-kernel durations in ms into ms[0..3],
- * synchronising on the last event: k_abasis, k_density, k_forces (FP64), or
- * k_abasis, k_density, k_b3 (with k_finish_fe), k_forces (split path of the
- * specialised layout). Entries beyond those are 0. */
+ * synchronising on the last event: k_abasis, k_density, k_b3 (with
+ * k_finish_fe), k_forces (specialised layout, either precision), or
+ * k_abasis, k_density, k_forces (generic kernels). Entries beyond those are
+ * 0. */
 int ace_set_kernel_timing(int on);
 int ace_kernel_times(float* ms);
 
@@ -160,7 +162,7 @@ int ace_table_stats(long long* out);
  * calls no cudaMalloc/cudaFree or allocating routine: its per-atom scratch
  * lives in one fixed 64 MiB device array that every GPU loading the library
  * holds until exit, which bounds natom: for the example Fe basis on a
- * 152-SM GB300, at most 2,097 atoms in FP64 and 3,305 in the split precision
+ * 152-SM GB300, at most 1,816 atoms in FP64 and 3,305 in the split precision
  * (the refusal's message gives the limit for the loaded potential). Larger
  * calls, and calls beyond ace_compute_device's bond limit, are refused with
  * MAGACE_ERR_ARGS. When the bond arrays are device memory, the A-basis

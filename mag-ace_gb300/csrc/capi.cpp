@@ -106,6 +106,7 @@ struct Runtime {
     }
   } gb1, gb2;
   DevBuf<float> b3_Cf, b3_cff, b3_mult, b3_cfw;
+  DevBuf<double> b3_C64, b3_cf64, b3_cfw64;
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
   DevBuf<uint16_t> b3_code, b3_code2;
   DevBuf<int32_t> d_rank1_n, d_begin;
@@ -275,10 +276,13 @@ int upload_tables() {
       CUDA_TRY(R.b3_code.upload(D.code));
       CUDA_TRY(R.b3_code2.upload(D.code2));
       {
-        std::vector<float> cfw(D.ntask);
-        for (int t = 0; t < D.ntask; ++t) cfw[t] = static_cast<float>(D.task_cf[t] * D.task_w[t]);
-        CUDA_TRY(R.b3_cfw.upload(cfw));
+        std::vector<double> cfw(D.ntask);
+        for (int t = 0; t < D.ntask; ++t) cfw[t] = D.task_cf[t] * D.task_w[t];
+        CUDA_TRY(R.b3_cfw.upload(to_float(cfw)));
+        CUDA_TRY(R.b3_cfw64.upload(cfw));
       }
+      CUDA_TRY(R.b3_C64.upload(D.C));
+      CUDA_TRY(R.b3_cf64.upload(D.task_cf));
       CUDA_TRY(R.b3_factor.upload(D.factor_of));
       CUDA_TRY(R.b3_cw.upload(D.compact_of_weight));
       CUDA_TRY(R.b3_mult.upload(to_float(D.mult)));
@@ -345,6 +349,10 @@ int upload_tables() {
   d.b3_factor = R.b3_factor.p;
   d.b3_cw = R.b3_cw.p;
   d.b3_mult = R.b3_mult.p;
+  d.b3_C64 = R.b3_C64.p;
+  d.b3_cf64 = R.b3_cf64.p;
+  d.b3_cfw64 = R.b3_cfw64.p;
+  d.b3_bound = M.db3.bound;
   d.tune_abasis = R.tune_abasis;
   d.tune_rest = R.tune_rest;
   d.tune_b3 = R.tune_b3;
@@ -924,6 +932,7 @@ void ace_release_device(void) {
   R.b3_code.release();
   R.b3_code2.release();
   R.b3_cfw.release();
+  for (auto* b : {&R.b3_C64, &R.b3_cf64, &R.b3_cfw64}) b->release();
   for (auto* b : {&R.d_rank1_n, &R.d_begin, &R.r_factor, &R.r_run, &R.r_g0, &R.r_warp_begin, &R.r_warp_slots})
     b->release();
   R.r_rec.release();

@@ -83,6 +83,12 @@ struct DeviceModel {
   const int32_t* b3_factor;   // [nc] factor index of each compact element
   const int32_t* b3_cw;       // [nW] compact element of each weight, or -1
   const float* b3_mult;       // [nc] half-plane multiplicity of each element's weight
+  // FP64 copies for the plain-precision 3-body kernel, and the bound of its
+  // gradients (model.hpp DenseB3::bound)
+  const double* b3_C64;       // [combo][NM][I][I]
+  const double* b3_cf64;      // [task]
+  const double* b3_cfw64;     // [task]
+  double b3_bound;
   // per-slot table of the 2- and 4-body terms (see model.hpp RestTable)
   int r_nfac, r_nslot;
   const int32_t* r_factor;

@@ -552,15 +552,21 @@ struct CSum {
   __device__ __forceinline__ double value() const { return static_cast<double>(hi) + static_cast<double>(lo); }
 };
 
-template <class R, int ND>
+template <class R, int ND, bool REST = false>
 __global__ void __launch_bounds__(kDensityThreads)
     k_density(DeviceModel m, int natom, const C<R>* __restrict__ F, const double* __restrict__ rho1,
               const double* __restrict__ core, C<R>* __restrict__ W, double* __restrict__ energy,
-              double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err) {
+              double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err,
+              double* __restrict__ rho_rest = nullptr) {
+  static_assert(!REST || ND == 1, "the rest pass serves the one-density specialised layout");
   extern __shared__ __align__(16) unsigned char smem[];
+  // REST: the table without the 3-body terms (g2); the pass writes the
+  // density of its terms to rho_rest and the weights without dE/drho, and
+  // the embedding follows in k_finish_fe once the 3-body part is known
+  const GatherView& G = REST ? m.g2 : m.g;
   C<R>* Fs = reinterpret_cast<C<R>*>(smem);
   C<R>* part = Fs + ((m.nF + 1) & ~1);
-  C<R>* tot = part + ((m.g.nseg * ND + 1) & ~1);
+  C<R>* tot = part + ((G.nseg * ND + 1) & ~1);
   __shared__ double s_red[kDensityThreads / 32][ND];
   __shared__ double s_dE[ND];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -570,12 +576,12 @@ __global__ void __launch_bounds__(kDensityThreads)
     const C<R>* Fa = F + static_cast<size_t>(atom) * m.nF;
     for (int s = threadIdx.x; s < m.nF; s += blockDim.x) Fs[s] = Fa[s];
     __syncthreads();
-    for (int g = warp; g < m.g.ngroup; g += nwarp) {
-      const int a = m.g.grp_arity[g], len = m.g.grp_len[g], base = m.g.grp_first[g] + lane;
-      const int seg = m.g.grp_seg[g * 32 + lane];
-      const R* kp = kap_ptr<R>(m.g, a) + base;
-      const uint32_t* op = m.g.o12[a] + base;
-      const int ks = m.g.kstride[a];
+    for (int g = warp; g < G.ngroup; g += nwarp) {
+      const int a = G.grp_arity[g], len = G.grp_len[g], base = G.grp_first[g] + lane;
+      const int seg = G.grp_seg[g * 32 + lane];
+      const R* kp = kap_ptr<R>(G, a) + base;
+      const uint32_t* op = G.o12[a] + base;
+      const int ks = G.kstride[a];
       C<R> acc[ND];
       for (int d = 0; d < ND; ++d) acc[d] = {R(0), R(0)};
       if (a == 2) {
@@ -600,7 +606,7 @@ __global__ void __launch_bounds__(kDensityThreads)
           }
         }
       } else {
-        const uint16_t* o3p = m.g.o3 + base;
+        const uint16_t* o3p = G.o3 + base;
         for (int e = 0; e < len; ++e) {
           const uint32_t o = __ldg(op + e * 32);
           const C<R> p = cmul(cmul(Fs[o & 0xffffu], Fs[o >> 16]), Fs[__ldg(o3p + e * 32)]);
@@ -617,8 +623,8 @@ __global__ void __launch_bounds__(kDensityThreads)
     __syncthreads();
     double rloc[ND];
     for (int d = 0; d < ND; ++d) rloc[d] = 0.0;
-    for (int s = threadIdx.x; s < m.g.nslot; s += blockDim.x) {
-      const int q0 = m.g.slot_seg[s], q1 = m.g.slot_seg[s + 1];
+    for (int s = threadIdx.x; s < G.nslot; s += blockDim.x) {
+      const int q0 = G.slot_seg[s], q1 = G.slot_seg[s + 1];
       for (int d = 0; d < ND; ++d) {
         CSum<R> tx, ty;
         for (int q = q0; q < q1; ++q) {
@@ -626,8 +632,8 @@ __global__ void __launch_bounds__(kDensityThreads)
           ty.add(part[q * ND + d].y);
         }
         tot[s * ND + d] = {tx.hi + tx.lo, ty.hi + ty.lo};
-        if (s < m.g.nG0) {
-          const C<R> f = Fs[m.g.slot_factor[s]];
+        if (s < G.nG0) {
+          const C<R> f = Fs[G.slot_factor[s]];
           rloc[d] += static_cast<double>(f.x) * tx.value() - static_cast<double>(f.y) * ty.value();
         }
       }
@@ -639,6 +645,22 @@ __global__ void __launch_bounds__(kDensityThreads)
       if (lane == 0) s_red[warp][d] = v;
     }
     __syncthreads();
+    if constexpr (REST) {
+      if (threadIdx.x == 0) {
+        double rho = 0.0;
+        for (int w = 0; w < kDensityThreads / 32; ++w) rho += s_red[w][0];
+        rho_rest[atom] = rho;
+      }
+      C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
+      for (int s = threadIdx.x; s < G.nslot; s += blockDim.x) {
+        const int w = G.slot_weight[s];
+        if (w < 0) continue;
+        const R mu = R(G.slot_mult[s]);
+        Wa[w] = {mu * tot[s].x, mu * tot[s].y};
+      }
+      __syncthreads();
+      continue;
+    }
     if (threadIdx.x == 0) {
       double energyi = 0.0, dE[ND];
       for (int d = 0; d < ND; ++d) {
@@ -674,10 +696,10 @@ __global__ void __launch_bounds__(kDensityThreads)
     }
     __syncthreads();
     C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
-    for (int s = threadIdx.x; s < m.g.nslot; s += blockDim.x) {
-      const int w = m.g.slot_weight[s];
+    for (int s = threadIdx.x; s < G.nslot; s += blockDim.x) {
+      const int w = G.slot_weight[s];
       if (w < 0) continue;
-      const R mu = R(m.g.slot_mult[s]);
+      const R mu = R(G.slot_mult[s]);
       C<R> v = {R(0), R(0)};
       for (int d = 0; d < ND; ++d) {
         const R sc = mu * R(s_dE[d]);
@@ -932,9 +954,10 @@ size_t abasis_smem(const DeviceModel& m) {
 }
 
 template <class R>
-size_t density_smem(const DeviceModel& m) {
-  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((m.g.nseg * m.nd + 1) & ~1) +
-                         static_cast<size_t>(m.g.nslot) * m.nd) + 64;
+size_t density_smem(const DeviceModel& m, bool rest = false) {
+  const GatherView& g = rest ? m.g2 : m.g;
+  return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((g.nseg * m.nd + 1) & ~1) +
+                         static_cast<size_t>(g.nslot) * m.nd) + 64;
 }
 
 template <class R>
@@ -1023,6 +1046,24 @@ AuxLayout aux_layout(const DeviceModel& m, int natom) {
   L.tail0 = L.g3 + up(sizeof(float) * 2 * static_cast<size_t>(m.b3_nc) * static_cast<size_t>(natom));
   L.rec = up(kTailG + sizeof(float) * 64 * static_cast<size_t>(m.b3_nc));
   L.end = L.tail0 + L.rec * ntail;
+  return L;
+}
+
+// The FP64 scratch of the specialised layout (EvalBuffers::aux):
+// rho_rest[natom] and rho3[natom] doubles, the 3-body gradients as 64-bit
+// fixed-point words g3i[ceil(natom/32)][nc][32][2] (k_b3_fe64; zeroed before
+// each evaluation) and their per-atom scales g3s[ceil(natom/32) * 32].
+struct AuxLayout64 {
+  size_t rho3, g3i, g3s, end;
+};
+AuxLayout64 aux_layout64(const DeviceModel& m, int natom) {
+  const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
+  const size_t nblk = (static_cast<size_t>(natom) + 31) / 32;
+  AuxLayout64 L;
+  L.rho3 = up(sizeof(double) * static_cast<size_t>(natom));
+  L.g3i = L.rho3 + up(sizeof(double) * static_cast<size_t>(natom));
+  L.g3s = L.g3i + up(sizeof(unsigned long long) * 64 * static_cast<size_t>(m.b3_nc) * nblk);
+  L.end = L.g3s + up(sizeof(double) * 32 * nblk);
   return L;
 }
 
@@ -1166,6 +1207,47 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       return 2;
     }
   }
+  if constexpr (sizeof(R) == 8) {
+    if (fe) {
+      // FP64, specialised layout: the 2-/4-body terms through the gather
+      // table without the 3-body terms (k_density, rest pass) on the side
+      // stream, beside the dense 3-body kernel k_b3_fe64 on `st`; then
+      // k_finish_fe (density, embedding, inner cutoff)
+      const AuxLayout64 al = aux_layout64(m, natom);
+      unsigned char* aux = static_cast<unsigned char*>(b.aux);
+      double* rho_rest = reinterpret_cast<double*>(aux);
+      double* rho3 = reinterpret_cast<double*>(aux + al.rho3);
+      auto* g3i = reinterpret_cast<unsigned long long*>(aux + al.g3i);
+      double* g3s = reinterpret_cast<double*>(aux + al.g3s);
+      const bool fork = b.side != nullptr;
+      cudaStream_t sr = fork ? b.side : st;
+      if (fork) {
+        cudaEventRecord(b.ev_fork, st);
+        cudaStreamWaitEvent(sr, b.ev_fork, 0);
+      }
+      const size_t s2 = density_smem<double>(m, true);
+      set_smem(k_density<double, 1, true>, s2);
+      k_density<double, 1, true><<<grid, kDensityThreads, s2, sr>>>(
+          m, natom, reinterpret_cast<const C<double>*>(b.F), b.rho1, b.core, reinterpret_cast<C<double>*>(b.W),
+          b.energy, b.edf, b.dedrho, b.err, rho_rest);
+      if (ev_between) cudaEventRecord(ev_between, st);
+      cudaMemsetAsync(g3i, 0, al.g3s - al.g3i, st);
+      const size_t sb = b3_fe64_smem<FeDims>(m, kB3Warps64);
+      set_smem(k_b3_fe64<FeDims, kB3Warps64>, sb);
+      const int nblk = (natom + 31) / 32;
+      const int gb = std::min(nblk, resident_grid(k_b3_fe64<FeDims, kB3Warps64>, kB3Warps64 * 32, sb));
+      k_b3_fe64<FeDims, kB3Warps64><<<gb, kB3Warps64 * 32, sb, st>>>(
+          m, natom, reinterpret_cast<const C<double>*>(b.F), g3i, g3s, rho3, b.err);
+      if (fork) {
+        cudaEventRecord(b.ev_join, sr);
+        cudaStreamWaitEvent(st, b.ev_join, 0);
+      }
+      const int gf = (natom + 255) / 256;
+      k_finish_fe<<<gf, 256, 0, st>>>(m, natom, b.rho1, rho_rest, rho3, b.core, b.energy, b.edf, b.dedrho, b.err);
+      if (kernels) *kernels += 3;
+      return 2;
+    }
+  }
   const size_t s2 = density_smem<R>(m);
   if (m.nd == 1) {
     set_smem(k_density<R, 1>, s2);
@@ -1203,6 +1285,14 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
         sizeof(R) == 4 ? reinterpret_cast<const C<float>*>(static_cast<unsigned char*>(b.aux) +
                                                            aux_layout(m, natom).g3)
                        : nullptr;
+    // FP64: k_b3_fe64's fixed-point gradients and their block scales
+    const unsigned long long* g3i = nullptr;
+    const double* g3s = nullptr;
+    if (sizeof(R) == 8) {
+      const AuxLayout64 al = aux_layout64(m, natom);
+      g3i = reinterpret_cast<const unsigned long long*>(static_cast<unsigned char*>(b.aux) + al.g3i);
+      g3s = reinterpret_cast<const double*>(static_cast<unsigned char*>(b.aux) + al.g3s);
+    }
     // outputs in host memory (acelib_ writing the caller's arrays directly):
     // the variants that store each tile's outputs as whole lines
 #define MAGACE_FORCES_SO(MB, PK, SO)                                                                                \
@@ -1212,7 +1302,7 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
     k_forces_fe<R, FeDims, MB, PK, SO><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi,       \
                                                              b.mhi, reinterpret_cast<const C<R>*>(b.W), b.edf,      \
                                                              b.dedrho, b.fij, b.tij, b.ti0,                         \
-                                                             static_cast<const R*>(b.stage), b.err, g3);            \
+                                                             static_cast<const R*>(b.stage), b.err, g3, g3i, g3s);  \
   }
 #define MAGACE_FORCES(MB, PK)                 \
   if (b.host_outputs) {                       \
@@ -1247,17 +1337,18 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
 }
 
 size_t eval_aux_bytes(const DeviceModel& m, int precision, int natom) {
-  // k_density_fe's per-atom 2- and 4-body density, read by k_b3_fe, and
-  // k_b3_fe's split-tail accumulators (aux_layout)
-  if (precision == 0 || !use_specialised(m) || natom <= 0) return 0;
-  return aux_layout(m, natom).end;
+  // the specialised kernels' per-atom densities and 3-body gradients
+  // (aux_layout, aux_layout64)
+  if (!use_specialised(m) || natom <= 0) return 0;
+  return precision == 0 ? aux_layout64(m, natom).end : aux_layout(m, natom).end;
 }
 
 size_t eval_aux_bytes_bound(const DeviceModel& m, int precision, int natom) {
   // as eval_aux_bytes, with room for the most tail records any split can
   // use (a split tail has at most half an SM count of blocks, and never more
   // blocks than there are), so that the bound never falls as natom grows
-  if (precision == 0 || !use_specialised(m) || natom <= 0) return 0;
+  if (!use_specialised(m) || natom <= 0) return 0;
+  if (precision == 0) return aux_layout64(m, natom).end;
   const AuxLayout L = aux_layout(m, natom);
   const size_t nblk = (static_cast<size_t>(natom) + 31) / 32;
   const size_t half = static_cast<size_t>(sm_count()) / 2;
@@ -1268,7 +1359,10 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
   if (use_specialised(m)) {
     if (precision == 0) {
       if (which == 0) return abasis_fe_smem<double, FeDims>();
-      if (which == 1) return density_smem<double>(m);
+      if (which == 1) {
+        const size_t a = density_smem<double>(m), b = b3_fe64_smem<FeDims>(m, kB3Warps64);
+        return a > b ? a : b;
+      }
       return forces_fe_smem<double, FeDims>(true);
     }
     if (which == 0) return abasis_fe_smem<float, FeDims>();

@@ -1191,6 +1191,216 @@ __global__ void __launch_bounds__(NW * 32, 1)
   }
 }
 
+// ===========================================================================
+// k_b3_fe64: the 3-body density and its gradients in FP64 (the plain
+// precision), the same dense tasks as k_b3_fe with 32 atoms in the lanes of
+// each warp; the coefficients C are read from global memory (one uniform
+// load serves the warp) and the factors Xs[nc][33] are staged in shared
+// memory. The warps take tasks in a fixed order (warp w: tasks w, w + NW,
+// ...), so the density of every atom sums in a fixed order.
+//
+// Gradients are exact integer sums: every contribution v is rounded once to
+// a 64-bit integer q = rint(v * 2^e) and added with an integer atomic into
+// G3i[block][c][lane] (re, im), so the result does not depend on the order
+// in which the warps' atomics arrive: the FP64 path stays bitwise
+// reproducible. The exponent e of each atom follows from a bound of every
+// partial sum of its gradients: with f = max over the atom's factors of
+// |x| + |y|, every gradient is at most b3_bound * f^2 (model.hpp
+// DenseB3::bound), so e = 61 - ceil(log2(b3_bound f^2)) keeps the sums below
+// 2^61; G3s[position] receives 2^-e. e depends on the atom alone, so an atom
+// gets the same result in any batch and any order. The rounding error of a
+// gradient is at most its number of contributions times 2^-e / 2, about
+// 1e-17 of the bound.
+constexpr int kB3Stride64 = 33;  // row stride of Xs in complex elements
+
+__device__ __forceinline__ C<double> b3_load64(const C<double>* Xs, unsigned code, int lane) {
+  const C<double> v = Xs[(code & 0x1fffu) * kB3Stride64 + lane];
+  const unsigned long long sx = static_cast<unsigned long long>(code & 0x8000u) << 48;
+  const unsigned long long sy = static_cast<unsigned long long>(code & 0x4000u) << 49;
+  return {__longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(__double_as_longlong(v.x)) ^ sx)),
+          __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(__double_as_longlong(v.y)) ^ sy))};
+}
+
+// one fixed-point contribution (v already scaled by 2^e)
+__device__ __forceinline__ void red_fix(unsigned long long* p, double v) {
+  atomicAdd(p, static_cast<unsigned long long>(__double2ll_rn(v)));
+}
+
+// as b3_add, into the fixed-point gradients of the lane's atom: G points at
+// element 0 of the lane ([c][32 lanes][2] words), cfs = cf * 2^e
+__device__ __forceinline__ void b3_add64(unsigned long long* G, const uint16_t* __restrict__ code,
+                                         const uint16_t* __restrict__ code2, int pos, C<double> v, double cfs) {
+  const unsigned c = __ldg(code + pos);
+  if (!(c & 0xe000u)) {
+    unsigned long long* g = G + 64 * static_cast<size_t>(c);
+    red_fix(g, cfs * v.x);
+    red_fix(g + 1, cfs * v.y);
+  }
+  const unsigned c2 = __ldg(code2 + pos);
+  if (c2 != 0xffffu) {
+    const double sc = (c2 & 0x8000u) ? -cfs : cfs;
+    unsigned long long* g = G + 64 * static_cast<size_t>(c2 & 0x3fffu);
+    red_fix(g, sc * v.x);
+    red_fix(g + 1, -sc * v.y);
+  }
+}
+
+// One task on the lane's atom in FP64 (as b3_task): returns
+// sum C[p][i][j] Re(a_p X_i Y_j) and adds the gradients. Cg points at the
+// combination's coefficients [NM][I][I] in global memory.
+template <int PAT, class D>
+__device__ __forceinline__ double b3_task64(const double* __restrict__ Cg, const C<double>* Xs,
+                                            unsigned long long* G, const uint16_t* __restrict__ code,
+                                            const uint16_t* __restrict__ code2, double cfs, int lane) {
+  constexpr int I = D::I, NM = D::NM;
+  static_assert(I % 2 == 0, "rows of C are read as double2");
+  constexpr int JUSED = jmax_of<PAT, I, NM>(I - 1);
+  C<double> Y[I], gY[I], a[NM], ga[NM];
+#pragma unroll
+  for (int j = 0; j < I; ++j) {
+    Y[j] = j < JUSED ? b3_load64(Xs, __ldg(code + NM + I + j), lane) : C<double>{0.0, 0.0};
+    gY[j] = {0.0, 0.0};
+  }
+#pragma unroll
+  for (int p = 0; p < NM; ++p) {
+    a[p] = b3_load64(Xs, __ldg(code + p), lane);
+    ga[p] = {0.0, 0.0};
+  }
+  double rt = 0.0;
+#pragma unroll
+  for (int i = 0; i < I; ++i) {
+    const int jm = jmax_of<PAT, I, NM>(i);
+    if (jm == 0) continue;
+    const C<double> x = b3_load64(Xs, __ldg(code + NM + i), lane);
+    C<double> az = {0.0, 0.0};
+#pragma unroll
+    for (int p = 0; p < NM; ++p) {
+      C<double> z = {0.0, 0.0};
+      const C<double> ax = cmul(a[p], x);
+      const double2* crow = reinterpret_cast<const double2*>(Cg + (p * I + i) * I);
+#pragma unroll
+      for (int j2 = 0; j2 < (jm + 1) / 2; ++j2) {
+        const double2 c2 = __ldg(crow + j2);
+        const double cv[2] = {c2.x, c2.y};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int j = 2 * j2 + u;
+          if (j < jm) {
+            z.x = fma(cv[u], Y[j].x, z.x);
+            z.y = fma(cv[u], Y[j].y, z.y);
+            gY[j].x = fma(cv[u], ax.x, gY[j].x);
+            gY[j].y = fma(cv[u], ax.y, gY[j].y);
+          }
+        }
+      }
+      const C<double> t = cmul(a[p], z);
+      az.x += t.x;
+      az.y += t.y;
+      const C<double> u = cmul(x, z);
+      ga[p].x += u.x;
+      ga[p].y += u.y;
+    }
+    rt += re_mul(x, az);
+    b3_add64(G, code, code2, NM + i, az, cfs);
+  }
+#pragma unroll
+  for (int j = 0; j < JUSED; ++j) b3_add64(G, code, code2, NM + I + j, gY[j], cfs);
+#pragma unroll
+  for (int p = 0; p < NM; ++p) b3_add64(G, code, code2, p, ga[p], cfs);
+  return rt;
+}
+
+// Shared memory: Xs[nc][33] (complex FP64), the per-warp density partials
+// [NW][32] and the factor map [nc]. G3i is [ceil(natom/32)][nc][32][2] words,
+// zeroed before the launch, and G3s [ceil(natom/32) * 32]; blocks are 32
+// consecutive queue positions.
+template <class D, int NW>
+__global__ void __launch_bounds__(NW * 32, 1)
+    k_b3_fe64(DeviceModel m, int natom, const C<double>* __restrict__ F, unsigned long long* __restrict__ G3i,
+              double* __restrict__ G3s, double* __restrict__ rho3, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
+  const int nc = m.b3_nc;
+  C<double>* Xs = reinterpret_cast<C<double>*>(smem);
+  double* rpart = reinterpret_cast<double*>(Xs + nc * kB3Stride64);  // [NW][32]
+  int* s_fac = reinterpret_cast<int*>(rpart + NW * 32);              // [nc]
+  __shared__ int s_atom[32];
+  // per atom, the largest |x| + |y| of its factors (non-negative doubles
+  // order as their bit patterns)
+  __shared__ unsigned long long s_fm[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (natom + 31) / 32;
+  for (int c = threadIdx.x; c < nc; c += blockDim.x) s_fac[c] = __ldg(m.b3_factor + c);
+  __syncthreads();
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int a0 = blk * 32;
+    const int na = min(32, natom - a0);
+    if (threadIdx.x < 32) {
+      if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
+      s_fm[threadIdx.x] = 0ull;
+    }
+    __syncthreads();
+    // stage: thread c takes element c of every atom
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+      const int fc = s_fac[c];
+      for (int ab = 0; ab < 32; ab += kBatch) {
+        C<double> v[kBatch];
+#pragma unroll
+        for (int b = 0; b < kBatch; ++b)
+          v[b] = ab + b < na ? F[static_cast<size_t>(s_atom[ab + b]) * m.nF + fc] : C<double>{0.0, 0.0};
+#pragma unroll
+        for (int b = 0; b < kBatch; ++b) {
+          Xs[c * kB3Stride64 + ab + b] = v[b];
+          const double f = fabs(v[b].x) + fabs(v[b].y);
+          // NaN compares as the largest pattern and is caught below
+          atomicMax(&s_fm[ab + b], static_cast<unsigned long long>(__double_as_longlong(f)));
+        }
+      }
+    }
+    __syncthreads();
+    // this lane's atom: its fixed-point exponent
+    double scale;
+    {
+      const double f = __longlong_as_double(static_cast<long long>(s_fm[lane]));
+      const double bound = m.b3_bound * f * f;
+      int ex = 0;
+      if (!(bound < 1e300)) {  // non-finite factors
+        if (lane < na) raise_error(err, kDevNaN);
+        ex = 1100;
+      } else if (bound > 0.0) {
+        frexp(bound, &ex);  // bound < 2^ex
+      }
+      const int e = max(-1000, min(1000, 61 - ex));
+      scale = ldexp(1.0, e);
+      if (warp == 0) G3s[a0 + lane] = ldexp(1.0, -e);
+    }
+    unsigned long long* G = G3i + static_cast<size_t>(blk) * nc * 64 + 2 * lane;
+    double rloc = 0.0;
+#pragma unroll 1
+    for (int tk = warp; tk < m.b3_ntask; tk += NW) {
+      const int k = __ldg(m.b3_combo + tk);
+      const int pat = __ldg(m.b3_pattern + k);
+      const double cfs = __ldg(m.b3_cf64 + tk) * scale;
+      const uint16_t* code = m.b3_code + tk * NPOS;
+      const uint16_t* code2 = m.b3_code2 + tk * NPOS;
+      const double* Ck = m.b3_C64 + static_cast<size_t>(k) * NM * I * I;
+      double r;
+      if (pat == 0) r = b3_task64<0, D>(Ck, Xs, G, code, code2, cfs, lane);
+      else if (pat == 1) r = b3_task64<1, D>(Ck, Xs, G, code, code2, cfs, lane);
+      else r = b3_task64<2, D>(Ck, Xs, G, code, code2, cfs, lane);
+      rloc = fma(__ldg(m.b3_cfw64 + tk), r, rloc);
+    }
+    rpart[warp * 32 + lane] = rloc;
+    __syncthreads();
+    if (warp == 0 && lane < na) {
+      double r3 = 0.0;
+      for (int w = 0; w < NW; ++w) r3 += rpart[w * 32 + lane];
+      rho3[s_atom[lane]] = r3;
+    }
+    __syncthreads();
+  }
+}
+
 // k_finish_fe: per atom (one per thread) rho = rho1 + rho_rest + rho3, the
 // FP64 embedding and the inner cutoff on the core energy; the energy, edf and
 // dE/drho outputs (the two density kernels before it may run side by side).
@@ -1251,7 +1461,8 @@ __global__ void __launch_bounds__(64, MINB)
                 const double* __restrict__ magi, const double* __restrict__ mhi, const C<R>* __restrict__ W,
                 const double* __restrict__ edf_in, const double* __restrict__ dedrho, double* __restrict__ fij,
                 double* __restrict__ tij, double* __restrict__ ti0, const R* __restrict__ stage, int* err,
-                const C<float>* __restrict__ g3) {
+                const C<float>* __restrict__ g3, const unsigned long long* __restrict__ g3i = nullptr,
+                const double* __restrict__ g3s = nullptr) {
   constexpr int T = 64;
   extern __shared__ __align__(16) unsigned char smem[];
   C<R>* W2T = reinterpret_cast<C<R>*>(smem);   // [NQ][NB]
@@ -1299,7 +1510,12 @@ __global__ void __launch_bounds__(64, MINB)
     // unscaled weights and g3 [atom][nc] the 3-body part per compact element;
     // the weight is dE/drho (W + g3)
     const C<float>* Ga = g3 ? g3 + static_cast<size_t>(atom) * m.b3_nc : nullptr;
-    const R sc = g3 ? to_r<R>(dedrho[static_cast<size_t>(atom) * 2]) : R(1);
+    // with g3i (FP64, Fe layout): the 3-body part as fixed-point words of
+    // the atom's queue position, times the block's scale and the element's
+    // multiplicity
+    const unsigned long long* Gi = g3i ? g3i + static_cast<size_t>(it >> 5) * m.b3_nc * 64 + 2 * (it & 31) : nullptr;
+    const double gs = g3i ? g3s[it] : 0.0;
+    const R sc = (g3 || g3i) ? to_r<R>(dedrho[static_cast<size_t>(atom) * 2]) : R(1);
     // weight w with its 3-body element c (-1: none); the A weights are the
     // first compact elements in the same order (c = w), the 2-body weights
     // have none, the on-site ones are looked up
@@ -1311,6 +1527,17 @@ __global__ void __launch_bounds__(64, MINB)
             const C<float> gv = ld_l2(Ga + c, pol_first);
             v.x += gv.x;
             v.y += gv.y;
+          }
+          v.x *= sc;
+          v.y *= sc;
+        }
+      } else {
+        if (Gi) {
+          if (c >= 0) {
+            const double mu = gs * static_cast<double>(__ldg(m.b3_mult + c));
+            const unsigned long long* q = Gi + 64 * static_cast<size_t>(c);
+            v.x += mu * static_cast<double>(static_cast<long long>(q[0]));
+            v.y += mu * static_cast<double>(static_cast<long long>(q[1]));
           }
           v.x *= sc;
           v.y *= sc;
@@ -1338,7 +1565,7 @@ __global__ void __launch_bounds__(64, MINB)
         WAT[k3 * D::NRY + i] = w;
       }
     }
-    for (int s = t; s < D::NQ; s += T) W0s[s] = weight(m.offW0 + s, Ga ? __ldg(m.b3_cw + m.offW0 + s) : -1);
+    for (int s = t; s < D::NQ; s += T) W0s[s] = weight(m.offW0 + s, (Ga || Gi) ? __ldg(m.b3_cw + m.offW0 + s) : -1);
     __syncthreads();
     const R edf = to_r<R>(edf_in[atom]);
     const int b0 = off[atom], b1 = off[atom + 1];
@@ -1683,6 +1910,12 @@ size_t b3_fe_smem(const DeviceModel& m, int nw) {
   return sizeof(float) * ((ncoef + 3) & ~static_cast<size_t>(3)) +
          sizeof(C<float>) * 2 * static_cast<size_t>(m.b3_nc) * kB3Stride + sizeof(double) * nw * 32 +
          sizeof(float) * m.b3_nc + sizeof(int) * m.b3_nc;
+}
+constexpr int kB3Warps64 = 8;  // warps per CTA of k_b3_fe64
+template <class D>
+size_t b3_fe64_smem(const DeviceModel& m, int nw) {
+  return sizeof(C<double>) * static_cast<size_t>(m.b3_nc) * kB3Stride64 + sizeof(double) * nw * 32 +
+         sizeof(int) * m.b3_nc;
 }
 template <class R, class D>
 size_t forces_fe_smem(bool sout) {

@@ -960,6 +960,32 @@ int build_tables(Model& M, std::string& msg) {
         uint16_t& c2 = D.code2[q];
         if (c2 != 0xffff && D.mult[c2 & 0x3fff] == 0.0) c2 = 0xffff;
       }
+    // coefficient mass of every element's gradient (DenseB3::bound): the
+    // gradient of position a_p is sum_{i,j} C[p][i][j] X_i Y_j, of X_i
+    // sum_{p,j} C a_p Y_j and of Y_j sum_{p,i} C a_p X_i, each times cf
+    const int I = D.I, NM = D.NM, npos = NM + 2 * I;
+    std::vector<double> mass(D.nc, 0.0), row(npos);
+    for (int t = 0; t < D.ntask; ++t) {
+      std::fill(row.begin(), row.end(), 0.0);
+      const double* Ck = D.C.data() + static_cast<size_t>(D.task_combo[t]) * NM * I * I;
+      for (int p = 0; p < NM; ++p)
+        for (int i = 0; i < I; ++i)
+          for (int j = 0; j < I; ++j) {
+            const double c = std::fabs(Ck[(p * I + i) * I + j]);
+            row[p] += c;
+            row[NM + i] += c;
+            row[NM + I + j] += c;
+          }
+      const double cf = std::fabs(D.task_cf[t]);
+      for (int q = 0; q < npos; ++q) {
+        const uint16_t c = D.code[static_cast<size_t>(t) * npos + q];
+        const uint16_t c2 = D.code2[static_cast<size_t>(t) * npos + q];
+        if (!(c & 0xe000)) mass[c & 0x1fff] += cf * row[q];
+        if (c2 != 0xffff) mass[c2 & 0x3fff] += cf * row[q];
+      }
+    }
+    D.bound = 0.0;
+    for (double v : mass) D.bound = std::max(D.bound, v);
   }
   return MAGACE_OK;
 }

@@ -103,6 +103,11 @@ struct DenseB3 {
   std::vector<int32_t> factor_of;           // [nc] factor index of each compact element
   std::vector<int32_t> compact_of_weight;   // [nW] compact element of each weight, or -1
   std::vector<double> mult;                 // [nc] half-plane multiplicity of each element's weight
+  // max over elements of the coefficient mass of the element's gradient:
+  // sum over the (task, position) pairs that add to it of |cf| times the
+  // sum of |C| over that position's products. With every factor bounded by
+  // |x| + |y| <= f, every partial sum of a gradient is bounded by bound * f^2.
+  double bound = 0.0;
 };
 
 // Per-cluster m-terms of the descriptors B_k, the basis functions that the

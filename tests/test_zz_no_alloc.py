@@ -69,7 +69,7 @@ def test_noalloc_matches_compute_device(seeded_potential, precision):
 
 # limits of the 64 MiB scratch for the seeded Fe-layout potential on a
 # 152-SM GB300 (FP64, split precision)
-DOCUMENTED_LIMIT = {0: 2097, 1: 3305}
+DOCUMENTED_LIMIT = {0: 1816, 1: 3305}
 
 
 @pytest.mark.parametrize("precision", [0, 1])
