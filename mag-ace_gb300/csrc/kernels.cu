@@ -57,6 +57,22 @@ __device__ __forceinline__ R re_mul(C<R> a, C<R> b) {
   return a.x * b.x - a.y * b.y;
 }
 
+// acc += a b (complex) and acc += Re(a b) as chains of fused multiply-adds:
+// two FMA instructions per real part instead of a multiply, an FMA and an
+// add (the form a * b - c * d + acc contracts to), which matters most on the
+// FP64 pipe
+template <class R>
+__device__ __forceinline__ void cmac(C<R>& acc, C<R> a, C<R> b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+template <class R>
+__device__ __forceinline__ R re_mac(R acc, C<R> a, C<R> b) {
+  return fma(-a.y, b.y, fma(a.x, b.x, acc));
+}
+
 __device__ __forceinline__ int ph(int l, int m) { return l * (l + 1) / 2 + m; }
 __device__ __forceinline__ double parity(int m) { return (m & 1) ? -1.0 : 1.0; }
 

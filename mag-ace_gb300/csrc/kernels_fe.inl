@@ -459,8 +459,7 @@ __global__ void __launch_bounds__(64)
           for (int c = 0; c < 9; ++c) {
             const int k3 = 9 * cb + c;
             const C<R> q = sQ[b * D::NQ + (k3 / D::H3) * D::H2 + k3 % D::H3];
-            acc[c].x += ry.x * q.x - ry.y * q.y;
-            acc[c].y += ry.x * q.y + ry.y * q.x;
+            cmac(acc[c], ry, q);
           }
         }
       } else {
@@ -470,8 +469,8 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
           for (int c = 0; c < 15; ++c) {
             const C<R> q = sQ[b * D::NQ + 15 * cb + c];
-            acc[c].x += gv * q.x;
-            acc[c].y += gv * q.y;
+            acc[c].x = fma(gv, q.x, acc[c].x);
+            acc[c].y = fma(gv, q.y, acc[c].y);
           }
         }
       }
@@ -1293,14 +1292,10 @@ __device__ __forceinline__ double b3_task64(const double* __restrict__ Cg, const
           }
         }
       }
-      const C<double> t = cmul(a[p], z);
-      az.x += t.x;
-      az.y += t.y;
-      const C<double> u = cmul(x, z);
-      ga[p].x += u.x;
-      ga[p].y += u.y;
+      cmac(az, a[p], z);
+      cmac(ga[p], x, z);
     }
-    rt += re_mul(x, az);
+    rt = re_mac(rt, x, az);
     b3_add64(G, code, code2, NM + i, az, cfs);
   }
 #pragma unroll
@@ -1728,28 +1723,24 @@ __global__ void __launch_bounds__(64, MINB)
                 const C<R> q = cscale(Ym[h], cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
                 const C<R>* w2 = W2T + k * D::NB;
   #pragma unroll
-                for (int n = 0; n < D::NB; ++n) sp[n] += re_mul(w2[n], q);
+                for (int n = 0; n < D::NB; ++n) sp[n] = re_mac(sp[n], w2[n], q);
                 if (nr < D::NM && h < D::H3) {
                   const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
   #pragma unroll
-                  for (int i = 0; i < D::NRY; ++i) {
-                    const C<R> w = wa[i];
-                    U[i].x += w.x * q.x - w.y * q.y;
-                    U[i].y += w.x * q.y + w.y * q.x;
-                  }
+                  for (int i = 0; i < D::NRY; ++i) cmac(U[i], wa[i], q);
                 }
               }
           }
   #pragma unroll
-          for (int n = 0; n < D::NB; ++n) fr += cgd[n * T + t] * sp[n];
+          for (int n = 0; n < D::NB; ++n) fr = fma(cgd[n * T + t], sp[n], fr);
           const R invr = rcp(r);
   #pragma unroll
           for (int i = 0; i < D::NRY; ++i) {
             const int n1 = i / D::LSA, lma = i % D::LSA, l1 = l_of_lm(lma);
-            fr += cRd[(n1 * (D::LA + 1) + l1) * T + t] * re_mul(U[i], cYa[lma * T + t]);
-            const R sc = invr * cR[(n1 * (D::LA + 1) + l1) * T + t];
+            fr = fma(cRd[(n1 * (D::LA + 1) + l1) * T + t], re_mul(U[i], cYa[lma * T + t]), fr);
+            const C<R> su = cscale(U[i], invr * cR[(n1 * (D::LA + 1) + l1) * T + t]);
   #pragma unroll
-            for (int c = 0; c < 3; ++c) ft[c] += sc * re_mul(U[i], cdYa[(lma * 3 + c) * T + t]);
+            for (int c = 0; c < 3; ++c) ft[c] = re_mac(ft[c], su, cdYa[(lma * 3 + c) * T + t]);
           }
         }
         *(SOUT ? sOut + 3 * t + 0 : fij + 3 * static_cast<size_t>(j) + 0) = to_d(fr * ex + ft[0]);
@@ -1768,10 +1759,10 @@ __global__ void __launch_bounds__(64, MINB)
           // V[k] = sum_n g_n W2[n][k] + sum_i W_A[i][k] RY_i, contracted per k
           const auto contract = [&](int nr, int h, C<R> V) {
             const int q = nr * (D::L2 + 1) + l_of_h(h);
-            tr += cMd[q * T + t] * re_mul(V, Ym[h]);
-            const R sc = invm * cM[q * T + t];
+            tr = fma(cMd[q * T + t], re_mul(V, Ym[h]), tr);
+            const C<R> sv = cscale(V, invm * cM[q * T + t]);
   #pragma unroll
-            for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(V, dYm[h][c]);
+            for (int c = 0; c < 3; ++c) tt[c] = re_mac(tt[c], sv, dYm[h][c]);
           };
           if constexpr (PACKED) {
             float2 g2[D::NB / 2], RYx2[D::NRY / 2], RYy2[D::NRY / 2], RYyn2[D::NRY / 2];
@@ -1826,17 +1817,13 @@ __global__ void __launch_bounds__(64, MINB)
                 C<R> V = {R(0), R(0)};
   #pragma unroll
                 for (int n = 0; n < D::NB; ++n) {
-                  V.x += g[n] * w2[n].x;
-                  V.y += g[n] * w2[n].y;
+                  V.x = fma(g[n], w2[n].x, V.x);
+                  V.y = fma(g[n], w2[n].y, V.y);
                 }
                 if (nr < D::NM && h < D::H3) {
                   const C<R>* wa = WAT + (nr * D::H3 + h) * D::NRY;
   #pragma unroll
-                  for (int i = 0; i < D::NRY; ++i) {
-                    const C<R> w = wa[i];
-                    V.x += w.x * RY[i].x - w.y * RY[i].y;
-                    V.y += w.x * RY[i].y + w.y * RY[i].x;
-                  }
+                  for (int i = 0; i < D::NRY; ++i) cmac(V, wa[i], RY[i]);
                 }
                 contract(nr, h, V);
               }
