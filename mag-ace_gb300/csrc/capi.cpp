@@ -353,6 +353,7 @@ int upload_tables() {
   d.b3_cf64 = R.b3_cf64.p;
   d.b3_cfw64 = R.b3_cfw64.p;
   d.b3_bound = M.db3.bound;
+  d.b3_bound_rho = M.db3.bound_rho;
   d.tune_abasis = R.tune_abasis;
   d.tune_rest = R.tune_rest;
   d.tune_b3 = R.tune_b3;

@@ -88,7 +88,7 @@ struct DeviceModel {
   const double* b3_C64;       // [combo][NM][I][I]
   const double* b3_cf64;      // [task]
   const double* b3_cfw64;     // [task]
-  double b3_bound;
+  double b3_bound, b3_bound_rho;
   // per-slot table of the 2- and 4-body terms (see model.hpp RestTable)
   int r_nfac, r_nslot;
   const int32_t* r_factor;

@@ -1066,20 +1066,22 @@ AuxLayout aux_layout(const DeviceModel& m, int natom) {
 }
 
 // The FP64 scratch of the specialised layout (EvalBuffers::aux):
-// rho_rest[natom] and rho3[natom] doubles, the 3-body gradients as 64-bit
-// fixed-point words g3i[ceil(natom/32)][nc][32][2] (k_b3_fe64; zeroed before
-// each evaluation) and their per-atom scales g3s[ceil(natom/32) * 32].
+// rho_rest[natom] doubles, then k_b3_fe64's 64-bit fixed-point sums (zeroed
+// before each evaluation, one range): the 3-body density r3i[P] and the
+// gradients g3i[nblk][nc][32][2]; then their scales g3s[P] and r3s[P], where
+// nblk = ceil(natom/32) and P = 32 nblk queue positions.
 struct AuxLayout64 {
-  size_t rho3, g3i, g3s, end;
+  size_t r3i, g3i, g3s, r3s, end;
 };
 AuxLayout64 aux_layout64(const DeviceModel& m, int natom) {
   const auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
   const size_t nblk = (static_cast<size_t>(natom) + 31) / 32;
   AuxLayout64 L;
-  L.rho3 = up(sizeof(double) * static_cast<size_t>(natom));
-  L.g3i = L.rho3 + up(sizeof(double) * static_cast<size_t>(natom));
+  L.r3i = up(sizeof(double) * static_cast<size_t>(natom));
+  L.g3i = L.r3i + up(sizeof(unsigned long long) * 32 * nblk);
   L.g3s = L.g3i + up(sizeof(unsigned long long) * 64 * static_cast<size_t>(m.b3_nc) * nblk);
-  L.end = L.g3s + up(sizeof(double) * 32 * nblk);
+  L.r3s = L.g3s + up(sizeof(double) * 32 * nblk);
+  L.end = L.r3s + up(sizeof(double) * 32 * nblk);
   return L;
 }
 
@@ -1232,9 +1234,10 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
       const AuxLayout64 al = aux_layout64(m, natom);
       unsigned char* aux = static_cast<unsigned char*>(b.aux);
       double* rho_rest = reinterpret_cast<double*>(aux);
-      double* rho3 = reinterpret_cast<double*>(aux + al.rho3);
+      auto* r3i = reinterpret_cast<unsigned long long*>(aux + al.r3i);
       auto* g3i = reinterpret_cast<unsigned long long*>(aux + al.g3i);
       double* g3s = reinterpret_cast<double*>(aux + al.g3s);
+      double* r3s = reinterpret_cast<double*>(aux + al.r3s);
       const bool fork = b.side != nullptr;
       cudaStream_t sr = fork ? b.side : st;
       if (fork) {
@@ -1247,19 +1250,22 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
           m, natom, reinterpret_cast<const C<double>*>(b.F), b.rho1, b.core, reinterpret_cast<C<double>*>(b.W),
           b.energy, b.edf, b.dedrho, b.err, rho_rest);
       if (ev_between) cudaEventRecord(ev_between, st);
-      cudaMemsetAsync(g3i, 0, al.g3s - al.g3i, st);
-      const size_t sb = b3_fe64_smem<FeDims>(m, kB3Warps64);
+      cudaMemsetAsync(r3i, 0, al.g3s - al.r3i, st);
+      const size_t sb = b3_fe64_smem<FeDims>(m);
       set_smem(k_b3_fe64<FeDims, kB3Warps64>, sb);
+      // one CTA per block, the last partial wave split by task range (B3Split)
       const int nblk = (natom + 31) / 32;
-      const int gb = std::min(nblk, resident_grid(k_b3_fe64<FeDims, kB3Warps64>, kB3Warps64 * 32, sb));
+      const B3Split sp = b3_split(nblk, grid_cap);
+      const int gb = sp.parts > 1 ? sp.nfull + sp.ntail * sp.parts : std::min(nblk, grid_cap);
       k_b3_fe64<FeDims, kB3Warps64><<<gb, kB3Warps64 * 32, sb, st>>>(
-          m, natom, reinterpret_cast<const C<double>*>(b.F), g3i, g3s, rho3, b.err);
+          m, natom, reinterpret_cast<const C<double>*>(b.F), g3i, g3s, r3i, r3s, b.err, sp.nfull, sp.parts);
       if (fork) {
         cudaEventRecord(b.ev_join, sr);
         cudaStreamWaitEvent(st, b.ev_join, 0);
       }
       const int gf = (natom + 255) / 256;
-      k_finish_fe<<<gf, 256, 0, st>>>(m, natom, b.rho1, rho_rest, rho3, b.core, b.energy, b.edf, b.dedrho, b.err);
+      k_finish_fe<<<gf, 256, 0, st>>>(m, natom, b.rho1, rho_rest, nullptr, b.core, b.energy, b.edf, b.dedrho, b.err,
+                                      r3i, r3s);
       if (kernels) *kernels += 3;
       return 2;
     }
@@ -1376,7 +1382,7 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
     if (precision == 0) {
       if (which == 0) return abasis_fe_smem<double, FeDims>();
       if (which == 1) {
-        const size_t a = density_smem<double>(m), b = b3_fe64_smem<FeDims>(m, kB3Warps64);
+        const size_t a = density_smem<double>(m), b = b3_fe64_smem<FeDims>(m);
         return a > b ? a : b;
       }
       return forces_fe_smem<double, FeDims>(true);

@@ -1195,21 +1195,26 @@ __global__ void __launch_bounds__(NW * 32, 1)
 // precision), the same dense tasks as k_b3_fe with 32 atoms in the lanes of
 // each warp; the coefficients C are read from global memory (one uniform
 // load serves the warp) and the factors Xs[nc][33] are staged in shared
-// memory. The warps take tasks in a fixed order (warp w: tasks w, w + NW,
-// ...), so the density of every atom sums in a fixed order.
+// memory. Warps take tasks from a shared counter.
 //
-// Gradients are exact integer sums: every contribution v is rounded once to
-// a 64-bit integer q = rint(v * 2^e) and added with an integer atomic into
-// G3i[block][c][lane] (re, im), so the result does not depend on the order
-// in which the warps' atomics arrive: the FP64 path stays bitwise
-// reproducible. The exponent e of each atom follows from a bound of every
-// partial sum of its gradients: with f = max over the atom's factors of
-// |x| + |y|, every gradient is at most b3_bound * f^2 (model.hpp
-// DenseB3::bound), so e = 61 - ceil(log2(b3_bound f^2)) keeps the sums below
-// 2^61; G3s[position] receives 2^-e. e depends on the atom alone, so an atom
-// gets the same result in any batch and any order. The rounding error of a
-// gradient is at most its number of contributions times 2^-e / 2, about
-// 1e-17 of the bound.
+// Every sum is exact integer arithmetic, so no result depends on which warp
+// or CTA took which task or in which order the atomics arrive: the FP64 path
+// stays bitwise reproducible, and an atom gets the same result in any batch
+// and any order. Each contribution v is rounded once to a 64-bit integer
+// q = rint(v * 2^e) and added with integer atomics: the gradients into
+// G3i[block][c][lane] (re, im), the density into R3i[position]. The
+// exponents of an atom follow from bounds of every partial sum: with f = max
+// over the atom's factors of |x| + |y|, every gradient is at most
+// b3_bound * f^2 and the density at most b3_bound_rho * f^3 (model.hpp
+// DenseB3), so e = 61 - ceil(log2(bound)) keeps the sums below 2^61;
+// G3s[position] and R3s[position] receive 2^-e. The rounding error of a sum
+// is at most its number of contributions times 2^-e / 2, about 1e-17 of its
+// bound.
+//
+// Split tail (parts > 1, one CTA per block): CTAs below `nfull` evaluate
+// their block whole; the remaining blocks, the last partial wave of one CTA
+// per SM, are each divided among `parts` CTAs by task range. The parts add
+// into the same integer sums, so nothing else is needed to combine them.
 constexpr int kB3Stride64 = 33;  // row stride of Xs in complex elements
 
 __device__ __forceinline__ C<double> b3_load64(const C<double>* Xs, unsigned code, int lane) {
@@ -1305,35 +1310,48 @@ __device__ __forceinline__ double b3_task64(const double* __restrict__ Cg, const
   return rt;
 }
 
-// Shared memory: Xs[nc][33] (complex FP64), the per-warp density partials
-// [NW][32] and the factor map [nc]. G3i is [ceil(natom/32)][nc][32][2] words,
-// zeroed before the launch, and G3s [ceil(natom/32) * 32]; blocks are 32
+// Shared memory: Xs[nc][33] (complex FP64) and the factor map [nc]. G3i is
+// [ceil(natom/32)][nc][32][2] words and R3i [ceil(natom/32) * 32], both
+// zeroed before the launch; G3s and R3s [ceil(natom/32) * 32]; blocks are 32
 // consecutive queue positions.
 template <class D, int NW>
 __global__ void __launch_bounds__(NW * 32, 1)
     k_b3_fe64(DeviceModel m, int natom, const C<double>* __restrict__ F, unsigned long long* __restrict__ G3i,
-              double* __restrict__ G3s, double* __restrict__ rho3, int* err) {
+              double* __restrict__ G3s, unsigned long long* __restrict__ R3i, double* __restrict__ R3s, int* err,
+              int nfull, int parts) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NPOS = D::NPOS, I = D::I, NM = D::NM;
   const int nc = m.b3_nc;
   C<double>* Xs = reinterpret_cast<C<double>*>(smem);
-  double* rpart = reinterpret_cast<double*>(Xs + nc * kB3Stride64);  // [NW][32]
-  int* s_fac = reinterpret_cast<int*>(rpart + NW * 32);              // [nc]
+  int* s_fac = reinterpret_cast<int*>(Xs + nc * kB3Stride64);  // [nc]
   __shared__ int s_atom[32];
   // per atom, the largest |x| + |y| of its factors (non-negative doubles
   // order as their bit patterns)
   __shared__ unsigned long long s_fm[32];
+  __shared__ int s_next;  // next task to take
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nblk = (natom + 31) / 32;
+  // this CTA's blocks and task range
+  int blk_first = blockIdx.x, blk_stride = gridDim.x, task0 = 0, task1 = m.b3_ntask;
+  if (parts > 1) {
+    blk_stride = nblk;  // one block per CTA
+    if (static_cast<int>(blockIdx.x) >= nfull) {
+      const int q = (blockIdx.x - nfull) / parts, p = (blockIdx.x - nfull) % parts;
+      blk_first = nfull + q;
+      task0 = m.b3_ntask * p / parts;
+      task1 = m.b3_ntask * (p + 1) / parts;
+    }
+  }
   for (int c = threadIdx.x; c < nc; c += blockDim.x) s_fac[c] = __ldg(m.b3_factor + c);
   __syncthreads();
-  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+  for (int blk = blk_first; blk < nblk; blk += blk_stride) {
     const int a0 = blk * 32;
     const int na = min(32, natom - a0);
     if (threadIdx.x < 32) {
       if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
       s_fm[threadIdx.x] = 0ull;
     }
+    if (threadIdx.x == 0) s_next = task0 + NW;
     __syncthreads();
     // stage: thread c takes element c of every atom
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
@@ -1353,29 +1371,36 @@ __global__ void __launch_bounds__(NW * 32, 1)
       }
     }
     __syncthreads();
-    // this lane's atom: its fixed-point exponent
-    double scale;
+    // this lane's atom: the fixed-point exponents of its gradients and density
+    double gscale, rscale;
     {
       const double f = __longlong_as_double(static_cast<long long>(s_fm[lane]));
-      const double bound = m.b3_bound * f * f;
-      int ex = 0;
-      if (!(bound < 1e300)) {  // non-finite factors
+      const double bg = m.b3_bound * f * f, br = m.b3_bound_rho * f * f * f;
+      int eg = 0, er = 0;
+      if (!(bg < 1e300) || !(br < 1e300)) {  // non-finite factors
         if (lane < na) raise_error(err, kDevNaN);
-        ex = 1100;
-      } else if (bound > 0.0) {
-        frexp(bound, &ex);  // bound < 2^ex
+        eg = er = 1100;
+      } else {
+        if (bg > 0.0) frexp(bg, &eg);  // bound < 2^eg
+        if (br > 0.0) frexp(br, &er);
       }
-      const int e = max(-1000, min(1000, 61 - ex));
-      scale = ldexp(1.0, e);
-      if (warp == 0) G3s[a0 + lane] = ldexp(1.0, -e);
+      eg = max(-1000, min(1000, 61 - eg));
+      er = max(-1000, min(1000, 61 - er));
+      gscale = ldexp(1.0, eg);
+      rscale = ldexp(1.0, er);
+      if (warp == 0) {  // every part of a split block writes the same values
+        G3s[a0 + lane] = ldexp(1.0, -eg);
+        R3s[a0 + lane] = ldexp(1.0, -er);
+      }
     }
     unsigned long long* G = G3i + static_cast<size_t>(blk) * nc * 64 + 2 * lane;
-    double rloc = 0.0;
+    long long racc = 0;
+    int tk = task0 + warp;
 #pragma unroll 1
-    for (int tk = warp; tk < m.b3_ntask; tk += NW) {
+    while (tk < task1) {
       const int k = __ldg(m.b3_combo + tk);
       const int pat = __ldg(m.b3_pattern + k);
-      const double cfs = __ldg(m.b3_cf64 + tk) * scale;
+      const double cfs = __ldg(m.b3_cf64 + tk) * gscale;
       const uint16_t* code = m.b3_code + tk * NPOS;
       const uint16_t* code2 = m.b3_code2 + tk * NPOS;
       const double* Ck = m.b3_C64 + static_cast<size_t>(k) * NM * I * I;
@@ -1383,15 +1408,12 @@ __global__ void __launch_bounds__(NW * 32, 1)
       if (pat == 0) r = b3_task64<0, D>(Ck, Xs, G, code, code2, cfs, lane);
       else if (pat == 1) r = b3_task64<1, D>(Ck, Xs, G, code, code2, cfs, lane);
       else r = b3_task64<2, D>(Ck, Xs, G, code, code2, cfs, lane);
-      rloc = fma(__ldg(m.b3_cfw64 + tk), r, rloc);
+      racc += __double2ll_rn(__ldg(m.b3_cfw64 + tk) * rscale * r);
+      int nx = 0;
+      if (lane == 0) nx = atomicAdd(&s_next, 1);
+      tk = __shfl_sync(0xffffffffu, nx, 0);
     }
-    rpart[warp * 32 + lane] = rloc;
-    __syncthreads();
-    if (warp == 0 && lane < na) {
-      double r3 = 0.0;
-      for (int w = 0; w < NW; ++w) r3 += rpart[w * 32 + lane];
-      rho3[s_atom[lane]] = r3;
-    }
+    if (lane < na) atomicAdd(R3i + a0 + lane, static_cast<unsigned long long>(racc));
     __syncthreads();
   }
 }
@@ -1399,13 +1421,19 @@ __global__ void __launch_bounds__(NW * 32, 1)
 // k_finish_fe: per atom (one per thread) rho = rho1 + rho_rest + rho3, the
 // FP64 embedding and the inner cutoff on the core energy; the energy, edf and
 // dE/drho outputs (the two density kernels before it may run side by side).
+// With R3i (FP64), the 3-body density is the fixed-point sum of k_b3_fe64 at
+// the atom's queue position times its scale R3s.
 __global__ void __launch_bounds__(256) k_finish_fe(DeviceModel m, int natom, const double* __restrict__ rho1,
                                                    const double* __restrict__ rho_rest,
                                                    const double* __restrict__ rho3, const double* __restrict__ core,
                                                    double* __restrict__ energy, double* __restrict__ edf_out,
-                                                   double* __restrict__ dedrho_out, int* err) {
-  for (int atom = blockIdx.x * blockDim.x + threadIdx.x; atom < natom; atom += gridDim.x * blockDim.x) {
-    const double rho = rho1[static_cast<size_t>(atom) * 2] + rho_rest[atom] + rho3[atom];
+                                                   double* __restrict__ dedrho_out, int* err,
+                                                   const unsigned long long* __restrict__ R3i = nullptr,
+                                                   const double* __restrict__ R3s = nullptr) {
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < natom; it += gridDim.x * blockDim.x) {
+    const int atom = R3i ? queue_atom(m, it) : it;
+    const double r3 = R3i ? static_cast<double>(static_cast<long long>(R3i[it])) * R3s[it] : rho3[atom];
+    const double rho = rho1[static_cast<size_t>(atom) * 2] + rho_rest[atom] + r3;
     if (!isfinite(rho)) raise_error(err, kDevNaN);
     double Fd, dFd;
     embed(m.nfemb, rho, m.par[0][0], m.par[1][0], Fd, dFd);
@@ -1900,9 +1928,8 @@ size_t b3_fe_smem(const DeviceModel& m, int nw) {
 }
 constexpr int kB3Warps64 = 8;  // warps per CTA of k_b3_fe64
 template <class D>
-size_t b3_fe64_smem(const DeviceModel& m, int nw) {
-  return sizeof(C<double>) * static_cast<size_t>(m.b3_nc) * kB3Stride64 + sizeof(double) * nw * 32 +
-         sizeof(int) * m.b3_nc;
+size_t b3_fe64_smem(const DeviceModel& m) {
+  return sizeof(C<double>) * static_cast<size_t>(m.b3_nc) * kB3Stride64 + sizeof(int) * m.b3_nc;
 }
 template <class R, class D>
 size_t forces_fe_smem(bool sout) {

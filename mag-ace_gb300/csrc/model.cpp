@@ -965,9 +965,11 @@ int build_tables(Model& M, std::string& msg) {
     // sum_{p,j} C a_p Y_j and of Y_j sum_{p,i} C a_p X_i, each times cf
     const int I = D.I, NM = D.NM, npos = NM + 2 * I;
     std::vector<double> mass(D.nc, 0.0), row(npos);
+    D.bound_rho = 0.0;
     for (int t = 0; t < D.ntask; ++t) {
       std::fill(row.begin(), row.end(), 0.0);
       const double* Ck = D.C.data() + static_cast<size_t>(D.task_combo[t]) * NM * I * I;
+      double csum = 0.0;
       for (int p = 0; p < NM; ++p)
         for (int i = 0; i < I; ++i)
           for (int j = 0; j < I; ++j) {
@@ -975,8 +977,10 @@ int build_tables(Model& M, std::string& msg) {
             row[p] += c;
             row[NM + i] += c;
             row[NM + I + j] += c;
+            csum += c;
           }
       const double cf = std::fabs(D.task_cf[t]);
+      D.bound_rho += cf * std::fabs(D.task_w[t]) * csum;
       for (int q = 0; q < npos; ++q) {
         const uint16_t c = D.code[static_cast<size_t>(t) * npos + q];
         const uint16_t c2 = D.code2[static_cast<size_t>(t) * npos + q];

@@ -108,6 +108,10 @@ struct DenseB3 {
   // sum of |C| over that position's products. With every factor bounded by
   // |x| + |y| <= f, every partial sum of a gradient is bounded by bound * f^2.
   double bound = 0.0;
+  // the same for the density: sum over tasks of |cf * w| times the sum of
+  // |C| over the task's products; every partial sum of the 3-body density
+  // is bounded by bound_rho * f^3
+  double bound_rho = 0.0;
 };
 
 // Per-cluster m-terms of the descriptors B_k, the basis functions that the
