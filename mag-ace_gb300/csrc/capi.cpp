@@ -106,7 +106,7 @@ struct Runtime {
     }
   } gb1, gb2;
   DevBuf<float> b3_Cf, b3_cff, b3_mult, b3_cfw;
-  DevBuf<double> b3_C64, b3_cf64, b3_cfw64;
+  DevBuf<double> b3_C64, b3_cf64, b3_cfw64, r_kap64;
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
   DevBuf<uint16_t> b3_code, b3_code2;
   DevBuf<int32_t> d_rank1_n, d_begin;
@@ -291,6 +291,7 @@ int upload_tables() {
       CUDA_TRY(R.r_run.upload(T.run));
       CUDA_TRY(R.r_g0.upload(T.slot_g0));
       CUDA_TRY(R.r_rec.upload(T.rec));
+      CUDA_TRY(R.r_kap64.upload(T.kap));
       CUDA_TRY(R.r_warp_begin.upload(T.warp_begin));
       CUDA_TRY(R.r_warp_slots.upload(T.warp_slots));
       CUDA_TRY(R.r_stream.upload(T.stream));
@@ -363,6 +364,7 @@ int upload_tables() {
   d.r_factor = R.r_factor.p;
   d.r_run = R.r_run.p;
   d.r_rec = R.r_rec.p;
+  d.r_kap64 = R.r_kap64.p;
   d.r_g0 = R.r_g0.p;
   d.r_warp_begin = R.r_warp_begin.p;
   d.r_warp_slots = R.r_warp_slots.p;
@@ -933,7 +935,7 @@ void ace_release_device(void) {
   R.b3_code.release();
   R.b3_code2.release();
   R.b3_cfw.release();
-  for (auto* b : {&R.b3_C64, &R.b3_cf64, &R.b3_cfw64}) b->release();
+  for (auto* b : {&R.b3_C64, &R.b3_cf64, &R.b3_cfw64, &R.r_kap64}) b->release();
   for (auto* b : {&R.d_rank1_n, &R.d_begin, &R.r_factor, &R.r_run, &R.r_g0, &R.r_warp_begin, &R.r_warp_slots})
     b->release();
   R.r_rec.release();

@@ -568,18 +568,13 @@ struct CSum {
   __device__ __forceinline__ double value() const { return static_cast<double>(hi) + static_cast<double>(lo); }
 };
 
-template <class R, int ND, bool REST = false>
+template <class R, int ND>
 __global__ void __launch_bounds__(kDensityThreads)
     k_density(DeviceModel m, int natom, const C<R>* __restrict__ F, const double* __restrict__ rho1,
               const double* __restrict__ core, C<R>* __restrict__ W, double* __restrict__ energy,
-              double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err,
-              double* __restrict__ rho_rest = nullptr) {
-  static_assert(!REST || ND == 1, "the rest pass serves the one-density specialised layout");
+              double* __restrict__ edf_out, double* __restrict__ dedrho_out, int* err) {
   extern __shared__ __align__(16) unsigned char smem[];
-  // REST: the table without the 3-body terms (g2); the pass writes the
-  // density of its terms to rho_rest and the weights without dE/drho, and
-  // the embedding follows in k_finish_fe once the 3-body part is known
-  const GatherView& G = REST ? m.g2 : m.g;
+  const GatherView& G = m.g;
   C<R>* Fs = reinterpret_cast<C<R>*>(smem);
   C<R>* part = Fs + ((m.nF + 1) & ~1);
   C<R>* tot = part + ((G.nseg * ND + 1) & ~1);
@@ -661,22 +656,6 @@ __global__ void __launch_bounds__(kDensityThreads)
       if (lane == 0) s_red[warp][d] = v;
     }
     __syncthreads();
-    if constexpr (REST) {
-      if (threadIdx.x == 0) {
-        double rho = 0.0;
-        for (int w = 0; w < kDensityThreads / 32; ++w) rho += s_red[w][0];
-        rho_rest[atom] = rho;
-      }
-      C<R>* Wa = W + static_cast<size_t>(atom) * m.nW;
-      for (int s = threadIdx.x; s < G.nslot; s += blockDim.x) {
-        const int w = G.slot_weight[s];
-        if (w < 0) continue;
-        const R mu = R(G.slot_mult[s]);
-        Wa[w] = {mu * tot[s].x, mu * tot[s].y};
-      }
-      __syncthreads();
-      continue;
-    }
     if (threadIdx.x == 0) {
       double energyi = 0.0, dE[ND];
       for (int d = 0; d < ND; ++d) {
@@ -970,8 +949,8 @@ size_t abasis_smem(const DeviceModel& m) {
 }
 
 template <class R>
-size_t density_smem(const DeviceModel& m, bool rest = false) {
-  const GatherView& g = rest ? m.g2 : m.g;
+size_t density_smem(const DeviceModel& m) {
+  const GatherView& g = m.g;
   return sizeof(C<R>) * (static_cast<size_t>((m.nF + 1) & ~1) + static_cast<size_t>((g.nseg * m.nd + 1) & ~1) +
                          static_cast<size_t>(g.nslot) * m.nd) + 64;
 }
@@ -1227,10 +1206,9 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
   }
   if constexpr (sizeof(R) == 8) {
     if (fe) {
-      // FP64, specialised layout: the 2-/4-body terms through the gather
-      // table without the 3-body terms (k_density, rest pass) on the side
-      // stream, beside the dense 3-body kernel k_b3_fe64 on `st`; then
-      // k_finish_fe (density, embedding, inner cutoff)
+      // FP64, specialised layout: the 2-/4-body terms through the rest table
+      // (k_rest64) on the side stream, beside the dense 3-body kernel
+      // k_b3_fe64 on `st`; then k_finish_fe (density, embedding, inner cutoff)
       const AuxLayout64 al = aux_layout64(m, natom);
       unsigned char* aux = static_cast<unsigned char*>(b.aux);
       double* rho_rest = reinterpret_cast<double*>(aux);
@@ -1244,11 +1222,11 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
         cudaEventRecord(b.ev_fork, st);
         cudaStreamWaitEvent(sr, b.ev_fork, 0);
       }
-      const size_t s2 = density_smem<double>(m, true);
-      set_smem(k_density<double, 1, true>, s2);
-      k_density<double, 1, true><<<grid, kDensityThreads, s2, sr>>>(
-          m, natom, reinterpret_cast<const C<double>*>(b.F), b.rho1, b.core, reinterpret_cast<C<double>*>(b.W),
-          b.energy, b.edf, b.dedrho, b.err, rho_rest);
+      const size_t s2 = rest64_smem<FeDims>(m);
+      set_smem(k_rest64<FeDims, kRestWarps64>, s2);
+      const int nb16 = (natom + 15) / 16;
+      k_rest64<FeDims, kRestWarps64><<<std::min(nb16, grid_cap), kRestWarps64 * 32, s2, sr>>>(
+          m, natom, reinterpret_cast<const C<double>*>(b.F), reinterpret_cast<C<double>*>(b.W), rho_rest);
       if (ev_between) cudaEventRecord(ev_between, st);
       cudaMemsetAsync(r3i, 0, al.g3s - al.r3i, st);
       const size_t sb = b3_fe64_smem<FeDims>(m);
@@ -1382,7 +1360,7 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
     if (precision == 0) {
       if (which == 0) return abasis_fe_smem<double, FeDims>();
       if (which == 1) {
-        const size_t a = density_smem<double>(m), b = b3_fe64_smem<FeDims>(m);
+        const size_t a = rest64_smem<FeDims>(m), b = b3_fe64_smem<FeDims>(m);
         return a > b ? a : b;
       }
       return forces_fe_smem<double, FeDims>(true);

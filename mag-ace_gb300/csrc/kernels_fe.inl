@@ -775,6 +775,96 @@ __global__ void __launch_bounds__(NW * 32, 1)
   }
 }
 
+// k_rest64: the 2- and 4-body terms in FP64 (the plain precision) through
+// the rest table, 16 atoms per CTA: lane & 15 is the atom, and the two
+// half-warps take alternate entries of the same slot, so that both follow
+// the same path; a shuffle adds their sums. Warp w walks the slots the host
+// schedule gave to table warps w, w + NW, ... in order, so every sum has a
+// fixed order. Writes rho_rest and the unscaled weights mult * dRho_rest/dF.
+constexpr int kRestStride64 = 17;  // row stride of Fs in complex elements
+constexpr int kRestWarps64 = 16;   // warps per CTA of k_rest64
+
+template <int A>
+__device__ __forceinline__ void rest_run64(const uint4* __restrict__ rec, const double* __restrict__ kap, int e0,
+                                           int e1, const C<double>* Fs, int al, C<double>& v) {
+#pragma unroll 2
+  for (int e = e0; e < e1; e += 2) {
+    const uint4 r = __ldg(rec + e);
+    const double k = __ldg(kap + e);
+    C<double> p = Fs[(r.y & 0xffffu) * kRestStride64 + al];
+    if (A >= 2) p = cmul(p, Fs[(r.y >> 16) * kRestStride64 + al]);
+    if (A >= 3) p = cmul(p, Fs[r.z * kRestStride64 + al]);
+    v.x = fma(k, p.x, v.x);
+    v.y = fma(k, p.y, v.y);
+  }
+}
+
+template <class D, int NW>
+__global__ void __launch_bounds__(NW * 32, 1)
+    k_rest64(DeviceModel m, int natom, const C<double>* __restrict__ F, C<double>* __restrict__ W,
+             double* __restrict__ rho_rest) {
+  static_assert(kRestTableWarps % NW == 0, "the slot schedule is dealt to kRestTableWarps warps");
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nf = m.r_nfac, nW = m.nW;
+  const GatherView& g = m.g2;  // slot weights and multiplicities (same slot numbering)
+  C<double>* Fs = reinterpret_cast<C<double>*>(smem);                    // [nf][17]
+  double* rpart = reinterpret_cast<double*>(Fs + nf * kRestStride64);    // [NW][16]
+  __shared__ int s_atom[16];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, al = lane & 15, half = lane >> 4;
+  const int nblk = (natom + 15) / 16;
+  const uint4* rec = reinterpret_cast<const uint4*>(m.r_rec);
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int a0 = blk * 16;
+    const int na = min(16, natom - a0);
+    if (threadIdx.x < na) s_atom[threadIdx.x] = queue_atom(m, a0 + threadIdx.x);
+    __syncthreads();
+    // stage: thread c takes factor c of every atom
+    for (int c = threadIdx.x; c < nf; c += blockDim.x) {
+      const int fc = __ldg(m.r_factor + c);
+      C<double> v[16];
+#pragma unroll
+      for (int b = 0; b < 16; ++b)
+        v[b] = b < na ? F[static_cast<size_t>(s_atom[b]) * m.nF + fc] : C<double>{0.0, 0.0};
+#pragma unroll
+      for (int b = 0; b < 16; ++b) Fs[c * kRestStride64 + b] = v[b];
+    }
+    __syncthreads();
+    const int atom = al < na ? s_atom[al] : -1;
+    double rloc = 0.0;
+    for (int sw = warp; sw < kRestTableWarps; sw += NW)
+      for (int q = __ldg(m.r_warp_begin + sw); q < __ldg(m.r_warp_begin + sw + 1); ++q) {
+        const int s = __ldg(m.r_warp_slots + q);
+        C<double> v = {0.0, 0.0};
+        rest_run64<1>(rec, m.r_kap64, __ldg(m.r_run + 3 * s) + half, __ldg(m.r_run + 3 * s + 1), Fs, al, v);
+        rest_run64<2>(rec, m.r_kap64, __ldg(m.r_run + 3 * s + 1) + half, __ldg(m.r_run + 3 * s + 2), Fs, al, v);
+        rest_run64<3>(rec, m.r_kap64, __ldg(m.r_run + 3 * s + 2) + half, __ldg(m.r_run + 3 * s + 3), Fs, al, v);
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, 16);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, 16);
+        if (half == 0) {
+          const int g0 = __ldg(m.r_g0 + s);
+          if (g0 >= 0) rloc = re_mac(rloc, Fs[g0 * kRestStride64 + al], v);
+          const int w = __ldg(g.slot_weight + s);
+          if (w >= 0 && atom >= 0) {
+            const double mu = __ldg(g.slot_mult + s);
+            W[static_cast<size_t>(atom) * nW + w] = {mu * v.x, mu * v.y};
+          }
+        }
+      }
+    if (half == 0) rpart[warp * 16 + al] = rloc;
+    __syncthreads();
+    if (threadIdx.x < na) {
+      double r = 0.0;
+      for (int w = 0; w < NW; ++w) r += rpart[w * 16 + threadIdx.x];
+      rho_rest[s_atom[threadIdx.x]] = r;
+    }
+    __syncthreads();
+  }
+}
+template <class D>
+size_t rest64_smem(const DeviceModel& m) {
+  return sizeof(C<double>) * static_cast<size_t>(m.r_nfac) * kRestStride64 + sizeof(double) * kRestWarps64 * 16;
+}
+
 constexpr int kB3Stride = 33;  // row stride of Xs/Gs in complex elements
 
 // pairs (i, j) the enumeration keeps for pattern PAT (0: l1' == l2' keeps

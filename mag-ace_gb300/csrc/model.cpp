@@ -481,6 +481,7 @@ void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
         std::memcpy(&kb, &k, sizeof(kb));
         const uint32_t o1 = use(e.o[0]), o2 = a >= 2 ? use(e.o[1]) : 0, o3 = a >= 3 ? use(e.o[2]) : 0;
         T.rec.insert(T.rec.end(), {kb, o1 | (o2 << 16), o3, 0u});
+        T.kap.push_back(e.kappa[0]);
         cost[s] += 2.0 * a;
       }
     }

@@ -141,6 +141,7 @@ struct RestTable {
   std::vector<int32_t> factor_of;  // [nfac] factor index
   std::vector<int32_t> run;        // [3 * nslot + 1]
   std::vector<uint32_t> rec;       // [entries][4]
+  std::vector<double> kap;         // [entries] kappa in FP64 (the plain-precision kernel)
   std::vector<int32_t> slot_g0;    // [nslot] compact A0 factor, or -1
   std::vector<int32_t> warp_begin; // [nwarp + 1]
   std::vector<int32_t> warp_slots; // [nslot]
