@@ -32,7 +32,7 @@ extern "C" {
 #define MAGACE_OK 0
 #define MAGACE_ERR_FILE 1        /* potential file missing or unreadable */
 #define MAGACE_ERR_FORMAT 2      /* malformed / inconsistent potential file */
-#define MAGACE_ERR_UNSUPPORTED 3 /* nele != 1, 5/6-body clusters, radtype 0-2, nfemb 3/4 */
+#define MAGACE_ERR_UNSUPPORTED 3 /* nele != 1, radtype 0-2, nfemb 3/4, 5/6-body dims beyond the 3-body ones */
 #define MAGACE_ERR_SMALL_R 4     /* bond shorter than one LUT bin (src/radial.F90:71-75) */
 #define MAGACE_ERR_MOMENT 5      /* |m| < 0, NaN, or >= magnetic cutoff (LUT overrun in the reference) */
 #define MAGACE_ERR_NOT_INIT 6    /* evaluation before a successful init */
@@ -91,8 +91,13 @@ int ace_get_precision(void);
 int ace_basis_sizes(int* out);
 
 /* Cluster index rows as in the file's 'clu' records: rank 1 -> 1 int per
- * cluster, 2 -> 4, 3 -> 9, 4 -> 15. */
+ * cluster, 2 -> 4, 3 -> 9, 4 -> 15, 5 -> 21, 6 -> 27 (the reference's
+ * b5index / b6index, src/util.F90:2817-3760). */
 int ace_basis_rows(int rank, int* out);
+
+/* Number of clusters of one rank (1..6) after init (nvar1..nvar6 of the
+ * reference, src/util.F90:1613-3760); sizes the ace_basis_rows output. */
+int ace_basis_count(int rank, int* count);
 
 /* Evaluation on device-resident arrays (no host copies). Bonds of atom i are
  * bond_offset[i] .. bond_offset[i+1]-1 (0-based CSR, natom+1 entries).

@@ -88,20 +88,21 @@ struct Runtime {
   DevBuf<float> c1f;
   DevBuf<float> lut_a32, lut_m32;
   struct GatherBufs {
-    DevBuf<double> kap[4], slot_mult;
-    DevBuf<float> kapf[4], slot_multf;
-    DevBuf<uint32_t> o12[4];
-    DevBuf<uint16_t> o3;
+    DevBuf<double> kap[kMaxArity + 1], slot_mult;
+    DevBuf<float> kapf[kMaxArity + 1], slot_multf;
+    DevBuf<uint32_t> o12[kMaxArity + 1], o34[kMaxArity + 1];
+    DevBuf<uint16_t> o5;
     DevBuf<int32_t> grp_arity, grp_len, grp_first, grp_seg, slot_seg, slot_factor, slot_weight;
     void release() {
-      for (int a = 0; a < 4; ++a) {
+      for (int a = 0; a <= kMaxArity; ++a) {
         kap[a].release();
         kapf[a].release();
         o12[a].release();
+        o34[a].release();
       }
       slot_mult.release();
       slot_multf.release();
-      o3.release();
+      o5.release();
       for (auto* b : {&grp_arity, &grp_len, &grp_first, &grp_seg, &slot_seg, &slot_factor, &slot_weight}) b->release();
     }
   } gb1, gb2;
@@ -192,14 +193,15 @@ std::vector<float> to_float(const std::vector<T>& v) {
 }
 
 int upload_gather(const GatherTable& g, Runtime::GatherBufs& B, GatherView& v) {
-  for (int a = 1; a <= 3; ++a) {
+  for (int a = 1; a <= kMaxArity; ++a) {
     std::vector<double> k(g.kap[a][0]);
     k.insert(k.end(), g.kap[a][1].begin(), g.kap[a][1].end());
     CUDA_TRY(B.kap[a].upload(k));
     CUDA_TRY(B.kapf[a].upload(to_float(k)));
     CUDA_TRY(B.o12[a].upload(g.o12[a]));
+    CUDA_TRY(B.o34[a].upload(g.o34[a]));
   }
-  CUDA_TRY(B.o3.upload(g.o3));
+  CUDA_TRY(B.o5.upload(g.o5));
   CUDA_TRY(B.grp_arity.upload(g.grp_arity));
   CUDA_TRY(B.grp_len.upload(g.grp_len));
   CUDA_TRY(B.grp_first.upload(g.grp_first));
@@ -220,14 +222,16 @@ int upload_gather(const GatherTable& g, Runtime::GatherBufs& B, GatherView& v) {
   v.kap[0] = nullptr;
   v.kapf[0] = nullptr;
   v.o12[0] = nullptr;
+  v.o34[0] = nullptr;
   v.kstride[0] = 0;
-  for (int a = 1; a <= 3; ++a) {
+  for (int a = 1; a <= kMaxArity; ++a) {
     v.kap[a] = B.kap[a].p;
     v.kapf[a] = B.kapf[a].p;
     v.o12[a] = B.o12[a].p;
+    v.o34[a] = B.o34[a].p;
     v.kstride[a] = static_cast<int>(g.kap[a][0].size());
   }
-  v.o3 = B.o3.p;
+  v.o5 = B.o5.p;
   v.slot_seg = B.slot_seg.p;
   v.slot_factor = B.slot_factor.p;
   v.slot_weight = B.slot_weight.p;
@@ -265,7 +269,7 @@ int upload_tables() {
   {
     int st = upload_gather(M.gt, R.gb1, R.dm.g);
     if (st) return st;
-    if (M.ndensity == 1) {
+    if (M.ndensity == 1 && !M.high) {
       st = upload_gather(M.gt_nob3, R.gb2, R.dm.g2);
       if (st) return st;
       const DenseB3& D = M.db3;
@@ -320,6 +324,7 @@ int upload_tables() {
   d.nF = L.nF; d.nWA = L.nWA; d.offW2 = L.offW2; d.offW0 = L.offW0; d.nW = L.nW;
   d.nd = M.ndensity;
   d.nfemb = M.nfemb;
+  d.high = M.high ? 1 : 0;
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 2; ++b) d.par[a][b] = M.par[a][b];
   d.ecut = M.ecut;
@@ -649,11 +654,19 @@ int ace_basis_sizes(int* out) {
 int ace_basis_rows(int rank, int* out) {
   Runtime& R = rt();
   if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
-  if (rank < 1 || rank > 4) return set_error(MAGACE_ERR_ARGS, "rank must be 1..4");
+  if (rank < 1 || rank > 6) return set_error(MAGACE_ERR_ARGS, "rank must be 1..6");
   size_t k = 0;
   for (const auto& row : R.model.rows[rank])
     for (int v : row) out[k++] = v;
   return MAGACE_OK;
+}
+
+int ace_basis_count(int rank, int* count) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  if (rank < 1 || rank > 6 || !count) return set_error(MAGACE_ERR_ARGS, "rank must be 1..6");
+  *count = static_cast<int>(R.model.rows[rank].size());
+  return set_error(MAGACE_OK, "");
 }
 
 int ace_last_launch_count(void) { return rt().last_kernels; }

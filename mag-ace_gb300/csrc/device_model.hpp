@@ -27,6 +27,12 @@ enum DeviceError : int {
   kDevTimeout = 5, // a bulk copy of bond inputs did not complete within the wait limit
 };
 
+// largest number of other factors in one gather entry: a 6-body term
+// A0 A1 .. A5 adds the product of five factors to each of its slots
+constexpr int kMaxArity = 5;
+// factor slots per descriptor term: six factors, ONE-padded to 16 bytes
+constexpr int kDescFactors = 8;
+
 // one gather table: group g has arity grp_arity[g], length grp_len[g] and its
 // entries at grp_first[g] + e*32 + lane
 struct GatherView {
@@ -35,11 +41,12 @@ struct GatherView {
   const int32_t* grp_len;
   const int32_t* grp_first;
   const int32_t* grp_seg;      // [ngroup*32] segment id per lane, -1 padding
-  const double* kap[4];        // [arity][density * kstride[arity] + slot] FP64
-  const float* kapf[4];        // FP32 copies (split path)
-  int kstride[4];
-  const uint32_t* o12[4];      // o1 | o2 << 16
-  const uint16_t* o3;          // third factor of arity-3 entries
+  const double* kap[kMaxArity + 1];   // [arity][density * kstride[arity] + slot] FP64
+  const float* kapf[kMaxArity + 1];   // FP32 copies (split path)
+  int kstride[kMaxArity + 1];
+  const uint32_t* o12[kMaxArity + 1]; // o1 | o2 << 16
+  const uint32_t* o34[kMaxArity + 1]; // o3 | o4 << 16 (arity >= 3)
+  const uint16_t* o5;                 // fifth factor of arity-5 entries
   const int32_t* slot_seg;     // [nslot+1]
   const int32_t* slot_factor;  // [nslot] (G0 slots only)
   const int32_t* slot_weight;  // [nslot]
@@ -54,6 +61,7 @@ struct DeviceModel {
   int offA, offA2, offA0, offOne, offZero, nF;
   int nWA, offW2, offW0, nW;
   int nd, nfemb;
+  int high;  // the potential has 5- or 6-body clusters (generic kernels only)
   double par[2][2];  // embedding parameters [order][density]
   double ecut, decut;
   // radial lookup tables: [(nlut+1)][nf] double4 of cubic coefficients

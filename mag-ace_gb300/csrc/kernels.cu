@@ -617,10 +617,14 @@ __global__ void __launch_bounds__(kDensityThreads)
           }
         }
       } else {
-        const uint16_t* o3p = G.o3 + base;
+        // arity 3 to 5 (the 4-, 5- and 6-body terms)
+        const uint32_t* o34p = G.o34[a] + base;
+        const uint16_t* o5p = G.o5 + base;
         for (int e = 0; e < len; ++e) {
-          const uint32_t o = __ldg(op + e * 32);
-          const C<R> p = cmul(cmul(Fs[o & 0xffffu], Fs[o >> 16]), Fs[__ldg(o3p + e * 32)]);
+          const uint32_t o = __ldg(op + e * 32), q = __ldg(o34p + e * 32);
+          C<R> p = cmul(cmul(Fs[o & 0xffffu], Fs[o >> 16]), Fs[q & 0xffffu]);
+          if (a >= 4) p = cmul(p, Fs[q >> 16]);
+          if (a == 5) p = cmul(p, Fs[__ldg(o5p + e * 32)]);
           for (int d = 0; d < ND; ++d) {
             const R k = __ldg(kp + d * ks + e * 32);
             acc[d].x += k * p.x;
@@ -963,13 +967,14 @@ size_t forces_smem(const DeviceModel& m, int T) {
 }
 
 // Whether the compile-time specialised kernels apply: the basis has the Fe
-// layout and one density, and MAGACE_GENERIC is not set.
+// layout, one density and no 5- or 6-body clusters, and MAGACE_GENERIC is
+// not set.
 bool use_specialised(const DeviceModel& m) {
   static const bool forced_generic = [] {
     const char* e = std::getenv("MAGACE_GENERIC");
     return e && e[0] == '1';
   }();
-  return !forced_generic && m.nd == 1 && dims_match<FeDims>(m);
+  return !forced_generic && m.nd == 1 && !m.high && dims_match<FeDims>(m);
 }
 
 // Opts a kernel into `bytes` of dynamic shared memory, once per kernel,
@@ -1429,8 +1434,8 @@ void launch_work_queue(int natom, const int* off, int* order, int* bins, cudaStr
 // ===========================================================================
 // k_descriptors: one CTA per atom, FP64. B[atom][k] for every cluster in
 // coefficient order: rank 1, g_n(|m_i|) - 1 (src/b_basis.F90:74-83); ranks
-// 2..4, Re sum over the cluster's m-terms of cf * F[o0] F[o1] F[o2] F[o3]
-// (src/b_basis.F90:91-307 without the coefficients).
+// 2..6, Re sum over the cluster's m-terms of cf * F[o0] .. F[o5] (missing
+// factors ONE; src/b_basis.F90:91-532 without the coefficients).
 constexpr int kDescThreads = 128;
 
 __global__ void __launch_bounds__(kDescThreads)
@@ -1458,8 +1463,9 @@ __global__ void __launch_bounds__(kDescThreads)
     for (int k = threadIdx.x; k < nB - n1; k += blockDim.x) {
       double acc = 0.0;
       for (int e = m.d_begin[k]; e < m.d_begin[k + 1]; ++e) {
-        const ushort4 o = *reinterpret_cast<const ushort4*>(m.d_o + 4 * static_cast<size_t>(e));
-        const C<double> p = cmul(cmul(Fs[o.x], Fs[o.y]), cmul(Fs[o.z], Fs[o.w]));
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(m.d_o + kDescFactors * static_cast<size_t>(e)));
+        const C<double> p = cmul(cmul(cmul(Fs[q.x & 0xffffu], Fs[q.x >> 16]), cmul(Fs[q.y & 0xffffu], Fs[q.y >> 16])),
+                                 cmul(Fs[q.z & 0xffffu], Fs[q.z >> 16]));
         acc += m.d_cf[e] * p.x;
       }
       Ba[n1 + k] = acc;

@@ -288,6 +288,8 @@ bool build_lut(const Model& mdl, RadialLUT& lut) {
 // (l1,l2,l3) an even triangle, and for the magnetic quadruple every
 // intermediate L01' coupling (l0' l1')L (l2' l3')L allowed, odd L excluded
 // when a pair is identical, even total.
+bool enumerate_high(const BasisDims& d, int rank, std::vector<std::vector<int>>& rows);
+
 void enumerate(const BasisDims& d, std::vector<std::vector<int>>* rows) {
   for (int n = 1; n <= d.nradbase_m; ++n) rows[1].push_back({n});
   for (int a = 1; a <= d.nradial2_m; ++a)
@@ -345,6 +347,170 @@ void enumerate(const BasisDims& d, std::vector<std::vector<int>>* rows) {
   }
 }
 
+// Intermediate couplings of one rank-4, -5 or -6 angular vector, by the
+// rules of the reference's coupling generator for one element
+// (src/util.F90:4790-4857, :4944-5022, :5131-5220): rank 4 ((1 2)L (3 4)L)0
+// gives L; rank 5 (((1 2)L12 (3 4)L34)l5 5)0 gives (L12, L34); rank 6
+// (((1 2)L12 (3 4)L34)L56 (5 6)L56)0 gives (L12, L34, L56); each in the loop
+// order of the generator. Two positions are identical when their (n, l)
+// are: then odd couplings of that pair are excluded. `basis` is false when
+// none is allowed or the l's have an odd sum.
+struct Couplings {
+  std::vector<std::array<int, 3>> v;
+  bool basis = false;
+};
+Couplings couplings(int rank, const int* n, const int* l) {
+  Couplings c;
+  const auto same = [&](int a, int b) { return n[a] == n[b] && l[a] == l[b]; };
+  const auto tri = [](int a, int b, int L) { return L <= a + b && L >= std::abs(a - b); };
+  int lmx = 0, lsum = 0;
+  for (int q = 0; q < rank; ++q) {
+    lmx = std::max(lmx, l[q]);
+    lsum += l[q];
+  }
+  const int lintmax = 2 * lmx;
+  if (rank == 4) {
+    for (int L = 0; L <= lintmax; ++L) {
+      if (!tri(l[0], l[1], L) || !tri(l[2], l[3], L)) continue;
+      if ((same(0, 1) || same(2, 3)) && L % 2) continue;
+      c.v.push_back({L, 0, 0});
+    }
+  } else if (rank == 5) {
+    for (int a = 0; a <= lintmax; ++a)
+      for (int b = 0; b <= lintmax; ++b) {
+        if (!tri(l[0], l[1], a) || !tri(l[2], l[3], b) || !tri(a, b, l[4])) continue;
+        if ((same(0, 1) && a % 2) || (same(2, 3) && b % 2)) continue;
+        if (same(0, 2) && same(1, 3) && a == b && l[4] % 2) continue;
+        c.v.push_back({a, b, 0});
+      }
+  } else {
+    for (int a = 0; a <= lintmax; ++a)
+      for (int b = 0; b <= lintmax; ++b)
+        for (int d = 0; d <= lintmax; ++d) {
+          if (!tri(l[0], l[1], a) || !tri(l[2], l[3], b) || !tri(l[4], l[5], d) || !tri(a, b, d)) continue;
+          if ((same(0, 1) && a % 2) || (same(2, 3) && b % 2) || (same(4, 5) && d % 2)) continue;
+          if (same(0, 2) && same(1, 3) && a == b && d % 2) continue;
+          c.v.push_back({a, b, d});
+        }
+  }
+  c.basis = !c.v.empty() && lsum % 2 == 0;
+  return c;
+}
+
+// Every tuple of `n` digits with ranges [lo[q], hi[q]], the last fastest (the
+// order of the reference's loop nests).
+template <class Fn>
+void odometer(int n, const int* lo, const int* hi, Fn&& fn) {
+  for (int q = 0; q < n; ++q)
+    if (lo[q] > hi[q]) return;
+  std::vector<int> v(lo, lo + n);
+  for (;;) {
+    fn(v.data());
+    int q = n - 1;
+    while (q >= 0 && v[q] == hi[q]) {
+      v[q] = lo[q];
+      --q;
+    }
+    if (q < 0) return;
+    ++v[q];
+  }
+}
+
+// The reference's reordering of couplings after the enumeration
+// (src/util.F90:3079-3094, :3705-3740): within each group of clusters that
+// differ only in their couplings, the entries after the group's first swap
+// the coupling columns [c0, c0 + w) so that smaller sums come first.
+void reorder_couplings(std::vector<std::vector<int>>& rows, size_t first, const std::vector<int>& group, int c0,
+                       int w) {
+  for (size_t n = 0; n < group.size(); ++n)
+    for (int m = 1; m <= group[n] - 2; ++m)
+      for (int k = m + 1; k <= group[n] - 1; ++k) {
+        auto& a = rows[first + n + m];
+        auto& b = rows[first + n + k];
+        int sa = 0, sb = 0;
+        for (int q = 0; q < w; ++q) {
+          sa += a[c0 + q];
+          sb += b[c0 + q];
+        }
+        if (sa > sb)
+          for (int q = 0; q < w; ++q) std::swap(a[c0 + q], b[c0 + q]);
+      }
+}
+
+// 5- and 6-body clusters (src/util.F90:2817-3100, :3436-3760). Candidate index
+// tuples in loop order whose (atomic, magnetic) keys do not increase; per
+// tuple the atomic couplings (rank 4 / 5) and the magnetic ones (rank 5 / 6);
+// the k-th cluster of a tuple pairs the k-th atomic with the k-th magnetic
+// coupling, and where one side has fewer its indices are zeros (such a
+// cluster has no defined basis function, see for_each_term). The 6-body key
+// takes the 5-body dims (src/util.F90:3490-3491). Returns false where the
+// reference stops: a candidate whose atomic keys are not ordered.
+bool enumerate_high(const BasisDims& d, int rank, std::vector<std::vector<int>>& rows) {
+  const int P = rank - 1;  // atomic factors
+  const int na = rank == 5 ? d.nradial5_a : d.nradial6_a, nm = rank == 5 ? d.nradial5_m : d.nradial6_m;
+  const int la = rank == 5 ? d.l5max_a : d.l6max_a, lm = rank == 5 ? d.l5max_m : d.l6max_m;
+  if (na == 0 || nm == 0) return true;
+  const long kma = static_cast<long>(d.nradial5_a) * (d.l5max_a + 1);
+  const long kmm = static_cast<long>(d.nradial5_m) * (d.l5max_m + 1);
+  const long base = (kmm + 1) * kma + kmm;
+  // digits: n1..nP, n0'..nP', l1..lP, l0'..lP'
+  const int nd = 4 * P + 2;
+  std::vector<int> lo(nd), hi(nd);
+  for (int q = 0; q < nd; ++q) {
+    const bool radial = q < 2 * P + 1, atomic = radial ? q < P : q < 3 * P + 1;
+    lo[q] = radial ? 1 : 0;
+    hi[q] = radial ? (atomic ? na : nm) : (atomic ? la : lm);
+  }
+  const int w = rank == 5 ? 21 : 27;
+  const int c_la = 4 * P + 2, c_lm = c_la + (rank == 5 ? 1 : 2), nlm = rank == 5 ? 2 : 3;
+  std::vector<int> group;
+  bool ok = true;
+  odometer(nd, lo.data(), hi.data(), [&](const int* v) {
+    const int* n = v;              // n1..nP
+    const int* np = v + P;         // n0'..nP'
+    const int* l = v + 2 * P + 1;  // l1..lP
+    const int* lp = v + 3 * P + 1; // l0'..lP'
+    long ka[6], nc[6];
+    for (int q = 0; q < P; ++q) {
+      ka[q] = static_cast<long>(na) * l[q] + n[q];
+      nc[q] = base + (kmm + 1) * ka[q] + static_cast<long>(nm) * lp[q + 1] + np[q + 1];
+      if (q > 0 && nc[q] > nc[q - 1]) return;
+    }
+    for (int q = 1; q < P; ++q)
+      if (ka[q] > ka[q - 1]) ok = false;
+    const Couplings ca = couplings(P, n, l), cm = couplings(P + 1, np, lp);
+    if (!ca.basis || !cm.basis) return;
+    const int numa = static_cast<int>(ca.v.size()), numm = static_cast<int>(cm.v.size());
+    const int num = std::max(numa, numm);
+    for (int k = 0; k < num; ++k) {
+      std::vector<int> r(w, 0);
+      if (k < numa) {
+        for (int q = 0; q < P; ++q) {
+          r[q] = n[q];
+          r[2 * P + 1 + q] = l[q];
+        }
+        for (int q = 0; q < nlm - 1; ++q) r[c_la + q] = ca.v[k][q];
+      }
+      if (k < numm) {
+        for (int q = 0; q <= P; ++q) {
+          r[P + q] = np[q];
+          r[3 * P + 1 + q] = lp[q];
+        }
+        for (int q = 0; q < nlm; ++q) r[c_lm + q] = cm.v[k][q];
+      }
+      rows.push_back(std::move(r));
+      group.push_back(k == 0 ? num : 0);
+    }
+  });
+  if (rank == 5) {
+    reorder_couplings(rows, 0, group, c_lm, 2);
+  } else {
+    reorder_couplings(rows, 0, group, c_la, 2);
+    reorder_couplings(rows, 0, group, c_lm, 3);
+  }
+  return ok;
+}
+
 // ---------------------------------------------------------------------------
 // Gather-table construction. Every product term kappa * A0 * X1 * ... of the
 // density becomes one entry of the A0 slot it contains (all m), and one entry
@@ -352,11 +518,11 @@ void enumerate(const BasisDims& d, std::vector<std::vector<int>>* rows) {
 struct TermSink {
   const FactorLayout& L;
   int nd;
-  std::vector<std::vector<Entry>> by_slot[4];  // [arity] -> slot -> entries
+  std::vector<std::vector<Entry>> by_slot[kMaxArity + 1];  // [arity] -> slot -> entries
   int nslot;
   explicit TermSink(const FactorLayout& l, int ndens) : L(l), nd(ndens) {
     nslot = l.n2m * l.ls2 + l.nWA + (l.offW0 - l.offW2);
-    for (int a = 1; a <= 3; ++a) by_slot[a].resize(nslot);
+    for (int a = 1; a <= kMaxArity; ++a) by_slot[a].resize(nslot);
   }
   int g0_slot(int a0_factor) const { return a0_factor - L.offA0; }
   int w_slot(int weight_index) const { return L.n2m * L.ls2 + weight_index; }  // WA and W2 only
@@ -365,17 +531,17 @@ struct TermSink {
     Entry e;
     e.kappa[0] = k[0];
     e.kappa[1] = nd > 1 ? k[1] : 0.0;
-    for (int q = 0; q < 3; ++q) e.o[q] = static_cast<uint16_t>(q < arity ? others[q] : L.offOne);
+    for (int q = 0; q < kMaxArity; ++q) e.o[q] = static_cast<uint16_t>(q < arity ? others[q] : L.offOne);
     by_slot[arity][slot].push_back(e);
   }
 };
 
-// Visits every m-term of the 2-, 3- (when with_b3) and 4-body clusters in
-// enumeration order as fn(rank, cluster, cf, f, w): cf is the coupling (the
-// product of Clebsch-Gordan coefficients), f[0] the A0 factor and f[1 ..
-// rank-1] the A2 (rank 2) or A factors, w[q] the weight index of factor q
-// (-1 where it has none: m' < 0; w[0] is unused). Terms with cf == 0 are
-// skipped.
+// Visits every m-term of the 2-, 3- (when with_b3), 4-, 5- and 6-body
+// clusters in enumeration order as fn(rank, cluster, cf, f, w): cf is the
+// coupling (the product of Clebsch-Gordan coefficients), f[0] the A0 factor
+// and f[1 .. rank-1] the A2 (rank 2) or A factors, w[q] the weight index of
+// factor q (-1 where it has none: m' < 0; w[0] is unused); f and w have six
+// entries, padded with ONE and -1. Terms with cf == 0 are skipped.
 template <class Fn>
 void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
   const FactorLayout& L = M.L;
@@ -386,8 +552,8 @@ void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
     for (int m = -l; m <= l; ++m) {
       const double cf = clebsch_gordan(l, l, 0, m, -m, 0);
       if (cf == 0.0) continue;
-      const int f[4] = {L.A0(n0, l, m), L.A2(n1, n1p, l, -m), L.offOne, L.offOne};
-      const int w[4] = {-1, -m >= 0 ? L.W2(n1, n1p, l, -m) : -1, -1, -1};
+      const int f[6] = {L.A0(n0, l, m), L.A2(n1, n1p, l, -m), L.offOne, L.offOne, L.offOne, L.offOne};
+      const int w[6] = {-1, -m >= 0 ? L.W2(n1, n1p, l, -m) : -1, -1, -1, -1, -1};
       fn(2, c, cf, f, w);
     }
   }
@@ -407,8 +573,9 @@ void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
           const double cfm = clebsch_gordan(q0, q1, q2, u0, u1, -u2) * clebsch_gordan(q2, q2, 0, u2, -u2, 0);
           const double cf = cfa * cfm;
           if (cf == 0.0) continue;
-          const int f[4] = {L.A0(p0, q0, u0), L.A(n1, l1, m1, p1, q1, u1), L.A(n2, l1, -m1, p2, q2, u2), L.offOne};
-          const int w[4] = {-1, L.WA(n1, l1, m1, p1, q1, u1), L.WA(n2, l1, -m1, p2, q2, u2), -1};
+          const int f[6] = {L.A0(p0, q0, u0), L.A(n1, l1, m1, p1, q1, u1), L.A(n2, l1, -m1, p2, q2, u2),
+                            L.offOne, L.offOne, L.offOne};
+          const int w[6] = {-1, L.WA(n1, l1, m1, p1, q1, u1), L.WA(n2, l1, -m1, p2, q2, u2), -1, -1, -1};
           fn(3, c, cf, f, w);
         }
     }
@@ -438,14 +605,115 @@ void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
                                  clebsch_gordan(Lc, Lc, 0, Mc, -Mc, 0);
               const double cf = cfa * cfm;
               if (cf == 0.0) continue;
-              const int f[4] = {L.A0(p0, q0, u0), L.A(n1, l1, m1, p1, q1, u1), L.A(n2, l2, m2, p2, q2, u2),
-                                L.A(n3, l3, m3, p3, q3, u3)};
-              const int w[4] = {-1, L.WA(n1, l1, m1, p1, q1, u1), L.WA(n2, l2, m2, p2, q2, u2),
-                                L.WA(n3, l3, m3, p3, q3, u3)};
+              const int f[6] = {L.A0(p0, q0, u0), L.A(n1, l1, m1, p1, q1, u1), L.A(n2, l2, m2, p2, q2, u2),
+                                L.A(n3, l3, m3, p3, q3, u3), L.offOne, L.offOne};
+              const int w[6] = {-1, L.WA(n1, l1, m1, p1, q1, u1), L.WA(n2, l2, m2, p2, q2, u2),
+                                L.WA(n3, l3, m3, p3, q3, u3), -1, -1};
               fn(4, c, cf, f, w);
             }
           }
       }
+  }
+  // 5- and 6-body: A0 A(1) .. A(P), P = rank - 1, with the generalized
+  // couplings cg04 / cg05 (src/b_basis.F90:310-532, src/util.F90:4389-4546):
+  //   atomic  5-body cg<l1 m1 l2 m2|L M12> cg<l3 m3 l4 m4|L -M12> cg<L M12 L -M12|00>
+  //           6-body cg<l1 m1 l2 m2|L12 M12> cg<l3 m3 l4 m4|L34 M34>
+  //                  cg<L12 M12 L34 M34|l5 -m5> cg<l5 -m5 l5 m5|00>
+  //   magnetic 5-body cg<l0' m0' l1' m1'|L01 M01> cg<l2' m2' l3' m3'|L23 M23>
+  //                  cg<L01 M01 L23 M23|l4' -m4'> cg<l4' -m4' l4' m4'|00>
+  //           6-body cg<..|L01 M01> cg<..|L23 M23> cg<l4' m4' l5' m5'|L45 M45>
+  //                  cg<L01 M01 L23 M23|L45 -M45> cg<L45 -M45 L45 M45|00>
+  // A cluster whose atomic or magnetic indices the enumeration padded with
+  // zeros has no terms: the reference reads its factors at radial index 0,
+  // outside its A basis, so the basis function is undefined there.
+  for (int rank = 5; rank <= 6; ++rank) {
+    const int P = rank - 1;
+    for (size_t c = 0; c < M.rows[rank].size(); ++c) {
+      const auto& r = M.rows[rank][c];
+      const int* n = r.data();               // n1..nP
+      const int* np = r.data() + P;          // n0'..nP'
+      const int* l = r.data() + 2 * P + 1;   // l1..lP
+      const int* lp = r.data() + 3 * P + 1;  // l0'..lP'
+      const int* lint = r.data() + 4 * P + 2;
+      if (n[0] == 0 || np[0] == 0) continue;
+      std::vector<std::pair<std::array<int, 6>, double>> ta, tm;
+      std::array<int, 6> mv{};
+      // atomic m-terms
+      {
+        std::vector<int> lo(P), hi(P);
+        for (int q = 0; q < P; ++q) {
+          lo[q] = -l[q];
+          hi[q] = l[q];
+        }
+        odometer(P, lo.data(), hi.data(), [&](const int* m) {
+          int sum = 0;
+          for (int q = 0; q < P; ++q) sum += m[q];
+          if (sum != 0) return;
+          double cf;
+          const int M12 = m[0] + m[1];
+          if (rank == 5) {
+            const int L = lint[0];
+            if (std::abs(M12) > L) return;
+            cf = clebsch_gordan(l[0], l[1], L, m[0], m[1], M12) * clebsch_gordan(l[2], l[3], L, m[2], m[3], -M12) *
+                 clebsch_gordan(L, L, 0, M12, -M12, 0);
+          } else {
+            const int A = lint[0], B = lint[1], M34 = m[2] + m[3];
+            if (std::abs(M12) > A || std::abs(M34) > B) return;
+            cf = clebsch_gordan(l[0], l[1], A, m[0], m[1], M12) * clebsch_gordan(l[2], l[3], B, m[2], m[3], M34) *
+                 clebsch_gordan(A, B, l[4], M12, M34, -m[4]) * clebsch_gordan(l[4], l[4], 0, -m[4], m[4], 0);
+          }
+          for (int q = 0; q < P; ++q) mv[q] = m[q];
+          ta.push_back({mv, cf});
+        });
+      }
+      // magnetic m-terms
+      {
+        const int* lm = lint + (rank == 5 ? 1 : 2);
+        std::vector<int> lo(P + 1), hi(P + 1);
+        for (int q = 0; q <= P; ++q) {
+          lo[q] = -lp[q];
+          hi[q] = lp[q];
+        }
+        odometer(P + 1, lo.data(), hi.data(), [&](const int* u) {
+          int sum = 0;
+          for (int q = 0; q <= P; ++q) sum += u[q];
+          if (sum != 0) return;
+          const int M01 = u[0] + u[1], M23 = u[2] + u[3];
+          const int A = lm[0], B = lm[1];
+          if (std::abs(M01) > A || std::abs(M23) > B) return;
+          double cf;
+          if (rank == 5) {
+            cf = clebsch_gordan(lp[0], lp[1], A, u[0], u[1], M01) * clebsch_gordan(lp[2], lp[3], B, u[2], u[3], M23) *
+                 clebsch_gordan(A, B, lp[4], M01, M23, -u[4]) * clebsch_gordan(lp[4], lp[4], 0, -u[4], u[4], 0);
+          } else {
+            const int Cc = lm[2], M45 = u[4] + u[5];
+            if (std::abs(M45) > Cc) return;
+            cf = clebsch_gordan(lp[0], lp[1], A, u[0], u[1], M01) * clebsch_gordan(lp[2], lp[3], B, u[2], u[3], M23) *
+                 clebsch_gordan(lp[4], lp[5], Cc, u[4], u[5], M45) * clebsch_gordan(A, B, Cc, M01, M23, -M45) *
+                 clebsch_gordan(Cc, Cc, 0, -M45, M45, 0);
+          }
+          for (int q = 0; q <= P; ++q) mv[q] = u[q];
+          tm.push_back({mv, cf});
+        });
+      }
+      for (const auto& a : ta)
+        for (const auto& b : tm) {
+          const double cf = a.second * b.second;
+          if (cf == 0.0) continue;
+          int f[6], w[6];
+          f[0] = L.A0(np[0] - 1, lp[0], b.first[0]);
+          w[0] = -1;
+          for (int q = 0; q < P; ++q) {
+            f[q + 1] = L.A(n[q] - 1, l[q], a.first[q], np[q + 1] - 1, lp[q + 1], b.first[q + 1]);
+            w[q + 1] = L.WA(n[q] - 1, l[q], a.first[q], np[q + 1] - 1, lp[q + 1], b.first[q + 1]);
+          }
+          for (int q = P + 1; q < 6; ++q) {
+            f[q] = L.offOne;
+            w[q] = -1;
+          }
+          fn(rank, c, cf, f, w);
+        }
+    }
   }
 }
 
@@ -531,7 +799,7 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
   const BasisDims& d = M.pot.dims;
   const int nd = M.ndensity;
   TermSink sink(L, nd);
-  long nterm[5] = {0, 0, 0, 0, 0};
+  long nterm[7] = {0, 0, 0, 0, 0, 0, 0};
   // mirror of every factor: negating all its m gives (-1)^(sum of the m)
   // times the conjugate (A(m1,m2) = (-1)^(m1+m2) conj A(-m1,-m2), likewise
   // A2 and A0)
@@ -575,10 +843,13 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
             if (w >= 0 && m1 < 0) wa_used[w] = 0;
           }
   // density (A0-slot) terms, summed per factor set {A0, sorted others}
-  using G0Key = std::array<int, 5>;  // arity, A0 factor, three others (ONE-padded)
+  using G0Key = std::array<int, 2 + kMaxArity>;  // arity, A0 factor, the others (ONE-padded)
   std::map<G0Key, std::array<double, 2>> g0;
   const auto g0_key = [&](int arity, int a0, const int* o) {
-    G0Key key{arity, a0, L.offOne, L.offOne, L.offOne};
+    G0Key key;
+    key.fill(L.offOne);
+    key[0] = arity;
+    key[1] = a0;
     for (int q = 0; q < arity; ++q) key[2 + q] = o[q];
     std::sort(key.begin() + 2, key.begin() + 2 + arity);
     return key;
@@ -595,14 +866,14 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
     kk[1] += k[1];
     for (int q = 1; q < rank; ++q) {
       if (w[q] < 0 || (rank >= 3 && !wa_used[w[q]])) continue;
-      int others[3], n = 0;
+      int others[kMaxArity], n = 0;
       for (int o = 0; o < rank; ++o)
         if (o != q) others[n++] = f[o];
       sink.add(sink.w_slot(w[q]), k, others, arity);
     }
   });
   if (with_b3)
-    for (int q = 0; q < 5; ++q) M.nterms[q] = nterm[q];
+    for (int q = 0; q < 7; ++q) M.nterms[q] = nterm[q];
   // Density entries folded over mirror pairs. A term's mirror (every m
   // negated) has the conjugate product times s = the product of its factors'
   // signs, so the pair adds (kappa + s kappa') Re(prod) to rho. The member
@@ -614,7 +885,7 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
   for (const auto& kv : g0) {
     const G0Key& key = kv.first;
     const int arity = key[0];
-    int mo[3];
+    int mo[kMaxArity];
     int s = sgn[key[1]];
     for (int q = 0; q < arity; ++q) {
       mo[q] = mir[key[2 + q]];
@@ -624,7 +895,8 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
     const auto emit = [&](const G0Key& at, double k0, double k1) {
       if (k0 == 0.0 && k1 == 0.0) return;
       const double k[2] = {k0, k1};
-      const int others[3] = {at[2], at[3], at[4]};
+      int others[kMaxArity];
+      for (int q = 0; q < kMaxArity; ++q) others[q] = at[2 + q];
       sink.add(sink.g0_slot(at[1]), k, others, arity);
     };
     const auto mit = g0.find(mkey);
@@ -652,7 +924,7 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
   std::vector<Seg> segs;
   for (int s = 0; s < g.nslot; ++s) {
     g.slot_seg_begin[s] = static_cast<int32_t>(segs.size());
-    for (int a = 1; a <= 3; ++a) {
+    for (int a = 1; a <= kMaxArity; ++a) {
       const auto& es = sink.by_slot[a][s];
       g.entries[a] += static_cast<long>(es.size());
       for (size_t e0 = 0; e0 < es.size(); e0 += GatherTable::kSegLen) {
@@ -689,12 +961,16 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
           g.kap[a][0].push_back(en.kappa[0]);
           g.kap[a][1].push_back(en.kappa[1]);
           g.o12[a].push_back(static_cast<uint32_t>(en.o[0]) | (static_cast<uint32_t>(a >= 2 ? en.o[1] : 0) << 16));
-          if (a == 3) g.o3.push_back(en.o[2]);
+          if (a >= 3)
+            g.o34[a].push_back(static_cast<uint32_t>(en.o[2]) | (static_cast<uint32_t>(a >= 4 ? en.o[3] : 0) << 16));
+          if (a == 5) g.o5.push_back(en.o[4]);
         } else {
+          const uint32_t z = static_cast<uint32_t>(L.offZero);
           g.kap[a][0].push_back(0.0);
           g.kap[a][1].push_back(0.0);
-          g.o12[a].push_back(static_cast<uint32_t>(L.offZero) | (static_cast<uint32_t>(L.offZero) << 16));
-          if (a == 3) g.o3.push_back(static_cast<uint16_t>(L.offZero));
+          g.o12[a].push_back(z | (z << 16));
+          if (a >= 3) g.o34[a].push_back(z | (z << 16));
+          if (a == 5) g.o5.push_back(static_cast<uint16_t>(L.offZero));
         }
       }
     i = j;
@@ -891,27 +1167,31 @@ void build_descriptors(Model& M) {
   DescriptorTable& T = M.desc;
   T = DescriptorTable();
   T.n1 = static_cast<int>(M.rows[1].size());
-  const int n2 = static_cast<int>(M.rows[2].size()), n3 = static_cast<int>(M.rows[3].size());
-  T.nB = T.n1 + n2 + n3 + static_cast<int>(M.rows[4].size());
+  int first[7] = {0, 0, 0, 0, 0, 0, 0};  // first cluster of each rank past rank 1
+  T.nB = T.n1;
+  for (int r = 2; r <= 6; ++r) {
+    first[r] = T.nB - T.n1;
+    T.nB += static_cast<int>(M.rows[r].size());
+  }
   for (const auto& r : M.rows[1]) T.rank1_n.push_back(r[0] - 1);
   std::vector<int32_t> count(T.nB - T.n1, 0);
-  std::vector<std::array<int, 5>> terms;  // cluster (0-based past rank 1), factors
+  std::vector<std::array<int, 7>> terms;  // cluster (0-based past rank 1), six factors
   std::vector<double> cfs;
   for_each_term(M, true, [&](int rank, size_t c, double cf, const int* f, const int*) {
-    const int k = static_cast<int>(c) + (rank == 2 ? 0 : (rank == 3 ? n2 : n2 + n3));
+    const int k = static_cast<int>(c) + first[rank];
     ++count[k];
-    terms.push_back({k, f[0], f[1], f[2], f[3]});
+    terms.push_back({k, f[0], f[1], f[2], f[3], f[4], f[5]});
     cfs.push_back(cf);
   });
   T.begin.assign(T.nB - T.n1 + 1, 0);
   for (int k = 0; k < T.nB - T.n1; ++k) T.begin[k + 1] = T.begin[k] + count[k];
   T.cf.assign(cfs.size(), 0.0);
-  T.o.assign(4 * cfs.size(), 0);
+  T.o.assign(kDescFactors * cfs.size(), static_cast<uint16_t>(M.L.offOne));
   std::vector<int32_t> fill(T.begin.begin(), T.begin.end() - 1);
   for (size_t e = 0; e < terms.size(); ++e) {
     const int pos = fill[terms[e][0]]++;
     T.cf[pos] = cfs[e];
-    for (int q = 0; q < 4; ++q) T.o[4 * pos + q] = static_cast<uint16_t>(terms[e][1 + q]);
+    for (int q = 0; q < 6; ++q) T.o[kDescFactors * pos + q] = static_cast<uint16_t>(terms[e][1 + q]);
   }
 }
 
@@ -929,7 +1209,7 @@ int build_tables(Model& M, std::string& msg) {
   if (st) return st;
   // tables of the specialised kernels: 3-body terms as dense per-(combo, m)
   // contractions, everything else through the gather table without them
-  if (M.ndensity == 1) {
+  if (M.ndensity == 1 && !M.high) {
     st = build_gather(M, false, M.gt_nob3, msg, &M.rest);
     if (st) return st;
     build_dense_b3(M);
@@ -997,7 +1277,7 @@ int build_tables(Model& M, std::string& msg) {
 
 int num_coefficients(const Model& M) {
   int n = 0;
-  for (int r = 1; r <= 4; ++r) n += static_cast<int>(M.rows[r].size());
+  for (int r = 1; r <= 6; ++r) n += static_cast<int>(M.rows[r].size());
   return n;
 }
 
@@ -1005,7 +1285,7 @@ void get_coefficients(const Model& M, double* c) {
   const int nB = num_coefficients(M);
   for (int d = 0; d < M.ndensity; ++d) {
     int k = 0;
-    for (int r = 1; r <= 4; ++r)
+    for (int r = 1; r <= 6; ++r)
       for (size_t q = 0; q < M.rows[r].size(); ++q) c[d * nB + k++] = M.coef[r][q][d];
   }
 }
@@ -1014,7 +1294,7 @@ int set_coefficients(Model& M, const double* c, std::string& msg) {
   const int nB = num_coefficients(M);
   for (int d = 0; d < M.ndensity; ++d) {
     int k = 0;
-    for (int r = 1; r <= 4; ++r)
+    for (int r = 1; r <= 6; ++r)
       for (size_t q = 0; q < M.rows[r].size(); ++q) M.coef[r][q][d] = c[d * nB + k++];
   }
   return build_tables(M, msg);
@@ -1026,13 +1306,11 @@ int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& 
   M.cutoff = rcut;
   M.cutoff_m = rcut_magnetic;
   const BasisDims& d = pot.dims;
-  if (d.nradial5_a || d.nradial5_m || d.nradial6_a || d.nradial6_m) {
-    msg = "5- and 6-body clusters are not supported by this build";
-    return MAGACE_ERR_UNSUPPORTED;
-  }
   // limits of src/util.F90:234-272
-  if (d.l3max_a < d.l4max_a || d.l2max_m < d.l3max_m || d.l2max_m < d.l4max_m ||
-      d.nradial3_a < d.nradial4_a || d.nradial2_m < d.nradial3_m || d.nradial2_m < d.nradial4_m ||
+  if (d.l3max_a < d.l4max_a || d.l3max_a < d.l5max_a || d.l3max_a < d.l6max_a || d.l2max_m < d.l3max_m ||
+      d.l2max_m < d.l4max_m || d.l2max_m < d.l5max_m || d.l2max_m < d.l6max_m || d.nradial3_a < d.nradial4_a ||
+      d.nradial3_a < d.nradial5_a || d.nradial3_a < d.nradial6_a || d.nradial2_m < d.nradial3_m ||
+      d.nradial2_m < d.nradial4_m || d.nradial2_m < d.nradial5_m || d.nradial2_m < d.nradial6_m ||
       d.nradial3_a > d.nradbase_a || d.nradial2_m > d.nradbase_m ||
       std::max(d.nradial3_a, d.nradial2_m) > std::max(d.nradbase_a, d.nradbase_m)) {
     msg = "basis dimensions violate the limits of the reference setup";
@@ -1040,6 +1318,27 @@ int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& 
   }
   if (d.nradial2_m == 0 || d.nradial3_a == 0 || d.nradial3_m == 0) {
     msg = "potentials without 2- or 3-body magnetic terms are not supported";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+  // 5- and 6-body factors come from the 3-body A basis, which holds n' <=
+  // nradial3_m and l' <= l3max_m here; the reference evaluates a rank only
+  // when the ranks below it are present (src/b_basis.F90:217-218, :312-313;
+  // without them its packs of the higher ranks stay uninitialised); its
+  // 6-body couplings stop for 2 l6max above l3max / l2max
+  // (src/util.F90:3430-3434)
+  if (d.nradial5_m > d.nradial3_m || d.nradial6_m > d.nradial3_m || d.l5max_m > d.l3max_m ||
+      d.l6max_m > d.l3max_m) {
+    msg = "5- and 6-body magnetic radial functions or l' beyond the 3-body ones are not supported";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+  const bool has4 = d.nradial4_a || d.nradial4_m, has5 = d.nradial5_a || d.nradial5_m,
+             has6 = d.nradial6_a || d.nradial6_m;
+  if ((has5 && !has4) || (has6 && !has5)) {
+    msg = "a rank of clusters without the rank below it is not evaluated by the reference either";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
+  if (has6 && d.nradial6_a && d.nradial6_m && (2 * d.l6max_a > d.l3max_a || 2 * d.l6max_m > d.l2max_m)) {
+    msg = "6-body couplings not worked for lmax > 6 (src/util.F90:3430-3434)";
     return MAGACE_ERR_UNSUPPORTED;
   }
   if (d.nfemb < 0 || d.nfemb > 2) {
@@ -1094,18 +1393,25 @@ int build_model(const Potential& pot, double rcut, double rcut_magnetic, Model& 
   }
 
   enumerate(d, M.rows);
-  // match the file's cluster records (src/util.F90:678-956)
-  std::map<std::vector<int>, size_t> index[5];
-  for (int r = 1; r <= 4; ++r) {
+  for (int rank = 5; rank <= 6; ++rank)
+    if (!enumerate_high(d, rank, M.rows[rank])) {
+      msg = "the atomic basis is not ordered lexicographically (src/util.F90:2884-2889, :3512-3517)";
+      return MAGACE_ERR_FORMAT;
+    }
+  M.high = !M.rows[5].empty() || !M.rows[6].empty();
+  // match the file's cluster records (src/util.F90:678-956); a record sets
+  // every cluster with its index tuple (padded 5-/6-body clusters can share one)
+  std::map<std::vector<int>, std::vector<size_t>> index[7];
+  for (int r = 1; r <= 6; ++r) {
     M.coef[r].assign(M.rows[r].size(), {0.0, 0.0});
-    for (size_t c = 0; c < M.rows[r].size(); ++c) index[r][M.rows[r][c]] = c;
+    for (size_t c = 0; c < M.rows[r].size(); ++c) index[r][M.rows[r][c]].push_back(c);
     for (const auto& kv : pot.clusters[r]) {
       auto it = index[r].find(kv.first);
       if (it == index[r].end()) {
         ++M.unmatched_records;
         continue;
       }
-      M.coef[r][it->second] = kv.second;
+      for (size_t c : it->second) M.coef[r][c] = kv.second;
     }
   }
   {

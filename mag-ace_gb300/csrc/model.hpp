@@ -43,7 +43,7 @@ struct FactorLayout {
 // One gather entry: out_slot accumulates kappa * prod(F[o[k]]), k < arity.
 struct Entry {
   double kappa[2];
-  uint16_t o[3];
+  uint16_t o[kMaxArity];
 };
 
 // Device-ready gather table. Entries are grouped by output slot and cut into
@@ -67,12 +67,12 @@ struct GatherTable {
   int ngroup = 0;
   std::vector<int32_t> grp_arity, grp_len, grp_first;  // [ngroup]
   std::vector<int32_t> grp_seg;         // [ngroup*32], -1 for padding lanes
-  // interleaved entries per arity (index 1..3): kappa per density, packed
-  // factor indices o1 | o2 << 16, and the third index for arity 3
-  std::vector<double> kap[4][2];
-  std::vector<uint32_t> o12[4];
-  std::vector<uint16_t> o3;
-  long entries[4] = {0, 0, 0, 0};       // real (unpadded) entries per arity
+  // interleaved entries per arity (index 1..5): kappa per density, packed
+  // factor indices o1 | o2 << 16, o3 | o4 << 16 (arity >= 3) and o5 (arity 5)
+  std::vector<double> kap[kMaxArity + 1][2];
+  std::vector<uint32_t> o12[kMaxArity + 1], o34[kMaxArity + 1];
+  std::vector<uint16_t> o5;
+  long entries[kMaxArity + 1] = {0, 0, 0, 0, 0, 0};  // real (unpadded) entries per arity
   // slot -> factor/weight index and multiplicity
   std::vector<int32_t> slot_factor;  // for G0 slots: A0 factor index
   std::vector<int32_t> slot_weight;  // weight index (or -1 when the slot stores no weight)
@@ -116,15 +116,15 @@ struct DenseB3 {
 
 // Per-cluster m-terms of the descriptors B_k, the basis functions that the
 // expansion coefficients multiply (rho_d = sum_k c[d][k] B_k): for clusters
-// of rank 2..4, B = Re sum_e cf_e F[o0] F[o1] F[o2] F[o3] with missing factors
-// ONE; for rank 1, B = g_n(|m_i|) - 1. Clusters are in coefficient order
-// (the file's record order, ranks 1..4).
+// of rank 2..6, B = Re sum_e cf_e F[o0] .. F[o5] with missing factors ONE;
+// for rank 1, B = g_n(|m_i|) - 1. Clusters are in coefficient order (the
+// file's record order, ranks 1..6).
 struct DescriptorTable {
   int n1 = 0, nB = 0;            // rank-1 clusters; all clusters
   std::vector<int32_t> rank1_n;  // [n1] magnetic radial function of each rank-1 cluster
   std::vector<int32_t> begin;    // [nB - n1 + 1] first term of cluster n1 + k
   std::vector<double> cf;        // [terms] coupling
-  std::vector<uint16_t> o;       // [terms][4] factor indices
+  std::vector<uint16_t> o;       // [terms][kDescFactors] factor indices
 };
 
 // The 2- and 4-body terms per output slot, for the split-precision kernel
@@ -170,11 +170,12 @@ struct Model {
   double par[2][2] = {{1, 1}, {1, 1}};
   double ecut = 0, decut = 0;
   double core_pre = 0, core_lambda = 0;
-  // enumerated clusters in file layout, rank 1..4, with coefficients
-  std::vector<std::vector<int>> rows[5];
-  std::vector<std::array<double, 2>> coef[5];
+  // enumerated clusters in file layout, rank 1..6, with coefficients
+  std::vector<std::vector<int>> rows[7];
+  std::vector<std::array<double, 2>> coef[7];
   int unmatched_records = 0;
-  long nterms[5] = {0, 0, 0, 0, 0};
+  long nterms[7] = {0, 0, 0, 0, 0, 0, 0};
+  bool high = false;  // 5- or 6-body clusters: only the generic kernels and tables
   std::vector<double> c1[2];  // 1-body coefficient per magnetic radial function n
   GatherTable gt;        // every term (generic kernels)
   GatherTable gt_nob3;   // every term except the 3-body ones (specialised kernels)

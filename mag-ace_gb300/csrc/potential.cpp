@@ -169,7 +169,7 @@ int read_potential(const std::string& path, const std::string& element, const st
     for (int nr = 1; nr <= d.nradial2_m; ++nr) cm(nr, nr, l) = 1.0;
 
   // typed records (src/util.F90:669-1106)
-  const size_t width[5] = {0, 1, 4, 9, 15};
+  const size_t width[7] = {0, 1, 4, 9, 15, 21, 27};
   while (rec.take(3, it)) {
     const std::string type = it[0];
     int order = 0, dens = 0;
@@ -177,10 +177,6 @@ int read_potential(const std::string& path, const std::string& element, const st
     ++pot.records_read;
     if (type == "clu") {
       if (order < 1 || order > 6) return fail("cluster order out of range");
-      if (order > 4) {  // 5/6-body records: header dims must have disabled them
-        if (!rec.skip_line()) break;
-        continue;
-      }
       const size_t nitem = order + width[order] + 2;
       if (!rec.take(nitem, it)) break;
       for (int q = 0; q < order; ++q)

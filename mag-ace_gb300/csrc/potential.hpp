@@ -26,7 +26,8 @@ struct BasisDims {
 };
 
 // A cluster record key: the integer index tuple of one 'clu' data line
-// (rank 1: n0'; rank 2: n0',n1',n1,l0'; rank 3: 9 ints; rank 4: 15 ints).
+// (rank 1: n0'; rank 2: n0',n1',n1,l0'; rank 3: 9 ints; rank 4: 15 ints;
+// rank 5: 21 ints; rank 6: 27 ints).
 typedef std::vector<int> ClusterKey;
 
 struct Potential {
@@ -45,7 +46,7 @@ struct Potential {
   double par[2][2] = {{1.0, 1.0}, {1.0, 1.0}};  // par[order-1][density-1]
 
   // cluster coefficients as read: rank -> key -> per-density value
-  std::map<ClusterKey, std::array<double, 2>> clusters[5];
+  std::map<ClusterKey, std::array<double, 2>> clusters[7];
   int records_read = 0;
 };
 

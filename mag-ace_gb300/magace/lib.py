@@ -38,6 +38,7 @@ SIGNATURES = {
     "ace_get_precision": (_i, []),
     "ace_basis_sizes": (_i, [_pi]),
     "ace_basis_rows": (_i, [_i, _pi]),
+    "ace_basis_count": (_i, [_i, _pi]),
     "ace_compute_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ace_device_status": (_i, []),
     "ace_last_launch_count": (_i, []),
@@ -120,9 +121,17 @@ def basis_sizes() -> dict:
             "nterms4": int(out[6]), "unmatched": int(out[7])}
 
 
+def basis_count(rank: int) -> int:
+    """Number of clusters of rank 1..6 of the loaded potential."""
+    n = ctypes.c_int()
+    _check(load().ace_basis_count(rank, ctypes.byref(n)))
+    return n.value
+
+
 def basis_rows(rank: int) -> np.ndarray:
-    width = {1: 1, 2: 4, 3: 9, 4: 15}[rank]
-    n = basis_sizes()["nvar"][rank - 1]
+    """Cluster index rows of rank 1..6 as in the file's 'clu' records."""
+    width = {1: 1, 2: 4, 3: 9, 4: 15, 5: 21, 6: 27}[rank]
+    n = basis_count(rank)
     out = np.zeros(max(1, n * width), dtype=np.int32)
     _check(load().ace_basis_rows(rank, _ip(out)))
     return out[: n * width].reshape(n, width)

@@ -20,6 +20,8 @@ import numpy as np
 
 from . import lib
 
+RANKS = (1, 2, 3, 4, 5, 6)  # cluster ranks of the 'clu' records (1 to 6 bodies)
+
 FE_LAYOUT = dict(nradbase_a=16, nradbase_m=16, nradial2_m=5, l2max_m=2,
                  nradial3_a=4, nradial3_m=3, l3max_a=1, l3max_m=2,
                  nradial4_a=3, nradial4_m=3, l4max_a=0, l4max_m=0,
@@ -33,6 +35,17 @@ ALT_LAYOUT = dict(nradbase_a=8, nradbase_m=6, nradial2_m=3, l2max_m=2,
                   nradial3_a=3, nradial3_m=2, l3max_a=2, l3max_m=1,
                   nradial4_a=2, nradial4_m=2, l4max_a=1, l4max_m=1,
                   ndensity=2, npot=5, nfemb=2, radtype_a=5, radtype_m=3)
+
+# A layout with 5- and 6-body clusters (src/b_basis.F90:310-532), small
+# enough for the oracle: 5-body with atomic l <= 1 and magnetic l' <= 1,
+# 6-body with atomic l = 0 and magnetic l' <= 1, one density, radial types
+# 4 (atomic) and 8 (magnetic).
+HIGH_LAYOUT = dict(nradbase_a=6, nradbase_m=6, nradial2_m=2, l2max_m=2,
+                   nradial3_a=2, nradial3_m=2, l3max_a=1, l3max_m=1,
+                   nradial4_a=2, nradial4_m=1, l4max_a=1, l4max_m=1,
+                   nradial5_a=1, nradial5_m=1, l5max_a=1, l5max_m=1,
+                   nradial6_a=1, nradial6_m=1, l6max_a=0, l6max_m=1,
+                   ndensity=1, npot=5, nfemb=1, radtype_a=4, radtype_m=8)
 
 
 def header_lines(element: str, xc: str, smearing: float, lam=(5.25, 5.25), cut=(5.0, 4.0),
@@ -49,8 +62,8 @@ def header_lines(element: str, xc: str, smearing: float, lam=(5.25, 5.25), cut=(
         f" nradbase l2max   {L['nradbase_a']} {L['nradbase_m']} {L['nradial2_m']} {L['l2max_m']}",
         f" nradial3 l3max   {L['nradial3_a']} {L['nradial3_m']} {L['l3max_a']} {L['l3max_m']}",
         f" nradial4 l4max   {L['nradial4_a']} {L['nradial4_m']} {L['l4max_a']} {L['l4max_m']}",
-        " nradial5 l5max   0 0 0 0",
-        " nradial6 l6max   0 0 0 0",
+        f" nradial5 l5max   {L.get('nradial5_a', 0)} {L.get('nradial5_m', 0)} {L.get('l5max_a', 0)} {L.get('l5max_m', 0)}",
+        f" nradial6 l6max   {L.get('nradial6_a', 0)} {L.get('nradial6_m', 0)} {L.get('l6max_a', 0)} {L.get('l6max_m', 0)}",
         f" ndensity   {L['ndensity']}",
         f" npot-nfemb-radtype   {L['npot']} {L['nfemb']} {L['radtype_a']} {L['radtype_m']}",
     ]
@@ -61,7 +74,7 @@ def library_basis_rows(header: str, element: str, rcut: float, rcut_magnetic: fl
     """The cluster rows of ranks 1..4 that the library enumerates for the
     potential file `header` (its host-only init; no GPU)."""
     lib.init(header, element, rcut, rcut_magnetic, smearing, xcnumber)
-    return {r: lib.basis_rows(r) for r in (1, 2, 3, 4)}
+    return {r: lib.basis_rows(r) for r in RANKS}
 
 
 def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, element: str = "Fe",
@@ -101,17 +114,17 @@ def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, elem
             for n in range(1, L["nradbase_m"] + 1):
                 out += [" rad_magnetic            0           0",
                         f" {element} {element}  {n} {nr} {l} {rng.normal(0.0, sigma)!r} T"]
-    for rank in (1, 2, 3, 4):
+    for rank in RANKS:
         els = " ".join([element] * rank)
-        for row in rows[rank]:
+        for row in rows.get(rank, ()):
             idx = " ".join(str(int(x)) for x in row)
             out += [f" clu            {rank}           1",
                     f" {els}   {idx}   {rng.normal(0.0, sigma)!r}   T"]
     if L["ndensity"] == 2:
         rng2 = np.random.default_rng(seed + 1)
-        for rank in (1, 2, 3, 4):
+        for rank in RANKS:
             els = " ".join([element] * rank)
-            for row in rows[rank]:
+            for row in rows.get(rank, ()):
                 idx = " ".join(str(int(x)) for x in row)
                 out += [f" clu            {rank}           2",
                         f" {els}   {idx}   {rng2.normal(0.0, sigma)!r}   T"]
@@ -120,20 +133,20 @@ def write_seeded_potential(path: str, seed: int = 2024, sigma: float = 0.1, elem
     return path
 
 
-_WIDTH = {1: 1, 2: 4, 3: 9, 4: 15}
+_WIDTH = {1: 1, 2: 4, 3: 9, 4: 15, 5: 21, 6: 27}
 
 
 def write_coefficients(src: str, dst: str, coefs, rows: dict, element: str = "Fe") -> str:
     """Copies the potential file `src` to `dst` with new expansion
     coefficients: coefs[d][k] for the clusters rows[1..4] in coefficient
-    order (ace_basis_rows, the library's order). The value of every 'clu'
-    record (src/util.F90:678-956) is replaced; clusters without a record in
+    order (ace_basis_rows, the library's order; ranks 1..6). The value of
+    every 'clu' record (src/util.F90:678-956) is replaced; clusters without a record in
     `src` and with a nonzero coefficient get one appended. Everything else is
     copied unchanged. Returns dst."""
     coefs = np.atleast_2d(np.asarray(coefs, dtype=np.float64))
     index, k = {}, 0
-    for rank in (1, 2, 3, 4):
-        for row in rows[rank]:
+    for rank in RANKS:
+        for row in rows.get(rank, ()):
             index[(rank, tuple(int(x) for x in row))] = k
             k += 1
     if coefs.shape[1] != k:

@@ -67,12 +67,27 @@ struct OracleState {
   FArr<int> b4lindex_atomic, b4occ, b4index, b4nint, b4map_atomic, b4map_magnetic;
   FArr<int> b4lindex_magnetic, madd4_atomic, madd4_magnetic, b4lm_atomic, b4lm_magnetic;
 
+  // 5- and 6-body clusters (src/util.F90:2817-3760): the index rows of the
+  // 'clu' records (b5index 21 ints, b6index 27 ints), and per cluster the
+  // m-terms of its atomic and of its magnetic part with their generalized
+  // couplings (cg04/cg05, src/util.F90:4389-4546). The reference shares
+  // these lists between the clusters of one angular part (b5map, b5lm,
+  // madd5); each cluster holds its own copy here. A cluster whose atomic or
+  // magnetic half the enumeration padded with zeros has empty lists.
+  struct MTerm {
+    int m[6];
+    double cf;
+  };
+  int nvar5 = 0, nvar6 = 0;
+  FArr<int> b5index, b6index;
+  std::vector<std::vector<MTerm>> b5mt_atomic, b5mt_magnetic, b6mt_atomic, b6mt_magnetic;
+
   // generalized couplings (src/util.F90:4256-4388)
   FArr<double> cg01_magnetic, cg02_atomic, cg02_magnetic, cg03_atomic, cg03_magnetic;
 
   // expansion coefficients and radial parameters (src/util.F90:281-350, 667-1106)
   FArr<double> crad_atomic, crad_magnetic, corepara, p1;
-  FArr<double> c0, c2, c3, c4;
+  FArr<double> c0, c2, c3, c4, c5, c6;
 
   // lookup tables (src/radial.F90:164-426)
   int nlut = 0;

@@ -83,9 +83,9 @@ class Oracle:
         self.lib = _load(fast)
         self._key = (potfile, element, rcut, rcut_magnetic, smear, xcnumber)
         self._activate(force=True)
-        sz = np.zeros(8, dtype=np.int32)
+        sz = np.zeros(9, dtype=np.int32)
         self.lib.oracle_basis_sizes(_ip(sz))
-        self.nvar = tuple(int(x) for x in sz[:4])
+        self.nvar = tuple(int(x) for x in sz[:4]) + (int(sz[7]), int(sz[8]))
         self.nterms3, self.nterms4, self.nterms2 = int(sz[4]), int(sz[5]), int(sz[6])
 
     def _activate(self, force: bool = False) -> None:
@@ -100,7 +100,7 @@ class Oracle:
 
     def basis_rows(self, rank: int) -> np.ndarray:
         self._activate()
-        width = {1: 1, 2: 4, 3: 9, 4: 15}[rank]
+        width = {1: 1, 2: 4, 3: 9, 4: 15, 5: 21, 6: 27}[rank]
         n = self.nvar[rank - 1]
         out = np.zeros(max(1, n) * width, dtype=np.int32)
         st = self.lib.oracle_basis_rows(rank, _ip(out))
@@ -128,9 +128,9 @@ class Oracle:
         return eout, flist, tlist, tlist0
 
     def descriptors(self, nb):
-        """(B [natom, nvar1+..+nvar4], dE/drho [natom, 2]) of every atom."""
+        """(B [natom, nvar1+..+nvar6], dE/drho [natom, 2]) of every atom."""
         self._activate()
-        nB = sum(self.nvar[:4])
+        nB = sum(self.nvar)
         B = np.zeros((max(1, nb.natom), nB))
         dedrho = np.zeros((max(1, nb.natom), 2))
         st = self.lib.oracle_descriptors(nb.natom, nb.nei, _ip(nb.nstart), _ip(nb.nstop), _dp(nb.dlist),

@@ -275,8 +275,8 @@ struct Chunk {
   FArr<cplx> shpack_magnetic_0, gradshpack_magnetic_0;
   FArr<cplx> abasepack, abase2pack, abase2pack_magnetic;
   FArr<double> abase2hcpack;
-  FArr<double> b1pack, b2pack, b2hcpack, b3pack, b4pack;
-  FArr<cplx> db2pack, db2pack_0, db3pack, db3pack_0, db4pack, db4pack_0;
+  FArr<double> b1pack, b2pack, b2hcpack, b3pack, b4pack, b5pack, b6pack;
+  FArr<cplx> db2pack, db2pack_0, db3pack, db3pack_0, db4pack, db4pack_0, db5pack, db5pack_0, db6pack, db6pack_0;
   FArr<double> wf1;
   FArr<cplx> wf2, wf, wf_0;
   std::vector<double> eicalc, edfcut, rho_out, dEdrho_out;
@@ -324,6 +324,13 @@ struct Chunk {
     db3pack_0.init({{-l3m, l3m}, {1, std::max(1, s.nvar3)}, {1, A}});
     db4pack.init({{1, 3}, {-l4a, l4a}, {-l4m, l4m}, {1, std::max(1, s.nvar4)}, {1, A}});
     db4pack_0.init({{-l4m, l4m}, {1, std::max(1, s.nvar4)}, {1, A}});
+    const int l5a = s.l5max_atomic, l5m = s.l5max_magnetic, l6a = s.l6max_atomic, l6m = s.l6max_magnetic;
+    b5pack.init({{1, std::max(1, s.nvar5)}, {1, A}});
+    b6pack.init({{1, std::max(1, s.nvar6)}, {1, A}});
+    db5pack.init({{1, 4}, {-l5a, l5a}, {-l5m, l5m}, {1, std::max(1, s.nvar5)}, {1, A}});
+    db5pack_0.init({{-l5m, l5m}, {1, std::max(1, s.nvar5)}, {1, A}});
+    db6pack.init({{1, 5}, {-l6a, l6a}, {-l6m, l6m}, {1, std::max(1, s.nvar6)}, {1, A}});
+    db6pack_0.init({{-l6m, l6m}, {1, std::max(1, s.nvar6)}, {1, A}});
     wf1.init({{1, nbm}, {1, A}});
     wf2.init({{1, nba}, {0, l2m}, {0, l2m}, {1, n2m}, {1, A}});
     wf.init({{-l3a, l3a}, {0, l3a}, {1, std::max(1, n3a)}, {0, l3m}, {0, l3m}, {1, std::max(1, n3m)}, {1, A}});
@@ -641,6 +648,101 @@ void prepB(const OracleState& s, Chunk& ch) {
       ch.b4pack(nclu, la) = xiy.real();
     }
   }
+
+  // 5-body (src/b_basis.F90:310-409). A cluster whose atomic or magnetic half
+  // the enumeration padded with zeros has no m-terms here: the reference
+  // reads its factors at radial index 0, outside abasepack.
+  if (s.nradial5_atomic == 0 && s.nradial5_magnetic == 0) return;
+  {
+    const int l5a = s.l5max_atomic, l5m = s.l5max_magnetic;
+    for (int la = 1; la <= ch.na; ++la) {
+      for (int nclu = 1; nclu <= s.nvar5; ++nclu) {
+        for (int q = 1; q <= 4; ++q)
+          for (int mm = -l5m; mm <= l5m; ++mm)
+            for (int ma = -l5a; ma <= l5a; ++ma) ch.db5pack(q, ma, mm, nclu, la) = cplx(0, 0);
+        for (int m = -l5m; m <= l5m; ++m) ch.db5pack_0(m, nclu, la) = cplx(0, 0);
+      }
+      for (int nclu = 1; nclu <= s.nvar5; ++nclu) {
+        int nr[10], l[10];
+        for (int q = 0; q < 9; ++q) {
+          nr[q] = s.b5index(q + 1, nclu);
+          l[q] = s.b5index(q + 10, nclu);
+        }
+        // nr/l: [0..3] n1..n4 / l1..l4, [4] n0' / l0', [5..8] n1'..n4' / l1'..l4'
+        cplx xiy(0, 0);
+        for (const auto& ta : s.b5mt_atomic[nclu - 1]) {
+          const int m1 = ta.m[0], m2 = ta.m[1], m3 = ta.m[2], m4 = ta.m[3];
+          const int k1 = sha(l[0], m1), k2 = sha(l[1], m2), k3 = sha(l[2], m3), k4 = sha(l[3], m4);
+          for (const auto& tm : s.b5mt_magnetic[nclu - 1]) {
+            const int m5 = tm.m[0], m6 = tm.m[1], m7 = tm.m[2], m8 = tm.m[3], m9 = tm.m[4];
+            const cplx ap0 = ch.abase2pack_magnetic(nr[4], shm(l[4], m5), la);
+            const cplx ap1 = ch.abasepack(nr[0], k1, nr[5], shm(l[5], m6), la);
+            const cplx ap2 = ch.abasepack(nr[1], k2, nr[6], shm(l[6], m7), la);
+            const cplx ap3 = ch.abasepack(nr[2], k3, nr[7], shm(l[7], m8), la);
+            const cplx ap4 = ch.abasepack(nr[3], k4, nr[8], shm(l[8], m9), la);
+            const double cf = ta.cf * tm.cf;
+            const cplx xb1 = ap0 * cf * ap1 * ap2;
+            const cplx xb2 = ap3 * ap4;
+            xiy += xb1 * xb2;
+            ch.db5pack(1, m1, m6, nclu, la) += ap0 * cf * ap2 * xb2;
+            ch.db5pack(2, m2, m7, nclu, la) += ap0 * cf * ap1 * xb2;
+            ch.db5pack(3, m3, m8, nclu, la) += xb1 * ap4;
+            ch.db5pack(4, m4, m9, nclu, la) += xb1 * ap3;
+            ch.db5pack_0(m5, nclu, la) += cf * ap1 * ap2 * xb2;
+          }
+        }
+        ch.b5pack(nclu, la) = xiy.real();
+      }
+    }
+  }
+
+  // 6-body (src/b_basis.F90:412-532)
+  if (s.nradial6_atomic == 0 && s.nradial6_magnetic == 0) return;
+  {
+    const int l6a = s.l6max_atomic, l6m = s.l6max_magnetic;
+    for (int la = 1; la <= ch.na; ++la) {
+      for (int nclu = 1; nclu <= s.nvar6; ++nclu) {
+        for (int q = 1; q <= 5; ++q)
+          for (int mm = -l6m; mm <= l6m; ++mm)
+            for (int ma = -l6a; ma <= l6a; ++ma) ch.db6pack(q, ma, mm, nclu, la) = cplx(0, 0);
+        for (int m = -l6m; m <= l6m; ++m) ch.db6pack_0(m, nclu, la) = cplx(0, 0);
+      }
+      for (int nclu = 1; nclu <= s.nvar6; ++nclu) {
+        int nr[11], l[11];
+        for (int q = 0; q < 11; ++q) {
+          nr[q] = s.b6index(q + 1, nclu);
+          l[q] = s.b6index(q + 12, nclu);
+        }
+        // nr/l: [0..4] n1..n5 / l1..l5, [5] n0' / l0', [6..10] n1'..n5' / l1'..l5'
+        cplx xiy(0, 0);
+        for (const auto& ta : s.b6mt_atomic[nclu - 1]) {
+          const int m1 = ta.m[0], m2 = ta.m[1], m3 = ta.m[2], m4 = ta.m[3], m5 = ta.m[4];
+          const int k1 = sha(l[0], m1), k2 = sha(l[1], m2), k3 = sha(l[2], m3), k4 = sha(l[3], m4),
+                    k5 = sha(l[4], m5);
+          for (const auto& tm : s.b6mt_magnetic[nclu - 1]) {
+            const int m6 = tm.m[0], m7 = tm.m[1], m8 = tm.m[2], m9 = tm.m[3], m10 = tm.m[4], m11 = tm.m[5];
+            const cplx ap0 = ch.abase2pack_magnetic(nr[5], shm(l[5], m6), la);
+            const cplx ap1 = ch.abasepack(nr[0], k1, nr[6], shm(l[6], m7), la);
+            const cplx ap2 = ch.abasepack(nr[1], k2, nr[7], shm(l[7], m8), la);
+            const cplx ap3 = ch.abasepack(nr[2], k3, nr[8], shm(l[8], m9), la);
+            const cplx ap4 = ch.abasepack(nr[3], k4, nr[9], shm(l[9], m10), la);
+            const cplx ap5 = ch.abasepack(nr[4], k5, nr[10], shm(l[10], m11), la);
+            const double cf = ta.cf * tm.cf;
+            const cplx xb1 = ap0 * cf * ap1 * ap2;
+            const cplx xb2 = ap3 * ap4 * ap5;
+            xiy += xb1 * xb2;
+            ch.db6pack(1, m1, m7, nclu, la) += ap0 * cf * ap2 * xb2;
+            ch.db6pack(2, m2, m8, nclu, la) += ap0 * cf * ap1 * xb2;
+            ch.db6pack(3, m3, m9, nclu, la) += xb1 * ap4 * ap5;
+            ch.db6pack(4, m4, m10, nclu, la) += xb1 * ap3 * ap5;
+            ch.db6pack(5, m5, m11, nclu, la) += xb1 * ap3 * ap4;
+            ch.db6pack_0(m6, nclu, la) += cf * ap1 * ap2 * xb2;
+          }
+        }
+        ch.b6pack(nclu, la) = xiy.real();
+      }
+    }
+  }
 }
 
 // src/forces.F90:5-362 with calcenergyatom (:1093-1130) and expansionvariables (:976-1048)
@@ -674,6 +776,19 @@ void forceweights(const OracleState& s, Chunk& ch) {
       for (int d = 1; d <= nd; ++d) {
         double x = 0;
         for (int n = 1; n <= s.nvar4; ++n) x += s.c4(n, d) * ch.b4pack(n, la);
+        rho[d - 1] += x;
+      }
+    // src/forces.F90:1030-1046
+    if (s.nradial5_atomic > 0 || s.nradial5_magnetic > 0)
+      for (int d = 1; d <= nd; ++d) {
+        double x = 0;
+        for (int n = 1; n <= s.nvar5; ++n) x += s.c5(n, d) * ch.b5pack(n, la);
+        rho[d - 1] += x;
+      }
+    if (s.nradial6_atomic > 0 || s.nradial6_magnetic > 0)
+      for (int d = 1; d <= nd; ++d) {
+        double x = 0;
+        for (int n = 1; n <= s.nvar6; ++n) x += s.c6(n, d) * ch.b6pack(n, la);
         rho[d - 1] += x;
       }
     // embedding
@@ -751,6 +866,31 @@ void forceweights(const OracleState& s, Chunk& ch) {
       for (int m3 = -l3; m3 <= l3; ++m3)
         for (int m7 = 0; m7 <= l7; ++m7) ch.wf(m3, l3, nr3, m7, l7, nr7, la) += c * ch.db4pack(3, m3, m7, n, la);
       for (int m4 = 0; m4 <= l4; ++m4) ch.wf_0(m4, l4, nr4, la) += c * ch.db4pack_0(m4, n, la);
+    }
+    // 5-body (src/forces.F90:234-277); padded clusters have no gradient
+    for (int n = 1; n <= s.nvar5; ++n) {
+      if (s.b5mt_atomic[n - 1].empty() || s.b5mt_magnetic[n - 1].empty()) continue;
+      const double c = ceff(s.c5, n);
+      for (int q = 1; q <= 4; ++q) {
+        const int nr = s.b5index(q, n), nrp = s.b5index(5 + q, n), l = s.b5index(9 + q, n), lp = s.b5index(14 + q, n);
+        for (int m = -l; m <= l; ++m)
+          for (int mp = 0; mp <= lp; ++mp) ch.wf(m, l, nr, mp, lp, nrp, la) += c * ch.db5pack(q, m, mp, n, la);
+      }
+      const int nr0 = s.b5index(5, n), l0 = s.b5index(14, n);
+      for (int m = 0; m <= l0; ++m) ch.wf_0(m, l0, nr0, la) += c * ch.db5pack_0(m, n, la);
+    }
+    // 6-body (src/forces.F90:280-331)
+    for (int n = 1; n <= s.nvar6; ++n) {
+      if (s.b6mt_atomic[n - 1].empty() || s.b6mt_magnetic[n - 1].empty()) continue;
+      const double c = ceff(s.c6, n);
+      for (int q = 1; q <= 5; ++q) {
+        const int nr = s.b6index(q, n), nrp = s.b6index(6 + q, n), l = s.b6index(11 + q, n),
+                  lp = s.b6index(17 + q, n);
+        for (int m = -l; m <= l; ++m)
+          for (int mp = 0; mp <= lp; ++mp) ch.wf(m, l, nr, mp, lp, nrp, la) += c * ch.db6pack(q, m, mp, n, la);
+      }
+      const int nr0 = s.b6index(6, n), l0 = s.b6index(17, n);
+      for (int m = 0; m <= l0; ++m) ch.wf_0(m, l0, nr0, la) += c * ch.db6pack_0(m, n, la);
     }
   }
 }
@@ -961,7 +1101,8 @@ int oracle_init(const char* path, const char* element, double rcut, double rcut_
 }
 
 // Sizes of the enumerated basis: out[0..3] = nvar1..nvar4, out[4] = number of
-// 3-body m terms, out[5] = 4-body m terms, out[6] = 2-body m terms.
+// 3-body m terms, out[5] = 4-body m terms, out[6] = 2-body m terms,
+// out[7..8] = nvar5, nvar6.
 int oracle_basis_sizes(int* out) {
   const OracleState& s = g_state;
   if (!s.initialized) return ORACLE_ERR_NOT_INIT;
@@ -978,6 +1119,8 @@ int oracle_basis_sizes(int* out) {
   out[4] = (int)t3;
   out[5] = (int)t4;
   out[6] = (int)t2;
+  out[7] = s.nvar5;
+  out[8] = s.nvar6;
   return ORACLE_OK;
 }
 
@@ -997,6 +1140,12 @@ int oracle_basis_rows(int rank, int* out) {
   else if (rank == 4)
     for (int n = 1; n <= s.nvar4; ++n)
       for (int q = 0; q < 15; ++q) out[15 * (n - 1) + q] = s.b4index(q + 1, n);
+  else if (rank == 5)
+    for (int n = 1; n <= s.nvar5; ++n)
+      for (int q = 0; q < 21; ++q) out[21 * (n - 1) + q] = s.b5index(q + 1, n);
+  else if (rank == 6)
+    for (int n = 1; n <= s.nvar6; ++n)
+      for (int q = 0; q < 27; ++q) out[27 * (n - 1) + q] = s.b6index(q + 1, n);
   else
     return ORACLE_ERR_ARGS;
   return ORACLE_OK;
@@ -1124,7 +1273,7 @@ int oracle_atom_state(int natom, int nei, const int* nstart, const int* nstop, c
   return ORACLE_OK;
 }
 
-// Descriptors B[natom][nvar1 + nvar2 + nvar3 + nvar4] (the prepB packs,
+// Descriptors B[natom][nvar1 + ... + nvar6] (the prepB packs,
 // src/b_basis.F90:6-536, in cluster order) and dE/drho [natom][2] (from the
 // embedding step of forceweights, src/forces.F90:976-1289). Not part of the
 // reference's interface: test support for the differentiation harness.
@@ -1146,7 +1295,7 @@ int oracle_descriptors(int natom, int nei, const int* nstart, const int* nstop, 
   in.elist_momi = elist_momi;
   in.dlist_mom = dlist_mom;
   in.elist_mom = elist_mom;
-  const int nB = s.nvar1 + s.nvar2 + s.nvar3 + s.nvar4;
+  const int nB = s.nvar1 + s.nvar2 + s.nvar3 + s.nvar4 + s.nvar5 + s.nvar6;
   const int chunk = 32;
   Chunk ch;
   for (int c0 = 1; c0 <= natom; c0 += chunk) {
@@ -1175,6 +1324,8 @@ int oracle_descriptors(int natom, int nei, const int* nstart, const int* nstop, 
       for (int c = 1; c <= s.nvar2; ++c) b[k++] = ch.b2pack(c, la);
       for (int c = 1; c <= s.nvar3; ++c) b[k++] = ch.b3pack(c, la);
       for (int c = 1; c <= s.nvar4; ++c) b[k++] = ch.b4pack(c, la);
+      for (int c = 1; c <= s.nvar5; ++c) b[k++] = ch.b5pack(c, la);
+      for (int c = 1; c <= s.nvar6; ++c) b[k++] = ch.b6pack(c, la);
       if (dedrho) {
         dedrho[2 * (c0 + la - 2)] = ch.dEdrho_out[2 * la];
         dedrho[2 * (c0 + la - 2) + 1] = ch.dEdrho_out[2 * la + 1];

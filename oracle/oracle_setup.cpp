@@ -854,6 +854,297 @@ bool setuptables(OracleState& s, std::string& err) {
   return true;
 }
 
+// bcreate rank 5 (src/util.F90:4944-5022): allowed intermediate couplings
+// (L12, L34) of ((1 2)L12 (3 4)L34)l5, in loop order
+void rank5_lints(const OracleState& s, const int* vecnr, const int* vecl, std::vector<std::array<int, 3>>& lints,
+                 bool& isbasis) {
+  int nc[5];
+  for (int i = 0; i < 5; ++i) nc[i] = veck(s, 1, vecl[i], vecnr[i]);
+  const int l1 = vecl[0], l2 = vecl[1], l3 = vecl[2], l4 = vecl[3], l5 = vecl[4];
+  const int lintmax = 2 * *std::max_element(vecl, vecl + 5);
+  lints.clear();
+  for (int a = 0; a <= lintmax; ++a)
+    for (int b = 0; b <= lintmax; ++b) {
+      bool ok = true;
+      if (a > l1 + l2 || b > l3 + l4) ok = false;
+      if (a < std::abs(l1 - l2) || b < std::abs(l3 - l4)) ok = false;
+      if (l5 > a + b || l5 < std::abs(a - b)) ok = false;
+      if (nc[0] == nc[1] && a % 2 != 0) ok = false;
+      if (nc[2] == nc[3] && b % 2 != 0) ok = false;
+      if (nc[0] == nc[2] && nc[1] == nc[3] && a == b && l5 % 2 != 0) ok = false;
+      if (ok) lints.push_back({a, b, 0});
+    }
+  isbasis = !lints.empty();
+  if ((l1 + l2 + l3 + l4 + l5) % 2 != 0) isbasis = false;
+}
+
+// bcreate rank 6 (src/util.F90:5131-5220): couplings (L12, L34, L56) of
+// (((1 2)L12 (3 4)L34)L56 (5 6)L56)0, in loop order
+void rank6_lints(const OracleState& s, const int* vecnr, const int* vecl, std::vector<std::array<int, 3>>& lints,
+                 bool& isbasis) {
+  int nc[6];
+  for (int i = 0; i < 6; ++i) nc[i] = veck(s, 1, vecl[i], vecnr[i]);
+  const int l1 = vecl[0], l2 = vecl[1], l3 = vecl[2], l4 = vecl[3], l5 = vecl[4], l6 = vecl[5];
+  const int lintmax = 2 * *std::max_element(vecl, vecl + 6);
+  lints.clear();
+  for (int a = 0; a <= lintmax; ++a)
+    for (int b = 0; b <= lintmax; ++b)
+      for (int c = 0; c <= lintmax; ++c) {
+        bool ok = true;
+        if (a > l1 + l2 || b > l3 + l4 || c > l5 + l6) ok = false;
+        if (a < std::abs(l1 - l2) || b < std::abs(l3 - l4) || c < std::abs(l5 - l6)) ok = false;
+        if (c > a + b || c < std::abs(a - b)) ok = false;
+        if (nc[0] == nc[1] && a % 2 != 0) ok = false;
+        if (nc[2] == nc[3] && b % 2 != 0) ok = false;
+        if (nc[4] == nc[5] && c % 2 != 0) ok = false;
+        if (nc[0] == nc[2] && nc[1] == nc[3] && a == b && c % 2 != 0) ok = false;
+        if (ok) lints.push_back({a, b, c});
+      }
+  isbasis = !lints.empty();
+  if ((l1 + l2 + l3 + l4 + l5 + l6) % 2 != 0) isbasis = false;
+}
+
+// Every tuple of a nested loop over `n` digits with ranges [lo[q], hi[q]],
+// the last digit fastest (the reference's loop nests).
+template <class Fn>
+void nested(int n, const int* lo, const int* hi, Fn&& fn) {
+  std::vector<int> v(lo, lo + n);
+  for (int q = 0; q < n; ++q)
+    if (lo[q] > hi[q]) return;
+  while (true) {
+    fn(v.data());
+    int q = n - 1;
+    while (q >= 0 && v[q] == hi[q]) {
+      v[q] = lo[q];
+      --q;
+    }
+    if (q < 0) return;
+    ++v[q];
+  }
+}
+
+// The reordering of the internal couplings after the enumeration
+// (src/util.F90:3079-3094, :3705-3740): within each group of clusters that
+// share everything but their couplings, the entries after the group's first
+// exchange the coupling columns [c0, c0 + w) so that smaller sums come first.
+void reorder_lints(std::vector<std::vector<int>>& rows, const std::vector<int>& nint, int c0, int w) {
+  for (size_t n = 0; n < rows.size(); ++n)
+    for (int m = 1; m <= nint[n] - 2; ++m)
+      for (int k = m + 1; k <= nint[n] - 1; ++k) {
+        int s1 = 0, s2 = 0;
+        for (int q = 0; q < w; ++q) {
+          s1 += rows[n + m][c0 + q];
+          s2 += rows[n + k][c0 + q];
+        }
+        if (s1 > s2)
+          for (int q = 0; q < w; ++q) std::swap(rows[n + m][c0 + q], rows[n + k][c0 + q]);
+      }
+}
+
+// 5- and 6-body clusters (src/util.F90:2817-3760) for one element, with the
+// m-terms and couplings of each (src/util.F90:3100-3420, :3760-4140,
+// :4389-4546). Returns false (with err) where the reference stops.
+bool setuptables56(OracleState& s, std::string& err) {
+  auto& cg = s.cgcoeff;
+  std::vector<std::array<int, 3>> la, lm;
+  bool ba = false, bm = false;
+  // ---- 5-body
+  {
+    std::vector<std::vector<int>> rows;
+    std::vector<int> nint;
+    const int na = s.nradial5_atomic, nm = s.nradial5_magnetic, lam = s.l5max_atomic, lmm = s.l5max_magnetic;
+    const long kma = (long)na * (lam + 1), kmm = (long)nm * (lmm + 1), base = (kmm + 1) * kma + kmm;
+    const int lo[18] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int hi[18] = {na, na, na, na, nm, nm, nm, nm, nm, lam, lam, lam, lam, lmm, lmm, lmm, lmm, lmm};
+    bool bad_order = false;
+    if (na > 0 && nm > 0)
+      nested(18, lo, hi, [&](const int* v) {
+        // v: n1..n4, n0'..n4', l1..l4, l0'..l4'
+        long nc[4];
+        long ka[4];
+        for (int q = 0; q < 4; ++q) {
+          ka[q] = (long)na * v[9 + q] + v[q];
+          const long km = (long)nm * v[14 + q] + v[5 + q];
+          nc[q] = base + (kmm + 1) * ka[q] + km;
+        }
+        if (nc[0] < nc[1] || nc[1] < nc[2] || nc[2] < nc[3]) return;
+        if (ka[0] < ka[1] || ka[1] < ka[2] || ka[2] < ka[3]) bad_order = true;
+        // atomic rank 4, magnetic rank 5 (bcreate)
+        std::vector<int> lints;
+        bool basis_a;
+        const int vn[4] = {1, 1, 1, 1};
+        rank4_lints(s, vn, v, v + 9, lints, basis_a);
+        rank5_lints(s, v + 4, v + 13, lm, bm);
+        if (!(basis_a && bm)) return;
+        const int numa = (int)lints.size(), numm = (int)lm.size(), num = std::max(numa, numm);
+        for (int k = 0; k < num; ++k) {
+          std::vector<int> r(21, 0);
+          if (k < numa) {
+            for (int q = 0; q < 4; ++q) {
+              r[q] = v[q];
+              r[9 + q] = v[9 + q];
+            }
+            r[18] = lints[k];
+          }
+          if (k < numm) {
+            for (int q = 0; q < 5; ++q) {
+              r[4 + q] = v[4 + q];
+              r[13 + q] = v[13 + q];
+            }
+            r[19] = lm[k][0];
+            r[20] = lm[k][1];
+          }
+          rows.push_back(r);
+          nint.push_back(k == 0 ? num : 0);
+        }
+      });
+    if (bad_order) {
+      err = "the atomic basis is not ordered lexicographically (5-body)";
+      return false;
+    }
+    reorder_lints(rows, nint, 19, 2);
+    s.nvar5 = (int)rows.size();
+    s.b5index.init({{1, 21}, {1, std::max(1, s.nvar5)}});
+    s.b5mt_atomic.assign(s.nvar5, {});
+    s.b5mt_magnetic.assign(s.nvar5, {});
+    for (int n = 0; n < s.nvar5; ++n) {
+      const auto& r = rows[n];
+      for (int q = 0; q < 21; ++q) s.b5index(q + 1, n + 1) = r[q];
+      if (r[0] > 0) {  // atomic m-terms: (m1..m4) with M12 = m1 + m2 = -(m3 + m4)
+        const int l1 = r[9], l2 = r[10], l3 = r[11], l4 = r[12], L = r[18];
+        for (int M = -L; M <= L; ++M)
+          for (int m1 = -l1; m1 <= l1; ++m1)
+            for (int m2 = -l2; m2 <= l2; ++m2)
+              for (int m3 = -l3; m3 <= l3; ++m3)
+                for (int m4 = -l4; m4 <= l4; ++m4) {
+                  if (M != m1 + m2 || M != -(m3 + m4)) continue;
+                  const double c = cg(l1, l2, L, m1, m2, M) * cg(l3, l4, L, m3, m4, -M) * cg(L, L, 0, M, -M, 0);
+                  s.b5mt_atomic[n].push_back({{m1, m2, m3, m4, 0, 0}, c});
+                }
+      }
+      if (r[4] > 0) {  // magnetic m-terms: (m0'..m4') with -m4' = M01' + M23'
+        const int l0 = r[13], l1 = r[14], l2 = r[15], l3 = r[16], l4 = r[17], A = r[19], B = r[20];
+        for (int Ma = -A; Ma <= A; ++Ma)
+          for (int Mb = -B; Mb <= B; ++Mb)
+            for (int m0 = -l0; m0 <= l0; ++m0)
+              for (int m1 = -l1; m1 <= l1; ++m1)
+                for (int m2 = -l2; m2 <= l2; ++m2)
+                  for (int m3 = -l3; m3 <= l3; ++m3)
+                    for (int m4 = -l4; m4 <= l4; ++m4) {
+                      if (Ma != m0 + m1 || Mb != m2 + m3 || -m4 != Ma + Mb) continue;
+                      const double c = cg(l0, l1, A, m0, m1, Ma) * cg(l2, l3, B, m2, m3, Mb) *
+                                       cg(A, B, l4, Ma, Mb, -m4) * cg(l4, l4, 0, -m4, m4, 0);
+                      s.b5mt_magnetic[n].push_back({{m0, m1, m2, m3, m4, 0}, c});
+                    }
+      }
+    }
+  }
+  // ---- 6-body (the ordering key takes the 5-body dims, src/util.F90:3490-3491)
+  {
+    std::vector<std::vector<int>> rows;
+    std::vector<int> nint;
+    const int na = s.nradial6_atomic, nm = s.nradial6_magnetic, lam = s.l6max_atomic, lmm = s.l6max_magnetic;
+    const long kma = (long)s.nradial5_atomic * (s.l5max_atomic + 1);
+    const long kmm = (long)s.nradial5_magnetic * (s.l5max_magnetic + 1), base = (kmm + 1) * kma + kmm;
+    const int lo[22] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int hi[22] = {na, na, na, na, na, nm, nm, nm, nm, nm, nm, lam, lam, lam, lam, lam, lmm, lmm, lmm, lmm, lmm, lmm};
+    bool bad_order = false;
+    if (na > 0 && nm > 0) {
+      if (2 * lam > s.l3max_atomic || 2 * lmm > s.l2max_magnetic) {
+        err = "6-body couplings not worked for lmax > 6 (src/util.F90:3430-3434)";
+        return false;
+      }
+      nested(22, lo, hi, [&](const int* v) {
+        // v: n1..n5, n0'..n5', l1..l5, l0'..l5'
+        long nc[5], ka[5];
+        for (int q = 0; q < 5; ++q) {
+          ka[q] = (long)na * v[11 + q] + v[q];
+          const long km = (long)nm * v[17 + q] + v[6 + q];
+          nc[q] = base + (kmm + 1) * ka[q] + km;
+        }
+        if (nc[0] < nc[1] || nc[1] < nc[2] || nc[2] < nc[3] || nc[3] < nc[4]) return;
+        if (ka[0] < ka[1] || ka[1] < ka[2] || ka[2] < ka[3] || ka[3] < ka[4]) bad_order = true;
+        rank5_lints(s, v, v + 11, la, ba);
+        rank6_lints(s, v + 5, v + 16, lm, bm);
+        if (!(ba && bm)) return;
+        const int numa = (int)la.size(), numm = (int)lm.size(), num = std::max(numa, numm);
+        for (int k = 0; k < num; ++k) {
+          std::vector<int> r(27, 0);
+          if (k < numa) {
+            for (int q = 0; q < 5; ++q) {
+              r[q] = v[q];
+              r[11 + q] = v[11 + q];
+            }
+            r[22] = la[k][0];
+            r[23] = la[k][1];
+          }
+          if (k < numm) {
+            for (int q = 0; q < 6; ++q) {
+              r[5 + q] = v[5 + q];
+              r[16 + q] = v[16 + q];
+            }
+            r[24] = lm[k][0];
+            r[25] = lm[k][1];
+            r[26] = lm[k][2];
+          }
+          rows.push_back(r);
+          nint.push_back(k == 0 ? num : 0);
+        }
+      });
+    }
+    if (bad_order) {
+      err = "the atomic basis is not ordered lexicographically (6-body, src/util.F90:3512-3517)";
+      return false;
+    }
+    reorder_lints(rows, nint, 22, 2);
+    reorder_lints(rows, nint, 24, 3);
+    s.nvar6 = (int)rows.size();
+    s.b6index.init({{1, 27}, {1, std::max(1, s.nvar6)}});
+    s.b6mt_atomic.assign(s.nvar6, {});
+    s.b6mt_magnetic.assign(s.nvar6, {});
+    for (int n = 0; n < s.nvar6; ++n) {
+      const auto& r = rows[n];
+      for (int q = 0; q < 27; ++q) s.b6index(q + 1, n + 1) = r[q];
+      if (r[0] > 0) {  // atomic: M12 = m1 + m2, M34 = m3 + m4, -m5 = M12 + M34
+        const int l1 = r[11], l2 = r[12], l3 = r[13], l4 = r[14], l5 = r[15], A = r[22], B = r[23];
+        for (int Ma = -A; Ma <= A; ++Ma)
+          for (int Mb = -B; Mb <= B; ++Mb)
+            for (int m1 = -l1; m1 <= l1; ++m1)
+              for (int m2 = -l2; m2 <= l2; ++m2)
+                for (int m3 = -l3; m3 <= l3; ++m3)
+                  for (int m4 = -l4; m4 <= l4; ++m4)
+                    for (int m5 = -l5; m5 <= l5; ++m5) {
+                      if (Ma != m1 + m2 || Mb != m3 + m4 || -m5 != Ma + Mb) continue;
+                      const double c = cg(l1, l2, A, m1, m2, Ma) * cg(l3, l4, B, m3, m4, Mb) *
+                                       cg(A, B, l5, Ma, Mb, -m5) * cg(l5, l5, 0, -m5, m5, 0);
+                      s.b6mt_atomic[n].push_back({{m1, m2, m3, m4, m5, 0}, c});
+                    }
+      }
+      if (r[5] > 0) {  // magnetic: M01', M23', M45' with M01' + M23' = -M45'
+        const int l0 = r[16], l1 = r[17], l2 = r[18], l3 = r[19], l4 = r[20], l5 = r[21];
+        const int A = r[24], B = r[25], Cc = r[26];
+        for (int Ma = -A; Ma <= A; ++Ma)
+          for (int Mb = -B; Mb <= B; ++Mb)
+            for (int Mc = -Cc; Mc <= Cc; ++Mc)
+              for (int m0 = -l0; m0 <= l0; ++m0)
+                for (int m1 = -l1; m1 <= l1; ++m1)
+                  for (int m2 = -l2; m2 <= l2; ++m2)
+                    for (int m3 = -l3; m3 <= l3; ++m3)
+                      for (int m4 = -l4; m4 <= l4; ++m4)
+                        for (int m5 = -l5; m5 <= l5; ++m5) {
+                          if (Ma != m0 + m1 || Mb != m2 + m3 || Mc != m4 + m5 || Ma + Mb != -Mc) continue;
+                          const double c = cg(l0, l1, A, m0, m1, Ma) * cg(l2, l3, B, m2, m3, Mb) *
+                                           cg(l4, l5, Cc, m4, m5, Mc) * cg(A, B, Cc, Ma, Mb, -Mc) *
+                                           cg(Cc, Cc, 0, -Mc, Mc, 0);
+                          s.b6mt_magnetic[n].push_back({{m0, m1, m2, m3, m4, m5}, c});
+                        }
+      }
+    }
+  }
+  (void)ba;
+  return true;
+}
+
 }  // namespace
 
 // Reads the potential file (src/util.F90:459-1108, read branch only) and builds
@@ -926,17 +1217,30 @@ int oracle_setup(OracleState& s, const char* path, const char* element, double r
   s.nradbase = std::max(s.nradbase_atomic, s.nradbase_magnetic);
   s.nradial = std::max(s.nradial3_atomic, s.nradial2_magnetic);
   s.lmax = std::max(s.l3max_atomic, s.l2max_magnetic);
-  if (s.nradial5_atomic || s.nradial5_magnetic || s.nradial6_atomic || s.nradial6_magnetic) {
-    err = "5- and 6-body clusters are not supported";
-    return ORACLE_ERR_UNSUPPORTED;
-  }
-  if (s.l3max_atomic < s.l4max_atomic || s.l2max_magnetic < s.l3max_magnetic ||
-      s.l2max_magnetic < s.l4max_magnetic || s.nradial3_atomic < s.nradial4_atomic ||
+  if (s.l3max_atomic < s.l4max_atomic || s.l3max_atomic < s.l5max_atomic || s.l3max_atomic < s.l6max_atomic ||
+      s.l2max_magnetic < s.l3max_magnetic || s.l2max_magnetic < s.l4max_magnetic ||
+      s.l2max_magnetic < s.l5max_magnetic || s.l2max_magnetic < s.l6max_magnetic ||
+      s.nradial3_atomic < s.nradial4_atomic || s.nradial3_atomic < s.nradial5_atomic ||
+      s.nradial3_atomic < s.nradial6_atomic || s.nradial2_magnetic < s.nradial5_magnetic ||
+      s.nradial2_magnetic < s.nradial6_magnetic ||
       s.nradial2_magnetic < s.nradial3_magnetic || s.nradial2_magnetic < s.nradial4_magnetic ||
       s.nradial3_atomic > s.nradbase_atomic || s.nradial2_magnetic > s.nradbase_magnetic ||
       s.nradial > s.nradbase) {
     err = "basis dimension limits violated";
     return ORACLE_ERR_FORMAT;
+  }
+  // 5/6-body factors live in the 3-body A basis (n' <= nradial3_magnetic,
+  // l' <= l3max_magnetic here); the reference evaluates a rank only when the
+  // ranks below it are present (src/b_basis.F90:217-218, :312-313)
+  if (s.nradial5_magnetic > s.nradial3_magnetic || s.nradial6_magnetic > s.nradial3_magnetic ||
+      s.l5max_magnetic > s.l3max_magnetic || s.l6max_magnetic > s.l3max_magnetic) {
+    err = "5/6-body magnetic dims beyond the 3-body ones";
+    return ORACLE_ERR_UNSUPPORTED;
+  }
+  if (((s.nradial5_atomic || s.nradial5_magnetic) && !(s.nradial4_atomic || s.nradial4_magnetic)) ||
+      ((s.nradial6_atomic || s.nradial6_magnetic) && !(s.nradial5_atomic || s.nradial5_magnetic))) {
+    err = "a rank of clusters without the rank below it";
+    return ORACLE_ERR_UNSUPPORTED;
   }
   if (s.ndensity < 1 || s.ndensity > 2) {
     err = "ndensity must be 1 or 2";
@@ -947,6 +1251,7 @@ int oracle_setup(OracleState& s, const char* path, const char* element, double r
     return ORACLE_ERR_UNSUPPORTED;
   }
   if (!setuptables(s, err)) return ORACLE_ERR_FORMAT;
+  if (!setuptables56(s, err)) return ORACLE_ERR_FORMAT;
 
   // defaults (src/util.F90:281-350)
   s.crad_atomic.init({{1, s.nradbase_atomic}, {1, std::max(1, s.nradial3_atomic)}, {0, s.l3max_atomic}});
@@ -964,6 +1269,8 @@ int oracle_setup(OracleState& s, const char* path, const char* element, double r
   s.c2.init({{1, std::max(1, s.nvar2)}, {1, s.ndensity}});
   s.c3.init({{1, std::max(1, s.nvar3)}, {1, s.ndensity}});
   s.c4.init({{1, std::max(1, s.nvar4)}, {1, s.ndensity}});
+  s.c5.init({{1, std::max(1, s.nvar5)}, {1, s.ndensity}});
+  s.c6.init({{1, std::max(1, s.nvar6)}, {1, s.ndensity}});
 
   // parameter records (src/util.F90:669-1106)
   while (true) {
@@ -1037,8 +1344,29 @@ int oracle_setup(OracleState& s, const char* path, const char* element, double r
             if (match) s.c4(n, nd) = x;
           }
       } else if (norder == 5 || norder == 6) {
-        // ranks 5/6 are disabled by the header check above; skip the record line
-        if (!rd.skip()) break;
+        // 5-body: 5 elements, 21 indices (src/util.F90:826-889); 6-body: 6
+        // elements, 27 indices (src/util.F90:894-955)
+        const int w = norder == 5 ? 21 : 27;
+        if (!rd.read(norder + w + 2, t)) break;
+        std::vector<int> v(w);
+        double x;
+        for (int q = 0; q < w; ++q)
+          if (!to_int(t[norder + q], v[q])) return bad("clu 5/6");
+        if (!to_double(t[norder + w], x)) return bad("clu 5/6 value");
+        for (int q = 0; q < norder; ++q)
+          if (t[q] != s.element) {
+            err = "incorrect elements for interaction of order 5/6";
+            return ORACLE_ERR_FORMAT;
+          }
+        const int nv = norder == 5 ? s.nvar5 : s.nvar6;
+        const FArr<int>& idx = norder == 5 ? s.b5index : s.b6index;
+        if (nd <= s.ndensity)
+          for (int n = 1; n <= nv; ++n) {
+            bool match = true;
+            for (int q = 0; q < w && match; ++q)
+              if (v[q] != idx(q + 1, n)) match = false;
+            if (match) (norder == 5 ? s.c5 : s.c6)(n, nd) = x;
+          }
       }
     } else if (paratype == "par") {
       if (norder < 1 || norder > 2) return bad("par order");

@@ -77,6 +77,23 @@ def alt_potential(tmp_path_factory):
 
 
 @pytest.fixture(scope="session")
+def high_potential(tmp_path_factory):
+    """A seeded potential with 5- and 6-body clusters (HIGH_LAYOUT: radial
+    types 4/8, a non-linear embedding exponent 0.5); it runs on the
+    generic kernels."""
+    from magace import potential
+    path = str(tmp_path_factory.mktemp("high") / "Fe.pbe.in")
+    potential.write_seeded_potential(path, seed=7, layout=potential.HIGH_LAYOUT, par=(1.0, 0.5))
+    return path
+
+
+@pytest.fixture(scope="session")
+def oracle_high(high_potential):
+    import oracle as orc
+    return orc.Oracle(high_potential, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)
+
+
+@pytest.fixture(scope="session")
 def oracle_alt(alt_potential):
     import oracle as orc
     return orc.Oracle(alt_potential, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)

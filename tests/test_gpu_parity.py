@@ -461,3 +461,85 @@ def test_every_split_variant_matches_oracle(gpu_lib, oracle_seeded):
         for x, y in zip(got, res[0]):
             assert rel_err(x, y) < 1e-6
 
+
+
+# ---------------------------------------------------------------------------
+# 5- and 6-body clusters (HIGH_LAYOUT, generic kernels with gather entries of
+# up to five other factors)
+
+@pytest.fixture()
+def high_lib(high_potential):
+    from magace import lib
+    lib.init(high_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    lib.set_precision(0)
+    yield lib
+    lib.set_precision(0)
+
+
+@pytest.mark.parametrize("case", ["bcc54", "slab"])
+def test_high_body_fp64_parity(high_lib, oracle_high, case):
+    """Energies, forces and magnetic forces with 5- and 6-body clusters
+    (src/b_basis.F90:310-532, src/forces.F90:234-331) equal the oracle's at
+    1e-10 relative."""
+    from magace import structures as S
+    assert high_lib.basis_count(5) > 0 and high_lib.basis_count(6) > 0
+    st = {"bcc54": lambda: S.bcc_fe_54(9), "slab": _ragged_slab}[case]()
+    _compare(high_lib, oracle_high, S.neighbor_data(st, 5.0))
+    assert high_lib.last_launch_count() == 3  # the generic kernels
+
+
+def test_high_body_split_precision(high_lib, oracle_high):
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_54(10), 5.0)
+    high_lib.set_precision(1)
+    e, f, t, t0 = high_lib.acelib(nb)
+    eo, fo, to, t0o = oracle_high.acelib(nb)
+    assert np.abs(e - eo).max() * 1e3 < 1.0
+    assert np.abs(f - fo).max() * 1e3 < 10.0
+    assert np.abs(t - to).max() * 1e3 < 10.0 and np.abs(t0 - t0o).max() * 1e3 < 10.0
+    for got, ref in ((e, eo), (f, fo), (t, to), (t0, t0o)):
+        assert rel_err(got, ref) < 1e-5
+
+
+def test_high_body_descriptors(high_lib, oracle_high):
+    """The 5- and 6-body basis functions B (six factors per m-term) through
+    ace_descriptors_device, against the oracle's prepB packs."""
+    import torch
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_54(13), 5.0)
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    arrs = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
+    ncoef, nd = high_lib.num_coefficients()
+    B = torch.zeros(nb.natom, ncoef, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    high_lib.descriptors_device(nb.natom, nb.nei, off.data_ptr(), *[a.data_ptr() for a in arrs], B.data_ptr(), 1)
+    torch.cuda.synchronize()
+    high_lib.device_status()
+    Bo, _ = oracle_high.descriptors(nb)
+    n4 = sum(high_lib.basis_count(r) for r in (1, 2, 3, 4))
+    assert np.abs(Bo[:, n4:]).max() > 1e-3  # non-trivial 5-/6-body basis functions
+    assert rel_err(B.cpu().numpy(), Bo) < 1e-10
+
+
+def test_padded_high_body_clusters_contribute_nothing(high_lib):
+    """A 5-/6-body cluster whose atomic or magnetic half the enumeration pads
+    with zeros has no basis function (the reference reads its factors outside
+    its A basis): its coefficient leaves every output unchanged."""
+    from magace import structures as S
+    nb = S.neighbor_data(S.bcc_fe_54(14), 5.0)
+    before = high_lib.acelib(nb)
+    c = high_lib.get_coefficients()
+    n4 = sum(high_lib.basis_count(r) for r in (1, 2, 3, 4))
+    r5, r6 = high_lib.basis_rows(5), high_lib.basis_rows(6)
+    padded = [n4 + k for k, r in enumerate(r5) if r[0] == 0 or r[4] == 0]
+    padded += [n4 + len(r5) + k for k, r in enumerate(r6) if r[0] == 0 or r[5] == 0]
+    assert padded
+    c2 = c.copy()
+    c2[:, padded] += 3.0
+    high_lib.set_coefficients(c2)
+    after = high_lib.acelib(nb)
+    high_lib.set_coefficients(c)
+    for a, b in zip(after, before):
+        assert np.array_equal(a, b)

@@ -49,6 +49,21 @@ def test_init_and_basis_match_oracle(lib, seeded_potential, oracle_seeded):
         assert np.array_equal(lib.basis_rows(r), oracle_seeded.basis_rows(r))
 
 
+def test_high_body_enumeration_matches_oracle(lib, high_potential, oracle_high):
+    """5- and 6-body clusters: the library's enumeration (model.cpp) and the
+    oracle's restatement of src/util.F90:2817-3760, written separately,
+    give the same rows in the same order, including the clusters whose
+    atomic or magnetic half the reference pads with zeros."""
+    lib.init(high_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    for r in (1, 2, 3, 4, 5, 6):
+        assert np.array_equal(lib.basis_rows(r), oracle_high.basis_rows(r)), r
+    r5, r6 = lib.basis_rows(5), lib.basis_rows(6)
+    assert len(r5) > 0 and len(r6) > 0
+    assert (r5[:, 0] == 0).any() and (r5[:, 4] == 0).any()  # padded halves exist
+    assert lib.basis_sizes()["unmatched"] == 0
+    assert lib.num_coefficients()[0] == sum(len(lib.basis_rows(r)) for r in range(1, 7))
+
+
 def test_reference_potential_matches_enumeration(lib, reference_fe):
     lib.init(reference_fe, "Fe", 4.5, 4.0, 0.2, 1)
     sz = lib.basis_sizes()
@@ -81,13 +96,16 @@ def test_error_codes(lib, tmp_path, seeded_potential):
     with pytest.raises(MagAceError) as e:
         lib.init(seeded_potential, rcut=4.0)  # shorter than the file's 5.0 A
     assert e.value.code == 2
-    # 5-body clusters are rejected
-    text = open(seeded_potential).read().replace(" nradial5 l5max   0 0 0 0", " nradial5 l5max   1 1 0 0")
-    p5 = tmp_path / "five.in"
-    p5.write_text(text)
-    with pytest.raises(MagAceError) as e:
-        lib.init(str(p5))
-    assert e.value.code == 3
+    # 5-/6-body dims the A basis does not hold (n' beyond nradial3_magnetic = 3),
+    # and 6-body clusters without 5-body ones (the reference skips them), are refused
+    text = open(seeded_potential).read()
+    for old, new in ((" nradial5 l5max   0 0 0 0", " nradial5 l5max   1 4 0 0"),
+                     (" nradial6 l6max   0 0 0 0", " nradial6 l6max   1 1 0 0")):
+        p5 = tmp_path / "high.in"
+        p5.write_text(text.replace(old, new))
+        with pytest.raises(MagAceError) as e:
+            lib.init(str(p5))
+        assert e.value.code == 3
     assert lib.load().ace_error_string(4).decode().startswith("bond shorter")
     # kernel variants: indices outside a kernel's range are refused, valid ones kept
     before = lib.get_tuning_indices()

@@ -15,8 +15,8 @@ NOTEBOOK_ETOT = -15.7479878560111  # example/basic_lammps.ipynb:272
 
 
 def test_basis_sizes_fe(oracle_fe):
-    # clusters of example/Fe.pbe.in: 16 'clu 1', 720 'clu 2', 4932 'clu 3', 495 'clu 4'
-    assert oracle_fe.nvar == (16, 720, 4932, 495)
+    # clusters of example/Fe.pbe.in: 16 'clu 1', 720 'clu 2', 4932 'clu 3', 495 'clu 4', no 5/6-body
+    assert oracle_fe.nvar == (16, 720, 4932, 495, 0, 0)
     assert (oracle_fe.nterms2, oracle_fe.nterms3, oracle_fe.nterms4) == (2160, 64008, 495)
 
 
@@ -68,14 +68,17 @@ def _energy(orc, st, rcut):
     return e.sum(), nb, f, t, t0
 
 
-@pytest.mark.parametrize("which", ["fe", "seeded", "alt"])
+@pytest.mark.parametrize("which", ["fe", "seeded", "alt", "high"])
 def test_finite_differences(which, request):
     """Forces and magnetic forces assembled as in lammps/pair_spin_ace.cpp
     equal -dE/dx and -dE/dm from centred differences (h = 1e-5), for the
-    example Fe potential and both seeded layouts (the second one with two
-    densities and a non-linear embedding)."""
+    example Fe potential and the seeded layouts (the second one with two
+    densities and a non-linear embedding, the third with 5- and 6-body
+    clusters; its radial basis has a larger third derivative, so it takes
+    h = 2e-6, where the truncation error falls as h^2)."""
     from magace import structures as S
-    orc = request.getfixturevalue({"fe": "oracle_fe", "seeded": "oracle_seeded", "alt": "oracle_alt"}[which])
+    orc = request.getfixturevalue({"fe": "oracle_fe", "seeded": "oracle_seeded", "alt": "oracle_alt",
+                                   "high": "oracle_high"}[which])
     rc = 4.5 if which == "fe" else 5.0
     rng = np.random.default_rng(3)
     pos, cell = S.bcc_cubic(2, 2, 2, 2.83)
@@ -89,7 +92,7 @@ def test_finite_differences(which, request):
 
     E, nb, f, t, t0 = _energy(orc, st_of(pos, mvec), rc)
     F, FM = S.total_forces(nb, f, t, t0)
-    h = 1e-5
+    h = 2e-6 if which == "high" else 1e-5
     for k in (0, 5, 11):
         for c in range(3):
             p = pos.copy(); p[k, c] += h
@@ -125,3 +128,25 @@ def test_rotation_and_moment_reversal(oracle_seeded):
     e2 = oracle_seeded.acelib(S.neighbor_data(S.Structure(pos, cell, (True,) * 3, mag, -mh), 5.0))[0]
     assert np.allclose(e1, e0, rtol=0, atol=1e-10)
     assert np.allclose(e2, e0, rtol=0, atol=1e-10)
+
+
+def test_high_body_rotation_invariance(oracle_high):
+    """With 5- and 6-body clusters the energy stays invariant under a joint
+    rotation of positions and moments and under rotating the moments alone:
+    the generalized couplings of src/util.F90:4389-4546 form invariants."""
+    from magace import structures as S
+    assert oracle_high.nvar[4] > 0 and oracle_high.nvar[5] > 0
+    rng = np.random.default_rng(12)
+    pos, cell = S.bcc_cubic(2, 2, 2, 2.83)
+    pos = pos + rng.normal(0, 0.08, pos.shape)
+    n = len(pos)
+    mag, mh = rng.uniform(1.8, 2.4, n), S.random_unit(rng, n)
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] *= -1
+    e0 = oracle_high.acelib(S.neighbor_data(S.Structure(pos, cell, (True,) * 3, mag, mh), 5.0))[0]
+    e1 = oracle_high.acelib(S.neighbor_data(S.Structure(pos, cell, (True,) * 3, mag, mh @ q.T), 5.0))[0]
+    e2 = oracle_high.acelib(S.neighbor_data(S.Structure(pos @ q.T, cell @ q.T, (True,) * 3, mag, mh @ q.T),
+                                            5.0))[0]
+    assert np.allclose(e1, e0, rtol=0, atol=1e-11)
+    assert np.allclose(e2, e0, rtol=0, atol=1e-11)
