@@ -241,6 +241,28 @@ int ace_descriptors_device(int natom, int nei, const int* bond_offset, const dou
                            const double* e, const double* mag_j, const double* mhat_j,
                            const double* mag_i, const double* mhat_i, double* B, void* stream);
 
+/* Descriptors and their directional derivatives, for the coefficient
+ * gradients of losses on forces and magnetic forces (fitting). Along the
+ * tangents dd[3*nei] of the bond vectors x_i - x_j (dd_ij = u_i - u_j for a
+ * displacement field u), dm_j[3*nei] of the neighbours' moments and
+ * dm_i[3*natom] of the atoms' own moments, writes B[natom][ncoef] (as
+ * ace_descriptors_device), Bdot[natom][ncoef] = dB/d(epsilon) at epsilon = 0
+ * of the inputs moved by epsilon times the tangents, and the core energy
+ * core[natom] and its derivative core_dot[natom]. FP64, asynchronous on
+ * `stream`; the other arguments as ace_compute_device. No counterpart in the
+ * reference, whose fitting code is not part of it (src/Makefile:107-108). */
+int ace_descriptors_tangent_device(int natom, int nei, const int* bond_offset, const double* r,
+                                   const double* e, const double* mag_j, const double* mhat_j,
+                                   const double* mag_i, const double* mhat_i, const double* dd,
+                                   const double* dm_j, const double* dm_i, double* B, double* Bdot,
+                                   double* core, double* core_dot, void* stream);
+
+/* The embedding of the loaded potential (src/forces.F90:1134-1266): nfemb,
+ * par[2*order + density] (order 0: prefactor, 1: exponent; density 0, 1),
+ * and the inner cutoff inner_cutoff[0..1] = ecut, decut on the core energy
+ * (src/forces.F90:1112-1128). Any pointer may be NULL. */
+int ace_embedding(int* nfemb, double* par, double* inner_cutoff);
+
 /* Copies dE_i/drho_d [natom][2] (d = 0, 1; the second is 0 for one density)
  * of the last ace_compute_device or acelib_ evaluation into a device array,
  * on `stream`. */

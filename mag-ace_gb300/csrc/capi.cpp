@@ -122,7 +122,7 @@ struct Runtime {
   // work buffers
   DevBuf<int> off, err;
   DevBuf<double> r, e, magj, mhj, magi, mhi, energy, fij, tij, ti0, rho1, core, edf, dedrho;
-  DevBuf<unsigned char> F, W, aux, bstage;
+  DevBuf<unsigned char> F, W, aux, bstage, Fd;
   std::vector<int> h_off;
 
   // pinned staging for host transfers, and whether the GPU reads pageable
@@ -917,6 +917,60 @@ int ace_descriptors_device(int natom, int nei, const int* bond_offset, const dou
   return set_error(MAGACE_OK, "");
 }
 
+int ace_descriptors_tangent_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
+                                   const double* mag_j, const double* mhat_j, const double* mag_i,
+                                   const double* mhat_i, const double* dd, const double* dm_j, const double* dm_i,
+                                   double* B, double* Bdot, double* core, double* core_dot, void* stream) {
+  Runtime& R = rt();
+  if (int st0 = check_sizes(natom, nei)) return st0;
+  if (natom > 0 && (!B || !Bdot || !core || !core_dot || !dm_i || (nei > 0 && (!dd || !dm_j))))
+    return set_error(MAGACE_ERR_ARGS, "null tangent or output array");
+  int st = upload_tables();
+  if (st) return st;
+  st = reserve_work(natom, nei, 0);
+  if (st) return st;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  int smem_max = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (descriptors_tangent_smem(R.dm) > static_cast<size_t>(smem_max))
+    return set_error(MAGACE_ERR_UNSUPPORTED, "basis too large for the tangent kernel's shared-memory tiles");
+  CUDA_TRY(R.Fd.reserve(static_cast<size_t>(natom) * R.dm.nF * 16));
+  EvalBuffers b;
+  b.natom = natom;
+  b.nei = nei;
+  b.off = bond_offset;
+  b.r = r;
+  b.e = e;
+  b.magj = mag_j;
+  b.mhj = mhat_j;
+  b.magi = mag_i;
+  b.mhi = mhat_i;
+  b.F = R.F.p;
+  b.err = R.err.p;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : R.stream;
+  CUDA_TRY(cudaMemsetAsync(R.err.p, 0, sizeof(int), s));
+  R.last_launches = R.last_kernels =
+      launch_descriptors_tangent(R.dm, b, dd, dm_j, dm_i, R.Fd.p, B, Bdot, core, core_dot, s, R.grid_cap);
+  R.ev_recorded = false;
+  CUDA_TRY(cudaGetLastError());
+  return set_error(MAGACE_OK, "");
+}
+
+int ace_embedding(int* nfemb, double* par, double* inner_cutoff) {
+  Runtime& R = rt();
+  if (!R.ready) return set_error(MAGACE_ERR_NOT_INIT, "no potential initialised");
+  if (nfemb) *nfemb = R.model.nfemb;
+  if (par)
+    for (int a = 0; a < 2; ++a)
+      for (int d = 0; d < 2; ++d) par[2 * a + d] = R.model.par[a][d];
+  if (inner_cutoff) {
+    inner_cutoff[0] = R.model.ecut;
+    inner_cutoff[1] = R.model.decut;
+  }
+  return set_error(MAGACE_OK, "");
+}
+
 int ace_density_gradient_device(int natom, double* dedrho, void* stream) {
   Runtime& R = rt();
   if (natom < 0 || natom > R.last_natom)
@@ -961,6 +1015,7 @@ void ace_release_device(void) {
   R.off.release();
   R.err.release();
   R.F.release();
+  R.Fd.release();
   R.aux.release();
   R.bstage.release();
   R.order.release();

@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kAbasisThreads)
       if (threadIdx.x < nb) {
         const int b = threadIdx.x, j = t0 + b;
         const double r = rr[j];
-        R g[32], Rv[16], Mv[32], cv[1], dummy[1];
+        R g[kMaxFeat], Rv[kMaxFeat], Mv[kMaxFeat], cv[1], dummy[1];
         double wl = 0.0;
         const int nla = atomic_bin(m, r, wl, err);
         if (nla > 0) {
@@ -1485,6 +1485,341 @@ int launch_descriptors(const DeviceModel& m0, const EvalBuffers& b, double* B, c
   set_smem(k_descriptors, sd);
   k_descriptors<<<grid, kDescThreads, sd, st>>>(m, natom, reinterpret_cast<const C<double>*>(b.F), b.magi, B, b.err);
   return 2;
+}
+
+// ===========================================================================
+// Tangents for the coefficient gradients of force losses. Along a
+// displacement field (bond-vector tangents dd_ij = u_i - u_j and moment
+// tangents dm), k_abasis_tangent evaluates the factors F (as k_abasis in
+// FP64) and their directional derivatives Fd, with
+//   dr = e . dd,  d(R Y_lm(e)) = R' dr Y + R (dY . dd) / r,
+//   d|m| = m_hat . dm,  d(M Y(m_hat)) = M' d|m| Y + M (dY . dm) / |m|,
+// (dY the tangential gradient of ylm_half; the force kernels use the same
+// derivatives), and the core energy and its derivative.
+// k_descriptors_tangent then forms B and dB of every cluster by dual-number
+// products: (p, dp) (f, df) = (p f, dp f + p df). One CTA per atom, FP64.
+__global__ void __launch_bounds__(kAbasisThreads)
+    k_abasis_tangent(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
+                     const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
+                     const double* __restrict__ magi, const double* __restrict__ mhi, const double* __restrict__ dd,
+                     const double* __restrict__ dmj, const double* __restrict__ dmi, C<double>* __restrict__ F,
+                     C<double>* __restrict__ Fd, double* __restrict__ core_out, double* __restrict__ cored_out,
+                     int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int TB = kAbasisTile;
+  const int nA2h = m.nba * m.n2m * m.h2;
+  const int nacc = m.nWA + nA2h;
+  const int nRY = m.n3a * m.lsa, nQ = m.n2m * m.h2;
+  C<double>* acc = reinterpret_cast<C<double>*>(smem);  // [nacc] value, then [nacc] tangent
+  C<double>* accd = acc + nacc;
+  C<double>* sRY = accd + nacc;   // [nRY][TB]
+  C<double>* sRYd = sRY + nRY * TB;
+  C<double>* sQ = sRYd + nRY * TB;  // [nQ][TB]
+  C<double>* sQd = sQ + nQ * TB;
+  double* sg = reinterpret_cast<double*>(sQd + nQ * TB);  // [nba][TB]
+  double* sgd = sg + m.nba * TB;
+  double* score = sgd + m.nba * TB;  // [TB] value, then [TB] tangent
+  __shared__ double s_core[2];
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
+    for (int s = threadIdx.x; s < 2 * nacc; s += blockDim.x) acc[s] = {0.0, 0.0};
+    if (threadIdx.x == 0) s_core[0] = s_core[1] = 0.0;
+    const int b0 = off[atom], b1 = off[atom + 1];
+    __syncthreads();
+    for (int t0 = b0; t0 < b1; t0 += TB) {
+      const int nb = min(TB, b1 - t0);
+      if (threadIdx.x < nb) {
+        const int b = threadIdx.x, j = t0 + b;
+        const double r = rr[j];
+        const double e[3] = {ee[3 * j], ee[3 * j + 1], ee[3 * j + 2]};
+        const double dv[3] = {dd[3 * j], dd[3 * j + 1], dd[3 * j + 2]};
+        const double rdot = e[0] * dv[0] + e[1] * dv[1] + e[2] * dv[2];
+        double g[kMaxFeat], gd[kMaxFeat], Rv[kMaxFeat], Rd[kMaxFeat], cv[1], cd[1], Mv[kMaxFeat], Md[kMaxFeat];
+        double wl = 0.0;
+        const int nla = atomic_bin(m, r, wl, err);
+        const int nR = m.n3a * (m.l3a + 1), nM = m.n2m * (m.l2m + 1);
+        if (nla > 0) {
+          lut_eval<true>(m.lut_a, m.nfa, 0, m.nba, nla, wl, m.rscale_a, g, gd);
+          lut_eval<true>(m.lut_a, m.nfa, m.nba, nR, nla, wl, m.rscale_a, Rv, Rd);
+          lut_eval<true>(m.lut_a, m.nfa, m.nba + nR, 1, nla, wl, m.rscale_a, cv, cd);
+        } else {
+          for (int q = 0; q < m.nba; ++q) g[q] = gd[q] = 0.0;
+          for (int q = 0; q < nR; ++q) Rv[q] = Rd[q] = 0.0;
+          cv[0] = cd[0] = 0.0;
+        }
+        const double mg = magj[j];
+        const double mh[3] = {mhj[3 * j], mhj[3 * j + 1], mhj[3 * j + 2]};
+        const double dm[3] = {dmj[3 * j], dmj[3 * j + 1], dmj[3 * j + 2]};
+        const double mgdot = mh[0] * dm[0] + mh[1] * dm[1] + mh[2] * dm[2];
+        double wm = 0.0;
+        const int nlm = magnetic_bin(m, mg, wm, err);
+        if (nlm > 0) {
+          lut_eval<true>(m.lut_m, m.nfm, 0, nM, nlm, wm, m.rscale_m, Mv, Md);
+        } else {
+          for (int q = 0; q < nM; ++q) {
+            Mv[q] = nlm == 0 ? 1.0 : 0.0;
+            Md[q] = 0.0;
+          }
+        }
+        C<double> Ya[kMaxHalf], dYa[kMaxHalf][3], Ym[kMaxHalf], dYm[kMaxHalf][3];
+        ylm_half<double, true>(m.l3a, e[0], e[1], e[2], Ya, dYa);
+        ylm_half<double, true>(m.l2m, mh[0], mh[1], mh[2], Ym, dYm);
+        const double ir = 1.0 / r, im = mg > 0.0 ? 1.0 / mg : 0.0;
+        for (int l1 = 0; l1 <= m.l3a; ++l1)
+          for (int m1 = -l1; m1 <= l1; ++m1) {
+            const int k = ph(l1, m1 < 0 ? -m1 : m1);
+            C<double> yd = {0.0, 0.0};
+            for (int c = 0; c < 3; ++c) {
+              yd.x = fma(dYa[k][c].x, dv[c], yd.x);
+              yd.y = fma(dYa[k][c].y, dv[c], yd.y);
+            }
+            yd = cscale(yd, ir);
+            if (m1 < 0) {
+              const double sgn = parity(m1);
+              yd = {yd.x * sgn, -yd.y * sgn};
+            }
+            const C<double> y = y_full(Ya, l1, m1);
+            for (int n1 = 0; n1 < m.n3a; ++n1) {
+              const int q = n1 * (m.l3a + 1) + l1, i = n1 * m.lsa + l1 * l1 + l1 + m1;
+              sRY[i * TB + b] = cscale(y, Rv[q]);
+              sRYd[i * TB + b] = {Rd[q] * rdot * y.x + Rv[q] * yd.x, Rd[q] * rdot * y.y + Rv[q] * yd.y};
+            }
+          }
+        for (int l = 0; l <= m.l2m; ++l)
+          for (int mm = 0; mm <= l; ++mm) {
+            const int k = ph(l, mm);
+            C<double> yd = {0.0, 0.0};
+            for (int c = 0; c < 3; ++c) {
+              yd.x = fma(dYm[k][c].x, dm[c], yd.x);
+              yd.y = fma(dYm[k][c].y, dm[c], yd.y);
+            }
+            yd = cscale(yd, im);
+            for (int nr = 0; nr < m.n2m; ++nr) {
+              const int q = nr * (m.l2m + 1) + l, i = nr * m.h2 + k;
+              sQ[i * TB + b] = cscale(Ym[k], Mv[q]);
+              sQd[i * TB + b] = {Md[q] * mgdot * Ym[k].x + Mv[q] * yd.x, Md[q] * mgdot * Ym[k].y + Mv[q] * yd.y};
+            }
+          }
+        for (int n = 0; n < m.nba; ++n) {
+          sg[n * TB + b] = g[n];
+          sgd[n * TB + b] = gd[n] * rdot;
+        }
+        score[b] = cv[0];
+        score[TB + b] = cd[0] * rdot;
+      }
+      __syncthreads();
+      for (int s = threadIdx.x; s < nacc; s += blockDim.x) {
+        C<double> a = acc[s], ad = accd[s];
+        if (s < m.nWA) {
+          const int h = s % m.h3, q = s / m.h3, n2 = q % m.n3m, ia = q / m.n3m;
+          const C<double>* ry = sRY + ia * TB;
+          const C<double>* ryd = sRYd + ia * TB;
+          const C<double>* qq = sQ + (n2 * m.h2 + h) * TB;
+          const C<double>* qd = sQd + (n2 * m.h2 + h) * TB;
+          for (int b = 0; b < nb; ++b) {
+            cmac(a, ry[b], qq[b]);
+            cmac(ad, ryd[b], qq[b]);
+            cmac(ad, ry[b], qd[b]);
+          }
+        } else {
+          const int t = s - m.nWA, h = t % m.h2, q = t / m.h2, nr = q % m.n2m, n = q / m.n2m;
+          const double* gg = sg + n * TB;
+          const double* ggd = sgd + n * TB;
+          const C<double>* qq = sQ + (nr * m.h2 + h) * TB;
+          const C<double>* qd = sQd + (nr * m.h2 + h) * TB;
+          for (int b = 0; b < nb; ++b) {
+            a.x = fma(gg[b], qq[b].x, a.x);
+            a.y = fma(gg[b], qq[b].y, a.y);
+            ad.x = fma(ggd[b], qq[b].x, fma(gg[b], qd[b].x, ad.x));
+            ad.y = fma(ggd[b], qq[b].y, fma(gg[b], qd[b].y, ad.y));
+          }
+        }
+        acc[s] = a;
+        accd[s] = ad;
+      }
+      if (threadIdx.x == 0)
+        for (int b = 0; b < nb; ++b) {
+          s_core[0] += score[b];
+          s_core[1] += score[TB + b];
+        }
+      __syncthreads();
+    }
+    // full A and A2 (m' < 0 by conjugate symmetry, linear: the same for the tangent)
+    for (int pass = 0; pass < 2; ++pass) {
+      const C<double>* src = pass ? accd : acc;
+      C<double>* Fa = (pass ? Fd : F) + static_cast<size_t>(atom) * m.nF;
+      const int nA = m.offA2 - m.offA;
+      for (int s = threadIdx.x; s < nA; s += blockDim.x) {
+        const int lmm = s % m.ls3, q = s / m.ls3, n2 = q % m.n3m, ia = q / m.n3m;
+        const int n1 = ia / m.lsa, lma = ia % m.lsa;
+        int l2 = 0;
+        while ((l2 + 1) * (l2 + 1) <= lmm) ++l2;
+        const int m2 = lmm - l2 * l2 - l2;
+        int l1 = 0;
+        while ((l1 + 1) * (l1 + 1) <= lma) ++l1;
+        const int m1 = lma - l1 * l1 - l1;
+        C<double> v;
+        if (m2 >= 0) {
+          v = src[((n1 * m.lsa + lma) * m.n3m + n2) * m.h3 + ph(l2, m2)];
+        } else {
+          const int lmb = l1 * l1 + l1 - m1;
+          const C<double> w = src[((n1 * m.lsa + lmb) * m.n3m + n2) * m.h3 + ph(l2, -m2)];
+          const double sgn = parity(m1 + m2);
+          v = {w.x * sgn, -w.y * sgn};
+        }
+        Fa[m.offA + s] = v;
+      }
+      const int nA2 = m.offA0 - m.offA2;
+      for (int s = threadIdx.x; s < nA2; s += blockDim.x) {
+        const int lm = s % m.ls2, q = s / m.ls2;
+        int l = 0;
+        while ((l + 1) * (l + 1) <= lm) ++l;
+        const int mm = lm - l * l - l;
+        const C<double> w = src[m.nWA + q * m.h2 + ph(l, mm < 0 ? -mm : mm)];
+        C<double> v = w;
+        if (mm < 0) {
+          const double sgn = parity(mm);
+          v = {w.x * sgn, -w.y * sgn};
+        }
+        Fa[m.offA2 + s] = v;
+      }
+    }
+    if (threadIdx.x == 0) {
+      // on-site A0 and its tangent, the constants
+      C<double>* Fa = F + static_cast<size_t>(atom) * m.nF;
+      C<double>* Fda = Fd + static_cast<size_t>(atom) * m.nF;
+      const double mg = magi[atom];
+      const double mh[3] = {mhi[3 * atom], mhi[3 * atom + 1], mhi[3 * atom + 2]};
+      const double dm[3] = {dmi[3 * atom], dmi[3 * atom + 1], dmi[3 * atom + 2]};
+      const double mgdot = mh[0] * dm[0] + mh[1] * dm[1] + mh[2] * dm[2], im = mg > 0.0 ? 1.0 / mg : 0.0;
+      double wl = 0.0, Mv[32], Md[32];
+      const int nl = magnetic_bin(m, mg, wl, err);
+      const int nM = m.n2m * (m.l2m + 1);
+      if (nl > 0) {
+        lut_eval<true>(m.lut_m, m.nfm, 0, nM, nl, wl, m.rscale_m, Mv, Md);
+      } else {
+        for (int q = 0; q < nM; ++q) {
+          Mv[q] = nl == 0 ? 1.0 : 0.0;
+          Md[q] = 0.0;
+        }
+      }
+      C<double> Yi[kMaxHalf], dYi[kMaxHalf][3];
+      ylm_half<double, true>(m.l2m, mh[0], mh[1], mh[2], Yi, dYi);
+      for (int l = 0; l <= m.l2m; ++l)
+        for (int mm = -l; mm <= l; ++mm) {
+          const int k = ph(l, mm < 0 ? -mm : mm);
+          C<double> yd = {0.0, 0.0};
+          for (int c = 0; c < 3; ++c) {
+            yd.x = fma(dYi[k][c].x, dm[c], yd.x);
+            yd.y = fma(dYi[k][c].y, dm[c], yd.y);
+          }
+          yd = cscale(yd, im);
+          if (mm < 0) {
+            const double sgn = parity(mm);
+            yd = {yd.x * sgn, -yd.y * sgn};
+          }
+          const C<double> y = y_full(Yi, l, mm);
+          for (int nr = 0; nr < m.n2m; ++nr) {
+            const int q = nr * (m.l2m + 1) + l, f = m.offA0 + nr * m.ls2 + l * l + l + mm;
+            Fa[f] = cscale(y, Mv[q]);
+            Fda[f] = {Md[q] * mgdot * y.x + Mv[q] * yd.x, Md[q] * mgdot * y.y + Mv[q] * yd.y};
+          }
+        }
+      Fa[m.offOne] = {1.0, 0.0};
+      Fa[m.offZero] = {0.0, 0.0};
+      Fda[m.offOne] = {0.0, 0.0};
+      Fda[m.offZero] = {0.0, 0.0};
+      core_out[atom] = s_core[0];
+      cored_out[atom] = s_core[1];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kDescThreads)
+    k_descriptors_tangent(DeviceModel m, int natom, const C<double>* __restrict__ F, const C<double>* __restrict__ Fd,
+                          const double* __restrict__ magi, const double* __restrict__ mhi,
+                          const double* __restrict__ dmi, double* __restrict__ B, double* __restrict__ Bd, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  C<double>* Fs = reinterpret_cast<C<double>*>(smem);
+  C<double>* Fds = Fs + m.nF;
+  const int nB = m.d_nB, n1 = m.d_n1;
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
+    for (int s = threadIdx.x; s < m.nF; s += blockDim.x) {
+      Fs[s] = F[static_cast<size_t>(atom) * m.nF + s];
+      Fds[s] = Fd[static_cast<size_t>(atom) * m.nF + s];
+    }
+    __syncthreads();
+    double* Ba = B + static_cast<size_t>(atom) * nB;
+    double* Bda = Bd + static_cast<size_t>(atom) * nB;
+    // rank 1: g_n(|m_i|) - 1 and g_n' (m_hat_i . dm_i)
+    for (int k = threadIdx.x; k < n1; k += blockDim.x) {
+      double wl = 0.0, g = 1.0, gd = 0.0;
+      const int nl = magnetic_bin(m, magi[atom], wl, err);
+      if (nl > 0) {
+        lut_eval<true>(m.lut_m, m.nfm, m.n2m * (m.l2m + 1) + m.d_rank1_n[k], 1, nl, wl, m.rscale_m, &g, &gd);
+      } else if (nl < 0) {
+        g = 0.0;
+      }
+      const double mgdot =
+          mhi[3 * atom] * dmi[3 * atom] + mhi[3 * atom + 1] * dmi[3 * atom + 1] + mhi[3 * atom + 2] * dmi[3 * atom + 2];
+      Ba[k] = g - 1.0;
+      Bda[k] = gd * mgdot;
+    }
+    for (int k = threadIdx.x; k < nB - n1; k += blockDim.x) {
+      double acc = 0.0, accd = 0.0;
+      for (int e = m.d_begin[k]; e < m.d_begin[k + 1]; ++e) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(m.d_o + kDescFactors * static_cast<size_t>(e)));
+        const unsigned o[6] = {q.x & 0xffffu, q.x >> 16, q.y & 0xffffu, q.y >> 16, q.z & 0xffffu, q.z >> 16};
+        C<double> p = Fs[o[0]], pd = Fds[o[0]];
+        for (int f = 1; f < 6; ++f) {
+          const C<double> v = Fs[o[f]], vd = Fds[o[f]];
+          pd = cmul(pd, v);
+          cmac(pd, p, vd);
+          p = cmul(p, v);
+        }
+        acc += m.d_cf[e] * p.x;
+        accd += m.d_cf[e] * pd.x;
+      }
+      Ba[n1 + k] = acc;
+      Bda[n1 + k] = accd;
+    }
+    __syncthreads();
+  }
+}
+
+int launch_descriptors_tangent(const DeviceModel& m0, const EvalBuffers& b, const double* dd, const double* dmj,
+                               const double* dmi, void* Fd, double* B, double* Bd, double* core, double* cored,
+                               cudaStream_t st, int grid_cap) {
+  DeviceModel m = m0;
+  m.order = b.order;
+  const int natom = b.natom;
+  if (natom <= 0) return 0;
+  const int grid = natom < grid_cap ? natom : grid_cap;
+  const int TB = kAbasisTile;
+  const size_t nacc = static_cast<size_t>(m.nWA) + static_cast<size_t>(m.nba) * m.n2m * m.h2;
+  const size_t sa = sizeof(C<double>) * (2 * nacc + 2 * static_cast<size_t>(m.n3a) * m.lsa * TB +
+                                         2 * static_cast<size_t>(m.n2m) * m.h2 * TB) +
+                    sizeof(double) * (2 * static_cast<size_t>(m.nba) * TB + 2 * TB);
+  set_smem(k_abasis_tangent, sa);
+  k_abasis_tangent<<<grid, kAbasisThreads, sa, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi, dd, dmj,
+                                                     dmi, reinterpret_cast<C<double>*>(b.F),
+                                                     reinterpret_cast<C<double>*>(Fd), core, cored, b.err);
+  const size_t sd = 2 * sizeof(C<double>) * static_cast<size_t>(m.nF);
+  set_smem(k_descriptors_tangent, sd);
+  k_descriptors_tangent<<<grid, kDescThreads, sd, st>>>(m, natom, reinterpret_cast<const C<double>*>(b.F),
+                                                        reinterpret_cast<const C<double>*>(Fd), b.magi, b.mhi, dmi, B,
+                                                        Bd, b.err);
+  return 2;
+}
+
+size_t descriptors_tangent_smem(const DeviceModel& m) {
+  const int TB = kAbasisTile;
+  const size_t nacc = static_cast<size_t>(m.nWA) + static_cast<size_t>(m.nba) * m.n2m * m.h2;
+  return sizeof(C<double>) * (2 * nacc + 2 * static_cast<size_t>(m.n3a) * m.lsa * TB +
+                              2 * static_cast<size_t>(m.n2m) * m.h2 * TB) +
+         sizeof(double) * (2 * static_cast<size_t>(m.nba) * TB + 2 * TB);
 }
 
 int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,

@@ -85,6 +85,16 @@ size_t eval_aux_bytes_bound(const DeviceModel& m, int precision, int natom);
 // Descriptors: the FP64 A-basis phase into b.F, then B[natom][nB] (see
 // model.hpp DescriptorTable); returns the number of kernels launched.
 int launch_descriptors(const DeviceModel& m, const EvalBuffers& b, double* B, cudaStream_t st, int grid_cap);
+// Descriptors B and their directional derivatives Bd along the tangents dd
+// [nei][3] (of the bond vectors x_i - x_j), dmj [nei][3] (of the neighbours'
+// moments) and dmi [natom][3] (of the atoms' moments), FP64: factors into b.F
+// and their tangents into Fd ([natom][nF] complex), then B and Bd
+// [natom][nB]; core and cored [natom] receive the core energy and its
+// derivative. Returns the number of kernels launched.
+int launch_descriptors_tangent(const DeviceModel& m, const EvalBuffers& b, const double* dd, const double* dmj,
+                               const double* dmi, void* Fd, double* B, double* Bd, double* core, double* cored,
+                               cudaStream_t st, int grid_cap);
+size_t descriptors_tangent_smem(const DeviceModel& m);
 int launch_eval_fp64(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,
                      int* kernels = nullptr);
 int launch_eval_fp32(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid_cap, cudaEvent_t* ev,

@@ -43,6 +43,25 @@ class Bonds:
     shift: torch.Tensor    # [nei, 3] integer image of j (x_j + shift @ cell)
     offsets: torch.Tensor  # [natom + 1] int32 CSR offsets
     config: torch.Tensor   # [natom] configuration of each atom
+    # for sums in a fixed order (no atomics): bonds per centre atom, the
+    # bonds ordered by neighbour atom (a stable sort) with their counts, and
+    # bonds per configuration (the bonds of configuration c are contiguous)
+    count_i: torch.Tensor = None
+    perm_j: torch.Tensor = None
+    count_j: torch.Tensor = None
+    count_config: torch.Tensor = None
+
+    def sum_by_i(self, x: torch.Tensor) -> torch.Tensor:
+        """Per centre atom, the sum of x over its bonds, in bond order."""
+        return torch.segment_reduce(x, "sum", lengths=self.count_i, axis=0)
+
+    def sum_by_j(self, x: torch.Tensor) -> torch.Tensor:
+        """Per atom, the sum of x over the bonds that have it as neighbour, in
+        bond order."""
+        return torch.segment_reduce(x[self.perm_j], "sum", lengths=self.count_j, axis=0)
+
+    def sum_by_config(self, x: torch.Tensor) -> torch.Tensor:
+        return torch.segment_reduce(x, "sum", lengths=self.count_config, axis=0)
 
 
 def _image_range(cell: torch.Tensor, pbc, rcut: float) -> list[int]:
@@ -94,7 +113,10 @@ def batch_bonds(configs, rcut: float) -> Bonds:
     counts = torch.bincount(i, minlength=natom)
     offsets = torch.zeros(natom + 1, dtype=torch.int32, device=i.device)
     offsets[1:] = torch.cumsum(counts, 0).to(torch.int32)
-    return Bonds(i=i, j=j, shift=shift, offsets=offsets, config=torch.cat(cfg))
+    config = torch.cat(cfg)
+    return Bonds(i=i, j=j, shift=shift, offsets=offsets, config=config, count_i=counts,
+                 perm_j=torch.argsort(j, stable=True), count_j=torch.bincount(j, minlength=natom),
+                 count_config=torch.bincount(config[i], minlength=len(configs)))
 
 
 def bond_vectors(x: torch.Tensor, cells: torch.Tensor, b: Bonds) -> torch.Tensor:
@@ -153,6 +175,27 @@ class LibraryEvaluator:
         lib.device_status()
         return B
 
+    def descriptors_tangent(self, offsets, r, e, magj, mhj, magi, mhi, dd, dmj, dmi):
+        """(B, dB [N, ncoef], core, dcore [N]) along the tangents dd (bond
+        vectors), dmj and dmi (moments)."""
+        natom, nei = magi.shape[0], r.shape[0]
+        dev = r.device
+        B = torch.empty(natom, self.ncoef, dtype=torch.float64, device=dev)
+        Bd = torch.empty_like(B)
+        core = torch.empty(natom, dtype=torch.float64, device=dev)
+        cored = torch.empty_like(core)
+        st, s = self._stream(dev)
+        ptr = lambda t: t.data_ptr() if t.numel() else 0
+        lib.descriptors_tangent_device(natom, nei, ptr(offsets), ptr(r), ptr(e), ptr(magj), ptr(mhj), ptr(magi),
+                                       ptr(mhi), ptr(dd), ptr(dmj), ptr(dmi), ptr(B), ptr(Bd), ptr(core),
+                                       ptr(cored), s)
+        st.synchronize()
+        lib.device_status()
+        return B, Bd, core, cored
+
+    def embedding(self) -> dict:
+        return lib.embedding()
+
     def get_coefficients(self) -> np.ndarray:
         return lib.get_coefficients()
 
@@ -205,24 +248,125 @@ class MagAceEnergy(torch.autograd.Function):
         gE = gE.to(torch.float64)
         gi = gE[b.i][:, None]
         gpos = gmom = gcell = gcoef = None
+        # every sum runs over segments in a fixed order: the backward pass is
+        # bitwise reproducible (no floating-point atomics)
         if ctx.needs_input_grad[0]:
-            gpos = torch.zeros(ctx.shapes[0], dtype=torch.float64, device=fij.device)
-            gpos.index_add_(0, b.i, gi * fij)
-            gpos.index_add_(0, b.j, -gi * fij)
+            gpos = b.sum_by_i(gi * fij) - b.sum_by_j(gi * fij)
         if ctx.needs_input_grad[1]:
-            gmom = gE[:, None] * ti0
-            gmom = gmom.index_add(0, b.j, gi * tij)
+            gmom = gE[:, None] * ti0 + b.sum_by_j(gi * tij)
         if ctx.needs_input_grad[2]:
             # d_ij = x_i - x_j - n_ij h: dd_b/dh_kb = -n_k
             per_bond = -b.shift.to(torch.float64)[:, :, None] * (gi * fij)[:, None, :]
-            gcell = torch.zeros(ctx.shapes[1], dtype=torch.float64, device=fij.device)
-            gcell.index_add_(0, b.config[b.i], per_bond)
+            gcell = b.sum_by_config(per_bond)
         if ctx.needs_input_grad[3]:
             B = ctx.potential.evaluator.descriptors(*ctx.lib_inputs)
             nd = ctx.potential.ndensity
             w = gE[:, None] * dedrho[:, :nd]                                   # [N, nd]
             gcoef = (w.T @ B).reshape(nd, -1)
         return gpos, gmom, gcell, gcoef, None
+
+
+def _embed(nfemb: int, rho: torch.Tensor, wpre: float, mexp: float) -> torch.Tensor:
+    """The embedding F(rho) (src/forces.F90:1134-1266, nfemb 0-2), elementwise
+    in torch so that autograd gives F' and F''."""
+    if nfemb == 0:
+        return rho.clone()
+    w, eps = 10.0, 1e-10
+    s = 1.0 + rho if nfemb == 2 else rho
+    small = s.abs() <= eps
+    ss = torch.where(small, torch.ones_like(s), s)
+    y1 = w * ss * ss
+    g = torch.where(y1 > 30.0, torch.zeros_like(y1), torch.exp(-torch.clamp(y1, max=30.0)))
+    a = ss.abs()
+    sg = torch.sign(ss)
+    big = sg * (torch.pow((1.0 - g) * a, mexp) + mexp * g * a)
+    big = wpre * (big - 1.0) if nfemb == 2 else wpre * big
+    lin = wpre * mexp * (s - 1.0) if nfemb == 2 else wpre * mexp * rho
+    return torch.where(small, lin, big)
+
+
+def _fcut(e: torch.Tensor, ecut: float, decut: float) -> torch.Tensor:
+    """The inner cutoff on the core energy (src/forces.F90:1112-1128)."""
+    elow = ecut - decut
+    mid = 0.5 * (1.0 + torch.cos(math.pi * (e - elow) / decut))
+    return torch.where(e >= ecut, torch.zeros_like(e), torch.where(e <= elow, torch.ones_like(e), mid))
+
+
+class MagAceForces(torch.autograd.Function):
+    """Per-atom energies E [N], forces F [N,3] = -dE_tot/dx and magnetic
+    forces FM [N,3] = -dE_tot/dm of a batch of configurations, differentiable
+    with respect to the coefficients: the gradient of any loss on E, F and FM
+    for fitting (src/modules.F90:57-72 weights energies and forces in the
+    reference's fitting loss).
+
+    With u = dL/dF and v = dL/dFM per atom, the force terms of dL/dc are
+    -d/de [dE_tot/dc] along the displacement (x + e u, m + e v); with
+    E_i = fcut(e_core,i) sum_d F_d(rho_id) + e_core,i and rho_id = c_d . B_i,
+      dL/dc_d = sum_i gE_i fcut F_d' B_i
+                - sum_i [fcut' de_core,i F_d' B_i + fcut (F_d'' drho_id B_i + F_d' dB_i)],
+    where dB_i, drho_id and de_core,i are the directional derivatives that
+    ace_descriptors_tangent_device evaluates (forward mode, exact). Gradients
+    with respect to positions, moments and cells (second derivatives of the
+    energy) are not provided."""
+
+    @staticmethod
+    def forward(ctx, positions, moments, cells, coeffs, potential):
+        potential._sync_coefficients(coeffs)
+        b = potential._bonds
+        d, r, e, magj, mhj, magi, mhi = _inputs(positions.detach(), moments.detach(), cells.detach(), b)
+        E, fij, tij, ti0, dedrho = potential.evaluator.evaluate(b.offsets, r, e, magj, mhj, magi, mhi)
+        F = b.sum_by_j(fij) - b.sum_by_i(fij)      # -dE_tot/dx
+        FM = -(ti0 + b.sum_by_j(tij))              # -dE_tot/dm
+        ctx.potential = potential
+        ctx.bonds = b
+        ctx.lib_inputs = (b.offsets, r, e, magj, mhj, magi, mhi)
+        ctx.save_for_backward(coeffs.detach().to(torch.float64))
+        return E, F, FM
+
+    @staticmethod
+    @torch.autograd.function.once_differentiable
+    def backward(ctx, gE, gF, gFM):
+        if any(ctx.needs_input_grad[:3]):
+            raise NotImplementedError("MagAceForces differentiates with respect to the coefficients only")
+        gcoef = None
+        if ctx.needs_input_grad[3]:
+            (c,) = ctx.saved_tensors
+            b = ctx.bonds
+            pot = ctx.potential
+            offsets, r, e, magj, mhj, magi, mhi = ctx.lib_inputs
+            dev = r.device
+            z3 = lambda n: torch.zeros(n, 3, dtype=torch.float64, device=dev)
+            u = gF.to(torch.float64) if gF is not None else z3(magi.shape[0])
+            v = gFM.to(torch.float64) if gFM is not None else z3(magi.shape[0])
+            gE = gE.to(torch.float64) if gE is not None else torch.zeros(magi.shape[0], dtype=torch.float64,
+                                                                        device=dev)
+            # tangents: bond vectors d_ij = x_i - x_j - n h move by u_i - u_j
+            dd = (u[b.i] - u[b.j]).contiguous()
+            dmj = v[b.j].contiguous()
+            B, Bd, core, cored = pot.evaluator.descriptors_tangent(offsets, r, e, magj, mhj, magi, mhi, dd, dmj,
+                                                                   v.contiguous())
+            emb = pot.evaluator.embedding()
+            c = c.to(dev)
+            rho = B @ c.T                                     # [N, nd]
+            rhod = Bd @ c.T
+            # F', F'' and fcut' by autograd of the elementwise functions (the
+            # backward pass runs with gradients off)
+            with torch.enable_grad():
+                rr = rho.detach().clone().requires_grad_(True)
+                Fsum = sum(_embed(emb["nfemb"], rr[:, k], float(emb["par"][0][k]), float(emb["par"][1][k])).sum()
+                           for k in range(rho.shape[1]))
+                (dF,) = torch.autograd.grad(Fsum, rr, create_graph=True)            # F_d'(rho_id)
+                d2F = torch.stack([torch.autograd.grad(dF[:, k].sum(), rr, retain_graph=True)[0][:, k]
+                                   for k in range(rho.shape[1])], dim=1)        # F_d''(rho_id)
+                ee = core.detach().clone().requires_grad_(True)
+                fc = _fcut(ee, emb["ecut"], emb["decut"])
+                (dfc,) = torch.autograd.grad(fc.sum(), ee)
+            dF, d2F, fc = dF.detach(), d2F.detach(), fc.detach()
+            w_e = (gE * fc)[:, None] * dF                                        # [N, nd]
+            w_b = (dfc * cored)[:, None] * dF + fc[:, None] * d2F * rhod
+            w_bd = fc[:, None] * dF
+            gcoef = (w_e - w_b).T @ B - w_bd.T @ Bd
+        return None, None, None, gcoef, None
 
 
 class MagAcePotential:
@@ -262,10 +406,19 @@ class MagAcePotential:
             coeffs = self.coefficients(device=positions.device)
         return MagAceEnergy.apply(positions, moments, cells, coeffs, self)
 
+    def forces(self, positions, moments, cells, pbcs, natoms, coeffs=None, rebuild: bool = True):
+        """(E [N], F [N,3], FM [N,3]): per-atom energies, forces -dE_tot/dx and
+        magnetic forces -dE_tot/dm, differentiable with respect to coeffs
+        (MagAceForces), for fitting on forces."""
+        if rebuild or self._bonds is None:
+            self._bonds = self.build_bonds(positions, cells, pbcs, natoms)
+        if coeffs is None:
+            coeffs = self.coefficients(device=positions.device)
+        return MagAceForces.apply(positions, moments, cells, coeffs, self)
+
     def config_energies(self, positions, moments, cells, pbcs, natoms, coeffs=None) -> torch.Tensor:
         E = self.energies(positions, moments, cells, pbcs, natoms, coeffs)
-        out = torch.zeros(len(natoms), dtype=E.dtype, device=E.device)
-        return out.index_add(0, self._bonds.config, E)
+        return torch.segment_reduce(E, "sum", lengths=torch.tensor(natoms, device=E.device), axis=0)
 
     def virial(self, positions, moments, cells, pbcs, natoms) -> torch.Tensor:
         """Per-configuration virial W_ab = -sum_bonds d_a dE/dd_b [C,3,3]
@@ -275,5 +428,4 @@ class MagAcePotential:
         self._bonds = b
         d, r, e, magj, mhj, magi, mhi = _inputs(positions.detach(), moments.detach(), cells.detach(), b)
         _, fij, _, _, _ = self.evaluator.evaluate(b.offsets, r, e, magj, mhj, magi, mhi)
-        W = torch.zeros(len(natoms), 3, 3, dtype=torch.float64, device=fij.device)
-        return W.index_add(0, b.config[b.i], -d[:, :, None] * fij[:, None, :])
+        return b.sum_by_config(-d[:, :, None] * fij[:, None, :])

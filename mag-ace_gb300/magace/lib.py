@@ -62,6 +62,8 @@ SIGNATURES = {
     "ace_set_coefficients": (_i, [_pd]),
     "ace_descriptors_device": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ace_density_gradient_device": (_i, [_i, _vp, _vp]),
+    "ace_descriptors_tangent_device": (_i, [_i, _i] + [_vp] * 14 + [_vp]),
+    "ace_embedding": (_i, [_pi, _pd, _pd]),
 }
 
 _lib = None
@@ -234,6 +236,23 @@ def set_coefficients(c) -> None:
 def descriptors_device(natom, nei, off, r, e, magj, mhj, magi, mhi, B, stream=0) -> None:
     """B[natom, ncoef] (FP64, device address) for the given device arrays."""
     _check(load().ace_descriptors_device(natom, nei, off, r, e, magj, mhj, magi, mhi, B, stream))
+
+
+def descriptors_tangent_device(natom, nei, off, r, e, magj, mhj, magi, mhi, dd, dmj, dmi, B, Bdot, core, cored,
+                               stream=0) -> None:
+    """B and dB along the tangents dd (bond vectors), dmj, dmi (moments), and
+    the core energy with its derivative; all device addresses, FP64."""
+    _check(load().ace_descriptors_tangent_device(natom, nei, off, r, e, magj, mhj, magi, mhi, dd, dmj, dmi, B, Bdot,
+                                                 core, cored, stream))
+
+
+def embedding() -> dict:
+    """nfemb, par[order][density] and the inner cutoff (ecut, decut)."""
+    n = ctypes.c_int()
+    par = np.zeros(4)
+    cut = np.zeros(2)
+    _check(load().ace_embedding(ctypes.byref(n), _dp(par), _dp(cut)))
+    return {"nfemb": n.value, "par": par.reshape(2, 2), "ecut": float(cut[0]), "decut": float(cut[1])}
 
 
 def density_gradient_device(natom, dedrho, stream=0) -> None:

@@ -32,7 +32,7 @@ class OracleEvaluator:
         self.path = potfile
         self.o = orc.Oracle(potfile, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)
         lib.init(potfile, "Fe", 5.0, 4.0, 0.2, 1)  # host-only: coefficient order and rows
-        self.rows = {r: lib.basis_rows(r) for r in (1, 2, 3, 4)}
+        self.rows = {r: lib.basis_rows(r) for r in (1, 2, 3, 4, 5, 6)}
         self.coef = lib.get_coefficients()
         self.generation = 0
 
@@ -266,9 +266,9 @@ def test_gpu_batch_forces_match_oracle(nonlinear_potential, precision):
 def test_gpu_gradcheck_all_inputs(nonlinear_potential):
     """gradcheck (FP64 path) of positions, moments and cell of a 54-atom
     configuration (steps as in _gradcheck_all), and of the coefficients
-    along random directions (h = 1e-5).
-    The backward scatter adds per-bond terms with atomics on the GPU, so two
-    backward passes may differ in the last bits (nondet_tol)."""
+    along random directions (h = 1e-5). The backward pass sums per-bond terms
+    over segments in a fixed order, so gradcheck's repeated backward passes
+    agree bit for bit (nondet_tol 0)."""
     from magace import autograd as AG, lib
     lib.init(nonlinear_potential, "Fe", 5.0, 4.0, 0.2, 1)
     lib.set_precision(0)
@@ -278,8 +278,73 @@ def test_gpu_gradcheck_all_inputs(nonlinear_potential):
     x.requires_grad_(True)
     m.requires_grad_(True)
     cells.requires_grad_(True)
-    _gradcheck_all(pot, x, m, cells, pbcs, nat, pot.coefficients(device=dev), nondet_tol=1e-12)
+    _gradcheck_all(pot, x, m, cells, pbcs, nat, pot.coefficients(device=dev), nondet_tol=0.0)
     c = pot.coefficients(device=dev, requires_grad=True)
     x0, m0, h0 = x.detach(), m.detach(), cells.detach()
     fc = lambda c_: pot.energies(x0, m0, h0, pbcs, nat, c_)
-    assert torch.autograd.gradcheck(fc, (c,), eps=1e-5, atol=1e-6, rtol=1e-5, fast_mode=True, nondet_tol=1e-12)
+    assert torch.autograd.gradcheck(fc, (c,), eps=1e-5, atol=1e-6, rtol=1e-5, fast_mode=True, nondet_tol=0.0)
+
+
+def test_embedding_derivatives_match_oracle(nonlinear_potential, oracle_seeded):
+    """The torch restatement of the embedding (autograd._embed) gives the
+    oracle's dE/drho (src/forces.F90:1134-1266) for the non-linear
+    embedding, over densities of both signs and near zero."""
+    import oracle as orc
+    from magace import autograd as AG, structures as S
+    o = orc.Oracle(nonlinear_potential, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)
+    nb = S.neighbor_data(S.bcc_fe_54(21), 5.0)
+    B, dedrho = o.descriptors(nb)
+    from magace import lib
+    lib.init(nonlinear_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    c = lib.get_coefficients()
+    emb = lib.embedding()
+    assert emb["nfemb"] == 1 and emb["par"][1][0] == 0.5
+    rho = torch.tensor(B @ c[0], requires_grad=True)
+    F = AG._embed(emb["nfemb"], rho, float(emb["par"][0][0]), float(emb["par"][1][0]))
+    (dF,) = torch.autograd.grad(F.sum(), rho)
+    assert rel_err(dF.numpy(), dedrho[:, 0]) < 1e-12
+    assert (rho.detach().numpy() < 0).any() and (rho.detach().numpy() > 0).any()
+
+
+def _force_loss_gradcheck(potfile):
+    """gradcheck, along random directions, of the coefficients' gradient of
+    E, F and FM (MagAceForces) and of a squared force loss."""
+    from magace import autograd as AG, lib
+    lib.init(potfile, "Fe", 5.0, 4.0, 0.2, 1)
+    lib.set_precision(0)
+    dev = torch.device("cuda", 0)
+    pot = AG.MagAcePotential(AG.LibraryEvaluator())
+    x, m, cells, pbcs, nat = _bcc_batch([3], [5], device=dev)
+    pot._bonds = pot.build_bonds(x, cells, pbcs, nat)
+    c = pot.coefficients(device=dev, requires_grad=True)
+    f = lambda c_: pot.forces(x, m, cells, pbcs, nat, c_, rebuild=False)
+    assert torch.autograd.gradcheck(f, (c,), eps=1e-5, atol=1e-6, rtol=1e-5, fast_mode=True, nondet_tol=0.0)
+    E0, F0, FM0 = (t.detach() for t in f(c.detach()))
+    rng = np.random.default_rng(1)
+    Fref = F0 + torch.tensor(rng.normal(0, 0.05, F0.shape), device=dev)
+    Mref = FM0 + torch.tensor(rng.normal(0, 0.05, FM0.shape), device=dev)
+
+    def loss(c_):
+        E, F, FM = pot.forces(x, m, cells, pbcs, nat, c_, rebuild=False)
+        return ((F - Fref) ** 2).sum() + 0.3 * ((FM - Mref) ** 2).sum() + 0.1 * E.sum() ** 2
+
+    assert torch.autograd.gradcheck(loss, (c,), eps=1e-5, atol=1e-6, rtol=1e-5, fast_mode=True, nondet_tol=0.0)
+    # bitwise-reproducible backward
+    g1 = torch.autograd.grad(loss(c), c)[0]
+    g2 = torch.autograd.grad(loss(c), c)[0]
+    assert torch.equal(g1, g2)
+    assert g1.abs().max() > 0
+
+
+@pytest.mark.gpu
+def test_gpu_force_loss_coefficient_gradients(nonlinear_potential):
+    """Fitting on forces: d(loss on E, F, FM)/dc through the forward-mode
+    tangents of the descriptors, against centred differences (h = 1e-5),
+    with a non-linear embedding (exponent 0.5)."""
+    _force_loss_gradcheck(nonlinear_potential)
+
+
+@pytest.mark.gpu
+def test_gpu_force_loss_coefficient_gradients_high_body(high_potential):
+    """The same with 5- and 6-body clusters (six-factor descriptor tangents)."""
+    _force_loss_gradcheck(high_potential)
