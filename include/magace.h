@@ -193,12 +193,13 @@ int ace_set_work_queue(int on);
 
 /* Autotuner (no counterpart in the reference): evaluates the given system
  * (same arrays as ace_compute_device) with every variant of the
- * split-precision kernels' CTA shapes (warps per CTA of the 2-/4-body and the
- * 3-body density kernels; CTAs per SM the force kernel's registers allow),
- * times each kernel with CUDA events and keeps each kernel's fastest variant
- * for later evaluations. Writes the choices. Synchronous. Results do not
- * change beyond the FP32 rounding order of the 3-body kernel. For the FP64
- * path or another basis layout it only reports the current choice. */
+ * split-precision kernels (CTA shapes of the A-basis, 2-/4-body and 3-body
+ * density kernels; the force kernel's CTAs per SM and its FP32 or
+ * tensor-core form), times each kernel with CUDA events and keeps each
+ * kernel's fastest variant for later evaluations. Writes the choices.
+ * Synchronous. Results change only within FP32 rounding (the 3-body sums'
+ * order; the tensor-core products' 3xTF32 split, below 2^-20 relative). For
+ * the FP64 path or another basis layout it only reports the current choice. */
 int ace_autotune_device(int natom, int nei, const int* bond_offset, const double* r, const double* e,
                         const double* mag_j, const double* mhat_j, const double* mag_i,
                         const double* mhat_i, void* stream, int* rest_warps, int* b3_warps,
@@ -211,13 +212,16 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
  * 32/16 warps reading record streams by shuffles, 4/5: through shared
  * memory), 3-body (0-2: 16/12/8 warps, 3: 12
  * warps with the n0' loop outermost, 4/5: 16/12 warps packed FP32x2), forces
- * (0-2: 4/6/8 CTAs per SM, 3-5: the same packed FP32x2). */
+ * (0-2: 4/6/8 CTAs per SM, 3-5: the same packed FP32x2, 6/7: 5/6 CTAs per SM
+ * with the contractions as GEMMs on the tensor cores, mma.sync TF32 in the
+ * 3xTF32 split). Until the autotuner or ace_set_tuning chooses, the variants
+ * are {3, 4, 4, 6}, the fastest on a 15,840-atom bcc Fe workload. */
 int ace_get_tuning(int* variants);
 
 /* Selects the kernel variants directly (no counterpart in the reference):
  * variants[4] as ace_get_tuning reports them; an index out of a kernel's
- * range is an error (MAGACE_ERR_ARGS). Results do not change beyond the FP32
- * rounding order of the 3-body kernel. */
+ * range is an error (MAGACE_ERR_ARGS). Results change only within FP32
+ * rounding (the 3-body sums' order, the tensor-core products' split). */
 int ace_set_tuning(const int* variants);
 
 /* ---- Differentiation and fitting (no counterpart in the reference's

@@ -77,7 +77,9 @@ struct Runtime {
   bool overlap = true;  // MAGACE_OVERLAP=0 keeps every kernel on the launch stream
   int last_natom = -1;  // atoms of the last evaluation (ace_density_gradient_device)
   bool work_queue = false;  // neighbour-count-sorted work queue
-  int tune_abasis = 0, tune_rest = 0, tune_b3 = 0, tune_forces = 0;  // kernel variants (ace_autotune_device)
+  // kernel variants (ace_autotune_device, ace_set_tuning)
+  int tune_abasis = kDefaultTuning[0], tune_rest = kDefaultTuning[1], tune_b3 = kDefaultTuning[2],
+      tune_forces = kDefaultTuning[3];
   DevBuf<int> order, queue_bins;
 
   // device tables

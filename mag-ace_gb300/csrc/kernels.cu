@@ -981,13 +981,17 @@ bool use_specialised(const DeviceModel& m) {
 // device and size: the attribute call is skipped when a launch needs no more
 // than was already set, so evaluations captured into a CUDA graph issue none.
 template <class K>
-void set_smem(K* kernel, size_t bytes) {
+void set_smem(K* kernel, size_t bytes, bool max_carveout = false) {
   static std::map<std::pair<const void*, int>, size_t> done;
   int dev = 0;
   cudaGetDevice(&dev);
   size_t& cur = done[{reinterpret_cast<const void*>(kernel), dev}];
   if (bytes > cur) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    // all of the unified L1 as shared memory, so that the CTAs per SM the
+    // kernel's registers allow also fit its shared memory
+    if (max_carveout)
+      cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     cur = bytes;
   }
 }
@@ -1315,21 +1319,42 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
   } else {                                    \
     MAGACE_FORCES_SO(MB, PK, false);          \
   }
+    // the contractions on the tensor cores (k_forces_tc, split precision only)
+#define MAGACE_FORCES_TC_SO(MB, SO)                                                                                 \
+  {                                                                                                                 \
+    const size_t s3 = forces_tc_smem<FeDims>(SO);                                                                   \
+    set_smem(k_forces_tc<FeDims, MB, SO>, s3, true);                                                                \
+    k_forces_tc<FeDims, MB, SO><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,      \
+                                                      reinterpret_cast<const C<float>*>(b.W), b.edf, b.dedrho,      \
+                                                      b.fij, b.tij, b.ti0, static_cast<const float*>(b.stage),      \
+                                                      b.err, g3);                                                   \
+  }
+#define MAGACE_FORCES_TC(MB)                  \
+  if (b.host_outputs) {                       \
+    MAGACE_FORCES_TC_SO(MB, true);            \
+  } else {                                    \
+    MAGACE_FORCES_TC_SO(MB, false);           \
+  }
     if constexpr (sizeof(R) == 8) {
       MAGACE_FORCES(4, false);
     } else {
-      // variants: CTAs per SM 4 / 6 / 8, scalar then packed FP32x2
+      // variants: CTAs per SM 4 / 6 / 8, scalar then packed FP32x2; then
+      // the tensor-core form at 5 / 6 CTAs per SM
       switch (m.tune_forces) {
         case 1: MAGACE_FORCES(6, false); break;
         case 2: MAGACE_FORCES(8, false); break;
         case 3: MAGACE_FORCES(4, true); break;
         case 4: MAGACE_FORCES(6, true); break;
         case 5: MAGACE_FORCES(8, true); break;
+        case 6: MAGACE_FORCES_TC(5); break;
+        case 7: MAGACE_FORCES_TC(6); break;
         default: MAGACE_FORCES(4, false); break;
       }
     }
 #undef MAGACE_FORCES
 #undef MAGACE_FORCES_SO
+#undef MAGACE_FORCES_TC
+#undef MAGACE_FORCES_TC_SO
   } else {
     const size_t s3 = forces_smem<R>(m, kForceThreads);
     set_smem(k_forces<R>, s3);
@@ -1375,7 +1400,7 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
       const size_t a = density_fe_smem(m, 32), b = b3_fe_smem<FeDims>(m, 16);
       return a > b ? a : b;
     }
-    return forces_fe_smem<float, FeDims>(true);
+    return std::max(forces_fe_smem<float, FeDims>(true), forces_tc_smem<FeDims>(true));
   }
   if (precision == 0) {
     if (which == 0) return abasis_smem<double>(m);

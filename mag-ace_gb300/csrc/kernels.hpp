@@ -26,8 +26,15 @@ constexpr int kRestWarpChoices[6] = {32, 16, 32, 16, 32, 16};
 // (b3 variants 3: n0' loop outermost; 4 and 5: packed FP32x2 arithmetic)
 constexpr int kB3WarpChoices[6] = {16, 12, 8, 12, 16, 12};
 // CTAs per SM the split-precision force kernel's registers must allow, for
-// its scalar (variants 0-2) and packed FP32x2 (3-5) forms (DeviceModel::tune_forces)
-constexpr int kForceMinBlocksChoices[6] = {4, 6, 8, 4, 6, 8};
+// its scalar (variants 0-2) and packed FP32x2 (3-5) forms, and for the form
+// with its contractions on the tensor cores (6-7) (DeviceModel::tune_forces)
+constexpr int kForceMinBlocksChoices[8] = {4, 6, 8, 4, 6, 8, 5, 6};
+// the variants used until ace_autotune_device or ace_set_tuning picks
+// others: the fastest on a 15,840-atom bcc Fe workload (A basis with
+// bulk-copied bond tiles on a persistent grid where the inputs are in device
+// memory, record streams through shared memory, packed FP32x2 3-body sums,
+// force contractions on the tensor cores)
+constexpr int kDefaultTuning[4] = {3, 4, 4, 6};
 
 // Device arrays of one evaluation. F and W are complex arrays of the selected
 // precision (FP64: 16 bytes per entry, FP32: 8 bytes).

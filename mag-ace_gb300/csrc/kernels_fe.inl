@@ -2004,6 +2004,478 @@ __global__ void __launch_bounds__(64, MINB)
   }
 }
 
+// ===========================================================================
+// k_forces_tc (split precision): the contractions of k_forces_fe as GEMMs on
+// the tensor cores (mma.sync m16n8k8 TF32 in the 3xTF32 split: each FP32
+// operand x = hi + lo with hi, lo TF32, products lo*hi + hi*lo + hi*hi
+// accumulated in FP32, so the error stays near FP32's), per 64-bond tile of
+// one atom, bonds as the M dimension, one warp per 32 bonds (two m16 tiles):
+//   F1  sp[b][n]         = sum_K Q[b][K] B1[K][n]    K = 64 (Re, Im of q_k), N = 16
+//   F2  U[b][2i + c]     = sum_K Q[b][K] B2[K][..]   K = 40 (Re, Im of q_k, k < NQ3), N = 32
+//   T   V[b][2k + c]     = sum_K G[b][K] B3[K][..]   K = 48 (g_n, Re, Im of RY_i), N = 64
+// with q_k = M_nl(|m_j|) Y_lm(m-hat_j) (m >= 0), RY_i = R_nl(r) Y_lm(e) and
+// B1..B3 the atom's weights (dE/drho (W + g3)) laid out as the real GEMMs of
+// the complex products: sp_n = Re sum_k W2[n][k] q_k, U_i = sum_k W_A[i][k] q_k,
+// V_k = sum_n g_n W2[n][k] + sum_i W_A[i][k] RY_i. The weights are arranged
+// once per atom in the order of the B fragments; each warp's Q and G rows and
+// its D results share one shared-memory row per bond. The per-bond features
+// stay in the registers of the bond's thread; the epilogues (f_ij from sp and
+// U, t_ij from V) are k_forces_fe's.
+//
+// Q row columns: Re q_k (k < 18), Im q_k (k < 18), Re q_k (k >= 18), Im q_k
+// (k >= 18), four zeros; G row: g_n, Re RY_i, Im RY_i.
+constexpr int kTcRow = 68;      // floats per bond row (64 + 4: conflict-free fragment loads)
+constexpr int kTcF1 = 8 * 2;    // B fragments of F1 (k-steps x n-tiles)
+constexpr int kTcF2 = 5 * 4;    // of F2
+constexpr int kTcT = 5 * 6 + 3 * 2;  // of T (n-tiles 5-7 hold k >= 20 only: the 2 k-steps of g)
+constexpr int kTcFrags = kTcF1 + kTcF2 + kTcT;
+
+// x = hi + lo: hi the TF32 truncation of x (its low 13 mantissa bits
+// cleared), lo = x - hi exactly (|lo| < 2^-10 |x|; the tensor cores read its
+// TF32 part, so the products' error is below 2^-20 relative)
+__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
+  hi = __float_as_uint(x) & 0xffffe000u;
+  lo = __float_as_uint(x - __uint_as_float(hi));
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+// d += a b in the 3xTF32 split (small terms first)
+__device__ __forceinline__ void mma_3xtf32(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
+                                           uint32_t bh0, uint32_t bh1, uint32_t bl0, uint32_t bl1) {
+  mma_tf32(d, al, bh0, bh1);
+  mma_tf32(d, ah, bl0, bl1);
+  mma_tf32(d, ah, bh0, bh1);
+}
+
+template <class D>
+size_t forces_tc_smem(bool sout) {
+  return sizeof(float2) * kTcFrags * 32 + sizeof(C<float>) * 32 + sizeof(float) * 64 * kTcRow +
+         (sout ? sizeof(double) * 6 * 64 : 0);
+}
+
+template <class D, int MINB, bool SOUT>
+__global__ void __launch_bounds__(64, MINB)
+    k_forces_tc(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
+                const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
+                const double* __restrict__ magi, const double* __restrict__ mhi, const C<float>* __restrict__ W,
+                const double* __restrict__ edf_in, const double* __restrict__ dedrho, double* __restrict__ fij,
+                double* __restrict__ tij, double* __restrict__ ti0, const float* __restrict__ stage, int* err,
+                const C<float>* __restrict__ g3) {
+  using R = float;
+  constexpr int T = 64;
+  static_assert(D::NQ3 == 18 && D::NQ == 30 && D::NB == 16 && D::NRY == 16 && D::H3 == D::H2,
+                "fragment shapes assume the Fe layout");
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* Bf = reinterpret_cast<float2*>(smem);                       // [kTcFrags][32 lanes]
+  C<float>* W0s = reinterpret_cast<C<float>*>(Bf + kTcFrags * 32);   // [32]
+  float* QA = reinterpret_cast<float*>(W0s + 32);                     // [64 bonds][kTcRow]
+  double* sOut = reinterpret_cast<double*>(QA + 64 * kTcRow);  // SOUT: f_ij [T][3], then t_ij [T][3]
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31, gid = lane >> 2, tig = lane & 3;
+  const uint64_t pol_first = l2_evict_first();
+
+  for (int it = blockIdx.x; it < natom; it += gridDim.x) {
+    const int atom = queue_atom(m, it);
+    const C<float>* Wa = W + static_cast<size_t>(atom) * m.nW;
+    if (t == 0) {
+      // the weights of the atom a CTA starting about one CTA lifetime later
+      // takes (MINB CTAs per SM resident), into L2
+      unsigned nsm;
+      asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+      const int ahead = it + MINB * static_cast<int>(nsm);
+      if (ahead < natom) {
+        const int a2 = queue_atom(m, ahead);
+        const size_t wb = sizeof(C<float>) * static_cast<size_t>(m.nW);
+        if (wb % 16 == 0) bulk_prefetch_l2(W + static_cast<size_t>(a2) * m.nW, static_cast<uint32_t>(wb));
+        const size_t gb = sizeof(C<float>) * static_cast<size_t>(m.b3_nc);
+        if (g3 && gb % 16 == 0) bulk_prefetch_l2(g3 + static_cast<size_t>(a2) * m.b3_nc, static_cast<uint32_t>(gb));
+      }
+    }
+    // the weight is dE/drho (W + g3): W the 2-/4-body part, g3 [atom][nc]
+    // the 3-body part per compact element c (-1: none)
+    const C<float>* Ga = g3 ? g3 + static_cast<size_t>(atom) * m.b3_nc : nullptr;
+    const R sc = g3 ? to_r<R>(dedrho[static_cast<size_t>(atom) * 2]) : R(1);
+    const auto weight = [&](int w, int c) {
+      C<R> v = ld_l2(Wa + w, pol_first);
+      if (Ga) {
+        if (c >= 0) {
+          const C<float> gv = ld_l2(Ga + c, pol_first);
+          v.x += gv.x;
+          v.y += gv.y;
+        }
+        v.x *= sc;
+        v.y *= sc;
+      }
+      return v;
+    };
+    // the B fragments: lane L of fragment (k-step s, n-tile u) holds
+    // B[8 s + L % 4][8 u + L / 4] and B[8 s + L % 4 + 4][8 u + L / 4]. Each
+    // weight goes to its places in F1 and T (W2[n][k]) or F2 and T
+    // (W_A[i][k]); the padding places stay zero.
+    // (the weights are staged in the rows' space first, then scattered)
+    C<R>* raw = reinterpret_cast<C<R>*>(QA);  // W2[n][k], then W_A[i][k]
+    static_assert(sizeof(C<R>) * (D::NA2H + D::NWA) <= sizeof(float) * 64 * kTcRow, "the weights fit in the rows");
+    for (int q = t; q < D::NA2H; q += T) raw[q] = weight(m.offW2 + q, -1);
+    for (int q = t; q < D::NWA; q += T) raw[D::NA2H + q] = weight(q, q);
+    if (t < D::NQ) W0s[t] = weight(m.offW0 + t, Ga ? __ldg(m.b3_cw + m.offW0 + t) : -1);
+    float* Bs = reinterpret_cast<float*>(Bf);
+    for (int q = t; q < kTcFrags * 16; q += T) reinterpret_cast<float4*>(Bs)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const auto place = [&](int f, int K, int n) { return f * 64 + ((n & 7) * 4 + (K & 3)) * 2 + ((K >> 2) & 1); };
+    const auto put1 = [&](int K, int n, float v) { Bs[place((K >> 3) * 2 + (n >> 3), K, n)] = v; };
+    const auto put2 = [&](int K, int n, float v) { Bs[place(kTcF1 + (K >> 3) * 4 + (n >> 3), K, n)] = v; };
+    const auto put3 = [&](int K, int n, float v) {
+      const int u = n >> 3, sk = K >> 3;
+      Bs[place(kTcF1 + kTcF2 + (u < 5 ? 6 * u + sk : 30 + 2 * (u - 5) + sk), K, n)] = v;
+    };
+#pragma unroll 1
+    for (int q = t; q < D::NA2H; q += T) {
+      const C<R> w = raw[q];
+      const int n = q / D::NQ, k = q % D::NQ;
+      put1(k < D::NQ3 ? k : D::NQ3 + k, n, w.x);            // Re q_k column
+      put1(k < D::NQ3 ? D::NQ3 + k : D::NQ + k, n, -w.y);   // Im q_k column
+      put3(n, 2 * k, w.x);
+      put3(n, 2 * k + 1, w.y);
+    }
+#pragma unroll 1
+    for (int q = t; q < D::NWA; q += T) {
+      const C<R> w = raw[D::NA2H + q];
+      const int i = q / D::NQ3, k = q % D::NQ3;
+      put2(k, 2 * i, w.x);
+      put2(D::NQ3 + k, 2 * i, -w.y);
+      put2(k, 2 * i + 1, w.y);
+      put2(D::NQ3 + k, 2 * i + 1, w.x);
+      put3(D::NB + i, 2 * k, w.x);
+      put3(D::NB + i, 2 * k + 1, w.y);
+      put3(D::NB + D::NRY + i, 2 * k, -w.y);
+      put3(D::NB + D::NRY + i, 2 * k + 1, w.x);
+    }
+    __syncthreads();  // the fragments are built; the rows are free
+    const R edf = to_r<R>(edf_in[atom]);
+    const int b0 = off[atom], b1 = off[atom + 1];
+    float* row = QA + t * kTcRow;                  // this thread's bond row
+    const float* wrows = QA + warp * 32 * kTcRow;  // the warp's 32 rows
+    for (int jt = b0; jt < b1; jt += T) {
+      const int j = jt + t;
+      const bool live = j < b1;
+      // ---- the bond's inputs, and its magnetic functions M_nl, M'_nl (kept
+      // in registers to the magnetic epilogue) with the Q row
+      R r = R(1), ex = R(0), ey = R(0), ez = R(1), mg = R(1), mx = R(0), my = R(0), mz = R(1);
+      R mv[D::NMF], Md[D::NMF];
+      {
+        if (live) {
+          if (stage) {  // the A-basis kernel's copy in device memory
+            R sp[8];
+            ld8_l2(stage + 8 * static_cast<size_t>(j), sp, pol_first);
+            r = sp[0];
+            ex = sp[1];
+            ey = sp[2];
+            ez = sp[3];
+            mg = sp[4];
+            mx = sp[5];
+            my = sp[6];
+            mz = sp[7];
+          } else {
+            r = to_r<R>(rr[j]);
+            ex = to_r<R>(ee[3 * j]);
+            ey = to_r<R>(ee[3 * j + 1]);
+            ez = to_r<R>(ee[3 * j + 2]);
+            mg = to_r<R>(magj[j]);
+            mx = to_r<R>(mhj[3 * j]);
+            my = to_r<R>(mhj[3 * j + 1]);
+            mz = to_r<R>(mhj[3 * j + 2]);
+          }
+        }
+        R wm = R(0);
+        const int nlm = live ? magnetic_bin_r<R>(m, mg, wm, err) : -1;
+        if (nlm > 0) {
+          lut_eval<true>(m.lut_m32, D::NFM, 0, D::NMF, nlm, wm, rscale_m<R>(m), mv, Md);
+        } else {
+#pragma unroll
+          for (int q = 0; q < D::NMF; ++q) {
+            mv[q] = R(nlm == 0 ? 1 : 0);
+            Md[q] = R(0);
+          }
+        }
+        // the Q row: q_k = M_{n, l(h)} Y_h(m-hat), k = n H2 + h, in the
+        // column order Re (k < 18), Im (k < 18), Re (k >= 18), Im (k >= 18), 0
+        C<R> Ym[D::H2];
+        ylm_half<R, false>(D::L2, mx, my, mz, Ym, nullptr);
+        const auto qcol = [&](int c) -> float {
+          const int k = c < 2 * D::NQ3 ? c % D::NQ3 : (c < D::NQ3 + D::NQ ? c - D::NQ3 : c - D::NQ);
+          const bool im = c < 2 * D::NQ3 ? c >= D::NQ3 : c >= D::NQ3 + D::NQ;
+          if (c >= 2 * D::NQ) return 0.f;
+          const int nr = k / D::H2, h = k % D::H2;
+          const R mq = mv[nr * (D::L2 + 1) + l_of_h(h)];
+          return im ? Ym[h].y * mq : Ym[h].x * mq;
+        };
+#pragma unroll
+        for (int c = 0; c < 2 * D::NQ + 4; c += 4)
+          *reinterpret_cast<float4*>(row + c) = make_float4(qcol(c), qcol(c + 1), qcol(c + 2), qcol(c + 3));
+      }
+      __syncwarp();
+      // ---- force GEMMs F1 (sp) and F2 (U) over the warp's two m16 tiles
+      {
+        float s1[2][2][4], s2[2][4][4];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              s2[a][u][e] = 0.f;
+              if (u < 2) s1[a][u][e] = 0.f;
+            }
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+          uint32_t ah[2][4], al[2][4];
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            const float* ra = wrows + (16 * a + gid) * kTcRow + 8 * s + tig;
+            tf32_split(ra[0], ah[a][0], al[a][0]);
+            tf32_split(ra[8 * kTcRow], ah[a][1], al[a][1]);
+            tf32_split(ra[4], ah[a][2], al[a][2]);
+            tf32_split(ra[8 * kTcRow + 4], ah[a][3], al[a][3]);
+          }
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const float2 bv = Bf[(2 * s + u) * 32 + lane];
+            uint32_t bh0, bl0, bh1, bl1;
+            tf32_split(bv.x, bh0, bl0);
+            tf32_split(bv.y, bh1, bl1);
+#pragma unroll
+            for (int a = 0; a < 2; ++a) mma_3xtf32(s1[a][u], ah[a], al[a], bh0, bh1, bl0, bl1);
+          }
+          if (s < 5) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float2 bv = Bf[(kTcF1 + 4 * s + u) * 32 + lane];
+              uint32_t bh0, bl0, bh1, bl1;
+              tf32_split(bv.x, bh0, bl0);
+              tf32_split(bv.y, bh1, bl1);
+#pragma unroll
+              for (int a = 0; a < 2; ++a) mma_3xtf32(s2[a][u], ah[a], al[a], bh0, bh1, bl0, bl1);
+            }
+          }
+        }
+        __syncwarp();  // every lane's Q fragments are read: the rows take the results
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          float* r0 = const_cast<float*>(wrows) + (16 * a + gid) * kTcRow + 2 * tig;
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            *reinterpret_cast<float2*>(r0 + 8 * u) = make_float2(s1[a][u][0], s1[a][u][1]);
+            *reinterpret_cast<float2*>(r0 + 8 * kTcRow + 8 * u) = make_float2(s1[a][u][2], s1[a][u][3]);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            *reinterpret_cast<float2*>(r0 + D::NB + 8 * u) = make_float2(s2[a][u][0], s2[a][u][1]);
+            *reinterpret_cast<float2*>(r0 + 8 * kTcRow + D::NB + 8 * u) = make_float2(s2[a][u][2], s2[a][u][3]);
+          }
+        }
+        __syncwarp();
+      }
+      // ---- the atomic functions g_n, R_nl and the core term with derivatives
+      R g[D::NB], gd[D::NB], tv[D::NR], td[D::NR], cdv = R(0);
+      {
+        R wl = R(0);
+        const int nla = live ? atomic_bin_r<R>(m, r, wl, err) : 0;
+        if (nla > 0) {
+          R cv[1], cd1[1];
+          lut_eval<true>(m.lut_a32, D::NFA, 0, D::NB, nla, wl, rscale_a<R>(m), g, gd);
+          lut_eval<true>(m.lut_a32, D::NFA, D::NB, D::NR, nla, wl, rscale_a<R>(m), tv, td);
+          lut_eval<true>(m.lut_a32, D::NFA, D::NB + D::NR, 1, nla, wl, rscale_a<R>(m), cv, cd1);
+          cdv = cd1[0];
+        } else {
+#pragma unroll
+          for (int q = 0; q < D::NB; ++q) g[q] = gd[q] = R(0);
+#pragma unroll
+          for (int q = 0; q < D::NR; ++q) tv[q] = td[q] = R(0);
+        }
+      }
+      // ---- force epilogue (k_forces_fe's): the row holds sp_n, then (Re U_i, Im U_i)
+      C<R> Ya[D::HA], dYa[D::HA][3];
+      ylm_half<R, true>(D::LA, ex, ey, ez, Ya, dYa);
+      if (live) {
+        R fr = edf * cdv, ft[3] = {R(0), R(0), R(0)};
+#pragma unroll
+        for (int n = 0; n < D::NB; n += 4) {
+          const float4 v = *reinterpret_cast<const float4*>(row + n);
+          fr = fma(gd[n], v.x, fr);
+          fr = fma(gd[n + 1], v.y, fr);
+          fr = fma(gd[n + 2], v.z, fr);
+          fr = fma(gd[n + 3], v.w, fr);
+        }
+        const R invr = rcp(r);
+#pragma unroll
+        for (int i = 0; i < D::NRY; i += 2) {
+          const float4 v = *reinterpret_cast<const float4*>(row + D::NB + 2 * i);
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const C<R> U = e ? C<R>{v.z, v.w} : C<R>{v.x, v.y};
+            const int ii = i + e, n1 = ii / D::LSA, lma = ii % D::LSA, l1 = l_of_lm(lma);
+            const int mm = lma - l1 * l1 - l1;
+            fr = fma(td[n1 * (D::LA + 1) + l1], re_mul(U, y_full(Ya, l1, mm)), fr);
+            const C<R> su = cscale(U, invr * tv[n1 * (D::LA + 1) + l1]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              C<R> d = dYa[ph(l1, mm < 0 ? -mm : mm)][c];
+              if (mm < 0) {
+                const R sg = R(parity(mm));
+                d = {d.x * sg, -d.y * sg};
+              }
+              ft[c] = re_mac(ft[c], su, d);
+            }
+          }
+        }
+        *(SOUT ? sOut + 3 * t + 0 : fij + 3 * static_cast<size_t>(j) + 0) = to_d(fr * ex + ft[0]);
+        *(SOUT ? sOut + 3 * t + 1 : fij + 3 * static_cast<size_t>(j) + 1) = to_d(fr * ey + ft[1]);
+        *(SOUT ? sOut + 3 * t + 2 : fij + 3 * static_cast<size_t>(j) + 2) = to_d(fr * ez + ft[2]);
+      }
+      __syncwarp();  // the row's results are read: it takes the G row
+      {
+        // the G row: g_n, then Re and Im of RY_i = R_{n1, l} Y_lm(e), i = n1 LSA + lm
+        const auto gcol = [&](int c) -> float {
+          if (c < D::NB) return g[c];
+          const int i = (c - D::NB) % D::NRY, n1 = i / D::LSA, lma = i % D::LSA, l1 = l_of_lm(lma);
+          const C<R> y = y_full(Ya, l1, lma - l1 * l1 - l1);
+          return (c < D::NB + D::NRY ? y.x : y.y) * tv[n1 * (D::LA + 1) + l1];
+        };
+#pragma unroll
+        for (int c = 0; c < D::NB + 2 * D::NRY; c += 4)
+          *reinterpret_cast<float4*>(row + c) = make_float4(gcol(c), gcol(c + 1), gcol(c + 2), gcol(c + 3));
+      }
+      __syncwarp();
+      // ---- magnetic GEMM T (V) over all eight n-tiles (n-tiles 5-7 hold
+      // k >= 20, which has no W_A terms: two k-steps)
+      {
+        float s3[2][8][4];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) s3[a][u][e] = 0.f;
+#pragma unroll
+        for (int s = 0; s < 6; ++s) {
+          uint32_t ah[2][4], al[2][4];
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            const float* ra = wrows + (16 * a + gid) * kTcRow + 8 * s + tig;
+            tf32_split(ra[0], ah[a][0], al[a][0]);
+            tf32_split(ra[8 * kTcRow], ah[a][1], al[a][1]);
+            tf32_split(ra[4], ah[a][2], al[a][2]);
+            tf32_split(ra[8 * kTcRow + 4], ah[a][3], al[a][3]);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            if (u >= 5 && s >= 2) continue;
+            const int f = kTcF1 + kTcF2 + (u < 5 ? 6 * u + s : 30 + 2 * (u - 5) + s);
+            const float2 bv = Bf[f * 32 + lane];
+            uint32_t bh0, bl0, bh1, bl1;
+            tf32_split(bv.x, bh0, bl0);
+            tf32_split(bv.y, bh1, bl1);
+#pragma unroll
+            for (int a = 0; a < 2; ++a) mma_3xtf32(s3[a][u], ah[a], al[a], bh0, bh1, bl0, bl1);
+          }
+        }
+        __syncwarp();  // every lane's G fragments are read: the rows take V
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          float* r0 = const_cast<float*>(wrows) + (16 * a + gid) * kTcRow + 2 * tig;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            *reinterpret_cast<float2*>(r0 + 8 * u) = make_float2(s3[a][u][0], s3[a][u][1]);
+            *reinterpret_cast<float2*>(r0 + 8 * kTcRow + 8 * u) = make_float2(s3[a][u][2], s3[a][u][3]);
+          }
+        }
+        __syncwarp();
+      }
+      // ---- magnetic epilogue (k_forces_fe's): the row holds (Re V_k, Im V_k)
+      if (live) {
+        C<R> Ym[D::H2], dYm[D::H2][3];
+        ylm_half<R, true>(D::L2, mx, my, mz, Ym, dYm);
+        const R invm = rcp(mg);
+        R tr = R(0), tt[3] = {R(0), R(0), R(0)};
+#pragma unroll
+        for (int k = 0; k < D::NQ; k += 2) {
+          const float4 v = *reinterpret_cast<const float4*>(row + 2 * k);
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const C<R> V = e ? C<R>{v.z, v.w} : C<R>{v.x, v.y};
+            const int kk = k + e, nr = kk / D::H2, h = kk % D::H2, q = nr * (D::L2 + 1) + l_of_h(h);
+            tr = fma(Md[q], re_mul(V, Ym[h]), tr);
+            const C<R> sv = cscale(V, invm * mv[q]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) tt[c] = re_mac(tt[c], sv, dYm[h][c]);
+          }
+        }
+        *(SOUT ? sOut + 3 * T + 3 * t + 0 : tij + 3 * static_cast<size_t>(j) + 0) = to_d(tr * mx + tt[0]);
+        *(SOUT ? sOut + 3 * T + 3 * t + 1 : tij + 3 * static_cast<size_t>(j) + 1) = to_d(tr * my + tt[1]);
+        *(SOUT ? sOut + 3 * T + 3 * t + 2 : tij + 3 * static_cast<size_t>(j) + 2) = to_d(tr * mz + tt[2]);
+      }
+      if constexpr (SOUT) {
+        __syncthreads();
+        store_tile(fij, sOut, jt, min(T, b1 - jt));
+        store_tile(tij, sOut + 3 * T, jt, min(T, b1 - jt));
+        __syncthreads();
+      }
+      __syncwarp();  // the row is read before the next tile's Q row
+    }
+    if (t >= 32) {
+      // on-site magnetic force dE_i/dm_i (src/forces.F90:690-749) on warp 1,
+      // as in k_forces_fe
+      static_assert(D::NMF + D::NBM <= 32 && D::NQ <= 32, "one function and one weight per lane");
+      const R mg = to_r<R>(magi[atom]);
+      const R mx = to_r<R>(mhi[3 * atom]), my = to_r<R>(mhi[3 * atom + 1]), mz = to_r<R>(mhi[3 * atom + 2]);
+      R wm = R(0);
+      const int nl = magnetic_bin_r<R>(m, mg, wm, err);
+      R v = R(nl == 0 ? 1 : 0), dv = R(0);
+      if (nl > 0 && lane < D::NMF + D::NBM) lut_eval<true>(m.lut_m32, D::NFM, lane, 1, nl, wm, rscale_m<R>(m), &v, &dv);
+      C<R> Yh[D::H2], dYh[D::H2][3];
+      ylm_half<R, true>(D::L2, mx, my, mz, Yh, dYh);
+      R tr = R(0), tt[3] = {R(0), R(0), R(0)};
+      const int n = lane - D::NMF;
+      if (n >= 0 && n < D::NBM) tr = to_r<R>(dedrho[static_cast<size_t>(atom) * 2]) * c1_of<R>(m, n) * dv;
+      const int k = lane < D::NQ ? lane : 0;
+      const int nr = k / D::H2, h = k % D::H2, q = nr * (D::L2 + 1) + l_of_h(h);
+      const R Mq = __shfl_sync(0xffffffffu, v, q), Mdq = __shfl_sync(0xffffffffu, dv, q);
+      if (lane < D::NQ) {
+        // Y_h and its gradient by selection (h differs across the lanes)
+        C<R> y = Yh[0], dy[3] = {dYh[0][0], dYh[0][1], dYh[0][2]};
+#pragma unroll
+        for (int hh = 1; hh < D::H2; ++hh)
+          if (h == hh) {
+            y = Yh[hh];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) dy[c] = dYh[hh][c];
+          }
+        const C<R> w = W0s[k];
+        const R invm = rcp(mg);
+        tr += Mdq * re_mul(w, y);
+        const R s = invm * Mq;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) tt[c] += s * re_mul(w, dy[c]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        tr += __shfl_xor_sync(0xffffffffu, tr, o);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) tt[c] += __shfl_xor_sync(0xffffffffu, tt[c], o);
+      }
+      if (lane == 0) {
+        ti0[3 * static_cast<size_t>(atom) + 0] = to_d(tr * mx + tt[0]);
+        ti0[3 * static_cast<size_t>(atom) + 1] = to_d(tr * my + tt[1]);
+        ti0[3 * static_cast<size_t>(atom) + 2] = to_d(tr * mz + tt[2]);
+      }
+    }
+    __syncthreads();  // the fragments, W0 and the rows are free for the next atom
+  }
+}
+
 inline size_t density_fe_smem(const DeviceModel& m, int nw) {
   // factors, per-warp density partials, per-warp 16-record buffers
   return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * nw * 32 +

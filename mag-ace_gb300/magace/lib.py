@@ -188,7 +188,7 @@ TUNING_NAMES = {
     "b3": ["16 warps", "12 warps", "8 warps", "12 warps, n0' outermost", "16 warps, packed FP32x2",
            "12 warps, packed FP32x2"],
     "forces": ["4 CTAs/SM", "6 CTAs/SM", "8 CTAs/SM", "4 CTAs/SM, packed FP32x2", "6 CTAs/SM, packed FP32x2",
-               "8 CTAs/SM, packed FP32x2"],
+               "8 CTAs/SM, packed FP32x2", "5 CTAs/SM, tensor cores (3xTF32)", "6 CTAs/SM, tensor cores (3xTF32)"],
 }
 
 

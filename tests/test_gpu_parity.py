@@ -296,8 +296,9 @@ def test_direct_mode_outputs_at_any_alignment(gpu_lib, monkeypatch, precision):
 
 
 def test_autotuner_keeps_results(gpu_lib, oracle_seeded):
-    """The autotuner times every density-kernel variant and keeps one; the
-    split results stay within the split tolerance of the oracle."""
+    """The autotuner times every variant of the split kernels and keeps the
+    fastest of each; the split results stay within the split tolerance of
+    the oracle."""
     import torch
     from magace import structures as S
     nb = S.neighbor_data(S.bcc_fe_128(3), 5.0)
@@ -309,7 +310,7 @@ def test_autotuner_keeps_results(gpu_lib, oracle_seeded):
         arrs = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
         torch.cuda.synchronize()
         rw, bw, fb = gpu_lib.autotune_device(nb.natom, nb.nei, off.data_ptr(), *[a.data_ptr() for a in arrs])
-        assert rw in (16, 32) and bw in (8, 12, 16) and fb in (4, 6, 8)
+        assert rw in (16, 32) and bw in (8, 12, 16) and fb in (4, 5, 6, 8)
         e, f, t, t0 = gpu_lib.acelib(nb)
     finally:
         gpu_lib.set_precision(0)
@@ -415,13 +416,14 @@ def test_abasis_variants_on_device_inputs(gpu_lib, oracle_seeded, shift):
     counts = nb.nstop - nb.nstart + 1
     assert counts.max() > 64 and counts.min() == 0
     gpu_lib.set_precision(1)
+    before = gpu_lib.get_tuning_indices()
     try:
         res = []
         for v in range(4):
             gpu_lib.set_tuning([v, 0, 0, 0])
             res.append(_device_eval(gpu_lib, nb, shift))
     finally:
-        gpu_lib.set_tuning([0, 0, 0, 0])
+        gpu_lib.set_tuning(before)
         gpu_lib.set_precision(0)
     eo, fo, to, t0o = oracle_seeded.acelib(nb)
     for got in res:
@@ -435,22 +437,24 @@ def test_abasis_variants_on_device_inputs(gpu_lib, oracle_seeded, shift):
 
 def test_every_split_variant_matches_oracle(gpu_lib, oracle_seeded):
     """Variant v of the 2-/4-body density, 3-body and force kernels together
-    (the A basis at min(v, 3)), on device arrays and through acelib_ with
-    host arrays (where the GPU writes host memory directly, the force
-    kernel's whole-line output form): every combination within the split
-    tolerance of the oracle and within 1e-6 of variant 0. Neighbours listed
-    out to 8.4 A give atoms of two 64-bond tiles."""
+    (the A basis at min(v, 3), the density kernels at min(v, 5): the force
+    kernel has two more forms, on the tensor cores), on device arrays
+    and through acelib_ with host arrays (where the GPU writes host memory
+    directly, the force kernel's whole-line output form): every combination
+    within the split tolerance of the oracle and within 1e-6 of variant 0.
+    Neighbours listed out to 8.4 A give atoms of two 64-bond tiles."""
     from magace import structures as S
     nb = S.neighbor_data(_ragged_slab(), 8.4)
     gpu_lib.set_precision(1)
+    before = gpu_lib.get_tuning_indices()
     try:
         res = []
-        for v in range(6):
-            gpu_lib.set_tuning([min(v, 3), v, v, v])
+        for v in range(8):
+            gpu_lib.set_tuning([min(v, 3), min(v, 5), min(v, 5), v])
             res.append(_device_eval(gpu_lib, nb))
             res.append(list(gpu_lib.acelib(nb)))
     finally:
-        gpu_lib.set_tuning([0, 0, 0, 0])
+        gpu_lib.set_tuning(before)
         gpu_lib.set_precision(0)
     eo, fo, to, t0o = oracle_seeded.acelib(nb)
     for got in res:

@@ -109,14 +109,15 @@ def test_error_codes(lib, tmp_path, seeded_potential):
     assert lib.load().ace_error_string(4).decode().startswith("bond shorter")
     # kernel variants: indices outside a kernel's range are refused, valid ones kept
     before = lib.get_tuning_indices()
-    for bad in ([4, 0, 0, 0], [0, 6, 0, 0], [0, 0, -1, 0], [0, 0, 0, 6]):
+    for bad in ([4, 0, 0, 0], [0, 6, 0, 0], [0, 0, -1, 0], [0, 0, 0, 8]):
         with pytest.raises(MagAceError) as e:
             lib.set_tuning(bad)
         assert e.value.code == 7
     assert lib.get_tuning_indices() == before
-    lib.set_tuning([3, 5, 5, 5])
-    assert lib.get_tuning_indices() == [3, 5, 5, 5]
+    lib.set_tuning([3, 5, 5, 7])
+    assert lib.get_tuning_indices() == [3, 5, 5, 7]
     assert lib.get_tuning()["abasis"] == "scalar, TMA-staged bond tiles, persistent grid"
+    assert lib.get_tuning()["forces"] == "6 CTAs/SM, tensor cores (3xTF32)"
     lib.set_tuning(before)
 
 
