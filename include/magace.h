@@ -207,15 +207,16 @@ int ace_autotune_device(int natom, int nei, const int* bond_offset, const double
 
 /* The kernel variants in use, variants[4]: A basis (0 scalar, 1 packed
  * FP32x2, 2 scalar with the bond tiles staged into shared memory by TMA bulk
- * copies, 3 the same on a persistent grid; 2/3 run only when the bond arrays
- * are device memory and otherwise fall back to 0), 2-/4-body density (0/1: 32/16 warps with per-entry loads, 2/3:
+ * copies, 3 the same on a persistent grid, 4 the bond sums on the tensor
+ * cores with 3's staging, 5 the tensor-core sums alone; 2-4 run only when the
+ * bond arrays are device memory and otherwise fall back to 0 (2, 3) or 5 (4)), 2-/4-body density (0/1: 32/16 warps with per-entry loads, 2/3:
  * 32/16 warps reading record streams by shuffles, 4/5: through shared
  * memory), 3-body (0-2: 16/12/8 warps, 3: 12
  * warps with the n0' loop outermost, 4/5: 16/12 warps packed FP32x2), forces
  * (0-2: 4/6/8 CTAs per SM, 3-5: the same packed FP32x2, 6/7: 5/6 CTAs per SM
  * with the contractions as GEMMs on the tensor cores, mma.sync TF32 in the
  * 3xTF32 split). Until the autotuner or ace_set_tuning chooses, the variants
- * are {3, 4, 4, 6}, the fastest on a 15,840-atom bcc Fe workload. */
+ * are {4, 4, 4, 6}, the fastest on a 15,840-atom bcc Fe workload. */
 int ace_get_tuning(int* variants);
 
 /* Selects the kernel variants directly (no counterpart in the reference):

@@ -1093,38 +1093,43 @@ int resident_grid(K* kernel, int threads, size_t smem_bytes) {
 // The A-basis phase: factors F, rank-1 density and core energy per atom.
 // Split-precision variants (DeviceModel::tune_abasis): 0 scalar, 1 packed
 // FP32x2, 2 scalar with the bond tiles staged by TMA, 3 the same on a
-// persistent grid; 2 and 3 run only when the bond inputs are device memory
-// (EvalBuffers::dev_inputs), else variant 0 runs.
+// persistent grid, 4 the bond sums on the tensor cores with TMA-staged tiles
+// on a persistent grid, 5 the tensor-core sums alone; 2-4 run only when the
+// bond inputs are device memory (EvalBuffers::dev_inputs), else 0 (for 2, 3)
+// or 5 (for 4) runs.
 template <class R>
 void launch_abasis(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, int grid, bool fe) {
   const int natom = b.natom;
   if (fe) {
-    const size_t s1 = abasis_fe_smem<R, FeDims>();
     int v = 0;
     if constexpr (sizeof(R) == 4) v = m.tune_abasis;
-    if (v >= 2 && !b.dev_inputs) v = 0;
-#define MAGACE_ABASIS(PK, TMA, PERSIST)                                                                            \
+    if ((v == 2 || v == 3) && !b.dev_inputs) v = 0;
+    if (v == 4 && !b.dev_inputs) v = 5;
+#define MAGACE_ABASIS(PK, TMA, PERSIST, TC)                                                                        \
   {                                                                                                                 \
+    const size_t s1 = abasis_fe_smem<R, FeDims, TC>();                                                              \
     const size_t sm = TMA ? ((s1 + 15) & ~static_cast<size_t>(15)) + kTileBarBytes : s1;                           \
-    set_smem(k_abasis_fe<R, FeDims, PK, TMA>, sm);                                                                 \
+    set_smem(k_abasis_fe<R, FeDims, PK, TMA, TC>, sm);                                                             \
     int g = grid;                                                                                                   \
     if (PERSIST) {                                                                                                  \
-      const int rg = resident_grid(k_abasis_fe<R, FeDims, PK, TMA>, 64, sm);                                        \
+      const int rg = resident_grid(k_abasis_fe<R, FeDims, PK, TMA, TC>, 64, sm);                                    \
       g = natom < rg ? natom : rg;                                                                                  \
     }                                                                                                               \
-    k_abasis_fe<R, FeDims, PK, TMA><<<g, 64, sm, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi, b.mhi,     \
-                                                       reinterpret_cast<C<R>*>(b.F), b.rho1, b.core,               \
-                                                       static_cast<R*>(b.stage), b.err);                            \
+    k_abasis_fe<R, FeDims, PK, TMA, TC><<<g, 64, sm, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi,        \
+                                                           b.mhi, reinterpret_cast<C<R>*>(b.F), b.rho1, b.core,    \
+                                                           static_cast<R*>(b.stage), b.err);                        \
   }
     if constexpr (sizeof(R) == 4) {
       switch (v) {
-        case 1: MAGACE_ABASIS(true, false, false); break;
-        case 2: MAGACE_ABASIS(false, true, false); break;
-        case 3: MAGACE_ABASIS(false, true, true); break;
-        default: MAGACE_ABASIS(false, false, false); break;
+        case 1: MAGACE_ABASIS(true, false, false, false); break;
+        case 2: MAGACE_ABASIS(false, true, false, false); break;
+        case 3: MAGACE_ABASIS(false, true, true, false); break;
+        case 4: MAGACE_ABASIS(false, true, true, true); break;
+        case 5: MAGACE_ABASIS(false, false, false, true); break;
+        default: MAGACE_ABASIS(false, false, false, false); break;
       }
     } else {
-      MAGACE_ABASIS(false, false, false);
+      MAGACE_ABASIS(false, false, false, false);
     }
 #undef MAGACE_ABASIS
   } else {
@@ -1395,7 +1400,7 @@ size_t eval_smem_bytes(const DeviceModel& m, int precision, int which) {
       }
       return forces_fe_smem<double, FeDims>(true);
     }
-    if (which == 0) return abasis_fe_smem<float, FeDims>();
+    if (which == 0) return abasis_fe_smem<float, FeDims, true>();
     if (which == 1) {
       const size_t a = density_fe_smem(m, 32), b = b3_fe_smem<FeDims>(m, 16);
       return a > b ? a : b;

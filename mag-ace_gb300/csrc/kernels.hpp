@@ -16,9 +16,10 @@ constexpr int kForceThreads = 64;
 constexpr int kMaxFeat = 32;     // per-bond radial functions of one kind
 constexpr int kMaxLaunches = 4;  // kernels of one evaluation
 // variants of the split-precision A-basis kernel: scalar, packed FP32x2,
-// scalar with TMA-staged bond tiles, the same on a persistent grid
-// (DeviceModel::tune_abasis)
-constexpr int kAbasisVariants = 4;
+// scalar with TMA-staged bond tiles, the same on a persistent grid, the bond
+// sums on the tensor cores with TMA-staged tiles on a persistent grid, the
+// tensor-core sums alone (DeviceModel::tune_abasis)
+constexpr int kAbasisVariants = 6;
 // warps per CTA of the split-precision density kernels, chosen by
 // DeviceModel::tune_rest / tune_b3 (ace_autotune_device picks them)
 // (2/3: record streams broadcast by shuffles, 4/5: through shared memory)
@@ -30,11 +31,11 @@ constexpr int kB3WarpChoices[6] = {16, 12, 8, 12, 16, 12};
 // with its contractions on the tensor cores (6-7) (DeviceModel::tune_forces)
 constexpr int kForceMinBlocksChoices[8] = {4, 6, 8, 4, 6, 8, 5, 6};
 // the variants used until ace_autotune_device or ace_set_tuning picks
-// others: the fastest on a 15,840-atom bcc Fe workload (A basis with
-// bulk-copied bond tiles on a persistent grid where the inputs are in device
-// memory, record streams through shared memory, packed FP32x2 3-body sums,
-// force contractions on the tensor cores)
-constexpr int kDefaultTuning[4] = {3, 4, 4, 6};
+// others: the fastest on a 15,840-atom bcc Fe workload (A-basis bond sums on
+// the tensor cores, with bulk-copied bond tiles on a persistent grid where
+// the inputs are in device memory; record streams through shared memory;
+// packed FP32x2 3-body sums; force contractions on the tensor cores)
+constexpr int kDefaultTuning[4] = {4, 4, 4, 6};
 
 // Device arrays of one evaluation. F and W are complex arrays of the selected
 // precision (FP64: 16 bytes per entry, FP32: 8 bytes).

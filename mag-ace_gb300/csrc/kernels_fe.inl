@@ -51,12 +51,20 @@ bool dims_match(const DeviceModel& m) {
 __host__ __device__ constexpr int l_of_h(int h) { return h == 0 ? 0 : (h < 3 ? 1 : (h < 6 ? 2 : (h < 10 ? 3 : 4))); }
 __host__ __device__ constexpr int l_of_lm(int lm) { return lm == 0 ? 0 : (lm < 4 ? 1 : (lm < 9 ? 2 : (lm < 16 ? 3 : 4))); }
 
+// bond-row strides of k_abasis_fe's tiles: RY (complex), q (complex) and g;
+// the tensor-core form pads them so that its fragment loads are free of
+// bank conflicts
+template <class D, bool TC>
+struct AbasisRows {
+  static constexpr int RY = TC ? D::NRY + 4 : D::NRY, Q = TC ? D::NQ + 6 : D::NQ, G = TC ? D::NB + 8 : D::NB;
+};
 // dynamic shared memory of k_abasis_fe without the staged tile
-template <class R, class D>
+template <class R, class D, bool TC = false>
 __host__ __device__ constexpr size_t abasis_fe_smem() {
-  // sQ holds NQ complex or, packed, 2 x 32 floats per bond
-  const size_t q = sizeof(C<R>) * D::NQ > sizeof(float) * 64 ? sizeof(C<R>) * D::NQ : sizeof(float) * 64;
-  return sizeof(C<R>) * 64 * D::NRY + q * 64 + sizeof(R) * 64 * (D::NB + 1) + 64;
+  using S = AbasisRows<D, TC>;
+  // sQ holds S::Q complex or, packed, 2 x 32 floats per bond
+  const size_t q = sizeof(C<R>) * S::Q > sizeof(float) * 64 ? sizeof(C<R>) * S::Q : sizeof(float) * 64;
+  return sizeof(C<R>) * 64 * S::RY + q * 64 + sizeof(R) * 64 * (S::G + 1) + 64;
 }
 
 // ===========================================================================
@@ -253,6 +261,28 @@ __device__ __forceinline__ int2 next_atom_tile(const DeviceModel& m, const int* 
 }
 
 // ===========================================================================
+// TF32 operands for mma.sync: x = hi + lo, hi the TF32 truncation of x (its
+// low 13 mantissa bits cleared), lo = x - hi exactly (|lo| < 2^-10 |x|; the
+// tensor cores read its TF32 part, so the products' error is below 2^-20
+// relative). d += a b in the 3xTF32 split: lo hi' + hi lo' + hi hi'.
+__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
+  hi = __float_as_uint(x) & 0xffffe000u;
+  lo = __float_as_uint(x - __uint_as_float(hi));
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ void mma_3xtf32(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
+                                           uint32_t bh0, uint32_t bh1, uint32_t bl0, uint32_t bl1) {
+  mma_tf32(d, al, bh0, bh1);
+  mma_tf32(d, ah, bl0, bl1);
+  mma_tf32(d, ah, bh0, bh1);
+}
+
+// ===========================================================================
 // PACKED (split precision only): the M Y tile is stored as real and
 // imaginary planes of 32 columns, and the lanes accumulate column pairs with
 // packed FP32x2 FMAs (warp 0: five pairs of the 18 A columns per half-row,
@@ -263,7 +293,15 @@ __device__ __forceinline__ int2 next_atom_tile(const DeviceModel& m, const int* 
 // is issued as soon as the current tile's features are computed, so that it
 // overlaps the bond sums and the completion of A (on a persistent grid every
 // tile after a CTA's first arrives this way).
-template <class R, class D, bool PACKED, bool TMA = false>
+//
+// TC (split precision only): the bond sums as GEMMs over the tile's bonds
+// (K) on the tensor cores, mma.sync m16n8k8 TF32 in the 3xTF32 split.
+// Warp 0: D1 = [Re RY; Im RY]^T (32 x K) times Q (K x 40, Re and Im of q_k
+// interleaved), so that each lane holds Re and Im of both parts of A_ik:
+// A = (D1[Re][Re q] - D1[Im][Im q], D1[Re][Im q] + D1[Im][Re q]). Warp 1:
+// D2 = g^T (16 x K) times Q (K x 64) is A2 itself. Bonds past the atom's
+// last are zero rows of both operands.
+template <class R, class D, bool PACKED, bool TMA = false, bool TC = false>
 __global__ void __launch_bounds__(64)
     k_abasis_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
@@ -272,17 +310,20 @@ __global__ void __launch_bounds__(64)
   constexpr int TB = 64;
   static_assert(D::NRY == 16 && D::NB == 16 && D::NQ3 == 18 && D::NQ == 30, "tile shapes assume the Fe layout");
   extern __shared__ __align__(16) unsigned char smem[];
-  C<R>* sRY = reinterpret_cast<C<R>*>(smem);             // [TB][NRY]
-  C<R>* sQ = sRY + TB * D::NRY;                           // [TB][NQ] (PACKED: 2 x [TB][32] floats)
-  constexpr size_t kQBytes = sizeof(C<R>) * D::NQ > sizeof(float) * 64 ? sizeof(C<R>) * D::NQ : sizeof(float) * 64;
-  R* sg = reinterpret_cast<R*>(reinterpret_cast<unsigned char*>(sQ) + TB * kQBytes);  // [TB][NB]
-  R* score = sg + TB * D::NB;                             // [TB]
+  using S = AbasisRows<D, TC>;
+  C<R>* sRY = reinterpret_cast<C<R>*>(smem);             // [TB][S::RY]
+  C<R>* sQ = sRY + TB * S::RY;                            // [TB][S::Q] (PACKED: 2 x [TB][32] floats)
+  constexpr size_t kQBytes = sizeof(C<R>) * S::Q > sizeof(float) * 64 ? sizeof(C<R>) * S::Q : sizeof(float) * 64;
+  R* sg = reinterpret_cast<R*>(reinterpret_cast<unsigned char*>(sQ) + TB * kQBytes);  // [TB][S::G]
+  R* score = sg + TB * S::G;                              // [TB]
   float* sQx = reinterpret_cast<float*>(sQ);              // PACKED: [TB][32] real, then imaginary
   float* sQy = sQx + TB * 32;
   C<R>* accA = sRY;                                       // reuse after the tiles: [NRY][NQ3]
   C<R>* accA2 = accA + D::NWA;                            // [NB][NQ]
   double core_acc = 0.0;  // warp 1: the atom's core energy, over its bond tiles
   static_assert(!PACKED || (sizeof(R) == 4 && D::H3 == D::H2 && D::NQ <= 32), "packed tiles: FP32, Fe layout");
+  static_assert(!TC || (sizeof(R) == 4 && !PACKED && D::H3 == D::H2), "tensor-core sums: FP32, Fe layout");
+  static_assert(D::NWA + D::NA2H <= TB * S::RY, "A and A2 fit in the RY tile");
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int row = lane >> 1, cb = lane & 1;
   const uint64_t pol_f = l2_evict_first();  // split path: the factors are read once per density kernel
@@ -291,7 +332,8 @@ __global__ void __launch_bounds__(64)
   // features; its mbarrier after the other buffers
   static_assert(sizeof(C<R>) * D::NQ * 64 >= kTileBytes || sizeof(float) * 64 * 64 >= kTileBytes,
                 "the staged tile fits in the M Y tile");
-  BondTile tile(reinterpret_cast<unsigned char*>(sQ), smem + ((abasis_fe_smem<R, D>() + 15) & ~static_cast<size_t>(15)));
+  BondTile tile(reinterpret_cast<unsigned char*>(sQ),
+                smem + ((abasis_fe_smem<R, D, TC>() + 15) & ~static_cast<size_t>(15)));
   constexpr int kIssuer = 32;  // lane 0 of warp 1 issues the copies
   uint32_t phase = 0;
   bool timed_out = false;
@@ -313,6 +355,11 @@ __global__ void __launch_bounds__(64)
     float2 accx[8], accy[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) accx[c] = accy[c] = make_float2(0.f, 0.f);
+    float dacc[10][4];  // TC: warp 0 D1 tiles [m-tile * 5 + n-tile], warp 1 D2 tiles [n-tile]
+#pragma unroll
+    for (int u = 0; u < 10; ++u)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) dacc[u][e] = 0.f;
     core_acc = 0.0;
     const int b0 = off[atom], b1 = off[atom + 1];
     for (int t0 = b0; t0 < b1; t0 += TB) {
@@ -399,7 +446,7 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
           for (int lm = 0; lm < D::LSA; ++lm) {
             const int l = l_of_lm(lm), mm = lm - l * l - l;
-            sRY[t * D::NRY + n1 * D::LSA + lm] = cscale(y_full(Ya, l, mm), Rv[n1 * (D::LA + 1) + l]);
+            sRY[t * S::RY + n1 * D::LSA + lm] = cscale(y_full(Ya, l, mm), Rv[n1 * (D::LA + 1) + l]);
           }
 #pragma unroll
         for (int nr = 0; nr < D::N2; ++nr)
@@ -410,22 +457,76 @@ __global__ void __launch_bounds__(64)
               sQx[t * 32 + nr * D::H2 + h] = q.x;
               sQy[t * 32 + nr * D::H2 + h] = q.y;
             } else {
-              sQ[t * D::NQ + nr * D::H2 + h] = q;
+              sQ[t * S::Q + nr * D::H2 + h] = q;
             }
           }
         if constexpr (PACKED) {
           for (int k = D::NQ; k < 32; ++k) sQx[t * 32 + k] = sQy[t * 32 + k] = 0.f;
         }
 #pragma unroll
-        for (int n = 0; n < D::NB; ++n) sg[t * D::NB + n] = g[n];
+        for (int n = 0; n < D::NB; ++n) sg[t * S::G + n] = g[n];
         score[t] = cv[0];
+      } else if constexpr (TC) {
+        // a bond past the atom's last: zero rows (the GEMMs sum over all 64)
+#pragma unroll
+        for (int i = 0; i < D::NRY; ++i) sRY[t * S::RY + i] = {R(0), R(0)};
+#pragma unroll
+        for (int k = 0; k < D::NQ; ++k) sQ[t * S::Q + k] = {R(0), R(0)};
+#pragma unroll
+        for (int n = 0; n < D::NB; ++n) sg[t * S::G + n] = R(0);
       }
       __syncthreads();
-      if constexpr (PACKED) {
+      if constexpr (TC) {
+        const int gid = lane >> 2, tig = lane & 3;
+        const int nks = (nb + 7) >> 3;  // k-steps of 8 bonds holding a bond
+        const float* Qf = reinterpret_cast<const float*>(sQ);  // [TB][2 S::Q]: Re, Im interleaved
+        if (warp == 0) {
+          const float2* RYf = reinterpret_cast<const float2*>(sRY);
+          for (int ks = 0; ks < nks; ++ks) {
+            const int k0 = 8 * ks + tig;
+            // A fragments of both m-tiles (Re RY rows, Im RY rows): rows gid, gid + 8
+            const float2 r00 = RYf[k0 * S::RY + gid], r10 = RYf[k0 * S::RY + gid + 8];
+            const float2 r01 = RYf[(k0 + 4) * S::RY + gid], r11 = RYf[(k0 + 4) * S::RY + gid + 8];
+            uint32_t ah[2][4], al[2][4];
+            tf32_split(r00.x, ah[0][0], al[0][0]);
+            tf32_split(r10.x, ah[0][1], al[0][1]);
+            tf32_split(r01.x, ah[0][2], al[0][2]);
+            tf32_split(r11.x, ah[0][3], al[0][3]);
+            tf32_split(r00.y, ah[1][0], al[1][0]);
+            tf32_split(r10.y, ah[1][1], al[1][1]);
+            tf32_split(r01.y, ah[1][2], al[1][2]);
+            tf32_split(r11.y, ah[1][3], al[1][3]);
+#pragma unroll
+            for (int nt = 0; nt < 5; ++nt) {
+              uint32_t bh0, bl0, bh1, bl1;
+              tf32_split(Qf[k0 * 2 * S::Q + 8 * nt + gid], bh0, bl0);
+              tf32_split(Qf[(k0 + 4) * 2 * S::Q + 8 * nt + gid], bh1, bl1);
+              mma_3xtf32(dacc[nt], ah[0], al[0], bh0, bh1, bl0, bl1);
+              mma_3xtf32(dacc[5 + nt], ah[1], al[1], bh0, bh1, bl0, bl1);
+            }
+          }
+        } else {
+          for (int ks = 0; ks < nks; ++ks) {
+            const int k0 = 8 * ks + tig;
+            uint32_t ah[4], al[4];
+            tf32_split(sg[k0 * S::G + gid], ah[0], al[0]);
+            tf32_split(sg[k0 * S::G + gid + 8], ah[1], al[1]);
+            tf32_split(sg[(k0 + 4) * S::G + gid], ah[2], al[2]);
+            tf32_split(sg[(k0 + 4) * S::G + gid + 8], ah[3], al[3]);
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+              uint32_t bh0, bl0, bh1, bl1;
+              tf32_split(Qf[k0 * 2 * S::Q + 8 * nt + gid], bh0, bl0);
+              tf32_split(Qf[(k0 + 4) * 2 * S::Q + 8 * nt + gid], bh1, bl1);
+              mma_3xtf32(dacc[nt], ah, al, bh0, bh1, bl0, bl1);
+            }
+          }
+        }
+      } else if constexpr (PACKED) {
         if (warp == 0) {
           // A[row][10cb .. 10cb+9] (columns 18, 19 padding)
           for (int b = 0; b < nb; ++b) {
-            const C<R> ry = sRY[b * D::NRY + row];
+            const C<R> ry = sRY[b * S::RY + row];
             const float2 rxx = make_float2(ry.x, ry.x), ryy = make_float2(ry.y, ry.y),
                          ryn = make_float2(-ry.y, -ry.y);
             const float2* qx = reinterpret_cast<const float2*>(sQx + b * 32 + 10 * cb);
@@ -440,7 +541,7 @@ __global__ void __launch_bounds__(64)
         } else {
           // A2[row][16cb .. 16cb+15] (columns 30, 31 padding)
           for (int b = 0; b < nb; ++b) {
-            const R gv = sg[b * D::NB + row];
+            const R gv = sg[b * S::G + row];
             const float2 gg = make_float2(gv, gv);
             const float2* qx = reinterpret_cast<const float2*>(sQx + b * 32 + 16 * cb);
             const float2* qy = reinterpret_cast<const float2*>(sQy + b * 32 + 16 * cb);
@@ -454,21 +555,21 @@ __global__ void __launch_bounds__(64)
       } else if (warp == 0) {
         // A[row][9cb .. 9cb+8], row = (n1, l1 m1), column = (n2, l2 m2 >= 0)
         for (int b = 0; b < nb; ++b) {
-          const C<R> ry = sRY[b * D::NRY + row];
+          const C<R> ry = sRY[b * S::RY + row];
 #pragma unroll
           for (int c = 0; c < 9; ++c) {
             const int k3 = 9 * cb + c;
-            const C<R> q = sQ[b * D::NQ + (k3 / D::H3) * D::H2 + k3 % D::H3];
+            const C<R> q = sQ[b * S::Q + (k3 / D::H3) * D::H2 + k3 % D::H3];
             cmac(acc[c], ry, q);
           }
         }
       } else {
         // A2[row][15cb .. 15cb+14], row = n, column = (n', l' m' >= 0)
         for (int b = 0; b < nb; ++b) {
-          const R gv = sg[b * D::NB + row];
+          const R gv = sg[b * S::G + row];
 #pragma unroll
           for (int c = 0; c < 15; ++c) {
-            const C<R> q = sQ[b * D::NQ + 15 * cb + c];
+            const C<R> q = sQ[b * S::Q + 15 * cb + c];
             acc[c].x = fma(gv, q.x, acc[c].x);
             acc[c].y = fma(gv, q.y, acc[c].y);
           }
@@ -491,7 +592,31 @@ __global__ void __launch_bounds__(64)
         if (nx.y > 0) tile.issue(rr, ee, magj, mhj, nx.x, nx.y);
       }
     }
-    if constexpr (PACKED) {
+    if constexpr (TC) {
+      // fragment c0..c3 = rows (gid, gid, gid + 8, gid + 8), columns (2 tig, 2 tig + 1) of n-tile nt
+      const int gid = lane >> 2, tig = lane & 3;
+      if (warp == 0) {
+#pragma unroll
+        for (int nt = 0; nt < 5; ++nt) {
+          const int k = 4 * nt + tig;
+          if (k < D::NQ3) {
+            const float* re = dacc[nt];
+            const float* im = dacc[5 + nt];
+            accA[gid * D::NQ3 + k] = {re[0] - im[1], re[1] + im[0]};
+            accA[(gid + 8) * D::NQ3 + k] = {re[2] - im[3], re[3] + im[2]};
+          }
+        }
+      } else {
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+          const int k = 4 * nt + tig;
+          if (k < D::NQ) {
+            accA2[gid * D::NQ + k] = {dacc[nt][0], dacc[nt][1]};
+            accA2[(gid + 8) * D::NQ + k] = {dacc[nt][2], dacc[nt][3]};
+          }
+        }
+      }
+    } else if constexpr (PACKED) {
       if (warp == 0) {
 #pragma unroll
         for (int c = 0; c < 10; ++c) {
@@ -2030,26 +2155,6 @@ constexpr int kTcF2 = 5 * 4;    // of F2
 constexpr int kTcT = 5 * 6 + 3 * 2;  // of T (n-tiles 5-7 hold k >= 20 only: the 2 k-steps of g)
 constexpr int kTcFrags = kTcF1 + kTcF2 + kTcT;
 
-// x = hi + lo: hi the TF32 truncation of x (its low 13 mantissa bits
-// cleared), lo = x - hi exactly (|lo| < 2^-10 |x|; the tensor cores read its
-// TF32 part, so the products' error is below 2^-20 relative)
-__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
-  hi = __float_as_uint(x) & 0xffffe000u;
-  lo = __float_as_uint(x - __uint_as_float(hi));
-}
-__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-      "{%0, %1, %2, %3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-// d += a b in the 3xTF32 split (small terms first)
-__device__ __forceinline__ void mma_3xtf32(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
-                                           uint32_t bh0, uint32_t bh1, uint32_t bl0, uint32_t bl1) {
-  mma_tf32(d, al, bh0, bh1);
-  mma_tf32(d, ah, bl0, bl1);
-  mma_tf32(d, ah, bh0, bh1);
-}
 
 template <class D>
 size_t forces_tc_smem(bool sout) {

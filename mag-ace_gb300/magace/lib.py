@@ -182,7 +182,8 @@ def autotune_device(natom, nei, off, r, e, magj, mhj, magi, mhi, stream=0) -> tu
 
 TUNING_NAMES = {
     "abasis": ["scalar", "packed FP32x2", "scalar, TMA-staged bond tiles",
-               "scalar, TMA-staged bond tiles, persistent grid"],
+               "scalar, TMA-staged bond tiles, persistent grid",
+               "tensor cores (3xTF32), TMA-staged bond tiles, persistent grid", "tensor cores (3xTF32)"],
     "density": ["32 warps", "16 warps", "32 warps, record streams", "16 warps, record streams",
                 "32 warps, record streams via shared memory", "16 warps, record streams via shared memory"],
     "b3": ["16 warps", "12 warps", "8 warps", "12 warps, n0' outermost", "16 warps, packed FP32x2",

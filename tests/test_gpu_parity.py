@@ -403,11 +403,11 @@ def _device_eval(lib, nb, shift=0):
 @pytest.mark.parametrize("shift", [0, 1])
 def test_abasis_variants_on_device_inputs(gpu_lib, oracle_seeded, shift):
     """Every A-basis variant on device-resident bond arrays, the TMA-staged
-    ones included: arrays that start on and 8 bytes past a 16-byte boundary,
+    and tensor-core ones included: arrays that start on and 8 bytes past a 16-byte boundary,
     atoms of two 64-bond tiles (neighbours listed out to 8.4 A,
     beyond the cutoff) and an atom without neighbours. Split results stay
     within the split tolerance of the oracle and within 1e-6 of the scalar
-    variant."""
+    variant (3e-6 where the tensor-core forms' 3xTF32 products enter)."""
     from magace import structures as S
     st = _ragged_slab()
     st = S.Structure(np.vstack([st.positions, [[1.0, 1.0, 90.0]]]), st.cell, st.pbc, np.append(st.mag, 2.0),
@@ -419,7 +419,7 @@ def test_abasis_variants_on_device_inputs(gpu_lib, oracle_seeded, shift):
     before = gpu_lib.get_tuning_indices()
     try:
         res = []
-        for v in range(4):
+        for v in range(6):
             gpu_lib.set_tuning([v, 0, 0, 0])
             res.append(_device_eval(gpu_lib, nb, shift))
     finally:
@@ -432,16 +432,17 @@ def test_abasis_variants_on_device_inputs(gpu_lib, oracle_seeded, shift):
         for x, y in zip(got, (eo, fo, to, t0o)):
             assert rel_err(x, y) < 1e-5
         for x, y in zip(got, res[0]):
-            assert rel_err(x, y) < 1e-6
+            # FP32 rounding; the tensor-core forms' 3xTF32 products are within 2^-20
+            assert rel_err(x, y) < 3e-6
 
 
 def test_every_split_variant_matches_oracle(gpu_lib, oracle_seeded):
     """Variant v of the 2-/4-body density, 3-body and force kernels together
-    (the A basis at min(v, 3), the density kernels at min(v, 5): the force
+    (the A basis and the density kernels at min(v, 5): the force
     kernel has two more forms, on the tensor cores), on device arrays
     and through acelib_ with host arrays (where the GPU writes host memory
     directly, the force kernel's whole-line output form): every combination
-    within the split tolerance of the oracle and within 1e-6 of variant 0.
+    within the split tolerance of the oracle and within 3e-6 of variant 0.
     Neighbours listed out to 8.4 A give atoms of two 64-bond tiles."""
     from magace import structures as S
     nb = S.neighbor_data(_ragged_slab(), 8.4)
@@ -450,7 +451,7 @@ def test_every_split_variant_matches_oracle(gpu_lib, oracle_seeded):
     try:
         res = []
         for v in range(8):
-            gpu_lib.set_tuning([min(v, 3), min(v, 5), min(v, 5), v])
+            gpu_lib.set_tuning([min(v, 5), min(v, 5), min(v, 5), v])
             res.append(_device_eval(gpu_lib, nb))
             res.append(list(gpu_lib.acelib(nb)))
     finally:
@@ -463,7 +464,8 @@ def test_every_split_variant_matches_oracle(gpu_lib, oracle_seeded):
         for x, y in zip(got, (eo, fo, to, t0o)):
             assert rel_err(x, y) < 1e-5
         for x, y in zip(got, res[0]):
-            assert rel_err(x, y) < 1e-6
+            # FP32 rounding; the tensor-core forms' 3xTF32 products are within 2^-20
+            assert rel_err(x, y) < 3e-6
 
 
 

@@ -109,7 +109,7 @@ def test_error_codes(lib, tmp_path, seeded_potential):
     assert lib.load().ace_error_string(4).decode().startswith("bond shorter")
     # kernel variants: indices outside a kernel's range are refused, valid ones kept
     before = lib.get_tuning_indices()
-    for bad in ([4, 0, 0, 0], [0, 6, 0, 0], [0, 0, -1, 0], [0, 0, 0, 8]):
+    for bad in ([6, 0, 0, 0], [0, 6, 0, 0], [0, 0, -1, 0], [0, 0, 0, 8]):
         with pytest.raises(MagAceError) as e:
             lib.set_tuning(bad)
         assert e.value.code == 7
