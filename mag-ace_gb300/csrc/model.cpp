@@ -757,6 +757,28 @@ void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
   }
   T.run[3 * T.nslot] = static_cast<int32_t>(T.rec.size() / 4);
   T.nfac = static_cast<int>(T.factor_of.size());
+  // compact factors renumbered in ascending factor order, so that the
+  // kernels' staging loops (thread c takes factor c) read each atom's row
+  // front to back
+  {
+    std::vector<int32_t> by(T.nfac);
+    for (int c = 0; c < T.nfac; ++c) by[c] = c;
+    std::sort(by.begin(), by.end(), [&](int32_t x, int32_t y) { return T.factor_of[x] < T.factor_of[y]; });
+    std::vector<uint32_t> nw(T.nfac);
+    std::vector<int32_t> fo(T.nfac);
+    for (int c = 0; c < T.nfac; ++c) {
+      nw[by[c]] = static_cast<uint32_t>(c);
+      fo[c] = T.factor_of[by[c]];
+    }
+    T.factor_of = fo;
+    const auto re = [&](uint32_t c) { return c < static_cast<uint32_t>(T.nfac) ? nw[c] : c; };
+    for (size_t e = 0; e < T.rec.size(); e += 4) {
+      T.rec[e + 1] = re(T.rec[e + 1] & 0xffffu) | (re(T.rec[e + 1] >> 16) << 16);
+      T.rec[e + 2] = re(T.rec[e + 2]);
+    }
+    for (auto& g0 : T.slot_g0)
+      if (g0 >= 0) g0 = static_cast<int32_t>(nw[g0]);
+  }
   // longest first onto the least loaded warp
   T.nwarp = kRestTableWarps;
   std::vector<int> order(T.nslot);
