@@ -93,6 +93,26 @@ def oracle_high(high_potential):
     return orc.Oracle(high_potential, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)
 
 
+RADTYPE_PAIRS = ((6, 5), (4, 6))  # (atomic, magnetic) radial basis types beyond the other layouts' 3/7, 5/3, 4/8
+
+
+@pytest.fixture(scope="session", params=RADTYPE_PAIRS, ids=lambda p: f"radtypes{p[0]}{p[1]}")
+def radtype_potential(request, tmp_path_factory):
+    """Seeded potentials in the Fe layout (so the specialised kernels run)
+    with other radial basis types, type 6 in either role."""
+    from magace import potential
+    ra, rm = request.param
+    path = str(tmp_path_factory.mktemp(f"rt{ra}{rm}") / "Fe.pbe.in")
+    potential.write_seeded_potential(path, seed=11 + ra, layout=dict(potential.FE_LAYOUT, radtype_a=ra, radtype_m=rm))
+    return path
+
+
+@pytest.fixture(scope="session")
+def oracle_radtype(radtype_potential):
+    import oracle as orc
+    return orc.Oracle(radtype_potential, "Fe", rcut=5.0, rcut_magnetic=4.0, smear=0.2)
+
+
 @pytest.fixture(scope="session")
 def oracle_alt(alt_potential):
     import oracle as orc

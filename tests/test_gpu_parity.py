@@ -549,3 +549,33 @@ def test_padded_high_body_clusters_contribute_nothing(high_lib):
     high_lib.set_coefficients(c)
     for a, b in zip(after, before):
         assert np.array_equal(a, b)
+
+
+# ---------------------------------------------------------------------------
+# Radial basis types 6/5 and 4/6 in the Fe layout (the specialised kernels)
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["bcc54", "slab"])
+def test_radial_types_parity(radtype_potential, oracle_radtype, case):
+    """FP64 equals the oracle at 1e-10 and split stays within the split
+    tolerance (1 meV/atom, 10 meV/A, 10 meV/mu_B), with radial types the
+    other seeded layouts do not use. The norm-relative bound is 2e-4 here:
+    the FP32 copies of these seeded bases' spline coefficients cancel more
+    than the Fe layout's (8e-5 measured on the per-bond magnetic forces, whose
+    largest value is ~8e-3 eV/mu_B)."""
+    from magace import lib, structures as S
+    lib.init(radtype_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    st = S.bcc_fe_54(4) if case == "bcc54" else _ragged_slab()
+    nb = S.neighbor_data(st, 5.0)
+    lib.set_precision(0)
+    _compare(lib, oracle_radtype, nb)
+    lib.set_precision(1)
+    try:
+        e, f, t, t0 = lib.acelib(nb)
+    finally:
+        lib.set_precision(0)
+    eo, fo, to, t0o = oracle_radtype.acelib(nb)
+    assert np.abs(e - eo).max() * 1e3 < 1.0 and np.abs(f - fo).max() * 1e3 < 10.0
+    assert np.abs(t - to).max() * 1e3 < 10.0 and np.abs(t0 - t0o).max() * 1e3 < 10.0
+    for got, ref in ((e, eo), (f, fo), (t, to), (t0, t0o)):
+        assert rel_err(got, ref) < 2e-4

@@ -68,18 +68,8 @@ def _energy(orc, st, rcut):
     return e.sum(), nb, f, t, t0
 
 
-@pytest.mark.parametrize("which", ["fe", "seeded", "alt", "high"])
-def test_finite_differences(which, request):
-    """Forces and magnetic forces assembled as in lammps/pair_spin_ace.cpp
-    equal -dE/dx and -dE/dm from centred differences (h = 1e-5), for the
-    example Fe potential and the seeded layouts (the second one with two
-    densities and a non-linear embedding, the third with 5- and 6-body
-    clusters; its radial basis has a larger third derivative, so it takes
-    h = 2e-6, where the truncation error falls as h^2)."""
+def _fd_check(orc, rc, h):
     from magace import structures as S
-    orc = request.getfixturevalue({"fe": "oracle_fe", "seeded": "oracle_seeded", "alt": "oracle_alt",
-                                   "high": "oracle_high"}[which])
-    rc = 4.5 if which == "fe" else 5.0
     rng = np.random.default_rng(3)
     pos, cell = S.bcc_cubic(2, 2, 2, 2.83)
     pos = pos + rng.normal(0, 0.08, pos.shape)
@@ -92,7 +82,6 @@ def test_finite_differences(which, request):
 
     E, nb, f, t, t0 = _energy(orc, st_of(pos, mvec), rc)
     F, FM = S.total_forces(nb, f, t, t0)
-    h = 2e-6 if which == "high" else 1e-5
     for k in (0, 5, 11):
         for c in range(3):
             p = pos.copy(); p[k, c] += h
@@ -105,6 +94,25 @@ def test_finite_differences(which, request):
             mv[k, c] -= 2 * h
             em = _energy(orc, st_of(pos, mv), rc)[0]
             assert abs(-(ep - em) / (2 * h) - FM[k, c]) < 5e-7 * max(1.0, abs(FM[k, c]))
+
+
+@pytest.mark.parametrize("which", ["fe", "seeded", "alt", "high"])
+def test_finite_differences(which, request):
+    """Forces and magnetic forces assembled as in lammps/pair_spin_ace.cpp
+    equal -dE/dx and -dE/dm from centred differences (h = 1e-5), for the
+    example Fe potential and the seeded layouts (the second one with two
+    densities and a non-linear embedding, the third with 5- and 6-body
+    clusters; its radial basis has a larger third derivative, so it takes
+    h = 2e-6, where the truncation error falls as h^2)."""
+    orc = request.getfixturevalue({"fe": "oracle_fe", "seeded": "oracle_seeded", "alt": "oracle_alt",
+                                   "high": "oracle_high"}[which])
+    _fd_check(orc, 4.5 if which == "fe" else 5.0, 2e-6 if which == "high" else 1e-5)
+
+
+def test_finite_differences_radial_types(oracle_radtype):
+    """The same with radial basis types 6/5 and 4/6 (type 6 is used by no
+    other layout)."""
+    _fd_check(oracle_radtype, 5.0, 1e-5)
 
 
 def test_rotation_and_moment_reversal(oracle_seeded):
