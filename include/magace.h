@@ -174,10 +174,11 @@ int ace_table_stats(long long* out);
  * kernel variants that stage bond tiles with bulk copies may run, as in
  * ace_compute_device. The potential's tables must already be on the device
  * (placed by any ace_compute_device call; natom = 0 is enough). The first call
- * on each device looks up the scratch address (cudaGetSymbolAddress); make
- * that first call before any stream capture. Calls share the scratch, so
- * calls that overlap on the GPU race. The call returns after the evaluation
- * has completed, with this call's device-side status. */
+ * on each device looks up the scratch address (cudaGetSymbolAddress). Calls
+ * share the scratch, so calls that overlap on the GPU race. The call is
+ * synchronous: it returns after the evaluation has completed, with this
+ * call's device-side status, so it cannot be captured into a CUDA graph; on a
+ * stream that is capturing it returns MAGACE_ERR_ARGS before any device work. */
 int ace_compute_device_noalloc(int natom, int nei, const int* bond_offset, const double* r,
                                const double* e, const double* mag_j, const double* mhat_j,
                                const double* mag_i, const double* mhat_i, double* energy,

@@ -104,6 +104,16 @@ extern "C" int ace_compute_device_noalloc(int natom, int nei, const int* bond_of
   cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) return runtime_error(MAGACE_ERR_CUDA, cudaGetErrorString(ce));
   if (dev < 0 || dev >= kMaxDevices) return runtime_error(MAGACE_ERR_CUDA, "device index beyond 64");
+  // the call reads its status back and synchronizes, so it cannot be part of
+  // a captured graph: refuse before any device work, which leaves the
+  // caller's capture intact
+  if (stream) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cs) == cudaSuccess &&
+        cs != cudaStreamCaptureStatusNone)
+      return runtime_error(MAGACE_ERR_ARGS,
+                           "ace_compute_device_noalloc is synchronous and cannot run in a stream capture");
+  }
   // one-time set-up per device, with that device current: the device
   // address of the scratch array
   if (!g_scratch_addr[dev]) {

@@ -125,3 +125,39 @@ def test_noalloc_takes_its_limit_and_refuses_one_more(seeded_potential, precisio
         assert np.all(np.isfinite(g))
         assert _rel(g, r) <= tol
     lib.set_precision(0)
+
+
+def test_noalloc_refuses_a_stream_capture(seeded_potential):
+    """The call is synchronous, so on a stream that is being captured into a
+    CUDA graph it returns MAGACE_ERR_ARGS before any device work; the
+    caller's capture stays valid and the library stays usable."""
+    import torch
+    from magace import lib, structures as S
+
+    lib.init(seeded_potential, "Fe", 5.0, 4.0, 0.2, 1)
+    lib.set_precision(0)
+    so = lib.load()
+    nb = S.neighbor_data(S.bcc_fe_54(1), 5.0)
+    dev = torch.device("cuda", 0)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(nb.nstop - nb.nstart + 1)]).astype(np.int32), device=dev)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    ins = [T(a) for a in (nb.dlist, nb.elist, nb.dlist_mom, nb.elist_mom, nb.dlist_momi, nb.elist_momi)]
+    outs = [torch.zeros(n, dtype=torch.float64, device=dev) for n in (nb.natom, 3 * nb.nei, 3 * nb.nei, 3 * nb.natom)]
+    ptr = lambda ts: [t.data_ptr() for t in ts]
+    # tables on the device first (an uncaptured call)
+    assert so.ace_compute_device(0, 0, off.data_ptr(), *ptr(ins), *ptr(outs), None) == 0
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    marker = torch.zeros(1, device=dev)
+    with torch.cuda.graph(graph, stream=stream):
+        code = so.ace_compute_device_noalloc(nb.natom, nb.nei, off.data_ptr(), *ptr(ins), *ptr(outs),
+                                             stream.cuda_stream)
+        marker += 1.0
+    assert code == 7, so.ace_last_error_message()  # MAGACE_ERR_ARGS
+    assert b"stream capture" in so.ace_last_error_message()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(marker.item()) == 1.0
+    # still usable outside the capture
+    assert so.ace_compute_device_noalloc(nb.natom, nb.nei, off.data_ptr(), *ptr(ins), *ptr(outs), None) == 0
