@@ -1312,8 +1312,9 @@ int launch_eval(const DeviceModel& m0, const EvalBuffers& b, cudaStream_t st, in
 #define MAGACE_FORCES_SO(MB, PK, SO)                                                                                \
   {                                                                                                                 \
     const size_t s3 = forces_fe_smem<R, FeDims>(SO);                                                                \
-    set_smem(k_forces_fe<R, FeDims, MB, PK, SO>, s3);                                                               \
-    k_forces_fe<R, FeDims, MB, PK, SO><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj, b.mhj, b.magi,       \
+    set_smem(k_forces_fe<R, FeDims, MB, PK, SO, sizeof(R) == 8>, s3);                                               \
+    k_forces_fe<R, FeDims, MB, PK, SO, sizeof(R) == 8><<<grid, 64, s3, st>>>(m, natom, b.off, b.r, b.e, b.magj,      \
+                                                                           b.mhj, b.magi,                           \
                                                              b.mhi, reinterpret_cast<const C<R>*>(b.W), b.edf,      \
                                                              b.dedrho, b.fij, b.tij, b.ti0,                         \
                                                              static_cast<const R*>(b.stage), b.err, g3, g3i, g3s);  \

@@ -1692,7 +1692,50 @@ __device__ __forceinline__ void store_tile(double* __restrict__ dst, const doubl
 // as contiguous 16-byte stores (whole lines); chosen when the outputs are
 // host memory read over NVLink-C2C, where scattered 8-byte stores cost far
 // more than in device memory.
-template <class R, class D, int MINB, bool PACKED, bool SOUT = false>
+// ---------------------------------------------------------------------------
+// Float-float arithmetic for the FP64 path's contractions (FF). A double x is
+// carried as hi + lo with hi = x rounded to FP32 and lo = x - hi rounded
+// (48 bits of x). A dot product accumulates in (s, c): each product a b is
+// split exactly into p + e (p = a.hi b.hi, e its FMA residual plus the cross
+// terms a.hi b.lo + a.lo b.hi), s takes p by an error-free two-sum whose
+// error, with e, goes to c; the result is s + c in FP64 (Ogita, Rump and
+// Oishi's compensated dot product, "Dot2"). Its error is about 2^-48 of the
+// sum of |products|, against 2^-53 in FP64, and it runs on the FP32 pipe,
+// which on this part issues 64 times the FP64 pipe's operations.
+struct FFv {
+  float hi, lo;
+};
+__device__ __forceinline__ FFv ff_of(double x) {
+  const float h = d2f(x);
+  return {h, d2f(x - f2d(h))};  // x - h is exact in FP64
+}
+__device__ __forceinline__ double ff_d(float s, float c) { return f2d(s) + f2d(c); }
+// (s, c) += a b
+__device__ __forceinline__ void ff_dot(float& s, float& c, FFv a, FFv b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float t = s + p, z = t - s;
+  c += ((s - (t - z)) + (p - z)) + e;
+  s = t;
+}
+__device__ __forceinline__ FFv ff_neg(FFv a) { return {-a.hi, -a.lo}; }
+// a[h] for an h that differs across the lanes, by selection (no local memory)
+template <int N, class V>
+__device__ __forceinline__ V pick_of(const V (&a)[N], int h) {
+  V v = a[0];
+#pragma unroll
+  for (int j = 1; j < N; ++j)
+    if (h == j) v = a[j];
+  return v;
+}
+// a complex weight staged as float-float in the 16 bytes of a C<double>
+struct FFc {
+  FFv x, y;
+};
+
+template <class R, class D, int MINB, bool PACKED, bool SOUT = false, bool FF = false>
 __global__ void __launch_bounds__(64, MINB)
     k_forces_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
                 const double* __restrict__ ee, const double* __restrict__ magj, const double* __restrict__ mhj,
@@ -1789,6 +1832,8 @@ __global__ void __launch_bounds__(64, MINB)
       if constexpr (PACKED) {
         W2x[k * D::NB + n] = w.x;
         W2y[k * D::NB + n] = w.y;
+      } else if constexpr (FF) {
+        reinterpret_cast<FFc*>(W2T)[k * D::NB + n] = {ff_of(w.x), ff_of(w.y)};
       } else {
         W2T[k * D::NB + n] = w;
       }
@@ -1799,6 +1844,8 @@ __global__ void __launch_bounds__(64, MINB)
       if constexpr (PACKED) {
         WAx[k3 * D::NRY + i] = w.x;
         WAy[k3 * D::NRY + i] = w.y;
+      } else if constexpr (FF) {
+        reinterpret_cast<FFc*>(WAT)[k3 * D::NRY + i] = {ff_of(w.x), ff_of(w.y)};
       } else {
         WAT[k3 * D::NRY + i] = w;
       }
@@ -1953,6 +2000,46 @@ __global__ void __launch_bounds__(64, MINB)
               U[2 * i] = {Ux2[i].x, Uy2[i].x};
               U[2 * i + 1] = {Ux2[i].y, Uy2[i].y};
             }
+          } else if constexpr (FF) {
+            static_assert(sizeof(R) == 8 && sizeof(FFc) == sizeof(C<double>), "float-float contractions: FP64 path");
+            // compensated float-float dot products (sum, compensation)
+            float sps[D::NB], spc[D::NB], uxs[D::NRY], uxc[D::NRY], uys[D::NRY], uyc[D::NRY];
+  #pragma unroll
+            for (int n = 0; n < D::NB; ++n) sps[n] = spc[n] = 0.f;
+  #pragma unroll
+            for (int i = 0; i < D::NRY; ++i) uxs[i] = uxc[i] = uys[i] = uyc[i] = 0.f;
+            // one magnetic product per iteration, not unrolled (the float-float
+            // loops unrolled over h overflow the instruction cache)
+  #pragma unroll 1
+            for (int k = 0; k < D::NQ; ++k) {
+              const int nr = k / D::H2, h = k - nr * D::H2;
+              {
+                const C<R> qd = cscale(pick_of(Ym, h), cM[(nr * (D::L2 + 1) + l_of_h(h)) * T + t]);
+                const FFv qx = ff_of(qd.x), qy = ff_of(qd.y), qyn = ff_neg(qy);
+                const FFc* w2 = reinterpret_cast<const FFc*>(W2T) + k * D::NB;
+  #pragma unroll
+                for (int n = 0; n < D::NB; ++n) {
+                  const FFc w = w2[n];
+                  ff_dot(sps[n], spc[n], w.x, qx);
+                  ff_dot(sps[n], spc[n], w.y, qyn);
+                }
+                if (nr < D::NM && h < D::H3) {
+                  const FFc* wa = reinterpret_cast<const FFc*>(WAT) + (nr * D::H3 + h) * D::NRY;
+  #pragma unroll
+                  for (int i = 0; i < D::NRY; ++i) {
+                    const FFc w = wa[i];
+                    ff_dot(uxs[i], uxc[i], w.x, qx);
+                    ff_dot(uxs[i], uxc[i], w.y, qyn);
+                    ff_dot(uys[i], uyc[i], w.x, qy);
+                    ff_dot(uys[i], uyc[i], w.y, qx);
+                  }
+                }
+              }
+            }
+  #pragma unroll
+            for (int n = 0; n < D::NB; ++n) sp[n] = ff_d(sps[n], spc[n]);
+  #pragma unroll
+            for (int i = 0; i < D::NRY; ++i) U[i] = {ff_d(uxs[i], uxc[i]), ff_d(uys[i], uyc[i])};
           } else {
   #pragma unroll
             for (int n = 0; n < D::NB; ++n) sp[n] = R(0);
@@ -2007,6 +2094,20 @@ __global__ void __launch_bounds__(64, MINB)
   #pragma unroll
             for (int c = 0; c < 3; ++c) tt[c] = re_mac(tt[c], sv, dYm[h][c]);
           };
+          // the same for an h only known at run time (Y and dY by selection)
+          const auto contract_at = [&](int nr, int h, C<R> V) {
+            const int q = nr * (D::L2 + 1) + l_of_h(h);
+            tr = fma(cMd[q * T + t], re_mul(V, pick_of(Ym, h)), tr);
+            const C<R> sv = cscale(V, invm * cM[q * T + t]);
+  #pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              C<R> d = dYm[0][c];
+  #pragma unroll
+              for (int j = 1; j < D::H2; ++j)
+                if (h == j) d = dYm[j][c];
+              tt[c] = re_mac(tt[c], sv, d);
+            }
+          };
           if constexpr (PACKED) {
             float2 g2[D::NB / 2], RYx2[D::NRY / 2], RYy2[D::NRY / 2], RYyn2[D::NRY / 2];
   #pragma unroll
@@ -2050,6 +2151,41 @@ __global__ void __launch_bounds__(64, MINB)
                 }
                 contract(nr, h, C<R>{vx2.x + vx2.y, vy2.x + vy2.y});
               }
+          } else if constexpr (FF) {
+            FFv gf[D::NB], rx[D::NRY], ry[D::NRY];
+  #pragma unroll
+            for (int n = 0; n < D::NB; ++n) gf[n] = ff_of(g[n]);
+  #pragma unroll
+            for (int i = 0; i < D::NRY; ++i) {
+              rx[i] = ff_of(RY[i].x);
+              ry[i] = ff_of(RY[i].y);
+            }
+  #pragma unroll 1
+            for (int k = 0; k < D::NQ; ++k) {
+              const int nr = k / D::H2, h = k - nr * D::H2;
+              {
+                const FFc* w2 = reinterpret_cast<const FFc*>(W2T) + k * D::NB;
+                float vxs = 0.f, vxc = 0.f, vys = 0.f, vyc = 0.f;
+  #pragma unroll
+                for (int n = 0; n < D::NB; ++n) {
+                  const FFc w = w2[n];
+                  ff_dot(vxs, vxc, gf[n], w.x);
+                  ff_dot(vys, vyc, gf[n], w.y);
+                }
+                if (nr < D::NM && h < D::H3) {
+                  const FFc* wa = reinterpret_cast<const FFc*>(WAT) + (nr * D::H3 + h) * D::NRY;
+  #pragma unroll
+                  for (int i = 0; i < D::NRY; ++i) {
+                    const FFc w = wa[i];
+                    ff_dot(vxs, vxc, w.x, rx[i]);
+                    ff_dot(vxs, vxc, ff_neg(w.y), ry[i]);
+                    ff_dot(vys, vyc, w.x, ry[i]);
+                    ff_dot(vys, vyc, w.y, rx[i]);
+                  }
+                }
+                contract_at(nr, h, C<R>{ff_d(vxs, vxc), ff_d(vys, vyc)});
+              }
+            }
           } else {
   #pragma unroll 1
             for (int nr = 0; nr < D::N2; ++nr)
@@ -2106,12 +2242,21 @@ __global__ void __launch_bounds__(64, MINB)
       const int nr = k / D::H2, h = k % D::H2, q = nr * (D::L2 + 1) + l_of_h(h);
       const R Mq = __shfl_sync(0xffffffffu, v, q), Mdq = __shfl_sync(0xffffffffu, dv, q);
       if (lane < D::NQ) {
+        // Y_h and its gradient by selection (h differs across the lanes)
+        C<R> y = Yh[0], dy[3] = {dYh[0][0], dYh[0][1], dYh[0][2]};
+#pragma unroll
+        for (int hh = 1; hh < D::H2; ++hh)
+          if (h == hh) {
+            y = Yh[hh];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) dy[c] = dYh[hh][c];
+          }
         const C<R> w = W0s[k];
         const R invm = rcp(mg);
-        tr += Mdq * re_mul(w, Yh[h]);
+        tr += Mdq * re_mul(w, y);
         const R sc = invm * Mq;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(w, dYh[h][c]);
+        for (int c = 0; c < 3; ++c) tt[c] += sc * re_mul(w, dy[c]);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
