@@ -282,6 +282,49 @@ __device__ __forceinline__ void mma_3xtf32(float (&d)[4], const uint32_t (&ah)[4
   mma_tf32(d, ah, bh0, bh1);
 }
 
+// ---------------------------------------------------------------------------
+// Float-float arithmetic for the FP64 path's contractions (FF). A double x is
+// carried as hi + lo with hi = x rounded to FP32 and lo = x - hi rounded
+// (48 bits of x). A dot product accumulates in (s, c): each product a b is
+// split exactly into p + e (p = a.hi b.hi, e its FMA residual plus the cross
+// terms a.hi b.lo + a.lo b.hi), s takes p by an error-free two-sum whose
+// error, with e, goes to c; the result is s + c in FP64 (Ogita, Rump and
+// Oishi's compensated dot product, "Dot2"). Its error is about 2^-48 of the
+// sum of |products|, against 2^-53 in FP64, and it runs on the FP32 pipe,
+// which on this part issues 64 times the FP64 pipe's operations.
+struct FFv {
+  float hi, lo;
+};
+__device__ __forceinline__ FFv ff_of(double x) {
+  const float h = d2f(x);
+  return {h, d2f(x - f2d(h))};  // x - h is exact in FP64
+}
+__device__ __forceinline__ double ff_d(float s, float c) { return f2d(s) + f2d(c); }
+// (s, c) += a b
+__device__ __forceinline__ void ff_dot(float& s, float& c, FFv a, FFv b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float t = s + p, z = t - s;
+  c += ((s - (t - z)) + (p - z)) + e;
+  s = t;
+}
+__device__ __forceinline__ FFv ff_neg(FFv a) { return {-a.hi, -a.lo}; }
+// a[h] for an h that differs across the lanes, by selection (no local memory)
+template <int N, class V>
+__device__ __forceinline__ V pick_of(const V (&a)[N], int h) {
+  V v = a[0];
+#pragma unroll
+  for (int j = 1; j < N; ++j)
+    if (h == j) v = a[j];
+  return v;
+}
+// a complex weight staged as float-float in the 16 bytes of a C<double>
+struct FFc {
+  FFv x, y;
+};
+
 // ===========================================================================
 // PACKED (split precision only): the M Y tile is stored as real and
 // imaginary planes of 32 columns, and the lanes accumulate column pairs with
@@ -311,6 +354,9 @@ __global__ void __launch_bounds__(64)
   static_assert(D::NRY == 16 && D::NB == 16 && D::NQ3 == 18 && D::NQ == 30, "tile shapes assume the Fe layout");
   extern __shared__ __align__(16) unsigned char smem[];
   using S = AbasisRows<D, TC>;
+  // FP64 path: the bond sums as float-float dot products on the FP32 pipe
+  constexpr bool FF = sizeof(R) == 8 && !PACKED && !TC;
+  static_assert(!FF || sizeof(FFc) == sizeof(C<R>), "float-float tiles reuse the FP64 rows");
   C<R>* sRY = reinterpret_cast<C<R>*>(smem);             // [TB][S::RY]
   C<R>* sQ = sRY + TB * S::RY;                            // [TB][S::Q] (PACKED: 2 x [TB][32] floats)
   constexpr size_t kQBytes = sizeof(C<R>) * S::Q > sizeof(float) * 64 ? sizeof(C<R>) * S::Q : sizeof(float) * 64;
@@ -356,6 +402,9 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
     for (int c = 0; c < 8; ++c) accx[c] = accy[c] = make_float2(0.f, 0.f);
     float dacc[10][4];  // TC: warp 0 D1 tiles [m-tile * 5 + n-tile], warp 1 D2 tiles [n-tile]
+    float ffa[15][4];   // FF: per column (Re sum, Re compensation, Im sum, Im compensation)
+#pragma unroll
+    for (int c = 0; c < 15; ++c) ffa[c][0] = ffa[c][1] = ffa[c][2] = ffa[c][3] = 0.f;
 #pragma unroll
     for (int u = 0; u < 10; ++u)
 #pragma unroll
@@ -446,7 +495,12 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
           for (int lm = 0; lm < D::LSA; ++lm) {
             const int l = l_of_lm(lm), mm = lm - l * l - l;
-            sRY[t * S::RY + n1 * D::LSA + lm] = cscale(y_full(Ya, l, mm), Rv[n1 * (D::LA + 1) + l]);
+            const C<R> ry = cscale(y_full(Ya, l, mm), Rv[n1 * (D::LA + 1) + l]);
+            if constexpr (FF) {
+              reinterpret_cast<FFc*>(sRY)[t * S::RY + n1 * D::LSA + lm] = {ff_of(ry.x), ff_of(ry.y)};
+            } else {
+              sRY[t * S::RY + n1 * D::LSA + lm] = ry;
+            }
           }
 #pragma unroll
         for (int nr = 0; nr < D::N2; ++nr)
@@ -457,14 +511,24 @@ __global__ void __launch_bounds__(64)
               sQx[t * 32 + nr * D::H2 + h] = q.x;
               sQy[t * 32 + nr * D::H2 + h] = q.y;
             } else {
-              sQ[t * S::Q + nr * D::H2 + h] = q;
+              if constexpr (FF) {
+                reinterpret_cast<FFc*>(sQ)[t * S::Q + nr * D::H2 + h] = {ff_of(q.x), ff_of(q.y)};
+              } else {
+                sQ[t * S::Q + nr * D::H2 + h] = q;
+              }
             }
           }
         if constexpr (PACKED) {
           for (int k = D::NQ; k < 32; ++k) sQx[t * 32 + k] = sQy[t * 32 + k] = 0.f;
         }
 #pragma unroll
-        for (int n = 0; n < D::NB; ++n) sg[t * S::G + n] = g[n];
+        for (int n = 0; n < D::NB; ++n) {
+          if constexpr (FF) {
+            reinterpret_cast<FFv*>(sg)[t * S::G + n] = ff_of(g[n]);
+          } else {
+            sg[t * S::G + n] = g[n];
+          }
+        }
         score[t] = cv[0];
       } else if constexpr (TC) {
         // a bond past the atom's last: zero rows (the GEMMs sum over all 64)
@@ -552,6 +616,38 @@ __global__ void __launch_bounds__(64)
             }
           }
         }
+      } else if constexpr (FF) {
+        // FP64 path: the same sums as compensated float-float dot products
+        // (the tile's features were split into hi/lo floats as they were
+        // written): ffa[c] = (Re sum, Re compensation, Im sum, Im compensation)
+        const FFc* RYf = reinterpret_cast<const FFc*>(sRY);
+        const FFc* Qf = reinterpret_cast<const FFc*>(sQ);
+        if (warp == 0) {
+          for (int b = 0; b < nb; ++b) {
+            const FFc ry = RYf[b * S::RY + row];
+            const FFv ryn = ff_neg(ry.y);
+#pragma unroll
+            for (int c = 0; c < 9; ++c) {
+              const int k3 = 9 * cb + c;
+              const FFc q = Qf[b * S::Q + (k3 / D::H3) * D::H2 + k3 % D::H3];
+              ff_dot(ffa[c][0], ffa[c][1], ry.x, q.x);
+              ff_dot(ffa[c][0], ffa[c][1], ryn, q.y);
+              ff_dot(ffa[c][2], ffa[c][3], ry.x, q.y);
+              ff_dot(ffa[c][2], ffa[c][3], ry.y, q.x);
+            }
+          }
+        } else {
+          const FFv* gf = reinterpret_cast<const FFv*>(sg);
+          for (int b = 0; b < nb; ++b) {
+            const FFv gv = gf[b * S::G + row];
+#pragma unroll
+            for (int c = 0; c < 15; ++c) {
+              const FFc q = Qf[b * S::Q + 15 * cb + c];
+              ff_dot(ffa[c][0], ffa[c][1], gv, q.x);
+              ff_dot(ffa[c][2], ffa[c][3], gv, q.y);
+            }
+          }
+        }
       } else if (warp == 0) {
         // A[row][9cb .. 9cb+8], row = (n1, l1 m1), column = (n2, l2 m2 >= 0)
         for (int b = 0; b < nb; ++b) {
@@ -632,6 +728,16 @@ __global__ void __launch_bounds__(64)
           if (k < D::NQ) accA2[row * D::NQ + k] = (c & 1) ? C<R>{x.y, y.y} : C<R>{x.x, y.x};
         }
       }
+    } else if constexpr (FF) {
+      if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c)
+          accA[row * D::NQ3 + 9 * cb + c] = {ff_d(ffa[c][0], ffa[c][1]), ff_d(ffa[c][2], ffa[c][3])};
+      } else {
+#pragma unroll
+        for (int c = 0; c < 15; ++c)
+          accA2[row * D::NQ + 15 * cb + c] = {ff_d(ffa[c][0], ffa[c][1]), ff_d(ffa[c][2], ffa[c][3])};
+      }
     } else if (warp == 0) {
 #pragma unroll
       for (int c = 0; c < 9; ++c) accA[row * D::NQ3 + 9 * cb + c] = acc[c];
@@ -704,7 +810,15 @@ __global__ void __launch_bounds__(64)
         const int k = k0 + lane;
         const int nr = k / D::LS2, lm = k % D::LS2, l = l_of_lm(lm), mm = lm - l * l - l;
         const R mv = __shfl_sync(0xffffffffu, v, k < D::N2 * D::LS2 ? nr * (D::L2 + 1) + l : 0);
-        if (k < D::N2 * D::LS2) Fa[m.offA0 + k] = cscale(y_full(Yi, l, mm), mv);
+        if (k < D::N2 * D::LS2) {
+          // y_full with (l, m) that differ across the lanes: Y by selection
+          C<R> yv = pick_of(Yi, ph(l, mm < 0 ? -mm : mm));
+          if (mm < 0) {
+            const R sg = R(parity(mm));
+            yv = {yv.x * sg, -yv.y * sg};
+          }
+          Fa[m.offA0 + k] = cscale(yv, mv);
+        }
       }
       if (lane == 0) {
         Fa[m.offOne] = {R(1), R(0)};
@@ -1692,49 +1806,6 @@ __device__ __forceinline__ void store_tile(double* __restrict__ dst, const doubl
 // as contiguous 16-byte stores (whole lines); chosen when the outputs are
 // host memory read over NVLink-C2C, where scattered 8-byte stores cost far
 // more than in device memory.
-// ---------------------------------------------------------------------------
-// Float-float arithmetic for the FP64 path's contractions (FF). A double x is
-// carried as hi + lo with hi = x rounded to FP32 and lo = x - hi rounded
-// (48 bits of x). A dot product accumulates in (s, c): each product a b is
-// split exactly into p + e (p = a.hi b.hi, e its FMA residual plus the cross
-// terms a.hi b.lo + a.lo b.hi), s takes p by an error-free two-sum whose
-// error, with e, goes to c; the result is s + c in FP64 (Ogita, Rump and
-// Oishi's compensated dot product, "Dot2"). Its error is about 2^-48 of the
-// sum of |products|, against 2^-53 in FP64, and it runs on the FP32 pipe,
-// which on this part issues 64 times the FP64 pipe's operations.
-struct FFv {
-  float hi, lo;
-};
-__device__ __forceinline__ FFv ff_of(double x) {
-  const float h = d2f(x);
-  return {h, d2f(x - f2d(h))};  // x - h is exact in FP64
-}
-__device__ __forceinline__ double ff_d(float s, float c) { return f2d(s) + f2d(c); }
-// (s, c) += a b
-__device__ __forceinline__ void ff_dot(float& s, float& c, FFv a, FFv b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  const float t = s + p, z = t - s;
-  c += ((s - (t - z)) + (p - z)) + e;
-  s = t;
-}
-__device__ __forceinline__ FFv ff_neg(FFv a) { return {-a.hi, -a.lo}; }
-// a[h] for an h that differs across the lanes, by selection (no local memory)
-template <int N, class V>
-__device__ __forceinline__ V pick_of(const V (&a)[N], int h) {
-  V v = a[0];
-#pragma unroll
-  for (int j = 1; j < N; ++j)
-    if (h == j) v = a[j];
-  return v;
-}
-// a complex weight staged as float-float in the 16 bytes of a C<double>
-struct FFc {
-  FFv x, y;
-};
-
 template <class R, class D, int MINB, bool PACKED, bool SOUT = false, bool FF = false>
 __global__ void __launch_bounds__(64, MINB)
     k_forces_fe(DeviceModel m, int natom, const int* __restrict__ off, const double* __restrict__ rr,
