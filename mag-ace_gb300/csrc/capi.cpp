@@ -108,7 +108,7 @@ struct Runtime {
       for (auto* b : {&grp_arity, &grp_len, &grp_first, &grp_seg, &slot_seg, &slot_factor, &slot_weight}) b->release();
     }
   } gb1, gb2;
-  DevBuf<float> b3_Cf, b3_cff, b3_mult, b3_cfw;
+  DevBuf<float> b3_Cf, b3_cff, b3_mult, b3_cfw, b3_Chl;
   DevBuf<double> b3_C64, b3_cf64, b3_cfw64, r_kap64;
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
   DevBuf<uint16_t> b3_code, b3_code2;
@@ -288,6 +288,14 @@ int upload_tables() {
         CUDA_TRY(R.b3_cfw64.upload(cfw));
       }
       CUDA_TRY(R.b3_C64.upload(D.C));
+      {
+        std::vector<float> hl(2 * D.C.size());
+        for (size_t q = 0; q < D.C.size(); ++q) {
+          hl[2 * q] = static_cast<float>(D.C[q]);
+          hl[2 * q + 1] = static_cast<float>(D.C[q] - static_cast<double>(hl[2 * q]));
+        }
+        CUDA_TRY(R.b3_Chl.upload(hl));
+      }
       CUDA_TRY(R.b3_cf64.upload(D.task_cf));
       CUDA_TRY(R.b3_factor.upload(D.factor_of));
       CUDA_TRY(R.b3_cw.upload(D.compact_of_weight));
@@ -358,6 +366,7 @@ int upload_tables() {
   d.b3_cw = R.b3_cw.p;
   d.b3_mult = R.b3_mult.p;
   d.b3_C64 = R.b3_C64.p;
+  d.b3_Chl = R.b3_Chl.p;
   d.b3_cf64 = R.b3_cf64.p;
   d.b3_cfw64 = R.b3_cfw64.p;
   d.b3_bound = M.db3.bound;
@@ -999,7 +1008,7 @@ void ace_release_device(void) {
   for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.r, &R.e, &R.magj, &R.mhj, &R.magi, &R.mhi, &R.energy, &R.fij,
                   &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
     b->release();
-  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult, &R.c1f}) b->release();
+  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult, &R.c1f, &R.b3_Chl}) b->release();
   for (auto* b : {&R.b3_pattern, &R.b3_combo, &R.b3_factor, &R.b3_cw}) b->release();
   R.b3_code.release();
   R.b3_code2.release();

@@ -94,6 +94,7 @@ struct DeviceModel {
   // FP64 copies for the plain-precision 3-body kernel, and the bound of its
   // gradients (model.hpp DenseB3::bound)
   const double* b3_C64;       // [combo][NM][I][I]
+  const float* b3_Chl;        // [combo][NM][I][I][2] the same as hi + lo floats (float-float tasks)
   const double* b3_cf64;      // [task]
   const double* b3_cfw64;     // [task]
   double b3_bound, b3_bound_rho;

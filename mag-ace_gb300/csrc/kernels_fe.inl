@@ -1546,14 +1546,6 @@ __global__ void __launch_bounds__(NW * 32, 1)
 // into the same integer sums, so nothing else is needed to combine them.
 constexpr int kB3Stride64 = 33;  // row stride of Xs in complex elements
 
-__device__ __forceinline__ C<double> b3_load64(const C<double>* Xs, unsigned code, int lane) {
-  const C<double> v = Xs[(code & 0x1fffu) * kB3Stride64 + lane];
-  const unsigned long long sx = static_cast<unsigned long long>(code & 0x8000u) << 48;
-  const unsigned long long sy = static_cast<unsigned long long>(code & 0x4000u) << 49;
-  return {__longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(__double_as_longlong(v.x)) ^ sx)),
-          __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(__double_as_longlong(v.y)) ^ sy))};
-}
-
 // one fixed-point contribution (v already scaled by 2^e)
 __device__ __forceinline__ void red_fix(unsigned long long* p, double v) {
   atomicAdd(p, static_cast<unsigned long long>(__double2ll_rn(v)));
@@ -1578,65 +1570,104 @@ __device__ __forceinline__ void b3_add64(unsigned long long* G, const uint16_t* 
   }
 }
 
-// One task on the lane's atom in FP64 (as b3_task): returns
-// sum C[p][i][j] Re(a_p X_i Y_j) and adds the gradients. Cg points at the
-// combination's coefficients [NM][I][I] in global memory.
-template <int PAT, class D>
-__device__ __forceinline__ double b3_task64(const double* __restrict__ Cg, const C<double>* Xs,
-                                            unsigned long long* G, const uint16_t* __restrict__ code,
-                                            const uint16_t* __restrict__ code2, double cfs, int lane) {
+// FF helpers for the 3-body task: a compensated sum (s, c) as hi + lo, and
+// acc += a b for complex float-float a, b into (Re s, Re c, Im s, Im c)
+__device__ __forceinline__ FFv ff_norm(float s, float c) {
+  const float h = s + c;
+  return {h, c - (h - s)};
+}
+__device__ __forceinline__ void ff_cmac(float (&acc)[4], FFc a, FFc b) {
+  ff_dot(acc[0], acc[1], a.x, b.x);
+  ff_dot(acc[0], acc[1], ff_neg(a.y), b.y);
+  ff_dot(acc[2], acc[3], a.x, b.y);
+  ff_dot(acc[2], acc[3], a.y, b.x);
+}
+__device__ __forceinline__ FFc b3_load_ff(const FFc* Xs, unsigned code, int lane) {
+  FFc v = Xs[(code & 0x1fffu) * kB3Stride64 + lane];
+  const unsigned sx = (code & 0x8000u) << 16, sy = (code & 0x4000u) << 17;
+  v.x = {__uint_as_float(__float_as_uint(v.x.hi) ^ sx), __uint_as_float(__float_as_uint(v.x.lo) ^ sx)};
+  v.y = {__uint_as_float(__float_as_uint(v.y.hi) ^ sy), __uint_as_float(__float_as_uint(v.y.lo) ^ sy)};
+  return v;
+}
+
+// b3_task64 with its arithmetic in float-float (the factors staged as hi/lo
+// floats, the coefficients Chl [NM][I][I] as hi/lo pairs): every sum a
+// compensated dot product on the FP32 pipe, the fixed-point contributions
+// formed in FP64 from them as before. One body serves the three patterns:
+// the loop over i is not unrolled and the row bounds are run-time values
+// (uniform over the warp), so that the code stays within the instruction
+// cache; Y and its gradient stay in registers (the loops over j unrolled).
+template <class D>
+__device__ __forceinline__ int jmax_rt(int pat, int i) {
+  constexpr int NM = D::NM;
+  return pat == 0 ? i + 1 : (pat == 1 ? (i / NM + 1) * NM : (i / NM) * NM);
+}
+template <class D>
+__device__ __forceinline__ double b3_task64_ff(int pat, const float* __restrict__ Chl, const FFc* Xs,
+                                               unsigned long long* G, const uint16_t* __restrict__ code,
+                                               const uint16_t* __restrict__ code2, double cfs, int lane) {
   constexpr int I = D::I, NM = D::NM;
-  static_assert(I % 2 == 0, "rows of C are read as double2");
-  constexpr int JUSED = jmax_of<PAT, I, NM>(I - 1);
-  C<double> Y[I], gY[I], a[NM], ga[NM];
+  static_assert(I % 2 == 0, "rows of C are read two coefficients at a time");
+  const int jused = jmax_rt<D>(pat, I - 1);
+  FFc Y[I], a[NM];
+  float gY[I][4], ga[NM][4];
 #pragma unroll
   for (int j = 0; j < I; ++j) {
-    Y[j] = j < JUSED ? b3_load64(Xs, __ldg(code + NM + I + j), lane) : C<double>{0.0, 0.0};
-    gY[j] = {0.0, 0.0};
+    Y[j] = j < jused ? b3_load_ff(Xs, __ldg(code + NM + I + j), lane) : FFc{{0.f, 0.f}, {0.f, 0.f}};
+    gY[j][0] = gY[j][1] = gY[j][2] = gY[j][3] = 0.f;
   }
 #pragma unroll
   for (int p = 0; p < NM; ++p) {
-    a[p] = b3_load64(Xs, __ldg(code + p), lane);
-    ga[p] = {0.0, 0.0};
+    a[p] = b3_load_ff(Xs, __ldg(code + p), lane);
+    ga[p][0] = ga[p][1] = ga[p][2] = ga[p][3] = 0.f;
   }
-  double rt = 0.0;
-#pragma unroll
+  float rts = 0.f, rtc = 0.f;
+#pragma unroll 1
   for (int i = 0; i < I; ++i) {
-    const int jm = jmax_of<PAT, I, NM>(i);
+    const int jm = jmax_rt<D>(pat, i);
     if (jm == 0) continue;
-    const C<double> x = b3_load64(Xs, __ldg(code + NM + i), lane);
-    C<double> az = {0.0, 0.0};
+    const FFc x = b3_load_ff(Xs, __ldg(code + NM + i), lane);
+    float az[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int p = 0; p < NM; ++p) {
-      C<double> z = {0.0, 0.0};
-      const C<double> ax = cmul(a[p], x);
-      const double2* crow = reinterpret_cast<const double2*>(Cg + (p * I + i) * I);
+      float t[4] = {0.f, 0.f, 0.f, 0.f};
+      ff_cmac(t, a[p], x);
+      const FFc ax = {ff_norm(t[0], t[1]), ff_norm(t[2], t[3])};
+      float z[4] = {0.f, 0.f, 0.f, 0.f};
+      const float4* crow = reinterpret_cast<const float4*>(Chl + 2 * (p * I + i) * I);
 #pragma unroll
-      for (int j2 = 0; j2 < (jm + 1) / 2; ++j2) {
-        const double2 c2 = __ldg(crow + j2);
-        const double cv[2] = {c2.x, c2.y};
+      for (int j2 = 0; j2 < I / 2; ++j2) {
+        if (2 * j2 >= jm) break;
+        const float4 c4 = __ldg(crow + j2);
+        const FFv cv[2] = {{c4.x, c4.y}, {c4.z, c4.w}};
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const int j = 2 * j2 + u;
           if (j < jm) {
-            z.x = fma(cv[u], Y[j].x, z.x);
-            z.y = fma(cv[u], Y[j].y, z.y);
-            gY[j].x = fma(cv[u], ax.x, gY[j].x);
-            gY[j].y = fma(cv[u], ax.y, gY[j].y);
+            ff_dot(z[0], z[1], cv[u], Y[j].x);
+            ff_dot(z[2], z[3], cv[u], Y[j].y);
+            ff_dot(gY[j][0], gY[j][1], cv[u], ax.x);
+            ff_dot(gY[j][2], gY[j][3], cv[u], ax.y);
           }
         }
       }
-      cmac(az, a[p], z);
-      cmac(ga[p], x, z);
+      const FFc zf = {ff_norm(z[0], z[1]), ff_norm(z[2], z[3])};
+      ff_cmac(az, a[p], zf);
+      ff_cmac(ga[p], x, zf);
     }
-    rt = re_mac(rt, x, az);
-    b3_add64(G, code, code2, NM + i, az, cfs);
+    const FFc azf = {ff_norm(az[0], az[1]), ff_norm(az[2], az[3])};
+    ff_dot(rts, rtc, x.x, azf.x);
+    ff_dot(rts, rtc, ff_neg(x.y), azf.y);
+    b3_add64(G, code, code2, NM + i, C<double>{ff_d(az[0], az[1]), ff_d(az[2], az[3])}, cfs);
   }
 #pragma unroll
-  for (int j = 0; j < JUSED; ++j) b3_add64(G, code, code2, NM + I + j, gY[j], cfs);
+  for (int j = 0; j < I; ++j)
+    if (j < jused)
+      b3_add64(G, code, code2, NM + I + j, C<double>{ff_d(gY[j][0], gY[j][1]), ff_d(gY[j][2], gY[j][3])}, cfs);
 #pragma unroll
-  for (int p = 0; p < NM; ++p) b3_add64(G, code, code2, p, ga[p], cfs);
-  return rt;
+  for (int p = 0; p < NM; ++p)
+    b3_add64(G, code, code2, p, C<double>{ff_d(ga[p][0], ga[p][1]), ff_d(ga[p][2], ga[p][3])}, cfs);
+  return ff_d(rts, rtc);
 }
 
 // Shared memory: Xs[nc][33] (complex FP64) and the factor map [nc]. G3i is
@@ -1692,7 +1723,8 @@ __global__ void __launch_bounds__(NW * 32, 1)
           v[b] = ab + b < na ? F[static_cast<size_t>(s_atom[ab + b]) * m.nF + fc] : C<double>{0.0, 0.0};
 #pragma unroll
         for (int b = 0; b < kBatch; ++b) {
-          Xs[c * kB3Stride64 + ab + b] = v[b];
+          // staged as hi/lo floats for the float-float tasks
+          reinterpret_cast<FFc*>(Xs)[c * kB3Stride64 + ab + b] = {ff_of(v[b].x), ff_of(v[b].y)};
           const double f = fabs(v[b].x) + fabs(v[b].y);
           // NaN compares as the largest pattern and is caught below
           atomicMax(&s_fm[ab + b], static_cast<unsigned long long>(__double_as_longlong(f)));
@@ -1732,11 +1764,9 @@ __global__ void __launch_bounds__(NW * 32, 1)
       const double cfs = __ldg(m.b3_cf64 + tk) * gscale;
       const uint16_t* code = m.b3_code + tk * NPOS;
       const uint16_t* code2 = m.b3_code2 + tk * NPOS;
-      const double* Ck = m.b3_C64 + static_cast<size_t>(k) * NM * I * I;
-      double r;
-      if (pat == 0) r = b3_task64<0, D>(Ck, Xs, G, code, code2, cfs, lane);
-      else if (pat == 1) r = b3_task64<1, D>(Ck, Xs, G, code, code2, cfs, lane);
-      else r = b3_task64<2, D>(Ck, Xs, G, code, code2, cfs, lane);
+      const float* Ck = m.b3_Chl + 2 * static_cast<size_t>(k) * NM * I * I;
+      const FFc* Xf = reinterpret_cast<const FFc*>(Xs);
+      const double r = b3_task64_ff<D>(pat, Ck, Xf, G, code, code2, cfs, lane);
       racc += __double2ll_rn(__ldg(m.b3_cfw64 + tk) * rscale * r);
       int nx = 0;
       if (lane == 0) nx = atomicAdd(&s_next, 1);
