@@ -108,7 +108,7 @@ struct Runtime {
       for (auto* b : {&grp_arity, &grp_len, &grp_first, &grp_seg, &slot_seg, &slot_factor, &slot_weight}) b->release();
     }
   } gb1, gb2;
-  DevBuf<float> b3_Cf, b3_cff, b3_mult, b3_cfw, b3_Chl;
+  DevBuf<float> b3_Cf, b3_cff, b3_mult, b3_cfw, b3_Chl, r_kaphl;
   DevBuf<double> b3_C64, b3_cf64, b3_cfw64, r_kap64;
   DevBuf<int32_t> b3_pattern, b3_combo, b3_factor, b3_cw;
   DevBuf<uint16_t> b3_code, b3_code2;
@@ -306,6 +306,14 @@ int upload_tables() {
       CUDA_TRY(R.r_g0.upload(T.slot_g0));
       CUDA_TRY(R.r_rec.upload(T.rec));
       CUDA_TRY(R.r_kap64.upload(T.kap));
+      {
+        std::vector<float> hl(2 * T.kap.size());
+        for (size_t q = 0; q < T.kap.size(); ++q) {
+          hl[2 * q] = static_cast<float>(T.kap[q]);
+          hl[2 * q + 1] = static_cast<float>(T.kap[q] - static_cast<double>(hl[2 * q]));
+        }
+        CUDA_TRY(R.r_kaphl.upload(hl));
+      }
       CUDA_TRY(R.r_warp_begin.upload(T.warp_begin));
       CUDA_TRY(R.r_warp_slots.upload(T.warp_slots));
       CUDA_TRY(R.r_stream.upload(T.stream));
@@ -381,6 +389,7 @@ int upload_tables() {
   d.r_run = R.r_run.p;
   d.r_rec = R.r_rec.p;
   d.r_kap64 = R.r_kap64.p;
+  d.r_kaphl = R.r_kaphl.p;
   d.r_g0 = R.r_g0.p;
   d.r_warp_begin = R.r_warp_begin.p;
   d.r_warp_slots = R.r_warp_slots.p;
@@ -1008,7 +1017,7 @@ void ace_release_device(void) {
   for (auto* b : {&R.lut_a, &R.lut_m, &R.c1, &R.r, &R.e, &R.magj, &R.mhj, &R.magi, &R.mhi, &R.energy, &R.fij,
                   &R.tij, &R.ti0, &R.rho1, &R.core, &R.edf, &R.dedrho})
     b->release();
-  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult, &R.c1f, &R.b3_Chl}) b->release();
+  for (auto* b : {&R.lut_a32, &R.lut_m32, &R.b3_Cf, &R.b3_cff, &R.b3_mult, &R.c1f, &R.b3_Chl, &R.r_kaphl}) b->release();
   for (auto* b : {&R.b3_pattern, &R.b3_combo, &R.b3_factor, &R.b3_cw}) b->release();
   R.b3_code.release();
   R.b3_code2.release();

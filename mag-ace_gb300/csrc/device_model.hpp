@@ -104,6 +104,7 @@ struct DeviceModel {
   const int32_t* r_run;         // [3 * nslot + 1]
   const uint32_t* r_rec;        // [entries][4]
   const double* r_kap64;        // [entries] kappa in FP64
+  const float* r_kaphl;         // [entries][2] kappa as hi + lo floats (float-float entries)
   const int32_t* r_g0;
   const int32_t* r_warp_begin;  // [warps + 1]
   const int32_t* r_warp_slots;

@@ -324,6 +324,18 @@ __device__ __forceinline__ V pick_of(const V (&a)[N], int h) {
 struct FFc {
   FFv x, y;
 };
+// a compensated sum (s, c) as hi + lo, and acc += a b for complex
+// float-float a, b into (Re s, Re c, Im s, Im c)
+__device__ __forceinline__ FFv ff_norm(float s, float c) {
+  const float h = s + c;
+  return {h, c - (h - s)};
+}
+__device__ __forceinline__ void ff_cmac(float (&acc)[4], FFc a, FFc b) {
+  ff_dot(acc[0], acc[1], a.x, b.x);
+  ff_dot(acc[0], acc[1], ff_neg(a.y), b.y);
+  ff_dot(acc[2], acc[3], a.x, b.y);
+  ff_dot(acc[2], acc[3], a.y, b.x);
+}
 
 // ===========================================================================
 // PACKED (split precision only): the M Y tile is stored as real and
@@ -1023,19 +1035,39 @@ __global__ void __launch_bounds__(NW * 32, 1)
 constexpr int kRestStride64 = 17;  // row stride of Fs in complex elements
 constexpr int kRestWarps64 = 16;   // warps per CTA of k_rest64
 
+// the entries [e0, e1) (every second one) of arity A in float-float: the
+// factors staged as hi/lo floats (Fs), the coefficients as hi/lo pairs
+// (kap), the slot sums compensated (vx, vy: sum, compensation); a product of
+// two or three factors is formed as a compensated complex product and
+// rounded to hi/lo before the next
 template <int A>
-__device__ __forceinline__ void rest_run64(const uint4* __restrict__ rec, const double* __restrict__ kap, int e0,
-                                           int e1, const C<double>* Fs, int al, C<double>& v) {
+__device__ __forceinline__ void rest_run64(const uint4* __restrict__ rec, const float* __restrict__ kap, int e0,
+                                           int e1, const FFc* Fs, int al, float (&vx)[2], float (&vy)[2]) {
 #pragma unroll 2
   for (int e = e0; e < e1; e += 2) {
     const uint4 r = __ldg(rec + e);
-    const double k = __ldg(kap + e);
-    C<double> p = Fs[(r.y & 0xffffu) * kRestStride64 + al];
-    if (A >= 2) p = cmul(p, Fs[(r.y >> 16) * kRestStride64 + al]);
-    if (A >= 3) p = cmul(p, Fs[r.z * kRestStride64 + al]);
-    v.x = fma(k, p.x, v.x);
-    v.y = fma(k, p.y, v.y);
+    const float2 kk = __ldg(reinterpret_cast<const float2*>(kap) + e);
+    const FFv k = {kk.x, kk.y};
+    FFc p = Fs[(r.y & 0xffffu) * kRestStride64 + al];
+    if (A >= 2) {
+      float t[4] = {0.f, 0.f, 0.f, 0.f};
+      ff_cmac(t, p, Fs[(r.y >> 16) * kRestStride64 + al]);
+      p = {ff_norm(t[0], t[1]), ff_norm(t[2], t[3])};
+    }
+    if (A >= 3) {
+      float t[4] = {0.f, 0.f, 0.f, 0.f};
+      ff_cmac(t, p, Fs[r.z * kRestStride64 + al]);
+      p = {ff_norm(t[0], t[1]), ff_norm(t[2], t[3])};
+    }
+    ff_dot(vx[0], vx[1], k, p.x);
+    ff_dot(vy[0], vy[1], k, p.y);
   }
+}
+// (s, c) += (s2, c2), error-free in s
+__device__ __forceinline__ void ff_add_sum(float& s, float& c, float s2, float c2) {
+  const float t = s + s2, z = t - s;
+  c += ((s - (t - z)) + (s2 - z)) + c2;
+  s = t;
 }
 
 template <class D, int NW>
@@ -1046,7 +1078,8 @@ __global__ void __launch_bounds__(NW * 32, 1)
   extern __shared__ __align__(16) unsigned char smem[];
   const int nf = m.r_nfac, nW = m.nW;
   const GatherView& g = m.g2;  // slot weights and multiplicities (same slot numbering)
-  C<double>* Fs = reinterpret_cast<C<double>*>(smem);                    // [nf][17]
+  C<double>* Fs = reinterpret_cast<C<double>*>(smem);                    // [nf][17] (as hi/lo floats)
+  const FFc* Ff = reinterpret_cast<const FFc*>(Fs);
   double* rpart = reinterpret_cast<double*>(Fs + nf * kRestStride64);    // [NW][16]
   __shared__ int s_atom[16];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, al = lane & 15, half = lane >> 4;
@@ -1065,7 +1098,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
       for (int b = 0; b < 16; ++b)
         v[b] = b < na ? F[static_cast<size_t>(s_atom[b]) * m.nF + fc] : C<double>{0.0, 0.0};
 #pragma unroll
-      for (int b = 0; b < 16; ++b) Fs[c * kRestStride64 + b] = v[b];
+      for (int b = 0; b < 16; ++b) reinterpret_cast<FFc*>(Fs)[c * kRestStride64 + b] = {ff_of(v[b].x), ff_of(v[b].y)};
     }
     __syncthreads();
     const int atom = al < na ? s_atom[al] : -1;
@@ -1073,15 +1106,23 @@ __global__ void __launch_bounds__(NW * 32, 1)
     for (int sw = warp; sw < kRestTableWarps; sw += NW)
       for (int q = __ldg(m.r_warp_begin + sw); q < __ldg(m.r_warp_begin + sw + 1); ++q) {
         const int s = __ldg(m.r_warp_slots + q);
-        C<double> v = {0.0, 0.0};
-        rest_run64<1>(rec, m.r_kap64, __ldg(m.r_run + 3 * s) + half, __ldg(m.r_run + 3 * s + 1), Fs, al, v);
-        rest_run64<2>(rec, m.r_kap64, __ldg(m.r_run + 3 * s + 1) + half, __ldg(m.r_run + 3 * s + 2), Fs, al, v);
-        rest_run64<3>(rec, m.r_kap64, __ldg(m.r_run + 3 * s + 2) + half, __ldg(m.r_run + 3 * s + 3), Fs, al, v);
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, 16);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, 16);
+        float vx[2] = {0.f, 0.f}, vy[2] = {0.f, 0.f};
+        rest_run64<1>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s) + half, __ldg(m.r_run + 3 * s + 1), Ff, al, vx, vy);
+        rest_run64<2>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s + 1) + half, __ldg(m.r_run + 3 * s + 2), Ff, al, vx,
+                      vy);
+        rest_run64<3>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s + 2) + half, __ldg(m.r_run + 3 * s + 3), Ff, al, vx,
+                      vy);
+        // the other half-warp's sums (lanes 16-31 add lanes 0-15's, and the
+        // reverse; only lanes 0-15 use the result)
+        ff_add_sum(vx[0], vx[1], __shfl_xor_sync(0xffffffffu, vx[0], 16), __shfl_xor_sync(0xffffffffu, vx[1], 16));
+        ff_add_sum(vy[0], vy[1], __shfl_xor_sync(0xffffffffu, vy[0], 16), __shfl_xor_sync(0xffffffffu, vy[1], 16));
+        const C<double> v = {ff_d(vx[0], vx[1]), ff_d(vy[0], vy[1])};
         if (half == 0) {
           const int g0 = __ldg(m.r_g0 + s);
-          if (g0 >= 0) rloc = re_mac(rloc, Fs[g0 * kRestStride64 + al], v);
+          if (g0 >= 0) {
+            const FFc f = Ff[g0 * kRestStride64 + al];
+            rloc = re_mac(rloc, C<double>{f2d(f.x.hi) + f2d(f.x.lo), f2d(f.y.hi) + f2d(f.y.lo)}, v);
+          }
           const int w = __ldg(g.slot_weight + s);
           if (w >= 0 && atom >= 0) {
             const double mu = __ldg(g.slot_mult + s);
@@ -1570,18 +1611,6 @@ __device__ __forceinline__ void b3_add64(unsigned long long* G, const uint16_t* 
   }
 }
 
-// FF helpers for the 3-body task: a compensated sum (s, c) as hi + lo, and
-// acc += a b for complex float-float a, b into (Re s, Re c, Im s, Im c)
-__device__ __forceinline__ FFv ff_norm(float s, float c) {
-  const float h = s + c;
-  return {h, c - (h - s)};
-}
-__device__ __forceinline__ void ff_cmac(float (&acc)[4], FFc a, FFc b) {
-  ff_dot(acc[0], acc[1], a.x, b.x);
-  ff_dot(acc[0], acc[1], ff_neg(a.y), b.y);
-  ff_dot(acc[2], acc[3], a.x, b.y);
-  ff_dot(acc[2], acc[3], a.y, b.x);
-}
 __device__ __forceinline__ FFc b3_load_ff(const FFc* Xs, unsigned code, int lane) {
   FFc v = Xs[(code & 0x1fffu) * kB3Stride64 + lane];
   const unsigned sx = (code & 0x8000u) << 16, sy = (code & 0x4000u) << 17;
