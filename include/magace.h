@@ -79,7 +79,10 @@ void ace_clear_error(void);
 int ace_init_file(const char* path, const char* element, double rcut, double rcut_magnetic,
                   double smear, int xcnumber);
 
-/* 0 = plain FP64 throughout (the drop-in default, parity <= 1e-10 relative).
+/* 0 = FP64 (the drop-in default, parity <= 1e-10 relative, bitwise
+ *     reproducible): features, densities, embedding and outputs in double;
+ *     with the specialised kernels the contractions run as compensated
+ *     float-float dot products (48-bit operands, about 1e-14 from FP64).
  * 1 = split precision: FP32 basis/products with FP64 accumulation of the
  *     per-atom energy and the embedding near zero density. */
 int ace_set_precision(int mode);
