@@ -219,14 +219,17 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def profiled_traffic(kernel: str, path: str, ncell: int):
+def profiled_traffic(kernel: str, path: str, ncell: int, tuning=None):
     """DRAM bytes (read + write) of one launch of `kernel` from the committed
     ncu summary of the same workload (profiles/*_split_16k.md, the default
-    20^3-cell workload in split precision), or None when there is none."""
+    20^3-cell workload in split precision), or None when there is none.
+    `tuning` (the four variant indices ace_get_tuning reports) picks the
+    force kernel's form: variants 6 and 7 are the tensor-core k_forces_tc."""
     if path != "split" or ncell != 20:
         return None
+    forces = "k_forces_tc" if tuning is None or tuning[3] >= 6 else "k_forces_fe"
     name = {"k_abasis": "k_abasis_fe", "k_density": "k_density_fe", "k_b3": "k_b3_fe",
-            "k_forces": "k_forces_fe"}.get(kernel)
+            "k_forces": forces}.get(kernel)
     f = os.path.join(REPO, "profiles", f"{name}_split_16k.md") if name else None
     if not f or not os.path.exists(f):
         return None
@@ -386,7 +389,7 @@ def gpu_arm(args, rank, world, local_rank):
     if P["launches"] >= 4:  # split path of the specialised layout: the density kernel has the rest terms only
         kflops["k_density"] = flops["k_density_rest"]
     dom = int(np.argmax(kms))
-    traffic = profiled_traffic(names[dom], headline, args.ncell)
+    traffic = profiled_traffic(names[dom], headline, args.ncell, lib.get_tuning_indices())
     fp_peak = peaks.get("fp64" if headline == "fp64" else "fp32")
     achieved = kflops[names[dom]] / (kms[dom] / 1e3) / 1e12
     line = {

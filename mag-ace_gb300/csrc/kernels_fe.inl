@@ -2224,20 +2224,6 @@ __global__ void __launch_bounds__(64, MINB)
   #pragma unroll
             for (int c = 0; c < 3; ++c) tt[c] = re_mac(tt[c], sv, dYm[h][c]);
           };
-          // the same for an h only known at run time (Y and dY by selection)
-          const auto contract_at = [&](int nr, int h, C<R> V) {
-            const int q = nr * (D::L2 + 1) + l_of_h(h);
-            tr = fma(cMd[q * T + t], re_mul(V, pick_of(Ym, h)), tr);
-            const C<R> sv = cscale(V, invm * cM[q * T + t]);
-  #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              C<R> d = dYm[0][c];
-  #pragma unroll
-              for (int j = 1; j < D::H2; ++j)
-                if (h == j) d = dYm[j][c];
-              tt[c] = re_mac(tt[c], sv, d);
-            }
-          };
           if constexpr (PACKED) {
             float2 g2[D::NB / 2], RYx2[D::NRY / 2], RYy2[D::NRY / 2], RYyn2[D::NRY / 2];
   #pragma unroll
@@ -2290,10 +2276,15 @@ __global__ void __launch_bounds__(64, MINB)
               rx[i] = ff_of(RY[i].x);
               ry[i] = ff_of(RY[i].y);
             }
+            // per h, Z = sum_nr M_q V_k and Zd = sum_nr M'_q V_k (q = nr (L2 + 1)
+            // + l(h), k = nr H2 + h), then one contraction with Y_h, dY_h:
+            // tr += Re(Zd Y_h), tt += Re(Z dY_h) / |m|
   #pragma unroll 1
-            for (int k = 0; k < D::NQ; ++k) {
-              const int nr = k / D::H2, h = k - nr * D::H2;
-              {
+            for (int h = 0; h < D::H2; ++h) {
+              C<R> Z = {R(0), R(0)}, Zd = {R(0), R(0)};
+  #pragma unroll 1
+              for (int nr = 0; nr < D::N2; ++nr) {
+                const int k = nr * D::H2 + h;
                 const FFc* w2 = reinterpret_cast<const FFc*>(W2T) + k * D::NB;
                 float vxs = 0.f, vxc = 0.f, vys = 0.f, vyc = 0.f;
   #pragma unroll
@@ -2313,7 +2304,23 @@ __global__ void __launch_bounds__(64, MINB)
                     ff_dot(vys, vyc, w.y, rx[i]);
                   }
                 }
-                contract_at(nr, h, C<R>{ff_d(vxs, vxc), ff_d(vys, vyc)});
+                const R vx = ff_d(vxs, vxc), vy = ff_d(vys, vyc);
+                const int q = nr * (D::L2 + 1) + l_of_h(h);
+                const R s = cM[q * T + t], sd = cMd[q * T + t];
+                Z.x = fma(s, vx, Z.x);
+                Z.y = fma(s, vy, Z.y);
+                Zd.x = fma(sd, vx, Zd.x);
+                Zd.y = fma(sd, vy, Zd.y);
+              }
+              tr += re_mul(Zd, pick_of(Ym, h));
+              const C<R> sz = cscale(Z, invm);
+  #pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                C<R> d = dYm[0][c];
+  #pragma unroll
+                for (int j = 1; j < D::H2; ++j)
+                  if (h == j) d = dYm[j][c];
+                tt[c] = re_mac(tt[c], sz, d);
               }
             }
           } else {
