@@ -2505,9 +2505,29 @@ __global__ void __launch_bounds__(64, MINB)
     // (the weights are staged in the rows' space first, then scattered)
     C<R>* raw = reinterpret_cast<C<R>*>(QA);  // W2[n][k], then W_A[i][k]
     static_assert(sizeof(C<R>) * (D::NA2H + D::NWA) <= sizeof(float) * 64 * kTcRow, "the weights fit in the rows");
-    for (int q = t; q < D::NA2H; q += T) raw[q] = weight(m.offW2 + q, -1);
-    for (int q = t; q < D::NWA; q += T) raw[D::NA2H + q] = weight(q, q);
-    if (t < D::NQ) W0s[t] = weight(m.offW0 + t, Ga ? __ldg(m.b3_cw + m.offW0 + t) : -1);
+    // the atom's bond range and scalars, then every weight load of the
+    // thread in flight at once, then the first tile's bond inputs (their
+    // latency hidden behind the weights' stores and scatter)
+    const R edf = to_r<R>(edf_in[atom]);
+    const int b0 = off[atom], b1 = off[atom + 1];
+    constexpr int N1 = (D::NA2H + T - 1) / T, N2 = (D::NWA + T - 1) / T;
+    {
+      C<R> v1[N1], v2[N2];
+#pragma unroll
+      for (int u = 0; u < N1; ++u)
+        v1[u] = t + u * T < D::NA2H ? weight(m.offW2 + t + u * T, -1) : C<R>{R(0), R(0)};
+#pragma unroll
+      for (int u = 0; u < N2; ++u) v2[u] = t + u * T < D::NWA ? weight(t + u * T, t + u * T) : C<R>{R(0), R(0)};
+      if (t < D::NQ) W0s[t] = weight(m.offW0 + t, Ga ? __ldg(m.b3_cw + m.offW0 + t) : -1);
+#pragma unroll
+      for (int u = 0; u < N1; ++u)
+        if (t + u * T < D::NA2H) raw[t + u * T] = v1[u];
+#pragma unroll
+      for (int u = 0; u < N2; ++u)
+        if (t + u * T < D::NWA) raw[D::NA2H + t + u * T] = v2[u];
+    }
+    R sp0[8];
+    if (stage && b0 + t < b1) ld8_l2(stage + 8 * static_cast<size_t>(b0 + t), sp0, pol_first);
     float* Bs = reinterpret_cast<float*>(Bf);
     for (int q = t; q < kTcFrags * 16; q += T) reinterpret_cast<float4*>(Bs)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
@@ -2541,8 +2561,6 @@ __global__ void __launch_bounds__(64, MINB)
       put3(D::NB + D::NRY + i, 2 * k + 1, w.x);
     }
     __syncthreads();  // the fragments are built; the rows are free
-    const R edf = to_r<R>(edf_in[atom]);
-    const int b0 = off[atom], b1 = off[atom + 1];
     float* row = QA + t * kTcRow;                  // this thread's bond row
     const float* wrows = QA + warp * 32 * kTcRow;  // the warp's 32 rows
     for (int jt = b0; jt < b1; jt += T) {
@@ -2556,7 +2574,12 @@ __global__ void __launch_bounds__(64, MINB)
         if (live) {
           if (stage) {  // the A-basis kernel's copy in device memory
             R sp[8];
-            ld8_l2(stage + 8 * static_cast<size_t>(j), sp, pol_first);
+            if (jt == b0) {
+#pragma unroll
+              for (int q = 0; q < 8; ++q) sp[q] = sp0[q];
+            } else {
+              ld8_l2(stage + 8 * static_cast<size_t>(j), sp, pol_first);
+            }
             r = sp[0];
             ex = sp[1];
             ey = sp[2];
