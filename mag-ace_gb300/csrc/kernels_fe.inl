@@ -1657,10 +1657,13 @@ __device__ __forceinline__ double b3_task64_ff(int pat, const float* __restrict_
     if (jm == 0) continue;
     const FFc x = b3_load_ff(Xs, __ldg(code + NM + i), lane);
     float az[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
+    // the n0' loop is not unrolled either (a by selection, ga by a guarded
+    // update): the body then fits the instruction cache
+#pragma unroll 1
     for (int p = 0; p < NM; ++p) {
+      const FFc ap = pick_of(a, p);
       float t[4] = {0.f, 0.f, 0.f, 0.f};
-      ff_cmac(t, a[p], x);
+      ff_cmac(t, ap, x);
       const FFc ax = {ff_norm(t[0], t[1]), ff_norm(t[2], t[3])};
       float z[4] = {0.f, 0.f, 0.f, 0.f};
       const float4* crow = reinterpret_cast<const float4*>(Chl + 2 * (p * I + i) * I);
@@ -1681,8 +1684,10 @@ __device__ __forceinline__ double b3_task64_ff(int pat, const float* __restrict_
         }
       }
       const FFc zf = {ff_norm(z[0], z[1]), ff_norm(z[2], z[3])};
-      ff_cmac(az, a[p], zf);
-      ff_cmac(ga[p], x, zf);
+      ff_cmac(az, ap, zf);
+#pragma unroll
+      for (int q = 0; q < NM; ++q)
+        if (q == p) ff_cmac(ga[q], x, zf);
     }
     const FFc azf = {ff_norm(az[0], az[1]), ff_norm(az[2], az[3])};
     ff_dot(rts, rtc, x.x, azf.x);
