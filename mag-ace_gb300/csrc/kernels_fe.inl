@@ -1891,8 +1891,7 @@ __global__ void __launch_bounds__(64, MINB)
   R* cM = cRd + D::NR * T;
   R* cMd = cM + D::NMF * T;
   C<R>* cYa = reinterpret_cast<C<R>*>(cMd + D::NMF * T);  // full [LSA]
-  C<R>* cdYa = cYa + D::LSA * T;                         // [LSA][3]
-  double* sOut = reinterpret_cast<double*>(cdYa + D::LSA * 3 * T);  // SOUT: the tile's f_ij [T][3], then t_ij [T][3]
+  double* sOut = reinterpret_cast<double*>(cYa + D::LSA * T);  // SOUT: the tile's f_ij [T][3], then t_ij [T][3]
   const int t = threadIdx.x;
   static_assert(!PACKED || sizeof(R) == 4, "packed contractions are FP32");
   static_assert(D::NB % 4 == 0 && D::NRY % 4 == 0, "planes are read four floats at a time");
@@ -2063,21 +2062,12 @@ __global__ void __launch_bounds__(64, MINB)
         }
         C<R> Ym[D::H2], dYm[D::H2][3];
         {
-          C<R> Ya[D::HA], dYa[D::HA][3];
-          ylm_half<R, true>(D::LA, ex, ey, ez, Ya, dYa);
+          C<R> Ya[D::HA];
+          ylm_half<R, false>(D::LA, ex, ey, ez, Ya, nullptr);
   #pragma unroll
           for (int lm = 0; lm < D::LSA; ++lm) {
             const int l = l_of_lm(lm), mm = lm - l * l - l;
             cYa[lm * T + t] = y_full(Ya, l, mm);
-  #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              C<R> d = dYa[ph(l, mm < 0 ? -mm : mm)][c];
-              if (mm < 0) {
-                const R s = R(parity(mm));
-                d = {d.x * s, -d.y * s};
-              }
-              cdYa[(lm * 3 + c) * T + t] = d;
-            }
           }
           ylm_half<R, true>(D::L2, mx, my, mz, Ym, dYm);
         }
@@ -2199,13 +2189,33 @@ __global__ void __launch_bounds__(64, MINB)
   #pragma unroll
           for (int n = 0; n < D::NB; ++n) fr = fma(cgd[n * T + t], sp[n], fr);
           const R invr = rcp(r);
+          // the angular part: S_lm = sum_n1 U R_n1,l / r, contracted once
+          // with dY_lm (recomputed here rather than kept per bond)
+          C<R> S[D::LSA];
+  #pragma unroll
+          for (int lm = 0; lm < D::LSA; ++lm) S[lm] = {R(0), R(0)};
   #pragma unroll
           for (int i = 0; i < D::NRY; ++i) {
             const int n1 = i / D::LSA, lma = i % D::LSA, l1 = l_of_lm(lma);
             fr = fma(cRd[(n1 * (D::LA + 1) + l1) * T + t], re_mul(U[i], cYa[lma * T + t]), fr);
             const C<R> su = cscale(U[i], invr * cR[(n1 * (D::LA + 1) + l1) * T + t]);
+            S[lma].x += su.x;
+            S[lma].y += su.y;
+          }
+          C<R> Ya[D::HA], dYa[D::HA][3];
+          ylm_half<R, true>(D::LA, ex, ey, ez, Ya, dYa);
   #pragma unroll
-            for (int c = 0; c < 3; ++c) ft[c] = re_mac(ft[c], su, cdYa[(lma * 3 + c) * T + t]);
+          for (int lm = 0; lm < D::LSA; ++lm) {
+            const int l = l_of_lm(lm), mm = lm - l * l - l;
+  #pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              C<R> d = dYa[ph(l, mm < 0 ? -mm : mm)][c];
+              if (mm < 0) {
+                const R s = R(parity(mm));
+                d = {d.x * s, -d.y * s};
+              }
+              ft[c] = re_mac(ft[c], S[lm], d);
+            }
           }
         }
         *(SOUT ? sOut + 3 * t + 0 : fij + 3 * static_cast<size_t>(j) + 0) = to_d(fr * ex + ft[0]);
@@ -2911,6 +2921,6 @@ size_t b3_fe64_smem(const DeviceModel& m) {
 template <class R, class D>
 size_t forces_fe_smem(bool sout) {
   return sizeof(C<R>) * (D::NQ * D::NB + D::NQ3 * D::NRY + D::NQ + 2) +
-         sizeof(R) * 64 * (D::NB + 2 * D::NR + 2 * D::NMF) + sizeof(C<R>) * 64 * D::LSA * 4 +
+         sizeof(R) * 64 * (D::NB + 2 * D::NR + 2 * D::NMF) + sizeof(C<R>) * 64 * D::LSA +
          (sout ? sizeof(double) * 6 * 64 : 0) + 64;
 }
