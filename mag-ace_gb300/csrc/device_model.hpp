@@ -16,6 +16,8 @@ constexpr int kMaxFull = (kMaxL + 1) * (kMaxL + 1);      // packed (l, -l..l)
 constexpr int kRestTableWarps = 32;
 // flag of a slot's end record in the rest kernel's record stream
 constexpr uint32_t kRestEnd = 0x80000000u;
+// record-stream tag of two one-factor entries in one record (see RestTable)
+constexpr uint32_t kRestPair1 = 4u;
 
 // device-side error codes (first one wins)
 enum DeviceError : int {

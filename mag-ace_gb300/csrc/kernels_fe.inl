@@ -984,6 +984,14 @@ __global__ void __launch_bounds__(NW * 32, 1)
                 st_l2(W + static_cast<size_t>(atom) * nW + w, {vx * mu, vy * mu}, pol_last);
               }
               vx = vy = 0.f;
+            } else if (rw == kRestPair1) {
+              // two one-factor entries, applied in order
+              const C<float> fa = Fs[(ry & 0xffffu) * kRestStride + lane], fb = Fs[(ry >> 16) * kRestStride + lane];
+              const float ka = __uint_as_float(rx), kb = __uint_as_float(rz);
+              vx += ka * fa.x;
+              vy += ka * fa.y;
+              vx += kb * fb.x;
+              vy += kb * fb.y;
             } else {
               const float k = __uint_as_float(rx);
               C<float> p = Fs[(ry & 0xffffu) * kRestStride + lane];

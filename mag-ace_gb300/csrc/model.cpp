@@ -797,13 +797,21 @@ void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
     T.warp_slots.insert(T.warp_slots.end(), per[w].begin(), per[w].end());
   }
   // record streams per warp: each slot's entries, then its end record
-  // {multiplicity bits, weight index, A0 factor, kRestEnd | slot}
+  // {multiplicity bits, weight index, A0 factor, kRestEnd | slot}; two
+  // consecutive one-factor entries share a record {k_a, o_a | o_b << 16,
+  // k_b, kRestPair1}
   T.stream_begin.assign(T.nwarp + 1, 0);
   for (int w = 0; w < T.nwarp; ++w) {
     for (int s : per[w]) {
       for (int a = 1; a <= 3; ++a)
         for (int e = T.run[3 * s + a - 1]; e < T.run[3 * s + a]; ++e) {
           const uint32_t* r = &T.rec[4 * static_cast<size_t>(e)];
+          if (a == 1 && e + 1 < T.run[3 * s + a]) {
+            const uint32_t* r2 = r + 4;
+            T.stream.insert(T.stream.end(), {r[0], (r[1] & 0xffffu) | ((r2[1] & 0xffffu) << 16), r2[0], kRestPair1});
+            ++e;
+            continue;
+          }
           T.stream.insert(T.stream.end(), {r[0], r[1], r[2], static_cast<uint32_t>(a)});
         }
       const float mu = T.slot_mult[s];

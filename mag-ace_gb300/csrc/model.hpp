@@ -148,8 +148,10 @@ struct RestTable {
   std::vector<int32_t> slot_weight; // [nslot] weight index, or -1
   std::vector<float> slot_mult;     // [nslot] half-plane multiplicity
   // The same entries as one record stream per warp, in schedule order:
-  // {kappa bits, o1 | o2 << 16, o3, arity} per entry and, after each slot's
-  // entries, {multiplicity bits, weight index, A0 factor, kRestEnd | slot}.
+  // {kappa bits, o1 | o2 << 16, o3, arity} per entry (two consecutive
+  // one-factor entries as {kappa_a bits, o_a | o_b << 16, kappa_b bits,
+  // kRestPair1}) and, after each slot's entries, {multiplicity bits, weight
+  // index, A0 factor, kRestEnd | slot}.
   std::vector<uint32_t> stream;      // [records][4]
   std::vector<int32_t> stream_begin; // [nwarp + 1] first record of each warp
 };
