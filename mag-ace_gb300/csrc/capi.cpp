@@ -115,7 +115,7 @@ struct Runtime {
   DevBuf<int32_t> d_rank1_n, d_begin;
   DevBuf<int32_t> r_factor, r_run, r_g0, r_warp_begin, r_warp_slots;
   DevBuf<uint32_t> r_rec, r_stream;
-  DevBuf<int32_t> r_stream_begin;
+  DevBuf<int32_t> r_stream_begin, r_split_w;
   DevBuf<double> d_cf;
   DevBuf<uint16_t> d_o;
   DeviceModel dm{};
@@ -318,6 +318,7 @@ int upload_tables() {
       CUDA_TRY(R.r_warp_slots.upload(T.warp_slots));
       CUDA_TRY(R.r_stream.upload(T.stream));
       CUDA_TRY(R.r_stream_begin.upload(T.stream_begin));
+      if (T.nsplit) CUDA_TRY(R.r_split_w.upload(T.split_weight));
     } else {
       R.dm.g2 = R.dm.g;
     }
@@ -395,6 +396,8 @@ int upload_tables() {
   d.r_warp_slots = R.r_warp_slots.p;
   d.r_stream = R.r_stream.p;
   d.r_stream_begin = R.r_stream_begin.p;
+  d.r_nsplit = M.rest.nsplit;
+  d.r_split_w = R.r_split_w.p;
   d.d_n1 = M.desc.n1;
   d.d_nB = M.desc.nB;
   d.d_rank1_n = R.d_rank1_n.p;
@@ -1028,6 +1031,7 @@ void ace_release_device(void) {
   R.r_rec.release();
   R.r_stream.release();
   R.r_stream_begin.release();
+  R.r_split_w.release();
   R.d_cf.release();
   R.d_o.release();
   R.gb1.release();

@@ -18,6 +18,8 @@ constexpr int kRestTableWarps = 32;
 constexpr uint32_t kRestEnd = 0x80000000u;
 // record-stream tag of two one-factor entries in one record (see RestTable)
 constexpr uint32_t kRestPair1 = 4u;
+// end-record flag of one part of a split slot (low bits: 2 * split + part)
+constexpr uint32_t kRestSplit = 0x40000000u;
 
 // device-side error codes (first one wins)
 enum DeviceError : int {
@@ -112,6 +114,8 @@ struct DeviceModel {
   const int32_t* r_warp_slots;
   const uint32_t* r_stream;     // [records][4] per-warp record streams
   const int32_t* r_stream_begin;  // [warps + 1]
+  int r_nsplit;                 // slots split in two stream items
+  const int32_t* r_split_w;     // [nsplit] their weight index, or -1
   // variants of the split-precision density kernels (indices into the
   // kernels.hpp choice tables)
   int tune_abasis, tune_rest, tune_b3, tune_forces;

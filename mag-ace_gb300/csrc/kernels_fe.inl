@@ -947,6 +947,7 @@ __global__ void __launch_bounds__(NW * 32, 1)
       const uint4* srec = reinterpret_cast<const uint4*>(m.r_stream);
       constexpr int CH = STREAM == 1 ? 32 : 16;  // records per load
       uint4* rbuf = reinterpret_cast<uint4*>(rpart + NW * 32) + warp * 16;  // STREAM 2
+      C<float>* psum = reinterpret_cast<C<float>*>(reinterpret_cast<uint4*>(rpart + NW * 32) + NW * 16);
       for (int sw = warp; sw < kRestTableWarps; sw += NW) {
         const int e0 = __ldg(m.r_stream_begin + sw), e1 = __ldg(m.r_stream_begin + sw + 1);
         float vx = 0.f, vy = 0.f;
@@ -973,14 +974,17 @@ __global__ void __launch_bounds__(NW * 32, 1)
               rw = __shfl_sync(0xffffffffu, mine.w, q);
             }
             if (rw & kRestEnd) {
-              // end of a slot: density term and unscaled weight
+              // end of a slot (or of one part of a split slot): density
+              // term and unscaled weight (a part's into psum)
               const int g0 = static_cast<int>(rz), w = static_cast<int>(ry);
               if (g0 >= 0) {
                 const C<float> f = Fs[g0 * kRestStride + lane];
                 rloc += f2d(f.x * vx) - f2d(f.y * vy);
               }
-              if (w >= 0 && atom >= 0) {
-                const float mu = __uint_as_float(rx);
+              const float mu = __uint_as_float(rx);
+              if (rw & kRestSplit) {
+                psum[(rw & 0xffffu) * 32 + lane] = {vx * mu, vy * mu};
+              } else if (w >= 0 && atom >= 0) {
                 st_l2(W + static_cast<size_t>(atom) * nW + w, {vx * mu, vy * mu}, pol_last);
               }
               vx = vy = 0.f;
@@ -1030,6 +1034,17 @@ __global__ void __launch_bounds__(NW * 32, 1)
       double r = 0.0;
       for (int w = 0; w < NW; ++w) r += rpart[w * 32 + lane];
       rho_rest[atom] = r;
+    }
+    if constexpr (STREAM > 0) {
+      // the split slots' weights: the sum of their two parts
+      const C<float>* psum = reinterpret_cast<const C<float>*>(reinterpret_cast<const uint4*>(rpart + NW * 32) + NW * 16);
+      for (int q = threadIdx.x - 32; q >= 0 && q < m.r_nsplit * 32; q += blockDim.x - 32) {
+        const int sp = q >> 5, a = q & 31, w = __ldg(m.r_split_w + sp);
+        if (a < na && w >= 0) {
+          const C<float> p0 = psum[(2 * sp) * 32 + a], p1 = psum[(2 * sp + 1) * 32 + a];
+          st_l2(W + static_cast<size_t>(s_atom[a]) * nW + w, {p0.x + p1.x, p0.y + p1.y}, pol_last);
+        }
+      }
     }
   }
 }
@@ -2910,9 +2925,10 @@ __global__ void __launch_bounds__(64, MINB)
 }
 
 inline size_t density_fe_smem(const DeviceModel& m, int nw) {
-  // factors, per-warp density partials, per-warp 16-record buffers
+  // factors, per-warp density partials, per-warp 16-record buffers, the
+  // split slots' part weights
   return sizeof(C<float>) * static_cast<size_t>(m.r_nfac) * kRestStride + sizeof(double) * nw * 32 +
-         sizeof(uint4) * 16 * nw;
+         sizeof(uint4) * 16 * nw + sizeof(C<float>) * 64 * static_cast<size_t>(m.r_nsplit);
 }
 template <class D>
 size_t b3_fe_smem(const DeviceModel& m, int nw) {

@@ -796,29 +796,124 @@ void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
     T.warp_begin[w + 1] = T.warp_begin[w] + static_cast<int32_t>(per[w].size());
     T.warp_slots.insert(T.warp_slots.end(), per[w].begin(), per[w].end());
   }
-  // record streams per warp: each slot's entries, then its end record
-  // {multiplicity bits, weight index, A0 factor, kRestEnd | slot}; two
-  // consecutive one-factor entries share a record {k_a, o_a | o_b << 16,
-  // k_b, kRestPair1}
+  // record streams per warp, dealt by their own cost (records, the
+  // three-factor ones and the slot ends weighted as the kernels take them):
+  // each item's entries, then its end record {multiplicity bits, weight
+  // index, A0 factor, kRestEnd | slot}; two consecutive one-factor entries
+  // share a record {k_a, o_a | o_b << 16, k_b, kRestPair1}. A slot longer
+  // than three quarters of a warp's mean share is split in two items (dealt
+  // to different warps): their end records carry kRestSplit | (2 sp + part),
+  // each part's density term is its own (the term is linear), and the kernel
+  // adds the parts' weights, split[sp] the slot's weight index.
+  struct Item {
+    int s, part;                 // part -1: the whole slot
+    std::vector<int32_t> ent;    // entries (indices into rec), arity order
+    double cost;
+  };
+  std::vector<Item> items;
+  std::vector<int> arity_of(T.run[3 * T.nslot], 0);
+  for (int s = 0; s < T.nslot; ++s)
+    for (int a = 1; a <= 3; ++a)
+      for (int e = T.run[3 * s + a - 1]; e < T.run[3 * s + a]; ++e) arity_of[e] = a;
+  const auto records_cost = [&](const std::vector<int32_t>& ent) {
+    double c = 1.5;  // the end record
+    int run1 = 0;
+    for (size_t q = 0; q <= ent.size(); ++q) {
+      const int a = q < ent.size() ? arity_of[ent[q]] : 0;
+      if (a == 1) {
+        ++run1;
+        continue;
+      }
+      c += 1.3 * (run1 / 2) + 1.0 * (run1 % 2);
+      run1 = 0;
+      if (a == 2) c += 1.4;
+      if (a == 3) c += 1.8;
+    }
+    return c;
+  };
+  double total = 0.0;
+  for (int s = 0; s < T.nslot; ++s) {
+    Item it{s, -1, {}, 0.0};
+    for (int e = T.run[3 * s]; e < T.run[3 * s + 3]; ++e) it.ent.push_back(e);
+    it.cost = records_cost(it.ent);
+    total += it.cost;
+    items.push_back(std::move(it));
+  }
+  const double limit = 0.75 * total / T.nwarp;
+  std::vector<Item> dealt;
+  for (auto& it : items) {
+    if (it.cost <= limit || it.ent.size() < 4) {
+      dealt.push_back(std::move(it));
+      continue;
+    }
+    // two parts of about equal cost (an even cut inside the one-factor run)
+    size_t cut = it.ent.size() / 2;
+    double best = 1e300;
+    for (size_t q = 2; q + 1 < it.ent.size(); q += 2) {
+      const std::vector<int32_t> p0(it.ent.begin(), it.ent.begin() + q), p1(it.ent.begin() + q, it.ent.end());
+      const double d = std::fabs(records_cost(p0) - records_cost(p1));
+      if (d < best) {
+        best = d;
+        cut = q;
+      }
+    }
+    const int sp = T.nsplit++;
+    T.split_weight.push_back(T.slot_weight[it.s]);
+    for (int part = 0; part < 2; ++part) {
+      Item p{it.s, 2 * sp + part, {}, 0.0};
+      if (part == 0) p.ent.assign(it.ent.begin(), it.ent.begin() + cut);
+      else p.ent.assign(it.ent.begin() + cut, it.ent.end());
+      p.cost = records_cost(p.ent);
+      dealt.push_back(std::move(p));
+    }
+  }
+  std::vector<int> iorder(dealt.size());
+  for (size_t q = 0; q < dealt.size(); ++q) iorder[q] = static_cast<int>(q);
+  std::stable_sort(iorder.begin(), iorder.end(), [&](int x, int y) { return dealt[x].cost > dealt[y].cost; });
+  std::vector<double> sload(T.nwarp, 0.0);
+  std::vector<std::vector<int>> sper(T.nwarp);
+  std::vector<int> part0_warp(T.nsplit, -1);
+  for (int q : iorder) {
+    int w = static_cast<int>(std::min_element(sload.begin(), sload.end()) - sload.begin());
+    const Item& it = dealt[q];
+    if (it.part >= 0) {
+      const int sp = it.part / 2;
+      if (part0_warp[sp] == w) {  // the other part went to this warp: take the next least loaded
+        double bl = 1e300;
+        for (int v = 0; v < T.nwarp; ++v)
+          if (v != w && sload[v] < bl) {
+            bl = sload[v];
+            w = v;
+          }
+      }
+      part0_warp[sp] = w;
+    }
+    sload[w] += it.cost;
+    sper[w].push_back(q);
+  }
   T.stream_begin.assign(T.nwarp + 1, 0);
   for (int w = 0; w < T.nwarp; ++w) {
-    for (int s : per[w]) {
-      for (int a = 1; a <= 3; ++a)
-        for (int e = T.run[3 * s + a - 1]; e < T.run[3 * s + a]; ++e) {
-          const uint32_t* r = &T.rec[4 * static_cast<size_t>(e)];
-          if (a == 1 && e + 1 < T.run[3 * s + a]) {
-            const uint32_t* r2 = r + 4;
-            T.stream.insert(T.stream.end(), {r[0], (r[1] & 0xffffu) | ((r2[1] & 0xffffu) << 16), r2[0], kRestPair1});
-            ++e;
-            continue;
-          }
-          T.stream.insert(T.stream.end(), {r[0], r[1], r[2], static_cast<uint32_t>(a)});
+    for (int q : sper[w]) {
+      const Item& it = dealt[q];
+      for (size_t x = 0; x < it.ent.size(); ++x) {
+        const int e = it.ent[x];
+        const uint32_t* r = &T.rec[4 * static_cast<size_t>(e)];
+        const int a = arity_of[e];
+        if (a == 1 && x + 1 < it.ent.size() && arity_of[it.ent[x + 1]] == 1) {
+          const uint32_t* r2 = &T.rec[4 * static_cast<size_t>(it.ent[x + 1])];
+          T.stream.insert(T.stream.end(), {r[0], (r[1] & 0xffffu) | ((r2[1] & 0xffffu) << 16), r2[0], kRestPair1});
+          ++x;
+          continue;
         }
-      const float mu = T.slot_mult[s];
+        T.stream.insert(T.stream.end(), {r[0], r[1], r[2], static_cast<uint32_t>(a)});
+      }
+      const float mu = T.slot_mult[it.s];
       uint32_t mb;
       std::memcpy(&mb, &mu, sizeof(mb));
-      T.stream.insert(T.stream.end(), {mb, static_cast<uint32_t>(T.slot_weight[s]), static_cast<uint32_t>(T.slot_g0[s]),
-                                       kRestEnd | static_cast<uint32_t>(s)});
+      const uint32_t tag = it.part < 0 ? (kRestEnd | static_cast<uint32_t>(it.s))
+                                       : (kRestEnd | kRestSplit | static_cast<uint32_t>(it.part));
+      T.stream.insert(T.stream.end(), {mb, static_cast<uint32_t>(T.slot_weight[it.s]),
+                                       static_cast<uint32_t>(T.slot_g0[it.s]), tag});
     }
     T.stream_begin[w + 1] = static_cast<int32_t>(T.stream.size() / 4);
   }

@@ -154,6 +154,8 @@ struct RestTable {
   // index, A0 factor, kRestEnd | slot}.
   std::vector<uint32_t> stream;      // [records][4]
   std::vector<int32_t> stream_begin; // [nwarp + 1] first record of each warp
+  int nsplit = 0;                    // slots split in two stream items
+  std::vector<int32_t> split_weight; // [nsplit] their weight index, or -1
 };
 
 struct RadialLUT {
