@@ -721,7 +721,7 @@ void for_each_term(const Model& M, bool with_b3, Fn&& fn) {
 // slot's entries contiguous (arity 1, then 2, then 3), factors renumbered
 // into the compact set the terms use, and the slots dealt to the kernel's
 // warps longest first onto the least loaded warp.
-void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, RestTable& T) {
+bool build_rest(const Model& M, const TermSink& sink, const GatherTable& g, RestTable& T) {
   const FactorLayout& L = M.L;
   T = RestTable();
   std::vector<int32_t> compact(L.nF, -1);
@@ -892,9 +892,11 @@ void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
     sper[w].push_back(q);
   }
   T.stream_begin.assign(T.nwarp + 1, 0);
+  std::vector<int> emitted(arity_of.size(), 0);  // each entry exactly once (checked below)
   for (int w = 0; w < T.nwarp; ++w) {
     for (int q : sper[w]) {
       const Item& it = dealt[q];
+      for (int e : it.ent) ++emitted[e];
       for (size_t x = 0; x < it.ent.size(); ++x) {
         const int e = it.ent[x];
         const uint32_t* r = &T.rec[4 * static_cast<size_t>(e)];
@@ -917,6 +919,17 @@ void build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
     }
     T.stream_begin[w + 1] = static_cast<int32_t>(T.stream.size() / 4);
   }
+  // the streams' invariants: every entry in exactly one item, the two parts
+  // of a split slot on different warps, every factor index below 2^16
+  for (int c : emitted)
+    if (c != 1) return false;
+  std::vector<int> warp_of_part(2 * static_cast<size_t>(T.nsplit), -1);
+  for (int w = 0; w < T.nwarp; ++w)
+    for (int q : sper[w])
+      if (dealt[q].part >= 0) warp_of_part[dealt[q].part] = w;
+  for (int sp = 0; sp < T.nsplit; ++sp)
+    if (warp_of_part[2 * sp] < 0 || warp_of_part[2 * sp] == warp_of_part[2 * sp + 1]) return false;
+  return T.nfac <= 0xffff;
 }
 
 int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestTable* rest = nullptr) {
@@ -1136,10 +1149,12 @@ int build_gather(Model& M, bool with_b3, GatherTable& g, std::string& msg, RestT
           g.slot_weight[s] = w;
           g.slot_mult[s] = m == 0 ? 1.0 : 2.0;
         }
-  if (rest) build_rest(M, sink, g, *rest);
+  if (rest && !build_rest(M, sink, g, *rest)) {
+    msg = "internal error: inconsistent 2-/4-body record streams";
+    return MAGACE_ERR_UNSUPPORTED;
+  }
   (void)d;
   (void)nd;
-  (void)msg;
   return MAGACE_OK;
 }
 
