@@ -115,7 +115,7 @@ struct Runtime {
   DevBuf<int32_t> d_rank1_n, d_begin;
   DevBuf<int32_t> r_factor, r_run, r_g0, r_warp_begin, r_warp_slots;
   DevBuf<uint32_t> r_rec, r_stream;
-  DevBuf<int32_t> r_stream_begin, r_split_w;
+  DevBuf<int32_t> r_stream_begin, r_split_w, r64_warp_begin, r64_warp_slots;
   DevBuf<double> d_cf;
   DevBuf<uint16_t> d_o;
   DeviceModel dm{};
@@ -319,6 +319,8 @@ int upload_tables() {
       CUDA_TRY(R.r_stream.upload(T.stream));
       CUDA_TRY(R.r_stream_begin.upload(T.stream_begin));
       if (T.nsplit) CUDA_TRY(R.r_split_w.upload(T.split_weight));
+      CUDA_TRY(R.r64_warp_begin.upload(T.warp64_begin));
+      CUDA_TRY(R.r64_warp_slots.upload(T.warp64_slots));
     } else {
       R.dm.g2 = R.dm.g;
     }
@@ -397,6 +399,8 @@ int upload_tables() {
   d.r_stream = R.r_stream.p;
   d.r_stream_begin = R.r_stream_begin.p;
   d.r_nsplit = M.rest.nsplit;
+  d.r64_warp_begin = R.r64_warp_begin.p;
+  d.r64_warp_slots = R.r64_warp_slots.p;
   d.r_split_w = R.r_split_w.p;
   d.d_n1 = M.desc.n1;
   d.d_nB = M.desc.nB;
@@ -1032,6 +1036,8 @@ void ace_release_device(void) {
   R.r_stream.release();
   R.r_stream_begin.release();
   R.r_split_w.release();
+  R.r64_warp_begin.release();
+  R.r64_warp_slots.release();
   R.d_cf.release();
   R.d_o.release();
   R.gb1.release();

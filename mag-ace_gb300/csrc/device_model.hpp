@@ -16,6 +16,9 @@ constexpr int kMaxFull = (kMaxL + 1) * (kMaxL + 1);      // packed (l, -l..l)
 constexpr int kRestTableWarps = 32;
 // flag of a slot's end record in the rest kernel's record stream
 constexpr uint32_t kRestEnd = 0x80000000u;
+// warps per CTA of the FP64 2-/4-body kernel (k_rest64), which walks its
+// own slot schedule (RestTable::warp64_begin)
+constexpr int kRestWarps64 = 16;
 // record-stream tag of two one-factor entries in one record (see RestTable)
 constexpr uint32_t kRestPair1 = 4u;
 // end-record flag of one part of a split slot (low bits: 2 * split + part)
@@ -114,6 +117,8 @@ struct DeviceModel {
   const int32_t* r_warp_slots;
   const uint32_t* r_stream;     // [records][4] per-warp record streams
   const int32_t* r_stream_begin;  // [warps + 1]
+  const int32_t* r64_warp_begin;  // [kRestWarps64 + 1] the FP64 kernel's slot schedule
+  const int32_t* r64_warp_slots;
   int r_nsplit;                 // slots split in two stream items
   const int32_t* r_split_w;     // [nsplit] their weight index, or -1
   // variants of the split-precision density kernels (indices into the

@@ -1053,10 +1053,10 @@ __global__ void __launch_bounds__(NW * 32, 1)
 // the rest table, 16 atoms per CTA: lane & 15 is the atom, and the two
 // half-warps take alternate entries of the same slot, so that both follow
 // the same path; a shuffle adds their sums. Warp w walks the slots the host
-// schedule gave to table warps w, w + NW, ... in order, so every sum has a
+// schedule gave it (RestTable::warp64_begin) in order, so every sum has a
 // fixed order. Writes rho_rest and the unscaled weights mult * dRho_rest/dF.
 constexpr int kRestStride64 = 17;  // row stride of Fs in complex elements
-constexpr int kRestWarps64 = 16;   // warps per CTA of k_rest64
+// (kRestWarps64, the warps per CTA of k_rest64, is in device_model.hpp)
 
 // the entries [e0, e1) (every second one) of arity A in float-float: the
 // factors staged as hi/lo floats (Fs), the coefficients as hi/lo pairs
@@ -1097,7 +1097,7 @@ template <class D, int NW>
 __global__ void __launch_bounds__(NW * 32, 1)
     k_rest64(DeviceModel m, int natom, const C<double>* __restrict__ F, C<double>* __restrict__ W,
              double* __restrict__ rho_rest) {
-  static_assert(kRestTableWarps % NW == 0, "the slot schedule is dealt to kRestTableWarps warps");
+  static_assert(NW == kRestWarps64, "the FP64 slot schedule is dealt to kRestWarps64 warps");
   extern __shared__ __align__(16) unsigned char smem[];
   const int nf = m.r_nfac, nW = m.nW;
   const GatherView& g = m.g2;  // slot weights and multiplicities (same slot numbering)
@@ -1126,33 +1126,32 @@ __global__ void __launch_bounds__(NW * 32, 1)
     __syncthreads();
     const int atom = al < na ? s_atom[al] : -1;
     double rloc = 0.0;
-    for (int sw = warp; sw < kRestTableWarps; sw += NW)
-      for (int q = __ldg(m.r_warp_begin + sw); q < __ldg(m.r_warp_begin + sw + 1); ++q) {
-        const int s = __ldg(m.r_warp_slots + q);
-        float vx[2] = {0.f, 0.f}, vy[2] = {0.f, 0.f};
-        rest_run64<1>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s) + half, __ldg(m.r_run + 3 * s + 1), Ff, al, vx, vy);
-        rest_run64<2>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s + 1) + half, __ldg(m.r_run + 3 * s + 2), Ff, al, vx,
-                      vy);
-        rest_run64<3>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s + 2) + half, __ldg(m.r_run + 3 * s + 3), Ff, al, vx,
-                      vy);
-        // the other half-warp's sums (lanes 16-31 add lanes 0-15's, and the
-        // reverse; only lanes 0-15 use the result)
-        ff_add_sum(vx[0], vx[1], __shfl_xor_sync(0xffffffffu, vx[0], 16), __shfl_xor_sync(0xffffffffu, vx[1], 16));
-        ff_add_sum(vy[0], vy[1], __shfl_xor_sync(0xffffffffu, vy[0], 16), __shfl_xor_sync(0xffffffffu, vy[1], 16));
-        const C<double> v = {ff_d(vx[0], vx[1]), ff_d(vy[0], vy[1])};
-        if (half == 0) {
-          const int g0 = __ldg(m.r_g0 + s);
-          if (g0 >= 0) {
-            const FFc f = Ff[g0 * kRestStride64 + al];
-            rloc = re_mac(rloc, C<double>{f2d(f.x.hi) + f2d(f.x.lo), f2d(f.y.hi) + f2d(f.y.lo)}, v);
-          }
-          const int w = __ldg(g.slot_weight + s);
-          if (w >= 0 && atom >= 0) {
-            const double mu = __ldg(g.slot_mult + s);
-            W[static_cast<size_t>(atom) * nW + w] = {mu * v.x, mu * v.y};
-          }
+    for (int q = __ldg(m.r64_warp_begin + warp); q < __ldg(m.r64_warp_begin + warp + 1); ++q) {
+      const int s = __ldg(m.r64_warp_slots + q);
+      float vx[2] = {0.f, 0.f}, vy[2] = {0.f, 0.f};
+      rest_run64<1>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s) + half, __ldg(m.r_run + 3 * s + 1), Ff, al, vx, vy);
+      rest_run64<2>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s + 1) + half, __ldg(m.r_run + 3 * s + 2), Ff, al, vx,
+                    vy);
+      rest_run64<3>(rec, m.r_kaphl, __ldg(m.r_run + 3 * s + 2) + half, __ldg(m.r_run + 3 * s + 3), Ff, al, vx,
+                    vy);
+      // the other half-warp's sums (lanes 16-31 add lanes 0-15's, and the
+      // reverse; only lanes 0-15 use the result)
+      ff_add_sum(vx[0], vx[1], __shfl_xor_sync(0xffffffffu, vx[0], 16), __shfl_xor_sync(0xffffffffu, vx[1], 16));
+      ff_add_sum(vy[0], vy[1], __shfl_xor_sync(0xffffffffu, vy[0], 16), __shfl_xor_sync(0xffffffffu, vy[1], 16));
+      const C<double> v = {ff_d(vx[0], vx[1]), ff_d(vy[0], vy[1])};
+      if (half == 0) {
+        const int g0 = __ldg(m.r_g0 + s);
+        if (g0 >= 0) {
+          const FFc f = Ff[g0 * kRestStride64 + al];
+          rloc = re_mac(rloc, C<double>{f2d(f.x.hi) + f2d(f.x.lo), f2d(f.y.hi) + f2d(f.y.lo)}, v);
+        }
+        const int w = __ldg(g.slot_weight + s);
+        if (w >= 0 && atom >= 0) {
+          const double mu = __ldg(g.slot_mult + s);
+          W[static_cast<size_t>(atom) * nW + w] = {mu * v.x, mu * v.y};
         }
       }
+    }
     if (half == 0) rpart[warp * 16 + al] = rloc;
     __syncthreads();
     if (threadIdx.x < na) {

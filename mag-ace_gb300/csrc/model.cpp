@@ -796,6 +796,31 @@ bool build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
     T.warp_begin[w + 1] = T.warp_begin[w] + static_cast<int32_t>(per[w].size());
     T.warp_slots.insert(T.warp_slots.end(), per[w].begin(), per[w].end());
   }
+  {
+    // the FP64 kernel: a half-warp takes every second entry, a three-factor
+    // entry costs about four one-factor ones in float-float, a slot end three
+    std::vector<double> c64(T.nslot);
+    for (int s = 0; s < T.nslot; ++s) {
+      const int n1 = T.run[3 * s + 1] - T.run[3 * s], n2 = T.run[3 * s + 2] - T.run[3 * s + 1],
+                n3 = T.run[3 * s + 3] - T.run[3 * s + 2];
+      c64[s] = (n1 + 1) / 2 + 2.5 * ((n2 + 1) / 2) + 4.0 * ((n3 + 1) / 2) + 3.0;
+    }
+    std::vector<int> o64(T.nslot);
+    for (int s = 0; s < T.nslot; ++s) o64[s] = s;
+    std::stable_sort(o64.begin(), o64.end(), [&](int x, int y) { return c64[x] > c64[y]; });
+    std::vector<double> l64(kRestWarps64, 0.0);
+    std::vector<std::vector<int32_t>> p64(kRestWarps64);
+    for (int s : o64) {
+      const int w = static_cast<int>(std::min_element(l64.begin(), l64.end()) - l64.begin());
+      l64[w] += c64[s];
+      p64[w].push_back(s);
+    }
+    T.warp64_begin.assign(kRestWarps64 + 1, 0);
+    for (int w = 0; w < kRestWarps64; ++w) {
+      T.warp64_begin[w + 1] = T.warp64_begin[w] + static_cast<int32_t>(p64[w].size());
+      T.warp64_slots.insert(T.warp64_slots.end(), p64[w].begin(), p64[w].end());
+    }
+  }
   // record streams per warp, dealt by their own cost (records, the
   // three-factor ones and the slot ends weighted as the kernels take them):
   // each item's entries, then its end record {multiplicity bits, weight

@@ -154,6 +154,9 @@ struct RestTable {
   // index, A0 factor, kRestEnd | slot}.
   std::vector<uint32_t> stream;      // [records][4]
   std::vector<int32_t> stream_begin; // [nwarp + 1] first record of each warp
+  // the FP64 kernel's schedule: slots dealt longest first to kRestWarps64
+  // warps by that kernel's cost (half-warps take alternate entries)
+  std::vector<int32_t> warp64_begin, warp64_slots;
   int nsplit = 0;                    // slots split in two stream items
   std::vector<int32_t> split_weight; // [nsplit] their weight index, or -1
 };
