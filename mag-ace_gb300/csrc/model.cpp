@@ -840,6 +840,8 @@ bool build_rest(const Model& M, const TermSink& sink, const GatherTable& g, Rest
   for (int s = 0; s < T.nslot; ++s)
     for (int a = 1; a <= 3; ++a)
       for (int e = T.run[3 * s + a - 1]; e < T.run[3 * s + a]; ++e) arity_of[e] = a;
+  // relative record costs (estimates: other weightings and split limits
+  // between a half and one share balanced the warps as well)
   const auto records_cost = [&](const std::vector<int32_t>& ent) {
     double c = 1.5;  // the end record
     int run1 = 0;
