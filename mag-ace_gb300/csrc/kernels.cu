@@ -1212,8 +1212,9 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
         cudaEventRecord(b.ev_join, sr);
         cudaStreamWaitEvent(st, b.ev_join, 0);
       }
-      const int gf = (natom + 255) / 256;
-      k_finish_fe<<<gf, 256, 0, st>>>(m, natom, b.rho1, rho_rest, rho3, b.core, b.energy, b.edf, b.dedrho, b.err);
+      // 64 threads per CTA: the FP64 embedding of every atom spread over all SMs
+      const int gf = (natom + 63) / 64;
+      k_finish_fe<<<gf, 64, 0, st>>>(m, natom, b.rho1, rho_rest, rho3, b.core, b.energy, b.edf, b.dedrho, b.err);
       if (kernels) *kernels += 3;
       return 2;
     }
@@ -1255,9 +1256,9 @@ int launch_density(const DeviceModel& m, const EvalBuffers& b, cudaStream_t st, 
         cudaEventRecord(b.ev_join, sr);
         cudaStreamWaitEvent(st, b.ev_join, 0);
       }
-      const int gf = (natom + 255) / 256;
-      k_finish_fe<<<gf, 256, 0, st>>>(m, natom, b.rho1, rho_rest, nullptr, b.core, b.energy, b.edf, b.dedrho, b.err,
-                                      r3i, r3s);
+      const int gf = (natom + 63) / 64;
+      k_finish_fe<<<gf, 64, 0, st>>>(m, natom, b.rho1, rho_rest, nullptr, b.core, b.energy, b.edf, b.dedrho, b.err,
+                                     r3i, r3s);
       if (kernels) *kernels += 3;
       return 2;
     }
